@@ -1,0 +1,142 @@
+"""ctypes front-end of the CPU oracle (florence_oracle.c).
+
+TEST INFRASTRUCTURE ONLY. Imported by tests/, by ``__graft_entry__.smoke()`` and by
+``bench.py``'s CPU-baseline leg, always as the checker or the timed CPU reference,
+never as part of the product path. It restates the reference's assembly
+(Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDF_.h:8-176 and
+the files cited in florence_oracle.c) and is pinned against golden vectors made by
+the reference's own code (tests/golden/make_golden.py, tests/test_oracle.py).
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+MATERIALS = {"NeoHookean": 1, "MooneyRivlin": 2}
+
+_lib = None
+
+
+def build(force=False):
+    """Compile liboracle.so from florence_oracle.c (seconds)."""
+    src = os.path.join(HERE, "florence_oracle.c")
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
+        subprocess.check_call(["make", "-s", "-C", HERE, "-B", "liboracle.so"])
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        i64 = ctypes.c_int64
+        L.orc_assemble_df.argtypes = [ctypes.c_int, P, P, P, P, P, P, i64, i64, i64, ctypes.c_int, ctypes.c_int,
+                                      P, P, P, P, P, P, P, P, ctypes.c_int]
+        L.orc_element_matrices.argtypes = [ctypes.c_int, P, P, P, P, P, P, i64, i64, ctypes.c_int, P, i64, P, P]
+        L.orc_internal_force.argtypes = [ctypes.c_int, P, P, P, P, P, P, i64, i64, i64, P, ctypes.c_int]
+        L.orc_lumped_mass.argtypes = [ctypes.c_double, P, P, P, P, P, i64, i64, i64, P]
+        L.orc_sparsity_nnz.argtypes = [P, i64, i64, i64, i64]
+        L.orc_sparsity_nnz.restype = i64
+        L.orc_sparsity.argtypes = [P, i64, i64, i64, i64, P, P, P, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+def max_threads():
+    return int(lib().orc_max_threads())
+
+
+def sparsity(elements, nnode, nvar=3, maps=True):
+    """Returns (indices, indptr, data_local, data_global) like the reference's ComputeSparsityPattern."""
+    el = _c(elements, np.int64)
+    nelem, npe = el.shape
+    nnz = lib().orc_sparsity_nnz(_p(el), nelem, npe, nnode, nvar)
+    if nnz < 0:
+        raise ValueError("every node must belong to at least one element")
+    indptr = np.zeros(nnode * nvar + 1, np.int32)
+    indices = np.zeros(nnz, np.int32)
+    cap = (npe * nvar) ** 2 * nelem
+    dl = np.zeros(cap, np.int32) if maps else None
+    dg = np.zeros(cap, np.int32) if maps else None
+    lib().orc_sparsity(_p(el), nelem, npe, nnode, nvar, _p(indptr), _p(indices), _p(dl), _p(dg))
+    return indices, indptr, dl, dg
+
+
+def assemble_df(material, params, points, elements, Eulerx, Jm, AllGauss, mode="csr", sparsity_arrays=None,
+                requires_geometry_update=1, nthreads=1):
+    """Global tangent and residual. mode: 'triplet' -> (I, J, V, T); 'csr'/'squeeze' -> (V, T)."""
+    mat = MATERIALS[material]
+    prm = _c(params, np.float64)
+    X = _c(points, np.float64)
+    el = _c(elements, np.int64)
+    x = _c(Eulerx, np.float64)
+    jm = _c(Jm, np.float64)
+    w = _c(np.ravel(AllGauss), np.float64)
+    nelem, npe = el.shape
+    nq = w.shape[0]
+    ndof = 3 * npe
+    T = np.zeros(X.shape[0] * 3)
+    if mode == "triplet":
+        I = np.zeros(nelem * ndof * ndof, np.int32)
+        J = np.zeros_like(I)
+        V = np.zeros(nelem * ndof * ndof)
+        lib().orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
+                              requires_geometry_update, 0, _p(I), _p(J), _p(V), _p(T), None, None, None, None, nthreads)
+        return I, J, V, T
+    indices, indptr, dl, dg = sparsity_arrays
+    indices = _c(indices, np.int32)
+    indptr = _c(indptr, np.int32)
+    V = np.zeros(indices.shape[0])
+    m = 1 if mode == "csr" else 2
+    lib().orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
+                          requires_geometry_update, m, None, None, _p(V), _p(T), _p(indptr), _p(indices),
+                          _p(_c(dl, np.int32) if m == 1 else None), _p(_c(dg, np.int32) if m == 1 else None), nthreads)
+    return V, T
+
+
+def element_matrices(material, params, points, elements, Eulerx, Jm, AllGauss, elem_ids, requires_geometry_update=1):
+    mat = MATERIALS[material]
+    el = _c(elements, np.int64)
+    npe = el.shape[1]
+    w = _c(np.ravel(AllGauss), np.float64)
+    ids = _c(elem_ids, np.int64)
+    ndof = 3 * npe
+    Ke = np.zeros((ids.shape[0], ndof, ndof))
+    te = np.zeros((ids.shape[0], ndof))
+    lib().orc_element_matrices(mat, _p(_c(params, np.float64)), _p(_c(points, np.float64)), _p(el),
+                               _p(_c(Eulerx, np.float64)), _p(_c(Jm, np.float64)), _p(w), npe, w.shape[0],
+                               requires_geometry_update, _p(ids), ids.shape[0], _p(Ke), _p(te))
+    return Ke, te
+
+
+def internal_force(material, params, points, elements, Eulerx, Jm, AllGauss, nthreads=1):
+    mat = MATERIALS[material]
+    el = _c(elements, np.int64)
+    w = _c(np.ravel(AllGauss), np.float64)
+    T = np.zeros(np.shape(points)[0] * 3)
+    lib().orc_internal_force(mat, _p(_c(params, np.float64)), _p(_c(points, np.float64)), _p(el),
+                             _p(_c(Eulerx, np.float64)), _p(_c(Jm, np.float64)), _p(w), el.shape[0], el.shape[1],
+                             w.shape[0], _p(T), nthreads)
+    return T
+
+
+def lumped_mass(rho, points, elements, Jm, AllGauss, Bases):
+    el = _c(elements, np.int64)
+    w = _c(np.ravel(AllGauss), np.float64)
+    M = np.zeros(np.shape(points)[0] * 3)
+    lib().orc_lumped_mass(float(rho), _p(_c(points, np.float64)), _p(el), _p(_c(Jm, np.float64)), _p(w),
+                          _p(_c(Bases, np.float64)), el.shape[0], el.shape[1], w.shape[0], _p(M))
+    return M

@@ -1,0 +1,232 @@
+"""Generates the golden fixtures in this folder from the reference Florence package.
+
+Test infrastructure only. Run in a container with the reference checkout at
+``/root/reference`` (it is not present on the GPU machine, which only reads the
+committed ``.npz`` files):
+
+    python tests/golden/make_golden.py
+
+Every output is produced by the reference's own pure-numpy assembly path
+(``AssembleForm`` -> ``AssemblySmall`` -> ``DisplacementFormulation.GetLocalStiffness``,
+Florence/FiniteElements/Assembly/Assembly.py:1454-1495, :99-252 and
+Florence/VariationalPrinciple/DisplacementFormulation.py:110-188), by its compiled
+``ComputeSparsityPattern`` (Florence/FiniteElements/Assembly/_Assembly_/ComputeSparsityPattern.pyx:44-112)
+and by its Python lumped-mass path (Florence/FiniteElements/Assembly/Assembly.py:608-657).
+Meshes come from the reference's own generators (``Mesh.Cube``, ``Mesh.Parallelepiped``,
+``GetHighOrderMesh``) or from a seeded jittered lattice split by ``scipy.spatial.Delaunay``.
+"""
+import hashlib
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import florence_harness  # noqa: E402
+
+
+def sha(a, dtype):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=dtype).tobytes()).hexdigest()
+
+
+def make_material(F, name, params):
+    if name == "NeoHookean":
+        m = F.NeoHookean(3, mu=params[0], lamb=params[1], rho=params[2] if len(params) > 2 else 1.0)
+    elif name == "MooneyRivlin":
+        m = F.MooneyRivlin(3, mu1=params[0], mu2=params[1], lamb=params[2], rho=params[3] if len(params) > 3 else 1.0)
+    else:
+        raise ValueError(name)
+    m.has_low_level_dispatcher = False
+    return m
+
+
+def jittered_tet_mesh(F, nx, ny, nz, L, seed, jitter=0.15):
+    """Seeded jittered lattice on [0,L[0]]x[0,L[1]]x[0,L[2]] split by Delaunay, reoriented positive."""
+    from scipy.spatial import Delaunay
+    rng = np.random.default_rng(seed)
+    xs = [np.linspace(0, L[i], n + 1) for i, n in enumerate((nx, ny, nz))]
+    P = np.stack(np.meshgrid(*xs, indexing="ij"), -1).reshape(-1, 3)
+    h = np.array([L[0] / nx, L[1] / ny, L[2] / nz])
+    interior = np.all((P > 1e-12) & (P < np.array(L) - 1e-12), axis=1)
+    P[interior] += rng.uniform(-jitter, jitter, size=(interior.sum(), 3)) * h
+    tri = Delaunay(P)
+    el = tri.simplices.astype(np.int64)
+    v = P[el]
+    vol = np.einsum("ij,ij->i", np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]), v[:, 3] - v[:, 0])
+    keep = np.abs(vol) > 1e-12 * np.prod(h)
+    el = el[keep]
+    vol = vol[keep]
+    neg = vol < 0
+    el[neg, 1], el[neg, 2] = el[neg, 2].copy(), el[neg, 1].copy()
+    mesh = F.Mesh()
+    mesh.element_type = "tet"
+    mesh.elements = el
+    mesh.points = P
+    mesh.nelem = el.shape[0]
+    mesh.nnode = P.shape[0]
+    mesh.GetBoundaryFacesTet()
+    mesh.GetBoundaryEdgesTet()
+    return mesh
+
+
+def build_mesh(F, spec):
+    kind = spec["mesh"]
+    if kind == "cube_hex":
+        mesh = F.Mesh()
+        mesh.Cube(element_type="hex", nx=spec["n"][0], ny=spec["n"][1], nz=spec["n"][2])
+    elif kind == "cube_tet":
+        mesh = F.Mesh()
+        mesh.Cube(element_type="tet", nx=spec["n"][0], ny=spec["n"][1], nz=spec["n"][2])
+    elif kind == "box_hex":
+        mesh = F.Mesh()
+        mesh.Parallelepiped(lower_left_rear_point=(0, 0, 0), upper_right_front_point=spec["L"],
+                            nx=spec["n"][0], ny=spec["n"][1], nz=spec["n"][2], element_type="hex")
+    elif kind == "jitter_tet":
+        mesh = jittered_tet_mesh(F, *spec["n"], L=spec["L"], seed=spec["mesh_seed"])
+    else:
+        raise ValueError(kind)
+    if mesh.element_type == "tet":
+        # the reference's numpy element path integrates with the signed Jacobian determinant
+        # (DisplacementFormulation.py:146) while its native path uses |det| (_KinematicMeasures_.h:94-99);
+        # the two agree only on positively oriented elements, so reorient before raising the order
+        el = np.asarray(mesh.elements).astype(np.int64)
+        v = np.asarray(mesh.points)[el]
+        vol = np.einsum("ij,ij->i", np.cross(v[:, 1] - v[:, 0], v[:, 2] - v[:, 0]), v[:, 3] - v[:, 0])
+        neg = vol < 0
+        el[neg, 1], el[neg, 2] = el[neg, 2].copy(), el[neg, 1].copy()
+        mesh.elements = el
+    if spec["p"] > 1:
+        mesh.GetHighOrderMesh(p=spec["p"])
+    mesh.ChangeType()
+    return mesh
+
+
+def reference_assembly(F, spec, mesh, x, recompute):
+    """K (CSR) and T from the reference's AssembleForm, pure-numpy element path."""
+    mat = make_material(F, spec["material"], spec["params"])
+    kw = {} if spec.get("qdeg") is None else {"quadrature_degree": spec["qdeg"]}
+    form = F.DisplacementFormulation(mesh, **kw)
+    solver = F.FEMSolver(optimise=False, recompute_sparsity_pattern=recompute)
+    K, T = F.AssembleForm(form, mesh, mat, solver, Eulerx=x)
+    return K.tocsr(), np.asarray(T).ravel(), form, mat, solver
+
+
+def element_matrices(F, form, mat, solver, mesh, x, elems):
+    fs = form.function_spaces[0]
+    Ks, ts = [], []
+    for e in elems:
+        X = mesh.points[mesh.elements[e].astype(np.int64)]
+        xe = x[mesh.elements[e].astype(np.int64)]
+        K_e, t_e = form.GetLocalStiffness(fs, mat, X, xe, solver, e)
+        Ks.append(K_e)
+        ts.append(np.asarray(t_e).ravel())
+    return np.array(Ks), np.array(ts)
+
+
+def lumped_mass(F, form, mat, mesh, x):
+    from Florence.FiniteElements.Assembly.Assembly import AssembleExplicit_NoLLD_Mass
+    fs = form.function_spaces[0]
+    form.GetConstantMassIntegrand(fs, mat)
+    solver = F.FEMSolver(optimise=False, analysis_type="dynamic", analysis_subtype="explicit", mass_type="lumped")
+    solver.is_mass_computed = False
+    M = AssembleExplicit_NoLLD_Mass(solver, fs, form, mesh, mat, x, np.zeros(mesh.points.shape[0]))
+    return np.asarray(M).ravel()
+
+
+CASES = [
+    dict(name="hex_p1_nh", mesh="cube_hex", n=(2, 2, 2), p=1, material="NeoHookean", params=(1.0, 10.0), seed=10,
+         amp=0.01, qdeg=None, emat=(0, 7), mass=True),
+    dict(name="hex_p2_nh_q5", mesh="cube_hex", n=(2, 2, 2), p=2, material="NeoHookean", params=(1.0, 10.0), seed=11,
+         amp=0.01, qdeg=5, emat=(0, 3, 7), mass=True, triplet=True),
+    dict(name="hex_p2_mr", mesh="cube_hex", n=(2, 2, 1), p=2, material="MooneyRivlin", params=(0.5, 0.5, 20.0),
+         seed=12, amp=0.05, qdeg=None, emat=(0, 3), mass=False),
+    dict(name="box_hex_p2_nh_big", mesh="box_hex", L=(4.0, 1.0, 1.0), n=(4, 2, 2), p=2, material="NeoHookean",
+         params=(1.0, 1000.0), seed=13, amp=0.02, qdeg=None, emat=(1,), mass=True),
+    dict(name="hex_p3_nh", mesh="cube_hex", n=(1, 1, 2), p=3, material="NeoHookean", params=(1.3, 7.0), seed=14,
+         amp=0.01, qdeg=None, emat=(1,), mass=False),
+    dict(name="hex_p4_nh", mesh="cube_hex", n=(1, 1, 1), p=4, material="NeoHookean", params=(0.8, 30.0), seed=15,
+         amp=0.01, qdeg=None, emat=(0,), mass=False),
+    dict(name="tet_p1_nh", mesh="cube_tet", n=(2, 2, 2), p=1, material="NeoHookean", params=(1.0, 10.0), seed=16,
+         amp=0.01, qdeg=None, emat=(0, 5), mass=True),
+    dict(name="tet_p2_mr", mesh="cube_tet", n=(1, 1, 1), p=2, material="MooneyRivlin", params=(0.5, 0.5, 20.0),
+         seed=17, amp=0.02, qdeg=None, emat=(0, 2), mass=True),
+    dict(name="tet_p3_mr_jitter", mesh="jitter_tet", L=(4.0, 1.0, 1.0), n=(4, 1, 1), mesh_seed=1, p=3,
+         material="MooneyRivlin", params=(0.5, 0.5, 20.0), seed=18, amp=0.01, qdeg=None, emat=(0, 4), mass=True,
+         triplet=True),
+]
+
+
+def make_case(F, spec):
+    t0 = time.time()
+    mesh = build_mesh(F, spec)
+    rng = np.random.default_rng(spec["seed"])
+    x = mesh.points + rng.uniform(-spec["amp"], spec["amp"], size=mesh.points.shape)
+    K, T, form, mat, solver = reference_assembly(F, spec, mesh, x, recompute=False)
+    fs = form.function_spaces[0]
+    out = dict(
+        points=mesh.points, elements=mesh.elements.astype(np.int64), Eulerx=x,
+        Jm=fs.Jm, AllGauss=fs.AllGauss.ravel(), Bases=fs.Bases,
+        material=np.array(spec["material"]), params=np.array(spec["params"], np.float64),
+        K_indptr=K.indptr.astype(np.int32), K_indices=K.indices.astype(np.int32), K_data=K.data, T=T,
+        sp_indices=solver.indices.astype(np.int32), sp_indptr=solver.indptr.astype(np.int32),
+        sp_data_local=solver.data_local_indices.astype(np.int32),
+        sp_data_global=solver.data_global_indices.astype(np.int32),
+    )
+    if spec.get("triplet"):
+        K2, T2, *_ = reference_assembly(F, spec, build_mesh(F, spec), x, recompute=True)
+        out["K_triplet_data"] = K2.data
+        assert np.array_equal(K2.indptr, K.indptr) and np.array_equal(K2.indices, K.indices)
+    emat = list(spec["emat"])
+    Ke, te = element_matrices(F, form, mat, solver, mesh, x, emat)
+    out["emat_ids"] = np.array(emat, np.int64)
+    out["emat_K"] = Ke
+    out["emat_t"] = te
+    if spec.get("mass"):
+        rho = 1.0
+        out["M_lumped"] = lumped_mass(F, form, mat, mesh, x)
+        out["rho"] = np.array(rho)
+    np.savez_compressed(os.path.join(HERE, spec["name"] + ".npz"), **out)
+    print("%-22s E=%-4d npe=%-3d nq=%-3d nnz=%-8d %.1fs" % (spec["name"], mesh.nelem, mesh.elements.shape[1],
+          fs.AllGauss.shape[0], K.nnz, time.time() - t0), flush=True)
+
+
+def make_config1(F):
+    """Structured 8x8x8 p=2 hex cube, Gauss order 5 (125 points), neo-Hookean mu=1, lambda=10,
+    u ~ U(-0.01, 0.01) per dof from default_rng(0). The full CSR is too large to commit, so the
+    fixture keeps the inputs, hashes of the exact integer structure, and value probes."""
+    t0 = time.time()
+    spec = dict(mesh="cube_hex", n=(8, 8, 8), p=2, material="NeoHookean", params=(1.0, 10.0), qdeg=5)
+    mesh = build_mesh(F, spec)
+    rng = np.random.default_rng(0)
+    x = mesh.points + rng.uniform(-0.01, 0.01, size=mesh.points.shape)
+    K, T, form, mat, solver = reference_assembly(F, spec, mesh, x, recompute=False)
+    fs = form.function_spaces[0]
+    v = np.random.default_rng(42).standard_normal(K.shape[0])
+    emat = [0, 137, 511]
+    Ke, te = element_matrices(F, form, mat, solver, mesh, x, emat)
+    out = dict(
+        points=mesh.points, elements=mesh.elements.astype(np.int64), Eulerx=x,
+        Jm=fs.Jm, AllGauss=fs.AllGauss.ravel(), Bases=fs.Bases,
+        material=np.array("NeoHookean"), params=np.array([1.0, 10.0]),
+        nnz=np.array(K.nnz), K_fro=np.array(np.linalg.norm(K.data)), K_sum=np.array(K.data.sum()),
+        K_matvec=K @ v, matvec_seed=np.array(42), T=T,
+        K_diag=K.diagonal(),
+        sha_indptr=np.array(sha(K.indptr, "<i4")), sha_indices=np.array(sha(K.indices, "<i4")),
+        sha_data_local=np.array(sha(solver.data_local_indices, "<i4")),
+        sha_data_global=np.array(sha(solver.data_global_indices, "<i4")),
+        emat_ids=np.array(emat, np.int64), emat_K=Ke, emat_t=te,
+    )
+    np.savez_compressed(os.path.join(HERE, "config1_hex8_p2_q5.npz"), **out)
+    print("config1 E=%d nnz=%d %.1fs" % (mesh.nelem, K.nnz, time.time() - t0), flush=True)
+
+
+if __name__ == "__main__":
+    F = florence_harness.import_florence()
+    only = sys.argv[1:]
+    for spec in CASES:
+        if not only or spec["name"] in only:
+            make_case(F, spec)
+    if not only or "config1" in only:
+        make_config1(F)
