@@ -1,0 +1,16 @@
+"""florence_gb300 -- GB300-native (sm_103a) low-level finite-element assembly for Florence's
+displacement formulation: fused FP64 tangent + residual kernels, a device-built CSR pattern
+with the reference's element-to-nonzero maps, a matrix-free explicit internal force and the
+lumped mass, behind Florence's own low-level assembly interface.
+
+The CUDA library (libflorence_gb300.so, built in-tree) is required: nothing here falls back to
+the CPU.
+"""
+from . import _native
+from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssemblyDF__MooneyRivlin_,
+                       _LowLevelAssemblyDF__NeoHookean_, _LowLevelAssemblyExplicit_DF_DPF_,
+                       __TotalConstantMassIntegrand__, device_sparsity, fp64_peak_gflops, install, material_params)
+
+__all__ = ["ComputeSparsityPattern", "DeviceAssembler", "_LowLevelAssemblyDF__NeoHookean_",
+           "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
+           "__TotalConstantMassIntegrand__", "device_sparsity", "fp64_peak_gflops", "install", "material_params"]

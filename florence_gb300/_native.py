@@ -1,0 +1,74 @@
+"""ctypes binding of libflorence_gb300.so (the C ABI declared in include/florence_gb300.h).
+
+The library is built in-tree by ``florence_gb300.build`` (or ``__graft_entry__.build()``).
+There is no fallback: if the library is missing or fails to load, every entry point raises.
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libflorence_gb300.so")
+
+FL_OK = 0
+FL_ERR_ARG = 1
+FL_ERR_UNSUPPORTED = 2
+FL_ERR_CUDA = 3
+FL_ERR_MESH = 4
+FL_ERR_CAPACITY = 5
+FL_FLAG_NONPOSITIVE_J = 1
+FL_FLAG_BAD_INDEX = 2
+FL_MATERIAL_NEOHOOKEAN = 1
+FL_MATERIAL_MOONEYRIVLIN = 2
+
+
+class FlorenceGB300Error(RuntimeError):
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = _lib.fl_status_string(status).decode() if _lib is not None else str(status)
+        super().__init__("%s failed: %s (status %d)" % (what or "florence_gb300", msg, status))
+
+
+_lib = None
+
+P = ctypes.c_void_p
+I64 = ctypes.c_int64
+D = ctypes.c_double
+INT = ctypes.c_int
+
+_DF_ARGS = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P, P, P, P, P, P, INT, INT, P, P, P, P,
+            D, D, D, D, D, D, D, D, D, D, D, P, P, P]
+
+
+def lib():
+    """The loaded library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("florence_gb300 CUDA library not built: %s is missing "
+                              "(run `python -m florence_gb300.build` or __graft_entry__.build())" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        L.fl_status_string.argtypes = [INT]
+        L.fl_status_string.restype = ctypes.c_char_p
+        L.fl_ComputeSparsityPattern_workspace_size.argtypes = [I64, I64, I64]
+        L.fl_ComputeSparsityPattern_workspace_size.restype = ctypes.c_size_t
+        L.fl_ComputeSparsityPattern.argtypes = [P, I64, I64, I64, I64, P, P, I64, ctypes.POINTER(I64), P, P, P,
+                                                ctypes.c_size_t, P]
+        for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_"):
+            getattr(L, name).argtypes = _DF_ARGS
+        L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
+                                                        D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
+        L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
+        L.fl_measure_fp64_peak.argtypes = [ctypes.POINTER(D), P]
+        _lib = L
+    return _lib
+
+
+def check(status, what=""):
+    if status != FL_OK:
+        raise FlorenceGB300Error(status, what)
+
+
+# every symbol include/florence_gb300.h declares
+EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_ComputeSparsityPattern",
+           "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
+           "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak"]

@@ -1,0 +1,334 @@
+"""Host side of the GB300 assembly engine: Florence's low-level assembly interface on the device.
+
+Two layers:
+
+* ``DeviceAssembler`` keeps a mesh, its function-space tables and its sparsity pattern resident
+  in GPU memory (torch tensors used as plain device buffers) and assembles from device-resident
+  current coordinates: the form a Newton or explicit time loop uses.
+* Drop-in callables with the names, arguments, return values and errors of the reference's
+  Cython wrappers, so that Florence's own dispatcher finds and calls them:
+
+  - ``_LowLevelAssemblyDF__NeoHookean_``, ``_LowLevelAssemblyDF__MooneyRivlin_``
+    (Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDF_.pyx:53-160, names made by
+    AOT_Assembler.py:36-118, looked up by _LowLevelAssembly_.py:45-83);
+  - ``_LowLevelAssemblyExplicit_DF_DPF_`` (_LowLevelAssemblyExplicit_DF_DPF_.pyx:44-152);
+  - ``ComputeSparsityPattern`` (_Assembly_/ComputeSparsityPattern.pyx:44-112);
+  - ``__TotalConstantMassIntegrand__`` for lumped mass (VariationalPrinciple/_Mass_/_MassIntegrand_.pyx:192-348).
+
+  ``install(Florence)`` registers them in Florence's module namespaces.
+
+Every call goes through the CUDA library; there is no CPU path.
+"""
+import ctypes
+import warnings
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+__all__ = ["DeviceAssembler", "ComputeSparsityPattern", "_LowLevelAssemblyDF__NeoHookean_",
+           "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
+           "__TotalConstantMassIntegrand__", "install", "material_params", "fp64_peak_gflops"]
+
+MATERIALS = {"NeoHookean": N.FL_MATERIAL_NEOHOOKEAN, "MooneyRivlin": N.FL_MATERIAL_MOONEYRIVLIN}
+
+
+class NonPositiveJacobianWarning(RuntimeWarning):
+    """det F <= 0 at some Gauss point (the reference propagates such values silently)."""
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _to_dev(a, dtype, device):
+    """Host array -> contiguous device tensor. uint64 node ids travel as int64 bits."""
+    if isinstance(a, torch.Tensor):
+        return a.to(device=device, dtype=dtype).contiguous()
+    a = np.asarray(a)
+    if a.dtype == np.uint64:
+        a = a.view(np.int64)
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=torch.empty(0, dtype=dtype).numpy().dtype)).to(device)
+
+
+def material_params(material, name=None):
+    """(material id, (p0, p1, p2)) for the kernels, read from a Florence material object."""
+    name = name or type(material).__name__
+    if name == "NeoHookean":
+        return N.FL_MATERIAL_NEOHOOKEAN, (float(material.mu), float(material.lamb), 0.0)
+    if name == "MooneyRivlin":
+        return N.FL_MATERIAL_MOONEYRIVLIN, (float(material.mu1), float(material.mu2), float(material.lamb))
+    raise NotImplementedError("Turning optimise option on for {} material is not supported yet. "
+                              "Consider 'optimise=False' for now".format(name))
+
+
+def _check_flags(flags, what):
+    f = int(flags.item())
+    if f & N.FL_FLAG_BAD_INDEX:
+        raise N.FlorenceGB300Error(N.FL_ERR_ARG, what + " (element node id or index map out of range)")
+    if f & N.FL_FLAG_NONPOSITIVE_J:
+        warnings.warn("det F <= 0 at some Gauss point in " + what, NonPositiveJacobianWarning, stacklevel=3)
+
+
+def device_sparsity(elements, nnode, nvar=3, maps=True, stream=None):
+    """Sparsity pattern on the device. elements: int64 device tensor [nelem, npe].
+    Returns (indices, indptr, data_local, data_global) device int32 tensors (maps None if not maps)."""
+    L = N.lib()
+    nelem, npe = elements.shape
+    dev = elements.device
+    ws_bytes = L.fl_ComputeSparsityPattern_workspace_size(nelem, npe, nnode)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    indptr = torch.empty(nnode * nvar + 1, dtype=torch.int32, device=dev)
+    cap = (npe * nvar) ** 2 * nelem
+    dl = torch.empty(cap, dtype=torch.int32, device=dev) if maps else None
+    dg = torch.empty(cap, dtype=torch.int32, device=dev) if maps else None
+    nnz = ctypes.c_int64(0)
+    # the first call only counts (no indices buffer yet), the second fills
+    indices = None
+    st = L.fl_ComputeSparsityPattern(_ptr(elements), nelem, npe, nnode, nvar, _ptr(indptr), None, 0,
+                                     ctypes.byref(nnz), _ptr(dl), _ptr(dg), _ptr(ws), ws_bytes, stream or _stream())
+    if st == N.FL_ERR_CAPACITY:
+        indices = torch.empty(max(nnz.value, 1), dtype=torch.int32, device=dev)
+        st = L.fl_ComputeSparsityPattern(_ptr(elements), nelem, npe, nnode, nvar, _ptr(indptr), _ptr(indices),
+                                         indices.numel(), ctypes.byref(nnz), _ptr(dl), _ptr(dg), _ptr(ws), ws_bytes,
+                                         stream or _stream())
+    if st == N.FL_ERR_MESH:
+        raise ValueError("every node must belong to at least one element")
+    N.check(st, "fl_ComputeSparsityPattern")
+    return indices[:nnz.value], indptr, dl, dg
+
+
+class DeviceAssembler:
+    """Mesh + function space + material resident on the GPU; assembles from device coordinates.
+
+    points [N,3] f64, elements [E,npe] (any integer dtype), Jm [3,npe,nq], AllGauss [nq] or [nq,1],
+    material: 'NeoHookean' (mu, lamb) or 'MooneyRivlin' (mu1, mu2, lamb).
+    mode: 'csr' (the reference's element-to-nonzero maps), 'squeeze' (binary search in each row)
+    or 'triplet' (I, J, V per element entry).
+    """
+
+    def __init__(self, points, elements, Jm, AllGauss, material, params, mode="csr", device="cuda",
+                 requires_geometry_update=1, Bases=None, sparsity=None):
+        self.device = torch.device(device)
+        self.points = _to_dev(points, torch.float64, self.device)
+        self.elements = _to_dev(elements, torch.int64, self.device)
+        self.Jm = _to_dev(Jm, torch.float64, self.device)
+        self.w = _to_dev(np.ravel(AllGauss) if not isinstance(AllGauss, torch.Tensor) else AllGauss.reshape(-1),
+                         torch.float64, self.device)
+        self.Bases = _to_dev(Bases, torch.float64, self.device) if Bases is not None else None
+        self.nnode = self.points.shape[0]
+        self.nelem, self.npe = self.elements.shape
+        self.nq = self.w.shape[0]
+        self.ndof = 3 * self.npe
+        self.material = material
+        self.mat_id = MATERIALS[material]
+        self.params = tuple(float(p) for p in params) + (0.0,) * (3 - len(params))
+        self.mode = mode
+        self.update = int(requires_geometry_update)
+        self.flags = torch.zeros(1, dtype=torch.int32, device=self.device)
+        if mode in ("csr", "squeeze"):
+            if sparsity is None:
+                sparsity = device_sparsity(self.elements, self.nnode, 3, maps=(mode == "csr"))
+            ind, ptr, dl, dg = sparsity
+            self.indices = _to_dev(ind, torch.int32, self.device)
+            self.indptr = _to_dev(ptr, torch.int32, self.device)
+            self.data_local = _to_dev(dl, torch.int32, self.device) if mode == "csr" else None
+            self.data_global = _to_dev(dg, torch.int32, self.device) if mode == "csr" else None
+            self.nnz = self.indices.shape[0]
+        elif mode != "triplet":
+            raise ValueError("mode must be 'csr', 'squeeze' or 'triplet'")
+
+    # -- implicit tangent + residual ------------------------------------------------------------
+    def assemble(self, Eulerx, V=None, T=None, I=None, J=None, stream=None):
+        """Tangent and residual at device coordinates Eulerx [N,3] f64. Accumulates into V/T when
+        given (zeroed tensors otherwise). Returns (V, T) or, in triplet mode, (I, J, V, T)."""
+        L = N.lib()
+        x = Eulerx if Eulerx.is_contiguous() else Eulerx.contiguous()
+        cap = self.nelem * self.ndof * self.ndof
+        if T is None:
+            T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
+        if self.mode == "triplet":
+            I = torch.empty(cap, dtype=torch.int32, device=self.device) if I is None else I
+            J = torch.empty(cap, dtype=torch.int32, device=self.device) if J is None else J
+            V = torch.empty(cap, dtype=torch.float64, device=self.device) if V is None else V
+            Ip, Jp, dl, dg = I, J, None, None
+        else:
+            V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
+            Ip, Jp, dl, dg = self.indptr, self.indices, self.data_local, self.data_global
+        fn = L.fl_GlobalAssemblyDF__NeoHookean_ if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN else \
+            L.fl_GlobalAssemblyDF__MooneyRivlin_
+        p0, p1, p2 = self.params
+        if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN:
+            mu, mu1, mu2, lamb = p0, 0.0, 0.0, p1
+        else:
+            mu, mu1, mu2, lamb = 0.0, p0, p1, p2
+        st = fn(_ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
+                3, 3, self.nq, self.nelem, self.npe, self.nnode, 6, self.update, None, None,
+                _ptr(Ip), _ptr(Jp), _ptr(V), _ptr(T), 1 if self.mode == "triplet" else 0,
+                1 if self.mode == "squeeze" else 0, _ptr(dl), _ptr(dg), None, None,
+                1.0, mu, mu1, mu2, 0.0, 0.0, lamb, 0.0, 0.0, 0.0, 0.0, None, _ptr(self.flags), stream or _stream())
+        N.check(st, "fl_GlobalAssemblyDF")
+        if self.mode == "triplet":
+            return I, J, V, T
+        return V, T
+
+    # -- explicit internal force ----------------------------------------------------------------
+    def internal_force(self, Eulerx, T=None, stream=None):
+        L = N.lib()
+        x = Eulerx if Eulerx.is_contiguous() else Eulerx.contiguous()
+        if T is None:
+            T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
+        p0, p1, p2 = self.params
+        if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN:
+            mu, mu1, mu2, lamb = p0, 0.0, 0.0, p1
+        else:
+            mu, mu1, mu2, lamb = 0.0, p0, p1, p2
+        st = L.fl_GlobalAssemblyExplicit_DF_DPF_(
+            _ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w), 3, 3, self.nq,
+            self.nelem, self.npe, self.nnode, 6, 1, _ptr(T), 1.0, mu, mu1, mu2, 0.0, 0.0, lamb, 0.0, 0.0, 0.0, 0.0,
+            None, self.mat_id, 0, _ptr(self.flags), stream or _stream())
+        N.check(st, "fl_GlobalAssemblyExplicit_DF_DPF_")
+        return T
+
+    # -- lumped mass ----------------------------------------------------------------------------
+    def lumped_mass(self, rho, Bases=None, M=None, stream=None):
+        L = N.lib()
+        B = self.Bases if Bases is None else _to_dev(Bases, torch.float64, self.device)
+        if B is None:
+            raise ValueError("lumped mass needs the basis values (Bases [npe, nq])")
+        if M is None:
+            M = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
+        st = L.fl_LumpedMass(_ptr(self.points), _ptr(self.elements), _ptr(B), _ptr(self.Jm), _ptr(self.w), 3, 3,
+                             self.nq, self.nelem, self.npe, self.nnode, float(rho), _ptr(M), _ptr(self.flags),
+                             stream or _stream())
+        N.check(st, "fl_LumpedMass")
+        return M
+
+    def check_flags(self, what="assembly"):
+        _check_flags(self.flags, what)
+        self.flags.zero_()
+
+
+# ------------------------------------------------------------------------------------------------
+# Drop-in callables (host numpy in, host numpy out, like the reference's Cython wrappers)
+# ------------------------------------------------------------------------------------------------
+
+def ComputeSparsityPattern(mesh, nvar, squeeze_sparsity_pattern=False):
+    """Device twin of ComputeSparsityPattern.pyx:44-112: returns (indices, indptr) when squeezed,
+    else (indices, indptr, data_local_indices, data_global_indices), int32 numpy arrays."""
+    nnode = mesh.points.shape[0]
+    el = _to_dev(mesh.elements, torch.int64, "cuda")
+    ind, ptr, dl, dg = device_sparsity(el, nnode, nvar, maps=not squeeze_sparsity_pattern)
+    torch.cuda.current_stream().synchronize()
+    if squeeze_sparsity_pattern:
+        return ind.cpu().numpy(), ptr.cpu().numpy()
+    return ind.cpu().numpy(), ptr.cpu().numpy(), dl.cpu().numpy(), dg.cpu().numpy()
+
+
+def _check_formulation(formulation, material):
+    if formulation.ndim != 3 or formulation.nvar != 3 or material.H_VoigtSize != 6:
+        raise NotImplementedError("the GB300 assembly covers three-dimensional mechanics (ndim = nvar = 3)")
+
+
+def _low_level_df(name, fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
+    _check_formulation(formulation, material)
+    mat_id, params = material_params(material, name)
+    recompute = bool(fem_solver.recompute_sparsity_pattern)
+    squeeze = bool(getattr(fem_solver, "squeeze_sparsity_pattern", False))
+    mode = "triplet" if recompute else ("squeeze" if squeeze else "csr")
+    sparsity = None
+    if not recompute:
+        sparsity = (fem_solver.indices, fem_solver.indptr,
+                    None if squeeze else fem_solver.data_local_indices,
+                    None if squeeze else fem_solver.data_global_indices)
+    asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, name, params,
+                          mode=mode, requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity)
+    x = _to_dev(Eulerx, torch.float64, asm.device)
+    out = asm.assemble(x)
+    host = [t.cpu().numpy() for t in out]
+    asm.check_flags("_LowLevelAssemblyDF_" + name)
+    return tuple(host)
+
+
+def _LowLevelAssemblyDF__NeoHookean_(fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDF_.pyx:53-160."""
+    return _low_level_df("NeoHookean", fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp)
+
+
+def _LowLevelAssemblyDF__MooneyRivlin_(fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDF_.pyx:53-160."""
+    return _low_level_df("MooneyRivlin", fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp)
+
+
+def _LowLevelAssemblyExplicit_DF_DPF_(function_space, formulation, mesh, material, Eulerx, Eulerp):
+    """Internal force T [nnode*nvar] -- _LowLevelAssemblyExplicit_DF_DPF_.pyx:44-152 (mechanics)."""
+    if formulation.fields != "mechanics":
+        raise NotImplementedError("the GB300 explicit assembly covers the displacement formulation")
+    _check_formulation(formulation, material)
+    name = getattr(material, "mtype", type(material).__name__)
+    if name not in MATERIALS:
+        raise NotImplementedError("Low level assembly for material {} not available for explicit analysis."
+                                  " Consider 'optimise=False' for now".format(name))
+    _, params = material_params(material, name)
+    asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, name, params,
+                          mode="triplet")
+    T = asm.internal_force(_to_dev(Eulerx, torch.float64, asm.device))
+    out = T.cpu().numpy()
+    asm.check_flags("_LowLevelAssemblyExplicit_DF_DPF_")
+    return out
+
+
+def __TotalConstantMassIntegrand__(mesh, function_space, formulation, mass_type="lumped",
+                                   recompute_sparsity_pattern=True, squeeze_sparsity_pattern=False,
+                                   indices=None, indptr=None, data_global_indices=None, data_local_indices=None):
+    """Lumped mass of _MassIntegrand_.pyx:192-348: returns (mass [nvar*N,1], I, J, V) or (mass, V),
+    with the 1-element placeholder I/J/V the reference returns for lumped mass."""
+    if mass_type != "lumped":
+        raise NotImplementedError("the GB300 mass assembly provides the lumped (row-sum) mass")
+    if formulation.nvar != 3 or mesh.points.shape[1] != 3:
+        raise NotImplementedError("the GB300 mass assembly covers three-dimensional mechanics")
+    # constant_mass_integrand[g] = rho N N^T (x) I3 (VariationalPrinciple.py:269-290): its entries sum
+    # to 3 rho (sum_a N_a)^2 at every Gauss point, which recovers rho
+    cmi = np.asarray(formulation.constant_mass_integrand)
+    nsum = float(np.asarray(function_space.Bases)[:, 0].sum())
+    rho = float(cmi[0].sum()) / (3.0 * nsum * nsum)
+    asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, "NeoHookean",
+                          (1.0, 1.0), mode="triplet", Bases=function_space.Bases)
+    M = asm.lumped_mass(rho).cpu().numpy()[:, None]
+    asm.check_flags("__TotalConstantMassIntegrand__")
+    z_i, z_v = np.zeros(1, np.int32), np.zeros(1, np.float64)
+    if recompute_sparsity_pattern:
+        return M, z_i, z_i.copy(), z_v
+    return M, z_v
+
+
+def install(florence):
+    """Registers the GB300 callables in the reference's module namespaces, so that
+    FEMSolver(optimise=True) / Assemble / AssembleExplicit dispatch to them."""
+    import importlib
+    ll = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly._LowLevelAssembly_")
+    ll._LowLevelAssemblyDF__NeoHookean_ = _LowLevelAssemblyDF__NeoHookean_
+    ll._LowLevelAssemblyDF__MooneyRivlin_ = _LowLevelAssemblyDF__MooneyRivlin_
+    ll._LowLevelAssemblyExplicit_DF_DPF_ = _LowLevelAssemblyExplicit_DF_DPF_
+    ll.has_low_level_dispatcher = True
+    try:
+        sp = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly.ComputeSparsityPattern")
+    except ImportError:
+        import sys
+        import types
+        sp = types.ModuleType(florence.__name__ + ".FiniteElements.Assembly.ComputeSparsityPattern")
+        sys.modules[sp.__name__] = sp
+    sp.ComputeSparsityPattern = ComputeSparsityPattern
+    return ll
+
+
+def fp64_peak_gflops():
+    """Measured FP64 FMA throughput of this GPU (GFLOP/s)."""
+    g = ctypes.c_double(0.0)
+    N.check(N.lib().fl_measure_fp64_peak(ctypes.byref(g), _stream()), "fl_measure_fp64_peak")
+    return g.value

@@ -1,0 +1,413 @@
+// fl_assembly.cu -- fused FP64 tangent + residual assembly for the displacement formulation
+// (replaces _GlobalAssemblyDF_, Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDF_.h:8-176).
+//
+// One CTA assembles EPC elements. Per element:
+//  1. gather X, x of the element's nodes into shared memory;
+//  2. one thread per Gauss point: kinematics, material, and the tangent pulled back to the
+//     reference element,   Ahat[(i,d),(k,e)] = detJ sum_{j,l} G[j][d] A_ijkl G[l][e],
+//     A_ijkl = c_ijkl + d_ik sigma_jl (constitutive + geometric stiffness in one tensor),
+//     G = (dx/dxi)^{-1}; plus S[i][d] = detJ sum_j sigma_ij G[j][d] for the residual.
+//     Ahat is symmetric (45 values); both live in shared memory for all Gauss points;
+//  3. K_e[(a,i),(b,k)] = sum_g sum_{d,e} Jm[d][a][g] Ahat_g[(i,d),(k,e)] Jm[e][b][g] with
+//     U_g[b][(i,d),k] = sum_e Ahat_g[(i,d),(k,e)] Jm[e][b][g] built cooperatively per Gauss-point
+//     chunk, then 3 FMAs per stiffness entry. Only node blocks a <= b are formed (K_e is
+//     symmetric), 9 register accumulators per block, blocks ordered b-major so a warp mostly
+//     reads the same U row (shared-memory broadcast);
+//  4. scatter: triplets, CSR through the reference's element-to-nonzero maps, or CSR by binary
+//     search in the row (squeeze); residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d] into T.
+// The FP64 pipe bounds this kernel (GB300 has a reduced FP64 rate), so the design minimises FP64
+// operations: 3 per stiffness entry per Gauss point plus a per-point cost linear in the nodes.
+#include "fl_common.cuh"
+
+namespace fl {
+
+template <int NPE>
+struct AsmCfg;
+// TPE threads per element, EPC elements per CTA, MAXB node blocks per thread per pass
+template <> struct AsmCfg<4> { static constexpr int TPE = 32, EPC = 8, MAXB = 1; };
+template <> struct AsmCfg<8> { static constexpr int TPE = 32, EPC = 8, MAXB = 2; };
+template <> struct AsmCfg<10> { static constexpr int TPE = 64, EPC = 4, MAXB = 1; };
+template <> struct AsmCfg<20> { static constexpr int TPE = 128, EPC = 2, MAXB = 2; };
+template <> struct AsmCfg<27> { static constexpr int TPE = 384, EPC = 1, MAXB = 1; };
+template <> struct AsmCfg<35> { static constexpr int TPE = 320, EPC = 1, MAXB = 2; };
+template <> struct AsmCfg<64> { static constexpr int TPE = 416, EPC = 1, MAXB = 5; };
+template <> struct AsmCfg<125> { static constexpr int TPE = 512, EPC = 1, MAXB = 4; };
+
+constexpr int QSTRIDE = 54;  // 45 symmetric Ahat entries + 9 residual entries per Gauss point
+
+struct AsmArgs {
+    const double *points;
+    const uint64_t *elements;
+    const double *Eulerx;
+    const double *Jm;
+    const double *w;
+    int64_t nelem, nnode;
+    int nq, update, mode, qc;  // mode: 0 triplets, 1 CSR via maps, 2 CSR via row search
+    int32_t *I, *J;
+    double *V, *T;
+    const int32_t *indptr, *indices, *dl, *dg;
+    MatParams mp;
+    int *flags;
+};
+
+// index of (I,K), I,K in 0..8, in the packed upper triangle of a symmetric 9x9
+__device__ __forceinline__ int sym9(int I, int K) {
+    const int r = I < K ? I : K, c = I < K ? K : I;
+    return r * 9 - (r * (r - 1)) / 2 + (c - r);
+}
+
+// Gauss-point data: Ahat (packed) and S, see the file comment.
+template <int NPE, int MAT>
+__device__ void qp_data(const AsmArgs &A, int g, const double *X, const double *x, double *q, int &flag) {
+    const double *Jm = A.Jm;
+    const int nq = A.nq;
+    auto jm = [&](int d, int a) { return __ldg(Jm + ((size_t)d * NPE + a) * nq + g); };
+    double G[9], F[9];
+    const double detJ = kinematics<NPE>(jm, X, x, __ldg(A.w + g), A.update, G, F);
+    double sig[6], b[6], J, c1, c2, cbb;
+    material<MAT>(F, A.mp, sig, b, J, c1, c2, cbb);
+    if (!(J > 0.0)) flag |= FL_FLAG_NONPOSITIVE_J;
+    // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G  (all indexed [d][e] or [i][d])
+    double GG[9], GsG[9], sG[9], bG[9], GbG[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            sG[i * 3 + d] = sig[s6(i, 0)] * G[0 * 3 + d] + sig[s6(i, 1)] * G[1 * 3 + d] + sig[s6(i, 2)] * G[2 * 3 + d];
+            bG[i * 3 + d] = b[s6(i, 0)] * G[0 * 3 + d] + b[s6(i, 1)] * G[1 * 3 + d] + b[s6(i, 2)] * G[2 * 3 + d];
+        }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            GG[d * 3 + e] = G[0 * 3 + d] * G[0 * 3 + e] + G[1 * 3 + d] * G[1 * 3 + e] + G[2 * 3 + d] * G[2 * 3 + e];
+            GsG[d * 3 + e] = G[0 * 3 + d] * sG[0 * 3 + e] + G[1 * 3 + d] * sG[1 * 3 + e] + G[2 * 3 + d] * sG[2 * 3 + e];
+            GbG[d * 3 + e] = G[0 * 3 + d] * bG[0 * 3 + e] + G[1 * 3 + d] * bG[1 * 3 + e] + G[2 * 3 + d] * bG[2 * 3 + e];
+        }
+    // Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
+    //                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ]
+#pragma unroll
+    for (int I = 0; I < 9; ++I)
+#pragma unroll
+        for (int K = I; K < 9; ++K) {
+            const int i = I / 3, d = I % 3, k = K / 3, e = K % 3;
+            double v = c1 * G[k * 3 + d] * G[i * 3 + e] + c2 * G[i * 3 + d] * G[k * 3 + e];
+            if (i == k) v += c1 * GG[d * 3 + e] + GsG[d * 3 + e];
+            if (MAT == MOONEYRIVLIN)
+                v += cbb * (2.0 * bG[i * 3 + d] * bG[k * 3 + e] - b[s6(i, k)] * GbG[d * 3 + e] - bG[k * 3 + d] * bG[i * 3 + e]);
+            q[sym9(I, K)] = detJ * v;
+        }
+#pragma unroll
+    for (int k = 0; k < 9; ++k) q[45 + k] = detJ * sG[k];  // S[i][d]
+}
+
+template <int NPE, int MAT>
+__global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
+    assemble_df_kernel(const AsmArgs A) {
+    constexpr int TPE = AsmCfg<NPE>::TPE, EPC = AsmCfg<NPE>::EPC, MAXB = AsmCfg<NPE>::MAXB;
+    constexpr int NT = TPE * EPC, NDOF = 3 * NPE, NBLK = NPE * (NPE + 1) / 2;
+    constexpr int PER_PASS = TPE * MAXB, NPASS = (NBLK + PER_PASS - 1) / PER_PASS;
+    const int nq = A.nq, QC = A.qc;
+
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *Xs = reinterpret_cast<double *>(smem_raw);      // [EPC][NPE*3]
+    double *xs = Xs + EPC * NPE * 3;                          // [EPC][NPE*3]
+    double *Qs = xs + EPC * NPE * 3;                          // [EPC][nq][QSTRIDE]
+    double *Jc = Qs + (size_t)EPC * nq * QSTRIDE;             // [QC][NPE][3]
+    double *Us = Jc + (size_t)QC * NPE * 3;                   // [EPC][QC][NPE][27]
+    int *nodes = reinterpret_cast<int *>(Us + (size_t)EPC * QC * NPE * 27);  // [EPC][NPE]
+    int *inv = nodes + EPC * NPE;                                             // [EPC][NDOF]
+    __shared__ int s_flag;
+    __shared__ int64_t s_nnz;
+
+    const int tid = threadIdx.x, slot = tid / TPE, lt = tid % TPE;
+    const int64_t e = (int64_t)blockIdx.x * EPC + slot;
+    const bool active = e < A.nelem;
+    int flag = 0;
+    if (tid == 0) {
+        s_flag = 0;
+        s_nnz = (A.mode != 0) ? (int64_t)A.indptr[3 * A.nnode] : 0;
+    }
+
+    // 1. gather
+    const int64_t cap = (int64_t)NDOF * NDOF;
+    if (active) {
+        for (int a = lt; a < NPE; a += TPE) {
+            uint64_t nd = A.elements[e * NPE + a];
+            if (nd >= (uint64_t)A.nnode) {
+                flag |= FL_FLAG_BAD_INDEX;
+                nd = 0;
+            }
+            nodes[slot * NPE + a] = (int)nd;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                Xs[(slot * NPE + a) * 3 + k] = A.points[nd * 3 + k];
+                xs[(slot * NPE + a) * 3 + k] = A.Eulerx[nd * 3 + k];
+            }
+        }
+        if (A.mode == 1) {
+            // invert the element's dof permutation carried by data_local_indices:
+            // dl[e*cap + i*NDOF + j] = perm[i]*NDOF + perm[j]  ->  inv[perm[i]] = i
+            for (int i = lt; i < NDOF; i += TPE) {
+                const int v = A.dl[e * cap + (int64_t)i * NDOF];
+                const int p = v / NDOF;
+                if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
+                else inv[slot * NDOF + p] = i;
+            }
+        }
+    }
+    __syncthreads();
+
+    // 2. Gauss-point data
+    if (active)
+        for (int g = lt; g < nq; g += TPE)
+            qp_data<NPE, MAT>(A, g, Xs + slot * NPE * 3, xs + slot * NPE * 3, Qs + ((size_t)slot * nq + g) * QSTRIDE, flag);
+    __syncthreads();
+
+    // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d]
+    if (active && A.update) {
+        for (int r = lt; r < NDOF; r += TPE) {
+            const int a = r / 3, i = r % 3;
+            double t = 0.0;
+            const double *q = Qs + (size_t)slot * nq * QSTRIDE + 45 + i * 3;
+            for (int g = 0; g < nq; ++g, q += QSTRIDE)
+                t += __ldg(A.Jm + (size_t)a * nq + g) * q[0] + __ldg(A.Jm + ((size_t)NPE + a) * nq + g) * q[1] +
+                     __ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g) * q[2];
+            atomicAdd(A.T + 3 * (int64_t)nodes[slot * NPE + a] + i, t);
+        }
+    }
+
+    // 3. stiffness, in passes over the node blocks (a <= b, b-major)
+    for (int pass = 0; pass < NPASS; ++pass) {
+        double acc[MAXB][9];
+        int ba[MAXB], bb[MAXB];
+#pragma unroll
+        for (int m = 0; m < MAXB; ++m) {
+            const int blk = pass * PER_PASS + m * TPE + lt;
+            int b = (int)((sqrtf(8.0f * blk + 1.0f) - 1.0f) * 0.5f);
+            while (b * (b + 1) / 2 > blk) --b;
+            while ((b + 1) * (b + 2) / 2 <= blk) ++b;
+            ba[m] = blk < NBLK ? blk - b * (b + 1) / 2 : -1;
+            bb[m] = b;
+#pragma unroll
+            for (int k = 0; k < 9; ++k) acc[m][k] = 0.0;
+        }
+        for (int c0 = 0; c0 < nq; c0 += QC) {
+            const int qc = min(QC, nq - c0);
+            for (int idx = tid; idx < qc * NPE * 3; idx += NT) {
+                const int q = idx / (NPE * 3), r = idx % (NPE * 3), a = r / 3, d = r % 3;
+                Jc[idx] = __ldg(A.Jm + ((size_t)d * NPE + a) * nq + c0 + q);
+            }
+            __syncthreads();
+            if (active) {
+                for (int idx = lt; idx < qc * NPE * 27; idx += TPE) {
+                    const int q = idx / (NPE * 27), r = idx % (NPE * 27), b = r / 27, s = r % 27;
+                    const int I = s / 3, k = s % 3;  // s = (i*3+d)*3 + k, I = i*3+d
+                    const double *qq = Qs + ((size_t)slot * nq + c0 + q) * QSTRIDE;
+                    const double *jb = Jc + (q * NPE + b) * 3;
+                    Us[(((size_t)slot * QC + q) * NPE + b) * 27 + s] =
+                        qq[sym9(I, k * 3 + 0)] * jb[0] + qq[sym9(I, k * 3 + 1)] * jb[1] + qq[sym9(I, k * 3 + 2)] * jb[2];
+                }
+            }
+            __syncthreads();
+            if (active) {
+                for (int q = 0; q < qc; ++q) {
+#pragma unroll
+                    for (int m = 0; m < MAXB; ++m) {
+                        if (ba[m] < 0) continue;
+                        const double *ja = Jc + (q * NPE + ba[m]) * 3;
+                        const double j0 = ja[0], j1 = ja[1], j2 = ja[2];
+                        const double *u = Us + (((size_t)slot * QC + q) * NPE + bb[m]) * 27;
+#pragma unroll
+                        for (int i = 0; i < 3; ++i)
+#pragma unroll
+                            for (int k = 0; k < 3; ++k)
+                                acc[m][i * 3 + k] += j0 * u[(i * 3 + 0) * 3 + k] + j1 * u[(i * 3 + 1) * 3 + k] +
+                                                     j2 * u[(i * 3 + 2) * 3 + k];
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        // 4. scatter this pass's blocks
+        if (active) {
+#pragma unroll
+            for (int m = 0; m < MAXB; ++m) {
+                if (ba[m] < 0) continue;
+                const int a = ba[m], b = bb[m];
+                const int na = nodes[slot * NPE + a], nb = nodes[slot * NPE + b];
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        const double v = acc[m][i * 3 + k];
+                        const int r = 3 * a + i, c = 3 * b + k;
+                        const int gr = 3 * na + i, gc = 3 * nb + k;
+                        for (int mirror = 0; mirror < (a == b ? 1 : 2); ++mirror) {
+                            const int rr = mirror ? c : r, cc = mirror ? r : c;
+                            const int grr = mirror ? gc : gr, gcc = mirror ? gr : gc;
+                            if (A.mode == 0) {
+                                const int64_t o = e * cap + (int64_t)rr * NDOF + cc;
+                                A.I[o] = grr;
+                                A.J[o] = gcc;
+                                A.V[o] = v;
+                            } else if (A.mode == 1) {
+                                const int ir = inv[slot * NDOF + rr], ic = inv[slot * NDOF + cc];
+                                const int64_t pos = ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
+                                                        ? (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic] : -1;
+                                if (pos >= 0 && pos < s_nnz) atomicAdd(A.V + pos, v);
+                                else flag |= FL_FLAG_BAD_INDEX;
+                            } else {
+                                int lo = A.indptr[grr], hi = A.indptr[grr + 1];
+                                while (hi - lo > 1) {
+                                    const int mid = lo + (hi - lo) / 2;
+                                    if (gcc < A.indices[mid]) hi = mid; else lo = mid;
+                                }
+                                if (lo < A.indptr[grr + 1] && A.indices[lo] == gcc) atomicAdd(A.V + lo, v);
+                                else flag |= FL_FLAG_BAD_INDEX;
+                            }
+                        }
+                    }
+            }
+        }
+    }
+    if (flag) atomicOr(&s_flag, flag);
+    __syncthreads();
+    if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
+}
+
+template <int NPE>
+static size_t asm_smem_bytes(int nq, int qc) {
+    constexpr int EPC = AsmCfg<NPE>::EPC;
+    return sizeof(double) * ((size_t)2 * EPC * NPE * 3 + (size_t)EPC * nq * QSTRIDE + (size_t)qc * NPE * 3 +
+                             (size_t)EPC * qc * NPE * 27) +
+           sizeof(int) * ((size_t)EPC * NPE + (size_t)EPC * 3 * NPE);
+}
+
+template <int NPE>
+static int asm_qc(int nq) {
+    constexpr int EPC = AsmCfg<NPE>::EPC;
+    int qc = 32768 / (EPC * NPE * 27 * 8);
+    if (qc < 1) qc = 1;
+    if (qc > nq) qc = nq;
+    return qc;
+}
+
+template <int NPE, int MAT>
+static int launch_asm(AsmArgs A, cudaStream_t stream) {
+    constexpr int EPC = AsmCfg<NPE>::EPC, NT = AsmCfg<NPE>::TPE * EPC;
+    A.qc = asm_qc<NPE>(A.nq);
+    const size_t smem = asm_smem_bytes<NPE>(A.nq, A.qc);
+    if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
+    FL_CUDA_TRY(cudaFuncSetAttribute(assemble_df_kernel<NPE, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int64_t grid = (A.nelem + EPC - 1) / EPC;
+    if (grid == 0) return FL_OK;
+    assemble_df_kernel<NPE, MAT><<<(unsigned)grid, NT, smem, stream>>>(A);
+    return launch_status();
+}
+
+template <int MAT>
+static int dispatch_asm(int npe, const AsmArgs &A, cudaStream_t s) {
+    switch (npe) {
+        case 4: return launch_asm<4, MAT>(A, s);
+        case 8: return launch_asm<8, MAT>(A, s);
+        case 10: return launch_asm<10, MAT>(A, s);
+        case 20: return launch_asm<20, MAT>(A, s);
+        case 27: return launch_asm<27, MAT>(A, s);
+        case 35: return launch_asm<35, MAT>(A, s);
+        case 64: return launch_asm<64, MAT>(A, s);
+        case 125: return launch_asm<125, MAT>(A, s);
+        default: return FL_ERR_UNSUPPORTED;
+    }
+}
+
+static int global_assembly_df(int mat, const double *points, const uint64_t *elements, const double *Eulerx,
+                              const double *Jm, const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss,
+                              int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t H_VoigtSize,
+                              int64_t requires_geometry_update, int32_t *I_stiff, int32_t *J_stiff, double *V_stiff,
+                              double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
+                              const int32_t *data_local_indices, const int32_t *data_global_indices, MatParams mp,
+                              int *flags, cudaStream_t stream) {
+    if (ndim != 3 || nvar != 3 || H_VoigtSize != 6) return FL_ERR_ARG;
+    if (nelem < 0 || nnode <= 0 || ngauss <= 0 || ngauss > 343) return nelem < 0 || nnode <= 0 ? FL_ERR_ARG : FL_ERR_UNSUPPORTED;
+    if (3 * nnode + 2 > INT32_MAX) return FL_ERR_UNSUPPORTED;
+    if (!points || !elements || !Eulerx || !Jm || !AllGauss || !V_stiff || !T) return FL_ERR_ARG;
+    AsmArgs A;
+    A.points = points;
+    A.elements = elements;
+    A.Eulerx = Eulerx;
+    A.Jm = Jm;
+    A.w = AllGauss;
+    A.nelem = nelem;
+    A.nnode = nnode;
+    A.nq = (int)ngauss;
+    A.update = requires_geometry_update ? 1 : 0;
+    A.I = nullptr;
+    A.J = nullptr;
+    A.V = V_stiff;
+    A.T = T;
+    A.indptr = A.indices = A.dl = A.dg = nullptr;
+    A.mp = mp;
+    A.flags = flags;
+    if (recompute_sparsity_pattern) {
+        if (!I_stiff || !J_stiff) return FL_ERR_ARG;
+        A.mode = 0;
+        A.I = I_stiff;
+        A.J = J_stiff;
+    } else {
+        // the reference's wrapper passes indptr in I_stiff and indices in J_stiff
+        if (!I_stiff || !J_stiff) return FL_ERR_ARG;
+        A.indptr = I_stiff;
+        A.indices = J_stiff;
+        if (squeeze_sparsity_pattern) {
+            A.mode = 2;
+        } else {
+            if (!data_local_indices || !data_global_indices) return FL_ERR_ARG;
+            A.mode = 1;
+            A.dl = data_local_indices;
+            A.dg = data_global_indices;
+        }
+    }
+    if (mat == NEOHOOKEAN) return dispatch_asm<NEOHOOKEAN>((int)nodeperelem, A, stream);
+    return dispatch_asm<MOONEYRIVLIN>((int)nodeperelem, A, stream);
+}
+
+}  // namespace fl
+
+extern "C" {
+
+const char *fl_status_string(int status) {
+    switch (status) {
+        case FL_OK: return "ok";
+        case FL_ERR_ARG: return "invalid argument";
+        case FL_ERR_UNSUPPORTED: return "unsupported element size, Gauss point count or material";
+        case FL_ERR_CUDA: return "CUDA error";
+        case FL_ERR_MESH: return "mesh rejected: a node belongs to no element";
+        case FL_ERR_CAPACITY: return "output or workspace buffer too small";
+        default: return "unknown status";
+    }
+}
+
+int fl_GlobalAssemblyDF__NeoHookean_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
+    (void)sorter; (void)rho; (void)mu1; (void)mu2; (void)mu3; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3;
+    (void)eps_e; (void)anisotropic_orientations;
+    fl::MatParams mp{mu, lamb, 0.0};
+    return fl::global_assembly_df(fl::NEOHOOKEAN, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem,
+                                  nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
+                                  recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
+                                  data_global_indices, mp, flags, (cudaStream_t)stream);
+}
+
+int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
+    (void)sorter; (void)rho; (void)mu; (void)mu3; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
+    (void)anisotropic_orientations;
+    fl::MatParams mp{mu1, mu2, lamb};
+    return fl::global_assembly_df(fl::MOONEYRIVLIN, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem,
+                                  nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
+                                  recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
+                                  data_global_indices, mp, flags, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,139 @@
+// fl_common.cuh -- device helpers shared by the sm_103a kernels: 3x3 algebra, the hyperelastic
+// materials at one Gauss point, and the launch/error plumbing of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/florence_gb300.h"
+
+#define FL_FLAG_BAD_INDEX 2 /* an element node id or a map entry is out of range; the entry was skipped */
+
+namespace fl {
+
+#define FL_CUDA_TRY(expr)                         \
+    do {                                          \
+        cudaError_t _e = (expr);                  \
+        if (_e != cudaSuccess) return FL_ERR_CUDA; \
+    } while (0)
+
+inline int launch_status() { return cudaGetLastError() == cudaSuccess ? FL_OK : FL_ERR_CUDA; }
+
+// Material numbers (match FL_MATERIAL_*).
+enum { NEOHOOKEAN = 1, MOONEYRIVLIN = 2 };
+
+struct MatParams {
+    double p0, p1, p2;  // neo-Hookean: mu, lamb; Mooney-Rivlin: mu1, mu2, lamb
+};
+
+// Inverse of a row-major 3x3 by adjugate over determinant; returns the determinant.
+__device__ __forceinline__ double inv3(const double *m, double *r) {
+    r[0] = m[4] * m[8] - m[5] * m[7];
+    r[1] = m[2] * m[7] - m[1] * m[8];
+    r[2] = m[1] * m[5] - m[2] * m[4];
+    r[3] = m[5] * m[6] - m[3] * m[8];
+    r[4] = m[0] * m[8] - m[2] * m[6];
+    r[5] = m[2] * m[3] - m[0] * m[5];
+    r[6] = m[3] * m[7] - m[4] * m[6];
+    r[7] = m[1] * m[6] - m[0] * m[7];
+    r[8] = m[0] * m[4] - m[1] * m[3];
+    const double det = m[0] * r[0] + m[1] * r[3] + m[2] * r[6];
+    const double s = 1.0 / det;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) r[i] *= s;
+    return det;
+}
+
+__device__ __forceinline__ double det3(const double *m) {
+    return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+// Symmetric 3x3 stored as xx,yy,zz,xy,xz,yz (the reference's Voigt order).
+__device__ __forceinline__ int s6(int i, int j) {
+    return i == j ? i : (i + j == 1 ? 3 : (i + j == 2 ? 4 : 5));
+}
+
+// Cauchy stress sigma (sym6), J = det F, b = F F^T (sym6) and the coefficients of the spatial
+// elasticity tensor written as
+//   c_ijkl = c1 (d_ik d_jl + d_il d_jk) + c2 d_ij d_kl + cbb (2 b_ij b_kl - b_ik b_jl - b_il b_jk).
+// Neo-Hookean (_NeoHookean_.h:34-46):  sigma = mu/J (b - I) + lamb (J-1) I,
+//   c1 = mu/J - lamb (J-1), c2 = lamb (2J-1), cbb = 0.
+// Mooney-Rivlin (_MooneyRivlin_.h:38-64): sigma = 2mu1/J b + 2mu2/J (tr(b) b - b^2) - 2(mu1+2mu2)/J I
+//   + lamb (J-1) I, c1 = 2(mu1+2mu2)/J - lamb (J-1), c2 = lamb (2J-1), cbb = 2 mu2/J.
+template <int MAT>
+__device__ __forceinline__ void material(const double *F, const MatParams &mp, double *sig, double *b, double &J,
+                                         double &c1, double &c2, double &cbb) {
+    J = det3(F);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = i; j < 3; ++j)
+            b[s6(i, j)] = F[i * 3 + 0] * F[j * 3 + 0] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
+    const double iJ = 1.0 / J;
+    if (MAT == NEOHOOKEAN) {
+        const double mu = mp.p0, lamb = mp.p1;
+        const double a = mu * iJ, dv = lamb * (J - 1.0);
+        sig[0] = a * (b[0] - 1.0) + dv;
+        sig[1] = a * (b[1] - 1.0) + dv;
+        sig[2] = a * (b[2] - 1.0) + dv;
+        sig[3] = a * b[3];
+        sig[4] = a * b[4];
+        sig[5] = a * b[5];
+        c1 = a - dv;
+        c2 = lamb * (2.0 * J - 1.0);
+        cbb = 0.0;
+    } else {
+        const double mu1 = mp.p0, mu2 = mp.p1, lamb = mp.p2;
+        const double trb = b[0] + b[1] + b[2];
+        double bb[6];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j)
+                bb[s6(i, j)] = b[s6(i, 0)] * b[s6(0, j)] + b[s6(i, 1)] * b[s6(1, j)] + b[s6(i, 2)] * b[s6(2, j)];
+        const double A = 2.0 * mu1 * iJ, B = 2.0 * mu2 * iJ, C = 2.0 * (mu1 + 2.0 * mu2) * iJ, dv = lamb * (J - 1.0);
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sig[k] = A * b[k] + B * (trb * b[k] - bb[k]);
+        sig[0] += dv - C;
+        sig[1] += dv - C;
+        sig[2] += dv - C;
+        c1 = C - dv;
+        c2 = lamb * (2.0 * J - 1.0);
+        cbb = B;
+    }
+}
+
+// Kinematics at one Gauss point from the reference-element gradients jm(d, a) (a callable) and
+// the element's reference/current coordinates X, x [npe*3]:
+//   Px = dx/dxi, PX = dX/dxi (rows d = xi direction), G = Px^{-1} (spatial gradients are
+//   grad N_a[j] = sum_d G[j][d] jm(d,a)), F[i][j] = sum_d Px[d][i] PX^{-1}[j][d], and
+//   detJ = w |det Px| (update) or w |det PX|, as _KinematicMeasures_.h:64-119 defines them.
+template <int NPE, class JmFn>
+__device__ __forceinline__ double kinematics(JmFn jm, const double *X, const double *x, double w, int update, double *G,
+                                             double *F) {
+    double PX[9], Px[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) PX[k] = Px[k] = 0.0;
+#pragma unroll 4
+    for (int a = 0; a < NPE; ++a) {
+        const double j0 = jm(0, a), j1 = jm(1, a), j2 = jm(2, a);
+        const double X0 = X[a * 3], X1 = X[a * 3 + 1], X2 = X[a * 3 + 2];
+        const double x0 = x[a * 3], x1 = x[a * 3 + 1], x2 = x[a * 3 + 2];
+        PX[0] += j0 * X0; PX[1] += j0 * X1; PX[2] += j0 * X2;
+        PX[3] += j1 * X0; PX[4] += j1 * X1; PX[5] += j1 * X2;
+        PX[6] += j2 * X0; PX[7] += j2 * X1; PX[8] += j2 * X2;
+        Px[0] += j0 * x0; Px[1] += j0 * x1; Px[2] += j0 * x2;
+        Px[3] += j1 * x0; Px[4] += j1 * x1; Px[5] += j1 * x2;
+        Px[6] += j2 * x0; Px[7] += j2 * x1; Px[8] += j2 * x2;
+    }
+    double iPX[9];
+    const double detX = inv3(PX, iPX);
+    const double detx = inv3(Px, G);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            F[i * 3 + j] = Px[0 * 3 + i] * iPX[j * 3 + 0] + Px[1 * 3 + i] * iPX[j * 3 + 1] + Px[2 * 3 + i] * iPX[j * 3 + 2];
+    return update ? w * fabs(detx) : w * fabs(detX);
+}
+
+}  // namespace fl

@@ -1,0 +1,343 @@
+// fl_sparsity.cu -- device construction of the global CSR pattern and of the reference's
+// element-to-nonzero maps, bit-identical to ComputeSparsityPattern
+// (Florence/FiniteElements/Assembly/_Assembly_/ComputeSparsityPattern.pyx:44-112 and
+//  ComputeSparsityPattern.h:22-125):
+//   - row nvar*n+j of node n lists, for every node m adjacent to n (sharing an element, n itself
+//     included) in increasing order, the columns nvar*m+0 .. nvar*m+nvar-1;
+//   - data_global_indices[e*cap + i*ndof + j] is the CSR position of (row rc[i], column rc[j]) and
+//     data_local_indices[e*cap + i*ndof + j] = rcl[i]*ndof + rcl[j], where rc/rcl enumerate the
+//     element's dofs in increasing node order (rc = global dof, rcl = local dof).
+// Steps: node incidence counts -> scan -> incidence lists; per node a CTA gathers the nodes of
+// its elements into shared memory, bitonic-sorts them and counts/writes the distinct ones; a
+// scan of the per-node counts gives indptr; per element a CTA ranks its nodes and binary-searches
+// each dof pair in its row.
+#include <algorithm>
+
+#include "fl_common.cuh"
+
+namespace fl {
+
+constexpr int SP_MAX_CAND = 16384;  // candidate neighbour entries per node held in shared memory
+
+struct SpWork {
+    int32_t *cnt;     // [nnode+1] incidence counts, then exclusive scan (starts)
+    int32_t *cursor;  // [nnode]
+    int32_t *list;    // [nelem*npe] incident elements per node
+    int64_t *nbr;     // [nnode+1] distinct neighbours per node, then exclusive scan
+    int64_t *bsum;    // [scan block sums]
+    int32_t *info;    // [4]: error bits, max incidence degree
+};
+
+constexpr int SCAN_ITEMS = 2048, SCAN_THREADS = 512;
+
+static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+static size_t sp_layout(int64_t nelem, int64_t npe, int64_t nnode, SpWork *w, char *base) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = base ? base + off : nullptr;
+        off += align256(bytes);
+        return p;
+    };
+    const int64_t nb = (nnode + 1 + SCAN_ITEMS - 1) / SCAN_ITEMS + 1;
+    SpWork t;
+    t.cnt = (int32_t *)take(sizeof(int32_t) * (nnode + 1));
+    t.cursor = (int32_t *)take(sizeof(int32_t) * nnode);
+    t.list = (int32_t *)take(sizeof(int32_t) * nelem * npe);
+    t.nbr = (int64_t *)take(sizeof(int64_t) * (nnode + 1));
+    t.bsum = (int64_t *)take(sizeof(int64_t) * (nb + SCAN_ITEMS));
+    t.info = (int32_t *)take(sizeof(int32_t) * 4);
+    if (w) *w = t;
+    return off;
+}
+
+__global__ void sp_count(const int64_t *el, int64_t n, int64_t nnode, int32_t *cnt, int32_t *info) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t nd = el[k];
+        if (nd < 0 || nd >= nnode) atomicOr(info, 1);
+        else atomicAdd(cnt + nd, 1);
+    }
+}
+
+// exclusive scan, three kernels: per-block totals, scan of totals (one CTA), per-block scan
+template <class T>
+__global__ void scan_totals(const T *in, int64_t n, int64_t *bsum) {
+    __shared__ int64_t red[SCAN_THREADS];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_ITEMS;
+    int64_t s = 0;
+    for (int i = threadIdx.x; i < SCAN_ITEMS; i += SCAN_THREADS)
+        if (base + i < n) s += (int64_t)in[base + i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = SCAN_THREADS / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) bsum[blockIdx.x] = red[0];
+}
+
+__global__ void scan_block_sums(int64_t *bsum, int64_t nb) {
+    // single CTA: exclusive scan of nb block totals, chunk by chunk
+    __shared__ int64_t buf[SCAN_THREADS];
+    __shared__ int64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (int64_t c0 = 0; c0 < nb; c0 += SCAN_THREADS) {
+        const int64_t i = c0 + threadIdx.x;
+        const int64_t v = i < nb ? bsum[i] : 0;
+        buf[threadIdx.x] = v;
+        __syncthreads();
+        for (int o = 1; o < SCAN_THREADS; o <<= 1) {
+            int64_t t = threadIdx.x >= o ? buf[threadIdx.x - o] : 0;
+            __syncthreads();
+            buf[threadIdx.x] += t;
+            __syncthreads();
+        }
+        if (i < nb) bsum[i] = carry + buf[threadIdx.x] - v;
+        __syncthreads();
+        if (threadIdx.x == SCAN_THREADS - 1) carry += buf[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+template <class TIN, class TOUT>
+__global__ void scan_apply(const TIN *in, TOUT *out, int64_t n, const int64_t *bsum) {
+    // each thread scans SCAN_ITEMS/SCAN_THREADS consecutive items
+    constexpr int PER = SCAN_ITEMS / SCAN_THREADS;
+    __shared__ int64_t buf[SCAN_THREADS];
+    const int64_t base = (int64_t)blockIdx.x * SCAN_ITEMS + (int64_t)threadIdx.x * PER;
+    int64_t v[PER], s = 0;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        v[k] = base + k < n ? (int64_t)in[base + k] : 0;
+        s += v[k];
+    }
+    buf[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 1; o < SCAN_THREADS; o <<= 1) {
+        int64_t t = threadIdx.x >= o ? buf[threadIdx.x - o] : 0;
+        __syncthreads();
+        buf[threadIdx.x] += t;
+        __syncthreads();
+    }
+    int64_t run = bsum[blockIdx.x] + buf[threadIdx.x] - s;
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+        if (base + k < n) out[base + k] = (TOUT)run;
+        run += v[k];
+    }
+}
+
+template <class TIN, class TOUT>
+static void exclusive_scan(const TIN *in, TOUT *out, int64_t n, int64_t *bsum, cudaStream_t s) {
+    const int64_t nb = (n + SCAN_ITEMS - 1) / SCAN_ITEMS;
+    scan_totals<TIN><<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, bsum);
+    scan_block_sums<<<1, SCAN_THREADS, 0, s>>>(bsum, nb);
+    scan_apply<TIN, TOUT><<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, bsum);
+}
+
+// node starts, zero-degree check, maximum degree (cnt already scanned into starts; degrees are
+// the differences)
+__global__ void sp_degree_check(const int32_t *start, int64_t nnode, int32_t *info) {
+    for (int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; n < nnode; n += (int64_t)gridDim.x * blockDim.x) {
+        const int deg = start[n + 1] - start[n];
+        if (deg == 0) atomicOr(info, 2);
+        atomicMax(info + 1, deg);
+    }
+}
+
+__global__ void sp_fill_lists(const int64_t *el, int64_t n, int64_t npe, const int32_t *start, int32_t *cursor,
+                              int32_t *list) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t nd = el[k];
+        const int pos = atomicAdd(cursor + nd, 1);
+        list[start[nd] + pos] = (int32_t)(k / npe);
+    }
+}
+
+// CTA per node: sorted distinct neighbours in shared memory. Returns the count (all threads).
+__device__ int node_neighbours(const int64_t *el, int64_t npe, const int32_t *start, const int32_t *list, int64_t n,
+                               int capc, int32_t *buf, int32_t *flagbuf) {
+    const int s0 = start[n], deg = start[n + 1] - s0;
+    const int m = deg * (int)npe;
+    for (int i = threadIdx.x; i < capc; i += blockDim.x) {
+        if (i < m) buf[i] = (int32_t)el[(int64_t)list[s0 + i / (int)npe] * npe + i % (int)npe];
+        else buf[i] = INT32_MAX;
+    }
+    __syncthreads();
+    // bitonic sort of capc (power of two) keys
+    for (int k = 2; k <= capc; k <<= 1)
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < capc; i += blockDim.x) {
+                const int p = i ^ j;
+                if (p > i) {
+                    const int32_t a = buf[i], b = buf[p];
+                    const bool up = (i & k) == 0;
+                    if ((a > b) == up) {
+                        buf[i] = b;
+                        buf[p] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    // mark first occurrences, compact in order (prefix count over flags)
+    for (int i = threadIdx.x; i < capc; i += blockDim.x)
+        flagbuf[i] = (i < m && (i == 0 || buf[i] != buf[i - 1])) ? 1 : 0;
+    __syncthreads();
+    // inclusive scan of flags (Hillis-Steele over capc entries)
+    for (int o = 1; o < capc; o <<= 1) {
+        int32_t tv[SP_MAX_CAND / 128];
+        int c = 0;
+        for (int i = threadIdx.x; i < capc; i += blockDim.x) tv[c++] = i >= o ? flagbuf[i - o] : 0;
+        __syncthreads();
+        c = 0;
+        for (int i = threadIdx.x; i < capc; i += blockDim.x) flagbuf[i] += tv[c++];
+        __syncthreads();
+    }
+    const int count = m > 0 ? flagbuf[m - 1] : 0;
+    return count;
+}
+
+__global__ void sp_count_neighbours(const int64_t *el, int64_t npe, const int32_t *start, const int32_t *list,
+                                    int capc, int64_t *nbr) {
+    extern __shared__ int32_t sbuf[];
+    const int64_t n = blockIdx.x;
+    const int count = node_neighbours(el, npe, start, list, n, capc, sbuf, sbuf + capc);
+    if (threadIdx.x == 0) nbr[n] = count;
+}
+
+__global__ void sp_write_rows(const int64_t *el, int64_t npe, const int32_t *start, const int32_t *list, int capc,
+                              const int64_t *off, int64_t nvar, int32_t *indptr, int32_t *indices) {
+    extern __shared__ int32_t sbuf[];
+    int32_t *buf = sbuf, *fl = sbuf + capc;
+    const int64_t n = blockIdx.x;
+    const int cnt = node_neighbours(el, npe, start, list, n, capc, buf, fl);
+    const int m = (start[n + 1] - start[n]) * (int)npe;
+    // compact distinct neighbours to buf[capc..]: position fl[i]-1 for first occurrences
+    // (reuse: write into the second half after reading; do it through registers per thread)
+    const int64_t base = off[n] * nvar * nvar;
+    const int64_t rowlen = (int64_t)cnt * nvar;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        if (i == 0 || buf[i] != buf[i - 1]) {
+            const int k = fl[i] - 1;
+            for (int64_t j = 0; j < nvar; ++j)
+                for (int64_t l = 0; l < nvar; ++l) indices[base + j * rowlen + (int64_t)k * nvar + l] = (int32_t)(nvar * buf[i] + l);
+        }
+    }
+    if (threadIdx.x < nvar) indptr[n * nvar + threadIdx.x] = (int32_t)(base + threadIdx.x * rowlen);
+}
+
+__global__ void sp_last_indptr(int32_t *indptr, int64_t nrows, const int64_t *off, int64_t nnode, int64_t nvar) {
+    indptr[nrows] = (int32_t)(off[nnode] * nvar * nvar);
+}
+
+// data maps: CTA per element
+__global__ void sp_data_maps(const int64_t *el, int64_t npe, int64_t nvar, const int32_t *indptr, const int32_t *indices,
+                             int32_t *dl, int32_t *dg) {
+    extern __shared__ int32_t sm[];
+    const int NPE = (int)npe, NDOF = (int)(npe * nvar);
+    int32_t *nodes = sm, *sorter = sm + NPE, *rc = sm + 2 * NPE, *rcl = rc + NDOF;
+    const int64_t e = blockIdx.x;
+    for (int k = threadIdx.x; k < NPE; k += blockDim.x) nodes[k] = (int32_t)el[e * npe + k];
+    __syncthreads();
+    for (int k = threadIdx.x; k < NPE; k += blockDim.x) {
+        int r = 0;  // rank of node k (ties broken by position, like a stable argsort)
+        for (int m = 0; m < NPE; ++m) r += (nodes[m] < nodes[k]) || (nodes[m] == nodes[k] && m < k);
+        sorter[r] = k;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < NDOF; i += blockDim.x) {
+        const int s = sorter[i / (int)nvar], c = i % (int)nvar;
+        rc[i] = (int32_t)(nvar * nodes[s] + c);
+        rcl[i] = (int32_t)(s * nvar + c);
+    }
+    __syncthreads();
+    const int64_t cap = (int64_t)NDOF * NDOF;
+    for (int64_t idx = threadIdx.x; idx < cap; idx += blockDim.x) {
+        const int i = (int)(idx / NDOF), j = (int)(idx % NDOF);
+        const int row = rc[i], col = rc[j];
+        int lo = indptr[row], hi = indptr[row + 1];
+        while (hi - lo > 1) {
+            const int mid = lo + (hi - lo) / 2;
+            if (col < indices[mid]) hi = mid; else lo = mid;
+        }
+        dg[e * cap + idx] = lo;
+        dl[e * cap + idx] = rcl[i] * NDOF + rcl[j];
+    }
+}
+
+static int compute_sparsity(const int64_t *elements, int64_t nelem, int64_t npe, int64_t nnode, int64_t nvar,
+                            int32_t *indptr, int32_t *indices, int64_t cap_indices, int64_t *nnz_out, int32_t *dl,
+                            int32_t *dg, void *workspace, size_t ws_bytes, cudaStream_t s) {
+    if (!elements || !indptr || !nnz_out || !workspace || nelem <= 0 || npe <= 0 || nnode <= 0 || nvar <= 0)
+        return FL_ERR_ARG;
+    if ((dl == nullptr) != (dg == nullptr)) return FL_ERR_ARG;
+    if (nnode * nvar + 1 > INT32_MAX) return FL_ERR_UNSUPPORTED;
+    SpWork w;
+    if (sp_layout(nelem, npe, nnode, nullptr, nullptr) > ws_bytes) return FL_ERR_CAPACITY;
+    sp_layout(nelem, npe, nnode, &w, (char *)workspace);
+    const int64_t n = nelem * npe;
+    FL_CUDA_TRY(cudaMemsetAsync(w.cnt, 0, sizeof(int32_t) * (nnode + 1), s));
+    FL_CUDA_TRY(cudaMemsetAsync(w.cursor, 0, sizeof(int32_t) * nnode, s));
+    FL_CUDA_TRY(cudaMemsetAsync(w.info, 0, sizeof(int32_t) * 4, s));
+    const unsigned g1 = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 16);
+    sp_count<<<g1, 256, 0, s>>>(elements, n, nnode, w.cnt, w.info);
+    int32_t hinfo[4];
+    FL_CUDA_TRY(cudaMemcpyAsync(hinfo, w.info, sizeof(hinfo), cudaMemcpyDeviceToHost, s));
+    FL_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hinfo[0] & 1) return FL_ERR_ARG;  // node id out of range
+    exclusive_scan<int32_t, int32_t>(w.cnt, w.cnt, nnode + 1, w.bsum, s);
+    const unsigned g2 = (unsigned)std::min<int64_t>((nnode + 255) / 256, 152 * 16);
+    sp_degree_check<<<g2, 256, 0, s>>>(w.cnt, nnode, w.info);
+    FL_CUDA_TRY(cudaMemcpyAsync(hinfo, w.info, sizeof(hinfo), cudaMemcpyDeviceToHost, s));
+    FL_CUDA_TRY(cudaStreamSynchronize(s));
+    if (hinfo[0] & 2) return FL_ERR_MESH;
+    const int64_t maxcand = (int64_t)hinfo[1] * npe;
+    if (maxcand > SP_MAX_CAND) return FL_ERR_UNSUPPORTED;
+    int capc = 128;
+    while (capc < maxcand) capc <<= 1;
+    sp_fill_lists<<<g1, 256, 0, s>>>(elements, n, npe, w.cnt, w.cursor, w.list);
+    const size_t shm = sizeof(int32_t) * 2 * capc;
+    if (shm > 48 * 1024) {
+        FL_CUDA_TRY(cudaFuncSetAttribute(sp_count_neighbours, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        FL_CUDA_TRY(cudaFuncSetAttribute(sp_write_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    }
+    sp_count_neighbours<<<(unsigned)nnode, 128, shm, s>>>(elements, npe, w.cnt, w.list, capc, w.nbr);
+    FL_CUDA_TRY(cudaMemsetAsync(w.nbr + nnode, 0, sizeof(int64_t), s));
+    exclusive_scan<int64_t, int64_t>(w.nbr, w.nbr, nnode + 1, w.bsum, s);
+    int64_t total_nodes_pairs = 0;
+    FL_CUDA_TRY(cudaMemcpyAsync(&total_nodes_pairs, w.nbr + nnode, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    FL_CUDA_TRY(cudaStreamSynchronize(s));
+    const int64_t nnz = total_nodes_pairs * nvar * nvar;
+    *nnz_out = nnz;
+    if (nnz > INT32_MAX) return FL_ERR_UNSUPPORTED;
+    if (!indices || cap_indices < nnz) return FL_ERR_CAPACITY;
+    sp_write_rows<<<(unsigned)nnode, 128, shm, s>>>(elements, npe, w.cnt, w.list, capc, w.nbr, nvar, indptr, indices);
+    sp_last_indptr<<<1, 1, 0, s>>>(indptr, nnode * nvar, w.nbr, nnode, nvar);
+    if (dl) {
+        const int ndof = (int)(npe * nvar);
+        const size_t shm2 = sizeof(int32_t) * (2 * npe + 2 * ndof);
+        sp_data_maps<<<(unsigned)nelem, 256, shm2, s>>>(elements, npe, nvar, indptr, indices, dl, dg);
+    }
+    return launch_status();
+}
+
+}  // namespace fl
+
+extern "C" {
+
+size_t fl_ComputeSparsityPattern_workspace_size(int64_t nelem, int64_t nodeperelem, int64_t nnode) {
+    return fl::sp_layout(nelem, nodeperelem, nnode, nullptr, nullptr);
+}
+
+int fl_ComputeSparsityPattern(const int64_t *elements, int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t nvar,
+                              int32_t *indptr, int32_t *indices, int64_t indices_capacity, int64_t *nnz,
+                              int32_t *data_local_indices, int32_t *data_global_indices, void *workspace,
+                              size_t workspace_bytes, fl_stream_t stream) {
+    return fl::compute_sparsity(elements, nelem, nodeperelem, nnode, nvar, indptr, indices, indices_capacity, nnz,
+                                data_local_indices, data_global_indices, workspace, workspace_bytes,
+                                (cudaStream_t)stream);
+}
+
+}  // extern "C"

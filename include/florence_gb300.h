@@ -1,0 +1,137 @@
+/*
+ * florence_gb300.h -- C ABI of the GB300 (sm_103a) displacement-formulation assembly engine.
+ *
+ * Every pointer argument named like an array is a DEVICE pointer (memory of the current CUDA
+ * device) unless its comment says "host". Sizes are element counts. Every entry point is
+ * asynchronous on `stream` unless its comment says it synchronises, and returns an int status
+ * (FL_OK == 0). Outputs that the reference accumulates into (V, T, M) are accumulated (+=) here
+ * too: the caller zero-initialises them, as the reference's Cython wrappers do.
+ *
+ * The entry points replace these reference interfaces (paths inside the Florence repository):
+ *   fl_ComputeSparsityPattern          FiniteElements/Assembly/_Assembly_/ComputeSparsityPattern.pyx:44-112
+ *                                      (+ _ComputeSparsityPattern_ / _ComputeDataIndices_, ComputeSparsityPattern.h:22-125)
+ *   fl_GlobalAssemblyDF__NeoHookean_   _GlobalAssemblyDF_ monomorphised for _NeoHookean_ by AOT_Assembler.py:36-118,
+ *   fl_GlobalAssemblyDF__MooneyRivlin_ FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDF_.h:8-47 (signature),
+ *                                      called from _LowLevelAssemblyDF_.pyx:115-154
+ *   fl_GlobalAssemblyExplicit_DF_DPF_  FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyExplicit_DF_DPF_.h:728-829
+ *                                      (signature), called from _LowLevelAssemblyExplicit_DF_DPF_.pyx:123-152
+ *   fl_LumpedMass                      VariationalPrinciple/_Mass_/_MassIntegrand_.h:249-400 (mass_type 0),
+ *                                      called from _MassIntegrand_.pyx:192-348 (__TotalConstantMassIntegrand__)
+ */
+#ifndef FLORENCE_GB300_H
+#define FLORENCE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* cudaStream_t without pulling in the CUDA headers (identical type) */
+typedef struct CUstream_st *fl_stream_t;
+
+/* status codes */
+#define FL_OK 0
+#define FL_ERR_ARG 1           /* invalid argument (null pointer, unsupported ndim/nvar, bad size) */
+#define FL_ERR_UNSUPPORTED 2   /* valid but not built: nodes per element, Gauss points or material */
+#define FL_ERR_CUDA 3          /* a CUDA runtime call or kernel launch failed */
+#define FL_ERR_MESH 4          /* mesh rejected: a node belongs to no element (the reference fails too) */
+#define FL_ERR_CAPACITY 5      /* an output or workspace buffer is smaller than required */
+
+/* bits OR-ed into the optional device word `flags` by the assembly kernels */
+#define FL_FLAG_NONPOSITIVE_J 1 /* det F <= 0 at some Gauss point; results are still written */
+
+/* material numbers of the explicit entry point (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-109) */
+#define FL_MATERIAL_NEOHOOKEAN 1
+#define FL_MATERIAL_MOONEYRIVLIN 2
+
+const char *fl_status_string(int status);
+
+/* ------------------------------------------------------------------------------------------
+ * Sparsity pattern of the global tangent: node adjacency expanded by nvar x nvar blocks, rows
+ * sorted, plus the reference's element-to-nonzero maps. Bit-identical to the reference.
+ *   elements        [nelem * nodeperelem] node ids (int64)
+ *   indptr          out [nnode*nvar + 1]
+ *   indices         out [indices_capacity]; the pattern needs nnz entries
+ *   nnz             host out: number of nonzeros
+ *   data_local_indices, data_global_indices
+ *                   out [nelem * (nvar*nodeperelem)^2] or both NULL (the reference's squeeze mode)
+ *   workspace       device scratch of fl_ComputeSparsityPattern_workspace_size() bytes
+ * Synchronises `stream` once (to read nnz). Returns FL_ERR_CAPACITY with *nnz set when
+ * indices_capacity < nnz (call again with a larger buffer).
+ * ------------------------------------------------------------------------------------------ */
+size_t fl_ComputeSparsityPattern_workspace_size(int64_t nelem, int64_t nodeperelem, int64_t nnode);
+int fl_ComputeSparsityPattern(const int64_t *elements, int64_t nelem, int64_t nodeperelem, int64_t nnode,
+                              int64_t nvar, int32_t *indptr, int32_t *indices, int64_t indices_capacity,
+                              int64_t *nnz, int32_t *data_local_indices, int32_t *data_global_indices,
+                              void *workspace, size_t workspace_bytes, fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Implicit assembly of the tangent stiffness and the internal-force residual (FP64), one
+ * entry per material, argument list of the reference's _GlobalAssemblyDF_<Mat> plus `flags`
+ * and `stream`:
+ *   points [nnode*3], elements [nelem*nodeperelem] (uint64), Eulerx [nnode*3],
+ *   Jm [ndim*nodeperelem*ngauss] (reference-element gradients, d-major then node then point),
+ *   AllGauss [ngauss] (weights). Eulerp, bases, local_rows_stiffness, local_cols_stiffness,
+ *   sorted_elements, sorter and anisotropic_orientations are accepted for signature parity and
+ *   not read (the kernel derives what they carry).
+ *   recompute_sparsity_pattern = 1: triplets, I_stiff/J_stiff/V_stiff of nelem*ndof^2 entries,
+ *     entry elem*ndof^2 + r*ndof + c holds (global row of local dof r, global column of c, K_e[r][c]).
+ *   recompute_sparsity_pattern = 0: CSR values V_stiff[nnz] += , with I_stiff = indptr and
+ *     J_stiff = indices (as the reference's wrapper passes them), through data_local_indices /
+ *     data_global_indices, or, if squeeze_sparsity_pattern = 1, by binary search in each row.
+ *   T [nnode*3] += residual (internal traction) when requires_geometry_update == 1.
+ *   ndim and nvar must be 3 and H_VoigtSize 6. flags: optional device int (FL_FLAG_* bits OR-ed in).
+ * Supported nodeperelem: 4, 8, 10, 20, 27, 35, 64, 125 (tet p=1..4, hex p=1..4); ngauss <= 343.
+ * ------------------------------------------------------------------------------------------ */
+#define FL_GLOBAL_ASSEMBLY_DF_ARGS                                                                          \
+    const double *points, const uint64_t *elements, const double *Eulerx, const double *Eulerp,            \
+        const double *bases, const double *Jm, const double *AllGauss, int64_t ndim, int64_t nvar,          \
+        int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t H_VoigtSize,             \
+        int64_t requires_geometry_update, const int64_t *local_rows_stiffness,                              \
+        const int64_t *local_cols_stiffness, int32_t *I_stiff, int32_t *J_stiff, double *V_stiff,           \
+        double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,                            \
+        const int32_t *data_local_indices, const int32_t *data_global_indices,                              \
+        const uint64_t *sorted_elements, const int64_t *sorter, double rho, double mu, double mu1,          \
+        double mu2, double mu3, double mue, double lamb, double eps_1, double eps_2, double eps_3,          \
+        double eps_e, const double *anisotropic_orientations, int *flags, fl_stream_t stream
+
+int fl_GlobalAssemblyDF__NeoHookean_(FL_GLOBAL_ASSEMBLY_DF_ARGS);   /* mu, lamb */
+int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu1, mu2, lamb */
+
+/* ------------------------------------------------------------------------------------------
+ * Explicit (matrix-free) internal force, T[nnode*nvar] += sum_e sum_g detJ (grad N_a . sigma).
+ * Argument list of the reference's _GlobalAssemblyExplicit_DF_DPF_ plus flags and stream.
+ * formulation_number must be 0 (mechanics), material_number FL_MATERIAL_NEOHOOKEAN (mu, lamb)
+ * or FL_MATERIAL_MOONEYRIVLIN (mu1, mu2, lamb). Unused pointers may be NULL.
+ * ------------------------------------------------------------------------------------------ */
+int fl_GlobalAssemblyExplicit_DF_DPF_(const double *points, const uint64_t *elements, const double *Eulerx,
+                                      const double *Eulerp, const double *bases, const double *Jm,
+                                      const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss,
+                                      int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t H_VoigtSize,
+                                      int64_t requires_geometry_update, double *T, double rho, double mu,
+                                      double mu1, double mu2, double mu3, double mue, double lamb, double eps_1,
+                                      double eps_2, double eps_3, double eps_e,
+                                      const double *anisotropic_orientations, int material_number,
+                                      int formulation_number, int *flags, fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Lumped (row-sum) mass: M[nnode*nvar] += row sums of sum_g rho N N^T w_g |det dX/dxi|.
+ * bases [nodeperelem*ngauss] (node-major), Jm and AllGauss as above. flags: optional device int.
+ * ------------------------------------------------------------------------------------------ */
+int fl_LumpedMass(const double *points, const uint64_t *elements, const double *bases, const double *Jm,
+                  const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss, int64_t nelem,
+                  int64_t nodeperelem, int64_t nnode, double rho, double *M, int *flags, fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Measurement helper: device time of a dependent FP64 FMA loop over the whole GPU, used to
+ * measure the FP64 roof that the assembly kernels are bound by. Synchronises the stream.
+ * gflops (host out) = achieved FP64 GFLOP/s (2 flops per FMA).
+ * ------------------------------------------------------------------------------------------ */
+int fl_measure_fp64_peak(double *gflops, fl_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,48 @@
+"""CPU-only checks of the C ABI: the library builds, loads, and exports every symbol the header declares."""
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "florence_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fl_\w+)\s*\(", text)))
+
+
+def test_header_lists_expected_entry_points():
+    syms = header_symbols()
+    for s in ("fl_ComputeSparsityPattern", "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
+              "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass"):
+        assert s in syms
+
+
+def test_library_exports_every_declared_symbol():
+    from florence_gb300 import _native
+    if not os.path.exists(_native.LIB_PATH):
+        from florence_gb300 import build
+        build.build()
+    L = _native.lib()
+    missing = [s for s in header_symbols() if not hasattr(L, s)]
+    assert not missing, missing
+    assert sorted(_native.EXPORTS) == sorted(header_symbols())
+    assert L.fl_status_string(0) == b"ok"
+
+
+def test_workspace_size_is_pure_host_arithmetic():
+    from florence_gb300 import _native
+    L = _native.lib()
+    a = L.fl_ComputeSparsityPattern_workspace_size(512, 27, 4913)
+    b = L.fl_ComputeSparsityPattern_workspace_size(1024, 27, 4913)
+    assert 0 < a < b
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    from florence_gb300 import _native
+    monkeypatch.setattr(_native, "_lib", None)
+    monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "absent.so"))
+    with pytest.raises(ImportError):
+        _native.lib()

@@ -1,0 +1,271 @@
+"""GPU parity tests: the CUDA path through the C ABI against the golden vectors of the reference
+and against the CPU oracle.
+
+Tolerances: CSR/sparsity integer arrays bit-exact; FP64 tangent and residual within 1e-12
+relative Frobenius (the criterion for the FP64 path); element matrices 1e-12.
+"""
+import hashlib
+import types
+import warnings
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import golden_cases, load_golden, rel_fro
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def fl():
+    import florence_gb300
+    from florence_gb300 import _native
+    _native.lib()
+    return florence_gb300
+
+
+def _asm(fl, d, mode, **kw):
+    return fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], str(d["material"]),
+                              tuple(d["params"]), mode=mode, **kw)
+
+
+def _sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, "<i4").tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_device_sparsity_bit_exact(fl, case):
+    d = load_golden(case)
+    el = torch.from_numpy(d["elements"]).cuda()
+    ind, ptr, dl, dg = fl.device_sparsity(el, d["points"].shape[0], 3)
+    assert np.array_equal(ptr.cpu().numpy(), d["sp_indptr"])
+    assert np.array_equal(ind.cpu().numpy(), d["sp_indices"])
+    assert np.array_equal(dl.cpu().numpy(), d["sp_data_local"])
+    assert np.array_equal(dg.cpu().numpy(), d["sp_data_global"])
+
+
+@pytest.mark.parametrize("case", golden_cases())
+@pytest.mark.parametrize("mode", ["csr", "squeeze"])
+def test_csr_assembly_matches_reference(fl, case, mode):
+    d = load_golden(case)
+    asm = _asm(fl, d, mode)
+    V, T = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda())
+    asm.check_flags()
+    assert np.array_equal(asm.indptr.cpu().numpy(), d["K_indptr"])
+    assert np.array_equal(asm.indices.cpu().numpy(), d["K_indices"])
+    assert rel_fro(V.cpu().numpy(), d["K_data"]) < TOL
+    assert rel_fro(T.cpu().numpy(), d["T"]) < TOL
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_triplets_and_element_matrices(fl, case):
+    d = load_golden(case)
+    asm = _asm(fl, d, "triplet")
+    I, J, V, T = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda())
+    asm.check_flags()
+    I, J, V = I.cpu().numpy(), J.cpu().numpy(), V.cpu().numpy()
+    n = d["points"].shape[0] * 3
+    K = sp.csr_matrix((V, (I, J)), shape=(n, n))
+    assert np.array_equal(K.indptr, d["K_indptr"]) and np.array_equal(K.indices, d["K_indices"])
+    assert rel_fro(K.data, d["K_data"]) < TOL
+    ndof = 3 * d["elements"].shape[1]
+    Ke = V.reshape(-1, ndof, ndof)[d["emat_ids"]]
+    assert rel_fro(Ke, d["emat_K"]) < TOL
+    # triplet rows/cols follow the element's own dof order (fill_triplet, _MassIntegrand_.h:68-111)
+    e = int(d["emat_ids"][0])
+    dofs = (3 * d["elements"][e][:, None] + np.arange(3)).ravel()
+    assert np.array_equal(I.reshape(-1, ndof, ndof)[e], np.repeat(dofs[:, None], ndof, 1))
+    assert np.array_equal(J.reshape(-1, ndof, ndof)[e], np.repeat(dofs[None, :], ndof, 0))
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_element_residual(fl, case):
+    d = load_golden(case)
+    for k, e in enumerate(d["emat_ids"]):
+        el = d["elements"][int(e):int(e) + 1]
+        asm = fl.DeviceAssembler(d["points"], el, d["Jm"], d["AllGauss"], str(d["material"]), tuple(d["params"]),
+                                 mode="triplet")
+        _, _, _, T = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda())
+        dofs = (3 * el[0][:, None] + np.arange(3)).ravel()
+        assert rel_fro(T.cpu().numpy()[dofs], d["emat_t"][k]) < TOL
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_internal_force(fl, case):
+    d = load_golden(case)
+    asm = _asm(fl, d, "triplet")
+    T = asm.internal_force(torch.from_numpy(d["Eulerx"]).cuda())
+    asm.check_flags()
+    assert rel_fro(T.cpu().numpy(), d["T"]) < TOL
+
+
+@pytest.mark.parametrize("case", [c for c in golden_cases() if "M_lumped" in load_golden(c)])
+def test_lumped_mass(fl, case):
+    d = load_golden(case)
+    asm = fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], "NeoHookean", (1.0, 1.0),
+                             mode="triplet", Bases=d["Bases"])
+    M = asm.lumped_mass(float(d["rho"]))
+    assert rel_fro(M.cpu().numpy(), d["M_lumped"]) < TOL
+
+
+def test_config1_full_size(fl, oracle):
+    """Structured 8x8x8 p=2 hex cube, 125 Gauss points, neo-Hookean: exact structure hashes from the
+    reference, value probes from the reference, full CSR values against the oracle."""
+    d = load_golden("config1_hex8_p2_q5")
+    asm = _asm(fl, d, "csr")
+    assert _sha(asm.indptr.cpu().numpy()) == str(d["sha_indptr"])
+    assert _sha(asm.indices.cpu().numpy()) == str(d["sha_indices"])
+    assert _sha(asm.data_local.cpu().numpy()) == str(d["sha_data_local"])
+    assert _sha(asm.data_global.cpu().numpy()) == str(d["sha_data_global"])
+    V, T = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda())
+    asm.check_flags()
+    V, T = V.cpu().numpy(), T.cpu().numpy()
+    n = d["points"].shape[0] * 3
+    K = sp.csr_matrix((V, asm.indices.cpu().numpy(), asm.indptr.cpu().numpy()), shape=(n, n))
+    v = np.random.default_rng(int(d["matvec_seed"])).standard_normal(n)
+    assert rel_fro(K @ v, d["K_matvec"]) < TOL
+    assert rel_fro(K.diagonal(), d["K_diag"]) < TOL
+    assert abs(np.linalg.norm(V) - float(d["K_fro"])) / float(d["K_fro"]) < TOL
+    assert rel_fro(T, d["T"]) < TOL
+    spa = (asm.indices.cpu().numpy(), asm.indptr.cpu().numpy(), asm.data_local.cpu().numpy(),
+           asm.data_global.cpu().numpy())
+    Vo, To = oracle.assemble_df("NeoHookean", d["params"], d["points"], d["elements"], d["Eulerx"], d["Jm"],
+                                d["AllGauss"], mode="csr", sparsity_arrays=spa, nthreads=oracle.max_threads())
+    assert rel_fro(V, Vo) < TOL
+    assert rel_fro(T, To) < TOL
+    tri = _asm(fl, d, "triplet")
+    _, _, Vt, _ = tri.assemble(torch.from_numpy(d["Eulerx"]).cuda())
+    ndof = 81
+    assert rel_fro(Vt.cpu().numpy().reshape(-1, ndof, ndof)[d["emat_ids"]], d["emat_K"]) < TOL
+
+
+def test_large_displacement_against_oracle(fl, oracle):
+    """Mooney-Rivlin on the config-1 mesh with a 10x larger seeded displacement: CUDA vs oracle."""
+    d = load_golden("config1_hex8_p2_q5")
+    x = d["points"] + np.random.default_rng(7).uniform(-0.1, 0.1, d["points"].shape) * 0.3
+    prm = (0.5, 0.5, 20.0)
+    asm = fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], "MooneyRivlin", prm, mode="csr")
+    V, T = asm.assemble(torch.from_numpy(x).cuda())
+    spa = (asm.indices.cpu().numpy(), asm.indptr.cpu().numpy(), asm.data_local.cpu().numpy(),
+           asm.data_global.cpu().numpy())
+    Vo, To = oracle.assemble_df("MooneyRivlin", prm, d["points"], d["elements"], x, d["Jm"], d["AllGauss"],
+                                mode="csr", sparsity_arrays=spa, nthreads=oracle.max_threads())
+    assert rel_fro(V.cpu().numpy(), Vo) < TOL
+    assert rel_fro(T.cpu().numpy(), To) < TOL
+
+
+def test_accumulates_and_is_linear_in_repeats(fl):
+    """Outputs are accumulated (+=) like the reference's: two calls into the same buffers give 2x."""
+    d = load_golden("hex_p2_nh_q5")
+    asm = _asm(fl, d, "csr")
+    x = torch.from_numpy(d["Eulerx"]).cuda()
+    V1, T1 = asm.assemble(x)
+    V2, T2 = asm.assemble(x, V=V1.clone(), T=T1.clone())
+    assert rel_fro(V2.cpu().numpy(), 2 * V1.cpu().numpy()) < 1e-15
+    assert rel_fro(T2.cpu().numpy(), 2 * T1.cpu().numpy()) < 1e-15
+
+
+def test_empty_mesh(fl):
+    d = load_golden("hex_p1_nh")
+    asm = fl.DeviceAssembler(d["points"], d["elements"][:0], d["Jm"], d["AllGauss"], "NeoHookean", (1.0, 10.0),
+                             mode="triplet")
+    I, J, V, T = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda())
+    assert V.numel() == 0 and float(T.abs().sum()) == 0.0
+    assert float(asm.internal_force(torch.from_numpy(d["Eulerx"]).cuda()).abs().sum()) == 0.0
+
+
+def test_bad_node_id_is_reported(fl):
+    """An element node id >= nnode is clamped inside the kernel (in-bounds) and reported."""
+    d = load_golden("hex_p1_nh")
+    el = d["elements"].copy()
+    el[3, 2] = d["points"].shape[0] + 5
+    asm = fl.DeviceAssembler(d["points"], el, d["Jm"], d["AllGauss"], "NeoHookean", (1.0, 10.0), mode="triplet")
+    asm.assemble(torch.from_numpy(d["Eulerx"]).cuda())
+    with pytest.raises(fl._native.FlorenceGB300Error):
+        asm.check_flags()
+    with pytest.raises(fl._native.FlorenceGB300Error):
+        fl.device_sparsity(torch.from_numpy(el).cuda(), d["points"].shape[0], 3)
+
+
+def test_unreferenced_node_rejected(fl):
+    d = load_golden("hex_p1_nh")
+    with pytest.raises(ValueError):
+        fl.device_sparsity(torch.from_numpy(d["elements"]).cuda(), d["points"].shape[0] + 1, 3)
+
+
+def test_inverted_element_warns(fl):
+    d = load_golden("hex_p1_nh")
+    x = d["Eulerx"].copy()
+    x[:, 0] *= -1.0  # mirror: det F < 0 everywhere
+    asm = _asm(fl, d, "csr")
+    asm.assemble(torch.from_numpy(x).cuda())
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        asm.check_flags()
+    assert any("det F" in str(x.message) for x in w)
+
+
+def _fake_florence_objects(d, recompute, squeeze=False):
+    """Objects with the attributes the reference's Cython wrapper reads (_LowLevelAssemblyDF_.pyx:55-113)."""
+    mat_name = str(d["material"])
+    p = d["params"]
+    material = types.SimpleNamespace(H_VoigtSize=6, is_transversely_isotropic=False, rho=1.0, mtype=mat_name)
+    if mat_name == "NeoHookean":
+        material.mu, material.lamb = p[0], p[1]
+    else:
+        material.mu1, material.mu2, material.lamb = p[0], p[1], p[2]
+    fs = types.SimpleNamespace(Jm=d["Jm"], AllGauss=d["AllGauss"][:, None], Bases=d["Bases"])
+    form = types.SimpleNamespace(ndim=3, nvar=3, fields="mechanics")
+    mesh = types.SimpleNamespace(points=d["points"], elements=d["elements"].astype(np.uint64),
+                                 nelem=d["elements"].shape[0])
+    solver = types.SimpleNamespace(requires_geometry_update=1, recompute_sparsity_pattern=recompute,
+                                   squeeze_sparsity_pattern=squeeze, indices=d["sp_indices"], indptr=d["sp_indptr"],
+                                   data_local_indices=d["sp_data_local"], data_global_indices=d["sp_data_global"])
+    return solver, fs, form, mesh, material
+
+
+@pytest.mark.parametrize("case", ["hex_p2_nh_q5", "tet_p3_mr_jitter"])
+@pytest.mark.parametrize("recompute,squeeze", [(True, False), (False, False), (False, True)])
+def test_drop_in_callables(fl, case, recompute, squeeze):
+    d = load_golden(case)
+    solver, fs, form, mesh, material = _fake_florence_objects(d, recompute, squeeze)
+    fn = getattr(fl, "_LowLevelAssemblyDF__" + str(d["material"]) + "_")
+    out = fn(solver, fs, form, mesh, material, d["Eulerx"], np.zeros(d["points"].shape[0]))
+    n = d["points"].shape[0] * 3
+    if recompute:
+        I, J, V, T = out
+        assert I.dtype == np.int32 and J.dtype == np.int32 and V.dtype == np.float64
+        K = sp.csr_matrix((V, (I, J)), shape=(n, n))
+    else:
+        V, T = out
+        K = sp.csr_matrix((V, d["sp_indices"], d["sp_indptr"]), shape=(n, n))
+    assert T.shape == (n,) and T.dtype == np.float64
+    assert rel_fro(K.data, d["K_data"]) < TOL and rel_fro(T, d["T"]) < TOL
+    Ti = fl._LowLevelAssemblyExplicit_DF_DPF_(fs, form, mesh, material, d["Eulerx"], np.zeros(d["points"].shape[0]))
+    assert rel_fro(Ti, d["T"]) < TOL
+
+
+def test_drop_in_sparsity(fl):
+    d = load_golden("tet_p3_mr_jitter")
+    mesh = types.SimpleNamespace(points=d["points"], elements=d["elements"].astype(np.uint64))
+    ind, ptr, dl, dg = fl.ComputeSparsityPattern(mesh, 3)
+    assert np.array_equal(ind, d["sp_indices"]) and np.array_equal(ptr, d["sp_indptr"])
+    assert np.array_equal(dl, d["sp_data_local"]) and np.array_equal(dg, d["sp_data_global"])
+    ind2, ptr2 = fl.ComputeSparsityPattern(mesh, 3, squeeze_sparsity_pattern=True)
+    assert np.array_equal(ind2, ind) and np.array_equal(ptr2, ptr)
+
+
+def test_unsupported_material_raises(fl):
+    d = load_golden("hex_p1_nh")
+    solver, fs, form, mesh, material = _fake_florence_objects(d, True)
+    with pytest.raises(NotImplementedError):
+        fl.material_params(material, "LinearElastic")
+
+
+def test_fp64_peak_is_measured(fl):
+    g = fl.fp64_peak_gflops()
+    assert 100.0 < g < 200000.0
