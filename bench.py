@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark of the FP64 tangent + residual assembly (Florence's low-level displacement-formulation
+assembly) on one GB300.
+
+Workload (default): the unstructured p=3 (20-node) tetrahedral mesh of a 4x1x1 beam, seeded
+jittered lattice (48x12x12 cells, jitter 0.15 h, default_rng(1)) split by Delaunay, Mooney-Rivlin
+mu1 = mu2 = 0.5, lambda = 20, 14 Gauss points per element, at a seeded first-increment state
+(downward bending u_z = -0.02 (x/4)^2 plus U(-1e-3, 1e-3) per dof, default_rng(2)). One step =
+zero the CSR values and the residual, assemble the tangent (CSR through the element-to-nonzero
+maps) and the residual: one pass of the hot path.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference] [--workload beam|cube]
+
+``--impl reference`` times the reference algorithm's CPU implementation (the C restatement of
+_GlobalAssemblyDF_ in oracle/, all host threads) on the same workload and prints its own line.
+Prints one JSON line.
+"""
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+import types
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+# ------------------------------------------------------------------------------------------------
+# workloads
+# ------------------------------------------------------------------------------------------------
+def workload(name):
+    from florence_gb300 import meshes
+    if name in ("beam", "beam_s"):
+        # beam_s: the same beam at half the lattice resolution (profiling case, ~6k elements)
+        t = np.load(os.path.join(GOLDEN, "tet_p3_mr_jitter.npz"))
+        pat = meshes.local_pattern(t["points"], t["elements"], 0, "tet")
+        cells = (48, 12, 12) if name == "beam" else (24, 6, 6)
+        P, el = meshes.jittered_tet_beam(cells, (4.0, 1.0, 1.0), 1, pat)
+        rng = np.random.default_rng(2)
+        x = P.copy()
+        x[:, 2] += -0.02 * (P[:, 0] / 4.0) ** 2
+        x += rng.uniform(-1e-3, 1e-3, P.shape)
+        desc = dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice, Delaunay), Mooney-Rivlin "
+                             "mu1=mu2=0.5 lambda=20, 14 Gauss points, FP64 tangent (CSR) + residual" % cells,
+                    element="tet20", material="MooneyRivlin")
+        return dict(points=P, elements=el, x=x, Jm=t["Jm"], w=t["AllGauss"], material="MooneyRivlin",
+                    params=(0.5, 0.5, 20.0), desc=desc)
+    if name == "cube":
+        d = np.load(os.path.join(GOLDEN, "config1_hex8_p2_q5.npz"))
+        desc = dict(workload="structured 8x8x8 p=2 hex cube (27-node), Gauss 5^3 = 125 points, neo-Hookean "
+                             "mu=1 lambda=10, u~U(-0.01,0.01) default_rng(0), FP64 tangent (CSR) + residual",
+                    element="hex27", material="NeoHookean")
+        return dict(points=d["points"], elements=d["elements"], x=d["Eulerx"], Jm=d["Jm"], w=d["AllGauss"],
+                    material="NeoHookean", params=(1.0, 10.0), desc=desc)
+    raise ValueError(name)
+
+
+def flops_alg(npe, nq, material):
+    """Algorithmic FP64 FLOPs per element of the tangent + residual, nq (6 ndof^2 + 288 npe + c),
+    c = 300 (neo-Hookean) / 500 (Mooney-Rivlin): folded constitutive+geometric tensor contracted
+    with the spatial gradients, kinematics, residual and material per Gauss point."""
+    ndof = 3 * npe
+    return nq * (6 * ndof * ndof + 288 * npe + (300 if material == "NeoHookean" else 500))
+
+
+def flops_executed(npe, nq, material):
+    """FP64 FLOPs the kernel executes per element (symmetric tangent: node blocks a <= b only):
+    per Gauss point 27 npe (npe+1) (stiffness) + 162 npe (U) + 36 npe (kinematics) + 18 npe
+    (residual) + c, c = 800 (neo-Hookean) / 1200 (Mooney-Rivlin)."""
+    return nq * (27 * npe * (npe + 1) + 216 * npe + (800 if material == "NeoHookean" else 1200))
+
+
+def bytes_min(nnode, nelem, npe, nnz):
+    """Compulsory HBM bytes of one assembly: X and x read, connectivity (int32 equivalent), CSR
+    values written once, residual written."""
+    return 8 * 3 * nnode * 2 + 4 * nelem * npe + 8 * nnz + 8 * 3 * nnode
+
+
+# ------------------------------------------------------------------------------------------------
+# clocks
+# ------------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.out = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.out, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        self.out.flush()
+        rows = []
+        with open(self.out.name) as f:
+            for line in f:
+                p = [c.strip() for c in line.split(",")]
+                if len(p) >= 7:
+                    try:
+                        rows.append((float(p[0]), float(p[1]), p[3:7]))
+                    except ValueError:
+                        pass
+        os.unlink(self.out.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower().startswith("active")})
+        return {"sm_mhz": float(np.median([r[0] for r in rows])), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def traffic_from_profile(kernel_tag):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", kernel_tag + ".md")
+    if not os.path.exists(path):
+        return None
+    m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", open(path).read())
+    return float(m.group(1)) if m else None
+
+
+# ------------------------------------------------------------------------------------------------
+# CPU reference (oracle restatement of _GlobalAssemblyDF_)
+# ------------------------------------------------------------------------------------------------
+def cpu_assembly_rate(W, spa, target_s=12.0, max_passes=5):
+    from oracle import oracle
+    nthreads = oracle.max_threads()
+    nelem = W["elements"].shape[0]
+    times = []
+    t_all = time.perf_counter()
+    while len(times) < max_passes and (time.perf_counter() - t_all) < target_s:
+        t0 = time.perf_counter()
+        oracle.assemble_df(W["material"], W["params"], W["points"], W["elements"], W["x"], W["Jm"], W["w"],
+                           mode="csr", sparsity_arrays=spa, nthreads=nthreads, fast=True)
+        times.append(time.perf_counter() - t0)
+    best = min(times)
+    return nelem / best / 1e6, nthreads, "%d full assemblies of all %d elements (%d threads), best pass %.3f s" % (
+        len(times), nelem, nthreads, best)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle
+    W = workload(args.workload)
+    spa = oracle.sparsity(W["elements"], W["points"].shape[0])
+    nthreads = oracle.max_threads()
+    nelem = W["elements"].shape[0]
+    for _ in range(args.warmup):
+        oracle.assemble_df(W["material"], W["params"], W["points"], W["elements"], W["x"], W["Jm"], W["w"],
+                           mode="csr", sparsity_arrays=spa, nthreads=nthreads, fast=True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.assemble_df(W["material"], W["params"], W["points"], W["elements"], W["x"], W["Jm"], W["w"],
+                           mode="csr", sparsity_arrays=spa, nthreads=nthreads, fast=True)
+    dt = time.perf_counter() - t0
+    value = nelem * args.steps / dt / 1e6
+    line = dict(metric="FP64 assembly throughput (tangent CSR + residual)", value=value, unit="Melem/s",
+                n_gpus=args.gpus, steps=args.steps, warmup=args.warmup, ms_per_step=dt / args.steps * 1e3,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(W["desc"], nelem=nelem, nnode=int(W["points"].shape[0]), nnz=int(spa[0].shape[0])),
+                impl="reference",
+                cpu_baseline=dict(value=value, unit="Melem/s", cores=nthreads, kind="port",
+                                  sample="%d steps, each a full assembly of all %d elements" % (args.steps, nelem)),
+                e2e=dict(value=value, unit="Melem/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------------------
+# GPU arm
+# ------------------------------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import florence_gb300 as fl
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    W = workload(args.workload)
+    nelem, npe = W["elements"].shape
+    nq = int(np.ravel(W["w"]).shape[0])
+    nnode = W["points"].shape[0]
+    asm = fl.DeviceAssembler(W["points"], W["elements"], W["Jm"], W["w"], W["material"], W["params"], mode="csr",
+                             device=dev)
+    x = torch.from_numpy(W["x"]).to(dev)
+    V = torch.zeros(asm.nnz, dtype=torch.float64, device=dev)
+    T = torch.zeros(nnode * 3, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def step(ev=None):
+        V.zero_()
+        T.zero_()
+        if ev is not None:
+            ev[0].record(stream)
+        asm.assemble(x, V=V, T=T)
+        if ev is not None:
+            ev[1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    asm.check_flags("bench warm-up")
+    fp64_peak = fl.fp64_peak_gflops() / 1e3  # TFLOP/s, measured in this run
+    kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0.record(stream)
+        for k in range(args.steps):
+            step(kev[k])
+        t1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    ms = t0.elapsed_time(t1)
+    if world > 1:
+        tt = torch.tensor([ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms = float(tt.item())
+    kernel_ms = float(np.mean([a.elapsed_time(b) for a, b in kev]))
+    clocks = clk.summary()
+    value = nelem * world * args.steps / (ms * 1e-3) / 1e6
+
+    # roofline of the dominant kernel (assemble_df_kernel): FP64-pipe bound
+    f_alg = flops_alg(npe, nq, W["material"]) * nelem
+    f_exe = flops_executed(npe, nq, W["material"]) * nelem
+    achieved = f_alg / (kernel_ms * 1e-3) / 1e12
+    bmin = bytes_min(nnode, nelem, npe, asm.nnz)
+    hbm_peak = json.load(open(PEAKS))["hbm_gbs"] if os.path.exists(PEAKS) else 6800.0
+    tag = "assemble_df_%s_%s" % (W["desc"]["element"], W["desc"]["material"])
+    roofline = dict(bound="fp64", achieved=achieved, peak=fp64_peak, unit="TFLOP/s", frac=achieved / fp64_peak,
+                    traffic=traffic_from_profile(tag),
+                    peak_source="FP64 FMA microkernel measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
+                    flop_alg_per_launch=f_alg, flop_executed_per_launch=f_exe,
+                    executed_frac=f_exe / (kernel_ms * 1e-3) / 1e12 / fp64_peak,
+                    kernel_ms=kernel_ms,
+                    hbm=dict(bytes_min_per_launch=bmin, achieved_gbs=bmin / (kernel_ms * 1e-3) / 1e9,
+                             peak_gbs=hbm_peak, frac=bmin / (kernel_ms * 1e-3) / 1e9 / hbm_peak,
+                             peak_source="MEASURED_PEAKS.json" if os.path.exists(PEAKS) else "fallback 6.8 TB/s"))
+
+    # end to end through the drop-in callable (host numpy in and out, copies inside)
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        e2e = e2e_dropin(W, asm, args)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        spa = (asm.indices.cpu().numpy(), asm.indptr.cpu().numpy(), asm.data_local.cpu().numpy(),
+               asm.data_global.cpu().numpy())
+        v, cores, sample = cpu_assembly_rate(W, spa)
+        cpu = dict(value=v, unit="Melem/s", cores=cores, kind="port", sample=sample)
+
+    if rank == 0:
+        line = dict(metric="FP64 assembly throughput (tangent CSR + residual)", value=value, unit="Melem/s",
+                    n_gpus=world, steps=args.steps, warmup=args.warmup, ms_per_step=ms / args.steps,
+                    higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                    config=dict(W["desc"], nelem=int(nelem), nnode=int(nnode), nnz=int(asm.nnz), gauss_points=nq,
+                                parallelism="replicas" if world > 1 else "single GPU",
+                                l2="inputs larger than L2: CSR values %.0f MB and element-to-nonzero map %.0f MB "
+                                   "per step" % (asm.nnz * 8 / 1e6, asm.data_global.numel() * 4 / 1e6)),
+                    roofline=roofline, cpu_baseline=cpu, e2e=e2e, clocks=clocks,
+                    gpu_launches=args.steps)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def e2e_dropin(W, asm, args):
+    """The reference-facing call (_LowLevelAssemblyDF__<Mat>_) with host arrays: uploads mesh,
+    tables, maps and coordinates, assembles, downloads V and T -- every step."""
+    import torch
+    import florence_gb300 as fl
+    spa = (asm.indices.cpu().numpy(), asm.indptr.cpu().numpy(), asm.data_local.cpu().numpy(),
+           asm.data_global.cpu().numpy())
+    mat = W["material"]
+    p = W["params"]
+    material = types.SimpleNamespace(H_VoigtSize=6, is_transversely_isotropic=False, rho=1.0, mtype=mat)
+    if mat == "NeoHookean":
+        material.mu, material.lamb = p[0], p[1]
+    else:
+        material.mu1, material.mu2, material.lamb = p
+    fs = types.SimpleNamespace(Jm=W["Jm"], AllGauss=np.ravel(W["w"])[:, None])
+    form = types.SimpleNamespace(ndim=3, nvar=3, fields="mechanics")
+    mesh = types.SimpleNamespace(points=W["points"], elements=W["elements"].astype(np.uint64),
+                                 nelem=W["elements"].shape[0])
+    solver = types.SimpleNamespace(requires_geometry_update=1, recompute_sparsity_pattern=False,
+                                   squeeze_sparsity_pattern=False, indices=spa[0], indptr=spa[1],
+                                   data_local_indices=spa[2], data_global_indices=spa[3])
+    fn = getattr(fl, "_LowLevelAssemblyDF__" + mat + "_")
+    Ep = np.zeros(W["points"].shape[0])
+    for _ in range(2):
+        fn(solver, fs, form, mesh, material, W["x"], Ep)
+    steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        V, T = fn(solver, fs, form, mesh, material, W["x"], Ep)
+    dt = (time.perf_counter() - t0) / steps
+    h2d = sum(a.nbytes for a in (W["points"], mesh.elements, W["x"], W["Jm"], np.ravel(W["w"])) + spa)
+    d2h = V.nbytes + T.nbytes
+    return dict(value=W["elements"].shape[0] / dt / 1e6, unit="Melem/s", h2d_bytes_per_step=int(h2d),
+                d2h_bytes_per_step=int(d2h), ms_per_step=dt * 1e3, steps=steps,
+                path="florence_gb300._LowLevelAssemblyDF__%s_ (host numpy, pageable)" % mat)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -15,24 +15,27 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+FAST_PATH = os.path.join(HERE, "liboracle_fast.so")
 MATERIALS = {"NeoHookean": 1, "MooneyRivlin": 2}
 
-_lib = None
+_libs = {}
 
 
 def build(force=False):
-    """Compile liboracle.so from florence_oracle.c (seconds)."""
+    """Compile liboracle.so (checker) and liboracle_fast.so (timed baseline) from florence_oracle.c."""
     src = os.path.join(HERE, "florence_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
-        subprocess.check_call(["make", "-s", "-C", HERE, "-B", "liboracle.so"])
+    for path in (LIB_PATH, FAST_PATH):
+        if force or not os.path.exists(path) or os.path.getmtime(path) < os.path.getmtime(src):
+            subprocess.check_call(["make", "-s", "-C", HERE, "-B", os.path.basename(path)])
     return LIB_PATH
 
 
-def lib():
-    global _lib
-    if _lib is None:
+def lib(fast=False):
+    """The checker build, or with fast=True the build with the reference's optimisation flags."""
+    key = "fast" if fast else "ieee"
+    if key not in _libs:
         build()
-        L = ctypes.CDLL(LIB_PATH)
+        L = ctypes.CDLL(FAST_PATH if fast else LIB_PATH)
         P = ctypes.c_void_p
         i64 = ctypes.c_int64
         L.orc_assemble_df.argtypes = [ctypes.c_int, P, P, P, P, P, P, i64, i64, i64, ctypes.c_int, ctypes.c_int,
@@ -43,8 +46,8 @@ def lib():
         L.orc_sparsity_nnz.argtypes = [P, i64, i64, i64, i64]
         L.orc_sparsity_nnz.restype = i64
         L.orc_sparsity.argtypes = [P, i64, i64, i64, i64, P, P, P, P]
-        _lib = L
-    return _lib
+        _libs[key] = L
+    return _libs[key]
 
 
 def _p(a):
@@ -76,7 +79,7 @@ def sparsity(elements, nnode, nvar=3, maps=True):
 
 
 def assemble_df(material, params, points, elements, Eulerx, Jm, AllGauss, mode="csr", sparsity_arrays=None,
-                requires_geometry_update=1, nthreads=1):
+                requires_geometry_update=1, nthreads=1, fast=False):
     """Global tangent and residual. mode: 'triplet' -> (I, J, V, T); 'csr'/'squeeze' -> (V, T)."""
     mat = MATERIALS[material]
     prm = _c(params, np.float64)
@@ -93,16 +96,16 @@ def assemble_df(material, params, points, elements, Eulerx, Jm, AllGauss, mode="
         I = np.zeros(nelem * ndof * ndof, np.int32)
         J = np.zeros_like(I)
         V = np.zeros(nelem * ndof * ndof)
-        lib().orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
-                              requires_geometry_update, 0, _p(I), _p(J), _p(V), _p(T), None, None, None, None, nthreads)
+        lib(fast).orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
+                                  requires_geometry_update, 0, _p(I), _p(J), _p(V), _p(T), None, None, None, None, nthreads)
         return I, J, V, T
     indices, indptr, dl, dg = sparsity_arrays
     indices = _c(indices, np.int32)
     indptr = _c(indptr, np.int32)
     V = np.zeros(indices.shape[0])
     m = 1 if mode == "csr" else 2
-    lib().orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
-                          requires_geometry_update, m, None, None, _p(V), _p(T), _p(indptr), _p(indices),
+    lib(fast).orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
+                              requires_geometry_update, m, None, None, _p(V), _p(T), _p(indptr), _p(indices),
                           _p(_c(dl, np.int32) if m == 1 else None), _p(_c(dg, np.int32) if m == 1 else None), nthreads)
     return V, T
 

@@ -143,13 +143,25 @@ def test_config1_full_size(fl, oracle):
     assert rel_fro(Vt.cpu().numpy().reshape(-1, ndof, ndof)[d["emat_ids"]], d["emat_K"]) < TOL
 
 
+def large_deformation(X, seed=7):
+    """Smooth finite deformation (about 15% stretch, shear and a rotation) plus small seeded noise;
+    det F stays well away from zero, so rounding is not amplified by a near-singular map."""
+    c, s = np.cos(0.4), np.sin(0.4)
+    R = np.array([[c, -s, 0.0], [s, c, 0.0], [0.0, 0.0, 1.0]])
+    Y = X @ np.diag([1.15, 0.95, 0.9]).T
+    Y[:, 0] += 0.1 * np.sin(np.pi * X[:, 1]) + 0.05 * X[:, 2]
+    Y[:, 2] += 0.08 * np.sin(np.pi * X[:, 0])
+    return Y @ R.T + np.random.default_rng(seed).uniform(-0.005, 0.005, X.shape)
+
+
 def test_large_displacement_against_oracle(fl, oracle):
-    """Mooney-Rivlin on the config-1 mesh with a 10x larger seeded displacement: CUDA vs oracle."""
+    """Mooney-Rivlin on the config-1 mesh under a finite deformation: CUDA vs oracle."""
     d = load_golden("config1_hex8_p2_q5")
-    x = d["points"] + np.random.default_rng(7).uniform(-0.1, 0.1, d["points"].shape) * 0.3
+    x = large_deformation(d["points"])
     prm = (0.5, 0.5, 20.0)
     asm = fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], "MooneyRivlin", prm, mode="csr")
     V, T = asm.assemble(torch.from_numpy(x).cuda())
+    asm.check_flags()
     spa = (asm.indices.cpu().numpy(), asm.indptr.cpu().numpy(), asm.data_local.cpu().numpy(),
            asm.data_global.cpu().numpy())
     Vo, To = oracle.assemble_df("MooneyRivlin", prm, d["points"], d["elements"], x, d["Jm"], d["AllGauss"],
