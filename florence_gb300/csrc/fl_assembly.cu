@@ -1,39 +1,45 @@
-// fl_assembly.cu -- fused FP64 tangent + residual assembly for the displacement formulation
+// fl_assembly.cu -- FP64 tangent + residual assembly for the displacement formulation
 // (replaces _GlobalAssemblyDF_, Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDF_.h:8-176).
 //
-// One CTA assembles EPC elements. Per element:
-//  1. gather X, x of the element's nodes into shared memory;
-//  2. one thread per Gauss point: kinematics, material, and the tangent pulled back to the
-//     reference element,   Ahat[(i,d),(k,e)] = detJ sum_{j,l} G[j][d] A_ijkl G[l][e],
-//     A_ijkl = c_ijkl + d_ik sigma_jl (constitutive + geometric stiffness in one tensor),
-//     G = (dx/dxi)^{-1}; plus S[i][d] = detJ sum_j sigma_ij G[j][d] for the residual.
-//     Ahat is symmetric (45 values); both live in shared memory for all Gauss points;
-//  3. K_e[(a,i),(b,k)] = sum_g sum_{d,e} Jm[d][a][g] Ahat_g[(i,d),(k,e)] Jm[e][b][g] with
-//     U_g[b][(i,d),k] = sum_e Ahat_g[(i,d),(k,e)] Jm[e][b][g] built cooperatively per Gauss-point
-//     chunk, then 3 FMAs per stiffness entry. Only node blocks a <= b are formed (K_e is
-//     symmetric), 9 register accumulators per block, blocks ordered b-major so a warp mostly
-//     reads the same U row (shared-memory broadcast);
-//  4. scatter: triplets, CSR through the reference's element-to-nonzero maps, or CSR by binary
-//     search in the row (squeeze); residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d] into T.
-// The FP64 pipe bounds this kernel (GB300 has a reduced FP64 rate), so the design minimises FP64
-// operations: 3 per stiffness entry per Gauss point plus a per-point cost linear in the nodes.
+// Two kernels per chunk of elements:
+//  A. qp_kernel, one thread per (element, Gauss point): kinematics, material, and the tangent
+//     pulled back to the reference element
+//        Ahat[(i,d),(k,e)] = detJ sum_{j,l} G[j][d] A_ijkl G[l][e],  A_ijkl = c_ijkl + d_ik sigma_jl
+//     (constitutive + geometric stiffness folded into one tensor, G = (dx/dxi)^{-1}; Ahat is
+//     symmetric, 45 values), and S[i][d] = detJ sum_j sigma_ij G[j][d] for the residual. Written to
+//     a scratch array Q[54][chunk Gauss points] (structure of arrays: coalesced stores and loads;
+//     a chunk is sized to stay in L2).
+//  B. contract_kernel, EPC elements per CTA:
+//        K_e[(a,i),(b,k)] = sum_g sum_{d,e} Jm[d][a][g] Ahat_g[(i,d),(k,e)] Jm[e][b][g]
+//     U_g[b][(i,d),k] = sum_e Ahat_g[(i,d),(k,e)] Jm[e][b][g] is built cooperatively in shared
+//     memory per Gauss-point chunk, then each stiffness entry costs 3 FMAs per Gauss point. Only
+//     node blocks a <= b are formed (K_e is symmetric), 9 register accumulators per block, blocks
+//     ordered b-major so a warp mostly reads the same U row (shared-memory broadcast). Scatter:
+//     triplets, CSR through the reference's element-to-nonzero maps, or CSR by binary search in
+//     the row; residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d] into T.
+// The FP64 pipe bounds both kernels (GB300 has a reduced FP64 rate); the design minimises FP64
+// instructions (fused multiply-adds throughout) and keeps kernel B's register footprint small
+// so several CTAs share an SM and hide the per-chunk barriers.
 #include "fl_common.cuh"
 
 namespace fl {
 
+// contraction kernel: TPE threads per element, EPC elements per CTA, MAXB node blocks per thread
+// per pass, MINB resident CTAs per SM requested from the compiler
 template <int NPE>
 struct AsmCfg;
-// TPE threads per element, EPC elements per CTA, MAXB node blocks per thread per pass
-template <> struct AsmCfg<4> { static constexpr int TPE = 32, EPC = 8, MAXB = 1; };
-template <> struct AsmCfg<8> { static constexpr int TPE = 32, EPC = 8, MAXB = 2; };
-template <> struct AsmCfg<10> { static constexpr int TPE = 64, EPC = 4, MAXB = 1; };
-template <> struct AsmCfg<20> { static constexpr int TPE = 128, EPC = 2, MAXB = 2; };
-template <> struct AsmCfg<27> { static constexpr int TPE = 384, EPC = 1, MAXB = 1; };
-template <> struct AsmCfg<35> { static constexpr int TPE = 320, EPC = 1, MAXB = 2; };
-template <> struct AsmCfg<64> { static constexpr int TPE = 416, EPC = 1, MAXB = 5; };
-template <> struct AsmCfg<125> { static constexpr int TPE = 512, EPC = 1, MAXB = 4; };
+template <> struct AsmCfg<4> { static constexpr int TPE = 32, EPC = 8, MAXB = 1, MINB = 4; };
+template <> struct AsmCfg<8> { static constexpr int TPE = 32, EPC = 8, MAXB = 2, MINB = 4; };
+template <> struct AsmCfg<10> { static constexpr int TPE = 64, EPC = 4, MAXB = 1, MINB = 4; };
+template <> struct AsmCfg<20> { static constexpr int TPE = 128, EPC = 2, MAXB = 2, MINB = 4; };
+template <> struct AsmCfg<27> { static constexpr int TPE = 384, EPC = 1, MAXB = 1, MINB = 2; };
+template <> struct AsmCfg<35> { static constexpr int TPE = 320, EPC = 1, MAXB = 2, MINB = 2; };
+template <> struct AsmCfg<64> { static constexpr int TPE = 416, EPC = 1, MAXB = 5, MINB = 1; };
+template <> struct AsmCfg<125> { static constexpr int TPE = 512, EPC = 1, MAXB = 4, MINB = 1; };
 
-constexpr int QSTRIDE = 54;  // 45 symmetric Ahat entries + 9 residual entries per Gauss point
+constexpr int QSTRIDE = 54;    // 45 symmetric Ahat entries + 9 residual entries per Gauss point
+constexpr int QP_THREADS = 128;
+constexpr size_t CHUNK_BYTES = (size_t)64 << 20;  // scratch per chunk: L2-resident between A and B
 
 struct AsmArgs {
     const double *points;
@@ -48,6 +54,9 @@ struct AsmArgs {
     const int32_t *indptr, *indices, *dl, *dg;
     MatParams mp;
     int *flags;
+    double *Q;       // scratch [QSTRIDE][ldq]
+    int64_t e0, ne;  // element chunk [e0, e0+ne)
+    int64_t ldq;     // leading dimension of Q (>= ne*nq)
 };
 
 // index of (I,K), I,K in 0..8, in the packed upper triangle of a symmetric 9x9
@@ -56,80 +65,103 @@ __device__ __forceinline__ int sym9(int I, int K) {
     return r * 9 - (r * (r - 1)) / 2 + (c - r);
 }
 
-// Gauss-point data: Ahat (packed) and S, see the file comment.
+// ------------------------------------------------------------------------------------------------
+// A. Gauss-point data
+// ------------------------------------------------------------------------------------------------
 template <int NPE, int MAT>
-__device__ void qp_data(const AsmArgs &A, int g, const double *X, const double *x, double *q, int &flag) {
-    const double *Jm = A.Jm;
+__global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
+    const int64_t t = (int64_t)blockIdx.x * QP_THREADS + threadIdx.x;
     const int nq = A.nq;
-    auto jm = [&](int d, int a) { return __ldg(Jm + ((size_t)d * NPE + a) * nq + g); };
-    double G[9], F[9];
-    const double detJ = kinematics<NPE>(jm, X, x, __ldg(A.w + g), A.update, G, F);
-    double sig[6], b[6], J, c1, c2, cbb;
-    material<MAT>(F, A.mp, sig, b, J, c1, c2, cbb);
-    if (!(J > 0.0)) flag |= FL_FLAG_NONPOSITIVE_J;
-    // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G  (all indexed [d][e] or [i][d])
-    double GG[9], GsG[9], sG[9], bG[9], GbG[9];
+    int flag = 0;
+    if (t < A.ne * nq) {
+        const int64_t e = A.e0 + t / nq;
+        const int g = (int)(t % nq);
+        const uint64_t *el = A.elements + e * NPE;
+        auto jm = [&](int d, int a) { return __ldg(A.Jm + ((size_t)d * NPE + a) * nq + g); };
+        auto coords = [&](int a, double &X0, double &X1, double &X2, double &x0, double &x1, double &x2) {
+            uint64_t nd = __ldg(el + a);
+            if (nd >= (uint64_t)A.nnode) {
+                flag |= FL_FLAG_BAD_INDEX;
+                nd = 0;
+            }
+            X0 = __ldg(A.points + nd * 3); X1 = __ldg(A.points + nd * 3 + 1); X2 = __ldg(A.points + nd * 3 + 2);
+            x0 = __ldg(A.Eulerx + nd * 3); x1 = __ldg(A.Eulerx + nd * 3 + 1); x2 = __ldg(A.Eulerx + nd * 3 + 2);
+        };
+        double G[9], F[9];
+        const double detJ = kinematics_fn<NPE>(jm, coords, __ldg(A.w + g), A.update, G, F);
+        double sig[6], b[6], J, c1, c2, cbb;
+        material<MAT>(F, A.mp, sig, b, J, c1, c2, cbb);
+        if (!(J > 0.0)) flag |= FL_FLAG_NONPOSITIVE_J;
+        // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G (indexed [d][e] or [i][d])
+        double GG[9], GsG[9], sG[9], bG[9], GbG[9];
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+        for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            sG[i * 3 + d] = sig[s6(i, 0)] * G[0 * 3 + d] + sig[s6(i, 1)] * G[1 * 3 + d] + sig[s6(i, 2)] * G[2 * 3 + d];
-            bG[i * 3 + d] = b[s6(i, 0)] * G[0 * 3 + d] + b[s6(i, 1)] * G[1 * 3 + d] + b[s6(i, 2)] * G[2 * 3 + d];
-        }
+            for (int d = 0; d < 3; ++d) {
+                sG[i * 3 + d] = fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
+                if (MAT == MOONEYRIVLIN)
+                    bG[i * 3 + d] = fma(b[s6(i, 0)], G[0 * 3 + d], fma(b[s6(i, 1)], G[1 * 3 + d], b[s6(i, 2)] * G[2 * 3 + d]));
+            }
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
+        for (int d = 0; d < 3; ++d)
 #pragma unroll
-        for (int e = 0; e < 3; ++e) {
-            GG[d * 3 + e] = G[0 * 3 + d] * G[0 * 3 + e] + G[1 * 3 + d] * G[1 * 3 + e] + G[2 * 3 + d] * G[2 * 3 + e];
-            GsG[d * 3 + e] = G[0 * 3 + d] * sG[0 * 3 + e] + G[1 * 3 + d] * sG[1 * 3 + e] + G[2 * 3 + d] * sG[2 * 3 + e];
-            GbG[d * 3 + e] = G[0 * 3 + d] * bG[0 * 3 + e] + G[1 * 3 + d] * bG[1 * 3 + e] + G[2 * 3 + d] * bG[2 * 3 + e];
-        }
-    // Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
-    //                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ]
+            for (int e2 = d; e2 < 3; ++e2) {
+                GG[d * 3 + e2] = fma(G[d], G[e2], fma(G[3 + d], G[3 + e2], G[6 + d] * G[6 + e2]));
+                GsG[d * 3 + e2] = fma(G[d], sG[e2], fma(G[3 + d], sG[3 + e2], G[6 + d] * sG[6 + e2]));
+                if (MAT == MOONEYRIVLIN) GbG[d * 3 + e2] = fma(G[d], bG[e2], fma(G[3 + d], bG[3 + e2], G[6 + d] * bG[6 + e2]));
+            }
+        // Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
+        //                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ]
+        double *q = A.Q + t;
+        const int64_t ld = A.ldq;
 #pragma unroll
-    for (int I = 0; I < 9; ++I)
+        for (int I = 0; I < 9; ++I)
 #pragma unroll
-        for (int K = I; K < 9; ++K) {
-            const int i = I / 3, d = I % 3, k = K / 3, e = K % 3;
-            double v = c1 * G[k * 3 + d] * G[i * 3 + e] + c2 * G[i * 3 + d] * G[k * 3 + e];
-            if (i == k) v += c1 * GG[d * 3 + e] + GsG[d * 3 + e];
-            if (MAT == MOONEYRIVLIN)
-                v += cbb * (2.0 * bG[i * 3 + d] * bG[k * 3 + e] - b[s6(i, k)] * GbG[d * 3 + e] - bG[k * 3 + d] * bG[i * 3 + e]);
-            q[sym9(I, K)] = detJ * v;
-        }
+            for (int K = I; K < 9; ++K) {
+                const int i = I / 3, d = I % 3, k = K / 3, e2 = K % 3;
+                const int dd = d < e2 ? d : e2, ee = d < e2 ? e2 : d;
+                double v = fma(c1 * G[k * 3 + d], G[i * 3 + e2], c2 * G[i * 3 + d] * G[k * 3 + e2]);
+                if (i == k) v = fma(c1, GG[dd * 3 + ee], v + GsG[dd * 3 + ee]);
+                if (MAT == MOONEYRIVLIN)
+                    v = fma(cbb, fma(2.0 * bG[i * 3 + d], bG[k * 3 + e2], -fma(b[s6(i, k)], GbG[dd * 3 + ee], bG[k * 3 + d] * bG[i * 3 + e2])), v);
+                q[sym9(I, K) * ld] = detJ * v;
+            }
 #pragma unroll
-    for (int k = 0; k < 9; ++k) q[45 + k] = detJ * sG[k];  // S[i][d]
+        for (int k = 0; k < 9; ++k) q[(45 + k) * ld] = detJ * sG[k];  // S[i][d]
+    }
+    if (flag && A.flags) atomicOr(A.flags, flag);
 }
 
-template <int NPE, int MAT>
-__global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
-    assemble_df_kernel(const AsmArgs A) {
+// ------------------------------------------------------------------------------------------------
+// B. contraction + scatter
+// ------------------------------------------------------------------------------------------------
+template <int NPE>
+__global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NPE>::MINB)
+    contract_kernel(const AsmArgs A) {
     constexpr int TPE = AsmCfg<NPE>::TPE, EPC = AsmCfg<NPE>::EPC, MAXB = AsmCfg<NPE>::MAXB;
     constexpr int NT = TPE * EPC, NDOF = 3 * NPE, NBLK = NPE * (NPE + 1) / 2;
     constexpr int PER_PASS = TPE * MAXB, NPASS = (NBLK + PER_PASS - 1) / PER_PASS;
     const int nq = A.nq, QC = A.qc;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double *Xs = reinterpret_cast<double *>(smem_raw);      // [EPC][NPE*3]
-    double *xs = Xs + EPC * NPE * 3;                          // [EPC][NPE*3]
-    double *Qs = xs + EPC * NPE * 3;                          // [EPC][nq][QSTRIDE]
-    double *Jc = Qs + (size_t)EPC * nq * QSTRIDE;             // [QC][NPE][3]
-    double *Us = Jc + (size_t)QC * NPE * 3;                   // [EPC][QC][NPE][27]
+    double *Qs = reinterpret_cast<double *>(smem_raw);                      // [EPC][nq][QSTRIDE]
+    double *Jc = Qs + (size_t)EPC * nq * QSTRIDE;                           // [QC][NPE][3]
+    double *Us = Jc + (size_t)QC * NPE * 3;                                 // [EPC][QC][NPE][27]
     int *nodes = reinterpret_cast<int *>(Us + (size_t)EPC * QC * NPE * 27);  // [EPC][NPE]
-    int *inv = nodes + EPC * NPE;                                             // [EPC][NDOF]
+    int *inv = nodes + EPC * NPE;                                           // [EPC][NDOF]
     __shared__ int s_flag;
     __shared__ int64_t s_nnz;
 
     const int tid = threadIdx.x, slot = tid / TPE, lt = tid % TPE;
-    const int64_t e = (int64_t)blockIdx.x * EPC + slot;
-    const bool active = e < A.nelem;
+    const int64_t el = (int64_t)blockIdx.x * EPC + slot;  // element within the chunk
+    const int64_t e = A.e0 + el;
+    const bool active = el < A.ne;
     int flag = 0;
     if (tid == 0) {
         s_flag = 0;
         s_nnz = (A.mode != 0) ? (int64_t)A.indptr[3 * A.nnode] : 0;
     }
 
-    // 1. gather
     const int64_t cap = (int64_t)NDOF * NDOF;
     if (active) {
         for (int a = lt; a < NPE; a += TPE) {
@@ -139,11 +171,6 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
                 nd = 0;
             }
             nodes[slot * NPE + a] = (int)nd;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                Xs[(slot * NPE + a) * 3 + k] = A.points[nd * 3 + k];
-                xs[(slot * NPE + a) * 3 + k] = A.Eulerx[nd * 3 + k];
-            }
         }
         if (A.mode == 1) {
             // invert the element's dof permutation carried by data_local_indices:
@@ -155,13 +182,13 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
                 else inv[slot * NDOF + p] = i;
             }
         }
+        // Gauss-point data of this element: Q[k][el*nq + g] -> Qs[slot][g][k]
+        const double *q = A.Q + el * nq;
+        for (int idx = lt; idx < nq * QSTRIDE; idx += TPE) {
+            const int k = idx / nq, g = idx % nq;
+            Qs[((size_t)slot * nq + g) * QSTRIDE + k] = q[k * A.ldq + g];
+        }
     }
-    __syncthreads();
-
-    // 2. Gauss-point data
-    if (active)
-        for (int g = lt; g < nq; g += TPE)
-            qp_data<NPE, MAT>(A, g, Xs + slot * NPE * 3, xs + slot * NPE * 3, Qs + ((size_t)slot * nq + g) * QSTRIDE, flag);
     __syncthreads();
 
     // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d]
@@ -169,15 +196,17 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
         for (int r = lt; r < NDOF; r += TPE) {
             const int a = r / 3, i = r % 3;
             double t = 0.0;
-            const double *q = Qs + (size_t)slot * nq * QSTRIDE + 45 + i * 3;
-            for (int g = 0; g < nq; ++g, q += QSTRIDE)
-                t += __ldg(A.Jm + (size_t)a * nq + g) * q[0] + __ldg(A.Jm + ((size_t)NPE + a) * nq + g) * q[1] +
-                     __ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g) * q[2];
+            const double *qs = Qs + (size_t)slot * nq * QSTRIDE + 45 + i * 3;
+            for (int g = 0; g < nq; ++g, qs += QSTRIDE) {
+                t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[0], t);
+                t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[1], t);
+                t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2], t);
+            }
             atomicAdd(A.T + 3 * (int64_t)nodes[slot * NPE + a] + i, t);
         }
     }
 
-    // 3. stiffness, in passes over the node blocks (a <= b, b-major)
+    // stiffness, in passes over the node blocks (a <= b, b-major)
     for (int pass = 0; pass < NPASS; ++pass) {
         double acc[MAXB][9];
         int ba[MAXB], bb[MAXB];
@@ -206,7 +235,7 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
                     const double *qq = Qs + ((size_t)slot * nq + c0 + q) * QSTRIDE;
                     const double *jb = Jc + (q * NPE + b) * 3;
                     Us[(((size_t)slot * QC + q) * NPE + b) * 27 + s] =
-                        qq[sym9(I, k * 3 + 0)] * jb[0] + qq[sym9(I, k * 3 + 1)] * jb[1] + qq[sym9(I, k * 3 + 2)] * jb[2];
+                        fma(qq[sym9(I, k * 3 + 0)], jb[0], fma(qq[sym9(I, k * 3 + 1)], jb[1], qq[sym9(I, k * 3 + 2)] * jb[2]));
                 }
             }
             __syncthreads();
@@ -221,15 +250,18 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
 #pragma unroll
                         for (int i = 0; i < 3; ++i)
 #pragma unroll
-                            for (int k = 0; k < 3; ++k)
-                                acc[m][i * 3 + k] += j0 * u[(i * 3 + 0) * 3 + k] + j1 * u[(i * 3 + 1) * 3 + k] +
-                                                     j2 * u[(i * 3 + 2) * 3 + k];
+                            for (int k = 0; k < 3; ++k) {
+                                double v = acc[m][i * 3 + k];
+                                v = fma(j0, u[(i * 3 + 0) * 3 + k], v);
+                                v = fma(j1, u[(i * 3 + 1) * 3 + k], v);
+                                acc[m][i * 3 + k] = fma(j2, u[(i * 3 + 2) * 3 + k], v);
+                            }
                     }
                 }
             }
             __syncthreads();
         }
-        // 4. scatter this pass's blocks
+        // scatter this pass's blocks
         if (active) {
 #pragma unroll
             for (int m = 0; m < MAXB; ++m) {
@@ -277,14 +309,6 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC)
 }
 
 template <int NPE>
-static size_t asm_smem_bytes(int nq, int qc) {
-    constexpr int EPC = AsmCfg<NPE>::EPC;
-    return sizeof(double) * ((size_t)2 * EPC * NPE * 3 + (size_t)EPC * nq * QSTRIDE + (size_t)qc * NPE * 3 +
-                             (size_t)EPC * qc * NPE * 27) +
-           sizeof(int) * ((size_t)EPC * NPE + (size_t)EPC * 3 * NPE);
-}
-
-template <int NPE>
 static int asm_qc(int nq) {
     constexpr int EPC = AsmCfg<NPE>::EPC;
     int qc = 32768 / (EPC * NPE * 27 * 8);
@@ -293,44 +317,88 @@ static int asm_qc(int nq) {
     return qc;
 }
 
+template <int NPE>
+static size_t asm_smem_bytes(int nq, int qc) {
+    constexpr int EPC = AsmCfg<NPE>::EPC;
+    return sizeof(double) * ((size_t)EPC * nq * QSTRIDE + (size_t)qc * NPE * 3 + (size_t)EPC * qc * NPE * 27) +
+           sizeof(int) * ((size_t)EPC * NPE + (size_t)EPC * 3 * NPE);
+}
+
+// Elements per chunk for a scratch of `bytes` (a multiple of the CTA's element count).
+static int64_t chunk_elements(size_t bytes, int nq, int epc) {
+    int64_t ce = (int64_t)(bytes / (sizeof(double) * QSTRIDE * (size_t)nq));
+    return ce - ce % epc;
+}
+
+// Runs A and B over [0, nelem) in chunks of at most `chunk` elements through scratch Q.
 template <int NPE, int MAT>
-static int launch_asm(AsmArgs A, cudaStream_t stream) {
+static int run_chunks(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) {
     constexpr int EPC = AsmCfg<NPE>::EPC, NT = AsmCfg<NPE>::TPE * EPC;
     A.qc = asm_qc<NPE>(A.nq);
     const size_t smem = asm_smem_bytes<NPE>(A.nq, A.qc);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    FL_CUDA_TRY(cudaFuncSetAttribute(assemble_df_kernel<NPE, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int64_t grid = (A.nelem + EPC - 1) / EPC;
-    if (grid == 0) return FL_OK;
-    assemble_df_kernel<NPE, MAT><<<(unsigned)grid, NT, smem, stream>>>(A);
+    FL_CUDA_TRY(cudaFuncSetAttribute(contract_kernel<NPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    A.Q = Q;
+    A.ldq = chunk * A.nq;
+    for (int64_t e0 = 0; e0 < A.nelem; e0 += chunk) {
+        A.e0 = e0;
+        A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
+        const int64_t nqp = A.ne * A.nq;
+        qp_kernel<NPE, MAT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        contract_kernel<NPE><<<(unsigned)((A.ne + EPC - 1) / EPC), NT, smem, stream>>>(A);
+    }
     return launch_status();
 }
 
+template <int NPE, int MAT>
+static int launch_asm(AsmArgs A, double *scratch, size_t scratch_bytes, cudaStream_t stream) {
+    constexpr int EPC = AsmCfg<NPE>::EPC;
+    if (A.nelem == 0) return FL_OK;
+    if (scratch) {  // caller-provided scratch
+        const int64_t chunk = chunk_elements(scratch_bytes, A.nq, EPC);
+        if (chunk < EPC) return FL_ERR_CAPACITY;
+        return run_chunks<NPE, MAT>(A, scratch, chunk, stream);
+    }
+    int64_t chunk = chunk_elements(CHUNK_BYTES, A.nq, EPC);
+    if (chunk > A.nelem) chunk = A.nelem + (EPC - A.nelem % EPC) % EPC;
+    double *Q = nullptr;
+    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sizeof(double) * QSTRIDE * (size_t)A.nq * chunk, stream));
+    const int st = run_chunks<NPE, MAT>(A, Q, chunk, stream);
+    const cudaError_t fe = cudaFreeAsync(Q, stream);
+    if (st != FL_OK) return st;
+    return fe == cudaSuccess ? FL_OK : FL_ERR_CUDA;
+}
+
 template <int MAT>
-static int dispatch_asm(int npe, const AsmArgs &A, cudaStream_t s) {
+static int dispatch_asm(int npe, const AsmArgs &A, double *scratch, size_t scratch_bytes, cudaStream_t s) {
     switch (npe) {
-        case 4: return launch_asm<4, MAT>(A, s);
-        case 8: return launch_asm<8, MAT>(A, s);
-        case 10: return launch_asm<10, MAT>(A, s);
-        case 20: return launch_asm<20, MAT>(A, s);
-        case 27: return launch_asm<27, MAT>(A, s);
-        case 35: return launch_asm<35, MAT>(A, s);
-        case 64: return launch_asm<64, MAT>(A, s);
-        case 125: return launch_asm<125, MAT>(A, s);
+        case 4: return launch_asm<4, MAT>(A, scratch, scratch_bytes, s);
+        case 8: return launch_asm<8, MAT>(A, scratch, scratch_bytes, s);
+        case 10: return launch_asm<10, MAT>(A, scratch, scratch_bytes, s);
+        case 20: return launch_asm<20, MAT>(A, scratch, scratch_bytes, s);
+        case 27: return launch_asm<27, MAT>(A, scratch, scratch_bytes, s);
+        case 35: return launch_asm<35, MAT>(A, scratch, scratch_bytes, s);
+        case 64: return launch_asm<64, MAT>(A, scratch, scratch_bytes, s);
+        case 125: return launch_asm<125, MAT>(A, scratch, scratch_bytes, s);
         default: return FL_ERR_UNSUPPORTED;
     }
 }
 
-static int global_assembly_df(int mat, const double *points, const uint64_t *elements, const double *Eulerx,
-                              const double *Jm, const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss,
-                              int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t H_VoigtSize,
-                              int64_t requires_geometry_update, int32_t *I_stiff, int32_t *J_stiff, double *V_stiff,
-                              double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
-                              const int32_t *data_local_indices, const int32_t *data_global_indices, MatParams mp,
-                              int *flags, cudaStream_t stream) {
+// Argument checks and mode selection shared by the entry points. scratch == nullptr: the
+// scratch is taken from the stream-ordered allocator for the duration of the call.
+int global_assembly_df(int mat, const double *points, const uint64_t *elements, const double *Eulerx,
+                       const double *Jm, const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss,
+                       int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t H_VoigtSize,
+                       int64_t requires_geometry_update, int32_t *I_stiff, int32_t *J_stiff, double *V_stiff,
+                       double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
+                       const int32_t *data_local_indices, const int32_t *data_global_indices, MatParams mp,
+                       int *flags, double *scratch, size_t scratch_bytes, cudaStream_t stream) {
     if (ndim != 3 || nvar != 3 || H_VoigtSize != 6) return FL_ERR_ARG;
-    if (nelem < 0 || nnode <= 0 || ngauss <= 0 || ngauss > 343) return nelem < 0 || nnode <= 0 ? FL_ERR_ARG : FL_ERR_UNSUPPORTED;
+    if (nelem < 0 || nnode <= 0) return FL_ERR_ARG;
+    if (ngauss <= 0 || ngauss > 343) return FL_ERR_UNSUPPORTED;
     if (3 * nnode + 2 > INT32_MAX) return FL_ERR_UNSUPPORTED;
+    if (mat != NEOHOOKEAN && mat != MOONEYRIVLIN) return FL_ERR_UNSUPPORTED;
+    if (nelem == 0) return FL_OK;  // nothing is read or written
     if (!points || !elements || !Eulerx || !Jm || !AllGauss || !V_stiff || !T) return FL_ERR_ARG;
     AsmArgs A;
     A.points = points;
@@ -349,6 +417,9 @@ static int global_assembly_df(int mat, const double *points, const uint64_t *ele
     A.indptr = A.indices = A.dl = A.dg = nullptr;
     A.mp = mp;
     A.flags = flags;
+    A.Q = nullptr;
+    A.e0 = A.ne = A.ldq = 0;
+    A.qc = 1;
     if (recompute_sparsity_pattern) {
         if (!I_stiff || !J_stiff) return FL_ERR_ARG;
         A.mode = 0;
@@ -368,8 +439,8 @@ static int global_assembly_df(int mat, const double *points, const uint64_t *ele
             A.dg = data_global_indices;
         }
     }
-    if (mat == NEOHOOKEAN) return dispatch_asm<NEOHOOKEAN>((int)nodeperelem, A, stream);
-    return dispatch_asm<MOONEYRIVLIN>((int)nodeperelem, A, stream);
+    if (mat == NEOHOOKEAN) return dispatch_asm<NEOHOOKEAN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
+    return dispatch_asm<MOONEYRIVLIN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
 }
 
 }  // namespace fl
@@ -396,7 +467,7 @@ int fl_GlobalAssemblyDF__NeoHookean_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
     return fl::global_assembly_df(fl::NEOHOOKEAN, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem,
                                   nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
                                   recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
-                                  data_global_indices, mp, flags, (cudaStream_t)stream);
+                                  data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream);
 }
 
 int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
@@ -407,7 +478,7 @@ int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
     return fl::global_assembly_df(fl::MOONEYRIVLIN, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem,
                                   nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
                                   recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
-                                  data_global_indices, mp, flags, (cudaStream_t)stream);
+                                  data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream);
 }
 
 }  // extern "C"

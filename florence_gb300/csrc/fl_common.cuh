@@ -107,17 +107,16 @@ __device__ __forceinline__ void material(const double *F, const MatParams &mp, d
 //   Px = dx/dxi, PX = dX/dxi (rows d = xi direction), G = Px^{-1} (spatial gradients are
 //   grad N_a[j] = sum_d G[j][d] jm(d,a)), F[i][j] = sum_d Px[d][i] PX^{-1}[j][d], and
 //   detJ = w |det Px| (update) or w |det PX|, as _KinematicMeasures_.h:64-119 defines them.
-template <int NPE, class JmFn>
-__device__ __forceinline__ double kinematics(JmFn jm, const double *X, const double *x, double w, int update, double *G,
-                                             double *F) {
+template <int NPE, class JmFn, class CoordFn>
+__device__ __forceinline__ double kinematics_fn(JmFn jm, CoordFn coords, double w, int update, double *G, double *F) {
     double PX[9], Px[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) PX[k] = Px[k] = 0.0;
 #pragma unroll 4
     for (int a = 0; a < NPE; ++a) {
         const double j0 = jm(0, a), j1 = jm(1, a), j2 = jm(2, a);
-        const double X0 = X[a * 3], X1 = X[a * 3 + 1], X2 = X[a * 3 + 2];
-        const double x0 = x[a * 3], x1 = x[a * 3 + 1], x2 = x[a * 3 + 2];
+        double X0, X1, X2, x0, x1, x2;
+        coords(a, X0, X1, X2, x0, x1, x2);
         PX[0] += j0 * X0; PX[1] += j0 * X1; PX[2] += j0 * X2;
         PX[3] += j1 * X0; PX[4] += j1 * X1; PX[5] += j1 * X2;
         PX[6] += j2 * X0; PX[7] += j2 * X1; PX[8] += j2 * X2;
@@ -134,6 +133,17 @@ __device__ __forceinline__ double kinematics(JmFn jm, const double *X, const dou
         for (int j = 0; j < 3; ++j)
             F[i * 3 + j] = Px[0 * 3 + i] * iPX[j * 3 + 0] + Px[1 * 3 + i] * iPX[j * 3 + 1] + Px[2 * 3 + i] * iPX[j * 3 + 2];
     return update ? w * fabs(detx) : w * fabs(detX);
+}
+
+// kinematics_fn with the element coordinates in arrays X, x [npe*3]
+template <int NPE, class JmFn>
+__device__ __forceinline__ double kinematics(JmFn jm, const double *X, const double *x, double w, int update, double *G,
+                                             double *F) {
+    auto coords = [&](int a, double &X0, double &X1, double &X2, double &x0, double &x1, double &x2) {
+        X0 = X[a * 3]; X1 = X[a * 3 + 1]; X2 = X[a * 3 + 2];
+        x0 = x[a * 3]; x1 = x[a * 3 + 1]; x2 = x[a * 3 + 2];
+    };
+    return kinematics_fn<NPE>(jm, coords, w, update, G, F);
 }
 
 }  // namespace fl

@@ -78,9 +78,11 @@ __global__ void __launch_bounds__(IF_NT) internal_force_kernel(const IfArgs A) {
         if (e0 + slot >= A.nelem) continue;
         const double *S = Ss + (size_t)slot * nq * 9 + i * 3;
         double t = 0.0;
-        for (int g = 0; g < nq; ++g, S += 9)
-            t += __ldg(A.Jm + (size_t)a * nq + g) * S[0] + __ldg(A.Jm + ((size_t)NPE + a) * nq + g) * S[1] +
-                 __ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g) * S[2];
+        for (int g = 0; g < nq; ++g, S += 9) {
+            t = fma(__ldg(A.Jm + (size_t)a * nq + g), S[0], t);
+            t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), S[1], t);
+            t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), S[2], t);
+        }
         atomicAdd(A.T + 3 * (int64_t)nodes[slot * NPE + a] + i, t);
     }
     if (flag) atomicOr(&s_flag, flag);
@@ -182,6 +184,7 @@ int fl_GlobalAssemblyExplicit_DF_DPF_(const double *points, const uint64_t *elem
     (void)Eulerp; (void)bases; (void)H_VoigtSize; (void)requires_geometry_update; (void)rho; (void)mu3; (void)mue;
     (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e; (void)anisotropic_orientations;
     if (ndim != 3 || nvar != 3 || formulation_number != 0) return FL_ERR_ARG;
+    if (nelem == 0 && nnode > 0 && ngauss > 0) return FL_OK;  // nothing is read or written
     if (!points || !elements || !Eulerx || !Jm || !AllGauss || !T || nelem < 0 || nnode <= 0 || ngauss <= 0)
         return FL_ERR_ARG;
     fl::IfArgs A{points, elements, Eulerx, Jm, AllGauss, nelem, nnode, (int)ngauss, T, {0, 0, 0}, flags};
@@ -200,6 +203,7 @@ int fl_LumpedMass(const double *points, const uint64_t *elements, const double *
                   const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss, int64_t nelem,
                   int64_t nodeperelem, int64_t nnode, double rho, double *M, int *flags, fl_stream_t stream) {
     if (ndim != 3 || nvar != 3) return FL_ERR_ARG;
+    if (nelem == 0 && nnode > 0 && ngauss > 0) return FL_OK;  // nothing is read or written
     if (!points || !elements || !bases || !Jm || !AllGauss || !M || nelem < 0 || nnode <= 0 || ngauss <= 0 ||
         nodeperelem <= 0)
         return FL_ERR_ARG;

@@ -5,13 +5,14 @@
 
 namespace fl {
 
-constexpr int PK_CHAINS = 8, PK_ITERS = 4096, PK_NT = 256;
+constexpr int PK_CHAINS = 16, PK_ITERS = 2048, PK_NT = 256;
 
 __global__ void __launch_bounds__(PK_NT) fp64_fma_kernel(double *out, double seed) {
     double a[PK_CHAINS];
 #pragma unroll
     for (int c = 0; c < PK_CHAINS; ++c) a[c] = seed + threadIdx.x * 1e-9 + c * 1e-7;
     const double m = 0.999999, k = 1e-9;
+#pragma unroll 4
     for (int it = 0; it < PK_ITERS; ++it) {
 #pragma unroll
         for (int c = 0; c < PK_CHAINS; ++c) a[c] = fma(a[c], m, k);
