@@ -1,0 +1,34 @@
+"""CPU check that install() wires the GPU callables into the reference's own dispatcher.
+
+Runs only where the reference package is importable (the container that builds the golden
+fixtures); the GPU parity of the callables themselves is in test_gpu_assembly.py.
+"""
+import os
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+HARNESS = os.path.join(ROOT, "baseline", "_ref", "Florence")
+
+
+@pytest.mark.skipif(not os.path.isdir(HARNESS) or not os.path.isdir("/root/reference"),
+                    reason="reference package not available here")
+def test_install_registers_callables_in_reference_namespaces():
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    import florence_harness
+    F = florence_harness.import_florence()
+    import florence_gb300
+    ll = florence_gb300.install(F)
+    from Florence.FiniteElements.Assembly import _LowLevelAssembly_ as mod
+    assert mod is ll
+    for mat in ("NeoHookean", "MooneyRivlin"):
+        name = "_LowLevelAssemblyDF__" + mat + "_"
+        assert getattr(mod, name) is getattr(florence_gb300, name)
+    assert mod._LowLevelAssemblyExplicit_DF_DPF_ is florence_gb300._LowLevelAssemblyExplicit_DF_DPF_
+    from Florence.FiniteElements.Assembly.ComputeSparsityPattern import ComputeSparsityPattern
+    assert ComputeSparsityPattern is florence_gb300.ComputeSparsityPattern
+    # the dispatcher's own name lookup now finds the GPU callable
+    mat = F.NeoHookean(3, mu=1.0, lamb=10.0)
+    assert ("_LowLevelAssemblyDF__" + type(mat).__name__ + "_") in vars(mod)
