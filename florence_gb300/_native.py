@@ -19,6 +19,7 @@ FL_FLAG_NONPOSITIVE_J = 1
 FL_FLAG_BAD_INDEX = 2
 FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
+FL_NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
 class FlorenceGB300Error(RuntimeError):
@@ -55,6 +56,7 @@ def lib():
                                                 ctypes.c_size_t, P]
         for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_"):
             getattr(L, name).argtypes = _DF_ARGS
+        L.fl_GlobalAssemblyDF_noalloc.argtypes = [INT] + _DF_ARGS
         L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
                                                         D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
         L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
@@ -70,5 +72,5 @@ def check(status, what=""):
 
 # every symbol include/florence_gb300.h declares
 EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_ComputeSparsityPattern",
-           "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
+           "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_", "fl_GlobalAssemblyDF_noalloc",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak"]

@@ -20,6 +20,8 @@
 // The FP64 pipe bounds both kernels (GB300 has a reduced FP64 rate); the design minimises FP64
 // instructions (fused multiply-adds throughout) and keeps kernel B's register footprint small
 // so several CTAs share an SM and hide the per-chunk barriers.
+#include <mutex>
+
 #include "fl_common.cuh"
 
 namespace fl {
@@ -443,9 +445,61 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     return dispatch_asm<MOONEYRIVLIN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
 }
 
+// ------------------------------------------------------------------------------------------------
+// Allocation-free variant. Its Gauss-point scratch is this file-scope device array (every GPU that
+// loads the library holds it until the process exits). Host code cannot use the array's name as
+// a device address, so the address is looked up once per device with cudaGetSymbolAddress and
+// cached. Every call shares the array: the Gauss-point kernel writes every entry the contraction
+// kernel reads, so nothing needs clearing between calls, but calls that overlap on the GPU (other
+// streams, other host threads) race on it.
+// ------------------------------------------------------------------------------------------------
+static __device__ __align__(256) double g_noalloc_scratch[FL_NOALLOC_SCRATCH_BYTES / sizeof(double)];
+
+constexpr int NOALLOC_MAX_DEVICES = 256;
+static void *g_noalloc_ptr[NOALLOC_MAX_DEVICES];
+static std::mutex g_noalloc_mutex;
+
+static int noalloc_scratch(double **out) {
+    int dev = 0;
+    FL_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return FL_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FL_ERR_CUDA;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = (double *)g_noalloc_ptr[dev];
+    return FL_OK;
+}
+
 }  // namespace fl
 
 extern "C" {
+
+int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
+    (void)sorter; (void)rho; (void)mu3; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
+    (void)anisotropic_orientations;
+    fl::MatParams mp;
+    if (material_number == FL_MATERIAL_NEOHOOKEAN) mp = {mu, lamb, 0.0};
+    else if (material_number == FL_MATERIAL_MOONEYRIVLIN) mp = {mu1, mu2, lamb};
+    else return FL_ERR_UNSUPPORTED;
+    if (ngauss <= 0 || ngauss > 343 || nelem < 0) return FL_ERR_ARG;
+    // the whole mesh must fit the array in one pass: nelem * ngauss Gauss points of 54 doubles
+    if ((double)nelem * (double)ngauss * fl::QSTRIDE * sizeof(double) > (double)FL_NOALLOC_SCRATCH_BYTES)
+        return FL_ERR_CAPACITY;
+    if (nelem == 0) return FL_OK;
+    double *scratch = nullptr;
+    const int st = fl::noalloc_scratch(&scratch);
+    if (st != FL_OK) return st;
+    return fl::global_assembly_df(material_number == FL_MATERIAL_NEOHOOKEAN ? fl::NEOHOOKEAN : fl::MOONEYRIVLIN,
+                                  points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem, nodeperelem,
+                                  nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
+                                  recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
+                                  data_global_indices, mp, flags, scratch, FL_NOALLOC_SCRATCH_BYTES,
+                                  (cudaStream_t)stream);
+}
 
 const char *fl_status_string(int status) {
     switch (status) {

@@ -101,6 +101,37 @@ int fl_GlobalAssemblyDF__NeoHookean_(FL_GLOBAL_ASSEMBLY_DF_ARGS);   /* mu, lamb 
 int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu1, mu2, lamb */
 
 /* ------------------------------------------------------------------------------------------
+ * Allocation-free tangent + residual assembly. No counterpart in the reference (its assembly
+ * runs on the CPU and mallocs its own work arrays).
+ *
+ * For callers that cannot allocate device memory while they run: cudaMalloc and cudaFree may
+ * synchronise the whole device and can fail under memory pressure, so an application that
+ * reserves its device memory once at start-up -- its own pool allocator handing out every byte,
+ * or a Newton / time-stepping loop that must not stall or fail half-way -- cannot let an
+ * assembly call allocate. fl_GlobalAssemblyDF__<Mat>_ takes its Gauss-point scratch from the
+ * stream-ordered allocator on every call; this entry point instead uses a fixed array of
+ * FL_NOALLOC_SCRATCH_BYTES (32 MiB) that the library places in device memory when it is loaded
+ * (every GPU that loads the library holds it until the process exits). It calls no cudaMalloc,
+ * cudaFree or other allocating routine. The caller still passes every input and output.
+ *
+ * Same arguments and results as fl_GlobalAssemblyDF__NeoHookean_ / __MooneyRivlin_, preceded by
+ * material_number (FL_MATERIAL_NEOHOOKEAN: mu, lamb; FL_MATERIAL_MOONEYRIVLIN: mu1, mu2, lamb).
+ * Limit: nelem * ngauss * 432 bytes (54 doubles per Gauss point) must fit in
+ * FL_NOALLOC_SCRATCH_BYTES, e.g. up to 621 hex p=2 elements with 125 Gauss points or 5 548 tet
+ * p=3 elements with 14; larger meshes return FL_ERR_CAPACITY without launching anything. Such a
+ * mesh can be assembled in consecutive element ranges, because the outputs accumulate: pass
+ * elements + e0*nodeperelem, nelem = range length and, in CSR mode, data_local_indices and
+ * data_global_indices + e0*ndof^2 (triplet mode: I/J/V_stiff + e0*ndof^2).
+ * The first call on each device looks up the array's device address (cudaGetSymbolAddress, with
+ * that device current); make that first call before any stream capture. Every call uses the same
+ * array and leaves its contents behind; each call writes all the scratch it reads, so nothing
+ * has to be cleared, but calls that overlap on the GPU (different streams or host threads) race
+ * on the array and must be serialised by the caller.
+ * ------------------------------------------------------------------------------------------ */
+#define FL_NOALLOC_SCRATCH_BYTES ((size_t)32 << 20)
+int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS);
+
+/* ------------------------------------------------------------------------------------------
  * Explicit (matrix-free) internal force, T[nnode*nvar] += sum_e sum_g detJ (grad N_a . sigma).
  * Argument list of the reference's _GlobalAssemblyExplicit_DF_DPF_ plus flags and stream.
  * formulation_number must be 0 (mechanics), material_number FL_MATERIAL_NEOHOOKEAN (mu, lamb)

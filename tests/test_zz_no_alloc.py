@@ -1,0 +1,121 @@
+"""GPU test of the allocation-free assembly entry point (fl_GlobalAssemblyDF_noalloc).
+
+Some callers cannot allocate device memory while they run (an application that reserves all its
+device memory at start-up, or a solver loop that must not stall on cudaMalloc/cudaFree, which can
+synchronise the device, or fail under memory pressure). For them the library keeps a fixed 32 MiB
+device array as the Gauss-point scratch of this one entry point. This test calls it through the C
+ABI, twice in a row (the array is reused and keeps the previous call's contents), and compares
+each result with the regular entry point's, within the parity tolerance of the other tests. It
+also checks that a mesh too large for the array is rejected. The file name makes pytest collect
+it last.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_fro
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _call(L, fn_name, material_number, d, bufs, mode, nelem=None):
+    """Calls an assembly entry point with the reference's argument list (device buffers)."""
+    mat = str(d["material"])
+    prm = tuple(float(p) for p in d["params"])
+    if mat == "NeoHookean":
+        mu, mu1, mu2, lamb = prm[0], 0.0, 0.0, prm[1]
+    else:
+        mu, mu1, mu2, lamb = 0.0, prm[0], prm[1], prm[2]
+    npe = d["elements"].shape[1]
+    nq = d["AllGauss"].shape[0]
+    nelem = d["elements"].shape[0] if nelem is None else nelem
+    args = [_p(bufs["points"]), _p(bufs["elements"]), _p(bufs["x"]), None, None, _p(bufs["Jm"]), _p(bufs["w"]),
+            3, 3, nq, nelem, npe, d["points"].shape[0], 6, 1, None, None,
+            _p(bufs["I"]), _p(bufs["J"]), _p(bufs["V"]), _p(bufs["T"]), 1 if mode == "triplet" else 0, 0,
+            _p(bufs.get("dl")), _p(bufs.get("dg")), None, None,
+            1.0, mu, mu1, mu2, 0.0, 0.0, lamb, 0.0, 0.0, 0.0, 0.0, None, _p(bufs["flags"]),
+            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)]
+    fn = getattr(L, fn_name)
+    if material_number is not None:
+        return fn(material_number, *args)
+    return fn(*args)
+
+
+def _buffers(d, mode):
+    dev = torch.device("cuda")
+    b = dict(points=torch.from_numpy(d["points"]).to(dev), elements=torch.from_numpy(d["elements"]).to(dev),
+             x=torch.from_numpy(d["Eulerx"]).to(dev), Jm=torch.from_numpy(np.ascontiguousarray(d["Jm"])).to(dev),
+             w=torch.from_numpy(np.ravel(d["AllGauss"]).copy()).to(dev),
+             T=torch.zeros(d["points"].shape[0] * 3, dtype=torch.float64, device=dev),
+             flags=torch.zeros(1, dtype=torch.int32, device=dev))
+    ndof = 3 * d["elements"].shape[1]
+    cap = d["elements"].shape[0] * ndof * ndof
+    if mode == "csr":
+        b["I"] = torch.from_numpy(d["sp_indptr"]).to(dev)
+        b["J"] = torch.from_numpy(d["sp_indices"]).to(dev)
+        b["dl"] = torch.from_numpy(d["sp_data_local"]).to(dev)
+        b["dg"] = torch.from_numpy(d["sp_data_global"]).to(dev)
+        b["V"] = torch.zeros(d["sp_indices"].shape[0], dtype=torch.float64, device=dev)
+    else:
+        b["I"] = torch.zeros(cap, dtype=torch.int32, device=dev)
+        b["J"] = torch.zeros(cap, dtype=torch.int32, device=dev)
+        b["V"] = torch.zeros(cap, dtype=torch.float64, device=dev)
+    return b
+
+
+def _zero(b):
+    for k in ("V", "T", "flags"):
+        b[k].zero_()
+
+
+@pytest.mark.parametrize("case,mode", [("hex_p2_nh_q5", "csr"), ("tet_p3_mr_jitter", "triplet")])
+def test_noalloc_matches_regular_entry_point_twice(case, mode):
+    from florence_gb300 import _native as N
+    L = N.lib()
+    d = load_golden(case)
+    mat = str(d["material"])
+    mat_no = N.FL_MATERIAL_NEOHOOKEAN if mat == "NeoHookean" else N.FL_MATERIAL_MOONEYRIVLIN
+    b = _buffers(d, mode)
+    assert _call(L, "fl_GlobalAssemblyDF__" + mat + "_", None, d, b, mode) == N.FL_OK
+    torch.cuda.synchronize()
+    V_ref, T_ref = b["V"].cpu().numpy().copy(), b["T"].cpu().numpy().copy()
+    I_ref, J_ref = b["I"].cpu().numpy().copy(), b["J"].cpu().numpy().copy()
+    assert int(b["flags"].item()) == 0
+    for call in range(2):
+        _zero(b)
+        if mode == "triplet":
+            b["I"].zero_()
+            b["J"].zero_()
+        assert _call(L, "fl_GlobalAssemblyDF_noalloc", mat_no, d, b, mode) == N.FL_OK, call
+        torch.cuda.synchronize()
+        assert int(b["flags"].item()) == 0
+        assert rel_fro(b["V"].cpu().numpy(), V_ref) < TOL, call
+        assert rel_fro(b["T"].cpu().numpy(), T_ref) < TOL, call
+        if mode == "triplet":
+            assert np.array_equal(b["I"].cpu().numpy(), I_ref) and np.array_equal(b["J"].cpu().numpy(), J_ref)
+    # and against the reference's own values
+    if mode == "csr":
+        assert rel_fro(b["V"].cpu().numpy(), d["K_data"]) < TOL
+    assert rel_fro(b["T"].cpu().numpy(), d["T"]) < TOL
+
+
+def test_noalloc_rejects_mesh_larger_than_its_array():
+    """nelem * ngauss * 432 bytes above the fixed array: FL_ERR_CAPACITY, nothing launched
+    (the check precedes every device access)."""
+    from florence_gb300 import _native as N
+    L = N.lib()
+    d = load_golden("hex_p2_nh_q5")
+    b = _buffers(d, "csr")
+    too_many = N.FL_NOALLOC_SCRATCH_BYTES // (432 * d["AllGauss"].shape[0]) + 1
+    st = _call(L, "fl_GlobalAssemblyDF_noalloc", N.FL_MATERIAL_NEOHOOKEAN, d, b, "csr", nelem=too_many)
+    assert st == N.FL_ERR_CAPACITY
+    torch.cuda.synchronize()
+    assert float(b["V"].abs().sum()) == 0.0 and float(b["T"].abs().sum()) == 0.0
