@@ -313,6 +313,35 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_newton(args):
+    """Newton load stepping of the tet p=3 beam (x=0 clamped, uniform downward traction 0.01 on
+    x=4, 10 increments, relative residual 1e-10), FP64 tangent, device block-Jacobi PCG."""
+    import torch
+    import florence_gb300 as fl
+    from florence_gb300.newton import NewtonSolver, build_beam_problem
+    cells = (48, 12, 12) if args.workload != "beam_s" else (24, 6, 6)
+    P, el, Jm, w, fixed, f = build_beam_problem(*cells, traction=0.01)
+    asm = fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
+    # warm-up: module loading, one assembly and one short linear solve
+    NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32).solve()
+    solver = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10)
+    out = solver.solve()
+    u = out["u"].cpu().numpy().reshape(-1, 3)
+    tip = np.abs(P[:, 0] - 4.0) < 1e-9
+    incs = [dict(increment=i["increment"], newton=i["newton_iters"],
+                 pcg=[h["pcg_iters"] for h in i["history"]], rel=[h["rel"] for h in i["history"]])
+            for i in out["increments"]]
+    line = dict(metric="Newton wall time to rel-res 1e-10 (10 load increments, FP64 tangent, device PCG)",
+                value=out["wall_s"], unit="s", n_gpus=1, steps=1, warmup=1, higher_is_better=False,
+                scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice), Mooney-Rivlin mu1=mu2=0.5 "
+                                     "lambda=20, x=0 clamped, traction (0,0,-0.01) on x=4" % cells,
+                            nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
+                newton_iters=out["newton_iters"], pcg_iters=out["pcg_iters"], failed=out["failed"],
+                tip_uz=float(u[tip, 2].mean()), increments=incs)
+    print(json.dumps(line), flush=True)
+
+
 def e2e_dropin(W, asm, args):
     """The reference-facing call (_LowLevelAssemblyDF__<Mat>_) with host arrays: uploads mesh,
     tables, maps and coordinates, assembles, downloads V and T -- every step."""
@@ -360,11 +389,14 @@ def main():
     ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.newton:
+        run_newton(args)
     else:
         run_ours(args)
 

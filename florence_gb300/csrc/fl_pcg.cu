@@ -1,0 +1,323 @@
+// fl_pcg.cu -- Newton's linear step on the device: FP64 conjugate gradients on the assembled CSR
+// tangent with a 3x3 nodal block-Jacobi preconditioner and Dirichlet dofs masked out (the
+// reference reduces the system by slicing the CSR matrix, BoundaryCondition.GetReducedMatrices,
+// Florence/BoundaryCondition/BoundaryCondition.py:842-857, then calls a direct solver,
+// Florence/Solver/LinearSolver.py:208-330).
+//
+// Masking instead of slicing: the iteration vectors are zero on fixed dofs, the matrix-vector
+// product zeroes fixed rows, and the preconditioner block of a node with fixed dofs has those
+// rows and columns replaced by the identity. This is CG on the reduced system K_ff, with the
+// matrix left as assembled.
+//
+// One iteration = three kernels, each a grid-stride pass over all rows:
+//   K1  q = K p (one warp per row), per-block partial of p.q
+//   K2  alpha = rz_k / p.q;  x += alpha p;  r -= alpha q;  z = B^-1 r;  partials of r.z and r.r
+//   K3  beta = rz_{k+1} / rz_k;  p = z + beta p;  convergence test, done flag
+// Scalars are never copied to the host inside the iteration: every block reduces the (few
+// hundred) partials itself in a fixed order, so all blocks agree bit for bit. The host checks
+// the done flag every CHECK iterations.
+#include <algorithm>
+#include <vector>
+
+#include "fl_common.cuh"
+
+namespace fl {
+
+constexpr int PCG_NT = 256;
+constexpr int PCG_CHECK = 16;
+
+struct PcgState {
+    double *r, *z, *p, *q, *Binv;  // vectors [n], block inverses [n/3][9]
+    double *pq, *rz, *rr;          // partials [nb], rz double-buffered [2][nb]
+    double *bnorm2;                // [nb] partials of |b|^2, then [0] = |b|^2
+    int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
+};
+
+static size_t pcg_layout(int64_t n, int nb, PcgState *s, char *base) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char *p = base ? base + off : nullptr;
+        off += (bytes + 255) & ~(size_t)255;
+        return p;
+    };
+    PcgState t;
+    t.r = (double *)take(sizeof(double) * n);
+    t.z = (double *)take(sizeof(double) * n);
+    t.p = (double *)take(sizeof(double) * n);
+    t.q = (double *)take(sizeof(double) * n);
+    t.Binv = (double *)take(sizeof(double) * (n / 3) * 9);
+    t.pq = (double *)take(sizeof(double) * nb);
+    t.rz = (double *)take(sizeof(double) * 2 * nb);
+    t.rr = (double *)take(sizeof(double) * nb);
+    t.bnorm2 = (double *)take(sizeof(double) * nb);
+    t.done = (int *)take(sizeof(int) * 4);
+    if (s) *s = t;
+    return off;
+}
+
+// Block sum of one value per thread into out[blockIdx.x] (fixed order).
+__device__ __forceinline__ void block_sum_store(double v, double *out) {
+    __shared__ double red[PCG_NT / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double w = threadIdx.x < PCG_NT / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+        if (threadIdx.x == 0) out[blockIdx.x] = w;
+    }
+    __syncthreads();
+}
+
+// Sum of nb partials, identical in every block (fixed order). Result in all threads.
+__device__ __forceinline__ double sum_partials(const double *part, int nb) {
+    __shared__ double red[PCG_NT / 32];
+    __shared__ double result;
+    double v = 0.0;
+    for (int i = threadIdx.x; i < nb; i += PCG_NT) v += part[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double w = threadIdx.x < PCG_NT / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
+        if (threadIdx.x == 0) result = w;
+    }
+    __syncthreads();
+    const double r = result;
+    __syncthreads();
+    return r;
+}
+
+// 3x3 diagonal block of node m, fixed rows/columns replaced by the identity, inverted.
+__global__ void __launch_bounds__(PCG_NT) bj_setup(const int32_t *indptr, const int32_t *indices, const double *vals,
+                                                   const int8_t *fixed, int64_t nnode, double *Binv, int *err) {
+    for (int64_t m = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; m < nnode; m += (int64_t)gridDim.x * PCG_NT) {
+        double B[9];
+        for (int i = 0; i < 3; ++i) {
+            const int64_t row = 3 * m + i;
+            int lo = indptr[row], hi = indptr[row + 1];
+            const int c0 = (int)(3 * m);
+            // first entry >= c0
+            while (lo < hi) {
+                const int mid = lo + (hi - lo) / 2;
+                if (indices[mid] < c0) lo = mid + 1; else hi = mid;
+            }
+            for (int j = 0; j < 3; ++j) {
+                const int pos = lo + j;
+                double v = 0.0;
+                if (pos < indptr[row + 1] && indices[pos] == c0 + j) v = vals[pos];
+                else atomicOr(err, 1);  // diagonal block entry missing from the pattern
+                B[i * 3 + j] = v;
+            }
+        }
+        for (int i = 0; i < 3; ++i)
+            if (fixed[3 * m + i])
+                for (int j = 0; j < 3; ++j) B[i * 3 + j] = B[j * 3 + i] = (i == j) ? 1.0 : 0.0;
+        double R[9];
+        const double det = inv3(B, R);
+        if (!(fabs(det) > 0.0) || !isfinite(det)) {
+            atomicOr(err, 2);
+            for (int k = 0; k < 9; ++k) R[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        }
+        for (int k = 0; k < 9; ++k) Binv[m * 9 + k] = R[k];
+    }
+}
+
+// r = mask(b - K x), z = B^-1 r, p = z, partials of r.z (rz[0]) and |b|^2
+__global__ void __launch_bounds__(PCG_NT) pcg_init(const int32_t *indptr, const int32_t *indices, const double *vals,
+                                                   const int8_t *fixed, const double *b, const double *x, int64_t n,
+                                                   PcgState s) {
+    // (1) r = b - K x with one warp per row
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
+    double bb = 0.0;
+    for (int64_t row = warp; row < n; row += nwarps) {
+        double acc = 0.0;
+        for (int k = indptr[row] + lane; k < indptr[row + 1]; k += 32) acc = fma(vals[k], x[indices[k]], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const double bi = fixed[row] ? 0.0 : b[row];
+            s.r[row] = fixed[row] ? 0.0 : bi - acc;
+            bb = fma(bi, bi, bb);
+        }
+    }
+    block_sum_store(bb, s.bnorm2);
+}
+
+// z = B^-1 r, p = z, partial r.z  (after pcg_init's r is complete)
+__global__ void __launch_bounds__(PCG_NT) pcg_init2(int64_t nnode, PcgState s) {
+    double rz = 0.0;
+    for (int64_t m = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; m < nnode; m += (int64_t)gridDim.x * PCG_NT) {
+        const double r0 = s.r[3 * m], r1 = s.r[3 * m + 1], r2 = s.r[3 * m + 2];
+        const double *B = s.Binv + m * 9;
+        const double z0 = fma(B[0], r0, fma(B[1], r1, B[2] * r2));
+        const double z1 = fma(B[3], r0, fma(B[4], r1, B[5] * r2));
+        const double z2 = fma(B[6], r0, fma(B[7], r1, B[8] * r2));
+        s.z[3 * m] = s.p[3 * m] = z0;
+        s.z[3 * m + 1] = s.p[3 * m + 1] = z1;
+        s.z[3 * m + 2] = s.p[3 * m + 2] = z2;
+        rz = fma(r0, z0, fma(r1, z1, fma(r2, z2, rz)));
+    }
+    block_sum_store(rz, s.rz);
+}
+
+// K1: q = mask(K p), partial p.q
+__global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const int32_t *indices, const double *vals,
+                                                 const int8_t *fixed, int64_t n, PcgState s) {
+    if (s.done[0]) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
+    double pq = 0.0;
+    for (int64_t row = warp; row < n; row += nwarps) {
+        double acc = 0.0;
+        for (int k = indptr[row] + lane; k < indptr[row + 1]; k += 32) acc = fma(vals[k], s.p[indices[k]], acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if (lane == 0) {
+            const double qv = fixed[row] ? 0.0 : acc;
+            s.q[row] = qv;
+            pq = fma(s.p[row], qv, pq);
+        }
+    }
+    block_sum_store(pq, s.pq);
+}
+
+// K2: alpha, x and r updates, z = B^-1 r, partials of r.z (into rz[(k+1)%2]) and r.r
+__global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int nb, int k, double *x, PcgState s) {
+    if (s.done[0]) return;
+    const double pq = sum_partials(s.pq, nb);
+    const double rz = sum_partials(s.rz + (k & 1) * nb, nb);
+    const double alpha = rz / pq;
+    double rzn = 0.0, rr = 0.0;
+    for (int64_t m = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; m < nnode; m += (int64_t)gridDim.x * PCG_NT) {
+        double rv[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int64_t d = 3 * m + i;
+            x[d] = fma(alpha, s.p[d], x[d]);
+            rv[i] = fma(-alpha, s.q[d], s.r[d]);
+            s.r[d] = rv[i];
+        }
+        const double *B = s.Binv + m * 9;
+        const double z0 = fma(B[0], rv[0], fma(B[1], rv[1], B[2] * rv[2]));
+        const double z1 = fma(B[3], rv[0], fma(B[4], rv[1], B[5] * rv[2]));
+        const double z2 = fma(B[6], rv[0], fma(B[7], rv[1], B[8] * rv[2]));
+        s.z[3 * m] = z0;
+        s.z[3 * m + 1] = z1;
+        s.z[3 * m + 2] = z2;
+        rzn = fma(rv[0], z0, fma(rv[1], z1, fma(rv[2], z2, rzn)));
+        rr = fma(rv[0], rv[0], fma(rv[1], rv[1], fma(rv[2], rv[2], rr)));
+    }
+    block_sum_store(rzn, s.rz + ((k + 1) & 1) * nb);
+    block_sum_store(rr, s.rr);
+}
+
+// K3: beta, p update, convergence test
+__global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int nb, int k, double tol2, PcgState s) {
+    if (s.done[0]) return;
+    const double rz_new = sum_partials(s.rz + ((k + 1) & 1) * nb, nb);
+    const double rz_old = sum_partials(s.rz + (k & 1) * nb, nb);
+    const double rr = sum_partials(s.rr, nb);
+    const double beta = rz_new / rz_old;
+    for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT)
+        s.p[d] = fma(beta, s.p[d], s.z[d]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (rr <= tol2) {
+            s.done[0] = 1;
+            s.done[1] = k + 1;
+        } else if (!isfinite(rr)) {
+            s.done[0] = 1;
+            s.done[1] = k + 1;
+            s.done[2] |= 4;
+        }
+    }
+}
+
+__global__ void pcg_bnorm(int nb, PcgState s) {
+    const double b2 = sum_partials(s.bnorm2, nb);
+    if (threadIdx.x == 0) s.bnorm2[0] = b2;
+}
+
+static int grid_blocks() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return std::max(1, sms * 4);
+}
+
+static int bj_pcg(const int32_t *indptr, const int32_t *indices, const double *vals, int64_t n, const int8_t *fixed,
+                  const double *b, double *x, double rtol, int64_t maxiter, void *ws, size_t ws_bytes,
+                  int64_t *iters, double *relres, cudaStream_t st) {
+    if (!indptr || !indices || !vals || !fixed || !b || !x || !iters || !relres || n <= 0 || n % 3) return FL_ERR_ARG;
+    const int nb = grid_blocks();
+    if (pcg_layout(n, nb, nullptr, nullptr) > ws_bytes || !ws) return FL_ERR_CAPACITY;
+    PcgState s;
+    pcg_layout(n, nb, &s, (char *)ws);
+    const int64_t nnode = n / 3;
+    FL_CUDA_TRY(cudaMemsetAsync(s.done, 0, sizeof(int) * 4, st));
+    bj_setup<<<nb, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, nnode, s.Binv, s.done + 2);
+    pcg_init<<<nb, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, b, x, n, s);
+    pcg_init2<<<nb, PCG_NT, 0, st>>>(nnode, s);
+    pcg_bnorm<<<1, PCG_NT, 0, st>>>(nb, s);
+    double b2 = 0.0;
+    int err = 0;
+    FL_CUDA_TRY(cudaMemcpyAsync(&b2, s.bnorm2, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FL_CUDA_TRY(cudaMemcpyAsync(&err, s.done + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+    FL_CUDA_TRY(cudaStreamSynchronize(st));
+    if (err & 3) return FL_ERR_ARG;  // pattern without diagonal blocks, or a singular block
+    if (b2 == 0.0) {                 // zero right-hand side: x unchanged is the solution
+        *iters = 0;
+        *relres = 0.0;
+        return FL_OK;
+    }
+    const double tol2 = rtol * rtol * b2;
+    int hd[4] = {0, 0, 0, 0};
+    int64_t k = 0;
+    while (k < maxiter) {
+        const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
+        for (; k < kend; ++k) {
+            pcg_k1<<<nb, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, s);
+            pcg_k2<<<nb, PCG_NT, 0, st>>>(nnode, nb, (int)k, x, s);
+            pcg_k3<<<nb, PCG_NT, 0, st>>>(n, nb, (int)k, tol2, s);
+        }
+        FL_CUDA_TRY(cudaGetLastError());
+        FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+        FL_CUDA_TRY(cudaStreamSynchronize(st));
+        if (hd[0]) break;
+    }
+    // final residual norm from the last r.r partials
+    std::vector<double> rrp(nb);
+    FL_CUDA_TRY(cudaMemcpyAsync(rrp.data(), s.rr, sizeof(double) * nb, cudaMemcpyDeviceToHost, st));
+    FL_CUDA_TRY(cudaStreamSynchronize(st));
+    double rr = 0.0;
+    for (double v : rrp) rr += v;
+    *iters = hd[0] ? hd[1] : maxiter;
+    *relres = sqrt(rr / b2);
+    if (hd[2] & 4) return FL_ERR_ARG;  // breakdown: non-finite residual
+    return FL_OK;
+}
+
+}  // namespace fl
+
+extern "C" {
+
+size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows) {
+    return fl::pcg_layout(nrows, fl::grid_blocks(), nullptr, nullptr);
+}
+
+int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
+                      const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter, void *workspace,
+                      size_t workspace_bytes, int64_t *iterations, double *relres, fl_stream_t stream) {
+    return fl::bj_pcg(indptr, indices, values, nrows, fixed, b, x, rtol, maxiter, workspace, workspace_bytes,
+                      iterations, relres, (cudaStream_t)stream);
+}
+
+}  // extern "C"

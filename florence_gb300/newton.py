@@ -1,0 +1,205 @@
+"""Device-resident Newton-Raphson load stepping on top of the GPU assembly and PCG.
+
+Mirrors the reference's static solver (Florence/Solver/FEMSolver.py:841-929 StaticSolver and
+:932-1045 NewtonRaphson): the load is applied in equal increments; in each increment Newton
+iterates  solve K du = -R,  u += du,  re-assemble K and T,  R = T - F  on the free dofs, with the
+reference's convergence test -- the residual norm relative to its value after the first update of
+the increment (NormForces, :983-997), or the absolute norm below the tolerance (:1001-1002) --
+and its failure flags (maximum iterations, NaN or relative residual above 1e6, :1009-1021).
+
+Differences by design: the Dirichlet dofs are masked instead of sliced out of the CSR matrix, and
+the linear step is the device FP64 block-Jacobi PCG (fl_BlockJacobiPCG) with an inexact-Newton
+forcing term, instead of a direct solver. Everything stays on the GPU; only scalars (norms,
+iteration counts) reach the host.
+"""
+import ctypes
+import time
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .assembly import DeviceAssembler, _ptr, _stream
+
+
+def pcg(asm, V, b, fixed, x=None, rtol=1e-8, maxiter=20000, workspace=None):
+    """Solves K_ff x = b_f with the CSR values V of `asm`'s pattern. Returns (x, iterations, relres)."""
+    L = N.lib()
+    n = asm.nnode * 3
+    if x is None:
+        x = torch.zeros(n, dtype=torch.float64, device=asm.device)
+    if workspace is None:
+        workspace = torch.empty(L.fl_BlockJacobiPCG_workspace_size(n), dtype=torch.uint8, device=asm.device)
+    it = ctypes.c_int64(0)
+    rel = ctypes.c_double(0.0)
+    st = L.fl_BlockJacobiPCG(_ptr(asm.indptr), _ptr(asm.indices), _ptr(V), n, _ptr(fixed), _ptr(b), _ptr(x),
+                             float(rtol), int(maxiter), _ptr(workspace), workspace.numel(), ctypes.byref(it),
+                             ctypes.byref(rel), _stream())
+    N.check(st, "fl_BlockJacobiPCG")
+    return x, it.value, rel.value
+
+
+class NewtonSolver:
+    """Static load stepping for a mesh held by a DeviceAssembler (csr mode).
+
+    fixed: bool/uint8 [3N] (Dirichlet dofs, prescribed value 0); f_ext: [3N] total external load.
+    """
+
+    def __init__(self, asm, fixed, f_ext, n_increments=10, tol=1e-10, max_iter=25, pcg_maxiter=50000,
+                 eta_max=1e-2, eta_min=1e-12):
+        if asm.mode != "csr":
+            raise ValueError("Newton needs the CSR tangent (mode='csr')")
+        self.asm = asm
+        dev = asm.device
+        self.fixed = torch.as_tensor(np.asarray(fixed, dtype=np.int8), device=dev).contiguous()
+        self.free = (self.fixed == 0).to(torch.float64)
+        self.f_ext = torch.as_tensor(np.asarray(f_ext, dtype=np.float64), device=dev).contiguous()
+        self.n_increments = n_increments
+        self.tol = tol
+        self.max_iter = max_iter
+        self.pcg_maxiter = pcg_maxiter
+        self.eta_max = eta_max
+        self.eta_min = eta_min
+        self.X = asm.points.reshape(-1)
+        n = asm.nnode * 3
+        self.V = torch.zeros(asm.nnz, dtype=torch.float64, device=dev)
+        self.T = torch.zeros(n, dtype=torch.float64, device=dev)
+        L = N.lib()
+        self.ws = torch.empty(L.fl_BlockJacobiPCG_workspace_size(n), dtype=torch.uint8, device=dev)
+        self.history = []
+
+    def _assemble(self, u):
+        self.V.zero_()
+        self.T.zero_()
+        self.asm.assemble((self.X + u).reshape(-1, 3), V=self.V, T=self.T)
+
+    def solve(self, u0=None, guesses=None):
+        """Runs all increments. guesses: optional callable(increment, u_prev) -> initial u for the
+        increment (a warm start; the previous increment's solution otherwise). Returns a dict."""
+        dev = self.asm.device
+        n = self.asm.nnode * 3
+        u = torch.zeros(n, dtype=torch.float64, device=dev) if u0 is None else u0.clone()
+        self._assemble(u)
+        t0 = time.perf_counter()
+        total_newton = 0
+        total_pcg = 0
+        failed = False
+        incs = []
+        for inc in range(1, self.n_increments + 1):
+            F = self.f_ext * (inc / self.n_increments)
+            if guesses is not None:
+                g = guesses(inc, u)
+                if g is not None:
+                    u = g.clone()
+                    self._assemble(u)
+            R = (self.T - F) * self.free
+            norm_forces = None
+            it = 0
+            rel = np.inf
+            eta = 1e-3
+            iters = []
+            while True:
+                du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
+                                     workspace=self.ws)
+                total_pcg += pits
+                u += du
+                self._assemble(u)
+                R = (self.T - F) * self.free
+                absn = float(torch.linalg.vector_norm(R))
+                if it == 0:
+                    norm_forces = absn if absn != 0.0 else 1e-14
+                rel = abs(absn / norm_forces)
+                iters.append(dict(iter=it, abs=absn, rel=rel, pcg_iters=pits, pcg_relres=prel, eta=eta))
+                if absn < self.tol:
+                    break
+                it += 1
+                if rel <= self.tol and it > 0:
+                    break
+                if it >= self.max_iter or not np.isfinite(rel) or rel > 1e6:
+                    failed = True
+                    break
+                # inexact Newton: solve to a tolerance proportional to the current relative residual
+                eta = float(min(self.eta_max, max(self.eta_min, 0.1 * rel)))
+            total_newton += len(iters)
+            incs.append(dict(increment=inc, newton_iters=len(iters), history=iters))
+            if failed:
+                break
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        self.history = incs
+        return dict(u=u, wall_s=wall, newton_iters=total_newton, pcg_iters=total_pcg, failed=failed,
+                    increments=incs)
+
+
+# ------------------------------------------------------------------------------------------------
+# Neumann loads on tetrahedral boundary faces (host preprocessing, once per mesh)
+# ------------------------------------------------------------------------------------------------
+
+def _triangle_rule(n=5):
+    """Collapsed Gauss rule on the reference triangle {s,t >= 0, s+t <= 1} (exact to degree 2n-2)."""
+    x, w = np.polynomial.legendre.leggauss(n)
+    x = (x + 1) / 2
+    w = w / 2
+    S, T, W = [], [], []
+    for i in range(n):
+        for j in range(n):
+            S.append(x[i])
+            T.append(x[j] * (1 - x[i]))
+            W.append(w[i] * w[j] * (1 - x[i]))
+    return np.array(S), np.array(T), np.array(W)
+
+
+def _face_weights(st):
+    """Integrals of the Lagrange basis on the face nodes st [m,2] over the reference triangle,
+    divided by its area (they sum to 1)."""
+    m = st.shape[0]
+    deg = int(round((np.sqrt(8 * m + 1) - 3) / 2))
+    mons = [(i, j) for i in range(deg + 1) for j in range(deg + 1 - i)]
+    Vm = np.array([[s ** i * t ** j for (i, j) in mons] for s, t in st])
+    Cinv = np.linalg.inv(Vm)  # basis_a(s,t) = sum_k Cinv[k,a] mon_k(s,t)
+    S, T, W = _triangle_rule(deg + 3)
+    mon_int = np.array([np.sum(W * S ** i * T ** j) for (i, j) in mons])
+    return (mon_int @ Cinv) / 0.5
+
+
+def tet_face_loads(points, elements, pattern, on_face, traction):
+    """Consistent nodal forces of a uniform dead-load traction on the boundary faces whose three
+    vertices satisfy on_face(X) (X: [3] coordinates). pattern: barycentric node layout [npe,4].
+    Returns f [3N]."""
+    P = np.asarray(points)
+    el = np.asarray(elements, dtype=np.int64)
+    lam = np.asarray(pattern)
+    f = np.zeros(P.shape[0] * 3)
+    tr = np.asarray(traction, dtype=np.float64)
+    vmask = np.array([[bool(on_face(P[el[e, v]])) for v in range(4)] for e in range(el.shape[0])])
+    cache = {}
+    for e in np.nonzero(vmask.sum(1) >= 3)[0]:
+        for opp in range(4):
+            verts = [v for v in range(4) if v != opp]
+            if not all(vmask[e, v] for v in verts):
+                continue
+            nodes = np.nonzero(np.abs(lam[:, opp]) < 1e-10)[0]
+            if opp not in cache:
+                st = lam[nodes][:, verts[1:]]  # (lambda of 2nd and 3rd face vertex) as (s, t)
+                cache[opp] = (nodes, _face_weights(st))
+            nodes, wts = cache[opp]
+            A = P[el[e, verts]]
+            area = 0.5 * np.linalg.norm(np.cross(A[1] - A[0], A[2] - A[0]))
+            for a, wa in zip(nodes, wts):
+                f[3 * el[e, a]:3 * el[e, a] + 3] += tr * area * wa
+    return f
+
+
+def build_beam_problem(nx=48, ny=12, nz=12, traction=0.01, seed=1):
+    """The Newton configuration: p=3 tet beam 4x1x1 (jittered lattice, Delaunay), Mooney-Rivlin
+    mu1 = mu2 = 0.5, lambda = 20, x=0 clamped, uniform downward traction on x=4. Returns
+    (points, elements, Jm, AllGauss, fixed [3N] bool, f_ext [3N])."""
+    import os
+    from . import meshes
+    here = os.path.dirname(os.path.abspath(__file__))
+    t = np.load(os.path.join(here, "..", "tests", "golden", "tet_p3_mr_jitter.npz"))
+    pat = meshes.local_pattern(t["points"], t["elements"], 0, "tet")
+    P, el = meshes.jittered_tet_beam((nx, ny, nz), (4.0, 1.0, 1.0), seed, pat)
+    fixed = np.repeat(np.abs(P[:, 0]) < 1e-9, 3)
+    f = tet_face_loads(P, el, pat, lambda X: abs(X[0] - 4.0) < 1e-9, (0.0, 0.0, -traction))
+    return P, el, t["Jm"], t["AllGauss"], fixed, f

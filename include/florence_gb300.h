@@ -156,6 +156,27 @@ int fl_LumpedMass(const double *points, const uint64_t *elements, const double *
                   int64_t nodeperelem, int64_t nnode, double rho, double *M, int *flags, fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Newton's linear step: K_ff x_f = b_f by conjugate gradients with a 3x3 nodal block-Jacobi
+ * preconditioner, FP64, on the assembled CSR tangent (replaces the reduce-and-solve of
+ * NewtonRaphson, Solver/FEMSolver.py:951-954: BoundaryCondition.GetReducedMatrices,
+ * BoundaryCondition.py:842-857, and LinearSolver.Solve, Solver/LinearSolver.py:208-330).
+ *   indptr/indices/values  CSR of K [nrows x nrows], nrows = 3 * nodes, every 3x3 diagonal block
+ *                          present in the pattern (true for assembled tangents)
+ *   fixed [nrows]          1 for Dirichlet dofs: their rows and columns are left out (masking)
+ *   b [nrows]              right-hand side (fixed entries ignored)
+ *   x [nrows]              in: initial guess with zero fixed entries; out: solution
+ *   stop when |r| <= rtol |b| (free dofs) or after maxiter iterations; iterations and relres
+ *   (host out) report where it stopped. workspace: fl_BlockJacobiPCG_workspace_size(nrows) bytes.
+ * Synchronises the stream every 16 iterations to test convergence. FL_ERR_ARG on a missing or
+ * singular diagonal block or a non-finite residual.
+ * ------------------------------------------------------------------------------------------ */
+size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows);
+int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
+                      const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter,
+                      void *workspace, size_t workspace_bytes, int64_t *iterations, double *relres,
+                      fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
  * Measurement helper: device time of a dependent FP64 FMA loop over the whole GPU, used to
  * measure the FP64 roof that the assembly kernels are bound by. Synchronises the stream.
  * gflops (host out) = achieved FP64 GFLOP/s (2 flops per FMA).
