@@ -342,6 +342,43 @@ def run_newton(args):
     print(json.dumps(line), flush=True)
 
 
+def run_explicit(args):
+    """Explicit dynamics of the p=2 hex beam (64x8x8 elements on [0,8]x[0,1]x[0,1], both ends
+    clamped, neo-Hookean mu=1 lambda=1000 rho=1, lumped mass, v_z = 0.1 sin(pi x / L) at t=0,
+    dt = 0.9 x critical, 10 000 central-difference steps), internal force in FP64 and in FP32."""
+    import torch
+    from florence_gb300.explicit import ExplicitSolver, build_explicit_beam
+    n = (64, 8, 8) if args.workload != "beam_s" else (32, 4, 4)
+    nsteps = args.explicit_steps
+    P, el, Jm, w, B, fixed = build_explicit_beam(*n, L=8.0)
+    s = ExplicitSolver(P, el, Jm, w, B, 1.0, 1000.0, 1.0, fixed)
+    dtc, lam = s.critical_dt(iters=30)
+    dt = 0.9 * dtc
+    v0 = np.zeros_like(P)
+    v0[:, 2] = 0.1 * np.sin(np.pi * P[:, 0] / 8.0)
+    res = {}
+    for mode in ("fp64", "fp32"):
+        s.run(v0.ravel(), dt, 200, mode=mode, energy_every=0)   # warm-up (graph capture, clocks)
+        r = s.run(v0.ravel(), dt, nsteps, mode=mode, energy_every=max(1, nsteps // 50))
+        E = np.array([k + i for _, k, i in r["energy"]])
+        res[mode] = dict(wall_s=r["wall_s"], steps=r["steps"], steps_per_s=r["steps"] / r["wall_s"],
+                         energy_drift_max=float(np.abs(E / E[0] - 1.0).max()),
+                         energy_drift_final=float(E[-1] / E[0] - 1.0), blowup=r["blowup"], u=r["u"])
+    l2 = float(torch.linalg.vector_norm(res["fp32"]["u"] - res["fp64"]["u"]) /
+               torch.linalg.vector_norm(res["fp64"]["u"]))
+    for m in res:
+        res[m].pop("u")
+    line = dict(metric="explicit central-difference steps per second (FP64 internal force)",
+                value=res["fp64"]["steps_per_s"], unit="steps/s", n_gpus=1, steps=nsteps, warmup=200,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(workload="p=2 hex beam %dx%dx%d on [0,8]x[0,1]x[0,1], ends clamped, neo-Hookean mu=1 "
+                                     "lambda=1000 rho=1, lumped mass, v_z=0.1 sin(pi x/8)" % n,
+                            nelem=int(el.shape[0]), nnode=int(P.shape[0]), gauss_points=int(np.ravel(w).shape[0]),
+                            dt=dt, dt_critical=dtc, omega_max=float(np.sqrt(lam))),
+                fp64=res["fp64"], fp32=res["fp32"], l2_fp32_vs_fp64=l2)
+    print(json.dumps(line), flush=True)
+
+
 def e2e_dropin(W, asm, args):
     """The reference-facing call (_LowLevelAssemblyDF__<Mat>_) with host arrays: uploads mesh,
     tables, maps and coordinates, assembles, downloads V and T -- every step."""
@@ -390,6 +427,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")
+    ap.add_argument("--explicit", action="store_true", help="explicit dynamics of the hex beam instead")
+    ap.add_argument("--explicit-steps", type=int, default=10000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -397,6 +436,8 @@ def main():
         run_reference(args)
     elif args.newton:
         run_newton(args)
+    elif args.explicit:
+        run_explicit(args)
     else:
         run_ours(args)
 

@@ -339,7 +339,7 @@ static int run_chunks(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) 
     A.qc = asm_qc<NPE>(A.nq);
     const size_t smem = asm_smem_bytes<NPE>(A.nq, A.qc);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    FL_CUDA_TRY(cudaFuncSetAttribute(contract_kernel<NPE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    { const int st = ensure_smem<contract_kernel<NPE>>(smem); if (st != FL_OK) return st; }
     A.Q = Q;
     A.ldq = chunk * A.nq;
     for (int64_t e0 = 0; e0 < A.nelem; e0 += chunk) {

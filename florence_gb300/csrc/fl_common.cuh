@@ -18,6 +18,24 @@ namespace fl {
 
 inline int launch_status() { return cudaGetLastError() == cudaSuccess ? FL_OK : FL_ERR_CUDA; }
 
+// Raises a kernel's dynamic shared-memory limit only when a launch needs more than any earlier
+// one did on this device (one attribute call per kernel, device and size in steady state, so
+// repeated launches -- e.g. inside a captured time loop -- make no runtime calls besides the
+// launch itself). Kernel is the kernel's address as a template argument: one record per kernel.
+template <auto Kernel>
+inline int ensure_smem(size_t bytes) {
+    constexpr int MAXDEV = 64;
+    static size_t set_bytes[MAXDEV] = {};
+    if (bytes <= 48 * 1024) return FL_OK;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FL_ERR_CUDA;
+    if (dev >= 0 && dev < MAXDEV && bytes <= set_bytes[dev]) return FL_OK;
+    if (cudaFuncSetAttribute(Kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+        return FL_ERR_CUDA;
+    if (dev >= 0 && dev < MAXDEV) set_bytes[dev] = bytes;
+    return FL_OK;
+}
+
 // Material numbers (match FL_MATERIAL_*).
 enum { NEOHOOKEAN = 1, MOONEYRIVLIN = 2 };
 

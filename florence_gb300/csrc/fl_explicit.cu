@@ -8,6 +8,8 @@
 //   one thread per (element, Gauss point): kinematics and stress, S[i][d] = detJ sum_j sigma_ij G[j][d];
 //   one thread per (element, node, component): t = sum_g sum_d Jm[d][a][g] S_g[i][d], added into T.
 // Same quantity as the implicit residual: T_(a,i) = sum_g detJ (sigma . grad N_a)_i.
+#include <algorithm>
+
 #include "fl_common.cuh"
 
 namespace fl {
@@ -94,7 +96,7 @@ template <int NPE, int MAT>
 static int launch_if(const IfArgs &A, cudaStream_t s) {
     const size_t smem = sizeof(double) * ((size_t)2 * IF_EPC * NPE * 3 + (size_t)IF_EPC * A.nq * 9) + sizeof(int) * IF_EPC * NPE;
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    FL_CUDA_TRY(cudaFuncSetAttribute(internal_force_kernel<NPE, MAT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    { const int st = ensure_smem<internal_force_kernel<NPE, MAT>>(smem); if (st != FL_OK) return st; }
     const int64_t grid = (A.nelem + IF_EPC - 1) / IF_EPC;
     if (grid == 0) return FL_OK;
     internal_force_kernel<NPE, MAT><<<(unsigned)grid, IF_NT, smem, s>>>(A);
@@ -209,11 +211,278 @@ int fl_LumpedMass(const double *points, const uint64_t *elements, const double *
         return FL_ERR_ARG;
     const size_t smem = sizeof(double) * ((size_t)fl::LM_EPC * ngauss + ngauss);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    FL_CUDA_TRY(cudaFuncSetAttribute(fl::lumped_mass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    { const int st = fl::ensure_smem<fl::lumped_mass_kernel>(smem); if (st != FL_OK) return st; }
     const int64_t grid = (nelem + fl::LM_EPC - 1) / fl::LM_EPC;
     if (grid == 0) return FL_OK;
     fl::lumped_mass_kernel<<<(unsigned)grid, fl::LM_NT, smem, (cudaStream_t)stream>>>(
         points, elements, bases, Jm, AllGauss, nelem, (int)nodeperelem, (int)ngauss, nnode, rho, M, flags);
+    return fl::launch_status();
+}
+
+}  // extern "C"
+
+// ================================================================================================
+// Explicit central-difference time stepping (replaces the lumped-mass loop of
+// ExplicitStructuralDynamicIntegrator.Solver, Florence/TimeIntegrators/
+// ExplicitStructuralDynamicIntegrator.py:28-245): reference gradients for the FP32 internal force,
+// the FP32 internal force, the leapfrog update, and the strain energy for energy bookkeeping.
+// ================================================================================================
+namespace fl {
+
+// grad0[((e*nq + g)*npe + a)*3 + d] = dN_a/dX_d at Gauss point g (FP32), dV[e*nq + g] = w |det dX/dxi|
+template <int NPE>
+__global__ void __launch_bounds__(128) ref_grad_kernel(const double *points, const uint64_t *elements, const double *Jm,
+                                                       const double *w, int64_t nelem, int nq, int64_t nnode,
+                                                       float *grad0, float *dV, int *flags) {
+    const int64_t t = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (t >= nelem * nq) return;
+    const int64_t e = t / nq;
+    const int g = (int)(t % nq);
+    double PX[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < NPE; ++a) {
+        uint64_t nd = elements[e * NPE + a];
+        if (nd >= (uint64_t)nnode) {
+            if (flags) atomicOr(flags, FL_FLAG_BAD_INDEX);
+            nd = 0;
+        }
+        for (int d = 0; d < 3; ++d) {
+            const double j = Jm[((size_t)d * NPE + a) * nq + g];
+            PX[d * 3] = fma(j, points[nd * 3], PX[d * 3]);
+            PX[d * 3 + 1] = fma(j, points[nd * 3 + 1], PX[d * 3 + 1]);
+            PX[d * 3 + 2] = fma(j, points[nd * 3 + 2], PX[d * 3 + 2]);
+        }
+    }
+    double iPX[9];
+    const double det = inv3(PX, iPX);
+    dV[t] = (float)(w[g] * fabs(det));
+    for (int a = 0; a < NPE; ++a) {
+        const double j0 = Jm[((size_t)0 * NPE + a) * nq + g], j1 = Jm[((size_t)1 * NPE + a) * nq + g],
+                     j2 = Jm[((size_t)2 * NPE + a) * nq + g];
+        for (int d = 0; d < 3; ++d)  // dN_a/dX_d = sum_k (dX/dxi)^{-1}[d][k] dN_a/dxi_k
+            grad0[((size_t)t * NPE + a) * 3 + d] = (float)fma(iPX[d * 3], j0, fma(iPX[d * 3 + 1], j1, iPX[d * 3 + 2] * j2));
+    }
+}
+
+// FP32 internal force (total Lagrangian form, neo-Hookean): H = grad_0 u, F = I + H,
+// P = mu/J (q I + H + H^T + j H - cof H) + lamb j cof F with j = J - 1 = tr H + q and
+// q = (tr^2 H - tr H^2)/2 + det H, cof F = (1 + tr H) I - H^T + cof H -- every term formed from
+// H directly, so small strains keep FP32's relative precision. T_a += P grad_0 N_a dV in FP32.
+// This is the same internal force as the reference's sum_g detJ sigma grad N_a, rewritten in the
+// reference configuration.
+constexpr int F32_EPC = 4, F32_NT = 128;
+
+template <int NPE>
+__global__ void __launch_bounds__(F32_NT) internal_force_f32_kernel(const uint64_t *elements, const double *u,
+                                                                    const float *grad0, const float *dV, int64_t nelem,
+                                                                    int nq, int64_t nnode, float mu, float lamb,
+                                                                    float *T, int *flags) {
+    __shared__ float us[F32_EPC][NPE * 3];
+    __shared__ float Ps[F32_EPC][32][9];  // first Piola stress x dV per Gauss point (nq <= 32)
+    __shared__ int nodes[F32_EPC][NPE];
+    const int64_t e0 = (int64_t)blockIdx.x * F32_EPC;
+    int flag = 0;
+    for (int idx = threadIdx.x; idx < F32_EPC * NPE; idx += F32_NT) {
+        const int s = idx / NPE, a = idx % NPE;
+        if (e0 + s >= nelem) continue;
+        uint64_t nd = elements[(e0 + s) * NPE + a];
+        if (nd >= (uint64_t)nnode) {
+            flag |= FL_FLAG_BAD_INDEX;
+            nd = 0;
+        }
+        nodes[s][a] = (int)nd;
+        us[s][a * 3] = (float)u[nd * 3];
+        us[s][a * 3 + 1] = (float)u[nd * 3 + 1];
+        us[s][a * 3 + 2] = (float)u[nd * 3 + 2];
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < F32_EPC * nq; idx += F32_NT) {
+        const int s = idx / nq, g = idx % nq;
+        const int64_t e = e0 + s;
+        if (e >= nelem) continue;
+        const float *gr = grad0 + ((size_t)(e * nq + g) * NPE) * 3;
+        float H[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        for (int a = 0; a < NPE; ++a) {
+            const float g0 = gr[a * 3], g1 = gr[a * 3 + 1], g2 = gr[a * 3 + 2];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const float ui = us[s][a * 3 + i];
+                H[i * 3] = fmaf(ui, g0, H[i * 3]);
+                H[i * 3 + 1] = fmaf(ui, g1, H[i * 3 + 1]);
+                H[i * 3 + 2] = fmaf(ui, g2, H[i * 3 + 2]);
+            }
+        }
+        const float trH = H[0] + H[4] + H[8];
+        const float trH2 = H[0] * H[0] + H[4] * H[4] + H[8] * H[8] + 2.f * (H[1] * H[3] + H[2] * H[6] + H[5] * H[7]);
+        float cH[9];  // cofactor of H
+        cH[0] = H[4] * H[8] - H[5] * H[7];
+        cH[1] = H[5] * H[6] - H[3] * H[8];
+        cH[2] = H[3] * H[7] - H[4] * H[6];
+        cH[3] = H[2] * H[7] - H[1] * H[8];
+        cH[4] = H[0] * H[8] - H[2] * H[6];
+        cH[5] = H[1] * H[6] - H[0] * H[7];
+        cH[6] = H[1] * H[5] - H[2] * H[4];
+        cH[7] = H[2] * H[3] - H[0] * H[5];
+        cH[8] = H[0] * H[4] - H[1] * H[3];
+        const float detH = H[0] * cH[0] + H[1] * cH[1] + H[2] * cH[2];
+        const float q = 0.5f * (trH * trH - trH2) + detH;
+        const float j = trH + q;
+        const float J = 1.f + j;
+        if (!(J > 0.f)) flag |= FL_FLAG_NONPOSITIVE_J;
+        const float a1 = mu / J, a2 = lamb * j;
+        const float dv = dV[e * nq + g];
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float id = (r == c) ? 1.f : 0.f;
+                const float A = q * id + H[r * 3 + c] + H[c * 3 + r] + j * H[r * 3 + c] - cH[r * 3 + c];
+                const float cofF = (1.f + trH) * id - H[c * 3 + r] + cH[r * 3 + c];
+                Ps[s][g][r * 3 + c] = (a1 * A + a2 * cofF) * dv;
+            }
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < F32_EPC * NPE * 3; idx += F32_NT) {
+        const int s = idx / (NPE * 3), r = idx % (NPE * 3), a = r / 3, i = r % 3;
+        const int64_t e = e0 + s;
+        if (e >= nelem) continue;
+        float t = 0.f;
+        for (int g = 0; g < nq; ++g) {
+            const float *gr = grad0 + ((size_t)(e * nq + g) * NPE + a) * 3;
+            t = fmaf(Ps[s][g][i * 3], gr[0], fmaf(Ps[s][g][i * 3 + 1], gr[1], fmaf(Ps[s][g][i * 3 + 2], gr[2], t)));
+        }
+        atomicAdd(T + 3 * (int64_t)nodes[s][a] + i, t);
+    }
+    if (flag && flags) atomicOr(flags, flag);
+}
+
+// leapfrog central difference: a = (F - T)/M on free dofs, v += dt a, u += dt v
+template <class TT>
+__global__ void cd_update_kernel(int64_t n, double dt, const TT *T, const double *Fext, const double *Minv,
+                                 const int8_t *fixed, double *u, double *v) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (fixed[i]) continue;
+        const double f = (Fext ? Fext[i] : 0.0) - (double)T[i];
+        const double vi = fma(dt, f * Minv[i], v[i]);
+        v[i] = vi;
+        u[i] = fma(dt, vi, u[i]);
+    }
+}
+
+// strain energy sum_e sum_g W(F) w |det dX/dxi|: neo-Hookean W = mu/2 (tr C - 3) - mu ln J + lamb/2 (J-1)^2
+// (NeoHookean.InternalEnergy, Florence/MaterialLibrary/NeoHookean.py:70-80)
+template <int NPE>
+__global__ void __launch_bounds__(128) strain_energy_kernel(const double *points, const uint64_t *elements,
+                                                            const double *Eulerx, const double *Jm, const double *w,
+                                                            int64_t nelem, int nq, int64_t nnode, double mu,
+                                                            double lamb, double *energy) {
+    const int64_t t = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    double W = 0.0;
+    if (t < nelem * nq) {
+        const int64_t e = t / nq;
+        const int g = (int)(t % nq);
+        const uint64_t *el = elements + e * NPE;
+        auto jm = [&](int d, int a) { return Jm[((size_t)d * NPE + a) * nq + g]; };
+        auto coords = [&](int a, double &X0, double &X1, double &X2, double &x0, double &x1, double &x2) {
+            uint64_t nd = el[a];
+            if (nd >= (uint64_t)nnode) nd = 0;
+            X0 = points[nd * 3]; X1 = points[nd * 3 + 1]; X2 = points[nd * 3 + 2];
+            x0 = Eulerx[nd * 3]; x1 = Eulerx[nd * 3 + 1]; x2 = Eulerx[nd * 3 + 2];
+        };
+        double G[9], F[9];
+        const double dV = kinematics_fn<NPE>(jm, coords, w[g], 0, G, F);  // w |det dX/dxi|
+        const double J = det3(F);
+        double trC = 0.0;
+        for (int k = 0; k < 9; ++k) trC = fma(F[k], F[k], trC);
+        W = (0.5 * mu * (trC - 3.0) - mu * log(J) + 0.5 * lamb * (J - 1.0) * (J - 1.0)) * dV;
+    }
+    __shared__ double red[4];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) W += __shfl_down_sync(0xffffffffu, W, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = W;
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(energy, red[0] + red[1] + red[2] + red[3]);
+}
+
+}  // namespace fl
+
+#define FL_NPE_CASES(MACRO) MACRO(4) MACRO(8) MACRO(10) MACRO(20) MACRO(27) MACRO(35) MACRO(64) MACRO(125)
+
+extern "C" {
+
+int fl_ReferenceGradients(const double *points, const uint64_t *elements, const double *Jm, const double *AllGauss,
+                          int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode, float *grad0, float *dV,
+                          int *flags, fl_stream_t stream) {
+    if (nelem < 0 || ngauss <= 0 || nnode <= 0) return FL_ERR_ARG;
+    if (nelem == 0) return FL_OK;
+    if (!points || !elements || !Jm || !AllGauss || !grad0 || !dV) return FL_ERR_ARG;
+    const unsigned grid = (unsigned)((nelem * ngauss + 127) / 128);
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (nodeperelem) {
+#define FL_CASE(N)                                                                                              \
+    case N:                                                                                                     \
+        fl::ref_grad_kernel<N><<<grid, 128, 0, s>>>(points, elements, Jm, AllGauss, nelem, (int)ngauss, nnode, \
+                                                    grad0, dV, flags);                                          \
+        break;
+        FL_NPE_CASES(FL_CASE)
+#undef FL_CASE
+        default: return FL_ERR_UNSUPPORTED;
+    }
+    return fl::launch_status();
+}
+
+int fl_InternalForceF32(const uint64_t *elements, const double *u, const float *grad0, const float *dV, int64_t ngauss,
+                        int64_t nelem, int64_t nodeperelem, int64_t nnode, int material_number, double mu, double lamb,
+                        float *T, int *flags, fl_stream_t stream) {
+    if (material_number != FL_MATERIAL_NEOHOOKEAN) return FL_ERR_UNSUPPORTED;
+    if (nelem < 0 || ngauss <= 0 || ngauss > 32 || nnode <= 0) return ngauss > 32 ? FL_ERR_UNSUPPORTED : FL_ERR_ARG;
+    if (nelem == 0) return FL_OK;
+    if (!elements || !u || !grad0 || !dV || !T) return FL_ERR_ARG;
+    const unsigned grid = (unsigned)((nelem + fl::F32_EPC - 1) / fl::F32_EPC);
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (nodeperelem) {
+#define FL_CASE(N)                                                                                          \
+    case N:                                                                                                 \
+        fl::internal_force_f32_kernel<N><<<grid, fl::F32_NT, 0, s>>>(elements, u, grad0, dV, nelem,         \
+                                                                     (int)ngauss, nnode, (float)mu,         \
+                                                                     (float)lamb, T, flags);                \
+        break;
+        FL_NPE_CASES(FL_CASE)
+#undef FL_CASE
+        default: return FL_ERR_UNSUPPORTED;
+    }
+    return fl::launch_status();
+}
+
+int fl_CentralDifferenceUpdate(int64_t n, double dt, const void *T, int T_is_f32, const double *Fext,
+                               const double *Minv, const int8_t *fixed, double *u, double *v, fl_stream_t stream) {
+    if (n < 0 || !T || !Minv || !fixed || !u || !v) return FL_ERR_ARG;
+    if (n == 0) return FL_OK;
+    const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 152 * 8);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (T_is_f32) fl::cd_update_kernel<float><<<grid, 256, 0, s>>>(n, dt, (const float *)T, Fext, Minv, fixed, u, v);
+    else fl::cd_update_kernel<double><<<grid, 256, 0, s>>>(n, dt, (const double *)T, Fext, Minv, fixed, u, v);
+    return fl::launch_status();
+}
+
+int fl_StrainEnergy(const double *points, const uint64_t *elements, const double *Eulerx, const double *Jm,
+                    const double *AllGauss, int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode,
+                    int material_number, double mu, double lamb, double *energy, fl_stream_t stream) {
+    if (material_number != FL_MATERIAL_NEOHOOKEAN) return FL_ERR_UNSUPPORTED;
+    if (nelem < 0 || ngauss <= 0 || nnode <= 0 || !energy) return FL_ERR_ARG;
+    if (nelem == 0) return FL_OK;
+    if (!points || !elements || !Eulerx || !Jm || !AllGauss) return FL_ERR_ARG;
+    const unsigned grid = (unsigned)((nelem * ngauss + 127) / 128);
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (nodeperelem) {
+#define FL_CASE(N)                                                                                               \
+    case N:                                                                                                      \
+        fl::strain_energy_kernel<N><<<grid, 128, 0, s>>>(points, elements, Eulerx, Jm, AllGauss, nelem,          \
+                                                         (int)ngauss, nnode, mu, lamb, energy);                  \
+        break;
+        FL_NPE_CASES(FL_CASE)
+#undef FL_CASE
+        default: return FL_ERR_UNSUPPORTED;
+    }
     return fl::launch_status();
 }
 
