@@ -61,6 +61,10 @@ def lib():
                                                         D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
         L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
         L.fl_measure_fp64_peak.argtypes = [ctypes.POINTER(D), P]
+        L.fl_ReferenceGradients.argtypes = [P, P, P, P, I64, I64, I64, I64, P, P, P, P]
+        L.fl_InternalForceF32.argtypes = [P, P, P, P, I64, I64, I64, I64, INT, D, D, P, P, P]
+        L.fl_CentralDifferenceUpdate.argtypes = [I64, D, P, INT, P, P, P, P, P, P]
+        L.fl_StrainEnergy.argtypes = [P, P, P, P, P, I64, I64, I64, I64, INT, D, D, P, P]
         L.fl_BlockJacobiPCG_workspace_size.argtypes = [I64]
         L.fl_BlockJacobiPCG_workspace_size.restype = ctypes.c_size_t
         L.fl_BlockJacobiPCG.argtypes = [P, P, P, I64, P, P, P, D, I64, P, ctypes.c_size_t, ctypes.POINTER(I64),
@@ -78,4 +82,5 @@ def check(status, what=""):
 EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_ComputeSparsityPattern",
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_", "fl_GlobalAssemblyDF_noalloc",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak",
-           "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG"]
+           "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
+           "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy"]

@@ -156,6 +156,36 @@ int fl_LumpedMass(const double *points, const uint64_t *elements, const double *
                   int64_t nodeperelem, int64_t nnode, double rho, double *M, int *flags, fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
+ * Explicit central-difference dynamics (the lumped-mass loop of
+ * ExplicitStructuralDynamicIntegrator.Solver, TimeIntegrators/ExplicitStructuralDynamicIntegrator.py:28-245).
+ *
+ * fl_ReferenceGradients: grad0 [nelem][ngauss][nodeperelem][3] (FP32) = dN_a/dX at each Gauss
+ *   point and dV [nelem][ngauss] (FP32) = w |det dX/dxi|, once per mesh, for fl_InternalForceF32.
+ * fl_InternalForceF32: T [nnode*3] (FP32) += internal force at displacement u [nnode*3] (FP64
+ *   state, converted per element), computed and accumulated in FP32 in the total-Lagrangian form
+ *   (first Piola stress from H = grad_0 u without forming I + H, so small strains keep FP32's
+ *   relative precision). The FP32 counterpart of fl_GlobalAssemblyExplicit_DF_DPF_ (same
+ *   quantity). Neo-Hookean only (mu, lamb); ngauss <= 32.
+ * fl_CentralDifferenceUpdate: on free dofs a = (Fext - T) / M (Minv given, Fext may be NULL),
+ *   v += dt a, u += dt v -- the leapfrog form of the reference's lumped update
+ *   (ExplicitStructuralDynamicIntegrator.py:131-139). T is FP64, or FP32 when T_is_f32 != 0.
+ * fl_StrainEnergy: *energy += sum_e sum_g W(F) w |det dX/dxi| at Eulerx (neo-Hookean
+ *   W = mu/2 (tr C - 3) - mu ln J + lamb/2 (J-1)^2, MaterialLibrary/NeoHookean.py:70-80; the
+ *   reference sums it in DisplacementFormulation.GetEnergy, DisplacementFormulation.py:326-371).
+ * ------------------------------------------------------------------------------------------ */
+int fl_ReferenceGradients(const double *points, const uint64_t *elements, const double *Jm, const double *AllGauss,
+                          int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode, float *grad0,
+                          float *dV, int *flags, fl_stream_t stream);
+int fl_InternalForceF32(const uint64_t *elements, const double *u, const float *grad0, const float *dV,
+                        int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode, int material_number,
+                        double mu, double lamb, float *T, int *flags, fl_stream_t stream);
+int fl_CentralDifferenceUpdate(int64_t n, double dt, const void *T, int T_is_f32, const double *Fext,
+                               const double *Minv, const int8_t *fixed, double *u, double *v, fl_stream_t stream);
+int fl_StrainEnergy(const double *points, const uint64_t *elements, const double *Eulerx, const double *Jm,
+                    const double *AllGauss, int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode,
+                    int material_number, double mu, double lamb, double *energy, fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
  * Newton's linear step: K_ff x_f = b_f by conjugate gradients with a 3x3 nodal block-Jacobi
  * preconditioner, FP64, on the assembled CSR tangent (replaces the reduce-and-solve of
  * NewtonRaphson, Solver/FEMSolver.py:951-954: BoundaryCondition.GetReducedMatrices,
