@@ -9,13 +9,14 @@
 // rows and columns replaced by the identity. This is CG on the reduced system K_ff, with the
 // matrix left as assembled.
 //
-// One iteration = three kernels, each a grid-stride pass over all rows:
-//   K1  q = K p (one warp per row), per-block partial of p.q
-//   K2  alpha = rz_k / p.q;  x += alpha p;  r -= alpha q;  z = B^-1 r;  partials of r.z and r.r
+// One iteration = four kernels:
+//   K1  q = K p (one warp per row, as many warps as rows), p.q
+//   K2  alpha = rz_k / p.q;  x += alpha p;  r -= alpha q;  z = B^-1 r;  r.z and r.r
 //   K3  beta = rz_{k+1} / rz_k;  p = z + beta p;  convergence test, done flag
-// Scalars are never copied to the host inside the iteration: every block reduces the (few
-// hundred) partials itself in a fixed order, so all blocks agree bit for bit. The host checks
-// the done flag every CHECK iterations.
+//   K4  clears the p.q slot for the next iteration
+// Dot products are block-reduced and added into device scalar slots with one FP64 atomic per
+// block; the scalars never travel to the host inside the iteration (kernels read them from the
+// slots), and the host checks the done flag every PCG_CHECK iterations.
 #include <algorithm>
 #include <vector>
 
@@ -28,8 +29,7 @@ constexpr int PCG_CHECK = 16;
 
 struct PcgState {
     double *r, *z, *p, *q, *Binv;  // vectors [n], block inverses [n/3][9]
-    double *pq, *rz, *rr;          // partials [nb], rz double-buffered [2][nb]
-    double *bnorm2;                // [nb] partials of |b|^2, then [0] = |b|^2
+    double *acc;                   // [0] p.q, [1],[2] r.z of even/odd iterates, [3] r.r, [4] |b|^2
     int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
 };
 
@@ -46,17 +46,14 @@ static size_t pcg_layout(int64_t n, int nb, PcgState *s, char *base) {
     t.p = (double *)take(sizeof(double) * n);
     t.q = (double *)take(sizeof(double) * n);
     t.Binv = (double *)take(sizeof(double) * (n / 3) * 9);
-    t.pq = (double *)take(sizeof(double) * nb);
-    t.rz = (double *)take(sizeof(double) * 2 * nb);
-    t.rr = (double *)take(sizeof(double) * nb);
-    t.bnorm2 = (double *)take(sizeof(double) * nb);
+    t.acc = (double *)take(sizeof(double) * 8);
     t.done = (int *)take(sizeof(int) * 4);
     if (s) *s = t;
     return off;
 }
 
-// Block sum of one value per thread into out[blockIdx.x] (fixed order).
-__device__ __forceinline__ void block_sum_store(double v, double *out) {
+// Block sum of one value per thread, added to *out with one atomic.
+__device__ __forceinline__ void block_atomic_add(double v, double *out) {
     __shared__ double red[PCG_NT / 32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -66,31 +63,9 @@ __device__ __forceinline__ void block_sum_store(double v, double *out) {
         double w = threadIdx.x < PCG_NT / 32 ? red[threadIdx.x] : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-        if (threadIdx.x == 0) out[blockIdx.x] = w;
+        if (threadIdx.x == 0) atomicAdd(out, w);
     }
     __syncthreads();
-}
-
-// Sum of nb partials, identical in every block (fixed order). Result in all threads.
-__device__ __forceinline__ double sum_partials(const double *part, int nb) {
-    __shared__ double red[PCG_NT / 32];
-    __shared__ double result;
-    double v = 0.0;
-    for (int i = threadIdx.x; i < nb; i += PCG_NT) v += part[i];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double w = threadIdx.x < PCG_NT / 32 ? red[threadIdx.x] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) w += __shfl_down_sync(0xffffffffu, w, o);
-        if (threadIdx.x == 0) result = w;
-    }
-    __syncthreads();
-    const double r = result;
-    __syncthreads();
-    return r;
 }
 
 // 3x3 diagonal block of node m, fixed rows/columns replaced by the identity, inverted.
@@ -148,7 +123,7 @@ __global__ void __launch_bounds__(PCG_NT) pcg_init(const int32_t *indptr, const 
             bb = fma(bi, bi, bb);
         }
     }
-    block_sum_store(bb, s.bnorm2);
+    block_atomic_add(bb, s.acc + 4);
 }
 
 // z = B^-1 r, p = z, partial r.z  (after pcg_init's r is complete)
@@ -165,20 +140,29 @@ __global__ void __launch_bounds__(PCG_NT) pcg_init2(int64_t nnode, PcgState s) {
         s.z[3 * m + 2] = s.p[3 * m + 2] = z2;
         rz = fma(r0, z0, fma(r1, z1, fma(r2, z2, rz)));
     }
-    block_sum_store(rz, s.rz);
+    block_atomic_add(rz, s.acc + 1);
 }
 
-// K1: q = mask(K p), partial p.q
+// Dot products of the iteration are accumulated with one FP64 atomic add per block into scalar
+// slots: acc[0] = p.q, acc[1 + (k & 1)] = r.z of iterate k (double-buffered), acc[3] = r.r.
+// Each kernel zeroes the slot the next kernel accumulates into, after every reader is done.
+
+// K1: q = mask(K p) with one warp per row, p.q; zeroes r.z of iterate k+1 and r.r for K2
 __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const int32_t *indices, const double *vals,
-                                                 const int8_t *fixed, int64_t n, PcgState s) {
+                                                 const int8_t *fixed, int64_t n, int k, PcgState s) {
     if (s.done[0]) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        s.acc[1 + ((k + 1) & 1)] = 0.0;
+        s.acc[3] = 0.0;
+    }
     const int lane = threadIdx.x & 31;
     const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
     double pq = 0.0;
     for (int64_t row = warp; row < n; row += nwarps) {
         double acc = 0.0;
-        for (int k = indptr[row] + lane; k < indptr[row + 1]; k += 32) acc = fma(vals[k], s.p[indices[k]], acc);
+        const int end = indptr[row + 1];
+        for (int kk = indptr[row] + lane; kk < end; kk += 32) acc = fma(vals[kk], s.p[indices[kk]], acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) {
@@ -187,15 +171,13 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
             pq = fma(s.p[row], qv, pq);
         }
     }
-    block_sum_store(pq, s.pq);
+    block_atomic_add(pq, s.acc + 0);
 }
 
-// K2: alpha, x and r updates, z = B^-1 r, partials of r.z (into rz[(k+1)%2]) and r.r
-__global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int nb, int k, double *x, PcgState s) {
+// K2: alpha = rz_k / p.q, x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r
+__global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x, PcgState s) {
     if (s.done[0]) return;
-    const double pq = sum_partials(s.pq, nb);
-    const double rz = sum_partials(s.rz + (k & 1) * nb, nb);
-    const double alpha = rz / pq;
+    const double alpha = s.acc[1 + (k & 1)] / s.acc[0];
     double rzn = 0.0, rr = 0.0;
     for (int64_t m = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; m < nnode; m += (int64_t)gridDim.x * PCG_NT) {
         double rv[3];
@@ -216,17 +198,15 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int nb, int k, d
         rzn = fma(rv[0], z0, fma(rv[1], z1, fma(rv[2], z2, rzn)));
         rr = fma(rv[0], rv[0], fma(rv[1], rv[1], fma(rv[2], rv[2], rr)));
     }
-    block_sum_store(rzn, s.rz + ((k + 1) & 1) * nb);
-    block_sum_store(rr, s.rr);
+    block_atomic_add(rzn, s.acc + 1 + ((k + 1) & 1));
+    block_atomic_add(rr, s.acc + 3);
 }
 
-// K3: beta, p update, convergence test
-__global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int nb, int k, double tol2, PcgState s) {
+// K3: beta = rz_{k+1} / rz_k, p = z + beta p, convergence test; zeroes p.q for the next K1
+__global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, PcgState s) {
     if (s.done[0]) return;
-    const double rz_new = sum_partials(s.rz + ((k + 1) & 1) * nb, nb);
-    const double rz_old = sum_partials(s.rz + (k & 1) * nb, nb);
-    const double rr = sum_partials(s.rr, nb);
-    const double beta = rz_new / rz_old;
+    const double beta = s.acc[1 + ((k + 1) & 1)] / s.acc[1 + (k & 1)];
+    const double rr = s.acc[3];
     for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT)
         s.p[d] = fma(beta, s.p[d], s.z[d]);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -241,9 +221,9 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int nb, int k, doubl
     }
 }
 
-__global__ void pcg_bnorm(int nb, PcgState s) {
-    const double b2 = sum_partials(s.bnorm2, nb);
-    if (threadIdx.x == 0) s.bnorm2[0] = b2;
+// zeroes p.q after every block of K3 has read the scalars of iterate k
+__global__ void pcg_k4(PcgState s) {
+    if (!s.done[0]) s.acc[0] = 0.0;
 }
 
 static int grid_blocks() {
@@ -262,18 +242,22 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const double *v
     PcgState s;
     pcg_layout(n, nb, &s, (char *)ws);
     const int64_t nnode = n / 3;
+    const unsigned g_rows = (unsigned)((n + (PCG_NT / 32) - 1) / (PCG_NT / 32));  // one warp per row
+    const unsigned g_nodes = (unsigned)std::min<int64_t>((nnode + PCG_NT - 1) / PCG_NT, 152 * 16);
+    const unsigned g_dofs = (unsigned)std::min<int64_t>((n + PCG_NT - 1) / PCG_NT, 152 * 16);
     FL_CUDA_TRY(cudaMemsetAsync(s.done, 0, sizeof(int) * 4, st));
-    bj_setup<<<nb, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, nnode, s.Binv, s.done + 2);
-    pcg_init<<<nb, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, b, x, n, s);
-    pcg_init2<<<nb, PCG_NT, 0, st>>>(nnode, s);
-    pcg_bnorm<<<1, PCG_NT, 0, st>>>(nb, s);
-    double b2 = 0.0;
+    FL_CUDA_TRY(cudaMemsetAsync(s.acc, 0, sizeof(double) * 8, st));
+    bj_setup<<<g_nodes, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, nnode, s.Binv, s.done + 2);
+    pcg_init<<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, b, x, n, s);
+    pcg_init2<<<g_nodes, PCG_NT, 0, st>>>(nnode, s);
+    double hacc[8];
     int err = 0;
-    FL_CUDA_TRY(cudaMemcpyAsync(&b2, s.bnorm2, sizeof(double), cudaMemcpyDeviceToHost, st));
+    FL_CUDA_TRY(cudaMemcpyAsync(hacc, s.acc, sizeof(hacc), cudaMemcpyDeviceToHost, st));
     FL_CUDA_TRY(cudaMemcpyAsync(&err, s.done + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
     FL_CUDA_TRY(cudaStreamSynchronize(st));
     if (err & 3) return FL_ERR_ARG;  // pattern without diagonal blocks, or a singular block
-    if (b2 == 0.0) {                 // zero right-hand side: x unchanged is the solution
+    const double b2 = hacc[4];
+    if (b2 == 0.0) {  // zero right-hand side: x unchanged is the solution
         *iters = 0;
         *relres = 0.0;
         return FL_OK;
@@ -284,23 +268,20 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const double *v
     while (k < maxiter) {
         const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
         for (; k < kend; ++k) {
-            pcg_k1<<<nb, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, s);
-            pcg_k2<<<nb, PCG_NT, 0, st>>>(nnode, nb, (int)k, x, s);
-            pcg_k3<<<nb, PCG_NT, 0, st>>>(n, nb, (int)k, tol2, s);
+            pcg_k1<<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
+            pcg_k2<<<g_nodes, PCG_NT, 0, st>>>(nnode, (int)k, x, s);
+            pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, s);
+            pcg_k4<<<1, 1, 0, st>>>(s);
         }
         FL_CUDA_TRY(cudaGetLastError());
         FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
         FL_CUDA_TRY(cudaStreamSynchronize(st));
         if (hd[0]) break;
     }
-    // final residual norm from the last r.r partials
-    std::vector<double> rrp(nb);
-    FL_CUDA_TRY(cudaMemcpyAsync(rrp.data(), s.rr, sizeof(double) * nb, cudaMemcpyDeviceToHost, st));
+    FL_CUDA_TRY(cudaMemcpyAsync(hacc, s.acc, sizeof(hacc), cudaMemcpyDeviceToHost, st));
     FL_CUDA_TRY(cudaStreamSynchronize(st));
-    double rr = 0.0;
-    for (double v : rrp) rr += v;
     *iters = hd[0] ? hd[1] : maxiter;
-    *relres = sqrt(rr / b2);
+    *relres = sqrt(hacc[3] / b2);
     if (hd[2] & 4) return FL_ERR_ARG;  // breakdown: non-finite residual
     return FL_OK;
 }
