@@ -57,6 +57,8 @@ def lib():
         for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_"):
             getattr(L, name).argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_noalloc.argtypes = [INT] + _DF_ARGS
+        L.fl_GlobalAssemblyDF_Mixed.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, D, D, D, D,
+                                                P, P]
         L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
                                                         D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
         L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
@@ -67,8 +69,8 @@ def lib():
         L.fl_StrainEnergy.argtypes = [P, P, P, P, P, I64, I64, I64, I64, INT, D, D, P, P]
         L.fl_BlockJacobiPCG_workspace_size.argtypes = [I64]
         L.fl_BlockJacobiPCG_workspace_size.restype = ctypes.c_size_t
-        L.fl_BlockJacobiPCG.argtypes = [P, P, P, I64, P, P, P, D, I64, P, ctypes.c_size_t, ctypes.POINTER(I64),
-                                        ctypes.POINTER(D), P]
+        L.fl_BlockJacobiPCG.argtypes = [P, P, P, INT, I64, P, P, P, D, I64, P, ctypes.c_size_t,
+                                        ctypes.POINTER(I64), ctypes.POINTER(D), P]
         _lib = L
     return _lib
 
@@ -83,4 +85,4 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_", "fl_GlobalAssemblyDF_noalloc",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
-           "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy"]
+           "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed"]

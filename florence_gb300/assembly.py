@@ -177,6 +177,29 @@ class DeviceAssembler:
             return I, J, V, T
         return V, T
 
+    def assemble_mixed(self, Eulerx, V32=None, T=None, stream=None):
+        """Inexact-Newton Jacobian: FP32 CSR values from the split-BF16 tensor-core contraction and
+        the FP64 residual (csr mode only). Accumulates into V32/T when given."""
+        if self.mode != "csr":
+            raise ValueError("the mixed tangent is assembled in csr mode")
+        L = N.lib()
+        x = Eulerx if Eulerx.is_contiguous() else Eulerx.contiguous()
+        if V32 is None:
+            V32 = torch.zeros(self.nnz, dtype=torch.float32, device=self.device)
+        if T is None:
+            T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
+        p0, p1, p2 = self.params
+        if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN:
+            mu, mu1, mu2, lamb = p0, 0.0, 0.0, p1
+        else:
+            mu, mu1, mu2, lamb = 0.0, p0, p1, p2
+        st = L.fl_GlobalAssemblyDF_Mixed(self.mat_id, _ptr(self.points), _ptr(self.elements), _ptr(x), _ptr(self.Jm),
+                                         _ptr(self.w), self.nq, self.nelem, self.npe, self.nnode, self.update,
+                                         _ptr(self.indptr), _ptr(self.data_local), _ptr(self.data_global), _ptr(V32),
+                                         _ptr(T), mu, mu1, mu2, lamb, _ptr(self.flags), stream or _stream())
+        N.check(st, "fl_GlobalAssemblyDF_Mixed")
+        return V32, T
+
     # -- explicit internal force ----------------------------------------------------------------
     def internal_force(self, Eulerx, T=None, stream=None):
         L = N.lib()

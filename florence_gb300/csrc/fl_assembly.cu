@@ -20,6 +20,9 @@
 // The FP64 pipe bounds both kernels (GB300 has a reduced FP64 rate); the design minimises FP64
 // instructions (fused multiply-adds throughout) and keeps kernel B's register footprint small
 // so several CTAs share an SM and hide the per-chunk barriers.
+#include <cuda_bf16.h>
+
+#include <algorithm>
 #include <mutex>
 
 #include "fl_common.cuh"
@@ -446,6 +449,205 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
 }
 
 // ------------------------------------------------------------------------------------------------
+// C. Mixed-precision contraction on the tensor cores (inexact-Newton Jacobian).
+//
+// Per element, K^T[(i,b,k), a] = sum_{(g,d)} U^T[(i,b,k),(g,d)] L[(g,d), a] with
+// U_g[(i,d),(b,k)] = sum_e Ahat_g[(i,d),(k,e)] Jm[e][b][g] (from the FP64 Gauss-point data, formed
+// in FP32) and L[(g,d), a] = Jm[d][a][g]. Both operands are split into BF16 pairs (hi = bf16(x),
+// lo = bf16(x - hi)) and multiplied as hi*hi + hi*lo + lo*hi with FP32 accumulation
+// (mma.sync m16n8k16 bf16): about 16 significant bits per operand, relative tangent error
+// ~1e-5. The result goes to FP32 CSR values (the Jacobian the FP64 PCG applies); the residual is
+// formed in FP64 exactly as in contract_kernel. Rows are processed in chunks of MX_MC and the
+// reduction dimension in chunks of MX_KC, so any element order fits in shared memory.
+// ------------------------------------------------------------------------------------------------
+constexpr int MX_NT = 128, MX_MC = 64, MX_KC = 96;
+
+__device__ __forceinline__ void bf16_split(float v, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+    hi = __float2bfloat16_rn(v);
+    lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+}
+
+__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint32_t *b) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+template <int NPE>
+__global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, float *V32) {
+    constexpr int NDOF = 3 * NPE, M = 9 * NPE, NP = (NPE + 7) / 8 * 8, NT8 = NP / 8;
+    constexpr int AST = MX_KC + 8;  // padded row stride (bf16) of the A chunk
+    const int nq = A.nq, K = 3 * nq;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *Qs = reinterpret_cast<double *>(smem_raw);                              // [nq][QSTRIDE]
+    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + (size_t)nq * QSTRIDE);  // [MX_MC][AST]
+    __nv_bfloat16 *Al = Ah + MX_MC * AST;
+    __nv_bfloat16 *Bh = Al + MX_MC * AST;                                            // [NP][AST]
+    __nv_bfloat16 *Bl = Bh + NP * AST;
+    int *nodes = reinterpret_cast<int *>(Bl + NP * AST);                             // [NPE]
+    int *inv = nodes + NPE;                                                          // [NDOF]
+    __shared__ int s_flag;
+    __shared__ int64_t s_nnz;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
+    const int64_t cap = (int64_t)NDOF * NDOF;
+    int flag = 0;
+    if (tid == 0) {
+        s_flag = 0;
+        s_nnz = (int64_t)A.indptr[3 * A.nnode];
+    }
+    for (int64_t el = blockIdx.x; el < A.ne; el += gridDim.x) {
+        const int64_t e = A.e0 + el;
+        __syncthreads();  // previous element done with the shared buffers
+        for (int a = tid; a < NPE; a += MX_NT) {
+            uint64_t nd = A.elements[e * NPE + a];
+            if (nd >= (uint64_t)A.nnode) {
+                flag |= FL_FLAG_BAD_INDEX;
+                nd = 0;
+            }
+            nodes[a] = (int)nd;
+        }
+        for (int i = tid; i < NDOF; i += MX_NT) {
+            const int v = A.dl[e * cap + (int64_t)i * NDOF];
+            const int p = v / NDOF;
+            if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
+            else inv[p] = i;
+        }
+        const double *q = A.Q + el * nq;
+        for (int idx = tid; idx < nq * QSTRIDE; idx += MX_NT) {
+            const int k = idx / nq, g = idx % nq;
+            Qs[(size_t)g * QSTRIDE + k] = q[k * A.ldq + g];
+        }
+        __syncthreads();
+        // residual in FP64
+        if (A.update) {
+            for (int r = tid; r < NDOF; r += MX_NT) {
+                const int a = r / 3, i = r % 3;
+                double t = 0.0;
+                const double *qs = Qs + 45 + i * 3;
+                for (int g = 0; g < nq; ++g, qs += QSTRIDE) {
+                    t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[0], t);
+                    t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[1], t);
+                    t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2], t);
+                }
+                atomicAdd(A.T + 3 * (int64_t)nodes[a] + i, t);
+            }
+        }
+        for (int m0 = 0; m0 < M; m0 += MX_MC) {
+            float acc[NT8][4];
+#pragma unroll
+            for (int t = 0; t < NT8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
+            for (int k0 = 0; k0 < K; k0 += MX_KC) {
+                const int kc = min(MX_KC, K - k0), kcp = (kc + 15) / 16 * 16;
+                __syncthreads();  // previous chunk's MMAs done
+                // A chunk: rows r = m0 + rr -> (i, b, k) with r = (i*NPE + b)*3 + k; cols c = k0 + cc -> (g, d)
+                for (int idx = tid; idx < MX_MC * kcp; idx += MX_NT) {
+                    const int rr = idx / kcp, cc = idx % kcp, r = m0 + rr, c = k0 + cc;
+                    float v = 0.f;
+                    if (r < M && cc < kc) {
+                        const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+                        const int g = c / 3, d = c % 3, I = i * 3 + d;
+                        const double *qq = Qs + (size_t)g * QSTRIDE;
+                        v = (float)fma(qq[sym9(I, k * 3 + 0)], __ldg(A.Jm + ((size_t)0 * NPE + b) * nq + g),
+                                       fma(qq[sym9(I, k * 3 + 1)], __ldg(A.Jm + ((size_t)1 * NPE + b) * nq + g),
+                                           qq[sym9(I, k * 3 + 2)] * __ldg(A.Jm + ((size_t)2 * NPE + b) * nq + g)));
+                    }
+                    bf16_split(v, Ah[rr * AST + cc], Al[rr * AST + cc]);
+                }
+                // B chunk, stored [n][k]: B[(g,d), a] = Jm[d][a][g]
+                for (int idx = tid; idx < NP * kcp; idx += MX_NT) {
+                    const int n = idx / kcp, cc = idx % kcp, c = k0 + cc;
+                    float v = 0.f;
+                    if (n < NPE && cc < kc) v = (float)__ldg(A.Jm + ((size_t)(c % 3) * NPE + n) * nq + c / 3);
+                    bf16_split(v, Bh[n * AST + cc], Bl[n * AST + cc]);
+                }
+                __syncthreads();
+                // warp w: m-tile w of the chunk (16 rows), all n-tiles
+                const int mr = warp * 16;
+                for (int ks = 0; ks < kcp; ks += 16) {
+                    uint32_t ah[4], al[4];
+                    const int c0 = ks + tig * 2;
+                    ah[0] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid) * AST + c0);
+                    ah[1] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid + 8) * AST + c0);
+                    ah[2] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid) * AST + c0 + 8);
+                    ah[3] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid + 8) * AST + c0 + 8);
+                    al[0] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid) * AST + c0);
+                    al[1] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid + 8) * AST + c0);
+                    al[2] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid) * AST + c0 + 8);
+                    al[3] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid + 8) * AST + c0 + 8);
+#pragma unroll
+                    for (int t = 0; t < NT8; ++t) {
+                        uint32_t bh[2], bl[2];
+                        const int n = t * 8 + gid;
+                        bh[0] = *reinterpret_cast<const uint32_t *>(Bh + n * AST + c0);
+                        bh[1] = *reinterpret_cast<const uint32_t *>(Bh + n * AST + c0 + 8);
+                        bl[0] = *reinterpret_cast<const uint32_t *>(Bl + n * AST + c0);
+                        bl[1] = *reinterpret_cast<const uint32_t *>(Bl + n * AST + c0 + 8);
+                        mma_bf16(acc[t], al, bh);
+                        mma_bf16(acc[t], ah, bl);
+                        mma_bf16(acc[t], ah, bh);
+                    }
+                }
+            }
+            // scatter: C[r, a] = K_e[(a,i),(b,k)]
+#pragma unroll
+            for (int t = 0; t < NT8; ++t)
+#pragma unroll
+                for (int h = 0; h < 4; ++h) {
+                    const int r = m0 + warp * 16 + gid + (h >> 1) * 8, a = t * 8 + tig * 2 + (h & 1);
+                    if (r >= M || a >= NPE) continue;
+                    const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+                    const int ir = inv[3 * a + i], ic = inv[3 * b + k];
+                    const int64_t pos = ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
+                                            ? (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic] : -1;
+                    if (pos >= 0 && pos < s_nnz) atomicAdd(V32 + pos, acc[t][h]);
+                    else flag |= FL_FLAG_BAD_INDEX;
+                }
+        }
+    }
+    if (flag) atomicOr(&s_flag, flag);
+    __syncthreads();
+    if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
+}
+
+template <int NPE>
+static size_t mixed_smem_bytes(int nq) {
+    constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
+    return sizeof(double) * (size_t)nq * QSTRIDE + sizeof(__nv_bfloat16) * 2 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
+           sizeof(int) * (NPE + 3 * NPE);
+}
+
+template <int NPE, int MAT>
+static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
+    if (A.nelem == 0) return FL_OK;
+    const size_t smem = mixed_smem_bytes<NPE>(A.nq);
+    if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
+    { const int st = ensure_smem<contract_mixed_kernel<NPE>>(smem); if (st != FL_OK) return st; }
+    int64_t chunk = chunk_elements(CHUNK_BYTES, A.nq, 1);
+    if (chunk > A.nelem) chunk = A.nelem;
+    double *Q = nullptr;
+    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sizeof(double) * QSTRIDE * (size_t)A.nq * chunk, stream));
+    A.Q = Q;
+    A.ldq = chunk * A.nq;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    for (int64_t e0 = 0; e0 < A.nelem; e0 += chunk) {
+        A.e0 = e0;
+        A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
+        const int64_t nqp = A.ne * A.nq;
+        qp_kernel<NPE, MAT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        const int64_t grid = std::min<int64_t>(A.ne, (int64_t)sms * 8);
+        contract_mixed_kernel<NPE><<<(unsigned)grid, MX_NT, smem, stream>>>(A, V32);
+    }
+    const int st = launch_status();
+    const cudaError_t fe = cudaFreeAsync(Q, stream);
+    if (st != FL_OK) return st;
+    return fe == cudaSuccess ? FL_OK : FL_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------------------------------------
 // Allocation-free variant. Its Gauss-point scratch is this file-scope device array (every GPU that
 // loads the library holds it until the process exits). Host code cannot use the array's name as
 // a device address, so the address is looked up once per device with cudaGetSymbolAddress and
@@ -499,6 +701,62 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
                                   recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
                                   data_global_indices, mp, flags, scratch, FL_NOALLOC_SCRATCH_BYTES,
                                   (cudaStream_t)stream);
+}
+
+int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const uint64_t *elements,
+                              const double *Eulerx, const double *Jm, const double *AllGauss, int64_t ngauss,
+                              int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
+                              const int32_t *indptr, const int32_t *data_local_indices,
+                              const int32_t *data_global_indices, float *V_stiff, double *T, double mu, double mu1,
+                              double mu2, double lamb, int *flags, fl_stream_t stream) {
+    if (nelem < 0 || nnode <= 0 || ngauss <= 0 || ngauss > 343) return FL_ERR_ARG;
+    if (nelem == 0) return FL_OK;
+    if (!points || !elements || !Eulerx || !Jm || !AllGauss || !indptr || !data_local_indices ||
+        !data_global_indices || !V_stiff || !T)
+        return FL_ERR_ARG;
+    if (3 * nnode + 2 > INT32_MAX) return FL_ERR_UNSUPPORTED;
+    fl::AsmArgs A;
+    A.points = points;
+    A.elements = elements;
+    A.Eulerx = Eulerx;
+    A.Jm = Jm;
+    A.w = AllGauss;
+    A.nelem = nelem;
+    A.nnode = nnode;
+    A.nq = (int)ngauss;
+    A.update = requires_geometry_update ? 1 : 0;
+    A.mode = 1;
+    A.qc = 1;
+    A.I = A.J = nullptr;
+    A.V = nullptr;
+    A.T = T;
+    A.indptr = indptr;
+    A.indices = nullptr;
+    A.dl = data_local_indices;
+    A.dg = data_global_indices;
+    A.flags = flags;
+    A.Q = nullptr;
+    A.e0 = A.ne = A.ldq = 0;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (material_number == FL_MATERIAL_NEOHOOKEAN) {
+        A.mp = {mu, lamb, 0.0};
+        switch (nodeperelem) {
+#define FL_CASE(N) case N: return fl::launch_mixed<N, fl::NEOHOOKEAN>(A, V_stiff, s);
+            FL_CASE(4) FL_CASE(8) FL_CASE(10) FL_CASE(20) FL_CASE(27) FL_CASE(35) FL_CASE(64) FL_CASE(125)
+#undef FL_CASE
+            default: return FL_ERR_UNSUPPORTED;
+        }
+    }
+    if (material_number == FL_MATERIAL_MOONEYRIVLIN) {
+        A.mp = {mu1, mu2, lamb};
+        switch (nodeperelem) {
+#define FL_CASE(N) case N: return fl::launch_mixed<N, fl::MOONEYRIVLIN>(A, V_stiff, s);
+            FL_CASE(4) FL_CASE(8) FL_CASE(10) FL_CASE(20) FL_CASE(27) FL_CASE(35) FL_CASE(64) FL_CASE(125)
+#undef FL_CASE
+            default: return FL_ERR_UNSUPPORTED;
+        }
+    }
+    return FL_ERR_UNSUPPORTED;
 }
 
 const char *fl_status_string(int status) {

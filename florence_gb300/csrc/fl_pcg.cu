@@ -9,11 +9,14 @@
 // rows and columns replaced by the identity. This is CG on the reduced system K_ff, with the
 // matrix left as assembled.
 //
-// One iteration = four kernels:
-//   K1  q = K p (one warp per row, as many warps as rows), p.q
+// One iteration = three kernels:
+//   K1  q = K p, p.q
 //   K2  alpha = rz_k / p.q;  x += alpha p;  r -= alpha q;  z = B^-1 r;  r.z and r.r
 //   K3  beta = rz_{k+1} / rz_k;  p = z + beta p;  convergence test, done flag
-//   K4  clears the p.q slot for the next iteration
+// The product K p reads the matrix as 3x3 node blocks when the pattern has the structure every
+// assembled tangent has (the three rows of a node list the same nodes, 3 columns each): one warp
+// per node row, lanes over neighbour nodes, 9 values and one column index per block, so the
+// column indices of two of the three rows are never read. Other patterns use one warp per row.
 // Dot products are block-reduced and added into device scalar slots with one FP64 atomic per
 // block; the scalars never travel to the host inside the iteration (kernels read them from the
 // slots), and the host checks the done flag every PCG_CHECK iterations.
@@ -69,7 +72,8 @@ __device__ __forceinline__ void block_atomic_add(double v, double *out) {
 }
 
 // 3x3 diagonal block of node m, fixed rows/columns replaced by the identity, inverted.
-__global__ void __launch_bounds__(PCG_NT) bj_setup(const int32_t *indptr, const int32_t *indices, const double *vals,
+template <class VT>
+__global__ void __launch_bounds__(PCG_NT) bj_setup(const int32_t *indptr, const int32_t *indices, const VT *vals,
                                                    const int8_t *fixed, int64_t nnode, double *Binv, int *err) {
     for (int64_t m = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; m < nnode; m += (int64_t)gridDim.x * PCG_NT) {
         double B[9];
@@ -85,7 +89,7 @@ __global__ void __launch_bounds__(PCG_NT) bj_setup(const int32_t *indptr, const 
             for (int j = 0; j < 3; ++j) {
                 const int pos = lo + j;
                 double v = 0.0;
-                if (pos < indptr[row + 1] && indices[pos] == c0 + j) v = vals[pos];
+                if (pos < indptr[row + 1] && indices[pos] == c0 + j) v = (double)vals[pos];
                 else atomicOr(err, 1);  // diagonal block entry missing from the pattern
                 B[i * 3 + j] = v;
             }
@@ -104,7 +108,8 @@ __global__ void __launch_bounds__(PCG_NT) bj_setup(const int32_t *indptr, const 
 }
 
 // r = mask(b - K x), z = B^-1 r, p = z, partials of r.z (rz[0]) and |b|^2
-__global__ void __launch_bounds__(PCG_NT) pcg_init(const int32_t *indptr, const int32_t *indices, const double *vals,
+template <class VT>
+__global__ void __launch_bounds__(PCG_NT) pcg_init(const int32_t *indptr, const int32_t *indices, const VT *vals,
                                                    const int8_t *fixed, const double *b, const double *x, int64_t n,
                                                    PcgState s) {
     // (1) r = b - K x with one warp per row
@@ -114,7 +119,7 @@ __global__ void __launch_bounds__(PCG_NT) pcg_init(const int32_t *indptr, const 
     double bb = 0.0;
     for (int64_t row = warp; row < n; row += nwarps) {
         double acc = 0.0;
-        for (int k = indptr[row] + lane; k < indptr[row + 1]; k += 32) acc = fma(vals[k], x[indices[k]], acc);
+        for (int k = indptr[row] + lane; k < indptr[row + 1]; k += 32) acc = fma((double)vals[k], x[indices[k]], acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         if (lane == 0) {
@@ -143,12 +148,58 @@ __global__ void __launch_bounds__(PCG_NT) pcg_init2(int64_t nnode, PcgState s) {
     block_atomic_add(rz, s.acc + 1);
 }
 
+// y[3n+i] = sum over neighbour slots s of K[3n+i][3m+j] x[3m+j], m = indices[indptr[3n] + 3s] / 3,
+// reading V[indptr[3n+i] + 3s + j]; one warp per node, lane = slot. Returns the 3 sums in lane 0.
+template <class VT>
+__device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const VT *vals,
+                                               const double *x, int64_t node, int lane, double &y0, double &y1,
+                                               double &y2) {
+    const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
+    const int nb = (r1 - r0) / 3;
+    y0 = y1 = y2 = 0.0;
+    for (int sl = lane; sl < nb; sl += 32) {
+        const int m3 = indices[r0 + 3 * sl];
+        const double x0 = x[m3], x1 = x[m3 + 1], x2 = x[m3 + 2];
+        const VT *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
+        y0 = fma((double)v0[0], x0, fma((double)v0[1], x1, fma((double)v0[2], x2, y0)));
+        y1 = fma((double)v1[0], x0, fma((double)v1[1], x1, fma((double)v1[2], x2, y1)));
+        y2 = fma((double)v2[0], x0, fma((double)v2[1], x1, fma((double)v2[2], x2, y2)));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        y0 += __shfl_down_sync(0xffffffffu, y0, o);
+        y1 += __shfl_down_sync(0xffffffffu, y1, o);
+        y2 += __shfl_down_sync(0xffffffffu, y2, o);
+    }
+}
+
+// pattern check for the node-block product: rows 3n, 3n+1, 3n+2 hold the same columns, in runs
+// 3m, 3m+1, 3m+2 (one warp per node)
+__global__ void pcg_check_blocks(const int32_t *indptr, const int32_t *indices, int64_t nnode, int *bad) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t m = warp; m < nnode; m += nwarps) {
+        const int r0 = indptr[3 * m], r1 = indptr[3 * m + 1], r2 = indptr[3 * m + 2], r3 = indptr[3 * m + 3];
+        const int l0 = r1 - r0;
+        bool ok = (r2 - r1 == l0) && (r3 - r2 == l0) && (l0 % 3 == 0);
+        if (ok)
+            for (int t = lane; t < l0; t += 32) {
+                const int c = indices[r0 + t];
+                ok = ok && (indices[r1 + t] == c) && (indices[r2 + t] == c) && (c % 3 == t % 3) &&
+                     (t % 3 == 0 || indices[r0 + t - 1] == c - 1);
+            }
+        if (!ok) atomicOr(bad, 8);
+    }
+}
+
 // Dot products of the iteration are accumulated with one FP64 atomic add per block into scalar
 // slots: acc[0] = p.q, acc[1 + (k & 1)] = r.z of iterate k (double-buffered), acc[3] = r.r.
 // Each kernel zeroes the slot the next kernel accumulates into, after every reader is done.
 
-// K1: q = mask(K p) with one warp per row, p.q; zeroes r.z of iterate k+1 and r.r for K2
-__global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const int32_t *indices, const double *vals,
+// K1: q = mask(K p), p.q; zeroes r.z of iterate k+1 and r.r for K2
+template <class VT, bool NODEBLK>
+__global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const int32_t *indices, const VT *vals,
                                                  const int8_t *fixed, int64_t n, int k, PcgState s) {
     if (s.done[0]) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -159,16 +210,31 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
     const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
     double pq = 0.0;
-    for (int64_t row = warp; row < n; row += nwarps) {
-        double acc = 0.0;
-        const int end = indptr[row + 1];
-        for (int kk = indptr[row] + lane; kk < end; kk += 32) acc = fma(vals[kk], s.p[indices[kk]], acc);
+    if (NODEBLK) {
+        for (int64_t m = warp; m < n / 3; m += nwarps) {
+            double y0, y1, y2;
+            node_block_row(indptr, indices, vals, s.p, m, lane, y0, y1, y2);
+            if (lane == 0) {
+                const double q0 = fixed[3 * m] ? 0.0 : y0, q1 = fixed[3 * m + 1] ? 0.0 : y1,
+                             q2 = fixed[3 * m + 2] ? 0.0 : y2;
+                s.q[3 * m] = q0;
+                s.q[3 * m + 1] = q1;
+                s.q[3 * m + 2] = q2;
+                pq = fma(s.p[3 * m], q0, fma(s.p[3 * m + 1], q1, fma(s.p[3 * m + 2], q2, pq)));
+            }
+        }
+    } else {
+        for (int64_t row = warp; row < n; row += nwarps) {
+            double acc = 0.0;
+            const int end = indptr[row + 1];
+            for (int kk = indptr[row] + lane; kk < end; kk += 32) acc = fma((double)vals[kk], s.p[indices[kk]], acc);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (lane == 0) {
-            const double qv = fixed[row] ? 0.0 : acc;
-            s.q[row] = qv;
-            pq = fma(s.p[row], qv, pq);
+            for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+            if (lane == 0) {
+                const double qv = fixed[row] ? 0.0 : acc;
+                s.q[row] = qv;
+                pq = fma(s.p[row], qv, pq);
+            }
         }
     }
     block_atomic_add(pq, s.acc + 0);
@@ -210,6 +276,7 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, 
     for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT)
         s.p[d] = fma(beta, s.p[d], s.z[d]);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        s.acc[0] = 0.0;  // p.q of the next iterate (K2, the only reader, has finished)
         if (rr <= tol2) {
             s.done[0] = 1;
             s.done[1] = k + 1;
@@ -221,11 +288,6 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, 
     }
 }
 
-// zeroes p.q after every block of K3 has read the scalars of iterate k
-__global__ void pcg_k4(PcgState s) {
-    if (!s.done[0]) s.acc[0] = 0.0;
-}
-
 static int grid_blocks() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -233,7 +295,8 @@ static int grid_blocks() {
     return std::max(1, sms * 4);
 }
 
-static int bj_pcg(const int32_t *indptr, const int32_t *indices, const double *vals, int64_t n, const int8_t *fixed,
+template <class VT>
+static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals, int64_t n, const int8_t *fixed,
                   const double *b, double *x, double rtol, int64_t maxiter, void *ws, size_t ws_bytes,
                   int64_t *iters, double *relres, cudaStream_t st) {
     if (!indptr || !indices || !vals || !fixed || !b || !x || !iters || !relres || n <= 0 || n % 3) return FL_ERR_ARG;
@@ -242,12 +305,13 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const double *v
     PcgState s;
     pcg_layout(n, nb, &s, (char *)ws);
     const int64_t nnode = n / 3;
-    const unsigned g_rows = (unsigned)((n + (PCG_NT / 32) - 1) / (PCG_NT / 32));  // one warp per row
+    const unsigned g_rows = (unsigned)std::min<int64_t>((n + (PCG_NT / 32) - 1) / (PCG_NT / 32), 152 * 16);
     const unsigned g_nodes = (unsigned)std::min<int64_t>((nnode + PCG_NT - 1) / PCG_NT, 152 * 16);
     const unsigned g_dofs = (unsigned)std::min<int64_t>((n + PCG_NT - 1) / PCG_NT, 152 * 16);
     FL_CUDA_TRY(cudaMemsetAsync(s.done, 0, sizeof(int) * 4, st));
     FL_CUDA_TRY(cudaMemsetAsync(s.acc, 0, sizeof(double) * 8, st));
     bj_setup<<<g_nodes, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, nnode, s.Binv, s.done + 2);
+    pcg_check_blocks<<<g_rows, PCG_NT, 0, st>>>(indptr, indices, nnode, s.done + 2);
     pcg_init<<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, b, x, n, s);
     pcg_init2<<<g_nodes, PCG_NT, 0, st>>>(nnode, s);
     double hacc[8];
@@ -256,6 +320,9 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const double *v
     FL_CUDA_TRY(cudaMemcpyAsync(&err, s.done + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
     FL_CUDA_TRY(cudaStreamSynchronize(st));
     if (err & 3) return FL_ERR_ARG;  // pattern without diagonal blocks, or a singular block
+    const bool nodeblk = !(err & 8);
+    const unsigned g_k1 = nodeblk ? (unsigned)std::min<int64_t>((nnode + (PCG_NT / 32) - 1) / (PCG_NT / 32), 152 * 16)
+                                  : g_rows;
     const double b2 = hacc[4];
     if (b2 == 0.0) {  // zero right-hand side: x unchanged is the solution
         *iters = 0;
@@ -268,10 +335,10 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const double *v
     while (k < maxiter) {
         const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
         for (; k < kend; ++k) {
-            pcg_k1<<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
+            if (nodeblk) pcg_k1<VT, true><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
+            else pcg_k1<VT, false><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
             pcg_k2<<<g_nodes, PCG_NT, 0, st>>>(nnode, (int)k, x, s);
             pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, s);
-            pcg_k4<<<1, 1, 0, st>>>(s);
         }
         FL_CUDA_TRY(cudaGetLastError());
         FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
@@ -294,11 +361,17 @@ size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows) {
     return fl::pcg_layout(nrows, fl::grid_blocks(), nullptr, nullptr);
 }
 
-int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
-                      const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter, void *workspace,
-                      size_t workspace_bytes, int64_t *iterations, double *relres, fl_stream_t stream) {
-    return fl::bj_pcg(indptr, indices, values, nrows, fixed, b, x, rtol, maxiter, workspace, workspace_bytes,
-                      iterations, relres, (cudaStream_t)stream);
+int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const void *values, int value_bits,
+                      int64_t nrows, const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter,
+                      void *workspace, size_t workspace_bytes, int64_t *iterations, double *relres,
+                      fl_stream_t stream) {
+    if (value_bits == 64)
+        return fl::bj_pcg(indptr, indices, (const double *)values, nrows, fixed, b, x, rtol, maxiter, workspace,
+                          workspace_bytes, iterations, relres, (cudaStream_t)stream);
+    if (value_bits == 32)
+        return fl::bj_pcg(indptr, indices, (const float *)values, nrows, fixed, b, x, rtol, maxiter, workspace,
+                          workspace_bytes, iterations, relres, (cudaStream_t)stream);
+    return FL_ERR_ARG;
 }
 
 }  // extern "C"

@@ -10,7 +10,9 @@ and its failure flags (maximum iterations, NaN or relative residual above 1e6, :
 Differences by design: the Dirichlet dofs are masked instead of sliced out of the CSR matrix, and
 the linear step is the device FP64 block-Jacobi PCG (fl_BlockJacobiPCG) with an inexact-Newton
 forcing term, instead of a direct solver. Everything stays on the GPU; only scalars (norms,
-iteration counts) reach the host.
+iteration counts) reach the host. With tangent="mixed" the Jacobian is the tensor-core tangent
+in FP32 (fl_GlobalAssemblyDF_Mixed) while the residual, the convergence test and the PCG
+arithmetic stay FP64, so the converged state is that of the FP64 residual.
 """
 import ctypes
 import time
@@ -32,7 +34,8 @@ def pcg(asm, V, b, fixed, x=None, rtol=1e-8, maxiter=20000, workspace=None):
         workspace = torch.empty(L.fl_BlockJacobiPCG_workspace_size(n), dtype=torch.uint8, device=asm.device)
     it = ctypes.c_int64(0)
     rel = ctypes.c_double(0.0)
-    st = L.fl_BlockJacobiPCG(_ptr(asm.indptr), _ptr(asm.indices), _ptr(V), n, _ptr(fixed), _ptr(b), _ptr(x),
+    bits = 32 if V.dtype == torch.float32 else 64
+    st = L.fl_BlockJacobiPCG(_ptr(asm.indptr), _ptr(asm.indices), _ptr(V), bits, n, _ptr(fixed), _ptr(b), _ptr(x),
                              float(rtol), int(maxiter), _ptr(workspace), workspace.numel(), ctypes.byref(it),
                              ctypes.byref(rel), _stream())
     N.check(st, "fl_BlockJacobiPCG")
@@ -46,7 +49,7 @@ class NewtonSolver:
     """
 
     def __init__(self, asm, fixed, f_ext, n_increments=10, tol=1e-10, max_iter=25, pcg_maxiter=50000,
-                 eta_max=1e-2, eta_min=1e-12):
+                 eta_max=1e-2, eta_min=1e-12, tangent="fp64"):
         if asm.mode != "csr":
             raise ValueError("Newton needs the CSR tangent (mode='csr')")
         self.asm = asm
@@ -62,7 +65,10 @@ class NewtonSolver:
         self.eta_min = eta_min
         self.X = asm.points.reshape(-1)
         n = asm.nnode * 3
-        self.V = torch.zeros(asm.nnz, dtype=torch.float64, device=dev)
+        if tangent not in ("fp64", "mixed"):
+            raise ValueError("tangent must be 'fp64' or 'mixed'")
+        self.tangent = tangent
+        self.V = torch.zeros(asm.nnz, dtype=torch.float64 if tangent == "fp64" else torch.float32, device=dev)
         self.T = torch.zeros(n, dtype=torch.float64, device=dev)
         L = N.lib()
         self.ws = torch.empty(L.fl_BlockJacobiPCG_workspace_size(n), dtype=torch.uint8, device=dev)
@@ -71,7 +77,10 @@ class NewtonSolver:
     def _assemble(self, u):
         self.V.zero_()
         self.T.zero_()
-        self.asm.assemble((self.X + u).reshape(-1, 3), V=self.V, T=self.T)
+        if self.tangent == "fp64":
+            self.asm.assemble((self.X + u).reshape(-1, 3), V=self.V, T=self.T)
+        else:  # FP32 Jacobian from the tensor cores, FP64 residual
+            self.asm.assemble_mixed((self.X + u).reshape(-1, 3), V32=self.V, T=self.T)
 
     def solve(self, u0=None, guesses=None):
         """Runs all increments. guesses: optional callable(increment, u_prev) -> initial u for the

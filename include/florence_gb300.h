@@ -132,6 +132,23 @@ int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu1, mu2,
 int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS);
 
 /* ------------------------------------------------------------------------------------------
+ * Mixed-precision tangent for inexact Newton: the tangent of fl_GlobalAssemblyDF__<Mat>_ with its
+ * dense per-element contraction on the tensor cores (split-BF16, three products, FP32
+ * accumulation) written to FP32 CSR values V_stiff[nnz] (+=), and the residual T[nnode*3] (+=)
+ * in FP64 exactly as the FP64 entry points form it. Kinematics and the constitutive update stay
+ * FP64. No reference counterpart: the reference assembles only in FP64
+ * (_LowLevelAssemblyDF_.h:8-176); this is the Jacobian fl_BlockJacobiPCG applies with
+ * value_bits = 32. CSR through the reference's element-to-nonzero maps only.
+ * material_number: FL_MATERIAL_NEOHOOKEAN (mu, lamb) or FL_MATERIAL_MOONEYRIVLIN (mu1, mu2, lamb).
+ * ------------------------------------------------------------------------------------------ */
+int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const uint64_t *elements,
+                              const double *Eulerx, const double *Jm, const double *AllGauss, int64_t ngauss,
+                              int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
+                              const int32_t *indptr, const int32_t *data_local_indices,
+                              const int32_t *data_global_indices, float *V_stiff, double *T, double mu, double mu1,
+                              double mu2, double lamb, int *flags, fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
  * Explicit (matrix-free) internal force, T[nnode*nvar] += sum_e sum_g detJ (grad N_a . sigma).
  * Argument list of the reference's _GlobalAssemblyExplicit_DF_DPF_ plus flags and stream.
  * formulation_number must be 0 (mechanics), material_number FL_MATERIAL_NEOHOOKEAN (mu, lamb)
@@ -191,7 +208,9 @@ int fl_StrainEnergy(const double *points, const uint64_t *elements, const double
  * NewtonRaphson, Solver/FEMSolver.py:951-954: BoundaryCondition.GetReducedMatrices,
  * BoundaryCondition.py:842-857, and LinearSolver.Solve, Solver/LinearSolver.py:208-330).
  *   indptr/indices/values  CSR of K [nrows x nrows], nrows = 3 * nodes, every 3x3 diagonal block
- *                          present in the pattern (true for assembled tangents)
+ *                          present in the pattern (true for assembled tangents); values are FP64
+ *                          (value_bits 64) or FP32 (value_bits 32: an inexact-Newton Jacobian,
+ *                          read as FP32 and applied in FP64 arithmetic)
  *   fixed [nrows]          1 for Dirichlet dofs: their rows and columns are left out (masking)
  *   b [nrows]              right-hand side (fixed entries ignored)
  *   x [nrows]              in: initial guess with zero fixed entries; out: solution
@@ -201,8 +220,8 @@ int fl_StrainEnergy(const double *points, const uint64_t *elements, const double
  * singular diagonal block or a non-finite residual.
  * ------------------------------------------------------------------------------------------ */
 size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows);
-int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
-                      const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter,
+int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const void *values, int value_bits,
+                      int64_t nrows, const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter,
                       void *workspace, size_t workspace_bytes, int64_t *iterations, double *relres,
                       fl_stream_t stream);
 
