@@ -260,14 +260,11 @@ def run_ours(args):
         torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
-    ms = t0.elapsed_time(t1)
-    if world > 1:
-        tt = torch.tensor([ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms = float(tt.item())
+    from florence_gb300.replicas import job_throughput
+    rate, ms, _ = job_throughput(nelem * args.steps, t0.elapsed_time(t1), device=dev)
     kernel_ms = float(np.mean([a.elapsed_time(b) for a, b in kev]))
     clocks = clk.summary()
-    value = nelem * world * args.steps / (ms * 1e-3) / 1e6
+    value = rate / 1e6
 
     # roofline of the dominant kernel (assemble_df_kernel): FP64-pipe bound
     f_alg = flops_alg(npe, nq, W["material"]) * nelem
@@ -323,17 +320,18 @@ def run_newton(args):
     P, el, Jm, w, fixed, f = build_beam_problem(*cells, traction=0.01)
     asm = fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
     # warm-up: module loading, one assembly and one short linear solve
-    NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32).solve()
-    solver = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10)
+    NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32, tangent=args.tangent).solve()
+    solver = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10, tangent=args.tangent)
     out = solver.solve()
     u = out["u"].cpu().numpy().reshape(-1, 3)
     tip = np.abs(P[:, 0] - 4.0) < 1e-9
     incs = [dict(increment=i["increment"], newton=i["newton_iters"],
                  pcg=[h["pcg_iters"] for h in i["history"]], rel=[h["rel"] for h in i["history"]])
             for i in out["increments"]]
-    line = dict(metric="Newton wall time to rel-res 1e-10 (10 load increments, FP64 tangent, device PCG)",
+    line = dict(metric="Newton wall time to rel-res 1e-10 (10 load increments, %s tangent, device PCG)"
+                       % ("FP64" if args.tangent == "fp64" else "split-BF16 tensor-core FP32"),
                 value=out["wall_s"], unit="s", n_gpus=1, steps=1, warmup=1, higher_is_better=False,
-                scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                scaling="weak", vs_baseline=None, dtype="f64", data="synthetic", tangent=args.tangent,
                 config=dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice), Mooney-Rivlin mu1=mu2=0.5 "
                                      "lambda=20, x=0 clamped, traction (0,0,-0.01) on x=4" % cells,
                             nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
@@ -429,6 +427,7 @@ def main():
     ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")
     ap.add_argument("--explicit", action="store_true", help="explicit dynamics of the hex beam instead")
     ap.add_argument("--explicit-steps", type=int, default=10000)
+    ap.add_argument("--tangent", default="fp64", choices=["fp64", "mixed"], help="Newton Jacobian")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

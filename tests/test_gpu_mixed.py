@@ -52,7 +52,9 @@ def test_pcg_with_fp32_values_matches_fp64_values():
     x64, _, r64 = pcg(asm, V64, b, fx, rtol=1e-10)
     x32, _, r32 = pcg(asm, V32, b, fx, rtol=1e-10)
     assert r64 <= 1e-10 and r32 <= 1e-10
-    assert rel_fro(x32.cpu().numpy(), x64.cpu().numpy()) < 1e-5   # FP32 rounding of the matrix
+    # each solve is exact for its own matrix; the two matrices differ by FP32 rounding (~6e-8
+    # relative per entry), which the condition number (~1e4 here) amplifies in the solution
+    assert rel_fro(x32.cpu().numpy(), x64.cpu().numpy()) < 5e-3
 
 
 def test_newton_mixed_reaches_fp64_solution():
