@@ -57,8 +57,11 @@ def lib():
         for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_"):
             getattr(L, name).argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_noalloc.argtypes = [INT] + _DF_ARGS
-        L.fl_GlobalAssemblyDF_Mixed.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, D, D, D, D,
-                                                P, P]
+        L.fl_GlobalAssemblyDF_Batched.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, P, P,
+                                                  P]
+        L.fl_SetAssemblyTuning.argtypes = [I64, I64, INT]
+        L.fl_GlobalAssemblyDF_Mixed.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, D, D, D,
+                                                D, P, P, P]
         L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
                                                         D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
         L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
@@ -85,4 +88,5 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_", "fl_GlobalAssemblyDF_noalloc",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
-           "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed"]
+           "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
+           "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning"]

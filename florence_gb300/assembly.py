@@ -179,9 +179,9 @@ class DeviceAssembler:
 
     def assemble_mixed(self, Eulerx, V32=None, T=None, stream=None):
         """Inexact-Newton Jacobian: FP32 CSR values from the split-BF16 tensor-core contraction and
-        the FP64 residual (csr mode only). Accumulates into V32/T when given."""
-        if self.mode != "csr":
-            raise ValueError("the mixed tangent is assembled in csr mode")
+        the FP64 residual (csr or squeeze mode). Accumulates into V32/T when given."""
+        if self.mode not in ("csr", "squeeze"):
+            raise ValueError("the mixed tangent is assembled into the CSR pattern (csr or squeeze mode)")
         L = N.lib()
         x = Eulerx if Eulerx.is_contiguous() else Eulerx.contiguous()
         if V32 is None:
@@ -195,8 +195,9 @@ class DeviceAssembler:
             mu, mu1, mu2, lamb = 0.0, p0, p1, p2
         st = L.fl_GlobalAssemblyDF_Mixed(self.mat_id, _ptr(self.points), _ptr(self.elements), _ptr(x), _ptr(self.Jm),
                                          _ptr(self.w), self.nq, self.nelem, self.npe, self.nnode, self.update,
-                                         _ptr(self.indptr), _ptr(self.data_local), _ptr(self.data_global), _ptr(V32),
-                                         _ptr(T), mu, mu1, mu2, lamb, _ptr(self.flags), stream or _stream())
+                                         _ptr(self.indptr), _ptr(self.indices), _ptr(self.data_local),
+                                         _ptr(self.data_global), _ptr(V32), _ptr(T), mu, mu1, mu2, lamb, None,
+                                         _ptr(self.flags), stream or _stream())
         N.check(st, "fl_GlobalAssemblyDF_Mixed")
         return V32, T
 

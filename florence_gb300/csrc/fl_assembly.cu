@@ -58,6 +58,7 @@ struct AsmArgs {
     double *V, *T;
     const int32_t *indptr, *indices, *dl, *dg;
     MatParams mp;
+    const double *eparams;  // optional per-element material parameters [nelem][3] (overrides mp)
     int *flags;
     double *Q;       // scratch [QSTRIDE][ldq]
     int64_t e0, ne;  // element chunk [e0, e0+ne)
@@ -95,7 +96,9 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         double G[9], F[9];
         const double detJ = kinematics_fn<NPE>(jm, coords, __ldg(A.w + g), A.update, G, F);
         double sig[6], b[6], J, c1, c2, cbb;
-        material<MAT>(F, A.mp, sig, b, J, c1, c2, cbb);
+        MatParams mp = A.mp;
+        if (A.eparams) mp = MatParams{__ldg(A.eparams + e * 3), __ldg(A.eparams + e * 3 + 1), __ldg(A.eparams + e * 3 + 2)};
+        material<MAT>(F, mp, sig, b, J, c1, c2, cbb);
         if (!(J > 0.0)) flag |= FL_FLAG_NONPOSITIVE_J;
         // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G (indexed [d][e] or [i][d])
         double GG[9], GsG[9], sG[9], bG[9], GbG[9];
@@ -313,10 +316,25 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
     if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
 }
 
+// Tuning table: Gauss points per shared-memory chunk of the contraction kernel, per
+// (nodes per element, Gauss points), set by fl_SetAssemblyTuning (the autotuner); 0 = default.
+constexpr int TUNE_SLOTS = 64;
+struct TuneEntry { int npe, nq, qc; };
+static TuneEntry g_tune[TUNE_SLOTS];
+static std::mutex g_tune_mutex;
+
+static int tuned_qc(int npe, int nq) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    for (int i = 0; i < TUNE_SLOTS; ++i)
+        if (g_tune[i].npe == npe && g_tune[i].nq == nq) return g_tune[i].qc;
+    return 0;
+}
+
 template <int NPE>
 static int asm_qc(int nq) {
     constexpr int EPC = AsmCfg<NPE>::EPC;
-    int qc = 32768 / (EPC * NPE * 27 * 8);
+    int qc = tuned_qc(NPE, nq);
+    if (qc <= 0) qc = 32768 / (EPC * NPE * 27 * 8);
     if (qc < 1) qc = 1;
     if (qc > nq) qc = nq;
     return qc;
@@ -397,7 +415,8 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
                        int64_t requires_geometry_update, int32_t *I_stiff, int32_t *J_stiff, double *V_stiff,
                        double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
                        const int32_t *data_local_indices, const int32_t *data_global_indices, MatParams mp,
-                       int *flags, double *scratch, size_t scratch_bytes, cudaStream_t stream) {
+                       int *flags, double *scratch, size_t scratch_bytes, cudaStream_t stream,
+                       const double *eparams = nullptr) {
     if (ndim != 3 || nvar != 3 || H_VoigtSize != 6) return FL_ERR_ARG;
     if (nelem < 0 || nnode <= 0) return FL_ERR_ARG;
     if (ngauss <= 0 || ngauss > 343) return FL_ERR_UNSUPPORTED;
@@ -421,6 +440,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.T = T;
     A.indptr = A.indices = A.dl = A.dg = nullptr;
     A.mp = mp;
+    A.eparams = eparams;
     A.flags = flags;
     A.Q = nullptr;
     A.e0 = A.ne = A.ldq = 0;
@@ -453,18 +473,23 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
 //
 // Per element, K^T[(i,b,k), a] = sum_{(g,d)} U^T[(i,b,k),(g,d)] L[(g,d), a] with
 // U_g[(i,d),(b,k)] = sum_e Ahat_g[(i,d),(k,e)] Jm[e][b][g] (from the FP64 Gauss-point data, formed
-// in FP32) and L[(g,d), a] = Jm[d][a][g]. Both operands are split into BF16 pairs (hi = bf16(x),
-// lo = bf16(x - hi)) and multiplied as hi*hi + hi*lo + lo*hi with FP32 accumulation
-// (mma.sync m16n8k16 bf16): about 16 significant bits per operand, relative tangent error
-// ~1e-5. The result goes to FP32 CSR values (the Jacobian the FP64 PCG applies); the residual is
+// in FP32) and L[(g,d), a] = Jm[d][a][g]. Both operands are split into three BF16 terms
+// (x = hi + mid + lo, 24 significant bits together) and multiplied as the six products whose
+// order is at least 2^-16 (hi*hi, hi*mid, mid*hi, hi*lo, lo*hi, mid*mid) with FP32 accumulation
+// (mma.sync m16n8k16 bf16): the tangent to about FP32 accuracy (~1e-7 relative), enough for
+// Newton to keep its FP64 iteration count on ill-conditioned problems (a two-term split, ~1e-5,
+// slows Newton down). The result goes to FP32 CSR values (the Jacobian the PCG applies); the residual is
 // formed in FP64 exactly as in contract_kernel. Rows are processed in chunks of MX_MC and the
 // reduction dimension in chunks of MX_KC, so any element order fits in shared memory.
 // ------------------------------------------------------------------------------------------------
 constexpr int MX_NT = 128, MX_MC = 64, MX_KC = 96;
 
-__device__ __forceinline__ void bf16_split(float v, __nv_bfloat16 &hi, __nv_bfloat16 &lo) {
+// x = hi + mid + lo, three BF16 terms with 8 significant bits each (FP32's 24 bits)
+__device__ __forceinline__ void bf16_split3(float v, __nv_bfloat16 &hi, __nv_bfloat16 &mid, __nv_bfloat16 &lo) {
     hi = __float2bfloat16_rn(v);
-    lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+    const float r1 = v - __bfloat162float(hi);
+    mid = __float2bfloat16_rn(r1);
+    lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
 }
 
 __device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint32_t *b) {
@@ -482,10 +507,12 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
     const int nq = A.nq, K = 3 * nq;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     double *Qs = reinterpret_cast<double *>(smem_raw);                              // [nq][QSTRIDE]
-    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + (size_t)nq * QSTRIDE);  // [MX_MC][AST]
-    __nv_bfloat16 *Al = Ah + MX_MC * AST;
-    __nv_bfloat16 *Bh = Al + MX_MC * AST;                                            // [NP][AST]
-    __nv_bfloat16 *Bl = Bh + NP * AST;
+    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + (size_t)nq * QSTRIDE);  // [3][MX_MC][AST]
+    __nv_bfloat16 *Am = Ah + MX_MC * AST;
+    __nv_bfloat16 *Al = Am + MX_MC * AST;
+    __nv_bfloat16 *Bh = Al + MX_MC * AST;                                            // [3][NP][AST]
+    __nv_bfloat16 *Bm = Bh + NP * AST;
+    __nv_bfloat16 *Bl = Bm + NP * AST;
     int *nodes = reinterpret_cast<int *>(Bl + NP * AST);                             // [NPE]
     int *inv = nodes + NPE;                                                          // [NDOF]
     __shared__ int s_flag;
@@ -508,12 +535,13 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
             }
             nodes[a] = (int)nd;
         }
-        for (int i = tid; i < NDOF; i += MX_NT) {
-            const int v = A.dl[e * cap + (int64_t)i * NDOF];
-            const int p = v / NDOF;
-            if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
-            else inv[p] = i;
-        }
+        if (A.dl)
+            for (int i = tid; i < NDOF; i += MX_NT) {
+                const int v = A.dl[e * cap + (int64_t)i * NDOF];
+                const int p = v / NDOF;
+                if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
+                else inv[p] = i;
+            }
         const double *q = A.Q + el * nq;
         for (int idx = tid; idx < nq * QSTRIDE; idx += MX_NT) {
             const int k = idx / nq, g = idx % nq;
@@ -553,39 +581,46 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                                        fma(qq[sym9(I, k * 3 + 1)], __ldg(A.Jm + ((size_t)1 * NPE + b) * nq + g),
                                            qq[sym9(I, k * 3 + 2)] * __ldg(A.Jm + ((size_t)2 * NPE + b) * nq + g)));
                     }
-                    bf16_split(v, Ah[rr * AST + cc], Al[rr * AST + cc]);
+                    bf16_split3(v, Ah[rr * AST + cc], Am[rr * AST + cc], Al[rr * AST + cc]);
                 }
                 // B chunk, stored [n][k]: B[(g,d), a] = Jm[d][a][g]
                 for (int idx = tid; idx < NP * kcp; idx += MX_NT) {
                     const int n = idx / kcp, cc = idx % kcp, c = k0 + cc;
                     float v = 0.f;
                     if (n < NPE && cc < kc) v = (float)__ldg(A.Jm + ((size_t)(c % 3) * NPE + n) * nq + c / 3);
-                    bf16_split(v, Bh[n * AST + cc], Bl[n * AST + cc]);
+                    bf16_split3(v, Bh[n * AST + cc], Bm[n * AST + cc], Bl[n * AST + cc]);
                 }
                 __syncthreads();
                 // warp w: m-tile w of the chunk (16 rows), all n-tiles
                 const int mr = warp * 16;
                 for (int ks = 0; ks < kcp; ks += 16) {
-                    uint32_t ah[4], al[4];
+                    uint32_t ah[4], am[4], al[4];
                     const int c0 = ks + tig * 2;
-                    ah[0] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid) * AST + c0);
-                    ah[1] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid + 8) * AST + c0);
-                    ah[2] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid) * AST + c0 + 8);
-                    ah[3] = *reinterpret_cast<const uint32_t *>(Ah + (mr + gid + 8) * AST + c0 + 8);
-                    al[0] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid) * AST + c0);
-                    al[1] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid + 8) * AST + c0);
-                    al[2] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid) * AST + c0 + 8);
-                    al[3] = *reinterpret_cast<const uint32_t *>(Al + (mr + gid + 8) * AST + c0 + 8);
+                    auto ldA = [&](const __nv_bfloat16 *X, uint32_t *f) {
+                        f[0] = *reinterpret_cast<const uint32_t *>(X + (mr + gid) * AST + c0);
+                        f[1] = *reinterpret_cast<const uint32_t *>(X + (mr + gid + 8) * AST + c0);
+                        f[2] = *reinterpret_cast<const uint32_t *>(X + (mr + gid) * AST + c0 + 8);
+                        f[3] = *reinterpret_cast<const uint32_t *>(X + (mr + gid + 8) * AST + c0 + 8);
+                    };
+                    ldA(Ah, ah);
+                    ldA(Am, am);
+                    ldA(Al, al);
 #pragma unroll
                     for (int t = 0; t < NT8; ++t) {
-                        uint32_t bh[2], bl[2];
+                        uint32_t bh[2], bm[2], bl[2];
                         const int n = t * 8 + gid;
                         bh[0] = *reinterpret_cast<const uint32_t *>(Bh + n * AST + c0);
                         bh[1] = *reinterpret_cast<const uint32_t *>(Bh + n * AST + c0 + 8);
+                        bm[0] = *reinterpret_cast<const uint32_t *>(Bm + n * AST + c0);
+                        bm[1] = *reinterpret_cast<const uint32_t *>(Bm + n * AST + c0 + 8);
                         bl[0] = *reinterpret_cast<const uint32_t *>(Bl + n * AST + c0);
                         bl[1] = *reinterpret_cast<const uint32_t *>(Bl + n * AST + c0 + 8);
+                        // smallest terms first
+                        mma_bf16(acc[t], am, bm);
                         mma_bf16(acc[t], al, bh);
                         mma_bf16(acc[t], ah, bl);
+                        mma_bf16(acc[t], am, bh);
+                        mma_bf16(acc[t], ah, bm);
                         mma_bf16(acc[t], ah, bh);
                     }
                 }
@@ -598,9 +633,20 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                     const int r = m0 + warp * 16 + gid + (h >> 1) * 8, a = t * 8 + tig * 2 + (h & 1);
                     if (r >= M || a >= NPE) continue;
                     const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
-                    const int ir = inv[3 * a + i], ic = inv[3 * b + k];
-                    const int64_t pos = ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
-                                            ? (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic] : -1;
+                    int64_t pos = -1;
+                    if (A.dl) {
+                        const int ir = inv[3 * a + i], ic = inv[3 * b + k];
+                        if ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
+                            pos = (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic];
+                    } else {  // binary search of the column in the row
+                        const int grr = 3 * nodes[a] + i, gcc = 3 * nodes[b] + k;
+                        int lo = A.indptr[grr], hi = A.indptr[grr + 1];
+                        while (hi - lo > 1) {
+                            const int mid = lo + (hi - lo) / 2;
+                            if (gcc < A.indices[mid]) hi = mid; else lo = mid;
+                        }
+                        if (lo < A.indptr[grr + 1] && A.indices[lo] == gcc) pos = lo;
+                    }
                     if (pos >= 0 && pos < s_nnz) atomicAdd(V32 + pos, acc[t][h]);
                     else flag |= FL_FLAG_BAD_INDEX;
                 }
@@ -614,7 +660,7 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
 template <int NPE>
 static size_t mixed_smem_bytes(int nq) {
     constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
-    return sizeof(double) * (size_t)nq * QSTRIDE + sizeof(__nv_bfloat16) * 2 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
+    return sizeof(double) * (size_t)nq * QSTRIDE + sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
            sizeof(int) * (NPE + 3 * NPE);
 }
 
@@ -706,14 +752,15 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
 int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const uint64_t *elements,
                               const double *Eulerx, const double *Jm, const double *AllGauss, int64_t ngauss,
                               int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
-                              const int32_t *indptr, const int32_t *data_local_indices,
+                              const int32_t *indptr, const int32_t *indices, const int32_t *data_local_indices,
                               const int32_t *data_global_indices, float *V_stiff, double *T, double mu, double mu1,
-                              double mu2, double lamb, int *flags, fl_stream_t stream) {
+                              double mu2, double lamb, const double *element_params, int *flags,
+                              fl_stream_t stream) {
     if (nelem < 0 || nnode <= 0 || ngauss <= 0 || ngauss > 343) return FL_ERR_ARG;
     if (nelem == 0) return FL_OK;
-    if (!points || !elements || !Eulerx || !Jm || !AllGauss || !indptr || !data_local_indices ||
-        !data_global_indices || !V_stiff || !T)
-        return FL_ERR_ARG;
+    const bool maps = data_local_indices && data_global_indices;
+    if (!points || !elements || !Eulerx || !Jm || !AllGauss || !indptr || !V_stiff || !T) return FL_ERR_ARG;
+    if (!maps && !indices) return FL_ERR_ARG;
     if (3 * nnode + 2 > INT32_MAX) return FL_ERR_UNSUPPORTED;
     fl::AsmArgs A;
     A.points = points;
@@ -731,9 +778,10 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.V = nullptr;
     A.T = T;
     A.indptr = indptr;
-    A.indices = nullptr;
-    A.dl = data_local_indices;
-    A.dg = data_global_indices;
+    A.indices = indices;
+    A.dl = maps ? data_local_indices : nullptr;
+    A.dg = maps ? data_global_indices : nullptr;
+    A.eparams = element_params;
     A.flags = flags;
     A.Q = nullptr;
     A.e0 = A.ne = A.ldq = 0;
@@ -757,6 +805,39 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
         }
     }
     return FL_ERR_UNSUPPORTED;
+}
+
+int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const uint64_t *elements,
+                                const double *Eulerx, const double *Jm, const double *AllGauss, int64_t ngauss,
+                                int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
+                                const double *element_params, const int32_t *indptr, const int32_t *indices,
+                                const int32_t *data_local_indices, const int32_t *data_global_indices,
+                                double *V_stiff, double *T, int *flags, fl_stream_t stream) {
+    if (!element_params && nelem > 0) return FL_ERR_ARG;
+    const int squeeze = (data_local_indices == nullptr || data_global_indices == nullptr) ? 1 : 0;
+    const int mat = material_number == FL_MATERIAL_NEOHOOKEAN ? fl::NEOHOOKEAN
+                    : material_number == FL_MATERIAL_MOONEYRIVLIN ? fl::MOONEYRIVLIN : -1;
+    if (mat < 0) return FL_ERR_UNSUPPORTED;
+    return fl::global_assembly_df(mat, points, elements, Eulerx, Jm, AllGauss, 3, 3, ngauss, nelem, nodeperelem, nnode,
+                                  6, requires_geometry_update, const_cast<int32_t *>(indptr),
+                                  const_cast<int32_t *>(indices), V_stiff, T, 0, squeeze, data_local_indices,
+                                  data_global_indices, fl::MatParams{0, 0, 0}, flags, nullptr, 0, (cudaStream_t)stream,
+                                  element_params);
+}
+
+int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk) {
+    std::lock_guard<std::mutex> lock(fl::g_tune_mutex);
+    int freeslot = -1;
+    for (int i = 0; i < fl::TUNE_SLOTS; ++i) {
+        if (fl::g_tune[i].npe == nodeperelem && fl::g_tune[i].nq == ngauss) {
+            fl::g_tune[i].qc = gauss_chunk;
+            return FL_OK;
+        }
+        if (freeslot < 0 && fl::g_tune[i].npe == 0) freeslot = i;
+    }
+    if (freeslot < 0) return FL_ERR_CAPACITY;
+    fl::g_tune[freeslot] = fl::TuneEntry{(int)nodeperelem, (int)ngauss, gauss_chunk};
+    return FL_OK;
 }
 
 const char *fl_status_string(int status) {

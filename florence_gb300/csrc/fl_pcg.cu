@@ -32,6 +32,7 @@ constexpr int PCG_CHECK = 16;
 
 struct PcgState {
     double *r, *z, *p, *q, *Binv;  // vectors [n], block inverses [n/3][9]
+    float *ph, *pl;                // p as a float pair (p ~ ph + pl), for FP32-valued matrices
     double *acc;                   // [0] p.q, [1],[2] r.z of even/odd iterates, [3] r.r, [4] |b|^2
     int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
 };
@@ -49,10 +50,19 @@ static size_t pcg_layout(int64_t n, int nb, PcgState *s, char *base) {
     t.p = (double *)take(sizeof(double) * n);
     t.q = (double *)take(sizeof(double) * n);
     t.Binv = (double *)take(sizeof(double) * (n / 3) * 9);
+    t.ph = (float *)take(sizeof(float) * n);
+    t.pl = (float *)take(sizeof(float) * n);
     t.acc = (double *)take(sizeof(double) * 8);
     t.done = (int *)take(sizeof(int) * 4);
     if (s) *s = t;
     return off;
+}
+
+// p as a float pair
+__device__ __forceinline__ void split_store(const PcgState &s, int64_t d, double v) {
+    const float h = (float)v;
+    s.ph[d] = h;
+    s.pl[d] = (float)(v - (double)h);
 }
 
 // Block sum of one value per thread, added to *out with one atomic.
@@ -143,34 +153,95 @@ __global__ void __launch_bounds__(PCG_NT) pcg_init2(int64_t nnode, PcgState s) {
         s.z[3 * m] = s.p[3 * m] = z0;
         s.z[3 * m + 1] = s.p[3 * m + 1] = z1;
         s.z[3 * m + 2] = s.p[3 * m + 2] = z2;
+        split_store(s, 3 * m, z0);
+        split_store(s, 3 * m + 1, z1);
+        split_store(s, 3 * m + 2, z2);
         rz = fma(r0, z0, fma(r1, z1, fma(r2, z2, rz)));
     }
     block_atomic_add(rz, s.acc + 1);
 }
 
-// y[3n+i] = sum over neighbour slots s of K[3n+i][3m+j] x[3m+j], m = indices[indptr[3n] + 3s] / 3,
-// reading V[indptr[3n+i] + 3s + j]; one warp per node, lane = slot. Returns the 3 sums in lane 0.
-template <class VT>
-__device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const VT *vals,
-                                               const double *x, int64_t node, int lane, double &y0, double &y1,
-                                               double &y2) {
-    const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
-    const int nb = (r1 - r0) / 3;
+// Node-block product with 8 lanes per node (4 nodes per warp): lanes over neighbour slots s,
+// m = indices[indptr[3n] + 3s] / 3, values V[indptr[3n+i] + 3s + j]; the 8 partial sums are
+// combined with 3 shuffle steps. FP64 values: FP64 products. FP32 values: each product and sum
+// is carried as an unevaluated float pair (error-free product by FMA, compensated two-sum), with
+// p given as a float pair too, so the FP32 matrix is applied to ~2^-44 relative accuracy while
+// every operation runs on the FP32 pipe (GB300's FP64 rate would otherwise bound this loop).
+constexpr int NB_LANES = 8;
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// (s, c) += v * (ph + pl)
+__device__ __forceinline__ void df_mac(float v, float ph, float pl, float &s, float &c) {
+    const float prod = v * ph;
+    const float perr = fmaf(v, ph, -prod);
+    float t, e;
+    two_sum(s, prod, t, e);
+    s = t;
+    c += e + fmaf(v, pl, perr);
+}
+
+__device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const double *vals,
+                                               const PcgState &st, int64_t node, bool valid, int sub, double &y0,
+                                               double &y1, double &y2) {
     y0 = y1 = y2 = 0.0;
-    for (int sl = lane; sl < nb; sl += 32) {
-        const int m3 = indices[r0 + 3 * sl];
-        const double x0 = x[m3], x1 = x[m3 + 1], x2 = x[m3 + 2];
-        const VT *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
-        y0 = fma((double)v0[0], x0, fma((double)v0[1], x1, fma((double)v0[2], x2, y0)));
-        y1 = fma((double)v1[0], x0, fma((double)v1[1], x1, fma((double)v1[2], x2, y1)));
-        y2 = fma((double)v2[0], x0, fma((double)v2[1], x1, fma((double)v2[2], x2, y2)));
+    if (valid) {
+        const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
+        const int nb = (r1 - r0) / 3;
+        for (int sl = sub; sl < nb; sl += NB_LANES) {
+            const int m3 = indices[r0 + 3 * sl];
+            const double x0 = st.p[m3], x1 = st.p[m3 + 1], x2 = st.p[m3 + 2];
+            const double *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
+            y0 = fma(v0[0], x0, fma(v0[1], x1, fma(v0[2], x2, y0)));
+            y1 = fma(v1[0], x0, fma(v1[1], x1, fma(v1[2], x2, y1)));
+            y2 = fma(v2[0], x0, fma(v2[1], x1, fma(v2[2], x2, y2)));
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        y0 += __shfl_down_sync(0xffffffffu, y0, o);
-        y1 += __shfl_down_sync(0xffffffffu, y1, o);
-        y2 += __shfl_down_sync(0xffffffffu, y2, o);
+    for (int o = NB_LANES / 2; o > 0; o >>= 1) {
+        y0 += __shfl_down_sync(0xffffffffu, y0, o, NB_LANES);
+        y1 += __shfl_down_sync(0xffffffffu, y1, o, NB_LANES);
+        y2 += __shfl_down_sync(0xffffffffu, y2, o, NB_LANES);
     }
+}
+
+__device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const float *vals,
+                                               const PcgState &st, int64_t node, bool valid, int sub, double &y0,
+                                               double &y1, double &y2) {
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+    if (valid) {
+        const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
+        const int nb = (r1 - r0) / 3;
+        for (int sl = sub; sl < nb; sl += NB_LANES) {
+            const int m3 = indices[r0 + 3 * sl];
+            const float h0 = st.ph[m3], h1 = st.ph[m3 + 1], h2 = st.ph[m3 + 2];
+            const float l0 = st.pl[m3], l1 = st.pl[m3 + 1], l2 = st.pl[m3 + 2];
+            const float *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
+            df_mac(v0[0], h0, l0, s0, c0); df_mac(v0[1], h1, l1, s0, c0); df_mac(v0[2], h2, l2, s0, c0);
+            df_mac(v1[0], h0, l0, s1, c1); df_mac(v1[1], h1, l1, s1, c1); df_mac(v1[2], h2, l2, s1, c1);
+            df_mac(v2[0], h0, l0, s2, c2); df_mac(v2[1], h1, l1, s2, c2); df_mac(v2[2], h2, l2, s2, c2);
+        }
+    }
+#pragma unroll
+    for (int o = NB_LANES / 2; o > 0; o >>= 1) {
+        float t, e;
+        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB_LANES), t, e);
+        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB_LANES);
+        s0 = t;
+        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB_LANES), t, e);
+        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB_LANES);
+        s1 = t;
+        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB_LANES), t, e);
+        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB_LANES);
+        s2 = t;
+    }
+    y0 = (double)s0 + (double)c0;
+    y1 = (double)s1 + (double)c1;
+    y2 = (double)s2 + (double)c2;
 }
 
 // pattern check for the node-block product: rows 3n, 3n+1, 3n+2 hold the same columns, in runs
@@ -211,10 +282,13 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
     const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
     double pq = 0.0;
     if (NODEBLK) {
-        for (int64_t m = warp; m < n / 3; m += nwarps) {
+        const int grp = lane / NB_LANES, sub = lane % NB_LANES;
+        const int64_t nnode = n / 3;
+        for (int64_t base = warp * (32 / NB_LANES); base < nnode; base += nwarps * (32 / NB_LANES)) {
+            const int64_t m = base + grp;
             double y0, y1, y2;
-            node_block_row(indptr, indices, vals, s.p, m, lane, y0, y1, y2);
-            if (lane == 0) {
+            node_block_row(indptr, indices, vals, s, m, m < nnode, sub, y0, y1, y2);
+            if (sub == 0 && m < nnode) {
                 const double q0 = fixed[3 * m] ? 0.0 : y0, q1 = fixed[3 * m + 1] ? 0.0 : y1,
                              q2 = fixed[3 * m + 2] ? 0.0 : y2;
                 s.q[3 * m] = q0;
@@ -269,12 +343,15 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x
 }
 
 // K3: beta = rz_{k+1} / rz_k, p = z + beta p, convergence test; zeroes p.q for the next K1
-__global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, PcgState s) {
+__global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, int split, PcgState s) {
     if (s.done[0]) return;
     const double beta = s.acc[1 + ((k + 1) & 1)] / s.acc[1 + (k & 1)];
     const double rr = s.acc[3];
-    for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT)
-        s.p[d] = fma(beta, s.p[d], s.z[d]);
+    for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT) {
+        const double pv = fma(beta, s.p[d], s.z[d]);
+        s.p[d] = pv;
+        if (split) split_store(s, d, pv);
+    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         s.acc[0] = 0.0;  // p.q of the next iterate (K2, the only reader, has finished)
         if (rr <= tol2) {
@@ -321,7 +398,8 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     FL_CUDA_TRY(cudaStreamSynchronize(st));
     if (err & 3) return FL_ERR_ARG;  // pattern without diagonal blocks, or a singular block
     const bool nodeblk = !(err & 8);
-    const unsigned g_k1 = nodeblk ? (unsigned)std::min<int64_t>((nnode + (PCG_NT / 32) - 1) / (PCG_NT / 32), 152 * 16)
+    const unsigned g_k1 = nodeblk ? (unsigned)std::min<int64_t>((nnode + PCG_NT / NB_LANES - 1) / (PCG_NT / NB_LANES),
+                                                                152 * 16)
                                   : g_rows;
     const double b2 = hacc[4];
     if (b2 == 0.0) {  // zero right-hand side: x unchanged is the solution
@@ -338,7 +416,7 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
             if (nodeblk) pcg_k1<VT, true><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
             else pcg_k1<VT, false><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
             pcg_k2<<<g_nodes, PCG_NT, 0, st>>>(nnode, (int)k, x, s);
-            pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, s);
+            pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, sizeof(VT) == 4 ? 1 : 0, s);
         }
         FL_CUDA_TRY(cudaGetLastError());
         FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));

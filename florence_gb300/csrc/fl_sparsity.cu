@@ -155,20 +155,27 @@ __global__ void sp_fill_lists(const int64_t *el, int64_t n, int64_t npe, const i
     }
 }
 
-// CTA per node: sorted distinct neighbours in shared memory. Returns the count (all threads).
+constexpr int SP_NT = 128;
+
+// CTA per node: the nodes of its elements are bitonic-sorted in shared memory (a power-of-two
+// buffer sized for this node's own candidate count), first occurrences are flagged, and a block
+// scan of per-thread segment counts gives every distinct neighbour its rank. Returns the number
+// of distinct neighbours; if out != nullptr, writes the sorted distinct neighbours to out[rank].
 __device__ int node_neighbours(const int64_t *el, int64_t npe, const int32_t *start, const int32_t *list, int64_t n,
-                               int capc, int32_t *buf, int32_t *flagbuf) {
+                               int32_t *buf, int32_t *out) {
+    __shared__ int warp_tot[SP_NT / 32];
     const int s0 = start[n], deg = start[n + 1] - s0;
     const int m = deg * (int)npe;
-    for (int i = threadIdx.x; i < capc; i += blockDim.x) {
+    int capc = 32;
+    while (capc < m) capc <<= 1;
+    for (int i = threadIdx.x; i < capc; i += SP_NT) {
         if (i < m) buf[i] = (int32_t)el[(int64_t)list[s0 + i / (int)npe] * npe + i % (int)npe];
         else buf[i] = INT32_MAX;
     }
     __syncthreads();
-    // bitonic sort of capc (power of two) keys
     for (int k = 2; k <= capc; k <<= 1)
         for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < capc; i += blockDim.x) {
+            for (int i = threadIdx.x; i < capc; i += SP_NT) {
                 const int p = i ^ j;
                 if (p > i) {
                     const int32_t a = buf[i], b = buf[p];
@@ -181,49 +188,57 @@ __device__ int node_neighbours(const int64_t *el, int64_t npe, const int32_t *st
             }
             __syncthreads();
         }
-    // mark first occurrences, compact in order (prefix count over flags)
-    for (int i = threadIdx.x; i < capc; i += blockDim.x)
-        flagbuf[i] = (i < m && (i == 0 || buf[i] != buf[i - 1])) ? 1 : 0;
-    __syncthreads();
-    // inclusive scan of flags (Hillis-Steele over capc entries)
-    for (int o = 1; o < capc; o <<= 1) {
-        int32_t tv[SP_MAX_CAND / 128];
-        int c = 0;
-        for (int i = threadIdx.x; i < capc; i += blockDim.x) tv[c++] = i >= o ? flagbuf[i - o] : 0;
-        __syncthreads();
-        c = 0;
-        for (int i = threadIdx.x; i < capc; i += blockDim.x) flagbuf[i] += tv[c++];
-        __syncthreads();
+    // contiguous segment per thread; first occurrences among the m real keys
+    const int per = (m + SP_NT - 1) / SP_NT;
+    const int lo = threadIdx.x * per, hi = min(m, lo + per);
+    int c = 0;
+    for (int i = lo; i < hi; ++i) c += (i == 0 || buf[i] != buf[i - 1]);
+    // block exclusive scan of c
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
     }
-    const int count = m > 0 ? flagbuf[m - 1] : 0;
-    return count;
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    int base = 0, total = 0;
+    for (int w = 0; w < SP_NT / 32; ++w) {
+        if (w < wid) base += warp_tot[w];
+        total += warp_tot[w];
+    }
+    if (out) {
+        int r = base + incl - c;
+        for (int i = lo; i < hi; ++i)
+            if (i == 0 || buf[i] != buf[i - 1]) out[r++] = buf[i];
+    }
+    __syncthreads();  // buf and warp_tot are reused by the caller's next node
+    return total;
 }
 
-__global__ void sp_count_neighbours(const int64_t *el, int64_t npe, const int32_t *start, const int32_t *list,
-                                    int capc, int64_t *nbr) {
+__global__ void __launch_bounds__(SP_NT) sp_count_neighbours(const int64_t *el, int64_t npe, const int32_t *start,
+                                                             const int32_t *list, int64_t *nbr) {
     extern __shared__ int32_t sbuf[];
     const int64_t n = blockIdx.x;
-    const int count = node_neighbours(el, npe, start, list, n, capc, sbuf, sbuf + capc);
+    const int count = node_neighbours(el, npe, start, list, n, sbuf, nullptr);
     if (threadIdx.x == 0) nbr[n] = count;
 }
 
-__global__ void sp_write_rows(const int64_t *el, int64_t npe, const int32_t *start, const int32_t *list, int capc,
-                              const int64_t *off, int64_t nvar, int32_t *indptr, int32_t *indices) {
+__global__ void __launch_bounds__(SP_NT) sp_write_rows(const int64_t *el, int64_t npe, const int32_t *start,
+                                                       const int32_t *list, int capc, const int64_t *off, int64_t nvar,
+                                                       int32_t *indptr, int32_t *indices) {
     extern __shared__ int32_t sbuf[];
-    int32_t *buf = sbuf, *fl = sbuf + capc;
+    int32_t *buf = sbuf, *uniq = sbuf + capc;
     const int64_t n = blockIdx.x;
-    const int cnt = node_neighbours(el, npe, start, list, n, capc, buf, fl);
-    const int m = (start[n + 1] - start[n]) * (int)npe;
-    // compact distinct neighbours to buf[capc..]: position fl[i]-1 for first occurrences
-    // (reuse: write into the second half after reading; do it through registers per thread)
+    const int cnt = node_neighbours(el, npe, start, list, n, buf, uniq);
+    __syncthreads();
     const int64_t base = off[n] * nvar * nvar;
     const int64_t rowlen = (int64_t)cnt * nvar;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        if (i == 0 || buf[i] != buf[i - 1]) {
-            const int k = fl[i] - 1;
-            for (int64_t j = 0; j < nvar; ++j)
-                for (int64_t l = 0; l < nvar; ++l) indices[base + j * rowlen + (int64_t)k * nvar + l] = (int32_t)(nvar * buf[i] + l);
-        }
+    // row nvar*n+j: columns nvar*uniq[k]+l in order (k-major, then l)
+    for (int64_t t = threadIdx.x; t < nvar * rowlen; t += SP_NT) {
+        const int64_t j = t / rowlen, r = t % rowlen, k = r / nvar, l = r % nvar;
+        indices[base + j * rowlen + r] = (int32_t)(nvar * uniq[k] + l);
     }
     if (threadIdx.x < nvar) indptr[n * nvar + threadIdx.x] = (int32_t)(base + threadIdx.x * rowlen);
 }
@@ -295,15 +310,15 @@ static int compute_sparsity(const int64_t *elements, int64_t nelem, int64_t npe,
     if (hinfo[0] & 2) return FL_ERR_MESH;
     const int64_t maxcand = (int64_t)hinfo[1] * npe;
     if (maxcand > SP_MAX_CAND) return FL_ERR_UNSUPPORTED;
-    int capc = 128;
+    int capc = 32;
     while (capc < maxcand) capc <<= 1;
     sp_fill_lists<<<g1, 256, 0, s>>>(elements, n, npe, w.cnt, w.cursor, w.list);
-    const size_t shm = sizeof(int32_t) * 2 * capc;
+    const size_t shm = sizeof(int32_t) * 2 * capc;  // sort buffer + distinct neighbours
     if (shm > 48 * 1024) {
         FL_CUDA_TRY(cudaFuncSetAttribute(sp_count_neighbours, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
         FL_CUDA_TRY(cudaFuncSetAttribute(sp_write_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     }
-    sp_count_neighbours<<<(unsigned)nnode, 128, shm, s>>>(elements, npe, w.cnt, w.list, capc, w.nbr);
+    sp_count_neighbours<<<(unsigned)nnode, SP_NT, shm, s>>>(elements, npe, w.cnt, w.list, w.nbr);
     FL_CUDA_TRY(cudaMemsetAsync(w.nbr + nnode, 0, sizeof(int64_t), s));
     exclusive_scan<int64_t, int64_t>(w.nbr, w.nbr, nnode + 1, w.bsum, s);
     int64_t total_nodes_pairs = 0;
@@ -313,7 +328,7 @@ static int compute_sparsity(const int64_t *elements, int64_t nelem, int64_t npe,
     *nnz_out = nnz;
     if (nnz > INT32_MAX) return FL_ERR_UNSUPPORTED;
     if (!indices || cap_indices < nnz) return FL_ERR_CAPACITY;
-    sp_write_rows<<<(unsigned)nnode, 128, shm, s>>>(elements, npe, w.cnt, w.list, capc, w.nbr, nvar, indptr, indices);
+    sp_write_rows<<<(unsigned)nnode, SP_NT, shm, s>>>(elements, npe, w.cnt, w.list, capc, w.nbr, nvar, indptr, indices);
     sp_last_indptr<<<1, 1, 0, s>>>(indptr, nnode * nvar, w.nbr, nnode, nvar);
     if (dl) {
         const int ndof = (int)(npe * nvar);

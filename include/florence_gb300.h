@@ -138,15 +138,41 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
  * in FP64 exactly as the FP64 entry points form it. Kinematics and the constitutive update stay
  * FP64. No reference counterpart: the reference assembles only in FP64
  * (_LowLevelAssemblyDF_.h:8-176); this is the Jacobian fl_BlockJacobiPCG applies with
- * value_bits = 32. CSR through the reference's element-to-nonzero maps only.
- * material_number: FL_MATERIAL_NEOHOOKEAN (mu, lamb) or FL_MATERIAL_MOONEYRIVLIN (mu1, mu2, lamb).
+ * value_bits = 32. CSR through the reference's element-to-nonzero maps, or, with both map
+ * pointers NULL, by binary search in the rows of indptr/indices.
+ * material_number: FL_MATERIAL_NEOHOOKEAN (mu, lamb) or FL_MATERIAL_MOONEYRIVLIN (mu1, mu2, lamb);
+ * element_params [nelem][3] (optional) overrides them per element, as in fl_GlobalAssemblyDF_Batched.
  * ------------------------------------------------------------------------------------------ */
 int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const uint64_t *elements,
                               const double *Eulerx, const double *Jm, const double *AllGauss, int64_t ngauss,
                               int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
-                              const int32_t *indptr, const int32_t *data_local_indices,
+                              const int32_t *indptr, const int32_t *indices, const int32_t *data_local_indices,
                               const int32_t *data_global_indices, float *V_stiff, double *T, double mu, double mu1,
-                              double mu2, double lamb, int *flags, fl_stream_t stream);
+                              double mu2, double lamb, const double *element_params, int *flags,
+                              fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Batched assembly of many independent meshes: the caller concatenates the instances of one
+ * element type into one mesh with disjoint node ranges (the CSR tangent is then the direct sum of
+ * the instances' tangents) and gives every element its own material parameters,
+ * element_params[nelem][3] = (mu, lamb, 0) for FL_MATERIAL_NEOHOOKEAN or (mu1, mu2, lamb) for
+ * FL_MATERIAL_MOONEYRIVLIN. CSR values V_stiff[nnz] (+=) through the element-to-nonzero maps, or,
+ * with both map pointers NULL, by binary search in each row (no per-element maps: the memory of
+ * large batches); residual T (+=). No reference counterpart: the reference assembles one mesh per
+ * call (_LowLevelAssemblyDF_.h:8-176); its DetachedParallelFEMSolver
+ * (Solver/DetachedParallelFEMSolver.py:11-248) runs independent problems as separate processes.
+ * ------------------------------------------------------------------------------------------ */
+int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const uint64_t *elements,
+                                const double *Eulerx, const double *Jm, const double *AllGauss, int64_t ngauss,
+                                int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
+                                const double *element_params, const int32_t *indptr, const int32_t *indices,
+                                const int32_t *data_local_indices, const int32_t *data_global_indices,
+                                double *V_stiff, double *T, int *flags, fl_stream_t stream);
+
+/* Autotuner hook: Gauss points per shared-memory chunk of the FP64 contraction kernel for one
+ * (nodeperelem, ngauss) pair (0 restores the default). Applies to every later FP64 assembly call
+ * in the process. FL_ERR_CAPACITY when the table (64 pairs) is full. */
+int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
 
 /* ------------------------------------------------------------------------------------------
  * Explicit (matrix-free) internal force, T[nnode*nvar] += sum_e sum_g detJ (grad N_a . sigma).
