@@ -319,24 +319,38 @@ def run_newton(args):
     cells = (48, 12, 12) if args.workload != "beam_s" else (24, 6, 6)
     P, el, Jm, w, fixed, f = build_beam_problem(*cells, traction=0.01)
     asm = fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
-    # warm-up: module loading, one assembly and one short linear solve
-    NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32, tangent=args.tangent).solve()
-    solver = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10, tangent=args.tangent)
-    out = solver.solve()
+    tangents = ["fp64", "mixed"] if args.tangent == "both" else [args.tangent]
+    runs = {}
+    for tg in tangents:
+        # warm-up: module loading, one assembly and one short linear solve
+        NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32, tangent=tg, spmv=args.spmv).solve()
+        runs[tg] = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10, tangent=tg, spmv=args.spmv).solve()
+    out = runs[tangents[-1]]
+    extra = {}
+    if len(runs) == 2:
+        a, b = runs["fp64"], runs["mixed"]
+        extra = dict(fp64=dict(wall_s=a["wall_s"], newton_iters=a["newton_iters"], pcg_iters=a["pcg_iters"],
+                               failed=a["failed"]),
+                     mixed=dict(wall_s=b["wall_s"], newton_iters=b["newton_iters"], pcg_iters=b["pcg_iters"],
+                                failed=b["failed"]),
+                     mixed_vs_fp64_rel_l2=float(torch.linalg.vector_norm(b["u"] - a["u"]) /
+                                                torch.linalg.vector_norm(a["u"])))
     u = out["u"].cpu().numpy().reshape(-1, 3)
     tip = np.abs(P[:, 0] - 4.0) < 1e-9
     incs = [dict(increment=i["increment"], newton=i["newton_iters"],
                  pcg=[h["pcg_iters"] for h in i["history"]], rel=[h["rel"] for h in i["history"]])
             for i in out["increments"]]
     line = dict(metric="Newton wall time to rel-res 1e-10 (10 load increments, %s tangent, device PCG)"
-                       % ("FP64" if args.tangent == "fp64" else "split-BF16 tensor-core FP32"),
+                       % {"fp64": "FP64", "mixed": "split-BF16 tensor-core FP32",
+                          "both": "split-BF16 tensor-core FP32 (FP64 run alongside)"}[args.tangent],
                 value=out["wall_s"], unit="s", n_gpus=1, steps=1, warmup=1, higher_is_better=False,
                 scaling="weak", vs_baseline=None, dtype="f64", data="synthetic", tangent=args.tangent,
+                spmv=args.spmv if args.tangent != "mixed" else "fp32 values, float-pair product",
                 config=dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice), Mooney-Rivlin mu1=mu2=0.5 "
                                      "lambda=20, x=0 clamped, traction (0,0,-0.01) on x=4" % cells,
                             nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
                 newton_iters=out["newton_iters"], pcg_iters=out["pcg_iters"], failed=out["failed"],
-                tip_uz=float(u[tip, 2].mean()), increments=incs)
+                tip_uz=float(u[tip, 2].mean()), increments=incs, **extra)
     print(json.dumps(line), flush=True)
 
 
@@ -489,6 +503,47 @@ def e2e_dropin(W, asm, args):
                 path="florence_gb300._LowLevelAssemblyDF__%s_ (host numpy, pageable)" % mat)
 
 
+def run_warmstart(args):
+    """Learned warm start on the p=2 tet plate (about 20k tets, [0,2]x[0,1]x[0,0.2], x=0 clamped,
+    in-plane traction on x=2, neo-Hookean): training solves over sampled (mu, lambda/mu,
+    traction), a 64-mode POD basis of their converged increments, the network trained on the GPU,
+    then held-out solves from the previous-increment guess and from the network's guess."""
+    import torch
+    from florence_gb300 import warmstart as W
+    t0 = time.perf_counter()
+    prob = W.build_plate_problem()
+    solver = W.PlateSolver(prob, n_increments=args.ws_increments, tol=1e-10)
+    solver.solve(1.0, 10.0, 0.1)                          # warm-up: module loading, first assembly
+    train = W.sample_parameters(args.ws_train, seed=3)
+    test = W.sample_parameters(args.ws_test, seed=4)
+    t1 = time.perf_counter()
+    X, U, stats = W.generate_snapshots(solver, train)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    ws, hist, sv, proj = W.train_warm_start(X, U, modes=64, steps=args.ws_steps)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    rows, tot = W.evaluate_warm_start(solver, ws, test)
+    t4 = time.perf_counter()
+    line = dict(metric="Newton wall time to rel-res 1e-10 over the held-out solves, network warm start",
+                value=tot["warm"]["wall_s"], unit="s", n_gpus=1, steps=len(test), warmup=1,
+                higher_is_better=False, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(workload="p=2 tet plate 2x1x0.2 (38x19x4 jittered lattice), neo-Hookean mu~U(0.5,2) "
+                                     "lambda/mu~U(2,100), traction~U(0,0.5) (+x) on x=2, x=0 clamped, "
+                                     "%d increments, |R| <= 1e-10 |F|" % args.ws_increments,
+                            nelem=int(prob[1].shape[0]), nnode=int(prob[0].shape[0]), train_solves=len(train),
+                            test_solves=len(test), snapshots=int(U.shape[1]), pod_modes=64,
+                            network="3-256-256-64 GELU, BF16 operands, FP32 master, Adam"),
+                plain=tot["plain"], warm=tot["warm"], increments=tot["increments"],
+                newton_ratio=tot["warm"]["newton"] / max(1, tot["plain"]["newton"]),
+                wall_ratio=tot["warm"]["wall_s"] / max(1e-12, tot["plain"]["wall_s"]),
+                max_solution_diff=max(r["du"] for r in rows),
+                training=dict(failed=sum(s_["failed"] for s_ in stats), generate_s=t2 - t1, train_s=t3 - t2,
+                              evaluate_s=t4 - t3, loss_first=hist[0], loss_last=hist[-1], pod_projection_err=proj,
+                              sv_ratio_64=float(sv[-1] / sv[0])))
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -501,10 +556,18 @@ def main():
     ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")
     ap.add_argument("--explicit", action="store_true", help="explicit dynamics of the hex beam instead")
     ap.add_argument("--explicit-steps", type=int, default=10000)
-    ap.add_argument("--tangent", default="fp64", choices=["fp64", "mixed"], help="Newton Jacobian")
+    ap.add_argument("--tangent", default="fp64", choices=["fp64", "mixed", "both"],
+                    help="Newton Jacobian (both: FP64 then mixed, with the difference of the solutions)")
+    ap.add_argument("--spmv", default="split", choices=["split", "fp64"],
+                    help="PCG product for FP64 tangents: float-pair split on the FP32 pipe, or FP64")
     ap.add_argument("--batched", action="store_true", help="batched uneven instances instead")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-gb", type=float, default=40.0, help="CSR memory budget per sub-batch")
+    ap.add_argument("--warmstart", action="store_true", help="learned warm start on the plate instead")
+    ap.add_argument("--ws-train", type=int, default=2000, help="training solves")
+    ap.add_argument("--ws-test", type=int, default=200, help="held-out solves")
+    ap.add_argument("--ws-increments", type=int, default=5)
+    ap.add_argument("--ws-steps", type=int, default=20000, help="Adam steps of the network")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -516,6 +579,8 @@ def main():
         run_explicit(args)
     elif args.batched:
         run_batched(args)
+    elif args.warmstart:
+        run_warmstart(args)
     else:
         run_ours(args)
 

@@ -19,6 +19,9 @@ FL_FLAG_NONPOSITIVE_J = 1
 FL_FLAG_BAD_INDEX = 2
 FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
+FL_PCG_F64 = 64
+FL_PCG_F32 = 32
+FL_PCG_F64_SPLIT = 6432
 FL_NOALLOC_SCRATCH_BYTES = 32 << 20
 
 
@@ -70,7 +73,15 @@ def lib():
         L.fl_InternalForceF32.argtypes = [P, P, P, P, I64, I64, I64, I64, INT, D, D, P, P, P]
         L.fl_CentralDifferenceUpdate.argtypes = [I64, D, P, INT, P, P, P, P, P, P]
         L.fl_StrainEnergy.argtypes = [P, P, P, P, P, I64, I64, I64, I64, INT, D, D, P, P]
-        L.fl_BlockJacobiPCG_workspace_size.argtypes = [I64]
+        L.fl_MLP_num_params.argtypes = []
+        L.fl_MLP_num_params.restype = I64
+        L.fl_MLP_workspace_size.argtypes = [I64]
+        L.fl_MLP_workspace_size.restype = ctypes.c_size_t
+        L.fl_MLPForward.argtypes = [P, P, I64, P, P, ctypes.c_size_t, P]
+        L.fl_MLPGradients.argtypes = [P, P, P, I64, P, P, P, ctypes.c_size_t, P]
+        L.fl_MLPAdamStep.argtypes = [P, P, P, P, I64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                     P]
+        L.fl_BlockJacobiPCG_workspace_size.argtypes = [I64, I64, INT]
         L.fl_BlockJacobiPCG_workspace_size.restype = ctypes.c_size_t
         L.fl_BlockJacobiPCG.argtypes = [P, P, P, INT, I64, P, P, P, D, I64, P, ctypes.c_size_t,
                                         ctypes.POINTER(I64), ctypes.POINTER(D), P]
@@ -89,4 +100,5 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
-           "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning"]
+           "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_MLP_num_params", "fl_MLP_workspace_size",
+           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep"]

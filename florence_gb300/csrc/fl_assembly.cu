@@ -65,6 +65,32 @@ struct AsmArgs {
     int64_t ldq;     // leading dimension of Q (>= ne*nq)
 };
 
+// Position of `col` in CSR row `row` (sorted columns) relative to the row start, -1 if absent.
+__device__ __forceinline__ int row_search(const int32_t *indptr, const int32_t *indices, int row, int col) {
+    const int r0 = indptr[row], r1 = indptr[row + 1];
+    int lo = r0, hi = r1;
+    while (hi - lo > 1) {
+        const int mid = lo + (hi - lo) / 2;
+        if (col < indices[mid]) hi = mid; else lo = mid;
+    }
+    return (lo < r1 && indices[lo] == col) ? lo - r0 : -1;
+}
+
+// CSR position of dof entry (3*nr + ri, 3*nc + ci) given the offset `off` of column 3*nc in row
+// 3*nr (a node-block CSR: the three rows of a node share one column pattern, so the entry sits at
+// indptr[3*nr + ri] + off + ci). The position is verified against `indices`; when it does not
+// match (a CSR without node blocks) the row is searched. -1 if the entry is absent.
+__device__ __forceinline__ int64_t block_entry(const int32_t *indptr, const int32_t *indices, int nr, int nc, int ri,
+                                               int ci, int off) {
+    const int row = 3 * nr + ri, col = 3 * nc + ci;
+    if (off >= 0) {
+        const int p = indptr[row] + off + ci;
+        if (p < indptr[row + 1] && indices[p] == col) return p;
+    }
+    const int o = row_search(indptr, indices, row, col);
+    return o < 0 ? -1 : (int64_t)indptr[row] + o;
+}
+
 // index of (I,K), I,K in 0..8, in the packed upper triangle of a symmetric 9x9
 __device__ __forceinline__ int sym9(int I, int K) {
     const int r = I < K ? I : K, c = I < K ? K : I;
@@ -276,6 +302,22 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
                 if (ba[m] < 0) continue;
                 const int a = ba[m], b = bb[m];
                 const int na = nodes[slot * NPE + a], nb = nodes[slot * NPE + b];
+                if (A.mode == 2) {  // one row search per node block and mirror
+                    for (int mirror = 0; mirror < (a == b ? 1 : 2); ++mirror) {
+                        const int nr = mirror ? nb : na, nc = mirror ? na : nb;
+                        const int off = row_search(A.indptr, A.indices, 3 * nr, 3 * nc);
+#pragma unroll
+                        for (int ri = 0; ri < 3; ++ri)
+#pragma unroll
+                            for (int ci = 0; ci < 3; ++ci) {
+                                const double v = mirror ? acc[m][ci * 3 + ri] : acc[m][ri * 3 + ci];
+                                const int64_t pos = block_entry(A.indptr, A.indices, nr, nc, ri, ci, off);
+                                if (pos >= 0 && pos < s_nnz) atomicAdd(A.V + pos, v);
+                                else flag |= FL_FLAG_BAD_INDEX;
+                            }
+                    }
+                    continue;
+                }
 #pragma unroll
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -291,19 +333,11 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
                                 A.I[o] = grr;
                                 A.J[o] = gcc;
                                 A.V[o] = v;
-                            } else if (A.mode == 1) {
+                            } else {  // mode 1
                                 const int ir = inv[slot * NDOF + rr], ic = inv[slot * NDOF + cc];
                                 const int64_t pos = ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
                                                         ? (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic] : -1;
                                 if (pos >= 0 && pos < s_nnz) atomicAdd(A.V + pos, v);
-                                else flag |= FL_FLAG_BAD_INDEX;
-                            } else {
-                                int lo = A.indptr[grr], hi = A.indptr[grr + 1];
-                                while (hi - lo > 1) {
-                                    const int mid = lo + (hi - lo) / 2;
-                                    if (gcc < A.indices[mid]) hi = mid; else lo = mid;
-                                }
-                                if (lo < A.indptr[grr + 1] && A.indices[lo] == gcc) atomicAdd(A.V + lo, v);
                                 else flag |= FL_FLAG_BAD_INDEX;
                             }
                         }
@@ -515,6 +549,7 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
     __nv_bfloat16 *Bl = Bm + NP * AST;
     int *nodes = reinterpret_cast<int *>(Bl + NP * AST);                             // [NPE]
     int *inv = nodes + NPE;                                                          // [NDOF]
+    int16_t *boff = reinterpret_cast<int16_t *>(inv + NDOF);                         // [NPE][NPE]
     __shared__ int s_flag;
     __shared__ int64_t s_nnz;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
@@ -548,6 +583,11 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
             Qs[(size_t)g * QSTRIDE + k] = q[k * A.ldq + g];
         }
         __syncthreads();
+        if (!A.dl)  // offset of column node b in row node a; consecutive threads share a row
+            for (int idx = tid; idx < NPE * NPE; idx += MX_NT) {
+                const int off = row_search(A.indptr, A.indices, 3 * nodes[idx / NPE], 3 * nodes[idx % NPE]);
+                boff[idx] = (int16_t)(off >= 0 && off < 32768 ? off : -1);
+            }
         // residual in FP64
         if (A.update) {
             for (int r = tid; r < NDOF; r += MX_NT) {
@@ -638,14 +678,8 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                         const int ir = inv[3 * a + i], ic = inv[3 * b + k];
                         if ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
                             pos = (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic];
-                    } else {  // binary search of the column in the row
-                        const int grr = 3 * nodes[a] + i, gcc = 3 * nodes[b] + k;
-                        int lo = A.indptr[grr], hi = A.indptr[grr + 1];
-                        while (hi - lo > 1) {
-                            const int mid = lo + (hi - lo) / 2;
-                            if (gcc < A.indices[mid]) hi = mid; else lo = mid;
-                        }
-                        if (lo < A.indptr[grr + 1] && A.indices[lo] == gcc) pos = lo;
+                    } else {
+                        pos = block_entry(A.indptr, A.indices, nodes[a], nodes[b], i, k, boff[a * NPE + b]);
                     }
                     if (pos >= 0 && pos < s_nnz) atomicAdd(V32 + pos, acc[t][h]);
                     else flag |= FL_FLAG_BAD_INDEX;
@@ -661,7 +695,7 @@ template <int NPE>
 static size_t mixed_smem_bytes(int nq) {
     constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
     return sizeof(double) * (size_t)nq * QSTRIDE + sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
-           sizeof(int) * (NPE + 3 * NPE);
+           sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
 }
 
 template <int NPE, int MAT>

@@ -13,6 +13,10 @@
 //   K1  q = K p, p.q
 //   K2  alpha = rz_k / p.q;  x += alpha p;  r -= alpha q;  z = B^-1 r;  r.z and r.r
 //   K3  beta = rz_{k+1} / rz_k;  p = z + beta p;  convergence test, done flag
+// Matrix values: FP64 (FP64 products), FP32 (an inexact-Newton Jacobian) or FP64 split once per
+// solve into float pairs hi + lo in the workspace (FL_PCG_F64_SPLIT): the product then runs on
+// the FP32 pipe in float-pair arithmetic (~2^-44 relative), which GB300's FP64 rate (1/64 of its
+// FP32 rate) would otherwise bound.
 // The product K p reads the matrix as 3x3 node blocks when the pattern has the structure every
 // assembled tangent has (the three rows of a node list the same nodes, 3 columns each): one warp
 // per node row, lanes over neighbour nodes, 9 values and one column index per block, so the
@@ -37,7 +41,7 @@ struct PcgState {
     int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
 };
 
-static size_t pcg_layout(int64_t n, int nb, PcgState *s, char *base) {
+static size_t pcg_layout(int64_t n, int64_t nnz, PcgState *s, char *base, float2 **vsplit = nullptr) {
     size_t off = 0;
     auto take = [&](size_t bytes) {
         char *p = base ? base + off : nullptr;
@@ -54,6 +58,8 @@ static size_t pcg_layout(int64_t n, int nb, PcgState *s, char *base) {
     t.pl = (float *)take(sizeof(float) * n);
     t.acc = (double *)take(sizeof(double) * 8);
     t.done = (int *)take(sizeof(int) * 4);
+    float2 *vs = (float2 *)take(sizeof(float2) * (size_t)nnz);
+    if (vsplit) *vsplit = vs;
     if (s) *s = t;
     return off;
 }
@@ -244,6 +250,66 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
     y2 = (double)s2 + (double)c2;
 }
 
+// (s, c) += (vh + vl) * (ph + pl), dropping vl*pl (2^-48 relative)
+__device__ __forceinline__ void df_mac2(float2 v, float ph, float pl, float &s, float &c) {
+    const float prod = v.x * ph;
+    const float perr = fmaf(v.x, ph, -prod);
+    float t, e;
+    two_sum(s, prod, t, e);
+    s = t;
+    c += e + fmaf(v.x, pl, fmaf(v.y, ph, perr));
+}
+
+__device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const float2 *vals,
+                                               const PcgState &st, int64_t node, bool valid, int sub, double &y0,
+                                               double &y1, double &y2) {
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+    if (valid) {
+        const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
+        const int nb = (r1 - r0) / 3;
+        for (int sl = sub; sl < nb; sl += NB_LANES) {
+            const int m3 = indices[r0 + 3 * sl];
+            const float h0 = st.ph[m3], h1 = st.ph[m3 + 1], h2 = st.ph[m3 + 2];
+            const float l0 = st.pl[m3], l1 = st.pl[m3 + 1], l2 = st.pl[m3 + 2];
+            const float2 *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
+            df_mac2(v0[0], h0, l0, s0, c0); df_mac2(v0[1], h1, l1, s0, c0); df_mac2(v0[2], h2, l2, s0, c0);
+            df_mac2(v1[0], h0, l0, s1, c1); df_mac2(v1[1], h1, l1, s1, c1); df_mac2(v1[2], h2, l2, s1, c1);
+            df_mac2(v2[0], h0, l0, s2, c2); df_mac2(v2[1], h1, l1, s2, c2); df_mac2(v2[2], h2, l2, s2, c2);
+        }
+    }
+#pragma unroll
+    for (int o = NB_LANES / 2; o > 0; o >>= 1) {
+        float t, e;
+        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB_LANES), t, e);
+        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB_LANES);
+        s0 = t;
+        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB_LANES), t, e);
+        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB_LANES);
+        s1 = t;
+        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB_LANES), t, e);
+        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB_LANES);
+        s2 = t;
+    }
+    y0 = (double)s0 + (double)c0;
+    y1 = (double)s1 + (double)c1;
+    y2 = (double)s2 + (double)c2;
+}
+
+__device__ __forceinline__ double to_d(double v) { return v; }
+__device__ __forceinline__ double to_d(float v) { return (double)v; }
+__device__ __forceinline__ double to_d(float2 v) { return (double)v.x + (double)v.y; }
+
+// FP64 values -> float pairs hi + lo (hi = RN(v), lo = RN(v - hi)), nnz = indptr[n]
+__global__ void __launch_bounds__(PCG_NT) split_values(const int32_t *indptr, int64_t n, const double *v,
+                                                       float2 *out) {
+    const int64_t nnz = indptr[n];
+    for (int64_t i = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; i < nnz; i += (int64_t)gridDim.x * PCG_NT) {
+        const double x = v[i];
+        const float h = (float)x;
+        out[i] = make_float2(h, (float)(x - (double)h));
+    }
+}
+
 // pattern check for the node-block product: rows 3n, 3n+1, 3n+2 hold the same columns, in runs
 // 3m, 3m+1, 3m+2 (one warp per node)
 __global__ void pcg_check_blocks(const int32_t *indptr, const int32_t *indices, int64_t nnode, int *bad) {
@@ -301,7 +367,7 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
         for (int64_t row = warp; row < n; row += nwarps) {
             double acc = 0.0;
             const int end = indptr[row + 1];
-            for (int kk = indptr[row] + lane; kk < end; kk += 32) acc = fma((double)vals[kk], s.p[indices[kk]], acc);
+            for (int kk = indptr[row] + lane; kk < end; kk += 32) acc = fma(to_d(vals[kk]), s.p[indices[kk]], acc);
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
             if (lane == 0) {
@@ -365,22 +431,21 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, 
     }
 }
 
-static int grid_blocks() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return std::max(1, sms * 4);
-}
-
 template <class VT>
 static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals, int64_t n, const int8_t *fixed,
                   const double *b, double *x, double rtol, int64_t maxiter, void *ws, size_t ws_bytes,
-                  int64_t *iters, double *relres, cudaStream_t st) {
+                  int64_t *iters, double *relres, cudaStream_t st, bool split = false) {
     if (!indptr || !indices || !vals || !fixed || !b || !x || !iters || !relres || n <= 0 || n % 3) return FL_ERR_ARG;
-    const int nb = grid_blocks();
-    if (pcg_layout(n, nb, nullptr, nullptr) > ws_bytes || !ws) return FL_ERR_CAPACITY;
+    int32_t nnz32 = 0;  // the split copy is sized by the matrix
+    if (split) {
+        FL_CUDA_TRY(cudaMemcpyAsync(&nnz32, indptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        FL_CUDA_TRY(cudaStreamSynchronize(st));
+        if (nnz32 < 0) return FL_ERR_ARG;
+    }
+    if (pcg_layout(n, nnz32, nullptr, nullptr) > ws_bytes || !ws) return FL_ERR_CAPACITY;
     PcgState s;
-    pcg_layout(n, nb, &s, (char *)ws);
+    float2 *vsplit = nullptr;
+    pcg_layout(n, nnz32, &s, (char *)ws, &vsplit);
     const int64_t nnode = n / 3;
     const unsigned g_rows = (unsigned)std::min<int64_t>((n + (PCG_NT / 32) - 1) / (PCG_NT / 32), 152 * 16);
     const unsigned g_nodes = (unsigned)std::min<int64_t>((nnode + PCG_NT - 1) / PCG_NT, 152 * 16);
@@ -398,6 +463,8 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     FL_CUDA_TRY(cudaStreamSynchronize(st));
     if (err & 3) return FL_ERR_ARG;  // pattern without diagonal blocks, or a singular block
     const bool nodeblk = !(err & 8);
+    split = split && nodeblk;  // the float-pair product is the node-block one
+    if (split) split_values<<<g_dofs, PCG_NT, 0, st>>>(indptr, n, (const double *)vals, vsplit);
     const unsigned g_k1 = nodeblk ? (unsigned)std::min<int64_t>((nnode + PCG_NT / NB_LANES - 1) / (PCG_NT / NB_LANES),
                                                                 152 * 16)
                                   : g_rows;
@@ -413,10 +480,11 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     while (k < maxiter) {
         const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
         for (; k < kend; ++k) {
-            if (nodeblk) pcg_k1<VT, true><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
+            if (split) pcg_k1<float2, true><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vsplit, fixed, n, (int)k, s);
+            else if (nodeblk) pcg_k1<VT, true><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
             else pcg_k1<VT, false><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
             pcg_k2<<<g_nodes, PCG_NT, 0, st>>>(nnode, (int)k, x, s);
-            pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, sizeof(VT) == 4 ? 1 : 0, s);
+            pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, (sizeof(VT) == 4 || split) ? 1 : 0, s);
         }
         FL_CUDA_TRY(cudaGetLastError());
         FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
@@ -435,18 +503,18 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
 
 extern "C" {
 
-size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows) {
-    return fl::pcg_layout(nrows, fl::grid_blocks(), nullptr, nullptr);
+size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows, int64_t nnz, int value_bits) {
+    return fl::pcg_layout(nrows, value_bits == FL_PCG_F64_SPLIT ? nnz : 0, nullptr, nullptr);
 }
 
 int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const void *values, int value_bits,
                       int64_t nrows, const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter,
                       void *workspace, size_t workspace_bytes, int64_t *iterations, double *relres,
                       fl_stream_t stream) {
-    if (value_bits == 64)
+    if (value_bits == FL_PCG_F64 || value_bits == FL_PCG_F64_SPLIT)
         return fl::bj_pcg(indptr, indices, (const double *)values, nrows, fixed, b, x, rtol, maxiter, workspace,
-                          workspace_bytes, iterations, relres, (cudaStream_t)stream);
-    if (value_bits == 32)
+                          workspace_bytes, iterations, relres, (cudaStream_t)stream, value_bits == FL_PCG_F64_SPLIT);
+    if (value_bits == FL_PCG_F32)
         return fl::bj_pcg(indptr, indices, (const float *)values, nrows, fixed, b, x, rtol, maxiter, workspace,
                           workspace_bytes, iterations, relres, (cudaStream_t)stream);
     return FL_ERR_ARG;

@@ -24,17 +24,33 @@ from . import _native as N
 from .assembly import DeviceAssembler, _ptr, _stream
 
 
-def pcg(asm, V, b, fixed, x=None, rtol=1e-8, maxiter=20000, workspace=None):
+def pcg_value_mode(V, spmv="split"):
+    """fl_BlockJacobiPCG value mode of CSR values V: FP32 values -> FL_PCG_F32; FP64 values ->
+    FL_PCG_F64_SPLIT (float-pair product on the FP32 pipe, spmv="split") or FL_PCG_F64."""
+    if V.dtype == torch.float32:
+        return N.FL_PCG_F32
+    if spmv not in ("split", "fp64"):
+        raise ValueError("spmv must be 'split' or 'fp64'")
+    return N.FL_PCG_F64_SPLIT if spmv == "split" else N.FL_PCG_F64
+
+
+def pcg_workspace(asm, V, spmv="split"):
+    L = N.lib()
+    size = L.fl_BlockJacobiPCG_workspace_size(asm.nnode * 3, asm.nnz, pcg_value_mode(V, spmv))
+    return torch.empty(size, dtype=torch.uint8, device=asm.device)
+
+
+def pcg(asm, V, b, fixed, x=None, rtol=1e-8, maxiter=20000, workspace=None, spmv="split"):
     """Solves K_ff x = b_f with the CSR values V of `asm`'s pattern. Returns (x, iterations, relres)."""
     L = N.lib()
     n = asm.nnode * 3
     if x is None:
         x = torch.zeros(n, dtype=torch.float64, device=asm.device)
     if workspace is None:
-        workspace = torch.empty(L.fl_BlockJacobiPCG_workspace_size(n), dtype=torch.uint8, device=asm.device)
+        workspace = pcg_workspace(asm, V, spmv)
     it = ctypes.c_int64(0)
     rel = ctypes.c_double(0.0)
-    bits = 32 if V.dtype == torch.float32 else 64
+    bits = pcg_value_mode(V, spmv)
     st = L.fl_BlockJacobiPCG(_ptr(asm.indptr), _ptr(asm.indices), _ptr(V), bits, n, _ptr(fixed), _ptr(b), _ptr(x),
                              float(rtol), int(maxiter), _ptr(workspace), workspace.numel(), ctypes.byref(it),
                              ctypes.byref(rel), _stream())
@@ -49,7 +65,7 @@ class NewtonSolver:
     """
 
     def __init__(self, asm, fixed, f_ext, n_increments=10, tol=1e-10, max_iter=25, pcg_maxiter=50000,
-                 eta_max=1e-2, eta_min=1e-12, tangent="fp64"):
+                 eta_max=1e-2, eta_min=1e-12, tangent="fp64", criterion="reference", spmv="split"):
         if asm.mode != "csr":
             raise ValueError("Newton needs the CSR tangent (mode='csr')")
         self.asm = asm
@@ -68,10 +84,16 @@ class NewtonSolver:
         if tangent not in ("fp64", "mixed"):
             raise ValueError("tangent must be 'fp64' or 'mixed'")
         self.tangent = tangent
+        if criterion not in ("reference", "load"):
+            raise ValueError("criterion must be 'reference' or 'load'")
+        # "reference": |R| relative to its value after the first update of the increment (the
+        # reference's NormForces); "load": |R| relative to the increment's external load, a test
+        # that does not depend on how good the initial state was (used to compare warm starts)
+        self.criterion = criterion
         self.V = torch.zeros(asm.nnz, dtype=torch.float64 if tangent == "fp64" else torch.float32, device=dev)
         self.T = torch.zeros(n, dtype=torch.float64, device=dev)
-        L = N.lib()
-        self.ws = torch.empty(L.fl_BlockJacobiPCG_workspace_size(n), dtype=torch.uint8, device=dev)
+        self.spmv = spmv
+        self.ws = pcg_workspace(asm, self.V, spmv)
         self.history = []
 
     def _assemble(self, u):
@@ -82,9 +104,15 @@ class NewtonSolver:
         else:  # FP32 Jacobian from the tensor cores, FP64 residual
             self.asm.assemble_mixed((self.X + u).reshape(-1, 3), V32=self.V, T=self.T)
 
-    def solve(self, u0=None, guesses=None):
-        """Runs all increments. guesses: optional callable(increment, u_prev) -> initial u for the
-        increment (a warm start; the previous increment's solution otherwise). Returns a dict."""
+    def residual_norm(self, F):
+        return float(torch.linalg.vector_norm((self.T - F) * self.free))
+
+    def solve(self, u0=None, guesses=None, keep_states=False):
+        """Runs all increments. guesses: optional callable(increment, u_prev) -> candidate initial
+        u for the increment (a warm start) or None. The candidate is kept only if its FP64
+        residual is smaller than that of the previous increment's solution (the default start);
+        otherwise the solver falls back to the previous solution. keep_states: also return each
+        increment's converged displacement (device FP64) under increments[k]["u"]. Returns a dict."""
         dev = self.asm.device
         n = self.asm.nnode * 3
         u = torch.zeros(n, dtype=torch.float64, device=dev) if u0 is None else u0.clone()
@@ -96,12 +124,22 @@ class NewtonSolver:
         incs = []
         for inc in range(1, self.n_increments + 1):
             F = self.f_ext * (inc / self.n_increments)
+            guess = "previous"
             if guesses is not None:
                 g = guesses(inc, u)
                 if g is not None:
+                    r_prev = self.residual_norm(F)
+                    u_prev = u
                     u = g.clone()
                     self._assemble(u)
+                    if self.residual_norm(F) < r_prev:
+                        guess = "predicted"
+                    else:  # fallback: the prediction is worse than the previous increment
+                        u = u_prev
+                        self._assemble(u)
+                        guess = "fallback"
             R = (self.T - F) * self.free
+            norm_load = float(torch.linalg.vector_norm(F * self.free))
             norm_forces = None
             it = 0
             rel = np.inf
@@ -109,20 +147,22 @@ class NewtonSolver:
             iters = []
             while True:
                 du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
-                                     workspace=self.ws)
+                                     workspace=self.ws, spmv=self.spmv)
                 total_pcg += pits
                 u += du
                 self._assemble(u)
                 R = (self.T - F) * self.free
                 absn = float(torch.linalg.vector_norm(R))
-                if it == 0:
+                if self.criterion == "load":
+                    norm_forces = norm_load if norm_load != 0.0 else 1.0
+                elif it == 0:
                     norm_forces = absn if absn != 0.0 else 1e-14
                 rel = abs(absn / norm_forces)
                 iters.append(dict(iter=it, abs=absn, rel=rel, pcg_iters=pits, pcg_relres=prel, eta=eta))
                 if absn < self.tol:
                     break
                 it += 1
-                if rel <= self.tol and it > 0:
+                if rel <= self.tol and (it > 0 or self.criterion == "load"):
                     break
                 if it >= self.max_iter or not np.isfinite(rel) or rel > 1e6:
                     failed = True
@@ -130,7 +170,9 @@ class NewtonSolver:
                 # inexact Newton: solve to a tolerance proportional to the current relative residual
                 eta = float(min(self.eta_max, max(self.eta_min, 0.1 * rel)))
             total_newton += len(iters)
-            incs.append(dict(increment=inc, newton_iters=len(iters), history=iters))
+            incs.append(dict(increment=inc, newton_iters=len(iters), history=iters, guess=guess))
+            if keep_states:
+                incs[-1]["u"] = u.clone()
             if failed:
                 break
         torch.cuda.synchronize()

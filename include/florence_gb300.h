@@ -234,22 +234,51 @@ int fl_StrainEnergy(const double *points, const uint64_t *elements, const double
  * NewtonRaphson, Solver/FEMSolver.py:951-954: BoundaryCondition.GetReducedMatrices,
  * BoundaryCondition.py:842-857, and LinearSolver.Solve, Solver/LinearSolver.py:208-330).
  *   indptr/indices/values  CSR of K [nrows x nrows], nrows = 3 * nodes, every 3x3 diagonal block
- *                          present in the pattern (true for assembled tangents); values are FP64
- *                          (value_bits 64) or FP32 (value_bits 32: an inexact-Newton Jacobian,
- *                          read as FP32 and applied in FP64 arithmetic)
+ *                          present in the pattern (true for assembled tangents); value_bits:
+ *                          FL_PCG_F64        FP64 values, FP64 products
+ *                          FL_PCG_F64_SPLIT  FP64 values, split once per solve into float pairs
+ *                                            (hi + lo) in the workspace; products in float-pair
+ *                                            arithmetic on the FP32 pipe (~2^-44 relative)
+ *                          FL_PCG_F32        FP32 values (an inexact-Newton Jacobian), float-pair
+ *                                            products
+ *                          the vectors, dot products and the preconditioner are FP64 in all three
  *   fixed [nrows]          1 for Dirichlet dofs: their rows and columns are left out (masking)
  *   b [nrows]              right-hand side (fixed entries ignored)
  *   x [nrows]              in: initial guess with zero fixed entries; out: solution
  *   stop when |r| <= rtol |b| (free dofs) or after maxiter iterations; iterations and relres
- *   (host out) report where it stopped. workspace: fl_BlockJacobiPCG_workspace_size(nrows) bytes.
+ *   (host out) report where it stopped. workspace: fl_BlockJacobiPCG_workspace_size(nrows, nnz,
+ *   value_bits) bytes.
  * Synchronises the stream every 16 iterations to test convergence. FL_ERR_ARG on a missing or
  * singular diagonal block or a non-finite residual.
  * ------------------------------------------------------------------------------------------ */
-size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows);
+#define FL_PCG_F64 64
+#define FL_PCG_F32 32
+#define FL_PCG_F64_SPLIT 6432
+size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows, int64_t nnz, int value_bits);
 int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const void *values, int value_bits,
                       int64_t nrows, const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter,
                       void *workspace, size_t workspace_bytes, int64_t *iterations, double *relres,
                       fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Learned Newton warm start (no reference counterpart: the reference starts every increment
+ * from the previous one, Solver/FEMSolver.py:841-929). An MLP 3 -> 256 -> 256 -> 64 with GELU
+ * maps (load, material) parameters to the coefficients of the displacement in a 64-mode POD
+ * basis. BF16 arithmetic (GEMM operands rounded to BF16, FP32 accumulation), FP32 master
+ * parameters: params [fl_MLP_num_params()] = W1[3][256], b1[256], W2[256][256], b2[256],
+ * W3[256][64], b3[64] (row-major, y = x W + b). x [batch][3], y/target [batch][64], FP32.
+ * fl_MLPForward: y = net(x). fl_MLPGradients: grads [num_params] = dL/dparams and *loss (device,
+ * optional) = L for L = sum (y - target)^2 / (2 batch 64). fl_MLPAdamStep: Adam update of params
+ * (m, v [num_params] state, step >= 1). workspace: fl_MLP_workspace_size(batch) bytes.
+ * ------------------------------------------------------------------------------------------ */
+int64_t fl_MLP_num_params(void);
+size_t fl_MLP_workspace_size(int64_t batch);
+int fl_MLPForward(const float *params, const float *x, int64_t batch, float *y, void *workspace, size_t ws_bytes,
+                  fl_stream_t stream);
+int fl_MLPGradients(const float *params, const float *x, const float *target, int64_t batch, float *grads,
+                    float *loss, void *workspace, size_t ws_bytes, fl_stream_t stream);
+int fl_MLPAdamStep(float *params, const float *grads, float *m, float *v, int64_t step, float lr, float beta1,
+                   float beta2, float eps, fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
  * Measurement helper: device time of a dependent FP64 FMA loop over the whole GPU, used to

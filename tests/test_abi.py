@@ -46,3 +46,12 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     monkeypatch.setattr(_native, "LIB_PATH", str(tmp_path / "absent.so"))
     with pytest.raises(ImportError):
         _native.lib()
+
+
+def test_pcg_workspace_sizes():
+    """The split mode carries a float-pair copy of the values (8 bytes per nonzero)."""
+    from florence_gb300 import _native as N
+    L = N.lib()
+    base = L.fl_BlockJacobiPCG_workspace_size(3000, 100000, N.FL_PCG_F64)
+    assert L.fl_BlockJacobiPCG_workspace_size(3000, 100000, N.FL_PCG_F32) == base
+    assert L.fl_BlockJacobiPCG_workspace_size(3000, 100000, N.FL_PCG_F64_SPLIT) >= base + 8 * 100000

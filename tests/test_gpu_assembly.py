@@ -61,6 +61,46 @@ def test_csr_assembly_matches_reference(fl, case, mode):
     assert rel_fro(T.cpu().numpy(), d["T"]) < TOL
 
 
+def _padded_csr(indptr, indices, every=3, phase=1):
+    """The CSR pattern with one extra column in every `every`-th row (the smallest column absent
+    from the row): the rows of a node no longer share a column pattern. Returns the padded
+    (indptr, indices) and, per original entry, its position in the padded arrays."""
+    rows, pos, ptr = [], [], [0]
+    for r in range(len(indptr) - 1):
+        cols = list(indices[indptr[r]:indptr[r + 1]])
+        if r % every == phase:
+            c = next(c for c in range(len(cols) + 1) if c not in set(cols))
+            cols = sorted(cols + [c])
+        base = ptr[-1]
+        keep = set(indices[indptr[r]:indptr[r + 1]])
+        pos += [base + j for j, c in enumerate(cols) if c in keep]
+        rows += cols
+        ptr.append(len(rows))
+    return np.array(ptr, np.int32), np.array(rows, np.int32), np.array(pos)
+
+
+@pytest.mark.parametrize("case", ["hex_p2_nh_q5", "tet_p3_mr_jitter"])
+def test_row_search_scatter_without_node_blocks(fl, case):
+    """Squeeze-mode scatter into a CSR whose rows of one node differ: every entry still lands in
+    its column (the node-block shortcut is verified per entry and falls back to a row search),
+    the extra entries stay zero. FP64 and split-BF16 tangents."""
+    d = load_golden(case)
+    ptr, ind, pos = _padded_csr(d["K_indptr"], d["K_indices"])
+    asm = _asm(fl, d, "squeeze", sparsity=(ind, ptr, None, None))
+    x = torch.from_numpy(d["Eulerx"]).cuda()
+    V, T = asm.assemble(x)
+    asm.check_flags()
+    v = V.cpu().numpy()
+    assert rel_fro(v[pos], d["K_data"]) < TOL
+    extra = np.setdiff1d(np.arange(v.shape[0]), pos)
+    assert extra.size > 0 and np.all(v[extra] == 0.0)
+    V32, _ = asm.assemble_mixed(x)
+    asm.check_flags()
+    v32 = V32.double().cpu().numpy()
+    assert rel_fro(v32[pos], d["K_data"]) < 5e-6
+    assert np.all(v32[extra] == 0.0)
+
+
 @pytest.mark.parametrize("case", golden_cases())
 def test_triplets_and_element_matrices(fl, case):
     d = load_golden(case)

@@ -1,7 +1,7 @@
 """GPU tests of the mixed-precision (tensor-core, split-BF16) tangent used as an inexact-Newton
 Jacobian, and of Newton with it.
 
-Bars: the FP32 Jacobian within 2e-6 relative Frobenius of the FP64 tangent (three-term BF16
+Bars: the FP32 Jacobian within 5e-6 relative Frobenius of the FP64 tangent (three-term BF16
 split, six products, FP32 accumulation and FP32 storage); the residual, formed in FP64, within
 1e-12; Newton with the mixed Jacobian converges to the FP64 Newton's displacement within 1e-8
 relative.
@@ -25,7 +25,7 @@ def test_mixed_tangent_close_to_fp64(case):
     V32, T = asm.assemble_mixed(x)
     asm.check_flags()
     assert V32.dtype == torch.float32
-    assert rel_fro(V32.double().cpu().numpy(), d["K_data"]) < 2e-6
+    assert rel_fro(V32.double().cpu().numpy(), d["K_data"]) < 5e-6
     assert rel_fro(T.cpu().numpy(), d["T"]) < 1e-12
 
 
@@ -37,7 +37,7 @@ def test_mixed_tangent_on_config1_cube():
     x = torch.from_numpy(d["Eulerx"]).cuda()
     V64, T64 = asm.assemble(x)
     V32, T = asm.assemble_mixed(x)
-    assert rel_fro(V32.double().cpu().numpy(), V64.cpu().numpy()) < 2e-6
+    assert rel_fro(V32.double().cpu().numpy(), V64.cpu().numpy()) < 5e-6
     assert rel_fro(T.cpu().numpy(), T64.cpu().numpy()) < 1e-13
 
 

@@ -28,7 +28,9 @@ def _asm(P, el, Jm, w):
     return fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
 
 
-def test_pcg_matches_direct_solve(small_beam):
+@pytest.mark.parametrize("spmv", ["fp64", "split"])
+def test_pcg_matches_direct_solve(small_beam, spmv):
+    """Both FP64-valued products: FP64 arithmetic and the float-pair split on the FP32 pipe."""
     from florence_gb300.newton import pcg
     P, el, Jm, w, fixed, f = small_beam
     asm = _asm(P, el, Jm, w)
@@ -38,7 +40,7 @@ def test_pcg_matches_direct_solve(small_beam):
     b = rng.standard_normal(n)
     b[fixed] = 0.0
     x, its, rel = pcg(asm, V, torch.from_numpy(b).cuda(), torch.from_numpy(fixed.astype(np.int8)).cuda(),
-                      rtol=1e-12, maxiter=20000)
+                      rtol=1e-12, maxiter=20000, spmv=spmv)
     assert rel <= 1e-12 and its > 0
     K = sp.csr_matrix((V.cpu().numpy(), asm.indices.cpu().numpy(), asm.indptr.cpu().numpy()), shape=(n, n))
     free = ~fixed

@@ -99,3 +99,30 @@ def test_unreferenced_node_is_rejected(oracle):
     el = np.array([[0, 1, 2, 3]], np.int64)
     with pytest.raises(ValueError):
         oracle.sparsity(el, 5)
+
+
+def test_mlp_oracle_gradients_match_finite_differences():
+    """The network oracle's backward pass (without BF16 rounding) against central differences."""
+    from oracle import mlp_oracle as M
+    rng = np.random.default_rng(0)
+    n = sum(int(np.prod(s)) for s in M.SIZES)
+    p = rng.normal(0, 0.1, n)
+    x = rng.normal(0, 1, (5, 3))
+    t = rng.normal(0, 1, (5, 64))
+    g, _, _ = M.gradients(p, x, t, rounding=False)
+    idx = rng.choice(n, 40, replace=False)
+    for i in idx:
+        h = 1e-6
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (M.gradients(pp, x, t, rounding=False)[1] - M.gradients(pm, x, t, rounding=False)[1]) / (2 * h)
+        assert abs(fd - g[i]) <= 1e-6 * max(1.0, abs(g[i])) + 1e-9
+
+
+def test_mlp_oracle_bf16_rounding_matches_torch():
+    import torch
+    from oracle import mlp_oracle as M
+    x = np.random.default_rng(1).normal(0, 3, 10000).astype(np.float32)
+    ref = torch.from_numpy(x).to(torch.bfloat16).double().numpy()
+    assert np.array_equal(M._bf16(x), ref)
