@@ -91,6 +91,23 @@ def flops_executed(npe, nq, material):
     return nq * (27 * npe * (npe + 1) + 216 * npe + (800 if material == "NeoHookean" else 1200))
 
 
+EPC = {4: 8, 8: 8, 10: 4, 20: 2, 27: 1, 35: 1, 64: 1, 125: 1}   # elements per CTA of the contraction
+
+
+def assembly_launches(nelem, npe, nq):
+    """Kernels one assembly call launches: (Gauss-point kernel + contraction) per chunk of the
+    64 MiB Gauss-point scratch (54 doubles per Gauss point)."""
+    ce = (64 << 20) // (8 * 54 * nq)
+    ce -= ce % EPC[npe]
+    return 2 * ((nelem + ce - 1) // ce)
+
+
+def pair_macs(npe, nq):
+    """Multiply-adds of the contraction per element (stiffness node blocks a <= b and the U
+    build), each 12 FP32-pipe instructions in the float-pair arithmetic."""
+    return nq * (27 * npe * (npe + 1) // 2 + 81 * npe)
+
+
 def bytes_min(nnode, nelem, npe, nnz):
     """Compulsory HBM bytes of one assembly: X and x read, connectivity (int32 equivalent), CSR
     values written once, residual written."""
@@ -241,11 +258,13 @@ def run_ours(args):
         if ev is not None:
             ev[1].record(stream)
 
+    fl.set_arithmetic(args.arith)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
     asm.check_flags("bench warm-up")
     fp64_peak = fl.fp64_peak_gflops() / 1e3  # TFLOP/s, measured in this run
+    fp32_peak = fl.fp32_peak_gflops() / 1e3
     kev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
@@ -272,12 +291,22 @@ def run_ours(args):
     achieved = f_alg / (kernel_ms * 1e-3) / 1e12
     bmin = bytes_min(nnode, nelem, npe, asm.nnz)
     hbm_peak = json.load(open(PEAKS))["hbm_gbs"] if os.path.exists(PEAKS) else 6800.0
-    tag = "assemble_df_%s_%s" % (W["desc"]["element"], W["desc"]["material"])
-    roofline = dict(bound="fp64", achieved=achieved, peak=fp64_peak, unit="TFLOP/s", frac=achieved / fp64_peak,
-                    traffic=traffic_from_profile(tag),
-                    peak_source="FP64 FMA microkernel measured in this run (no FP64 figure in MEASURED_PEAKS.json)",
-                    flop_alg_per_launch=f_alg, flop_executed_per_launch=f_exe,
-                    executed_frac=f_exe / (kernel_ms * 1e-3) / 1e12 / fp64_peak,
+    if args.arith == "fp64":
+        roofline = dict(bound="fp64", achieved=achieved, peak=fp64_peak, unit="TFLOP/s", frac=achieved / fp64_peak,
+                        peak_source="FP64 FMA microkernel measured in this run (no FP64 figure in "
+                                    "MEASURED_PEAKS.json)",
+                        executed_frac=f_exe / (kernel_ms * 1e-3) / 1e12 / fp64_peak)
+    else:  # the contraction runs as float pairs on the FP32 pipe
+        instr = 12.0 * pair_macs(npe, nq) * nelem
+        ach_i = instr / (kernel_ms * 1e-3) / 1e12
+        roofline = dict(bound="fp32", achieved=ach_i, peak=fp32_peak / 2, unit="T FP32-pipe instr/s",
+                        frac=ach_i / (fp32_peak / 2),
+                        peak_source="FP32 FMA microkernel measured in this run (instructions/s = FLOP/s / 2)",
+                        fp64_equivalent_tflops=achieved, fp64_equivalent_frac=achieved / fp64_peak,
+                        instr_per_launch=instr)
+    tag = "assemble_df_%s_%s%s" % (W["desc"]["element"], W["desc"]["material"],
+                                   "" if args.arith == "fp64" else "_float_pair")
+    roofline.update(traffic=traffic_from_profile(tag), flop_alg_per_launch=f_alg, flop_executed_per_launch=f_exe,
                     kernel_ms=kernel_ms,
                     hbm=dict(bytes_min_per_launch=bmin, achieved_gbs=bmin / (kernel_ms * 1e-3) / 1e9,
                              peak_gbs=hbm_peak, frac=bmin / (kernel_ms * 1e-3) / 1e9 / hbm_peak,
@@ -297,6 +326,7 @@ def run_ours(args):
 
     if rank == 0:
         line = dict(metric="FP64 assembly throughput (tangent CSR + residual)", value=value, unit="Melem/s",
+                    arithmetic=args.arith,
                     n_gpus=world, steps=args.steps, warmup=args.warmup, ms_per_step=ms / args.steps,
                     higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
                     config=dict(W["desc"], nelem=int(nelem), nnode=int(nnode), nnz=int(asm.nnz), gauss_points=nq,
@@ -304,7 +334,7 @@ def run_ours(args):
                                 l2="inputs larger than L2: CSR values %.0f MB and element-to-nonzero map %.0f MB "
                                    "per step" % (asm.nnz * 8 / 1e6, asm.data_global.numel() * 4 / 1e6)),
                     roofline=roofline, cpu_baseline=cpu, e2e=e2e, clocks=clocks,
-                    gpu_launches=args.steps)
+                    gpu_launches=args.steps * assembly_launches(nelem, npe, nq))
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -324,7 +354,8 @@ def run_newton(args):
     for tg in tangents:
         # warm-up: module loading, one assembly and one short linear solve
         NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32, tangent=tg, spmv=args.spmv).solve()
-        runs[tg] = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10, tangent=tg, spmv=args.spmv).solve()
+        runs[tg] = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10, tangent=tg, spmv=args.spmv,
+                                max_iter=args.newton_max_iter, forcing=args.forcing).solve()
     out = runs[tangents[-1]]
     extra = {}
     if len(runs) == 2:
@@ -346,6 +377,7 @@ def run_newton(args):
                 value=out["wall_s"], unit="s", n_gpus=1, steps=1, warmup=1, higher_is_better=False,
                 scaling="weak", vs_baseline=None, dtype="f64", data="synthetic", tangent=args.tangent,
                 spmv=args.spmv if args.tangent != "mixed" else "fp32 values, float-pair product",
+                forcing=args.forcing,
                 config=dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice), Mooney-Rivlin mu1=mu2=0.5 "
                                      "lambda=20, x=0 clamped, traction (0,0,-0.01) on x=4" % cells,
                             nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
@@ -551,6 +583,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
+    ap.add_argument("--arith", default="fp64", choices=["fp64", "float_pair"],
+                    help="arithmetic of the stiffness contraction (FP64, or float pairs on the FP32 pipe)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")
@@ -558,6 +592,10 @@ def main():
     ap.add_argument("--explicit-steps", type=int, default=10000)
     ap.add_argument("--tangent", default="fp64", choices=["fp64", "mixed", "both"],
                     help="Newton Jacobian (both: FP64 then mixed, with the difference of the solutions)")
+    ap.add_argument("--newton-max-iter", type=int, default=25,
+                    help="Newton iterations per increment before failing (small values give a short profile run)")
+    ap.add_argument("--forcing", default="ew", choices=["ew", "rel"],
+                    help="PCG tolerance per Newton step: Eisenstat-Walker, or 0.1 x relative residual")
     ap.add_argument("--spmv", default="split", choices=["split", "fp64"],
                     help="PCG product for FP64 tangents: float-pair split on the FP32 pipe, or FP64")
     ap.add_argument("--batched", action="store_true", help="batched uneven instances instead")

@@ -9,8 +9,10 @@ the CPU.
 from . import _native
 from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssemblyDF__MooneyRivlin_,
                        _LowLevelAssemblyDF__NeoHookean_, _LowLevelAssemblyExplicit_DF_DPF_,
-                       __TotalConstantMassIntegrand__, device_sparsity, fp64_peak_gflops, install, material_params)
+                       __TotalConstantMassIntegrand__, arithmetic, device_sparsity, fp32_peak_gflops, fp64_peak_gflops,
+                       get_arithmetic, install, material_params, set_arithmetic)
 
 __all__ = ["ComputeSparsityPattern", "DeviceAssembler", "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
-           "__TotalConstantMassIntegrand__", "device_sparsity", "fp64_peak_gflops", "install", "material_params"]
+           "__TotalConstantMassIntegrand__", "arithmetic", "device_sparsity", "fp32_peak_gflops", "fp64_peak_gflops", "get_arithmetic",
+           "install", "material_params", "set_arithmetic"]

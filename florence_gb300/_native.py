@@ -19,6 +19,8 @@ FL_FLAG_NONPOSITIVE_J = 1
 FL_FLAG_BAD_INDEX = 2
 FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
+FL_ARITH_FP64 = 0
+FL_ARITH_FLOAT_PAIR = 1
 FL_PCG_F64 = 64
 FL_PCG_F32 = 32
 FL_PCG_F64_SPLIT = 6432
@@ -63,12 +65,15 @@ def lib():
         L.fl_GlobalAssemblyDF_Batched.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, P, P,
                                                   P]
         L.fl_SetAssemblyTuning.argtypes = [I64, I64, INT]
+        L.fl_SetAssemblyArithmetic.argtypes = [INT]
+        L.fl_GetAssemblyArithmetic.argtypes = []
         L.fl_GlobalAssemblyDF_Mixed.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, D, D, D,
                                                 D, P, P, P]
         L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
                                                         D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
         L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
         L.fl_measure_fp64_peak.argtypes = [ctypes.POINTER(D), P]
+        L.fl_measure_fp32_peak.argtypes = [ctypes.POINTER(D), P]
         L.fl_ReferenceGradients.argtypes = [P, P, P, P, I64, I64, I64, I64, P, P, P, P]
         L.fl_InternalForceF32.argtypes = [P, P, P, P, I64, I64, I64, I64, INT, D, D, P, P, P]
         L.fl_CentralDifferenceUpdate.argtypes = [I64, D, P, INT, P, P, P, P, P, P]
@@ -97,8 +102,8 @@ def check(status, what=""):
 # every symbol include/florence_gb300.h declares
 EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_ComputeSparsityPattern",
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_", "fl_GlobalAssemblyDF_noalloc",
-           "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak",
+           "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
-           "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_MLP_num_params", "fl_MLP_workspace_size",
+           "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_MLP_num_params", "fl_MLP_workspace_size",
            "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep"]

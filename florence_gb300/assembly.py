@@ -19,6 +19,7 @@ Two layers:
 
 Every call goes through the CUDA library; there is no CPU path.
 """
+import contextlib
 import ctypes
 import warnings
 
@@ -356,3 +357,35 @@ def fp64_peak_gflops():
     g = ctypes.c_double(0.0)
     N.check(N.lib().fl_measure_fp64_peak(ctypes.byref(g), _stream()), "fl_measure_fp64_peak")
     return g.value
+
+
+def fp32_peak_gflops():
+    """Measured FP32 FMA throughput of this GPU (GFLOP/s)."""
+    g = ctypes.c_double(0.0)
+    N.check(N.lib().fl_measure_fp32_peak(ctypes.byref(g), _stream()), "fl_measure_fp32_peak")
+    return g.value
+
+
+ARITHMETIC = {"fp64": N.FL_ARITH_FP64, "float_pair": N.FL_ARITH_FLOAT_PAIR}
+
+
+def set_arithmetic(name):
+    """Arithmetic of the stiffness contraction for every later FP64 assembly in the process:
+    'fp64' (FP64 multiply-adds) or 'float_pair' (hi + lo float pairs on the FP32 pipe, ~1e-14
+    relative to FP64). Kinematics, material, residual and scatter are FP64 in both."""
+    N.check(N.lib().fl_SetAssemblyArithmetic(ARITHMETIC[name]), "fl_SetAssemblyArithmetic")
+
+
+def get_arithmetic():
+    code = N.lib().fl_GetAssemblyArithmetic()
+    return next(k for k, v in ARITHMETIC.items() if v == code)
+
+
+@contextlib.contextmanager
+def arithmetic(name):
+    old = get_arithmetic()
+    set_arithmetic(name)
+    try:
+        yield
+    finally:
+        set_arithmetic(old)

@@ -23,6 +23,7 @@
 #include <cuda_bf16.h>
 
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 
 #include "fl_common.cuh"
@@ -30,19 +31,22 @@
 namespace fl {
 
 // contraction kernel: TPE threads per element, EPC elements per CTA, MAXB node blocks per thread
-// per pass, MINB resident CTAs per SM requested from the compiler
+// per pass, MINB resident CTAs per SM requested from the compiler; the float-pair arithmetic
+// needs more registers per accumulator update and has its own MAXB_DF / MINB_DF (same TPE/EPC,
+// so the host-side chunking and shared-memory sizes are shared)
 template <int NPE>
 struct AsmCfg;
-template <> struct AsmCfg<4> { static constexpr int TPE = 32, EPC = 8, MAXB = 1, MINB = 4; };
-template <> struct AsmCfg<8> { static constexpr int TPE = 32, EPC = 8, MAXB = 2, MINB = 4; };
-template <> struct AsmCfg<10> { static constexpr int TPE = 64, EPC = 4, MAXB = 1, MINB = 4; };
-template <> struct AsmCfg<20> { static constexpr int TPE = 128, EPC = 2, MAXB = 2, MINB = 4; };
-template <> struct AsmCfg<27> { static constexpr int TPE = 384, EPC = 1, MAXB = 1, MINB = 2; };
-template <> struct AsmCfg<35> { static constexpr int TPE = 320, EPC = 1, MAXB = 2, MINB = 2; };
-template <> struct AsmCfg<64> { static constexpr int TPE = 416, EPC = 1, MAXB = 5, MINB = 1; };
-template <> struct AsmCfg<125> { static constexpr int TPE = 512, EPC = 1, MAXB = 4, MINB = 1; };
+template <> struct AsmCfg<4> { static constexpr int TPE = 32, EPC = 8, MAXB = 1, MINB = 4, MAXB_DF = 1, MINB_DF = 4; };
+template <> struct AsmCfg<8> { static constexpr int TPE = 32, EPC = 8, MAXB = 2, MINB = 4, MAXB_DF = 2, MINB_DF = 2; };
+template <> struct AsmCfg<10> { static constexpr int TPE = 64, EPC = 4, MAXB = 1, MINB = 4, MAXB_DF = 1, MINB_DF = 4; };
+template <> struct AsmCfg<20> { static constexpr int TPE = 128, EPC = 2, MAXB = 2, MINB = 4, MAXB_DF = 2, MINB_DF = 2; };
+template <> struct AsmCfg<27> { static constexpr int TPE = 384, EPC = 1, MAXB = 1, MINB = 2, MAXB_DF = 1, MINB_DF = 2; };
+template <> struct AsmCfg<35> { static constexpr int TPE = 320, EPC = 1, MAXB = 2, MINB = 2, MAXB_DF = 2, MINB_DF = 2; };
+template <> struct AsmCfg<64> { static constexpr int TPE = 416, EPC = 1, MAXB = 5, MINB = 1, MAXB_DF = 3, MINB_DF = 1; };
+template <> struct AsmCfg<125> { static constexpr int TPE = 512, EPC = 1, MAXB = 4, MINB = 1, MAXB_DF = 3, MINB_DF = 1; };
 
 constexpr int QSTRIDE = 54;    // 45 symmetric Ahat entries + 9 residual entries per Gauss point
+constexpr int QSM = 45;        // entries per Gauss point held in shared memory (the tangent part)
 constexpr int QP_THREADS = 128;
 constexpr size_t CHUNK_BYTES = (size_t)64 << 20;  // scratch per chunk: L2-resident between A and B
 
@@ -168,21 +172,79 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
 
 // ------------------------------------------------------------------------------------------------
 // B. contraction + scatter
+//
+// Arithmetic of the contraction (template parameter DF):
+//  false: FP64 fused multiply-adds.
+//  true:  float pairs on the FP32 pipe. Every operand is held as hi + lo (hi = RN_f32(x),
+//         lo = RN_f32(x - hi)); a product is formed error-free in its leading part
+//         (p = ah*bh, e = fma(ah, bh, -p)) plus the cross terms ah*bl + al*bh, and added to the
+//         accumulator with Knuth's two-sum, the rounding error carried in the low word. The
+//         relative error of one multiply-add is about 2^-46 (the dropped al*bl and the low word's
+//         own rounding), so the element matrix is FP64-accurate to ~1e-14 relative while the
+//         work runs at the FP32 rate, 64x GB300's FP64 rate. The residual stays FP64.
 // ------------------------------------------------------------------------------------------------
-template <int NPE>
-__global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NPE>::MINB)
+template <bool DF>
+struct Arith;
+
+template <>
+struct Arith<false> {
+    using S = double;  // shared-memory operand
+    struct Acc {
+        double v;
+    };
+    static __device__ __forceinline__ S split(double x) { return x; }
+    static __device__ __forceinline__ void zero(Acc &a) { a.v = 0.0; }
+    static __device__ __forceinline__ void mac(Acc &a, S x, S y) { a.v = fma(x, y, a.v); }
+    static __device__ __forceinline__ double value(const Acc &a) { return a.v; }
+    static __device__ __forceinline__ S store(const Acc &a) { return a.v; }
+};
+
+template <>
+struct Arith<true> {
+    using S = float2;
+    struct Acc {
+        float h, l;
+    };
+    static __device__ __forceinline__ S split(double x) {
+        const float h = (float)x;
+        return make_float2(h, (float)(x - (double)h));
+    }
+    static __device__ __forceinline__ void zero(Acc &a) { a.h = a.l = 0.f; }
+    static __device__ __forceinline__ void mac(Acc &a, S x, S y) {
+        const float p = x.x * y.x;
+        const float pe = fmaf(x.x, y.y, fmaf(x.y, y.x, fmaf(x.x, y.x, -p)));
+        const float s = a.h + p;
+        const float bv = s - a.h;
+        const float e = (a.h - (s - bv)) + (p - bv);
+        a.h = s;
+        a.l += e + pe;
+    }
+    static __device__ __forceinline__ double value(const Acc &a) { return (double)a.h + (double)a.l; }
+    static __device__ __forceinline__ S store(const Acc &a) {  // renormalised pair
+        const float h = a.h + a.l;
+        return make_float2(h, a.l - (h - a.h));
+    }
+};
+
+template <int NPE, bool DF>
+__global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, DF ? AsmCfg<NPE>::MINB_DF : AsmCfg<NPE>::MINB)
     contract_kernel(const AsmArgs A) {
-    constexpr int TPE = AsmCfg<NPE>::TPE, EPC = AsmCfg<NPE>::EPC, MAXB = AsmCfg<NPE>::MAXB;
+    using AR = Arith<DF>;
+    using S = typename AR::S;
+    using Acc = typename AR::Acc;
+    constexpr int TPE = AsmCfg<NPE>::TPE, EPC = AsmCfg<NPE>::EPC;
+    constexpr int MAXB = DF ? AsmCfg<NPE>::MAXB_DF : AsmCfg<NPE>::MAXB;
     constexpr int NT = TPE * EPC, NDOF = 3 * NPE, NBLK = NPE * (NPE + 1) / 2;
     constexpr int PER_PASS = TPE * MAXB, NPASS = (NBLK + PER_PASS - 1) / PER_PASS;
+    static_assert(sizeof(S) == sizeof(double), "shared-memory layout assumes 8-byte operands");
     const int nq = A.nq, QC = A.qc;
 
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double *Qs = reinterpret_cast<double *>(smem_raw);                      // [EPC][nq][QSTRIDE]
-    double *Jc = Qs + (size_t)EPC * nq * QSTRIDE;                           // [QC][NPE][3]
-    double *Us = Jc + (size_t)QC * NPE * 3;                                 // [EPC][QC][NPE][27]
+    S *Qs = reinterpret_cast<S *>(smem_raw);                                 // [EPC][nq][QSM]
+    S *Jc = Qs + (size_t)EPC * nq * QSM;                                     // [QC][NPE][3]
+    S *Us = Jc + (size_t)QC * NPE * 3;                                       // [EPC][QC][NPE][27]
     int *nodes = reinterpret_cast<int *>(Us + (size_t)EPC * QC * NPE * 27);  // [EPC][NPE]
-    int *inv = nodes + EPC * NPE;                                           // [EPC][NDOF]
+    int *inv = nodes + EPC * NPE;                                            // [EPC][NDOF]
     __shared__ int s_flag;
     __shared__ int64_t s_nnz;
 
@@ -197,6 +259,7 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
     }
 
     const int64_t cap = (int64_t)NDOF * NDOF;
+    const double *qg = A.Q + el * nq;  // this element's Gauss-point data, Q[k][el*nq + g]
     if (active) {
         for (int a = lt; a < NPE; a += TPE) {
             uint64_t nd = A.elements[e * NPE + a];
@@ -216,25 +279,24 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
                 else inv[slot * NDOF + p] = i;
             }
         }
-        // Gauss-point data of this element: Q[k][el*nq + g] -> Qs[slot][g][k]
-        const double *q = A.Q + el * nq;
-        for (int idx = lt; idx < nq * QSTRIDE; idx += TPE) {
+        // tangent part of the Gauss-point data -> Qs[slot][g][k]
+        for (int idx = lt; idx < nq * 45; idx += TPE) {
             const int k = idx / nq, g = idx % nq;
-            Qs[((size_t)slot * nq + g) * QSTRIDE + k] = q[k * A.ldq + g];
+            Qs[((size_t)slot * nq + g) * QSM + k] = AR::split(qg[k * A.ldq + g]);
         }
     }
     __syncthreads();
 
-    // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d]
+    // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d], FP64 (S from the L2-resident scratch)
     if (active && A.update) {
         for (int r = lt; r < NDOF; r += TPE) {
             const int a = r / 3, i = r % 3;
             double t = 0.0;
-            const double *qs = Qs + (size_t)slot * nq * QSTRIDE + 45 + i * 3;
-            for (int g = 0; g < nq; ++g, qs += QSTRIDE) {
-                t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[0], t);
-                t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[1], t);
-                t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2], t);
+            const double *qs = qg + (size_t)(45 + i * 3) * A.ldq;
+            for (int g = 0; g < nq; ++g) {
+                t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[g], t);
+                t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[A.ldq + g], t);
+                t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2 * A.ldq + g], t);
             }
             atomicAdd(A.T + 3 * (int64_t)nodes[slot * NPE + a] + i, t);
         }
@@ -242,7 +304,7 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
 
     // stiffness, in passes over the node blocks (a <= b, b-major)
     for (int pass = 0; pass < NPASS; ++pass) {
-        double acc[MAXB][9];
+        Acc acc[MAXB][9];
         int ba[MAXB], bb[MAXB];
 #pragma unroll
         for (int m = 0; m < MAXB; ++m) {
@@ -253,23 +315,27 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
             ba[m] = blk < NBLK ? blk - b * (b + 1) / 2 : -1;
             bb[m] = b;
 #pragma unroll
-            for (int k = 0; k < 9; ++k) acc[m][k] = 0.0;
+            for (int k = 0; k < 9; ++k) AR::zero(acc[m][k]);
         }
         for (int c0 = 0; c0 < nq; c0 += QC) {
             const int qc = min(QC, nq - c0);
             for (int idx = tid; idx < qc * NPE * 3; idx += NT) {
                 const int q = idx / (NPE * 3), r = idx % (NPE * 3), a = r / 3, d = r % 3;
-                Jc[idx] = __ldg(A.Jm + ((size_t)d * NPE + a) * nq + c0 + q);
+                Jc[idx] = AR::split(__ldg(A.Jm + ((size_t)d * NPE + a) * nq + c0 + q));
             }
             __syncthreads();
             if (active) {
                 for (int idx = lt; idx < qc * NPE * 27; idx += TPE) {
                     const int q = idx / (NPE * 27), r = idx % (NPE * 27), b = r / 27, s = r % 27;
                     const int I = s / 3, k = s % 3;  // s = (i*3+d)*3 + k, I = i*3+d
-                    const double *qq = Qs + ((size_t)slot * nq + c0 + q) * QSTRIDE;
-                    const double *jb = Jc + (q * NPE + b) * 3;
-                    Us[(((size_t)slot * QC + q) * NPE + b) * 27 + s] =
-                        fma(qq[sym9(I, k * 3 + 0)], jb[0], fma(qq[sym9(I, k * 3 + 1)], jb[1], qq[sym9(I, k * 3 + 2)] * jb[2]));
+                    const S *qq = Qs + ((size_t)slot * nq + c0 + q) * QSM;
+                    const S *jb = Jc + (q * NPE + b) * 3;
+                    Acc u;
+                    AR::zero(u);
+                    AR::mac(u, qq[sym9(I, k * 3 + 2)], jb[2]);
+                    AR::mac(u, qq[sym9(I, k * 3 + 1)], jb[1]);
+                    AR::mac(u, qq[sym9(I, k * 3 + 0)], jb[0]);
+                    Us[(((size_t)slot * QC + q) * NPE + b) * 27 + s] = AR::store(u);
                 }
             }
             __syncthreads();
@@ -278,17 +344,16 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
 #pragma unroll
                     for (int m = 0; m < MAXB; ++m) {
                         if (ba[m] < 0) continue;
-                        const double *ja = Jc + (q * NPE + ba[m]) * 3;
-                        const double j0 = ja[0], j1 = ja[1], j2 = ja[2];
-                        const double *u = Us + (((size_t)slot * QC + q) * NPE + bb[m]) * 27;
+                        const S *ja = Jc + (q * NPE + ba[m]) * 3;
+                        const S j0 = ja[0], j1 = ja[1], j2 = ja[2];
+                        const S *u = Us + (((size_t)slot * QC + q) * NPE + bb[m]) * 27;
 #pragma unroll
                         for (int i = 0; i < 3; ++i)
 #pragma unroll
                             for (int k = 0; k < 3; ++k) {
-                                double v = acc[m][i * 3 + k];
-                                v = fma(j0, u[(i * 3 + 0) * 3 + k], v);
-                                v = fma(j1, u[(i * 3 + 1) * 3 + k], v);
-                                acc[m][i * 3 + k] = fma(j2, u[(i * 3 + 2) * 3 + k], v);
+                                AR::mac(acc[m][i * 3 + k], j0, u[(i * 3 + 0) * 3 + k]);
+                                AR::mac(acc[m][i * 3 + k], j1, u[(i * 3 + 1) * 3 + k]);
+                                AR::mac(acc[m][i * 3 + k], j2, u[(i * 3 + 2) * 3 + k]);
                             }
                     }
                 }
@@ -310,7 +375,7 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
                         for (int ri = 0; ri < 3; ++ri)
 #pragma unroll
                             for (int ci = 0; ci < 3; ++ci) {
-                                const double v = mirror ? acc[m][ci * 3 + ri] : acc[m][ri * 3 + ci];
+                                const double v = AR::value(mirror ? acc[m][ci * 3 + ri] : acc[m][ri * 3 + ci]);
                                 const int64_t pos = block_entry(A.indptr, A.indices, nr, nc, ri, ci, off);
                                 if (pos >= 0 && pos < s_nnz) atomicAdd(A.V + pos, v);
                                 else flag |= FL_FLAG_BAD_INDEX;
@@ -322,7 +387,7 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, AsmCfg<NP
                 for (int i = 0; i < 3; ++i)
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        const double v = acc[m][i * 3 + k];
+                        const double v = AR::value(acc[m][i * 3 + k]);
                         const int r = 3 * a + i, c = 3 * b + k;
                         const int gr = 3 * na + i, gc = 3 * nb + k;
                         for (int mirror = 0; mirror < (a == b ? 1 : 2); ++mirror) {
@@ -377,7 +442,7 @@ static int asm_qc(int nq) {
 template <int NPE>
 static size_t asm_smem_bytes(int nq, int qc) {
     constexpr int EPC = AsmCfg<NPE>::EPC;
-    return sizeof(double) * ((size_t)EPC * nq * QSTRIDE + (size_t)qc * NPE * 3 + (size_t)EPC * qc * NPE * 27) +
+    return sizeof(double) * ((size_t)EPC * nq * QSM + (size_t)qc * NPE * 3 + (size_t)EPC * qc * NPE * 27) +
            sizeof(int) * ((size_t)EPC * NPE + (size_t)EPC * 3 * NPE);
 }
 
@@ -387,14 +452,17 @@ static int64_t chunk_elements(size_t bytes, int nq, int epc) {
     return ce - ce % epc;
 }
 
+// Arithmetic of the contraction kernel (fl_SetAssemblyArithmetic)
+static std::atomic<int> g_arith{FL_ARITH_FP64};
+
 // Runs A and B over [0, nelem) in chunks of at most `chunk` elements through scratch Q.
-template <int NPE, int MAT>
-static int run_chunks(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) {
+template <int NPE, int MAT, bool DF>
+static int run_chunks_t(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) {
     constexpr int EPC = AsmCfg<NPE>::EPC, NT = AsmCfg<NPE>::TPE * EPC;
     A.qc = asm_qc<NPE>(A.nq);
     const size_t smem = asm_smem_bytes<NPE>(A.nq, A.qc);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    { const int st = ensure_smem<contract_kernel<NPE>>(smem); if (st != FL_OK) return st; }
+    { const int st = ensure_smem<contract_kernel<NPE, DF>>(smem); if (st != FL_OK) return st; }
     A.Q = Q;
     A.ldq = chunk * A.nq;
     for (int64_t e0 = 0; e0 < A.nelem; e0 += chunk) {
@@ -402,9 +470,15 @@ static int run_chunks(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) 
         A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
         const int64_t nqp = A.ne * A.nq;
         qp_kernel<NPE, MAT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
-        contract_kernel<NPE><<<(unsigned)((A.ne + EPC - 1) / EPC), NT, smem, stream>>>(A);
+        contract_kernel<NPE, DF><<<(unsigned)((A.ne + EPC - 1) / EPC), NT, smem, stream>>>(A);
     }
     return launch_status();
+}
+
+template <int NPE, int MAT>
+static int run_chunks(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) {
+    if (g_arith.load() == FL_ARITH_FLOAT_PAIR) return run_chunks_t<NPE, MAT, true>(A, Q, chunk, stream);
+    return run_chunks_t<NPE, MAT, false>(A, Q, chunk, stream);
 }
 
 template <int NPE, int MAT>
@@ -540,8 +614,8 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
     constexpr int AST = MX_KC + 8;  // padded row stride (bf16) of the A chunk
     const int nq = A.nq, K = 3 * nq;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double *Qs = reinterpret_cast<double *>(smem_raw);                              // [nq][QSTRIDE]
-    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + (size_t)nq * QSTRIDE);  // [3][MX_MC][AST]
+    double *Qs = reinterpret_cast<double *>(smem_raw);                              // [nq][QSM]
+    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + (size_t)nq * QSM);      // [3][MX_MC][AST]
     __nv_bfloat16 *Am = Ah + MX_MC * AST;
     __nv_bfloat16 *Al = Am + MX_MC * AST;
     __nv_bfloat16 *Bh = Al + MX_MC * AST;                                            // [3][NP][AST]
@@ -578,9 +652,9 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                 else inv[p] = i;
             }
         const double *q = A.Q + el * nq;
-        for (int idx = tid; idx < nq * QSTRIDE; idx += MX_NT) {
+        for (int idx = tid; idx < nq * QSM; idx += MX_NT) {
             const int k = idx / nq, g = idx % nq;
-            Qs[(size_t)g * QSTRIDE + k] = q[k * A.ldq + g];
+            Qs[(size_t)g * QSM + k] = q[k * A.ldq + g];
         }
         __syncthreads();
         if (!A.dl)  // offset of column node b in row node a; consecutive threads share a row
@@ -593,11 +667,11 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
             for (int r = tid; r < NDOF; r += MX_NT) {
                 const int a = r / 3, i = r % 3;
                 double t = 0.0;
-                const double *qs = Qs + 45 + i * 3;
-                for (int g = 0; g < nq; ++g, qs += QSTRIDE) {
-                    t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[0], t);
-                    t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[1], t);
-                    t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2], t);
+                const double *qs = q + (size_t)(45 + i * 3) * A.ldq;  // S from the L2-resident scratch
+                for (int g = 0; g < nq; ++g) {
+                    t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[g], t);
+                    t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[A.ldq + g], t);
+                    t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2 * A.ldq + g], t);
                 }
                 atomicAdd(A.T + 3 * (int64_t)nodes[a] + i, t);
             }
@@ -616,7 +690,7 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                     if (r < M && cc < kc) {
                         const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
                         const int g = c / 3, d = c % 3, I = i * 3 + d;
-                        const double *qq = Qs + (size_t)g * QSTRIDE;
+                        const double *qq = Qs + (size_t)g * QSM;
                         v = (float)fma(qq[sym9(I, k * 3 + 0)], __ldg(A.Jm + ((size_t)0 * NPE + b) * nq + g),
                                        fma(qq[sym9(I, k * 3 + 1)], __ldg(A.Jm + ((size_t)1 * NPE + b) * nq + g),
                                            qq[sym9(I, k * 3 + 2)] * __ldg(A.Jm + ((size_t)2 * NPE + b) * nq + g)));
@@ -694,7 +768,7 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
 template <int NPE>
 static size_t mixed_smem_bytes(int nq) {
     constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
-    return sizeof(double) * (size_t)nq * QSTRIDE + sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
+    return sizeof(double) * (size_t)nq * QSM + sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
            sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
 }
 
@@ -858,6 +932,14 @@ int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const
                                   data_global_indices, fl::MatParams{0, 0, 0}, flags, nullptr, 0, (cudaStream_t)stream,
                                   element_params);
 }
+
+int fl_SetAssemblyArithmetic(int arithmetic) {
+    if (arithmetic != FL_ARITH_FP64 && arithmetic != FL_ARITH_FLOAT_PAIR) return FL_ERR_ARG;
+    fl::g_arith.store(arithmetic);
+    return FL_OK;
+}
+
+int fl_GetAssemblyArithmetic(void) { return fl::g_arith.load(); }
 
 int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk) {
     std::lock_guard<std::mutex> lock(fl::g_tune_mutex);

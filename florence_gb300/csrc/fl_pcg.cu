@@ -25,6 +25,8 @@
 // block; the scalars never travel to the host inside the iteration (kernels read them from the
 // slots), and the host checks the done flag every PCG_CHECK iterations.
 #include <algorithm>
+#include <mutex>
+#include <utility>
 #include <vector>
 
 #include "fl_common.cuh"
@@ -173,7 +175,8 @@ __global__ void __launch_bounds__(PCG_NT) pcg_init2(int64_t nnode, PcgState s) {
 // is carried as an unevaluated float pair (error-free product by FMA, compensated two-sum), with
 // p given as a float pair too, so the FP32 matrix is applied to ~2^-44 relative accuracy while
 // every operation runs on the FP32 pipe (GB300's FP64 rate would otherwise bound this loop).
-constexpr int NB_LANES = 8;
+// lanes per node of the node-block product: 4, 8, 16 or 32, chosen per matrix by timing
+// (pick_lanes)
 
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
@@ -191,6 +194,7 @@ __device__ __forceinline__ void df_mac(float v, float ph, float pl, float &s, fl
     c += e + fmaf(v, pl, perr);
 }
 
+template <int NB>
 __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const double *vals,
                                                const PcgState &st, int64_t node, bool valid, int sub, double &y0,
                                                double &y1, double &y2) {
@@ -198,7 +202,7 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
     if (valid) {
         const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
         const int nb = (r1 - r0) / 3;
-        for (int sl = sub; sl < nb; sl += NB_LANES) {
+        for (int sl = sub; sl < nb; sl += NB) {
             const int m3 = indices[r0 + 3 * sl];
             const double x0 = st.p[m3], x1 = st.p[m3 + 1], x2 = st.p[m3 + 2];
             const double *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
@@ -208,13 +212,14 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
         }
     }
 #pragma unroll
-    for (int o = NB_LANES / 2; o > 0; o >>= 1) {
-        y0 += __shfl_down_sync(0xffffffffu, y0, o, NB_LANES);
-        y1 += __shfl_down_sync(0xffffffffu, y1, o, NB_LANES);
-        y2 += __shfl_down_sync(0xffffffffu, y2, o, NB_LANES);
+    for (int o = NB / 2; o > 0; o >>= 1) {
+        y0 += __shfl_down_sync(0xffffffffu, y0, o, NB);
+        y1 += __shfl_down_sync(0xffffffffu, y1, o, NB);
+        y2 += __shfl_down_sync(0xffffffffu, y2, o, NB);
     }
 }
 
+template <int NB>
 __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const float *vals,
                                                const PcgState &st, int64_t node, bool valid, int sub, double &y0,
                                                double &y1, double &y2) {
@@ -222,7 +227,7 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
     if (valid) {
         const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
         const int nb = (r1 - r0) / 3;
-        for (int sl = sub; sl < nb; sl += NB_LANES) {
+        for (int sl = sub; sl < nb; sl += NB) {
             const int m3 = indices[r0 + 3 * sl];
             const float h0 = st.ph[m3], h1 = st.ph[m3 + 1], h2 = st.ph[m3 + 2];
             const float l0 = st.pl[m3], l1 = st.pl[m3 + 1], l2 = st.pl[m3 + 2];
@@ -233,16 +238,16 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
         }
     }
 #pragma unroll
-    for (int o = NB_LANES / 2; o > 0; o >>= 1) {
+    for (int o = NB / 2; o > 0; o >>= 1) {
         float t, e;
-        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB_LANES), t, e);
-        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB_LANES);
+        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB), t, e);
+        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB);
         s0 = t;
-        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB_LANES), t, e);
-        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB_LANES);
+        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB), t, e);
+        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB);
         s1 = t;
-        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB_LANES), t, e);
-        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB_LANES);
+        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB), t, e);
+        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB);
         s2 = t;
     }
     y0 = (double)s0 + (double)c0;
@@ -260,6 +265,7 @@ __device__ __forceinline__ void df_mac2(float2 v, float ph, float pl, float &s, 
     c += e + fmaf(v.x, pl, fmaf(v.y, ph, perr));
 }
 
+template <int NB>
 __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const float2 *vals,
                                                const PcgState &st, int64_t node, bool valid, int sub, double &y0,
                                                double &y1, double &y2) {
@@ -267,7 +273,7 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
     if (valid) {
         const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
         const int nb = (r1 - r0) / 3;
-        for (int sl = sub; sl < nb; sl += NB_LANES) {
+        for (int sl = sub; sl < nb; sl += NB) {
             const int m3 = indices[r0 + 3 * sl];
             const float h0 = st.ph[m3], h1 = st.ph[m3 + 1], h2 = st.ph[m3 + 2];
             const float l0 = st.pl[m3], l1 = st.pl[m3 + 1], l2 = st.pl[m3 + 2];
@@ -278,16 +284,16 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
         }
     }
 #pragma unroll
-    for (int o = NB_LANES / 2; o > 0; o >>= 1) {
+    for (int o = NB / 2; o > 0; o >>= 1) {
         float t, e;
-        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB_LANES), t, e);
-        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB_LANES);
+        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB), t, e);
+        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB);
         s0 = t;
-        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB_LANES), t, e);
-        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB_LANES);
+        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB), t, e);
+        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB);
         s1 = t;
-        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB_LANES), t, e);
-        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB_LANES);
+        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB), t, e);
+        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB);
         s2 = t;
     }
     y0 = (double)s0 + (double)c0;
@@ -335,7 +341,7 @@ __global__ void pcg_check_blocks(const int32_t *indptr, const int32_t *indices, 
 // Each kernel zeroes the slot the next kernel accumulates into, after every reader is done.
 
 // K1: q = mask(K p), p.q; zeroes r.z of iterate k+1 and r.r for K2
-template <class VT, bool NODEBLK>
+template <class VT, bool NODEBLK, int NB = 8>
 __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const int32_t *indices, const VT *vals,
                                                  const int8_t *fixed, int64_t n, int k, PcgState s) {
     if (s.done[0]) return;
@@ -348,12 +354,12 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
     const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
     double pq = 0.0;
     if (NODEBLK) {
-        const int grp = lane / NB_LANES, sub = lane % NB_LANES;
+        const int grp = lane / NB, sub = lane % NB;
         const int64_t nnode = n / 3;
-        for (int64_t base = warp * (32 / NB_LANES); base < nnode; base += nwarps * (32 / NB_LANES)) {
+        for (int64_t base = warp * (32 / NB); base < nnode; base += nwarps * (32 / NB)) {
             const int64_t m = base + grp;
             double y0, y1, y2;
-            node_block_row(indptr, indices, vals, s, m, m < nnode, sub, y0, y1, y2);
+            node_block_row<NB>(indptr, indices, vals, s, m, m < nnode, sub, y0, y1, y2);
             if (sub == 0 && m < nnode) {
                 const double q0 = fixed[3 * m] ? 0.0 : y0, q1 = fixed[3 * m + 1] ? 0.0 : y1,
                              q2 = fixed[3 * m + 2] ? 0.0 : y2;
@@ -380,29 +386,35 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
     block_atomic_add(pq, s.acc + 0);
 }
 
-// K2: alpha = rz_k / p.q, x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r
+// K2: alpha = rz_k / p.q, x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r. One thread per
+// dof, 30 lanes of a warp = 10 nodes; a node's three residual entries meet through shuffles.
 __global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x, PcgState s) {
     if (s.done[0]) return;
     const double alpha = s.acc[1 + (k & 1)] / s.acc[0];
+    const int lane = threadIdx.x & 31, ln = lane / 3, i = lane % 3, l0 = 3 * ln;
+    const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
     double rzn = 0.0, rr = 0.0;
-    for (int64_t m = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; m < nnode; m += (int64_t)gridDim.x * PCG_NT) {
-        double rv[3];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const int64_t d = 3 * m + i;
+    for (int64_t base = warp * 10; base < nnode; base += nwarps * 10) {  // warp-uniform trip count
+        const int64_t m = base + ln;
+        const bool valid = lane < 30 && m < nnode;
+        const int64_t d = 3 * m + i;
+        double rv = 0.0;
+        if (valid) {
             x[d] = fma(alpha, s.p[d], x[d]);
-            rv[i] = fma(-alpha, s.q[d], s.r[d]);
-            s.r[d] = rv[i];
+            rv = fma(-alpha, s.q[d], s.r[d]);
+            s.r[d] = rv;
         }
-        const double *B = s.Binv + m * 9;
-        const double z0 = fma(B[0], rv[0], fma(B[1], rv[1], B[2] * rv[2]));
-        const double z1 = fma(B[3], rv[0], fma(B[4], rv[1], B[5] * rv[2]));
-        const double z2 = fma(B[6], rv[0], fma(B[7], rv[1], B[8] * rv[2]));
-        s.z[3 * m] = z0;
-        s.z[3 * m + 1] = z1;
-        s.z[3 * m + 2] = z2;
-        rzn = fma(rv[0], z0, fma(rv[1], z1, fma(rv[2], z2, rzn)));
-        rr = fma(rv[0], rv[0], fma(rv[1], rv[1], fma(rv[2], rv[2], rr)));
+        const double r0 = __shfl_sync(0xffffffffu, rv, l0);
+        const double r1 = __shfl_sync(0xffffffffu, rv, (l0 + 1) & 31);
+        const double r2 = __shfl_sync(0xffffffffu, rv, (l0 + 2) & 31);
+        if (valid) {
+            const double *B = s.Binv + m * 9 + i * 3;
+            const double z = fma(B[0], r0, fma(B[1], r1, B[2] * r2));
+            s.z[d] = z;
+            rzn = fma(rv, z, rzn);
+            rr = fma(rv, rv, rr);
+        }
     }
     block_atomic_add(rzn, s.acc + 1 + ((k + 1) & 1));
     block_atomic_add(rr, s.acc + 3);
@@ -431,25 +443,115 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, 
     }
 }
 
+// Resident blocks of a kernel over the whole GPU (one wave), for grid sizes of the grid-stride
+// kernels.
+template <auto Kernel>
+static int64_t resident_blocks() {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, Kernel, PCG_NT, 0);
+    return (int64_t)std::max(1, sms) * std::max(1, per_sm);
+}
+
+// K1 launch for a value type and lanes per node; grid = one wave, or fewer blocks if the nodes
+// run out first
+template <class MT, int NB>
+static void launch_k1(const int32_t *indptr, const int32_t *indices, const MT *vals, const int8_t *fixed, int64_t n,
+                      int k, const PcgState &s, cudaStream_t st) {
+    static thread_local int64_t wave[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int64_t &w = wave[dev & 63];
+    if (w == 0) w = resident_blocks<pcg_k1<MT, true, NB>>();
+    const int64_t nodes_per_block = (PCG_NT / 32) * (32 / NB);
+    const int64_t need = (n / 3 + nodes_per_block - 1) / nodes_per_block;
+    pcg_k1<MT, true, NB><<<(unsigned)std::max<int64_t>(1, std::min(need, w)), PCG_NT, 0, st>>>(indptr, indices, vals,
+                                                                                              fixed, n, k, s);
+}
+
+template <class MT>
+static void launch_k1_nb(int nb, const int32_t *indptr, const int32_t *indices, const MT *vals, const int8_t *fixed,
+                         int64_t n, int k, const PcgState &s, cudaStream_t st) {
+    switch (nb) {
+        case 4: launch_k1<MT, 4>(indptr, indices, vals, fixed, n, k, s, st); break;
+        case 16: launch_k1<MT, 16>(indptr, indices, vals, fixed, n, k, s, st); break;
+        case 32: launch_k1<MT, 32>(indptr, indices, vals, fixed, n, k, s, st); break;
+        default: launch_k1<MT, 8>(indptr, indices, vals, fixed, n, k, s, st); break;
+    }
+}
+
+// Lanes per node of the node-block product, picked by timing two products with each choice on
+// the first solve of a matrix shape (device, rows, nonzeros, value type) and cached. The timed
+// launches only write q and the p.q slot, which the caller resets afterwards.
+struct LaneKey {
+    int dev, kind;
+    int64_t n, nnz;
+};
+static std::mutex g_lane_mutex;
+static std::vector<std::pair<LaneKey, int>> g_lane_cache;
+
+template <class MT>
+static int pick_lanes(const int32_t *indptr, const int32_t *indices, const MT *vals, const int8_t *fixed, int64_t n,
+                      int64_t nnz, int kind, const PcgState &s, cudaStream_t st) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    {
+        std::lock_guard<std::mutex> lock(g_lane_mutex);
+        for (auto &e : g_lane_cache)
+            if (e.first.dev == dev && e.first.kind == kind && e.first.n == n && e.first.nnz == nnz) return e.second;
+    }
+    int best = 8;
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    if (cudaEventCreate(&e0) != cudaSuccess) return best;
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return best;
+    }
+    for (int nb : {4, 8, 16, 32}) {
+        launch_k1_nb<MT>(nb, indptr, indices, vals, fixed, n, 0, s, st);  // first touch
+        cudaEventRecord(e0, st);
+        for (int r = 0; r < 2; ++r) launch_k1_nb<MT>(nb, indptr, indices, vals, fixed, n, 0, s, st);
+        cudaEventRecord(e1, st);
+        float ms = 0.f;
+        if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
+            ms < best_ms) {
+            best_ms = ms;
+            best = nb;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::lock_guard<std::mutex> lock(g_lane_mutex);
+    g_lane_cache.push_back({LaneKey{dev, kind, n, nnz}, best});
+    return best;
+}
+
 template <class VT>
 static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals, int64_t n, const int8_t *fixed,
                   const double *b, double *x, double rtol, int64_t maxiter, void *ws, size_t ws_bytes,
                   int64_t *iters, double *relres, cudaStream_t st, bool split = false) {
     if (!indptr || !indices || !vals || !fixed || !b || !x || !iters || !relres || n <= 0 || n % 3) return FL_ERR_ARG;
-    int32_t nnz32 = 0;  // the split copy is sized by the matrix
-    if (split) {
-        FL_CUDA_TRY(cudaMemcpyAsync(&nnz32, indptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-        FL_CUDA_TRY(cudaStreamSynchronize(st));
-        if (nnz32 < 0) return FL_ERR_ARG;
-    }
-    if (pcg_layout(n, nnz32, nullptr, nullptr) > ws_bytes || !ws) return FL_ERR_CAPACITY;
+    int32_t nnz32 = 0;
+    FL_CUDA_TRY(cudaMemcpyAsync(&nnz32, indptr + n, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+    FL_CUDA_TRY(cudaStreamSynchronize(st));
+    if (nnz32 < 0) return FL_ERR_ARG;
+    // the split copy is sized by the matrix
+    if (pcg_layout(n, split ? nnz32 : 0, nullptr, nullptr) > ws_bytes || !ws) return FL_ERR_CAPACITY;
     PcgState s;
     float2 *vsplit = nullptr;
-    pcg_layout(n, nnz32, &s, (char *)ws, &vsplit);
+    pcg_layout(n, split ? nnz32 : 0, &s, (char *)ws, &vsplit);
     const int64_t nnode = n / 3;
     const unsigned g_rows = (unsigned)std::min<int64_t>((n + (PCG_NT / 32) - 1) / (PCG_NT / 32), 152 * 16);
     const unsigned g_nodes = (unsigned)std::min<int64_t>((nnode + PCG_NT - 1) / PCG_NT, 152 * 16);
     const unsigned g_dofs = (unsigned)std::min<int64_t>((n + PCG_NT - 1) / PCG_NT, 152 * 16);
+    static thread_local int64_t k2_wave[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (k2_wave[dev & 63] == 0) k2_wave[dev & 63] = resident_blocks<pcg_k2>();
+    const int64_t k2_need = ((nnode + 9) / 10 + PCG_NT / 32 - 1) / (PCG_NT / 32);
+    const unsigned g_k2 = (unsigned)std::max<int64_t>(1, std::min(k2_need, k2_wave[dev & 63]));
     FL_CUDA_TRY(cudaMemsetAsync(s.done, 0, sizeof(int) * 4, st));
     FL_CUDA_TRY(cudaMemsetAsync(s.acc, 0, sizeof(double) * 8, st));
     bj_setup<<<g_nodes, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, nnode, s.Binv, s.done + 2);
@@ -464,15 +566,18 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     if (err & 3) return FL_ERR_ARG;  // pattern without diagonal blocks, or a singular block
     const bool nodeblk = !(err & 8);
     split = split && nodeblk;  // the float-pair product is the node-block one
-    if (split) split_values<<<g_dofs, PCG_NT, 0, st>>>(indptr, n, (const double *)vals, vsplit);
-    const unsigned g_k1 = nodeblk ? (unsigned)std::min<int64_t>((nnode + PCG_NT / NB_LANES - 1) / (PCG_NT / NB_LANES),
-                                                                152 * 16)
-                                  : g_rows;
     const double b2 = hacc[4];
     if (b2 == 0.0) {  // zero right-hand side: x unchanged is the solution
         *iters = 0;
         *relres = 0.0;
         return FL_OK;
+    }
+    if (split) split_values<<<g_dofs, PCG_NT, 0, st>>>(indptr, n, (const double *)vals, vsplit);
+    int nb = 8;
+    if (nodeblk) {
+        nb = split ? pick_lanes<float2>(indptr, indices, vsplit, fixed, n, nnz32, 2, s, st)
+                   : pick_lanes<VT>(indptr, indices, vals, fixed, n, nnz32, (int)sizeof(VT), s, st);
+        FL_CUDA_TRY(cudaMemsetAsync(s.acc, 0, sizeof(double), st));  // p.q of the timed products
     }
     const double tol2 = rtol * rtol * b2;
     int hd[4] = {0, 0, 0, 0};
@@ -480,10 +585,10 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     while (k < maxiter) {
         const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
         for (; k < kend; ++k) {
-            if (split) pcg_k1<float2, true><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vsplit, fixed, n, (int)k, s);
-            else if (nodeblk) pcg_k1<VT, true><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
-            else pcg_k1<VT, false><<<g_k1, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
-            pcg_k2<<<g_nodes, PCG_NT, 0, st>>>(nnode, (int)k, x, s);
+            if (split) launch_k1_nb<float2>(nb, indptr, indices, vsplit, fixed, n, (int)k, s, st);
+            else if (nodeblk) launch_k1_nb<VT>(nb, indptr, indices, vals, fixed, n, (int)k, s, st);
+            else pcg_k1<VT, false><<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
+            pcg_k2<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, x, s);
             pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, (sizeof(VT) == 4 || split) ? 1 : 0, s);
         }
         FL_CUDA_TRY(cudaGetLastError());

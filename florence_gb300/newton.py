@@ -65,7 +65,8 @@ class NewtonSolver:
     """
 
     def __init__(self, asm, fixed, f_ext, n_increments=10, tol=1e-10, max_iter=25, pcg_maxiter=50000,
-                 eta_max=1e-2, eta_min=1e-12, tangent="fp64", criterion="reference", spmv="split"):
+                 eta_max=1e-2, eta_min=1e-12, tangent="fp64", criterion="reference", spmv="split",
+                 forcing="ew", eta0=1e-3):
         if asm.mode != "csr":
             raise ValueError("Newton needs the CSR tangent (mode='csr')")
         self.asm = asm
@@ -93,6 +94,15 @@ class NewtonSolver:
         self.V = torch.zeros(asm.nnz, dtype=torch.float64 if tangent == "fp64" else torch.float32, device=dev)
         self.T = torch.zeros(n, dtype=torch.float64, device=dev)
         self.spmv = spmv
+        if forcing not in ("ew", "rel"):
+            raise ValueError("forcing must be 'ew' or 'rel'")
+        # PCG tolerance of each Newton step. "rel": 0.1 x the relative residual. "ew":
+        # Eisenstat-Walker (choice 2, gamma 0.9, alpha 2): the square of the last residual
+        # reduction, so that a Jacobian that only converges linearly (the FP32 tangent) is not
+        # solved far below what its own error allows, with the standard safeguards, and never
+        # below half of what the convergence test still needs.
+        self.forcing = forcing
+        self.eta0 = eta0
         self.ws = pcg_workspace(asm, self.V, spmv)
         self.history = []
 
@@ -109,9 +119,10 @@ class NewtonSolver:
 
     def solve(self, u0=None, guesses=None, keep_states=False):
         """Runs all increments. guesses: optional callable(increment, u_prev) -> candidate initial
-        u for the increment (a warm start) or None. The candidate is kept only if its FP64
-        residual is smaller than that of the previous increment's solution (the default start);
-        otherwise the solver falls back to the previous solution. keep_states: also return each
+        u for the increment (a warm start), a list of candidates, or None. The candidate with the
+        smallest FP64 residual is kept if that residual is below the previous increment's
+        solution's (the default start); otherwise the solver falls back to the previous solution.
+        keep_states: also return each
         increment's converged displacement (device FP64) under increments[k]["u"]. Returns a dict."""
         dev = self.asm.device
         n = self.asm.nnode * 3
@@ -126,24 +137,28 @@ class NewtonSolver:
             F = self.f_ext * (inc / self.n_increments)
             guess = "previous"
             if guesses is not None:
-                g = guesses(inc, u)
-                if g is not None:
-                    r_prev = self.residual_norm(F)
-                    u_prev = u
-                    u = g.clone()
-                    self._assemble(u)
-                    if self.residual_norm(F) < r_prev:
-                        guess = "predicted"
-                    else:  # fallback: the prediction is worse than the previous increment
-                        u = u_prev
+                cands = guesses(inc, u)
+                if cands is not None:
+                    if isinstance(cands, torch.Tensor):
+                        cands = [cands]
+                    # the FP64 residual judges every candidate; the previous solution is the fallback
+                    best, best_r, best_k = u, self.residual_norm(F), -1
+                    for k, g in enumerate(cands):
+                        self._assemble(g)
+                        r = self.residual_norm(F)
+                        if r < best_r:
+                            best, best_r, best_k = g, r, k
+                    u = best.clone()
+                    if best_k != len(cands) - 1:  # the tangent and residual of the chosen state
                         self._assemble(u)
-                        guess = "fallback"
+                    guess = "fallback" if best_k < 0 else "candidate%d" % best_k
             R = (self.T - F) * self.free
             norm_load = float(torch.linalg.vector_norm(F * self.free))
             norm_forces = None
             it = 0
             rel = np.inf
-            eta = 1e-3
+            eta = self.eta0
+            r_before = float(torch.linalg.vector_norm(R))
             iters = []
             while True:
                 du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
@@ -167,8 +182,17 @@ class NewtonSolver:
                 if it >= self.max_iter or not np.isfinite(rel) or rel > 1e6:
                     failed = True
                     break
-                # inexact Newton: solve to a tolerance proportional to the current relative residual
-                eta = float(min(self.eta_max, max(self.eta_min, 0.1 * rel)))
+                if self.forcing == "rel":
+                    # solve to a tolerance proportional to the current relative residual
+                    eta = float(min(self.eta_max, max(self.eta_min, 0.1 * rel)))
+                else:
+                    e_new = 0.9 * (absn / r_before) ** 2 if r_before > 0 else self.eta_max
+                    if 0.9 * eta ** 2 > 0.1:
+                        e_new = max(e_new, 0.9 * eta ** 2)
+                    e_new = min(self.eta_max, e_new)
+                    e_new = max(e_new, 0.5 * self.tol * norm_forces / absn)
+                    eta = float(min(self.eta_max, max(self.eta_min, e_new)))
+                r_before = absn
             total_newton += len(iters)
             incs.append(dict(increment=inc, newton_iters=len(iters), history=iters, guess=guess))
             if keep_states:

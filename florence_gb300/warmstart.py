@@ -181,23 +181,28 @@ class PlateSolver:
         self.newton.f_ext = self.f_unit * float(traction)
         return self.newton.solve(guesses=guesses, keep_states=keep_states)
 
-    def increment_inputs(self, prm):
-        """Network inputs (mu, ratio, traction at increment k) of every increment of one solve."""
+    def increment_inputs(self, prm, with_zero=False):
+        """Network inputs (mu, ratio, traction at increment k) of every increment of one solve
+        (k = 1..n, and k = 0 first when with_zero)."""
         mu, ratio, t = prm
-        return np.array([[mu, ratio, t * k / self.n_increments] for k in range(1, self.n_increments + 1)])
+        return np.array([[mu, ratio, t * k / self.n_increments]
+                         for k in range(0 if with_zero else 1, self.n_increments + 1)])
 
 
 def generate_snapshots(solver, params):
     """Training data: for every parameter set one Newton solve; every converged increment is a
-    snapshot. Returns (X [S,3] FP64 host, U [ndof, S] FP64 device, solve statistics)."""
+    snapshot, and so is the unloaded state (u = 0 at zero traction, which anchors the network's
+    prediction at the start of the load path). Returns (X [S,3] FP64 host, U [ndof, S] FP64
+    device, solve statistics)."""
     X, cols, stats = [], [], []
+    zero = torch.zeros(solver.ndof, dtype=torch.float64, device=solver.asm.device)
     for prm in params:
         r = solver.solve(*prm, keep_states=True)
         if r["failed"]:
             stats.append(dict(params=list(map(float, prm)), failed=True))
             continue
-        X.append(solver.increment_inputs(prm))
-        cols += [inc["u"] for inc in r["increments"]]
+        X.append(solver.increment_inputs(prm, with_zero=True))
+        cols += [zero] + [inc["u"] for inc in r["increments"]]
         stats.append(dict(newton=r["newton_iters"], pcg=r["pcg_iters"], wall_s=r["wall_s"], failed=False))
     return np.concatenate(X), torch.stack(cols, 1), stats
 
@@ -237,24 +242,29 @@ def evaluate_warm_start(solver, ws, params):
     Returns per-set records and totals."""
     rows = []
     for prm in params:
-        inputs = solver.increment_inputs(prm)
+        inputs = solver.increment_inputs(prm, with_zero=True)
         base = solver.solve(*prm)
         t0 = time.perf_counter()
-        pred = ws.predict(inputs).reshape(len(inputs), -1)   # [n_increments, ndof], one forward
+        pred = ws.predict(inputs).reshape(len(inputs), -1)   # [1 + n_increments, ndof], one forward
         torch.cuda.synchronize()
         t_pred = time.perf_counter() - t0
-        warm = solver.solve(*prm, guesses=lambda inc, u_prev: pred[inc - 1])
+        # candidates: the predicted state, and the previous solution moved by the predicted step
+        # (the network's error largely cancels in the step)
+        warm = solver.solve(*prm, guesses=lambda inc, u_prev: [pred[inc], u_prev + (pred[inc] - pred[inc - 1])])
         warm["wall_s"] += t_pred
         rows.append(dict(params=list(map(float, prm)),
                          plain=dict(newton=base["newton_iters"], pcg=base["pcg_iters"], wall_s=base["wall_s"],
                                     failed=base["failed"]),
                          warm=dict(newton=warm["newton_iters"], pcg=warm["pcg_iters"], wall_s=warm["wall_s"],
                                    failed=warm["failed"],
-                                   accepted=sum(i["guess"] == "predicted" for i in warm["increments"])),
+                                   accepted=sum(i["guess"].startswith("candidate") for i in warm["increments"]),
+                                   chosen=[i["guess"] for i in warm["increments"]]),
                          du=float(torch.linalg.norm(warm["u"] - base["u"]) / max(1e-300, float(torch.linalg.norm(base["u"]))))))
     tot = {k: dict(newton=sum(r[k]["newton"] for r in rows), pcg=sum(r[k]["pcg"] for r in rows),
                    wall_s=sum(r[k]["wall_s"] for r in rows), failed=sum(r[k]["failed"] for r in rows))
            for k in ("plain", "warm")}
     tot["warm"]["accepted"] = sum(r["warm"]["accepted"] for r in rows)
+    kinds = {"candidate0": "predicted_state", "candidate1": "predicted_step", "fallback": "previous"}
+    tot["warm"]["chosen"] = {v: sum(c == k for r in rows for c in r["warm"]["chosen"]) for k, v in kinds.items()}
     tot["increments"] = len(rows) * solver.n_increments
     return rows, tot

@@ -174,6 +174,18 @@ int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const
  * in the process. FL_ERR_CAPACITY when the table (64 pairs) is full. */
 int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
 
+/* Arithmetic of the stiffness contraction in every later FP64-valued assembly call of the process
+ * (no reference counterpart; the reference contracts in FP64). FL_ARITH_FP64: FP64 fused
+ * multiply-adds (the default). FL_ARITH_FLOAT_PAIR: each operand held as an unevaluated pair of
+ * floats (hi + lo), products formed error-free in their leading part and summed with a
+ * compensated two-sum on the FP32 pipe, ~2^-46 relative per multiply-add (element matrices
+ * within ~1e-14 of FP64). The kinematics, the material law, the residual and the scatter stay FP64
+ * in both. FL_ERR_ARG for other values. */
+#define FL_ARITH_FP64 0
+#define FL_ARITH_FLOAT_PAIR 1
+int fl_SetAssemblyArithmetic(int arithmetic);
+int fl_GetAssemblyArithmetic(void);
+
 /* ------------------------------------------------------------------------------------------
  * Explicit (matrix-free) internal force, T[nnode*nvar] += sum_e sum_g detJ (grad N_a . sigma).
  * Argument list of the reference's _GlobalAssemblyExplicit_DF_DPF_ plus flags and stream.
@@ -281,11 +293,13 @@ int fl_MLPAdamStep(float *params, const float *grads, float *m, float *v, int64_
                    float beta2, float eps, fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
- * Measurement helper: device time of a dependent FP64 FMA loop over the whole GPU, used to
- * measure the FP64 roof that the assembly kernels are bound by. Synchronises the stream.
- * gflops (host out) = achieved FP64 GFLOP/s (2 flops per FMA).
+ * Measurement helpers: device time of independent FMA chains over the whole GPU, used to measure
+ * the FP64 and FP32 roofs that the assembly kernels are bound by (FP64 arithmetic, and the
+ * float-pair arithmetic on the FP32 pipe). Synchronise the stream. gflops (host out) = achieved
+ * GFLOP/s (2 flops per FMA).
  * ------------------------------------------------------------------------------------------ */
 int fl_measure_fp64_peak(double *gflops, fl_stream_t stream);
+int fl_measure_fp32_peak(double *gflops, fl_stream_t stream);
 
 #ifdef __cplusplus
 }

@@ -14,7 +14,7 @@ def test_warm_start_saves_newton_iterations(tmp_path):
     solver = W.PlateSolver(prob, n_increments=4, tol=1e-10)
     X, U, stats = W.generate_snapshots(solver, W.sample_parameters(32, seed=3))
     assert not any(s["failed"] for s in stats)
-    assert X.shape == (32 * 4, 3) and U.shape == (solver.ndof, 32 * 4)
+    assert X.shape == (32 * 5, 3) and U.shape == (solver.ndof, 32 * 5)
     ws, hist, sv, proj = W.train_warm_start(X, U, modes=64, steps=6000)
     assert hist[-1] < 0.01 * hist[0]
     assert proj < 1e-3
@@ -26,5 +26,5 @@ def test_warm_start_saves_newton_iterations(tmp_path):
     # the checkpoint reproduces the predictions
     W.save(ws, tmp_path / "ws.npz")
     ws2 = W.load(tmp_path / "ws.npz")
-    x = solver.increment_inputs(W.sample_parameters(1, seed=9)[0])
+    x = solver.increment_inputs(W.sample_parameters(1, seed=9)[0], with_zero=True)
     assert torch.allclose(ws.predict(x), ws2.predict(x))
