@@ -349,7 +349,7 @@ def run_newton(args):
     cells = (48, 12, 12) if args.workload != "beam_s" else (24, 6, 6)
     P, el, Jm, w, fixed, f = build_beam_problem(*cells, traction=0.01)
     asm = fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
-    tangents = ["fp64", "mixed"] if args.tangent == "both" else [args.tangent]
+    tangents = {"both": ["fp64", "mixed"], "all": ["fp64", "mixed", "hybrid"]}.get(args.tangent, [args.tangent])
     runs = {}
     for tg in tangents:
         # warm-up: module loading, one assembly and one short linear solve
@@ -358,14 +358,14 @@ def run_newton(args):
                                 max_iter=args.newton_max_iter, forcing=args.forcing).solve()
     out = runs[tangents[-1]]
     extra = {}
-    if len(runs) == 2:
-        a, b = runs["fp64"], runs["mixed"]
-        extra = dict(fp64=dict(wall_s=a["wall_s"], newton_iters=a["newton_iters"], pcg_iters=a["pcg_iters"],
-                               failed=a["failed"]),
-                     mixed=dict(wall_s=b["wall_s"], newton_iters=b["newton_iters"], pcg_iters=b["pcg_iters"],
-                                failed=b["failed"]),
-                     mixed_vs_fp64_rel_l2=float(torch.linalg.vector_norm(b["u"] - a["u"]) /
-                                                torch.linalg.vector_norm(a["u"])))
+    if len(runs) > 1:
+        a = runs["fp64"]
+        for tg, b in runs.items():
+            extra[tg] = dict(wall_s=b["wall_s"], newton_iters=b["newton_iters"], pcg_iters=b["pcg_iters"],
+                             failed=b["failed"])
+            if tg != "fp64":
+                extra[tg]["rel_l2_vs_fp64"] = float(torch.linalg.vector_norm(b["u"] - a["u"]) /
+                                                    torch.linalg.vector_norm(a["u"]))
     u = out["u"].cpu().numpy().reshape(-1, 3)
     tip = np.abs(P[:, 0] - 4.0) < 1e-9
     incs = [dict(increment=i["increment"], newton=i["newton_iters"],
@@ -373,7 +373,9 @@ def run_newton(args):
             for i in out["increments"]]
     line = dict(metric="Newton wall time to rel-res 1e-10 (10 load increments, %s tangent, device PCG)"
                        % {"fp64": "FP64", "mixed": "split-BF16 tensor-core FP32",
-                          "both": "split-BF16 tensor-core FP32 (FP64 run alongside)"}[args.tangent],
+                          "hybrid": "split-BF16 FP32 far from the solution, FP64 near it",
+                          "both": "split-BF16 tensor-core FP32 (FP64 run alongside)",
+                          "all": "hybrid split-BF16/FP64 (FP64 and split-BF16 runs alongside)"}[args.tangent],
                 value=out["wall_s"], unit="s", n_gpus=1, steps=1, warmup=1, higher_is_better=False,
                 scaling="weak", vs_baseline=None, dtype="f64", data="synthetic", tangent=args.tangent,
                 spmv=args.spmv if args.tangent != "mixed" else "fp32 values, float-pair product",
@@ -555,10 +557,13 @@ def run_warmstart(args):
     ws, hist, sv, proj = W.train_warm_start(X, U, modes=64, steps=args.ws_steps)
     torch.cuda.synchronize()
     t3 = time.perf_counter()
-    rows, tot = W.evaluate_warm_start(solver, ws, test)
+    hybrid = W.PlateSolver(prob, n_increments=args.ws_increments, tol=1e-10, tangent="hybrid")
+    hybrid.solve(1.0, 10.0, 0.1)                          # warm-up of the mixed kernels
+    rows, tot = W.evaluate_warm_start(solver, ws, test, {"warm": solver, "mixed_warm": hybrid})
     t4 = time.perf_counter()
-    line = dict(metric="Newton wall time to rel-res 1e-10 over the held-out solves, network warm start",
-                value=tot["warm"]["wall_s"], unit="s", n_gpus=1, steps=len(test), warmup=1,
+    line = dict(metric="Newton wall time to rel-res 1e-10 over the held-out solves: split-BF16/FP64 hybrid "
+                       "tangent with the network warm start (plain FP64 Newton alongside)",
+                value=tot["mixed_warm"]["wall_s"], unit="s", n_gpus=1, steps=len(test), warmup=1,
                 higher_is_better=False, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
                 config=dict(workload="p=2 tet plate 2x1x0.2 (38x19x4 jittered lattice), neo-Hookean mu~U(0.5,2) "
                                      "lambda/mu~U(2,100), traction~U(0,0.5) (+x) on x=2, x=0 clamped, "
@@ -566,10 +571,11 @@ def run_warmstart(args):
                             nelem=int(prob[1].shape[0]), nnode=int(prob[0].shape[0]), train_solves=len(train),
                             test_solves=len(test), snapshots=int(U.shape[1]), pod_modes=64,
                             network="3-256-256-64 GELU, BF16 operands, FP32 master, Adam"),
-                plain=tot["plain"], warm=tot["warm"], increments=tot["increments"],
+                plain=tot["plain"], warm=tot["warm"], mixed_warm=tot["mixed_warm"], increments=tot["increments"],
                 newton_ratio=tot["warm"]["newton"] / max(1, tot["plain"]["newton"]),
-                wall_ratio=tot["warm"]["wall_s"] / max(1e-12, tot["plain"]["wall_s"]),
-                max_solution_diff=max(r["du"] for r in rows),
+                wall_ratio_warm=tot["warm"]["wall_s"] / max(1e-12, tot["plain"]["wall_s"]),
+                wall_ratio_mixed_warm=tot["mixed_warm"]["wall_s"] / max(1e-12, tot["plain"]["wall_s"]),
+                max_solution_diff=max(tot["warm"]["max_du"], tot["mixed_warm"]["max_du"]),
                 training=dict(failed=sum(s_["failed"] for s_ in stats), generate_s=t2 - t1, train_s=t3 - t2,
                               evaluate_s=t4 - t3, loss_first=hist[0], loss_last=hist[-1], pod_projection_err=proj,
                               sv_ratio_64=float(sv[-1] / sv[0])))
@@ -590,8 +596,9 @@ def main():
     ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")
     ap.add_argument("--explicit", action="store_true", help="explicit dynamics of the hex beam instead")
     ap.add_argument("--explicit-steps", type=int, default=10000)
-    ap.add_argument("--tangent", default="fp64", choices=["fp64", "mixed", "both"],
-                    help="Newton Jacobian (both: FP64 then mixed, with the difference of the solutions)")
+    ap.add_argument("--tangent", default="fp64", choices=["fp64", "mixed", "hybrid", "both", "all"],
+                    help="Newton Jacobian (both: FP64 then mixed; all: FP64, mixed, hybrid; with the "
+                         "differences of the solutions)")
     ap.add_argument("--newton-max-iter", type=int, default=25,
                     help="Newton iterations per increment before failing (small values give a short profile run)")
     ap.add_argument("--forcing", default="ew", choices=["ew", "rel"],

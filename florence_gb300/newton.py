@@ -66,7 +66,7 @@ class NewtonSolver:
 
     def __init__(self, asm, fixed, f_ext, n_increments=10, tol=1e-10, max_iter=25, pcg_maxiter=50000,
                  eta_max=1e-2, eta_min=1e-12, tangent="fp64", criterion="reference", spmv="split",
-                 forcing="ew", eta0=1e-3):
+                 forcing="ew", eta0=1e-3, hybrid_switch=1e-2):
         if asm.mode != "csr":
             raise ValueError("Newton needs the CSR tangent (mode='csr')")
         self.asm = asm
@@ -82,16 +82,24 @@ class NewtonSolver:
         self.eta_min = eta_min
         self.X = asm.points.reshape(-1)
         n = asm.nnode * 3
-        if tangent not in ("fp64", "mixed"):
-            raise ValueError("tangent must be 'fp64' or 'mixed'")
+        if tangent not in ("fp64", "mixed", "hybrid"):
+            raise ValueError("tangent must be 'fp64', 'mixed' or 'hybrid'")
+        # "hybrid": the split-BF16 tensor-core Jacobian (FP32 values) while the residual is above
+        # hybrid_switch x the increment's load, the FP64 Jacobian below. Far from the solution
+        # the FP32 Jacobian's error (~1e-7 relative, amplified by the condition number) is small
+        # against the Newton step's own linearisation error, and its PCG products move half the
+        # bytes; close to the solution it would turn Newton's quadratic convergence linear.
         self.tangent = tangent
+        self.hybrid_switch = hybrid_switch
         if criterion not in ("reference", "load"):
             raise ValueError("criterion must be 'reference' or 'load'")
         # "reference": |R| relative to its value after the first update of the increment (the
         # reference's NormForces); "load": |R| relative to the increment's external load, a test
         # that does not depend on how good the initial state was (used to compare warm starts)
         self.criterion = criterion
-        self.V = torch.zeros(asm.nnz, dtype=torch.float64 if tangent == "fp64" else torch.float32, device=dev)
+        self.V64 = torch.zeros(asm.nnz, dtype=torch.float64, device=dev) if tangent != "mixed" else None
+        self.V32 = torch.zeros(asm.nnz, dtype=torch.float32, device=dev) if tangent != "fp64" else None
+        self.V = self.V64 if tangent != "mixed" else self.V32
         self.T = torch.zeros(n, dtype=torch.float64, device=dev)
         self.spmv = spmv
         if forcing not in ("ew", "rel"):
@@ -103,16 +111,30 @@ class NewtonSolver:
         # below half of what the convergence test still needs.
         self.forcing = forcing
         self.eta0 = eta0
-        self.ws = pcg_workspace(asm, self.V, spmv)
+        self.ws = pcg_workspace(asm, self.V, spmv)   # the FP64 workspace is the larger one
         self.history = []
 
-    def _assemble(self, u):
+    def _assemble(self, u, mixed=None):
+        """Tangent and residual at u; mixed selects the FP32 tensor-core Jacobian (default: as
+        the tangent option says; "hybrid" keeps the Jacobian it currently uses)."""
+        if mixed is None:
+            mixed = self.tangent == "mixed" or (self.tangent == "hybrid" and self.V is self.V32)
+        self.V = self.V32 if mixed else self.V64
         self.V.zero_()
         self.T.zero_()
-        if self.tangent == "fp64":
+        if not mixed:
             self.asm.assemble((self.X + u).reshape(-1, 3), V=self.V, T=self.T)
         else:  # FP32 Jacobian from the tensor cores, FP64 residual
             self.asm.assemble_mixed((self.X + u).reshape(-1, 3), V32=self.V, T=self.T)
+
+    def _set_jacobian(self, u, absn, ref):
+        """hybrid: the FP32 Jacobian while |R| > hybrid_switch * ref, FP64 below (re-assembles
+        at u when the choice changes)."""
+        if self.tangent != "hybrid":
+            return
+        want_mixed = absn > self.hybrid_switch * ref
+        if want_mixed != (self.V is self.V32):
+            self._assemble(u, mixed=want_mixed)
 
     def residual_norm(self, F):
         return float(torch.linalg.vector_norm((self.T - F) * self.free))
@@ -161,6 +183,7 @@ class NewtonSolver:
             r_before = float(torch.linalg.vector_norm(R))
             iters = []
             while True:
+                self._set_jacobian(u, r_before, norm_load)
                 du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
                                      workspace=self.ws, spmv=self.spmv)
                 total_pcg += pits
@@ -173,7 +196,8 @@ class NewtonSolver:
                 elif it == 0:
                     norm_forces = absn if absn != 0.0 else 1e-14
                 rel = abs(absn / norm_forces)
-                iters.append(dict(iter=it, abs=absn, rel=rel, pcg_iters=pits, pcg_relres=prel, eta=eta))
+                iters.append(dict(iter=it, abs=absn, rel=rel, pcg_iters=pits, pcg_relres=prel, eta=eta,
+                                  jacobian="fp32" if self.V is self.V32 else "fp64"))
                 if absn < self.tol:
                     break
                 it += 1

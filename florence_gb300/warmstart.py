@@ -3,9 +3,11 @@
 The method generates its own training data: converged increments of Newton solves over a range
 of (material, load) parameters. A 64-mode POD basis of the converged displacements is built by
 the method of snapshots, and an MLP 3 -> 256 -> 256 -> 64 (GELU, BF16 arithmetic, FP32 master
-weights, Adam; kernels in csrc/fl_mlp.cu) maps the normalised parameters to the normalised POD
-coefficients. At solve time the prediction is a candidate initial state for Newton; the FP64
-residual judges it against the previous-increment guess, and the better one is used.
+weights, Adam; kernels in csrc/fl_mlp.cu) maps three features of the parameters (t/mu, Poisson's
+ratio, mu) to the POD coefficients of the displacement per unit load-to-stiffness ratio t/mu. At
+solve time the prediction gives two candidate initial states for each increment (the predicted
+state, and the previous solution moved by the predicted step); the FP64 residual judges them
+against the previous-increment guess, which is the fallback.
 """
 import time
 
@@ -108,29 +110,46 @@ def pod_basis(U, modes=64):
     return Phi, out
 
 
+def features(x):
+    """Network inputs from (mu, lambda/mu, traction): the load-to-stiffness ratio t/mu, Poisson's
+    ratio nu = r / (2 (r + 1)) (the small-strain response is (t/mu) g(nu)), and mu."""
+    mu, r, t = x[:, 0], x[:, 1], x[:, 2]
+    return torch.stack([t / mu, r / (2.0 * (r + 1.0)), mu], 1)
+
+
 class WarmStart:
-    """POD + MLP predictor u(params). Inputs are standardised per parameter; the POD
-    coefficients are centred and divided by ONE common scale, so that the training loss is the
-    squared displacement error (the basis is orthonormal) and the small, hard-to-predict trailing
-    modes weigh what they weigh in the displacement."""
+    """POD + MLP predictor u(params) = (t/mu) Phi c(features).
+
+    The network maps the three features to the POD coefficients of u / (t/mu): the displacement
+    per unit load-to-stiffness ratio, an O(1) shape that varies smoothly with nu and the
+    nonlinearity, instead of u itself, whose size spans the whole load range (and which is 0 at
+    zero load exactly, by construction). Inputs are standardised per feature; the targets are
+    centred and divided by one common scale, so that the training loss is the squared
+    displacement error per unit t/mu (the basis is orthonormal)."""
 
     def __init__(self, Phi, X, C, seed=0):
         self.Phi = Phi                                  # [n, 64] FP64
-        self.xm, self.xs = X.mean(0), X.std(0) + 1e-12
-        self.cm = C.mean(0)
-        self.cs = torch.sqrt(((C - self.cm) ** 2).sum(1).mean()) + 1e-300
+        F, Y = self._targets(X, C)
+        self.fm, self.fs = F.mean(0), F.std(0) + 1e-12
+        self.ym = Y.mean(0)
+        self.ys = torch.sqrt(((Y - self.ym) ** 2).sum(1).mean()) + 1e-300
         self.net = MLP(seed=seed, device=Phi.device)
 
+    @staticmethod
+    def _targets(X, C):
+        s = X[:, 2] / X[:, 0]
+        keep = s > 0                                    # zero-load states carry no shape
+        return features(X[keep]), C[keep] / s[keep, None]
+
     def fit(self, X, C, **kw):
-        Xn = ((X - self.xm) / self.xs).float()
-        Cn = ((C - self.cm) / self.cs).float()
-        return self.net.train(Xn, Cn, **kw)
+        F, Y = self._targets(X, C)
+        return self.net.train(((F - self.fm) / self.fs).float(), ((Y - self.ym) / self.ys).float(), **kw)
 
     def predict(self, x):
-        """x: [3] or [B,3] parameters -> displacement [n] or [B,n] (FP64)."""
+        """x: [3] or [B,3] parameters (mu, lambda/mu, traction) -> displacement [n] or [B,n] (FP64)."""
         x = torch.as_tensor(x, dtype=torch.float64, device=self.Phi.device).reshape(-1, 3)
-        c = self.net.forward(((x - self.xm) / self.xs).float()).double() * self.cs + self.cm
-        u = c @ self.Phi.T
+        y = self.net.forward(((features(x) - self.fm) / self.fs).float()).double() * self.ys + self.ym
+        u = (y * (x[:, 2] / x[:, 0])[:, None]) @ self.Phi.T
         return u[0] if u.shape[0] == 1 else u
 
 
@@ -221,50 +240,58 @@ def train_warm_start(X, U, modes=64, steps=20000, batch=64, lr=2e-3, seed=0):
 
 def save(ws, path):
     """Checkpoint of a trained warm start: POD basis, normalisation and FP32 master weights."""
-    np.savez(path, Phi=ws.Phi.cpu().numpy(), xm=ws.xm.cpu().numpy(), xs=ws.xs.cpu().numpy(),
-             cm=ws.cm.cpu().numpy(), cs=ws.cs.cpu().numpy(), params=ws.net.params.cpu().numpy())
+    np.savez(path, Phi=ws.Phi.cpu().numpy(), fm=ws.fm.cpu().numpy(), fs=ws.fs.cpu().numpy(),
+             ym=ws.ym.cpu().numpy(), ys=ws.ys.cpu().numpy(), params=ws.net.params.cpu().numpy())
 
 
 def load(path, device="cuda"):
     d = np.load(path)
     dev = torch.device(device)
-    t = {k: torch.as_tensor(d[k], device=dev) for k in ("Phi", "xm", "xs", "cm", "cs")}
+    t = {k: torch.as_tensor(d[k], device=dev) for k in ("Phi", "fm", "fs", "ym", "ys")}
     ws = WarmStart.__new__(WarmStart)
-    ws.Phi, ws.xm, ws.xs, ws.cm, ws.cs = t["Phi"], t["xm"], t["xs"], t["cm"], t["cs"]
+    ws.Phi, ws.fm, ws.fs, ws.ym, ws.ys = t["Phi"], t["fm"], t["fs"], t["ym"], t["ys"]
     ws.net = MLP(device=dev)
     ws.net.params.copy_(torch.as_tensor(d["params"], device=dev))
     return ws
 
 
-def evaluate_warm_start(solver, ws, params):
-    """Each held-out parameter set solved twice: from the previous increment's solution (the
-    plain method) and from the network's prediction (kept only if its residual is smaller).
-    Returns per-set records and totals."""
+def evaluate_warm_start(solver, ws, params, warm_solvers=None):
+    """Each held-out parameter set solved from the previous increment's solution (the plain
+    method, `solver`) and, with every solver in warm_solvers (name -> PlateSolver; default
+    {"warm": solver}), from the network's prediction, each candidate kept only if its FP64
+    residual beats the previous increment's. Returns per-set records and totals per variant;
+    "du" is each variant's converged displacement against the plain one (relative L2)."""
+    warm_solvers = warm_solvers or {"warm": solver}
     rows = []
     for prm in params:
         inputs = solver.increment_inputs(prm, with_zero=True)
         base = solver.solve(*prm)
-        t0 = time.perf_counter()
-        pred = ws.predict(inputs).reshape(len(inputs), -1)   # [1 + n_increments, ndof], one forward
-        torch.cuda.synchronize()
-        t_pred = time.perf_counter() - t0
-        # candidates: the predicted state, and the previous solution moved by the predicted step
-        # (the network's error largely cancels in the step)
-        warm = solver.solve(*prm, guesses=lambda inc, u_prev: [pred[inc], u_prev + (pred[inc] - pred[inc - 1])])
-        warm["wall_s"] += t_pred
-        rows.append(dict(params=list(map(float, prm)),
-                         plain=dict(newton=base["newton_iters"], pcg=base["pcg_iters"], wall_s=base["wall_s"],
-                                    failed=base["failed"]),
-                         warm=dict(newton=warm["newton_iters"], pcg=warm["pcg_iters"], wall_s=warm["wall_s"],
-                                   failed=warm["failed"],
-                                   accepted=sum(i["guess"].startswith("candidate") for i in warm["increments"]),
-                                   chosen=[i["guess"] for i in warm["increments"]]),
-                         du=float(torch.linalg.norm(warm["u"] - base["u"]) / max(1e-300, float(torch.linalg.norm(base["u"]))))))
+        row = dict(params=list(map(float, prm)),
+                   plain=dict(newton=base["newton_iters"], pcg=base["pcg_iters"], wall_s=base["wall_s"],
+                              failed=base["failed"]))
+        for name, ws_solver in warm_solvers.items():
+            t0 = time.perf_counter()
+            pred = ws.predict(inputs).reshape(len(inputs), -1)   # [1 + n_increments, ndof], one forward
+            torch.cuda.synchronize()
+            t_pred = time.perf_counter() - t0
+            # candidates: the predicted state, and the previous solution moved by the predicted step
+            # (the network's error largely cancels in the step)
+            warm = ws_solver.solve(*prm, guesses=lambda inc, u_prev: [pred[inc], u_prev + (pred[inc] - pred[inc - 1])])
+            row[name] = dict(newton=warm["newton_iters"], pcg=warm["pcg_iters"], wall_s=warm["wall_s"] + t_pred,
+                             failed=warm["failed"],
+                             accepted=sum(i["guess"].startswith("candidate") for i in warm["increments"]),
+                             chosen=[i["guess"] for i in warm["increments"]],
+                             du=float(torch.linalg.norm(warm["u"] - base["u"]) /
+                                      max(1e-300, float(torch.linalg.norm(base["u"])))))
+        rows.append(row)
+    names = ["plain"] + list(warm_solvers)
     tot = {k: dict(newton=sum(r[k]["newton"] for r in rows), pcg=sum(r[k]["pcg"] for r in rows),
                    wall_s=sum(r[k]["wall_s"] for r in rows), failed=sum(r[k]["failed"] for r in rows))
-           for k in ("plain", "warm")}
-    tot["warm"]["accepted"] = sum(r["warm"]["accepted"] for r in rows)
+           for k in names}
     kinds = {"candidate0": "predicted_state", "candidate1": "predicted_step", "fallback": "previous"}
-    tot["warm"]["chosen"] = {v: sum(c == k for r in rows for c in r["warm"]["chosen"]) for k, v in kinds.items()}
+    for k in warm_solvers:
+        tot[k]["accepted"] = sum(r[k]["accepted"] for r in rows)
+        tot[k]["chosen"] = {v: sum(c == kk for r in rows for c in r[k]["chosen"]) for kk, v in kinds.items()}
+        tot[k]["max_du"] = max(r[k]["du"] for r in rows)
     tot["increments"] = len(rows) * solver.n_increments
     return rows, tot

@@ -67,7 +67,7 @@ def test_csr_assembly_matches_reference(fl, case, mode):
 def test_float_pair_contraction_matches_reference(fl, case, mode):
     """The contraction in float-pair arithmetic on the FP32 pipe meets the FP64 path's bar
     (1e-12 relative Frobenius against the reference) in every scatter mode; the residual is
-    FP64 and identical to the FP64-arithmetic run."""
+    formed in FP64 as before (equal to the FP64 run's up to the order of the atomic sums)."""
     d = load_golden(case)
     asm = _asm(fl, d, mode)
     x = torch.from_numpy(d["Eulerx"]).cuda()
@@ -78,7 +78,8 @@ def test_float_pair_contraction_matches_reference(fl, case, mode):
     assert fl.get_arithmetic() == "fp64"
     asm.check_flags()
     V, T = out[-2], out[-1]
-    assert torch.equal(T, out64[-1])
+    assert rel_fro(T.cpu().numpy(), out64[-1].cpu().numpy()) < 1e-14
+    assert rel_fro(T.cpu().numpy(), d["T"]) < TOL
     if mode == "triplet":
         I, J = out[0].cpu().numpy(), out[1].cpu().numpy()
         n = d["points"].shape[0] * 3

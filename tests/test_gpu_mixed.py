@@ -58,12 +58,18 @@ def test_pcg_with_fp32_values_matches_fp64_values():
     assert rel_fro(x32.cpu().numpy(), x64.cpu().numpy()) < 5e-3
 
 
-def test_newton_mixed_reaches_fp64_solution():
+@pytest.mark.parametrize("tangent", ["mixed", "hybrid"])
+def test_newton_mixed_reaches_fp64_solution(tangent):
+    """The split-BF16 Jacobian throughout, or only while the residual is above 1e-2 of the
+    load (hybrid), converges to the FP64 Newton's displacement; the hybrid run's log shows both
+    Jacobians in use."""
     import florence_gb300 as fl
     from florence_gb300.newton import NewtonSolver, build_beam_problem
     P, el, Jm, w, fixed, f = build_beam_problem(nx=8, ny=2, nz=2, traction=0.01)
     asm = fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
     r64 = NewtonSolver(asm, fixed, f, n_increments=3, tol=1e-10, tangent="fp64").solve()
-    rmx = NewtonSolver(asm, fixed, f, n_increments=3, tol=1e-10, tangent="mixed").solve()
+    rmx = NewtonSolver(asm, fixed, f, n_increments=3, tol=1e-10, tangent=tangent).solve()
     assert not r64["failed"] and not rmx["failed"]
     assert rel_fro(rmx["u"].cpu().numpy(), r64["u"].cpu().numpy()) < 1e-8
+    used = {h["jacobian"] for i in rmx["increments"] for h in i["history"]}
+    assert used == ({"fp32"} if tangent == "mixed" else {"fp32", "fp64"})
