@@ -264,13 +264,13 @@ def _low_level_df(name, fem_solver, function_space, formulation, mesh, material,
     _check_formulation(formulation, material)
     mat_id, params = material_params(material, name)
     recompute = bool(fem_solver.recompute_sparsity_pattern)
-    squeeze = bool(getattr(fem_solver, "squeeze_sparsity_pattern", False))
-    mode = "triplet" if recompute else ("squeeze" if squeeze else "csr")
+    # CSR output with or without the reference's element-to-nonzero maps: the device scatter
+    # finds every entry's position in the pattern itself (one row search per node pair), which
+    # lands each value where the maps would and spares uploading the two E*ndof^2 maps per call
+    mode = "triplet" if recompute else "squeeze"
     sparsity = None
     if not recompute:
-        sparsity = (fem_solver.indices, fem_solver.indptr,
-                    None if squeeze else fem_solver.data_local_indices,
-                    None if squeeze else fem_solver.data_global_indices)
+        sparsity = (fem_solver.indices, fem_solver.indptr, None, None)
     asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, name, params,
                           mode=mode, requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity)
     x = _to_dev(Eulerx, torch.float64, asm.device)
