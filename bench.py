@@ -245,7 +245,8 @@ def run_ours(args):
     asm = fl.DeviceAssembler(W["points"], W["elements"], W["Jm"], W["w"], W["material"], W["params"], mode="csr",
                              device=dev)
     x = torch.from_numpy(W["x"]).to(dev)
-    V = torch.zeros(asm.nnz, dtype=torch.float64, device=dev)
+    mixed = args.arith == "mixed"
+    V = torch.zeros(asm.nnz, dtype=torch.float32 if mixed else torch.float64, device=dev)
     T = torch.zeros(nnode * 3, dtype=torch.float64, device=dev)
     stream = torch.cuda.current_stream(dev)
 
@@ -254,11 +255,14 @@ def run_ours(args):
         T.zero_()
         if ev is not None:
             ev[0].record(stream)
-        asm.assemble(x, V=V, T=T)
+        if mixed:
+            asm.assemble_mixed(x, V32=V, T=T)
+        else:
+            asm.assemble(x, V=V, T=T)
         if ev is not None:
             ev[1].record(stream)
 
-    fl.set_arithmetic(args.arith)
+    fl.set_arithmetic("fp64" if mixed else args.arith)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -296,6 +300,16 @@ def run_ours(args):
                         peak_source="FP64 FMA microkernel measured in this run (no FP64 figure in "
                                     "MEASURED_PEAKS.json)",
                         executed_frac=f_exe / (kernel_ms * 1e-3) / 1e12 / fp64_peak)
+    elif mixed:  # split-BF16 tangent: six BF16 MMA products per element contraction
+        npad = (npe + 7) // 8 * 8
+        kpad = (3 * nq + 15) // 16 * 16
+        tflop = 6 * 2.0 * (9 * npe) * npad * kpad * nelem / (kernel_ms * 1e-3) / 1e12
+        peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+        bf16_peak = peaks.get("bf16_tflops", 1900.0)
+        roofline = dict(bound="tensor", achieved=tflop, peak=bf16_peak, unit="TFLOP/s", frac=tflop / bf16_peak,
+                        peak_source="MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
+                        note="the tensor work per element is small; the FP64 Gauss-point kernel and the scatter "
+                             "bound the step", fp64_equivalent_tflops=achieved)
     else:  # the contraction runs as float pairs on the FP32 pipe
         instr = 12.0 * pair_macs(npe, nq) * nelem
         ach_i = instr / (kernel_ms * 1e-3) / 1e12
@@ -304,8 +318,8 @@ def run_ours(args):
                         peak_source="FP32 FMA microkernel measured in this run (instructions/s = FLOP/s / 2)",
                         fp64_equivalent_tflops=achieved, fp64_equivalent_frac=achieved / fp64_peak,
                         instr_per_launch=instr)
-    tag = "assemble_df_%s_%s%s" % (W["desc"]["element"], W["desc"]["material"],
-                                   "" if args.arith == "fp64" else "_float_pair")
+    tag = {"fp64": "assemble_df_%s_%s", "float_pair": "contract_float_pair_%s_%s",
+           "mixed": "contract_mixed_%s_%s"}[args.arith] % (W["desc"]["element"], W["desc"]["material"])
     roofline.update(traffic=traffic_from_profile(tag), flop_alg_per_launch=f_alg, flop_executed_per_launch=f_exe,
                     kernel_ms=kernel_ms,
                     hbm=dict(bytes_min_per_launch=bmin, achieved_gbs=bmin / (kernel_ms * 1e-3) / 1e9,
@@ -314,7 +328,7 @@ def run_ours(args):
 
     # end to end through the drop-in callable (host numpy in and out, copies inside)
     e2e = None
-    if rank == 0 and not args.no_e2e:
+    if rank == 0 and not args.no_e2e and not mixed:  # the drop-in returns the FP64 tangent
         e2e = e2e_dropin(W, asm, args)
 
     cpu = None
@@ -325,10 +339,13 @@ def run_ours(args):
         cpu = dict(value=v, unit="Melem/s", cores=cores, kind="port", sample=sample)
 
     if rank == 0:
-        line = dict(metric="FP64 assembly throughput (tangent CSR + residual)", value=value, unit="Melem/s",
-                    arithmetic=args.arith,
+        line = dict(metric="FP64 assembly throughput (tangent CSR + residual)" if not mixed else
+                    "split-BF16 tangent assembly throughput (FP32 CSR values + FP64 residual)",
+                    value=value, unit="Melem/s", arithmetic=args.arith,
                     n_gpus=world, steps=args.steps, warmup=args.warmup, ms_per_step=ms / args.steps,
-                    higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                    higher_is_better=True, scaling="weak", vs_baseline=None,
+                    dtype={"fp64": "f64", "float_pair": "f64 (float-pair contraction)",
+                           "mixed": "bf16x3 products, f32 accumulate; f64 residual"}[args.arith], data="synthetic",
                     config=dict(W["desc"], nelem=int(nelem), nnode=int(nnode), nnz=int(asm.nnz), gauss_points=nq,
                                 parallelism="replicas" if world > 1 else "single GPU",
                                 l2="inputs larger than L2: CSR values %.0f MB and element-to-nonzero map %.0f MB "
@@ -590,8 +607,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
-    ap.add_argument("--arith", default="fp64", choices=["fp64", "float_pair"],
-                    help="arithmetic of the stiffness contraction (FP64, or float pairs on the FP32 pipe)")
+    ap.add_argument("--arith", default="fp64", choices=["fp64", "float_pair", "mixed"],
+                    help="arithmetic of the stiffness contraction (FP64, float pairs on the FP32 pipe, or the "
+                         "split-BF16 tensor-core tangent with FP32 values)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")

@@ -65,6 +65,7 @@ struct AsmArgs {
     const double *eparams;  // optional per-element material parameters [nelem][3] (overrides mp)
     int *flags;
     double *Q;       // scratch [QSTRIDE][ldq]
+    const float *Jmf;  // FP32 copy of Jm (the split-BF16 tangent's operand), or null
     int64_t e0, ne;  // element chunk [e0, e0+ne)
     int64_t ldq;     // leading dimension of Q (>= ne*nq)
 };
@@ -96,9 +97,8 @@ __device__ __forceinline__ int64_t block_entry(const int32_t *indptr, const int3
 }
 
 // index of (I,K), I,K in 0..8, in the packed upper triangle of a symmetric 9x9
-__device__ __forceinline__ int sym9(int I, int K) {
-    const int r = I < K ? I : K, c = I < K ? K : I;
-    return r * 9 - (r * (r - 1)) / 2 + (c - r);
+__host__ __device__ __forceinline__ constexpr int sym9(int I, int K) {
+    return (I < K ? I : K) * 9 - ((I < K ? I : K) * ((I < K ? I : K) - 1)) / 2 + ((I < K ? K : I) - (I < K ? I : K));
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -325,17 +325,31 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, DF ? AsmC
             }
             __syncthreads();
             if (active) {
-                for (int idx = lt; idx < qc * NPE * 27; idx += TPE) {
-                    const int q = idx / (NPE * 27), r = idx % (NPE * 27), b = r / 27, s = r % 27;
-                    const int I = s / 3, k = s % 3;  // s = (i*3+d)*3 + k, I = i*3+d
+                // U_g[b][(i,d),k] for one (Gauss point, node b, component i) per work item: the
+                // nine entries of row block i, with compile-time indices into the packed tensor
+                for (int it = lt; it < qc * NPE * 3; it += TPE) {
+                    const int i = it % 3, qb = it / 3, q = qb / NPE, b = qb % NPE;
                     const S *qq = Qs + ((size_t)slot * nq + c0 + q) * QSM;
                     const S *jb = Jc + (q * NPE + b) * 3;
-                    Acc u;
-                    AR::zero(u);
-                    AR::mac(u, qq[sym9(I, k * 3 + 2)], jb[2]);
-                    AR::mac(u, qq[sym9(I, k * 3 + 1)], jb[1]);
-                    AR::mac(u, qq[sym9(I, k * 3 + 0)], jb[0]);
-                    Us[(((size_t)slot * QC + q) * NPE + b) * 27 + s] = AR::store(u);
+                    const S j0 = jb[0], j1 = jb[1], j2 = jb[2];
+                    S *uo = Us + (((size_t)slot * QC + q) * NPE + b) * 27;
+#pragma unroll
+                    for (int ii = 0; ii < 3; ++ii) {
+                        if (ii != i) continue;
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            const int I = ii * 3 + d;
+#pragma unroll
+                            for (int k = 0; k < 3; ++k) {
+                                Acc u;
+                                AR::zero(u);
+                                AR::mac(u, qq[sym9(I, k * 3 + 2)], j2);
+                                AR::mac(u, qq[sym9(I, k * 3 + 1)], j1);
+                                AR::mac(u, qq[sym9(I, k * 3 + 0)], j0);
+                                uo[I * 3 + k] = AR::store(u);
+                            }
+                        }
+                    }
                 }
             }
             __syncthreads();
@@ -537,6 +551,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.elements = elements;
     A.Eulerx = Eulerx;
     A.Jm = Jm;
+    A.Jmf = nullptr;
     A.w = AllGauss;
     A.nelem = nelem;
     A.nnode = nnode;
@@ -608,14 +623,19 @@ __device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+__global__ void to_float(const double *a, float *b, int64_t n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) b[i] = (float)a[i];
+}
+
 template <int NPE>
 __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, float *V32) {
     constexpr int NDOF = 3 * NPE, M = 9 * NPE, NP = (NPE + 7) / 8 * 8, NT8 = NP / 8;
     constexpr int AST = MX_KC + 8;  // padded row stride (bf16) of the A chunk
     const int nq = A.nq, K = 3 * nq;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double *Qs = reinterpret_cast<double *>(smem_raw);                              // [nq][QSM]
-    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + (size_t)nq * QSM);      // [3][MX_MC][AST]
+    float *Qs = reinterpret_cast<float *>(smem_raw);                                // [nq][QSM]
+    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + ((size_t)nq * QSM + 3) / 4 * 4);  // [3][MX_MC][AST]
     __nv_bfloat16 *Am = Ah + MX_MC * AST;
     __nv_bfloat16 *Al = Am + MX_MC * AST;
     __nv_bfloat16 *Bh = Al + MX_MC * AST;                                            // [3][NP][AST]
@@ -654,7 +674,7 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
         const double *q = A.Q + el * nq;
         for (int idx = tid; idx < nq * QSM; idx += MX_NT) {
             const int k = idx / nq, g = idx % nq;
-            Qs[(size_t)g * QSM + k] = q[k * A.ldq + g];
+            Qs[(size_t)g * QSM + k] = (float)q[k * A.ldq + g];
         }
         __syncthreads();
         if (!A.dl)  // offset of column node b in row node a; consecutive threads share a row
@@ -690,10 +710,10 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                     if (r < M && cc < kc) {
                         const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
                         const int g = c / 3, d = c % 3, I = i * 3 + d;
-                        const double *qq = Qs + (size_t)g * QSM;
-                        v = (float)fma(qq[sym9(I, k * 3 + 0)], __ldg(A.Jm + ((size_t)0 * NPE + b) * nq + g),
-                                       fma(qq[sym9(I, k * 3 + 1)], __ldg(A.Jm + ((size_t)1 * NPE + b) * nq + g),
-                                           qq[sym9(I, k * 3 + 2)] * __ldg(A.Jm + ((size_t)2 * NPE + b) * nq + g)));
+                        const float *qq = Qs + (size_t)g * QSM;  // U in FP32: the tangent's target accuracy
+                        v = fmaf(qq[sym9(I, k * 3 + 0)], __ldg(A.Jmf + ((size_t)0 * NPE + b) * nq + g),
+                                 fmaf(qq[sym9(I, k * 3 + 1)], __ldg(A.Jmf + ((size_t)1 * NPE + b) * nq + g),
+                                      qq[sym9(I, k * 3 + 2)] * __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g)));
                     }
                     bf16_split3(v, Ah[rr * AST + cc], Am[rr * AST + cc], Al[rr * AST + cc]);
                 }
@@ -701,7 +721,7 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                 for (int idx = tid; idx < NP * kcp; idx += MX_NT) {
                     const int n = idx / kcp, cc = idx % kcp, c = k0 + cc;
                     float v = 0.f;
-                    if (n < NPE && cc < kc) v = (float)__ldg(A.Jm + ((size_t)(c % 3) * NPE + n) * nq + c / 3);
+                    if (n < NPE && cc < kc) v = __ldg(A.Jmf + ((size_t)(c % 3) * NPE + n) * nq + c / 3);
                     bf16_split3(v, Bh[n * AST + cc], Bm[n * AST + cc], Bl[n * AST + cc]);
                 }
                 __syncthreads();
@@ -768,7 +788,8 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
 template <int NPE>
 static size_t mixed_smem_bytes(int nq) {
     constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
-    return sizeof(double) * (size_t)nq * QSM + sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
+    return sizeof(float) * (((size_t)nq * QSM + 3) / 4 * 4) +
+           sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
            sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
 }
 
@@ -780,10 +801,15 @@ static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
     { const int st = ensure_smem<contract_mixed_kernel<NPE>>(smem); if (st != FL_OK) return st; }
     int64_t chunk = chunk_elements(CHUNK_BYTES, A.nq, 1);
     if (chunk > A.nelem) chunk = A.nelem;
-    double *Q = nullptr;
-    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sizeof(double) * QSTRIDE * (size_t)A.nq * chunk, stream));
+    double *Q = nullptr;  // Gauss-point scratch, then the FP32 copy of Jm
+    const size_t qbytes = (sizeof(double) * QSTRIDE * (size_t)A.nq * chunk + 255) & ~(size_t)255;
+    const int64_t njm = (int64_t)3 * NPE * A.nq;
+    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, qbytes + sizeof(float) * (size_t)njm, stream));
     A.Q = Q;
     A.ldq = chunk * A.nq;
+    float *Jmf = reinterpret_cast<float *>(reinterpret_cast<char *>(Q) + qbytes);
+    to_float<<<(unsigned)((njm + 255) / 256), 256, 0, stream>>>(A.Jm, Jmf, njm);
+    A.Jmf = Jmf;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -875,6 +901,7 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.elements = elements;
     A.Eulerx = Eulerx;
     A.Jm = Jm;
+    A.Jmf = nullptr;
     A.w = AllGauss;
     A.nelem = nelem;
     A.nnode = nnode;
