@@ -446,7 +446,8 @@ def run_batched(args):
     """512 independent cube meshes (n^3 hexes, n ~ U{2..12}, p ~ U{1..4}, per-instance neo-Hookean
     parameters, displacement U(-0.01, 0.01)): FP64 tangent + residual of all instances, one
     launch pair per element order and sub-batch (sub-batches keep CSR values and indices under a
-    memory budget), Gauss-point chunk autotuned per order; then the split-BF16 variant."""
+    memory budget and below 2^31 nonzeros), Gauss-point chunk autotuned per order; then the
+    split-BF16 variant."""
     import torch
     from florence_gb300.batched import BatchedAssembler, build_instance, config4_instances, hex_tables
     specs = config4_instances(args.instances, seed=2)
@@ -458,9 +459,10 @@ def run_batched(args):
     for p in (1, 2, 3, 4):
         pat, Jm, w = hex_tables(p)
         group, gbytes, groups = [], 0.0, []
+        nnz_cap = 1.8e9          # int32 CSR positions: a sub-batch stays below 2^31 nonzeros
         for sp in [s_ for s_ in specs if s_["p"] == p]:
             b = sp["n"] ** 3 * nnz_per_elem[p] * 16.0
-            if group and gbytes + b > budget:
+            if group and (gbytes + b > budget or (gbytes + b) / 16.0 > nnz_cap):
                 groups.append(group)
                 group, gbytes = [], 0.0
             group.append(sp)

@@ -321,5 +321,6 @@ def evaluate_warm_start(solver, ws, params, warm_solvers=None):
         tot[k]["accepted"] = sum(r[k]["accepted"] for r in rows)
         tot[k]["chosen"] = {v: sum(c == kk for r in rows for c in r[k]["chosen"]) for kk, v in kinds.items()}
         tot[k]["max_du"] = max(r[k]["du"] for r in rows)
+        tot[k]["median_du"] = float(np.median([r[k]["du"] for r in rows]))
     tot["increments"] = len(rows) * solver.n_increments
     return rows, tot
