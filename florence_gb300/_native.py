@@ -19,6 +19,8 @@ FL_FLAG_NONPOSITIVE_J = 1
 FL_FLAG_BAD_INDEX = 2
 FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
+FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN = 3
+FL_MATERIAL_LINEARELASTIC = 10
 FL_ARITH_FP64 = 0
 FL_ARITH_FLOAT_PAIR = 1
 FL_PCG_F64 = 64
@@ -59,7 +61,8 @@ def lib():
         L.fl_ComputeSparsityPattern_workspace_size.restype = ctypes.c_size_t
         L.fl_ComputeSparsityPattern.argtypes = [P, I64, I64, I64, I64, P, P, I64, ctypes.POINTER(I64), P, P, P,
                                                 ctypes.c_size_t, P]
-        for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_"):
+        for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
+                     "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_"):
             getattr(L, name).argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_noalloc.argtypes = [INT] + _DF_ARGS
         L.fl_GlobalAssemblyDF_Batched.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, P, P,
@@ -101,7 +104,9 @@ def check(status, what=""):
 
 # every symbol include/florence_gb300.h declares
 EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_ComputeSparsityPattern",
-           "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_", "fl_GlobalAssemblyDF_noalloc",
+           "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
+           "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
+           "fl_GlobalAssemblyDF_noalloc",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",

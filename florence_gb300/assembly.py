@@ -32,7 +32,23 @@ __all__ = ["DeviceAssembler", "ComputeSparsityPattern", "_LowLevelAssemblyDF__Ne
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
            "__TotalConstantMassIntegrand__", "install", "material_params", "fp64_peak_gflops"]
 
-MATERIALS = {"NeoHookean": N.FL_MATERIAL_NEOHOOKEAN, "MooneyRivlin": N.FL_MATERIAL_MOONEYRIVLIN}
+MATERIALS = {"NeoHookean": N.FL_MATERIAL_NEOHOOKEAN, "MooneyRivlin": N.FL_MATERIAL_MOONEYRIVLIN,
+             "NearlyIncompressibleMooneyRivlin": N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
+             "LinearElastic": N.FL_MATERIAL_LINEARELASTIC}
+_DF_ENTRY = {N.FL_MATERIAL_NEOHOOKEAN: "fl_GlobalAssemblyDF__NeoHookean_",
+             N.FL_MATERIAL_MOONEYRIVLIN: "fl_GlobalAssemblyDF__MooneyRivlin_",
+             N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN: "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_",
+             N.FL_MATERIAL_LINEARELASTIC: "fl_GlobalAssemblyDF__LinearElastic_"}
+
+
+def _abi_params(mat_id, params):
+    """(mu, mu1, mu2, lamb) of the reference's argument list for kernel parameters (p0, p1, p2):
+    neo-Hookean and linear elastic (mu, lamb); Mooney-Rivlin (mu1, mu2, lamb); nearly
+    incompressible Mooney-Rivlin (alpha, beta, kappa) passed as (mu1, mu2, lamb)."""
+    p0, p1, p2 = params
+    if mat_id in (N.FL_MATERIAL_NEOHOOKEAN, N.FL_MATERIAL_LINEARELASTIC):
+        return p0, 0.0, 0.0, p1
+    return 0.0, p0, p1, p2
 
 
 class NonPositiveJacobianWarning(RuntimeWarning):
@@ -57,13 +73,23 @@ def _to_dev(a, dtype, device):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=torch.empty(0, dtype=dtype).numpy().dtype)).to(device)
 
 
-def material_params(material, name=None):
-    """(material id, (p0, p1, p2)) for the kernels, read from a Florence material object."""
+def material_params(material, name=None, explicit=False):
+    """(material id, (p0, p1, p2)) for the kernels, read from a Florence material object as the
+    reference's implicit (or, explicit=True, explicit) low-level wrapper reads it."""
     name = name or type(material).__name__
+    if explicit and name == "NearlyIncompressibleMooneyRivlin":  # _LowLevelAssemblyExplicit_DF_DPF_.pyx:82-84
+        return (N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
+                (float(material.alpha), float(material.beta), float(material.kappa)))
     if name == "NeoHookean":
         return N.FL_MATERIAL_NEOHOOKEAN, (float(material.mu), float(material.lamb), 0.0)
     if name == "MooneyRivlin":
         return N.FL_MATERIAL_MOONEYRIVLIN, (float(material.mu1), float(material.mu2), float(material.lamb))
+    if name == "LinearElastic":
+        return N.FL_MATERIAL_LINEARELASTIC, (float(material.mu), float(material.lamb), 0.0)
+    if name == "NearlyIncompressibleMooneyRivlin":
+        # the low-level path constructs the material from (mu1, mu2, lamb) (AOT_Assembler.py:68-69, 110-111)
+        return (N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
+                (float(material.mu1), float(material.mu2), float(material.lamb)))
     raise NotImplementedError("Turning optimise option on for {} material is not supported yet. "
                               "Consider 'optimise=False' for now".format(name))
 
@@ -161,13 +187,8 @@ class DeviceAssembler:
         else:
             V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
             Ip, Jp, dl, dg = self.indptr, self.indices, self.data_local, self.data_global
-        fn = L.fl_GlobalAssemblyDF__NeoHookean_ if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN else \
-            L.fl_GlobalAssemblyDF__MooneyRivlin_
-        p0, p1, p2 = self.params
-        if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN:
-            mu, mu1, mu2, lamb = p0, 0.0, 0.0, p1
-        else:
-            mu, mu1, mu2, lamb = 0.0, p0, p1, p2
+        fn = getattr(L, _DF_ENTRY[self.mat_id])
+        mu, mu1, mu2, lamb = _abi_params(self.mat_id, self.params)
         st = fn(_ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
                 3, 3, self.nq, self.nelem, self.npe, self.nnode, 6, self.update, None, None,
                 _ptr(Ip), _ptr(Jp), _ptr(V), _ptr(T), 1 if self.mode == "triplet" else 0,
@@ -189,11 +210,7 @@ class DeviceAssembler:
             V32 = torch.zeros(self.nnz, dtype=torch.float32, device=self.device)
         if T is None:
             T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
-        p0, p1, p2 = self.params
-        if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN:
-            mu, mu1, mu2, lamb = p0, 0.0, 0.0, p1
-        else:
-            mu, mu1, mu2, lamb = 0.0, p0, p1, p2
+        mu, mu1, mu2, lamb = _abi_params(self.mat_id, self.params)
         st = L.fl_GlobalAssemblyDF_Mixed(self.mat_id, _ptr(self.points), _ptr(self.elements), _ptr(x), _ptr(self.Jm),
                                          _ptr(self.w), self.nq, self.nelem, self.npe, self.nnode, self.update,
                                          _ptr(self.indptr), _ptr(self.indices), _ptr(self.data_local),
@@ -208,14 +225,13 @@ class DeviceAssembler:
         x = Eulerx if Eulerx.is_contiguous() else Eulerx.contiguous()
         if T is None:
             T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
-        p0, p1, p2 = self.params
-        if self.mat_id == N.FL_MATERIAL_NEOHOOKEAN:
-            mu, mu1, mu2, lamb = p0, 0.0, 0.0, p1
-        else:
-            mu, mu1, mu2, lamb = 0.0, p0, p1, p2
+        mu, mu1, mu2, lamb = _abi_params(self.mat_id, self.params)
+        # the explicit entry takes the nearly incompressible material's (alpha, beta, kappa) as
+        # (mu1, mu2, mu3) (_LowLevelAssemblyExplicit_DF_DPF_.pyx:82-84)
+        mu3 = self.params[2] if self.mat_id == N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN else 0.0
         st = L.fl_GlobalAssemblyExplicit_DF_DPF_(
             _ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w), 3, 3, self.nq,
-            self.nelem, self.npe, self.nnode, 6, 1, _ptr(T), 1.0, mu, mu1, mu2, 0.0, 0.0, lamb, 0.0, 0.0, 0.0, 0.0,
+            self.nelem, self.npe, self.nnode, 6, 1, _ptr(T), 1.0, mu, mu1, mu2, mu3, 0.0, lamb, 0.0, 0.0, 0.0, 0.0,
             None, self.mat_id, 0, _ptr(self.flags), stream or _stream())
         N.check(st, "fl_GlobalAssemblyExplicit_DF_DPF_")
         return T
@@ -290,6 +306,18 @@ def _LowLevelAssemblyDF__MooneyRivlin_(fem_solver, function_space, formulation, 
     return _low_level_df("MooneyRivlin", fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp)
 
 
+def _LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_(fem_solver, function_space, formulation, mesh, material,
+                                                            Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDF_.pyx:53-160."""
+    return _low_level_df("NearlyIncompressibleMooneyRivlin", fem_solver, function_space, formulation, mesh, material,
+                         Eulerx, Eulerp)
+
+
+def _LowLevelAssemblyDF__LinearElastic_(fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDF_.pyx:53-160."""
+    return _low_level_df("LinearElastic", fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp)
+
+
 def _LowLevelAssemblyExplicit_DF_DPF_(function_space, formulation, mesh, material, Eulerx, Eulerp):
     """Internal force T [nnode*nvar] -- _LowLevelAssemblyExplicit_DF_DPF_.pyx:44-152 (mechanics)."""
     if formulation.fields != "mechanics":
@@ -299,7 +327,7 @@ def _LowLevelAssemblyExplicit_DF_DPF_(function_space, formulation, mesh, materia
     if name not in MATERIALS:
         raise NotImplementedError("Low level assembly for material {} not available for explicit analysis."
                                   " Consider 'optimise=False' for now".format(name))
-    _, params = material_params(material, name)
+    _, params = material_params(material, name, explicit=True)
     asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, name, params,
                           mode="triplet")
     T = asm.internal_force(_to_dev(Eulerx, torch.float64, asm.device))
@@ -339,6 +367,8 @@ def install(florence):
     ll = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly._LowLevelAssembly_")
     ll._LowLevelAssemblyDF__NeoHookean_ = _LowLevelAssemblyDF__NeoHookean_
     ll._LowLevelAssemblyDF__MooneyRivlin_ = _LowLevelAssemblyDF__MooneyRivlin_
+    ll._LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_ = _LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_
+    ll._LowLevelAssemblyDF__LinearElastic_ = _LowLevelAssemblyDF__LinearElastic_
     ll._LowLevelAssemblyExplicit_DF_DPF_ = _LowLevelAssemblyExplicit_DF_DPF_
     ll.has_low_level_dispatcher = True
     try:

@@ -128,25 +128,32 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         double sig[6], b[6], J, c1, c2, cbb;
         MatParams mp = A.mp;
         if (A.eparams) mp = MatParams{__ldg(A.eparams + e * 3), __ldg(A.eparams + e * 3 + 1), __ldg(A.eparams + e * 3 + 2)};
-        material<MAT>(F, mp, sig, b, J, c1, c2, cbb);
+        ExtraTangent ex;
+        material<MAT>(F, mp, sig, b, J, c1, c2, cbb, &ex);
         if (!(J > 0.0)) flag |= FL_FLAG_NONPOSITIVE_J;
-        // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G (indexed [d][e] or [i][d])
-        double GG[9], GsG[9], sG[9], bG[9], GbG[9];
+        constexpr bool NIMR = MAT == NEARLYINCOMPRESSIBLEMR;
+        // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G, gG = g G, GgG = G^T g G
+        double GG[9], GsG[9], sG[9], bG[9], GbG[9], gG[9], GgG[9];
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
                 sG[i * 3 + d] = fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
-                if (MAT == MOONEYRIVLIN)
+                if (MAT == MOONEYRIVLIN || NIMR)
                     bG[i * 3 + d] = fma(b[s6(i, 0)], G[0 * 3 + d], fma(b[s6(i, 1)], G[1 * 3 + d], b[s6(i, 2)] * G[2 * 3 + d]));
+                if (NIMR)
+                    gG[i * 3 + d] = fma(ex.g[s6(i, 0)], G[0 * 3 + d], fma(ex.g[s6(i, 1)], G[1 * 3 + d], ex.g[s6(i, 2)] * G[2 * 3 + d]));
             }
 #pragma unroll
         for (int d = 0; d < 3; ++d)
 #pragma unroll
             for (int e2 = d; e2 < 3; ++e2) {
                 GG[d * 3 + e2] = fma(G[d], G[e2], fma(G[3 + d], G[3 + e2], G[6 + d] * G[6 + e2]));
-                GsG[d * 3 + e2] = fma(G[d], sG[e2], fma(G[3 + d], sG[3 + e2], G[6 + d] * sG[6 + e2]));
+                // no geometric stiffness for the linear elastic material (the reference builds that
+                // assembler without it, AOT_Assembler.py:74-81)
+                GsG[d * 3 + e2] = MAT == LINEARELASTIC ? 0.0 : fma(G[d], sG[e2], fma(G[3 + d], sG[3 + e2], G[6 + d] * sG[6 + e2]));
                 if (MAT == MOONEYRIVLIN) GbG[d * 3 + e2] = fma(G[d], bG[e2], fma(G[3 + d], bG[3 + e2], G[6 + d] * bG[6 + e2]));
+                if (NIMR) GgG[d * 3 + e2] = fma(G[d], gG[e2], fma(G[3 + d], gG[3 + e2], G[6 + d] * gG[6 + e2]));
             }
         // Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
         //                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ]
@@ -162,6 +169,16 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
                 if (i == k) v = fma(c1, GG[dd * 3 + ee], v + GsG[dd * 3 + ee]);
                 if (MAT == MOONEYRIVLIN)
                     v = fma(cbb, fma(2.0 * bG[i * 3 + d], bG[k * 3 + e2], -fma(b[s6(i, k)], GbG[dd * 3 + ee], bG[k * 3 + d] * bG[i * 3 + e2])), v);
+                if (NIMR) {
+                    // kbI (bG_id G_ke + G_id bG_ke) + kgI (gG_id G_ke + G_id gG_ke) + kgg gG_id gG_ke
+                    // + kg4 (g_ik GG_de + gG_ie G_kd + gG_kd G_ie + d_ik GgG_de)
+                    v = fma(ex.kbI, fma(bG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * bG[k * 3 + e2]), v);
+                    v = fma(ex.kgI, fma(gG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * gG[k * 3 + e2]), v);
+                    v = fma(ex.kgg, gG[i * 3 + d] * gG[k * 3 + e2], v);
+                    double t4 = fma(ex.g[s6(i, k)], GG[dd * 3 + ee], fma(gG[i * 3 + e2], G[k * 3 + d], gG[k * 3 + d] * G[i * 3 + e2]));
+                    if (i == k) t4 += GgG[dd * 3 + ee];
+                    v = fma(ex.kg4, t4, v);
+                }
                 q[sym9(I, K) * ld] = detJ * v;
             }
 #pragma unroll
@@ -243,7 +260,8 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, DF ? AsmC
     S *Qs = reinterpret_cast<S *>(smem_raw);                                 // [EPC][nq][QSM]
     S *Jc = Qs + (size_t)EPC * nq * QSM;                                     // [QC][NPE][3]
     S *Us = Jc + (size_t)QC * NPE * 3;                                       // [EPC][QC][NPE][27]
-    int *nodes = reinterpret_cast<int *>(Us + (size_t)EPC * QC * NPE * 27);  // [EPC][NPE]
+    double *Ss = reinterpret_cast<double *>(Us + (size_t)EPC * QC * NPE * 27);  // [EPC][nq][9] residual part
+    int *nodes = reinterpret_cast<int *>(Ss + (size_t)EPC * nq * 9);          // [EPC][NPE]
     int *inv = nodes + EPC * NPE;                                            // [EPC][NDOF]
     __shared__ int s_flag;
     __shared__ int64_t s_nnz;
@@ -279,24 +297,27 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, DF ? AsmC
                 else inv[slot * NDOF + p] = i;
             }
         }
-        // tangent part of the Gauss-point data -> Qs[slot][g][k]
-        for (int idx = lt; idx < nq * 45; idx += TPE) {
+        // Gauss-point data -> tangent part Qs[slot][g][k] (operand format), residual part
+        // Ss[slot][g][k] (FP64)
+        for (int idx = lt; idx < nq * QSTRIDE; idx += TPE) {
             const int k = idx / nq, g = idx % nq;
-            Qs[((size_t)slot * nq + g) * QSM + k] = AR::split(qg[k * A.ldq + g]);
+            const double v = qg[k * A.ldq + g];
+            if (k < QSM) Qs[((size_t)slot * nq + g) * QSM + k] = AR::split(v);
+            else Ss[((size_t)slot * nq + g) * 9 + (k - QSM)] = v;
         }
     }
     __syncthreads();
 
-    // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d], FP64 (S from the L2-resident scratch)
+    // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d], FP64
     if (active && A.update) {
         for (int r = lt; r < NDOF; r += TPE) {
             const int a = r / 3, i = r % 3;
             double t = 0.0;
-            const double *qs = qg + (size_t)(45 + i * 3) * A.ldq;
-            for (int g = 0; g < nq; ++g) {
-                t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[g], t);
-                t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[A.ldq + g], t);
-                t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2 * A.ldq + g], t);
+            const double *qs = Ss + (size_t)slot * nq * 9 + i * 3;
+            for (int g = 0; g < nq; ++g, qs += 9) {
+                t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[0], t);
+                t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[1], t);
+                t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2], t);
             }
             atomicAdd(A.T + 3 * (int64_t)nodes[slot * NPE + a] + i, t);
         }
@@ -325,29 +346,25 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, DF ? AsmC
             }
             __syncthreads();
             if (active) {
-                // U_g[b][(i,d),k] for one (Gauss point, node b, component i) per work item: the
-                // nine entries of row block i, with compile-time indices into the packed tensor
-                for (int it = lt; it < qc * NPE * 3; it += TPE) {
-                    const int i = it % 3, qb = it / 3, q = qb / NPE, b = qb % NPE;
+                // U_g[b][(i,d),k] for one (Gauss point, node b, row I = (i,d)) per work item: three
+                // entries, with compile-time indices into the packed tensor
+                for (int it = lt; it < qc * NPE * 9; it += TPE) {
+                    const int I = it % 9, qb = it / 9, q = qb / NPE, b = qb % NPE;
                     const S *qq = Qs + ((size_t)slot * nq + c0 + q) * QSM;
                     const S *jb = Jc + (q * NPE + b) * 3;
                     const S j0 = jb[0], j1 = jb[1], j2 = jb[2];
                     S *uo = Us + (((size_t)slot * QC + q) * NPE + b) * 27;
 #pragma unroll
-                    for (int ii = 0; ii < 3; ++ii) {
-                        if (ii != i) continue;
+                    for (int II = 0; II < 9; ++II) {
+                        if (II != I) continue;
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            const int I = ii * 3 + d;
-#pragma unroll
-                            for (int k = 0; k < 3; ++k) {
-                                Acc u;
-                                AR::zero(u);
-                                AR::mac(u, qq[sym9(I, k * 3 + 2)], j2);
-                                AR::mac(u, qq[sym9(I, k * 3 + 1)], j1);
-                                AR::mac(u, qq[sym9(I, k * 3 + 0)], j0);
-                                uo[I * 3 + k] = AR::store(u);
-                            }
+                        for (int k = 0; k < 3; ++k) {
+                            Acc u;
+                            AR::zero(u);
+                            AR::mac(u, qq[sym9(II, k * 3 + 2)], j2);
+                            AR::mac(u, qq[sym9(II, k * 3 + 1)], j1);
+                            AR::mac(u, qq[sym9(II, k * 3 + 0)], j0);
+                            uo[II * 3 + k] = AR::store(u);
                         }
                     }
                 }
@@ -456,7 +473,8 @@ static int asm_qc(int nq) {
 template <int NPE>
 static size_t asm_smem_bytes(int nq, int qc) {
     constexpr int EPC = AsmCfg<NPE>::EPC;
-    return sizeof(double) * ((size_t)EPC * nq * QSM + (size_t)qc * NPE * 3 + (size_t)EPC * qc * NPE * 27) +
+    return sizeof(double) * ((size_t)EPC * nq * QSM + (size_t)qc * NPE * 3 + (size_t)EPC * qc * NPE * 27 +
+                             (size_t)EPC * nq * 9) +
            sizeof(int) * ((size_t)EPC * NPE + (size_t)EPC * 3 * NPE);
 }
 
@@ -543,7 +561,8 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     if (nelem < 0 || nnode <= 0) return FL_ERR_ARG;
     if (ngauss <= 0 || ngauss > 343) return FL_ERR_UNSUPPORTED;
     if (3 * nnode + 2 > INT32_MAX) return FL_ERR_UNSUPPORTED;
-    if (mat != NEOHOOKEAN && mat != MOONEYRIVLIN) return FL_ERR_UNSUPPORTED;
+    if (mat != NEOHOOKEAN && mat != MOONEYRIVLIN && mat != NEARLYINCOMPRESSIBLEMR && mat != LINEARELASTIC)
+        return FL_ERR_UNSUPPORTED;
     if (nelem == 0) return FL_OK;  // nothing is read or written
     if (!points || !elements || !Eulerx || !Jm || !AllGauss || !V_stiff || !T) return FL_ERR_ARG;
     AsmArgs A;
@@ -587,8 +606,26 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
             A.dg = data_global_indices;
         }
     }
-    if (mat == NEOHOOKEAN) return dispatch_asm<NEOHOOKEAN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
-    return dispatch_asm<MOONEYRIVLIN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
+    switch (mat) {
+        case NEOHOOKEAN: return dispatch_asm<NEOHOOKEAN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
+        case MOONEYRIVLIN: return dispatch_asm<MOONEYRIVLIN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
+        case NEARLYINCOMPRESSIBLEMR:
+            return dispatch_asm<NEARLYINCOMPRESSIBLEMR>((int)nodeperelem, A, scratch, scratch_bytes, stream);
+        default: return dispatch_asm<LINEARELASTIC>((int)nodeperelem, A, scratch, scratch_bytes, stream);
+    }
+}
+
+// Material of a C-ABI material number and its parameters from the reference's argument names:
+// neo-Hookean and linear elastic (mu, lamb), Mooney-Rivlin (mu1, mu2, lamb), nearly incompressible
+// Mooney-Rivlin (alpha, beta, kappa) = (mu1, mu2, lamb) (AOT_Assembler.py:62-71).
+static int material_of(int material_number, double mu, double mu1, double mu2, double lamb, int *mat, MatParams *mp) {
+    switch (material_number) {
+        case FL_MATERIAL_NEOHOOKEAN: *mat = NEOHOOKEAN; *mp = {mu, lamb, 0.0}; return FL_OK;
+        case FL_MATERIAL_MOONEYRIVLIN: *mat = MOONEYRIVLIN; *mp = {mu1, mu2, lamb}; return FL_OK;
+        case FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN: *mat = NEARLYINCOMPRESSIBLEMR; *mp = {mu1, mu2, lamb}; return FL_OK;
+        case FL_MATERIAL_LINEARELASTIC: *mat = LINEARELASTIC; *mp = {mu, lamb, 0.0}; return FL_OK;
+        default: return FL_ERR_UNSUPPORTED;
+    }
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -827,6 +864,21 @@ static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
     return fe == cudaSuccess ? FL_OK : FL_ERR_CUDA;
 }
 
+template <int MAT>
+static int mixed_dispatch(int npe, const AsmArgs &A, float *V32, cudaStream_t s) {
+    switch (npe) {
+        case 4: return launch_mixed<4, MAT>(A, V32, s);
+        case 8: return launch_mixed<8, MAT>(A, V32, s);
+        case 10: return launch_mixed<10, MAT>(A, V32, s);
+        case 20: return launch_mixed<20, MAT>(A, V32, s);
+        case 27: return launch_mixed<27, MAT>(A, V32, s);
+        case 35: return launch_mixed<35, MAT>(A, V32, s);
+        case 64: return launch_mixed<64, MAT>(A, V32, s);
+        case 125: return launch_mixed<125, MAT>(A, V32, s);
+        default: return FL_ERR_UNSUPPORTED;
+    }
+}
+
 // ------------------------------------------------------------------------------------------------
 // Allocation-free variant. Its Gauss-point scratch is this file-scope device array (every GPU that
 // loads the library holds it until the process exits). Host code cannot use the array's name as
@@ -864,9 +916,8 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
     (void)sorter; (void)rho; (void)mu3; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
     (void)anisotropic_orientations;
     fl::MatParams mp;
-    if (material_number == FL_MATERIAL_NEOHOOKEAN) mp = {mu, lamb, 0.0};
-    else if (material_number == FL_MATERIAL_MOONEYRIVLIN) mp = {mu1, mu2, lamb};
-    else return FL_ERR_UNSUPPORTED;
+    int mat = 0;
+    if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &mp) != FL_OK) return FL_ERR_UNSUPPORTED;
     if (ngauss <= 0 || ngauss > 343 || nelem < 0) return FL_ERR_ARG;
     // the whole mesh must fit the array in one pass: nelem * ngauss Gauss points of 54 doubles
     if ((double)nelem * (double)ngauss * fl::QSTRIDE * sizeof(double) > (double)FL_NOALLOC_SCRATCH_BYTES)
@@ -875,8 +926,7 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
     double *scratch = nullptr;
     const int st = fl::noalloc_scratch(&scratch);
     if (st != FL_OK) return st;
-    return fl::global_assembly_df(material_number == FL_MATERIAL_NEOHOOKEAN ? fl::NEOHOOKEAN : fl::MOONEYRIVLIN,
-                                  points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem, nodeperelem,
+    return fl::global_assembly_df(mat, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem, nodeperelem,
                                   nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
                                   recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
                                   data_global_indices, mp, flags, scratch, FL_NOALLOC_SCRATCH_BYTES,
@@ -920,26 +970,16 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.flags = flags;
     A.Q = nullptr;
     A.e0 = A.ne = A.ldq = 0;
+    int mat = 0;
+    if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &A.mp) != FL_OK) return FL_ERR_UNSUPPORTED;
     cudaStream_t s = (cudaStream_t)stream;
-    if (material_number == FL_MATERIAL_NEOHOOKEAN) {
-        A.mp = {mu, lamb, 0.0};
-        switch (nodeperelem) {
-#define FL_CASE(N) case N: return fl::launch_mixed<N, fl::NEOHOOKEAN>(A, V_stiff, s);
-            FL_CASE(4) FL_CASE(8) FL_CASE(10) FL_CASE(20) FL_CASE(27) FL_CASE(35) FL_CASE(64) FL_CASE(125)
-#undef FL_CASE
-            default: return FL_ERR_UNSUPPORTED;
-        }
+    switch (mat) {
+        case fl::NEOHOOKEAN: return fl::mixed_dispatch<fl::NEOHOOKEAN>((int)nodeperelem, A, V_stiff, s);
+        case fl::MOONEYRIVLIN: return fl::mixed_dispatch<fl::MOONEYRIVLIN>((int)nodeperelem, A, V_stiff, s);
+        case fl::NEARLYINCOMPRESSIBLEMR:
+            return fl::mixed_dispatch<fl::NEARLYINCOMPRESSIBLEMR>((int)nodeperelem, A, V_stiff, s);
+        default: return fl::mixed_dispatch<fl::LINEARELASTIC>((int)nodeperelem, A, V_stiff, s);
     }
-    if (material_number == FL_MATERIAL_MOONEYRIVLIN) {
-        A.mp = {mu1, mu2, lamb};
-        switch (nodeperelem) {
-#define FL_CASE(N) case N: return fl::launch_mixed<N, fl::MOONEYRIVLIN>(A, V_stiff, s);
-            FL_CASE(4) FL_CASE(8) FL_CASE(10) FL_CASE(20) FL_CASE(27) FL_CASE(35) FL_CASE(64) FL_CASE(125)
-#undef FL_CASE
-            default: return FL_ERR_UNSUPPORTED;
-        }
-    }
-    return FL_ERR_UNSUPPORTED;
 }
 
 int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const uint64_t *elements,
@@ -950,9 +990,9 @@ int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const
                                 double *V_stiff, double *T, int *flags, fl_stream_t stream) {
     if (!element_params && nelem > 0) return FL_ERR_ARG;
     const int squeeze = (data_local_indices == nullptr || data_global_indices == nullptr) ? 1 : 0;
-    const int mat = material_number == FL_MATERIAL_NEOHOOKEAN ? fl::NEOHOOKEAN
-                    : material_number == FL_MATERIAL_MOONEYRIVLIN ? fl::MOONEYRIVLIN : -1;
-    if (mat < 0) return FL_ERR_UNSUPPORTED;
+    int mat = 0;
+    fl::MatParams unused;
+    if (fl::material_of(material_number, 0, 0, 0, 0, &mat, &unused) != FL_OK) return FL_ERR_UNSUPPORTED;
     return fl::global_assembly_df(mat, points, elements, Eulerx, Jm, AllGauss, 3, 3, ngauss, nelem, nodeperelem, nnode,
                                   6, requires_geometry_update, const_cast<int32_t *>(indptr),
                                   const_cast<int32_t *>(indices), V_stiff, T, 0, squeeze, data_local_indices,
@@ -1003,6 +1043,28 @@ int fl_GlobalAssemblyDF__NeoHookean_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
     return fl::global_assembly_df(fl::NEOHOOKEAN, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem,
                                   nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
                                   recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
+                                  data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream);
+}
+
+int fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
+    (void)sorter; (void)rho; (void)mu; (void)mu3; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
+    (void)anisotropic_orientations;
+    fl::MatParams mp{mu1, mu2, lamb};  // (alpha, beta, kappa)
+    return fl::global_assembly_df(fl::NEARLYINCOMPRESSIBLEMR, points, elements, Eulerx, Jm, AllGauss, ndim, nvar,
+                                  ngauss, nelem, nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff,
+                                  J_stiff, V_stiff, T, recompute_sparsity_pattern, squeeze_sparsity_pattern,
+                                  data_local_indices, data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream);
+}
+
+int fl_GlobalAssemblyDF__LinearElastic_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
+    (void)sorter; (void)rho; (void)mu1; (void)mu2; (void)mu3; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3;
+    (void)eps_e; (void)anisotropic_orientations;
+    fl::MatParams mp{mu, lamb, 0.0};
+    return fl::global_assembly_df(fl::LINEARELASTIC, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss,
+                                  nelem, nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff,
+                                  V_stiff, T, recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
                                   data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream);
 }
 

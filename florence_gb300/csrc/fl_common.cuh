@@ -37,7 +37,17 @@ inline int ensure_smem(size_t bytes) {
 }
 
 // Material numbers (match FL_MATERIAL_*).
-enum { NEOHOOKEAN = 1, MOONEYRIVLIN = 2 };
+// material numbers follow the reference's explicit dispatcher
+// (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-106)
+enum { NEOHOOKEAN = 1, MOONEYRIVLIN = 2, NEARLYINCOMPRESSIBLEMR = 3, LINEARELASTIC = 10 };
+
+// Extra elasticity terms of the nearly incompressible Mooney-Rivlin material:
+//   c += kbI (b_ij d_kl + d_ij b_kl) + kgI (g_ij d_kl + d_ij g_kl)
+//      + kg4 (g_ik d_jl + g_il d_jk + d_ik g_jl + d_il g_jk) + kgg g_ij g_kl,  g = cof(F) cof(F)^T
+struct ExtraTangent {
+    double kbI, kgI, kg4, kgg;
+    double g[6];
+};
 
 struct MatParams {
     double p0, p1, p2;  // neo-Hookean: mu, lamb; Mooney-Rivlin: mu1, mu2, lamb
@@ -79,8 +89,23 @@ __device__ __forceinline__ int s6(int i, int j) {
 //   + lamb (J-1) I, c1 = 2(mu1+2mu2)/J - lamb (J-1), c2 = lamb (2J-1), cbb = 2 mu2/J.
 template <int MAT>
 __device__ __forceinline__ void material(const double *F, const MatParams &mp, double *sig, double *b, double &J,
-                                         double &c1, double &c2, double &cbb) {
+                                         double &c1, double &c2, double &cbb, ExtraTangent *ex = nullptr) {
     J = det3(F);
+    if (MAT == LINEARELASTIC) {  // _LinearElastic_.h:26-60: sigma = 2 mu eps + lamb tr(eps) I, eps = sym(F - I)
+        const double mu = mp.p0, lamb = mp.p1;
+        const double tre = F[0] + F[4] + F[8] - 3.0;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                b[s6(i, j)] = 0.0;
+                sig[s6(i, j)] = mu * (F[i * 3 + j] + F[j * 3 + i]) + (i == j ? lamb * tre - 2.0 * mu : 0.0);
+            }
+        c1 = mu;
+        c2 = lamb;
+        cbb = 0.0;
+        return;
+    }
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -99,6 +124,34 @@ __device__ __forceinline__ void material(const double *F, const MatParams &mp, d
         c1 = a - dv;
         c2 = lamb * (2.0 * J - 1.0);
         cbb = 0.0;
+    } else if (MAT == NEARLYINCOMPRESSIBLEMR) {
+        // _NearlyIncompressibleMooneyRivlin_.h:26-90, parameters (alpha, beta, kappa)
+        const double alpha = mp.p0, beta = mp.p1, kappa = mp.p2;
+        double iF[9], g[6];
+        inv3(F, iF);
+        // cof(F) = J F^-T, g = cof cof^T = J^2 F^-T F^-1: g_ij = J^2 sum_k iF[k][i] iF[k][j]
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j)
+                g[s6(i, j)] = J * J * (iF[0 * 3 + i] * iF[0 * 3 + j] + iF[1 * 3 + i] * iF[1 * 3 + j] + iF[2 * 3 + i] * iF[2 * 3 + j]);
+        const double trb = b[0] + b[1] + b[2], trg = g[0] + g[1] + g[2];
+        const double A = 2.0 * alpha * pow(J, -5.0 / 3.0), iJ3 = iJ * iJ * iJ, strg = sqrt(trg);
+        const double B3 = beta * iJ3 * trg * strg, B1 = 3.0 * beta * iJ3 * strg, dv = kappa * (J - 1.0);
+        const double diag = -A / 3.0 * trb + B3 + dv;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) sig[k] = A * b[k] - B1 * g[k] + (k < 3 ? diag : 0.0);
+        c1 = A / 3.0 * trb - B3 - dv;
+        c2 = 2.0 / 9.0 * A * trb + B3 + kappa * (2.0 * J - 1.0);
+        cbb = 0.0;
+        if (ex) {
+            ex->kbI = -2.0 / 3.0 * A;
+            ex->kgI = -B1;
+            ex->kg4 = B1;
+            ex->kgg = B1 / trg;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) ex->g[k] = g[k];
+        }
     } else {
         const double mu1 = mp.p0, mu2 = mp.p1, lamb = mp.p2;
         const double trb = b[0] + b[1] + b[2];

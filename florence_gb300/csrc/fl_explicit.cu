@@ -183,7 +183,7 @@ int fl_GlobalAssemblyExplicit_DF_DPF_(const double *points, const uint64_t *elem
                                       double eps_2, double eps_3, double eps_e,
                                       const double *anisotropic_orientations, int material_number,
                                       int formulation_number, int *flags, fl_stream_t stream) {
-    (void)Eulerp; (void)bases; (void)H_VoigtSize; (void)requires_geometry_update; (void)rho; (void)mu3; (void)mue;
+    (void)Eulerp; (void)bases; (void)H_VoigtSize; (void)requires_geometry_update; (void)rho; (void)mue;
     (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e; (void)anisotropic_orientations;
     if (ndim != 3 || nvar != 3 || formulation_number != 0) return FL_ERR_ARG;
     if (nelem == 0 && nnode > 0 && ngauss > 0) return FL_OK;  // nothing is read or written
@@ -197,6 +197,14 @@ int fl_GlobalAssemblyExplicit_DF_DPF_(const double *points, const uint64_t *elem
     if (material_number == FL_MATERIAL_MOONEYRIVLIN) {
         A.mp = {mu1, mu2, lamb};
         return fl::dispatch_if<fl::MOONEYRIVLIN>((int)nodeperelem, A, (cudaStream_t)stream);
+    }
+    if (material_number == FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN) {  // (alpha, beta, kappa) as (mu1, mu2, mu3)
+        A.mp = {mu1, mu2, mu3};
+        return fl::dispatch_if<fl::NEARLYINCOMPRESSIBLEMR>((int)nodeperelem, A, (cudaStream_t)stream);
+    }
+    if (material_number == FL_MATERIAL_LINEARELASTIC) {
+        A.mp = {mu, lamb, 0.0};
+        return fl::dispatch_if<fl::LINEARELASTIC>((int)nodeperelem, A, (cudaStream_t)stream);
     }
     return FL_ERR_UNSUPPORTED;
 }

@@ -250,9 +250,13 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
         c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB);
         s2 = t;
     }
-    y0 = (double)s0 + (double)c0;
-    y1 = (double)s1 + (double)c1;
-    y2 = (double)s2 + (double)c2;
+    if (sub == 0) {  // only the group's first lane holds the sums (the conversions run on the FP64 pipe)
+        y0 = (double)s0 + (double)c0;
+        y1 = (double)s1 + (double)c1;
+        y2 = (double)s2 + (double)c2;
+    } else {
+        y0 = y1 = y2 = 0.0;
+    }
 }
 
 // (s, c) += (vh + vl) * (ph + pl), dropping vl*pl (2^-48 relative)
@@ -296,9 +300,13 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
         c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB);
         s2 = t;
     }
-    y0 = (double)s0 + (double)c0;
-    y1 = (double)s1 + (double)c1;
-    y2 = (double)s2 + (double)c2;
+    if (sub == 0) {  // only the group's first lane holds the sums (the conversions run on the FP64 pipe)
+        y0 = (double)s0 + (double)c0;
+        y1 = (double)s1 + (double)c1;
+        y2 = (double)s2 + (double)c2;
+    } else {
+        y0 = y1 = y2 = 0.0;
+    }
 }
 
 __device__ __forceinline__ double to_d(double v) { return v; }
@@ -389,8 +397,17 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
 // K2: alpha = rz_k / p.q, x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r. One thread per
 // dof, 30 lanes of a warp = 10 nodes; a node's three residual entries meet through shuffles.
 __global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x, PcgState s) {
-    if (s.done[0]) return;
-    const double alpha = s.acc[1 + (k & 1)] / s.acc[0];
+    // one read of the done flag and one division per CTA (FP64 division is a long FP64-pipe
+    // sequence); the flag read by one thread keeps the early return uniform across the CTA
+    __shared__ double s_alpha;
+    __shared__ int s_done;
+    if (threadIdx.x == 0) {
+        s_done = s.done[0];
+        s_alpha = s_done ? 0.0 : s.acc[1 + (k & 1)] / s.acc[0];
+    }
+    __syncthreads();
+    if (s_done) return;
+    const double alpha = s_alpha;
     const int lane = threadIdx.x & 31, ln = lane / 3, i = lane % 3, l0 = 3 * ln;
     const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
@@ -422,8 +439,17 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x
 
 // K3: beta = rz_{k+1} / rz_k, p = z + beta p, convergence test; zeroes p.q for the next K1
 __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, int split, PcgState s) {
-    if (s.done[0]) return;
-    const double beta = s.acc[1 + ((k + 1) & 1)] / s.acc[1 + (k & 1)];
+    // block 0 sets the done flag at its end while other CTAs of this launch may still start:
+    // one thread reads it for the whole CTA, so every thread takes the same branch
+    __shared__ double s_beta;
+    __shared__ int s_done;
+    if (threadIdx.x == 0) {
+        s_done = s.done[0];
+        s_beta = s_done ? 0.0 : s.acc[1 + ((k + 1) & 1)] / s.acc[1 + (k & 1)];
+    }
+    __syncthreads();
+    if (s_done) return;
+    const double beta = s_beta;
     const double rr = s.acc[3];
     for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT) {
         const double pv = fma(beta, s.p[d], s.z[d]);

@@ -139,13 +139,63 @@ class NewtonSolver:
     def residual_norm(self, F):
         return float(torch.linalg.vector_norm((self.T - F) * self.free))
 
+    def _iterate(self, u, F):
+        """Newton iterations of one increment from u (tangent and residual at u assembled).
+        Returns (u, iteration log, failed, PCG iterations)."""
+        R = (self.T - F) * self.free
+        norm_load = float(torch.linalg.vector_norm(F * self.free))
+        norm_forces = None
+        it = 0
+        eta = self.eta0
+        r_before = float(torch.linalg.vector_norm(R))
+        iters = []
+        pcg_total = 0
+        failed = False
+        while True:
+            self._set_jacobian(u, r_before, norm_load)
+            du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
+                                 workspace=self.ws, spmv=self.spmv)
+            pcg_total += pits
+            u += du
+            self._assemble(u)
+            R = (self.T - F) * self.free
+            absn = float(torch.linalg.vector_norm(R))
+            if self.criterion == "load":
+                norm_forces = norm_load if norm_load != 0.0 else 1.0
+            elif it == 0:
+                norm_forces = absn if absn != 0.0 else 1e-14
+            rel = abs(absn / norm_forces)
+            iters.append(dict(iter=it, abs=absn, rel=rel, pcg_iters=pits, pcg_relres=prel, eta=eta,
+                              jacobian="fp32" if self.V is self.V32 else "fp64"))
+            if absn < self.tol:
+                break
+            it += 1
+            if rel <= self.tol and (it > 0 or self.criterion == "load"):
+                break
+            if it >= self.max_iter or not np.isfinite(rel) or rel > 1e6:
+                failed = True
+                break
+            if self.forcing == "rel":
+                # solve to a tolerance proportional to the current relative residual
+                eta = float(min(self.eta_max, max(self.eta_min, 0.1 * rel)))
+            else:
+                e_new = 0.9 * (absn / r_before) ** 2 if r_before > 0 else self.eta_max
+                if 0.9 * eta ** 2 > 0.1:
+                    e_new = max(e_new, 0.9 * eta ** 2)
+                e_new = min(self.eta_max, e_new)
+                e_new = max(e_new, 0.5 * self.tol * norm_forces / absn)
+                eta = float(min(self.eta_max, max(self.eta_min, e_new)))
+            r_before = absn
+        return u, iters, failed, pcg_total
+
     def solve(self, u0=None, guesses=None, keep_states=False):
         """Runs all increments. guesses: optional callable(increment, u_prev) -> candidate initial
         u for the increment (a warm start), a list of candidates, or None. The candidate with the
         smallest FP64 residual is kept if that residual is below the previous increment's
-        solution's (the default start); otherwise the solver falls back to the previous solution.
-        keep_states: also return each
-        increment's converged displacement (device FP64) under increments[k]["u"]. Returns a dict."""
+        solution's (the default start) and no element of it is inverted; otherwise the solver
+        falls back to the previous solution, and it restarts the increment from there if Newton
+        fails from a candidate. keep_states: also return each increment's converged displacement
+        (device FP64) under increments[k]["u"]. Returns a dict."""
         dev = self.asm.device
         n = self.asm.nnode * 3
         u = torch.zeros(n, dtype=torch.float64, device=dev) if u0 is None else u0.clone()
@@ -158,70 +208,46 @@ class NewtonSolver:
         for inc in range(1, self.n_increments + 1):
             F = self.f_ext * (inc / self.n_increments)
             guess = "previous"
+            u_prev = u
             if guesses is not None:
                 cands = guesses(inc, u)
                 if cands is not None:
                     if isinstance(cands, torch.Tensor):
                         cands = [cands]
-                    # the FP64 residual judges every candidate; the previous solution is the fallback
+                    # the FP64 residual judges every candidate (one with an inverted element,
+                    # det F <= 0, is rejected); the previous solution is the fallback
                     best, best_r, best_k = u, self.residual_norm(F), -1
                     for k, g in enumerate(cands):
+                        self.asm.flags.zero_()
                         self._assemble(g)
                         r = self.residual_norm(F)
+                        if int(self.asm.flags.item()) & N.FL_FLAG_NONPOSITIVE_J:
+                            r = np.inf
                         if r < best_r:
                             best, best_r, best_k = g, r, k
+                    self.asm.flags.zero_()
                     u = best.clone()
                     if best_k != len(cands) - 1:  # the tangent and residual of the chosen state
                         self._assemble(u)
                     guess = "fallback" if best_k < 0 else "candidate%d" % best_k
-            R = (self.T - F) * self.free
-            norm_load = float(torch.linalg.vector_norm(F * self.free))
-            norm_forces = None
-            it = 0
-            rel = np.inf
-            eta = self.eta0
-            r_before = float(torch.linalg.vector_norm(R))
-            iters = []
-            while True:
-                self._set_jacobian(u, r_before, norm_load)
-                du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
-                                     workspace=self.ws, spmv=self.spmv)
-                total_pcg += pits
-                u += du
+            if guess.startswith("candidate"):
+                u_keep = u_prev.clone()
+            u, iters, inc_failed, pits = self._iterate(u, F)
+            total_pcg += pits
+            if inc_failed and guess.startswith("candidate"):
+                # Newton did not converge from the prediction: restart from the previous solution
+                u = u_keep
                 self._assemble(u)
-                R = (self.T - F) * self.free
-                absn = float(torch.linalg.vector_norm(R))
-                if self.criterion == "load":
-                    norm_forces = norm_load if norm_load != 0.0 else 1.0
-                elif it == 0:
-                    norm_forces = absn if absn != 0.0 else 1e-14
-                rel = abs(absn / norm_forces)
-                iters.append(dict(iter=it, abs=absn, rel=rel, pcg_iters=pits, pcg_relres=prel, eta=eta,
-                                  jacobian="fp32" if self.V is self.V32 else "fp64"))
-                if absn < self.tol:
-                    break
-                it += 1
-                if rel <= self.tol and (it > 0 or self.criterion == "load"):
-                    break
-                if it >= self.max_iter or not np.isfinite(rel) or rel > 1e6:
-                    failed = True
-                    break
-                if self.forcing == "rel":
-                    # solve to a tolerance proportional to the current relative residual
-                    eta = float(min(self.eta_max, max(self.eta_min, 0.1 * rel)))
-                else:
-                    e_new = 0.9 * (absn / r_before) ** 2 if r_before > 0 else self.eta_max
-                    if 0.9 * eta ** 2 > 0.1:
-                        e_new = max(e_new, 0.9 * eta ** 2)
-                    e_new = min(self.eta_max, e_new)
-                    e_new = max(e_new, 0.5 * self.tol * norm_forces / absn)
-                    eta = float(min(self.eta_max, max(self.eta_min, e_new)))
-                r_before = absn
+                u, iters2, inc_failed, pits = self._iterate(u, F)
+                total_pcg += pits
+                iters = iters + iters2
+                guess = "restarted"
             total_newton += len(iters)
             incs.append(dict(increment=inc, newton_iters=len(iters), history=iters, guess=guess))
             if keep_states:
                 incs[-1]["u"] = u.clone()
-            if failed:
+            if inc_failed:
+                failed = True
                 break
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0

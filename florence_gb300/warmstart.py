@@ -316,7 +316,8 @@ def evaluate_warm_start(solver, ws, params, warm_solvers=None):
     tot = {k: dict(newton=sum(r[k]["newton"] for r in rows), pcg=sum(r[k]["pcg"] for r in rows),
                    wall_s=sum(r[k]["wall_s"] for r in rows), failed=sum(r[k]["failed"] for r in rows))
            for k in names}
-    kinds = {"candidate0": "corrected_state", "candidate1": "predicted_step", "fallback": "previous"}
+    kinds = {"candidate0": "corrected_state", "candidate1": "predicted_step", "fallback": "previous",
+             "restarted": "restarted"}
     for k in warm_solvers:
         tot[k]["accepted"] = sum(r[k]["accepted"] for r in rows)
         tot[k]["chosen"] = {v: sum(c == kk for r in rows for c in r[k]["chosen"]) for kk, v in kinds.items()}

@@ -45,6 +45,8 @@ typedef struct CUstream_st *fl_stream_t;
 /* material numbers of the explicit entry point (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-109) */
 #define FL_MATERIAL_NEOHOOKEAN 1
 #define FL_MATERIAL_MOONEYRIVLIN 2
+#define FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN 3
+#define FL_MATERIAL_LINEARELASTIC 10
 
 const char *fl_status_string(int status);
 
@@ -99,6 +101,13 @@ int fl_ComputeSparsityPattern(const int64_t *elements, int64_t nelem, int64_t no
 
 int fl_GlobalAssemblyDF__NeoHookean_(FL_GLOBAL_ASSEMBLY_DF_ARGS);   /* mu, lamb */
 int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu1, mu2, lamb */
+/* The same for the two other isotropic low-level DF materials of the reference
+ * (AOT_Assembler.py:8-14): _GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_ (parameters
+ * alpha, beta, kappa passed as mu1, mu2, lamb; _NearlyIncompressibleMooneyRivlin_.h:26-90) and
+ * _GlobalAssemblyDF__LinearElastic_ (mu, lamb; _LinearElastic_.h:26-60; built without the geometric
+ * stiffness, AOT_Assembler.py:74-81). */
+int fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS);
+int fl_GlobalAssemblyDF__LinearElastic_(FL_GLOBAL_ASSEMBLY_DF_ARGS);
 
 /* ------------------------------------------------------------------------------------------
  * Allocation-free tangent + residual assembly. No counterpart in the reference (its assembly

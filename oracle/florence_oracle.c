@@ -39,6 +39,8 @@
 
 #define ORC_NEOHOOKEAN 1
 #define ORC_MOONEYRIVLIN 2
+#define ORC_NEARLYINCOMPRESSIBLEMOONEYRIVLIN 3
+#define ORC_LINEARELASTIC 10
 
 /* Voigt pairs in the reference's order xx,yy,zz,xy,xz,yz (_ConstitutiveStiffnessDF_.h:17-22). */
 static const int VI[6] = {0, 1, 2, 0, 0, 1};
@@ -114,7 +116,46 @@ static void material_qp(int mat, const double *prm, const double *F, double *sig
             b[i * 3 + j] = s;
         }
     double c1, c2, cbb = 0.0; /* c = c1 (d_ik d_jl + d_il d_jk) + c2 d_ij d_kl + cbb (2 b_ij b_kl - b_ik b_jl - b_il b_jk) */
-    if (mat == ORC_NEOHOOKEAN) {
+    /* nearly incompressible Mooney-Rivlin (_NearlyIncompressibleMooneyRivlin_.h:26-90, parameters
+     * alpha, beta, kappa): c += kbI (b_ij d_kl + d_ij b_kl) + kgI (g_ij d_kl + d_ij g_kl)
+     * + kg4 (g_ik d_jl + g_il d_jk + d_ik g_jl + d_il g_jk) + kgg g_ij g_kl, g = cof(F) cof(F)^T */
+    double kbI = 0.0, kgI = 0.0, kg4 = 0.0, kgg = 0.0, g[9] = {0};
+    if (mat == ORC_LINEARELASTIC) { /* _LinearElastic_.h:26-60: stress from the small strain */
+        double mu = prm[0], lamb = prm[1];
+        double tre = F[0] + F[4] + F[8] - 3.0;
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+                sig[i * 3 + j] = mu * (F[i * 3 + j] + F[j * 3 + i] - 2.0 * (i == j)) + (i == j ? lamb * tre : 0.0);
+        c1 = mu;
+        c2 = lamb;
+    } else if (mat == ORC_NEARLYINCOMPRESSIBLEMOONEYRIVLIN) {
+        double alpha = prm[0], beta = prm[1], kappa = prm[2];
+        double iF[9];
+        inv3(F, iF);
+        double H[9]; /* cofactor J F^-T */
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) H[i * 3 + j] = J * iF[j * 3 + i];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double s = 0.0;
+                for (int k = 0; k < 3; ++k) s += H[i * 3 + k] * H[j * 3 + k];
+                g[i * 3 + j] = s;
+            }
+        double trb = b[0] + b[4] + b[8], trg = g[0] + g[4] + g[8];
+        double A = 2.0 * alpha * pow(J, -5.0 / 3.0);
+        double B3 = beta / (J * J * J) * trg * sqrt(trg), B1 = 3.0 * beta / (J * J * J) * sqrt(trg);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double d = (i == j) ? 1.0 : 0.0;
+                sig[i * 3 + j] = A * b[i * 3 + j] - A / 3.0 * trb * d + B3 * d - B1 * g[i * 3 + j] + kappa * (J - 1.0) * d;
+            }
+        kbI = -2.0 / 3.0 * A;
+        c2 = 2.0 / 9.0 * A * trb + B3 + kappa * (2.0 * J - 1.0);
+        c1 = A / 3.0 * trb - B3 - kappa * (J - 1.0);
+        kgI = -B1;
+        kg4 = B1;
+        kgg = B1 / trg;
+    } else if (mat == ORC_NEOHOOKEAN) {
         double mu = prm[0], lamb = prm[1];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j)
@@ -141,6 +182,12 @@ static void material_qp(int mat, const double *prm, const double *F, double *sig
             int i = VI[I], j = VJ[I], k = VI[K], l = VJ[K];
             double v = c1 * ((i == k) * (j == l) + (i == l) * (j == k)) + c2 * (i == j) * (k == l);
             if (cbb != 0.0) v += cbb * (2.0 * b[i * 3 + j] * b[k * 3 + l] - b[i * 3 + k] * b[j * 3 + l] - b[i * 3 + l] * b[j * 3 + k]);
+            if (mat == ORC_NEARLYINCOMPRESSIBLEMOONEYRIVLIN) {
+                double dij = (i == j), dkl = (k == l), dik = (i == k), djl = (j == l), dil = (i == l), djk = (j == k);
+                v += kbI * (b[i * 3 + j] * dkl + dij * b[k * 3 + l]) + kgI * (g[i * 3 + j] * dkl + dij * g[k * 3 + l]) +
+                     kg4 * (g[i * 3 + k] * djl + g[i * 3 + l] * djk + dik * g[j * 3 + l] + dil * g[j * 3 + k]) +
+                     kgg * g[i * 3 + j] * g[k * 3 + l];
+            }
             H[I * 6 + K] = v;
         }
 }
@@ -191,7 +238,9 @@ static void element_df(int mat, const double *prm, const double *Jm, const doubl
                 te[r] += s * detJ;
             }
         }
-        /* geometric stiffness (ABI==1 branch) */
+        /* geometric stiffness (ABI==1 branch); the reference builds the linear elastic assembler
+         * without it (AOT_Assembler.py:74-81) */
+        if (mat != ORC_LINEARELASTIC)
         for (int a = 0; a < npe; ++a) {
             double a0 = sp[a * 3], a1 = sp[a * 3 + 1], a2 = sp[a * 3 + 2];
             for (int b = 0; b < npe; ++b) {

@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 FAST_PATH = os.path.join(HERE, "liboracle_fast.so")
-MATERIALS = {"NeoHookean": 1, "MooneyRivlin": 2}
+MATERIALS = {"NeoHookean": 1, "MooneyRivlin": 2, "NearlyIncompressibleMooneyRivlin": 3, "LinearElastic": 10}
 
 _libs = {}
 

@@ -36,6 +36,14 @@ def make_material(F, name, params):
         m = F.NeoHookean(3, mu=params[0], lamb=params[1], rho=params[2] if len(params) > 2 else 1.0)
     elif name == "MooneyRivlin":
         m = F.MooneyRivlin(3, mu1=params[0], mu2=params[1], lamb=params[2], rho=params[3] if len(params) > 3 else 1.0)
+    elif name == "LinearElastic":
+        m = F.LinearElastic(3, mu=params[0], lamb=params[1], rho=1.0)
+    elif name == "NearlyIncompressibleMooneyRivlin":
+        # params (alpha, beta, kappa): the numpy path reads alpha/beta/kappa, the low-level path
+        # (AOT_Assembler.py:66-71, 110-112) mu1/mu2/lamb -- set both to the same values
+        m = F.NearlyIncompressibleMooneyRivlin(3, mu=2.0 * params[0], lamb=params[2], rho=1.0)
+        m.alpha, m.beta, m.kappa = params
+        m.mu1, m.mu2, m.lamb = params
     else:
         raise ValueError(name)
     m.has_low_level_dispatcher = False
@@ -108,7 +116,8 @@ def reference_assembly(F, spec, mesh, x, recompute):
     mat = make_material(F, spec["material"], spec["params"])
     kw = {} if spec.get("qdeg") is None else {"quadrature_degree": spec["qdeg"]}
     form = F.DisplacementFormulation(mesh, **kw)
-    solver = F.FEMSolver(optimise=False, recompute_sparsity_pattern=recompute)
+    solver = F.FEMSolver(optimise=False, recompute_sparsity_pattern=recompute,
+                         analysis_nature=spec.get("nature", "nonlinear"))
     K, T = F.AssembleForm(form, mesh, mat, solver, Eulerx=x)
     return K.tocsr(), np.asarray(T).ravel(), form, mat, solver
 
@@ -152,6 +161,13 @@ CASES = [
          amp=0.01, qdeg=None, emat=(0, 5), mass=True),
     dict(name="tet_p2_mr", mesh="cube_tet", n=(1, 1, 1), p=2, material="MooneyRivlin", params=(0.5, 0.5, 20.0),
          seed=17, amp=0.02, qdeg=None, emat=(0, 2), mass=True),
+    # linear analysis (no geometry update, no residual): at x = X the low-level and numpy paths agree
+    # (the low-level kinematics take spatial gradients from x even without the update,
+    # _KinematicMeasures_.h:95-103; the numpy path then takes material gradients)
+    dict(name="hex_p2_le", mesh="cube_hex", n=(2, 2, 1), p=2, material="LinearElastic", params=(1.0, 2.5), seed=19,
+         amp=0.0, qdeg=None, emat=(0, 2), mass=False, nature="linear"),
+    dict(name="tet_p2_nimr", mesh="cube_tet", n=(1, 1, 1), p=2, material="NearlyIncompressibleMooneyRivlin",
+         params=(0.4, 0.1, 15.0), seed=20, amp=0.03, qdeg=None, emat=(0, 3), mass=False, triplet=True),
     dict(name="tet_p3_mr_jitter", mesh="jitter_tet", L=(4.0, 1.0, 1.0), n=(4, 1, 1), mesh_seed=1, p=3,
          material="MooneyRivlin", params=(0.5, 0.5, 20.0), seed=18, amp=0.01, qdeg=None, emat=(0, 4), mass=True,
          triplet=True),
@@ -169,6 +185,7 @@ def make_case(F, spec):
         points=mesh.points, elements=mesh.elements.astype(np.int64), Eulerx=x,
         Jm=fs.Jm, AllGauss=fs.AllGauss.ravel(), Bases=fs.Bases,
         material=np.array(spec["material"]), params=np.array(spec["params"], np.float64),
+        update=np.array(int(solver.requires_geometry_update)),
         K_indptr=K.indptr.astype(np.int32), K_indices=K.indices.astype(np.int32), K_data=K.data, T=T,
         sp_indices=solver.indices.astype(np.int32), sp_indptr=solver.indptr.astype(np.int32),
         sp_data_local=solver.data_local_indices.astype(np.int32),

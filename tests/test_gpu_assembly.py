@@ -30,6 +30,7 @@ def fl():
 
 
 def _asm(fl, d, mode, **kw):
+    kw.setdefault("requires_geometry_update", int(d["update"]))
     return fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], str(d["material"]),
                               tuple(d["params"]), mode=mode, **kw)
 
