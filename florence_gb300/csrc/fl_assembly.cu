@@ -66,6 +66,7 @@ struct AsmArgs {
     int *flags;
     double *Q;       // scratch [QSTRIDE][ldq]
     const float *Jmf;  // FP32 copy of Jm (the split-BF16 tangent's operand), or null
+    int utab;          // split-BF16 kernel: 1 = the element's U table is built in shared memory first
     int64_t e0, ne;  // element chunk [e0, e0+ne)
     int64_t ldq;     // leading dimension of Q (>= ne*nq)
 };
@@ -346,27 +347,19 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, DF ? AsmC
             }
             __syncthreads();
             if (active) {
-                // U_g[b][(i,d),k] for one (Gauss point, node b, row I = (i,d)) per work item: three
-                // entries, with compile-time indices into the packed tensor
-                for (int it = lt; it < qc * NPE * 9; it += TPE) {
-                    const int I = it % 9, qb = it / 9, q = qb / NPE, b = qb % NPE;
+                // U_g[b][(i,d),k], one entry per work item (balanced over the CTA's threads; the
+                // tensor index varies across a warp, so it is computed, not unrolled)
+                for (int idx = lt; idx < qc * NPE * 27; idx += TPE) {
+                    const int q = idx / (NPE * 27), r = idx % (NPE * 27), b = r / 27, s = r % 27;
+                    const int I = s / 3, k = s % 3;  // s = (i*3+d)*3 + k, I = i*3+d
                     const S *qq = Qs + ((size_t)slot * nq + c0 + q) * QSM;
                     const S *jb = Jc + (q * NPE + b) * 3;
-                    const S j0 = jb[0], j1 = jb[1], j2 = jb[2];
-                    S *uo = Us + (((size_t)slot * QC + q) * NPE + b) * 27;
-#pragma unroll
-                    for (int II = 0; II < 9; ++II) {
-                        if (II != I) continue;
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) {
-                            Acc u;
-                            AR::zero(u);
-                            AR::mac(u, qq[sym9(II, k * 3 + 2)], j2);
-                            AR::mac(u, qq[sym9(II, k * 3 + 1)], j1);
-                            AR::mac(u, qq[sym9(II, k * 3 + 0)], j0);
-                            uo[II * 3 + k] = AR::store(u);
-                        }
-                    }
+                    Acc u;
+                    AR::zero(u);
+                    AR::mac(u, qq[sym9(I, k * 3 + 2)], jb[2]);
+                    AR::mac(u, qq[sym9(I, k * 3 + 1)], jb[1]);
+                    AR::mac(u, qq[sym9(I, k * 3 + 0)], jb[0]);
+                    Us[(((size_t)slot * QC + q) * NPE + b) * 27 + s] = AR::store(u);
                 }
             }
             __syncthreads();
@@ -571,6 +564,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.Eulerx = Eulerx;
     A.Jm = Jm;
     A.Jmf = nullptr;
+    A.utab = 0;
     A.w = AllGauss;
     A.nelem = nelem;
     A.nnode = nnode;
@@ -665,6 +659,16 @@ __global__ void to_float(const double *a, float *b, int64_t n) {
     if (i < n) b[i] = (float)a[i];
 }
 
+// shared memory of the split-BF16 kernel without the U table (16-byte multiple)
+template <int NPE>
+__host__ __device__ inline size_t mixed_base_bytes(int nq) {
+    constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
+    const size_t b = sizeof(float) * (((size_t)nq * QSM + 3) / 4 * 4) +
+                     sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
+                     sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
+    return (b + 15) / 16 * 16;
+}
+
 template <int NPE>
 __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, float *V32) {
     constexpr int NDOF = 3 * NPE, M = 9 * NPE, NP = (NPE + 7) / 8 * 8, NT8 = NP / 8;
@@ -681,6 +685,7 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
     int *nodes = reinterpret_cast<int *>(Bl + NP * AST);                             // [NPE]
     int *inv = nodes + NPE;                                                          // [NDOF]
     int16_t *boff = reinterpret_cast<int16_t *>(inv + NDOF);                         // [NPE][NPE]
+    float *Ut = reinterpret_cast<float *>(smem_raw + mixed_base_bytes<NPE>(nq));      // [nq][NPE][27] if utab
     __shared__ int s_flag;
     __shared__ int64_t s_nnz;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
@@ -733,6 +738,21 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                 atomicAdd(A.T + 3 * (int64_t)nodes[a] + i, t);
             }
         }
+        if (A.utab)  // U_g[b][(i,d),k] of the whole element: all 27 entries of one (g, b) per work item,
+                     // compile-time tensor indices, no divergence
+            for (int it = tid; it < nq * NPE; it += MX_NT) {
+                const int g = it / NPE, b = it % NPE;
+                const float *qq = Qs + (size_t)g * QSM;
+                const float j0 = __ldg(A.Jmf + (size_t)b * nq + g), j1 = __ldg(A.Jmf + ((size_t)NPE + b) * nq + g),
+                            j2 = __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g);
+                float *uo = Ut + ((size_t)g * NPE + b) * 27;
+#pragma unroll
+                for (int II = 0; II < 9; ++II)
+#pragma unroll
+                    for (int k = 0; k < 3; ++k)
+                        uo[II * 3 + k] = fmaf(qq[sym9(II, k * 3 + 0)], j0,
+                                              fmaf(qq[sym9(II, k * 3 + 1)], j1, qq[sym9(II, k * 3 + 2)] * j2));
+            }
         for (int m0 = 0; m0 < M; m0 += MX_MC) {
             float acc[NT8][4];
 #pragma unroll
@@ -747,10 +767,14 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
                     if (r < M && cc < kc) {
                         const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
                         const int g = c / 3, d = c % 3, I = i * 3 + d;
-                        const float *qq = Qs + (size_t)g * QSM;  // U in FP32: the tangent's target accuracy
-                        v = fmaf(qq[sym9(I, k * 3 + 0)], __ldg(A.Jmf + ((size_t)0 * NPE + b) * nq + g),
-                                 fmaf(qq[sym9(I, k * 3 + 1)], __ldg(A.Jmf + ((size_t)1 * NPE + b) * nq + g),
-                                      qq[sym9(I, k * 3 + 2)] * __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g)));
+                        if (A.utab) {
+                            v = Ut[((size_t)g * NPE + b) * 27 + I * 3 + k];
+                        } else {
+                            const float *qq = Qs + (size_t)g * QSM;  // U in FP32: the tangent's target accuracy
+                            v = fmaf(qq[sym9(I, k * 3 + 0)], __ldg(A.Jmf + ((size_t)0 * NPE + b) * nq + g),
+                                     fmaf(qq[sym9(I, k * 3 + 1)], __ldg(A.Jmf + ((size_t)1 * NPE + b) * nq + g),
+                                          qq[sym9(I, k * 3 + 2)] * __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g)));
+                        }
                     }
                     bf16_split3(v, Ah[rr * AST + cc], Am[rr * AST + cc], Al[rr * AST + cc]);
                 }
@@ -823,17 +847,16 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
 }
 
 template <int NPE>
-static size_t mixed_smem_bytes(int nq) {
-    constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
-    return sizeof(float) * (((size_t)nq * QSM + 3) / 4 * 4) +
-           sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
-           sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
+static size_t mixed_smem_bytes(int nq, bool utab) {
+    return mixed_base_bytes<NPE>(nq) + (utab ? sizeof(float) * (size_t)nq * NPE * 27 : 0);
 }
 
 template <int NPE, int MAT>
 static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
     if (A.nelem == 0) return FL_OK;
-    const size_t smem = mixed_smem_bytes<NPE>(A.nq);
+    // the element's U table in shared memory when it fits with two CTAs per SM
+    A.utab = mixed_smem_bytes<NPE>(A.nq, true) <= 110 * 1024 ? 1 : 0;
+    const size_t smem = mixed_smem_bytes<NPE>(A.nq, A.utab != 0);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
     { const int st = ensure_smem<contract_mixed_kernel<NPE>>(smem); if (st != FL_OK) return st; }
     int64_t chunk = chunk_elements(CHUNK_BYTES, A.nq, 1);
@@ -952,6 +975,7 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.Eulerx = Eulerx;
     A.Jm = Jm;
     A.Jmf = nullptr;
+    A.utab = 0;
     A.w = AllGauss;
     A.nelem = nelem;
     A.nnode = nnode;

@@ -36,8 +36,7 @@ inline int ensure_smem(size_t bytes) {
     return FL_OK;
 }
 
-// Material numbers (match FL_MATERIAL_*).
-// material numbers follow the reference's explicit dispatcher
+// Material numbers (FL_MATERIAL_*), as the reference's explicit dispatcher numbers them
 // (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-106)
 enum { NEOHOOKEAN = 1, MOONEYRIVLIN = 2, NEARLYINCOMPRESSIBLEMR = 3, LINEARELASTIC = 10 };
 

@@ -347,7 +347,7 @@ def test_unsupported_material_raises(fl):
     d = load_golden("hex_p1_nh")
     solver, fs, form, mesh, material = _fake_florence_objects(d, True)
     with pytest.raises(NotImplementedError):
-        fl.material_params(material, "LinearElastic")
+        fl.material_params(material, "AnisotropicMooneyRivlin_1")
 
 
 def test_fp64_peak_is_measured(fl):
