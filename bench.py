@@ -609,7 +609,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
-    ap.add_argument("--arith", default="fp64", choices=["fp64", "float_pair", "mixed"],
+    ap.add_argument("--arith", default="float_pair", choices=["fp64", "float_pair", "mixed"],
                     help="arithmetic of the stiffness contraction (FP64, float pairs on the FP32 pipe, or the "
                          "split-BF16 tensor-core tangent with FP32 values)")
     ap.add_argument("--no-cpu", action="store_true")

@@ -401,8 +401,8 @@ ARITHMETIC = {"fp64": N.FL_ARITH_FP64, "float_pair": N.FL_ARITH_FLOAT_PAIR}
 
 def set_arithmetic(name):
     """Arithmetic of the stiffness contraction for every later FP64 assembly in the process:
-    'fp64' (FP64 multiply-adds) or 'float_pair' (hi + lo float pairs on the FP32 pipe, ~1e-14
-    relative to FP64). Kinematics, material, residual and scatter are FP64 in both."""
+    'float_pair' (the default: hi + lo float pairs on the FP32 pipe, ~1e-14 relative to FP64) or
+    'fp64' (FP64 multiply-adds). Kinematics, material, residual and scatter are FP64 in both."""
     N.check(N.lib().fl_SetAssemblyArithmetic(ARITHMETIC[name]), "fl_SetAssemblyArithmetic")
 
 

@@ -477,8 +477,9 @@ static int64_t chunk_elements(size_t bytes, int nq, int epc) {
     return ce - ce % epc;
 }
 
-// Arithmetic of the contraction kernel (fl_SetAssemblyArithmetic)
-static std::atomic<int> g_arith{FL_ARITH_FP64};
+// Arithmetic of the contraction kernel (fl_SetAssemblyArithmetic): float pairs by default, the
+// faster of the two on GB300, within the FP64 path's accuracy bar
+static std::atomic<int> g_arith{FL_ARITH_FLOAT_PAIR};
 
 // Runs A and B over [0, nelem) in chunks of at most `chunk` elements through scratch Q.
 template <int NPE, int MAT, bool DF>
@@ -854,8 +855,10 @@ static size_t mixed_smem_bytes(int nq, bool utab) {
 template <int NPE, int MAT>
 static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
     if (A.nelem == 0) return FL_OK;
-    // the element's U table in shared memory when it fits with two CTAs per SM
-    A.utab = mixed_smem_bytes<NPE>(A.nq, true) <= 110 * 1024 ? 1 : 0;
+    // the element's U table in shared memory when it costs no resident CTA per SM (the kernel is
+    // latency bound: fewer CTAs lose more than the table saves)
+    auto ctas = [](size_t bytes) { return (228 * 1024) / (bytes + 1024); };
+    A.utab = ctas(mixed_smem_bytes<NPE>(A.nq, true)) >= ctas(mixed_smem_bytes<NPE>(A.nq, false)) ? 1 : 0;
     const size_t smem = mixed_smem_bytes<NPE>(A.nq, A.utab != 0);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
     { const int st = ensure_smem<contract_mixed_kernel<NPE>>(smem); if (st != FL_OK) return st; }

@@ -26,6 +26,7 @@
 // slots), and the host checks the done flag every PCG_CHECK iterations.
 #include <algorithm>
 #include <mutex>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -38,7 +39,8 @@ constexpr int PCG_CHECK = 16;
 
 struct PcgState {
     double *r, *z, *p, *q, *Binv;  // vectors [n], block inverses [n/3][9]
-    float *ph, *pl;                // p as a float pair (p ~ ph + pl), for FP32-valued matrices
+    float *ph, *pl;                // p as a float pair (p ~ ph + pl), for the float-pair products
+    float *qh, *ql;                // q = K p as a float pair, written by the float-pair products
     double *acc;                   // [0] p.q, [1],[2] r.z of even/odd iterates, [3] r.r, [4] |b|^2
     int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
 };
@@ -58,6 +60,8 @@ static size_t pcg_layout(int64_t n, int64_t nnz, PcgState *s, char *base, float2
     t.Binv = (double *)take(sizeof(double) * (n / 3) * 9);
     t.ph = (float *)take(sizeof(float) * n);
     t.pl = (float *)take(sizeof(float) * n);
+    t.qh = (float *)take(sizeof(float) * n);
+    t.ql = (float *)take(sizeof(float) * n);
     t.acc = (double *)take(sizeof(double) * 8);
     t.done = (int *)take(sizeof(int) * 4);
     float2 *vs = (float2 *)take(sizeof(float2) * (size_t)nnz);
@@ -169,14 +173,14 @@ __global__ void __launch_bounds__(PCG_NT) pcg_init2(int64_t nnode, PcgState s) {
     block_atomic_add(rz, s.acc + 1);
 }
 
-// Node-block product with 8 lanes per node (4 nodes per warp): lanes over neighbour slots s,
-// m = indices[indptr[3n] + 3s] / 3, values V[indptr[3n+i] + 3s + j]; the 8 partial sums are
-// combined with 3 shuffle steps. FP64 values: FP64 products. FP32 values: each product and sum
-// is carried as an unevaluated float pair (error-free product by FMA, compensated two-sum), with
-// p given as a float pair too, so the FP32 matrix is applied to ~2^-44 relative accuracy while
-// every operation runs on the FP32 pipe (GB300's FP64 rate would otherwise bound this loop).
-// lanes per node of the node-block product: 4, 8, 16 or 32, chosen per matrix by timing
-// (pick_lanes)
+// Node-block product with NB lanes per node (32 / NB nodes per warp; NB = 4, 8, 16 or 32,
+// chosen per matrix by timing, pick_lanes): lanes over neighbour slots s,
+// m = indices[indptr[3n] + 3s] / 3, values V[indptr[3n+i] + 3s + j]; the NB partial sums are
+// combined with log2(NB) shuffle steps. FP64 values: FP64 products (node_block_row). FP32 values
+// and split FP64 values: each product and sum is carried as an unevaluated float pair
+// (error-free product by FMA, compensated two-sum), with p given as a float pair too, so the
+// matrix is applied to ~2^-44 relative accuracy while every operation runs on the FP32 pipe
+// (node_block_pair; GB300's FP64 rate would otherwise bound this loop).
 
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
@@ -219,46 +223,6 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
     }
 }
 
-template <int NB>
-__device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const float *vals,
-                                               const PcgState &st, int64_t node, bool valid, int sub, double &y0,
-                                               double &y1, double &y2) {
-    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
-    if (valid) {
-        const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
-        const int nb = (r1 - r0) / 3;
-        for (int sl = sub; sl < nb; sl += NB) {
-            const int m3 = indices[r0 + 3 * sl];
-            const float h0 = st.ph[m3], h1 = st.ph[m3 + 1], h2 = st.ph[m3 + 2];
-            const float l0 = st.pl[m3], l1 = st.pl[m3 + 1], l2 = st.pl[m3 + 2];
-            const float *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
-            df_mac(v0[0], h0, l0, s0, c0); df_mac(v0[1], h1, l1, s0, c0); df_mac(v0[2], h2, l2, s0, c0);
-            df_mac(v1[0], h0, l0, s1, c1); df_mac(v1[1], h1, l1, s1, c1); df_mac(v1[2], h2, l2, s1, c1);
-            df_mac(v2[0], h0, l0, s2, c2); df_mac(v2[1], h1, l1, s2, c2); df_mac(v2[2], h2, l2, s2, c2);
-        }
-    }
-#pragma unroll
-    for (int o = NB / 2; o > 0; o >>= 1) {
-        float t, e;
-        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB), t, e);
-        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB);
-        s0 = t;
-        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB), t, e);
-        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB);
-        s1 = t;
-        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB), t, e);
-        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB);
-        s2 = t;
-    }
-    if (sub == 0) {  // only the group's first lane holds the sums (the conversions run on the FP64 pipe)
-        y0 = (double)s0 + (double)c0;
-        y1 = (double)s1 + (double)c1;
-        y2 = (double)s2 + (double)c2;
-    } else {
-        y0 = y1 = y2 = 0.0;
-    }
-}
-
 // (s, c) += (vh + vl) * (ph + pl), dropping vl*pl (2^-48 relative)
 __device__ __forceinline__ void df_mac2(float2 v, float ph, float pl, float &s, float &c) {
     const float prod = v.x * ph;
@@ -269,10 +233,16 @@ __device__ __forceinline__ void df_mac2(float2 v, float ph, float pl, float &s, 
     c += e + fmaf(v.x, pl, fmaf(v.y, ph, perr));
 }
 
-template <int NB>
-__device__ __forceinline__ void node_block_row(const int32_t *indptr, const int32_t *indices, const float2 *vals,
-                                               const PcgState &st, int64_t node, bool valid, int sub, double &y0,
-                                               double &y1, double &y2) {
+__device__ __forceinline__ void pair_mac(float v, float ph, float pl, float &s, float &c) { df_mac(v, ph, pl, s, c); }
+__device__ __forceinline__ void pair_mac(float2 v, float ph, float pl, float &s, float &c) { df_mac2(v, ph, pl, s, c); }
+
+// Node-block product rows of node `node` as unevaluated float pairs (s_i + c_i), summed over the
+// NB lanes of the group; lane sub == 0 holds the totals. No FP64 instruction: on GB300 each one
+// occupies the FP64 pipe for a whole warp, even with one lane active.
+template <int NB, class VT>
+__device__ __forceinline__ void node_block_pair(const int32_t *indptr, const int32_t *indices, const VT *vals,
+                                                const PcgState &st, int64_t node, bool valid, int sub, float *sh,
+                                                float *sc) {
     float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
     if (valid) {
         const int r0 = indptr[3 * node], r1 = indptr[3 * node + 1], r2 = indptr[3 * node + 2];
@@ -281,10 +251,10 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
             const int m3 = indices[r0 + 3 * sl];
             const float h0 = st.ph[m3], h1 = st.ph[m3 + 1], h2 = st.ph[m3 + 2];
             const float l0 = st.pl[m3], l1 = st.pl[m3 + 1], l2 = st.pl[m3 + 2];
-            const float2 *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
-            df_mac2(v0[0], h0, l0, s0, c0); df_mac2(v0[1], h1, l1, s0, c0); df_mac2(v0[2], h2, l2, s0, c0);
-            df_mac2(v1[0], h0, l0, s1, c1); df_mac2(v1[1], h1, l1, s1, c1); df_mac2(v1[2], h2, l2, s1, c1);
-            df_mac2(v2[0], h0, l0, s2, c2); df_mac2(v2[1], h1, l1, s2, c2); df_mac2(v2[2], h2, l2, s2, c2);
+            const VT *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
+            pair_mac(v0[0], h0, l0, s0, c0); pair_mac(v0[1], h1, l1, s0, c0); pair_mac(v0[2], h2, l2, s0, c0);
+            pair_mac(v1[0], h0, l0, s1, c1); pair_mac(v1[1], h1, l1, s1, c1); pair_mac(v1[2], h2, l2, s1, c1);
+            pair_mac(v2[0], h0, l0, s2, c2); pair_mac(v2[1], h1, l1, s2, c2); pair_mac(v2[2], h2, l2, s2, c2);
         }
     }
 #pragma unroll
@@ -300,13 +270,8 @@ __device__ __forceinline__ void node_block_row(const int32_t *indptr, const int3
         c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB);
         s2 = t;
     }
-    if (sub == 0) {  // only the group's first lane holds the sums (the conversions run on the FP64 pipe)
-        y0 = (double)s0 + (double)c0;
-        y1 = (double)s1 + (double)c1;
-        y2 = (double)s2 + (double)c2;
-    } else {
-        y0 = y1 = y2 = 0.0;
-    }
+    sh[0] = s0; sh[1] = s1; sh[2] = s2;
+    sc[0] = c0; sc[1] = c1; sc[2] = c2;
 }
 
 __device__ __forceinline__ double to_d(double v) { return v; }
@@ -361,7 +326,32 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
     const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
     double pq = 0.0;
-    if (NODEBLK) {
+    constexpr bool PAIR = !std::is_same<VT, double>::value;
+    if constexpr (NODEBLK && PAIR) {  // float-pair products: q and p.q stay float pairs (FP32 pipe only)
+        const int grp = lane / NB, sub = lane % NB;
+        const int64_t nnode = n / 3;
+        float pqs = 0.f, pqc = 0.f;
+        for (int64_t base = warp * (32 / NB); base < nnode; base += nwarps * (32 / NB)) {
+            const int64_t m = base + grp;
+            float sh[3], sc[3];
+            node_block_pair<NB>(indptr, indices, vals, s, m, m < nnode, sub, sh, sc);
+            if (sub == 0 && m < nnode) {
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int64_t d = 3 * m + i;
+                    float h = 0.f, l = 0.f;
+                    if (!fixed[d]) {  // renormalised pair
+                        h = sh[i] + sc[i];
+                        l = sc[i] - (h - sh[i]);
+                    }
+                    s.qh[d] = h;
+                    s.ql[d] = l;
+                    df_mac2(make_float2(h, l), s.ph[d], s.pl[d], pqs, pqc);
+                }
+            }
+        }
+        pq = (double)pqs + (double)pqc;  // once per thread
+    } else if constexpr (NODEBLK) {
         const int grp = lane / NB, sub = lane % NB;
         const int64_t nnode = n / 3;
         for (int64_t base = warp * (32 / NB); base < nnode; base += nwarps * (32 / NB)) {
@@ -396,7 +386,7 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
 
 // K2: alpha = rz_k / p.q, x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r. One thread per
 // dof, 30 lanes of a warp = 10 nodes; a node's three residual entries meet through shuffles.
-__global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x, PcgState s) {
+__global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x, PcgState s, int qpair) {
     // one read of the done flag and one division per CTA (FP64 division is a long FP64-pipe
     // sequence); the flag read by one thread keeps the early return uniform across the CTA
     __shared__ double s_alpha;
@@ -419,7 +409,8 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x
         double rv = 0.0;
         if (valid) {
             x[d] = fma(alpha, s.p[d], x[d]);
-            rv = fma(-alpha, s.q[d], s.r[d]);
+            const double qd = qpair ? (double)s.qh[d] + (double)s.ql[d] : s.q[d];
+            rv = fma(-alpha, qd, s.r[d]);
             s.r[d] = rv;
         }
         const double r0 = __shfl_sync(0xffffffffu, rv, l0);
@@ -614,7 +605,7 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
             if (split) launch_k1_nb<float2>(nb, indptr, indices, vsplit, fixed, n, (int)k, s, st);
             else if (nodeblk) launch_k1_nb<VT>(nb, indptr, indices, vals, fixed, n, (int)k, s, st);
             else pcg_k1<VT, false><<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
-            pcg_k2<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, x, s);
+            pcg_k2<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, x, s, (nodeblk && (split || sizeof(VT) == 4)) ? 1 : 0);
             pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, (sizeof(VT) == 4 || split) ? 1 : 0, s);
         }
         FL_CUDA_TRY(cudaGetLastError());

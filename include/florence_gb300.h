@@ -185,10 +185,10 @@ int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
 
 /* Arithmetic of the stiffness contraction in every later FP64-valued assembly call of the process
  * (no reference counterpart; the reference contracts in FP64). FL_ARITH_FP64: FP64 fused
- * multiply-adds (the default). FL_ARITH_FLOAT_PAIR: each operand held as an unevaluated pair of
+ * multiply-adds. FL_ARITH_FLOAT_PAIR (the default): each operand held as an unevaluated pair of
  * floats (hi + lo), products formed error-free in their leading part and summed with a
  * compensated two-sum on the FP32 pipe, ~2^-46 relative per multiply-add (element matrices
- * within ~1e-14 of FP64). The kinematics, the material law, the residual and the scatter stay FP64
+ * within ~1e-14 of FP64), about 1.6x faster on GB300, whose FP64 rate is 1/64 of its FP32 rate. The kinematics, the material law, the residual and the scatter stay FP64
  * in both. FL_ERR_ARG for other values. */
 #define FL_ARITH_FP64 0
 #define FL_ARITH_FLOAT_PAIR 1

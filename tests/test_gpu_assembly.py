@@ -65,18 +65,27 @@ def test_csr_assembly_matches_reference(fl, case, mode):
 
 @pytest.mark.parametrize("case", golden_cases())
 @pytest.mark.parametrize("mode", ["csr", "squeeze", "triplet"])
-def test_float_pair_contraction_matches_reference(fl, case, mode):
-    """The contraction in float-pair arithmetic on the FP32 pipe meets the FP64 path's bar
-    (1e-12 relative Frobenius against the reference) in every scatter mode; the residual is
-    formed in FP64 as before (equal to the FP64 run's up to the order of the atomic sums)."""
+def test_both_contraction_arithmetics_match_reference(fl, case, mode):
+    """The contraction in FP64 multiply-adds and in float-pair arithmetic on the FP32 pipe (the
+    default; every other test runs it) both meet the FP64 path's bar (1e-12 relative Frobenius
+    against the reference) in every scatter mode; the residual is formed in FP64 either way (the
+    two agree up to the order of the atomic sums)."""
     d = load_golden(case)
     asm = _asm(fl, d, mode)
     x = torch.from_numpy(d["Eulerx"]).cuda()
-    out64 = asm.assemble(x)
-    with fl.arithmetic("float_pair"):
-        assert fl.get_arithmetic() == "float_pair"
-        out = asm.assemble(x)
-    assert fl.get_arithmetic() == "fp64"
+    assert fl.get_arithmetic() == "float_pair"
+    with fl.arithmetic("fp64"):
+        assert fl.get_arithmetic() == "fp64"
+        out64 = asm.assemble(x)
+    assert fl.get_arithmetic() == "float_pair"
+    out = asm.assemble(x)
+    if mode == "triplet":
+        n = d["points"].shape[0] * 3
+        K64 = sp.csr_matrix((out64[2].cpu().numpy(), (out64[0].cpu().numpy(), out64[1].cpu().numpy())), shape=(n, n))
+        ref = sp.csr_matrix((d["K_data"], d["K_indices"], d["K_indptr"]), shape=(n, n))
+        assert spla.norm(K64 - ref) / spla.norm(ref) < TOL
+    else:
+        assert rel_fro(out64[0].cpu().numpy(), d["K_data"]) < TOL
     asm.check_flags()
     V, T = out[-2], out[-1]
     assert rel_fro(T.cpu().numpy(), out64[-1].cpu().numpy()) < 1e-14
