@@ -43,7 +43,6 @@ struct PcgState {
     float *qh, *ql;                // q = K p as a float pair, written by the float-pair products
     double *acc;                   // [0] p.q, [1],[2] r.z of even/odd iterates, [3] r.r, [4] |b|^2
     int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
-    unsigned *bar;                 // [0] arrivals, [1] generation: grid barrier of the persistent kernel
 };
 
 static size_t pcg_layout(int64_t n, int64_t nnz, PcgState *s, char *base, float2 **vsplit = nullptr) {
@@ -65,7 +64,6 @@ static size_t pcg_layout(int64_t n, int64_t nnz, PcgState *s, char *base, float2
     t.ql = (float *)take(sizeof(float) * n);
     t.acc = (double *)take(sizeof(double) * 8);
     t.done = (int *)take(sizeof(int) * 4);
-    t.bar = (unsigned *)take(sizeof(unsigned) * 2);
     float2 *vs = (float2 *)take(sizeof(float2) * (size_t)nnz);
     if (vsplit) *vsplit = vs;
     if (s) *s = t;
@@ -462,177 +460,6 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, 
     }
 }
 
-// ------------------------------------------------------------------------------------------------
-// Persistent variant: the three phases of many iterations in one cooperative launch (every CTA
-// resident), separated by grid barriers instead of kernel boundaries. Same arithmetic as
-// K1/K2/K3 with the node-block float-pair product. Vectors written by other CTAs within the launch
-// are read through L2 (__ldcg), never from a possibly stale L1 line.
-//
-// Grid barrier: arrival counter + generation word; the last arriving CTA resets the counter and
-// bumps the generation, the others wait for the bump. The wait is bounded (PCG_SPIN_LIMIT polls,
-// ~1 s): on expiry the CTA sets error bit 16 and every CTA leaves at its next barrier check, so
-// a launch that cannot complete ends with an error status instead of hanging.
-// ------------------------------------------------------------------------------------------------
-constexpr long long PCG_SPIN_LIMIT = 1ll << 22;
-
-__device__ __forceinline__ bool grid_barrier(const PcgState &s, unsigned nblocks) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *gen = s.bar + 1;
-        const unsigned g = *gen;
-        __threadfence();  // this CTA's writes before its arrival
-        if (atomicAdd(s.bar, 1u) == nblocks - 1) {
-            atomicExch(s.bar, 0u);
-            __threadfence();
-            atomicAdd(s.bar + 1, 1u);
-        } else {
-            long long spins = 0;
-            while (*gen == g) {
-                if (++spins > PCG_SPIN_LIMIT) {
-                    atomicOr(s.done + 2, 16);
-                    break;
-                }
-                __nanosleep(64);
-            }
-        }
-        __threadfence();
-        s_ok = !(*(volatile int *)(s.done + 2) & 16);
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-template <class MT, int NB>
-__global__ void __launch_bounds__(PCG_NT) pcg_persistent(const int32_t *indptr, const int32_t *indices,
-                                                         const MT *vals, const int8_t *fixed, int64_t n, int k0,
-                                                         int kend, double tol2, double *x, PcgState s) {
-    const unsigned nblocks = gridDim.x;
-    const int lane = threadIdx.x & 31;
-    const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
-    const int64_t nnode = n / 3;
-    __shared__ double s_sc[2];
-    for (int k = k0; k < kend; ++k) {
-        // A: q = mask(K p) as float pairs, p.q; zero the slots B accumulates into
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            s.acc[1 + ((k + 1) & 1)] = 0.0;
-            s.acc[3] = 0.0;
-        }
-        {
-            const int grp = lane / NB, sub = lane % NB;
-            float pqs = 0.f, pqc = 0.f;
-            for (int64_t base = warp * (32 / NB); base < nnode; base += nwarps * (32 / NB)) {
-                const int64_t m = base + grp;
-                float sh[3] = {0.f, 0.f, 0.f}, sc[3] = {0.f, 0.f, 0.f};
-                {
-                    // the product reads ph/pl through L2: they were written by phase C
-                    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
-                    if (m < nnode) {
-                        const int r0 = indptr[3 * m], r1 = indptr[3 * m + 1], r2 = indptr[3 * m + 2];
-                        const int nbk = (r1 - r0) / 3;
-                        for (int sl = sub; sl < nbk; sl += NB) {
-                            const int m3 = indices[r0 + 3 * sl];
-                            const float h0 = __ldcg(s.ph + m3), h1 = __ldcg(s.ph + m3 + 1), h2 = __ldcg(s.ph + m3 + 2);
-                            const float l0 = __ldcg(s.pl + m3), l1 = __ldcg(s.pl + m3 + 1), l2 = __ldcg(s.pl + m3 + 2);
-                            const MT *v0 = vals + r0 + 3 * sl, *v1 = vals + r1 + 3 * sl, *v2 = vals + r2 + 3 * sl;
-                            pair_mac(v0[0], h0, l0, s0, c0); pair_mac(v0[1], h1, l1, s0, c0); pair_mac(v0[2], h2, l2, s0, c0);
-                            pair_mac(v1[0], h0, l0, s1, c1); pair_mac(v1[1], h1, l1, s1, c1); pair_mac(v1[2], h2, l2, s1, c1);
-                            pair_mac(v2[0], h0, l0, s2, c2); pair_mac(v2[1], h1, l1, s2, c2); pair_mac(v2[2], h2, l2, s2, c2);
-                        }
-                    }
-#pragma unroll
-                    for (int o = NB / 2; o > 0; o >>= 1) {
-                        float t, e;
-                        two_sum(s0, __shfl_down_sync(0xffffffffu, s0, o, NB), t, e);
-                        c0 += e + __shfl_down_sync(0xffffffffu, c0, o, NB);
-                        s0 = t;
-                        two_sum(s1, __shfl_down_sync(0xffffffffu, s1, o, NB), t, e);
-                        c1 += e + __shfl_down_sync(0xffffffffu, c1, o, NB);
-                        s1 = t;
-                        two_sum(s2, __shfl_down_sync(0xffffffffu, s2, o, NB), t, e);
-                        c2 += e + __shfl_down_sync(0xffffffffu, c2, o, NB);
-                        s2 = t;
-                    }
-                    sh[0] = s0; sh[1] = s1; sh[2] = s2;
-                    sc[0] = c0; sc[1] = c1; sc[2] = c2;
-                }
-                if (sub == 0 && m < nnode) {
-#pragma unroll
-                    for (int i = 0; i < 3; ++i) {
-                        const int64_t d = 3 * m + i;
-                        float h = 0.f, l = 0.f;
-                        if (!fixed[d]) {
-                            h = sh[i] + sc[i];
-                            l = sc[i] - (h - sh[i]);
-                        }
-                        s.qh[d] = h;
-                        s.ql[d] = l;
-                        df_mac2(make_float2(h, l), __ldcg(s.ph + d), __ldcg(s.pl + d), pqs, pqc);
-                    }
-                }
-            }
-            block_atomic_add((double)pqs + (double)pqc, s.acc + 0);
-        }
-        if (!grid_barrier(s, nblocks)) return;
-        // B: alpha, x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r
-        if (threadIdx.x == 0) s_sc[0] = __ldcg(s.acc + 1 + (k & 1)) / __ldcg(s.acc + 0);
-        __syncthreads();
-        {
-            const double alpha = s_sc[0];
-            const int ln = lane / 3, i = lane % 3, l0 = 3 * ln;
-            double rzn = 0.0, rr = 0.0;
-            for (int64_t base = warp * 10; base < nnode; base += nwarps * 10) {
-                const int64_t m = base + ln;
-                const bool valid = lane < 30 && m < nnode;
-                const int64_t d = 3 * m + i;
-                double rv = 0.0;
-                if (valid) {
-                    x[d] = fma(alpha, __ldcg(s.p + d), x[d]);
-                    const double qd = (double)__ldcg(s.qh + d) + (double)__ldcg(s.ql + d);
-                    rv = fma(-alpha, qd, s.r[d]);
-                    s.r[d] = rv;
-                }
-                const double r0 = __shfl_sync(0xffffffffu, rv, l0);
-                const double r1 = __shfl_sync(0xffffffffu, rv, (l0 + 1) & 31);
-                const double r2 = __shfl_sync(0xffffffffu, rv, (l0 + 2) & 31);
-                if (valid) {
-                    const double *B = s.Binv + m * 9 + i * 3;
-                    const double z = fma(B[0], r0, fma(B[1], r1, B[2] * r2));
-                    s.z[d] = z;
-                    rzn = fma(rv, z, rzn);
-                    rr = fma(rv, rv, rr);
-                }
-            }
-            block_atomic_add(rzn, s.acc + 1 + ((k + 1) & 1));
-            block_atomic_add(rr, s.acc + 3);
-        }
-        if (!grid_barrier(s, nblocks)) return;
-        // C: convergence test (every CTA reads the same sums), beta, p = z + beta p
-        if (threadIdx.x == 0) {
-            s_sc[0] = __ldcg(s.acc + 1 + ((k + 1) & 1)) / __ldcg(s.acc + 1 + (k & 1));
-            s_sc[1] = __ldcg(s.acc + 3);
-        }
-        __syncthreads();
-        const double beta = s_sc[0], rrk = s_sc[1];
-        if (rrk <= tol2 || !isfinite(rrk)) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) {
-                s.done[0] = 1;
-                s.done[1] = k + 1;
-                if (!isfinite(rrk)) s.done[2] |= 4;
-            }
-            return;
-        }
-        for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT) {
-            const double pv = fma(beta, __ldcg(s.p + d), __ldcg(s.z + d));
-            s.p[d] = pv;
-            split_store(s, d, pv);
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) s.acc[0] = 0.0;  // B has read p.q
-        if (!grid_barrier(s, nblocks)) return;
-    }
-}
-
 // Resident blocks of a kernel over the whole GPU (one wave), for grid sizes of the grid-stride
 // kernels.
 template <auto Kernel>
@@ -718,42 +545,6 @@ static int pick_lanes(const int32_t *indptr, const int32_t *indices, const MT *v
     return best;
 }
 
-// Persistent launch: returns cudaSuccess, or the launch error (the caller then uses the
-// three-kernel loop).
-template <class MT, int NB>
-static cudaError_t launch_persistent(const int32_t *indptr, const int32_t *indices, const MT *vals,
-                                     const int8_t *fixed, int64_t n, int k0, int kend, double tol2, double *x,
-                                     const PcgState &s, cudaStream_t st) {
-    static thread_local int64_t grid[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    int64_t &g = grid[dev & 63];
-    if (g == 0) g = resident_blocks<pcg_persistent<MT, NB>>();
-    const int64_t need = (n / 3 + (PCG_NT / 32) * (32 / NB) - 1) / ((PCG_NT / 32) * (32 / NB));
-    const unsigned blocks = (unsigned)std::max<int64_t>(1, std::min(g, need));
-    cudaError_t e = cudaMemsetAsync(s.bar, 0, sizeof(unsigned) * 2, st);
-    if (e != cudaSuccess) return e;
-    PcgState sc = s;
-    void *args[] = {(void *)&indptr, (void *)&indices, (void *)&vals, (void *)&fixed, (void *)&n, (void *)&k0,
-                    (void *)&kend,   (void *)&tol2,    (void *)&x,    (void *)&sc};
-    return cudaLaunchCooperativeKernel((const void *)pcg_persistent<MT, NB>, dim3(blocks), dim3(PCG_NT), args, 0, st);
-}
-
-template <class MT>
-static cudaError_t launch_persistent_nb(int nb, const int32_t *indptr, const int32_t *indices, const MT *vals,
-                                        const int8_t *fixed, int64_t n, int k0, int kend, double tol2, double *x,
-                                        const PcgState &s, cudaStream_t st) {
-    switch (nb) {
-        case 4: return launch_persistent<MT, 4>(indptr, indices, vals, fixed, n, k0, kend, tol2, x, s, st);
-        case 16: return launch_persistent<MT, 16>(indptr, indices, vals, fixed, n, k0, kend, tol2, x, s, st);
-        case 32: return launch_persistent<MT, 32>(indptr, indices, vals, fixed, n, k0, kend, tol2, x, s, st);
-        default: return launch_persistent<MT, 8>(indptr, indices, vals, fixed, n, k0, kend, tol2, x, s, st);
-    }
-}
-
-// iterations per persistent launch (the host reads the done flag between launches)
-constexpr int PCG_PERSIST = 256;
-
 template <class VT>
 static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals, int64_t n, const int8_t *fixed,
                   const double *b, double *x, double rtol, int64_t maxiter, void *ws, size_t ws_bytes,
@@ -808,27 +599,7 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     const double tol2 = rtol * rtol * b2;
     int hd[4] = {0, 0, 0, 0};
     int64_t k = 0;
-    // float-pair products: all iterations in persistent cooperative launches
-    const bool pair = nodeblk && (split || sizeof(VT) == 4);
-    bool persistent = pair;
-    while (persistent && k < maxiter) {
-        const int64_t kend = std::min<int64_t>(maxiter, k + PCG_PERSIST);
-        cudaError_t e;
-        if (split) e = launch_persistent_nb<float2>(nb, indptr, indices, vsplit, fixed, n, (int)k, (int)kend, tol2, x, s, st);
-        else e = launch_persistent_nb<float>(nb, indptr, indices, reinterpret_cast<const float *>(vals), fixed, n,
-                                             (int)k, (int)kend, tol2, x, s, st);
-        if (e != cudaSuccess) {  // cooperative launch unavailable: the three-kernel loop below
-            cudaGetLastError();
-            persistent = false;
-            break;
-        }
-        FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
-        FL_CUDA_TRY(cudaStreamSynchronize(st));
-        if (hd[2] & 16) return FL_ERR_CUDA;  // a grid barrier timed out
-        if (hd[0]) break;
-        k = kend;
-    }
-    while (!persistent && k < maxiter) {
+    while (k < maxiter) {
         const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
         for (; k < kend; ++k) {
             if (split) launch_k1_nb<float2>(nb, indptr, indices, vsplit, fixed, n, (int)k, s, st);
@@ -844,7 +615,6 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     }
     FL_CUDA_TRY(cudaMemcpyAsync(hacc, s.acc, sizeof(hacc), cudaMemcpyDeviceToHost, st));
     FL_CUDA_TRY(cudaStreamSynchronize(st));
-    if (persistent && !hd[0]) k = maxiter;
     *iters = hd[0] ? hd[1] : maxiter;
     *relres = sqrt(hacc[3] / b2);
     if (hd[2] & 4) return FL_ERR_ARG;  // breakdown: non-finite residual
