@@ -660,12 +660,20 @@ __global__ void to_float(const double *a, float *b, int64_t n) {
     if (i < n) b[i] = (float)a[i];
 }
 
+// reduction-chunk width of the split-BF16 kernel: the padded 3*nq, at most MX_KC (the operand
+// buffers are sized by it, so short reductions leave room for more resident CTAs)
+__host__ __device__ inline int mixed_kc(int nq) {
+    const int kp = (3 * nq + 15) / 16 * 16;
+    return kp < MX_KC ? kp : MX_KC;
+}
+
 // shared memory of the split-BF16 kernel without the U table (16-byte multiple)
 template <int NPE>
 __host__ __device__ inline size_t mixed_base_bytes(int nq) {
-    constexpr int NP = (NPE + 7) / 8 * 8, AST = MX_KC + 8;
+    constexpr int NP = (NPE + 7) / 8 * 8;
+    const int ast = mixed_kc(nq) + 8;
     const size_t b = sizeof(float) * (((size_t)nq * QSM + 3) / 4 * 4) +
-                     sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * AST + (size_t)NP * AST) +
+                     sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * ast + (size_t)NP * ast) +
                      sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
     return (b + 15) / 16 * 16;
 }
@@ -673,8 +681,8 @@ __host__ __device__ inline size_t mixed_base_bytes(int nq) {
 template <int NPE>
 __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, float *V32) {
     constexpr int NDOF = 3 * NPE, M = 9 * NPE, NP = (NPE + 7) / 8 * 8, NT8 = NP / 8;
-    constexpr int AST = MX_KC + 8;  // padded row stride (bf16) of the A chunk
     const int nq = A.nq, K = 3 * nq;
+    const int KC = mixed_kc(nq), AST = KC + 8;  // chunk width and padded row stride (bf16) of the operands
     extern __shared__ __align__(16) unsigned char smem_raw[];
     float *Qs = reinterpret_cast<float *>(smem_raw);                                // [nq][QSM]
     __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + ((size_t)nq * QSM + 3) / 4 * 4);  // [3][MX_MC][AST]
@@ -758,8 +766,8 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
             float acc[NT8][4];
 #pragma unroll
             for (int t = 0; t < NT8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-            for (int k0 = 0; k0 < K; k0 += MX_KC) {
-                const int kc = min(MX_KC, K - k0), kcp = (kc + 15) / 16 * 16;
+            for (int k0 = 0; k0 < K; k0 += KC) {
+                const int kc = min(KC, K - k0), kcp = (kc + 15) / 16 * 16;
                 __syncthreads();  // previous chunk's MMAs done
                 // A chunk: rows r = m0 + rr -> (i, b, k) with r = (i*NPE + b)*3 + k; cols c = k0 + cc -> (g, d)
                 for (int idx = tid; idx < MX_MC * kcp; idx += MX_NT) {
