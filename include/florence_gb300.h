@@ -310,6 +310,12 @@ int fl_MLPAdamStep(float *params, const float *grads, float *m, float *v, int64_
 int fl_measure_fp64_peak(double *gflops, fl_stream_t stream);
 int fl_measure_fp32_peak(double *gflops, fl_stream_t stream);
 
+/* Self-test of the tcgen05 tensor-core path (no reference counterpart): D [128 x 32] (FP32,
+ * row-major) = A [128 x 48] * B [32 x 48]^T with BF16 A and B (row-major, device pointers), one
+ * CTA, operands in shared memory, accumulator in tensor memory. *status (device) gets bit 1 if
+ * the completion wait timed out. */
+int fl_TensorCoreSelfTest(const void *A_bf16, const void *B_bf16, float *D, int *status, fl_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
