@@ -27,6 +27,7 @@
 #include <mutex>
 
 #include "fl_common.cuh"
+#include "fl_tc.cuh"
 
 namespace fl {
 
@@ -855,6 +856,218 @@ __global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, 
     if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
 }
 
+// ------------------------------------------------------------------------------------------------
+// D. The split-BF16 tangent on the fifth-generation tensor cores (tcgen05). Same operands and
+// products as contract_mixed_kernel, organised for the tensor core: per element and 128-row tile
+// of K^T[(i,b,k), a], the three BF16 terms of U (A operand, 128 x KC) and of Jm (B operand,
+// NB x KC, NB = NPE padded to 16) are written to shared memory in the K-major core-matrix layout;
+// one thread issues the six products per 16-wide K step as tcgen05.mma into an FP32 accumulator
+// in tensor memory and commits them to an mbarrier; after the last K chunk each warp reads its 32
+// accumulator rows with tcgen05.ld and scatters them. The B operand depends only on the element
+// type: with a single K chunk it is built once per CTA. Waits are bounded (on expiry the element
+// is skipped and FL_FLAG_BAD_INDEX raised, so the call reports an error).
+// ------------------------------------------------------------------------------------------------
+constexpr int TC_MT = 128;
+constexpr long long TC_WAIT = 1ll << 22;
+
+template <int NPE>
+__host__ __device__ constexpr int tc_nb() { return (NPE + 15) / 16 * 16; }
+
+template <int NPE>
+__host__ __device__ constexpr int tc_tmem_cols() {
+    const int n = (tc_nb<NPE>() + 31) / 32 * 32;
+    return n <= 32 ? 32 : (n <= 64 ? 64 : (n <= 128 ? 128 : 256));
+}
+
+// shared memory: Qs float [nq][QSM] | A terms 3 x [128][KC] bf16 | B terms 3 x [NB][KC] bf16 |
+// nodes, inv, boff
+template <int NPE>
+__host__ __device__ inline size_t tc_smem_bytes(int nq) {
+    const int kc = mixed_kc(nq);
+    const size_t b = sizeof(float) * (((size_t)nq * QSM + 31) / 32 * 32) +
+                     sizeof(__nv_bfloat16) * 3 * ((size_t)TC_MT * kc + (size_t)tc_nb<NPE>() * kc) +
+                     sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
+    return (b + 127) / 128 * 128;
+}
+
+template <int NPE>
+__global__ void __launch_bounds__(128) contract_tc_kernel(const AsmArgs A, float *V32) {
+    constexpr int NDOF = 3 * NPE, M = 9 * NPE, NB = (NPE + 15) / 16 * 16;
+    const int nq = A.nq, K = 3 * nq, KC = mixed_kc(nq);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float *Qs = reinterpret_cast<float *>(smem_raw);  // [nq][QSM]
+    __nv_bfloat16 *At[3], *Bt[3];
+    At[0] = reinterpret_cast<__nv_bfloat16 *>(smem_raw + sizeof(float) * (((size_t)nq * QSM + 31) / 32 * 32));
+    At[1] = At[0] + TC_MT * KC;
+    At[2] = At[1] + TC_MT * KC;
+    Bt[0] = At[2] + TC_MT * KC;
+    Bt[1] = Bt[0] + NB * KC;
+    Bt[2] = Bt[1] + NB * KC;
+    int *nodes = reinterpret_cast<int *>(Bt[2] + NB * KC);  // [NPE]
+    int *inv = nodes + NPE;                                 // [NDOF]
+    int16_t *boff = reinterpret_cast<int16_t *>(inv + NDOF);  // [NPE][NPE]
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t taddr_s;
+    __shared__ int s_flag;
+    __shared__ int64_t s_nnz;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t cap = (int64_t)NDOF * NDOF;
+    constexpr int TCOLS = tc_tmem_cols<NPE>();
+    int flag = 0;
+    uint32_t phase = 0;
+    if (tid == 0) {
+        s_flag = 0;
+        s_nnz = (int64_t)A.indptr[3 * A.nnode];
+        tc::mbar_init(&mbar, 1);
+    }
+    if (warp == 0) tc::tmem_alloc(&taddr_s, TCOLS);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = taddr_s;
+    const uint32_t idesc = tc::idesc_bf16_f32(TC_MT, NB);
+    const uint32_t sbo = (uint32_t)(KC / 8) * 128;
+    const bool b_once = K <= KC;  // one K chunk: the Jm operand is built once per CTA
+    bool b_built = false;
+    bool ok = true;
+
+    auto build_b = [&](int k0, int kc) {
+        for (int idx = tid; idx < NB * KC; idx += 128) {
+            const int n = idx / KC, cc = idx % KC, c = k0 + cc;
+            float v = 0.f;
+            if (n < NPE && cc < kc) v = __ldg(A.Jmf + ((size_t)(c % 3) * NPE + n) * nq + c / 3);
+            const uint32_t off = tc::kmajor_offset(n, cc, KC) / 2;
+            bf16_split3(v, Bt[0][off], Bt[1][off], Bt[2][off]);
+        }
+    };
+
+    for (int64_t el = blockIdx.x; el < A.ne && ok; el += gridDim.x) {
+        const int64_t e = A.e0 + el;
+        __syncthreads();  // previous element done with the shared buffers
+        for (int a = tid; a < NPE; a += 128) {
+            uint64_t nd = A.elements[e * NPE + a];
+            if (nd >= (uint64_t)A.nnode) {
+                flag |= FL_FLAG_BAD_INDEX;
+                nd = 0;
+            }
+            nodes[a] = (int)nd;
+        }
+        if (A.dl)
+            for (int i = tid; i < NDOF; i += 128) {
+                const int v = A.dl[e * cap + (int64_t)i * NDOF];
+                const int p = v / NDOF;
+                if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
+                else inv[p] = i;
+            }
+        const double *q = A.Q + el * nq;
+        for (int idx = tid; idx < nq * QSM; idx += 128) {
+            const int k = idx / nq, g = idx % nq;
+            Qs[(size_t)g * QSM + k] = (float)q[k * A.ldq + g];
+        }
+        __syncthreads();
+        if (!A.dl)  // offset of column node b in row node a; consecutive threads share a row
+            for (int idx = tid; idx < NPE * NPE; idx += 128) {
+                const int off = row_search(A.indptr, A.indices, 3 * nodes[idx / NPE], 3 * nodes[idx % NPE]);
+                boff[idx] = (int16_t)(off >= 0 && off < 32768 ? off : -1);
+            }
+        // residual in FP64
+        if (A.update) {
+            for (int r = tid; r < NDOF; r += 128) {
+                const int a = r / 3, i = r % 3;
+                double t = 0.0;
+                const double *qs = q + (size_t)(45 + i * 3) * A.ldq;
+                for (int g = 0; g < nq; ++g) {
+                    t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[g], t);
+                    t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[A.ldq + g], t);
+                    t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2 * A.ldq + g], t);
+                }
+                atomicAdd(A.T + 3 * (int64_t)nodes[a] + i, t);
+            }
+        }
+        for (int m0 = 0; m0 < M; m0 += TC_MT) {
+            for (int k0 = 0; k0 < K; k0 += KC) {
+                const int kc = min(KC, K - k0);
+                // operands of this chunk (the previous chunk's MMAs completed: waited below)
+                for (int idx = tid; idx < TC_MT * KC; idx += 128) {
+                    const int rr = idx / KC, cc = idx % KC, r = m0 + rr, c = k0 + cc;
+                    float v = 0.f;
+                    if (r < M && cc < kc) {
+                        const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+                        const int g = c / 3, d = c % 3, I = i * 3 + d;
+                        const float *qq = Qs + (size_t)g * QSM;  // U in FP32: the tangent's target accuracy
+                        v = fmaf(qq[sym9(I, k * 3 + 0)], __ldg(A.Jmf + ((size_t)0 * NPE + b) * nq + g),
+                                 fmaf(qq[sym9(I, k * 3 + 1)], __ldg(A.Jmf + ((size_t)1 * NPE + b) * nq + g),
+                                      qq[sym9(I, k * 3 + 2)] * __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g)));
+                    }
+                    const uint32_t off = tc::kmajor_offset(rr, cc, KC) / 2;
+                    bf16_split3(v, At[0][off], At[1][off], At[2][off]);
+                }
+                if (!b_once || !b_built) {
+                    build_b(k0, kc);
+                    b_built = true;
+                }
+                tc::fence_async_smem();
+                tc::fence_before_sync();
+                __syncthreads();
+                tc::fence_after_sync();
+                if (tid == 0) {
+                    // the six products of order >= 2^-16, smallest first (term 0 = hi, 1 = mid, 2 = lo)
+                    const int pa[6] = {1, 2, 0, 1, 0, 0}, pb[6] = {1, 0, 2, 0, 1, 0};
+                    for (int ks = 0; ks < KC / 16; ++ks) {
+                        if (16 * ks >= kc) break;
+                        for (int t = 0; t < 6; ++t) {
+                            const uint64_t da = tc::smem_desc(At[pa[t]] + ks * 16 * 8, 128, sbo);
+                            const uint64_t db = tc::smem_desc(Bt[pb[t]] + ks * 16 * 8, 128, sbo);
+                            tc::mma_bf16(taddr, da, db, idesc, k0 > 0 || ks > 0 || t > 0);
+                        }
+                    }
+                    tc::mma_commit(&mbar);
+                }
+                ok = __syncthreads_and(tc::mbar_wait(&mbar, phase & 1, TC_WAIT)) != 0;  // uniform in the CTA
+                ++phase;
+                tc::fence_after_sync();
+                if (!ok) break;
+            }
+            if (!ok) {
+                flag |= FL_FLAG_BAD_INDEX;  // reported as an error by the caller
+                break;
+            }
+            // read back: warp w holds rows m0 + 32 w + lane of the tile
+            const int r = m0 + 32 * warp + lane;
+            const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+#pragma unroll 1
+            for (int c0 = 0; c0 < NB; c0 += 32) {
+                float v[32];
+                tc::tmem_ld32(taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
+                if (r >= M) continue;
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int a = c0 + j;  // C[r, a] = K_e[(a,i),(b,k)]
+                    if (a >= NPE) continue;
+                    int64_t pos = -1;
+                    if (A.dl) {
+                        const int ir = inv[3 * a + i], ic = inv[3 * b + k];
+                        if ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
+                            pos = (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic];
+                    } else {
+                        pos = block_entry(A.indptr, A.indices, nodes[a], nodes[b], i, k, boff[a * NPE + b]);
+                    }
+                    if (pos >= 0 && pos < s_nnz) atomicAdd(V32 + pos, v[j]);
+                    else flag |= FL_FLAG_BAD_INDEX;
+                }
+            }
+            tc::fence_before_sync();
+            __syncthreads();  // every warp has read the accumulator before the next tile's MMAs
+            tc::fence_after_sync();
+        }
+    }
+    if (flag) atomicOr(&s_flag, flag);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(taddr, TCOLS);
+    if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
+}
+
 template <int NPE>
 static size_t mixed_smem_bytes(int nq, bool utab) {
     return mixed_base_bytes<NPE>(nq) + (utab ? sizeof(float) * (size_t)nq * NPE * 27 : 0);
@@ -863,13 +1076,10 @@ static size_t mixed_smem_bytes(int nq, bool utab) {
 template <int NPE, int MAT>
 static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
     if (A.nelem == 0) return FL_OK;
-    // the element's U table in shared memory when it costs no resident CTA per SM (the kernel is
-    // latency bound: fewer CTAs lose more than the table saves)
-    auto ctas = [](size_t bytes) { return (228 * 1024) / (bytes + 1024); };
-    A.utab = ctas(mixed_smem_bytes<NPE>(A.nq, true)) >= ctas(mixed_smem_bytes<NPE>(A.nq, false)) ? 1 : 0;
-    const size_t smem = mixed_smem_bytes<NPE>(A.nq, A.utab != 0);
+    A.utab = 0;
+    const size_t smem = tc_smem_bytes<NPE>(A.nq);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    { const int st = ensure_smem<contract_mixed_kernel<NPE>>(smem); if (st != FL_OK) return st; }
+    { const int st = ensure_smem<contract_tc_kernel<NPE>>(smem); if (st != FL_OK) return st; }
     int64_t chunk = chunk_elements(CHUNK_BYTES, A.nq, 1);
     if (chunk > A.nelem) chunk = A.nelem;
     double *Q = nullptr;  // Gauss-point scratch, then the FP32 copy of Jm
@@ -890,7 +1100,7 @@ static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
         const int64_t nqp = A.ne * A.nq;
         qp_kernel<NPE, MAT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
         const int64_t grid = std::min<int64_t>(A.ne, (int64_t)sms * 8);
-        contract_mixed_kernel<NPE><<<(unsigned)grid, MX_NT, smem, stream>>>(A, V32);
+        contract_tc_kernel<NPE><<<(unsigned)grid, 128, smem, stream>>>(A, V32);
     }
     const int st = launch_status();
     const cudaError_t fe = cudaFreeAsync(Q, stream);

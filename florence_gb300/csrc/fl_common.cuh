@@ -90,7 +90,7 @@ template <int MAT>
 __device__ __forceinline__ void material(const double *F, const MatParams &mp, double *sig, double *b, double &J,
                                          double &c1, double &c2, double &cbb, ExtraTangent *ex = nullptr) {
     J = det3(F);
-    if (MAT == LINEARELASTIC) {  // _LinearElastic_.h:26-60: sigma = 2 mu eps + lamb tr(eps) I, eps = sym(F - I)
+    if constexpr (MAT == LINEARELASTIC) {  // _LinearElastic_.h:26-60: sigma = 2 mu eps + lamb tr(eps) I, eps = sym(F - I)
         const double mu = mp.p0, lamb = mp.p1;
         const double tre = F[0] + F[4] + F[8] - 3.0;
 #pragma unroll
@@ -103,8 +103,9 @@ __device__ __forceinline__ void material(const double *F, const MatParams &mp, d
         c1 = mu;
         c2 = lamb;
         cbb = 0.0;
+        (void)ex;
         return;
-    }
+    } else {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -170,6 +171,7 @@ __device__ __forceinline__ void material(const double *F, const MatParams &mp, d
         c2 = lamb * (2.0 * J - 1.0);
         cbb = B;
     }
+    }  // not the linear elastic material
 }
 
 // Kinematics at one Gauss point from the reference-element gradients jm(d, a) (a callable) and

@@ -68,9 +68,11 @@ __device__ __forceinline__ void mma_commit(uint64_t *mbar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(a));
 }
 
+// initialisation, made visible to the asynchronous proxy that tcgen05.commit arrives through
 __device__ __forceinline__ void mbar_init(uint64_t *mbar, uint32_t count) {
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(mbar);
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(a), "r"(count));
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 
 // bounded wait for phase `parity` of the mbarrier (non-blocking test + short sleep per poll, so
