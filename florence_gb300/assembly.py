@@ -419,3 +419,10 @@ def arithmetic(name):
         yield
     finally:
         set_arithmetic(old)
+
+
+def set_tensor_core_tiling(tile_group=0, reduction_chunk=0):
+    """Tiling of the split-BF16 tensor-core tangent for every later mixed assembly in the process:
+    128-row tiles per work item and (Gauss point, direction) columns per tensor-core round
+    (a multiple of 16 up to 96); 0 = chosen from the element type's shared-memory needs."""
+    N.check(N.lib().fl_SetTensorCoreTiling(int(tile_group), int(reduction_chunk)), "fl_SetTensorCoreTiling")

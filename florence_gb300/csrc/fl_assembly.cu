@@ -66,8 +66,7 @@ struct AsmArgs {
     const double *eparams;  // optional per-element material parameters [nelem][3] (overrides mp)
     int *flags;
     double *Q;       // scratch [QSTRIDE][ldq]
-    const float *Jmf;  // FP32 copy of Jm (the split-BF16 tangent's operand), or null
-    int utab;          // split-BF16 kernel: 1 = the element's U table is built in shared memory first
+    float *Qf;       // split-BF16 path: FP32 tangent part [45][ldq] (Q then holds S [9][ldq])
     int64_t e0, ne;  // element chunk [e0, e0+ne)
     int64_t ldq;     // leading dimension of Q (>= ne*nq)
 };
@@ -106,7 +105,76 @@ __host__ __device__ __forceinline__ constexpr int sym9(int I, int K) {
 // ------------------------------------------------------------------------------------------------
 // A. Gauss-point data
 // ------------------------------------------------------------------------------------------------
-template <int NPE, int MAT>
+// Pulled-back tangent of one Gauss point in arithmetic T from the FP64 kinematics and material:
+// Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
+//                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ] (+ the
+// nearly incompressible material's terms), written as out[sym9(I, K) * ld], I = 3 i + d, K = 3 k + e
+template <typename T, int MAT>
+__device__ __forceinline__ void pulled_back_tangent(const double *Gd, const double *sigd, const double *bd,
+                                                    const ExtraTangent &exd, double c1d, double c2d, double cbbd,
+                                                    double detJd, T *out, int64_t ld) {
+    constexpr bool NIMR = MAT == NEARLYINCOMPRESSIBLEMR;
+    T G[9], sig[6], b[6], g6[6];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) G[i] = (T)Gd[i];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        sig[i] = (T)sigd[i];
+        b[i] = (T)bd[i];
+        g6[i] = (T)exd.g[i];
+    }
+    const T c1 = (T)c1d, c2 = (T)c2d, cbb = (T)cbbd, detJ = (T)detJd;
+    const T kbI = (T)exd.kbI, kgI = (T)exd.kgI, kgg = (T)exd.kgg, kg4 = (T)exd.kg4;
+    // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G, gG = g G, GgG = G^T g G
+    T GG[9], GsG[9], sG[9], bG[9], GbG[9], gG[9], GgG[9];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            sG[i * 3 + d] = fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
+            if (MAT == MOONEYRIVLIN || NIMR)
+                bG[i * 3 + d] = fma(b[s6(i, 0)], G[0 * 3 + d], fma(b[s6(i, 1)], G[1 * 3 + d], b[s6(i, 2)] * G[2 * 3 + d]));
+            if (NIMR)
+                gG[i * 3 + d] = fma(g6[s6(i, 0)], G[0 * 3 + d], fma(g6[s6(i, 1)], G[1 * 3 + d], g6[s6(i, 2)] * G[2 * 3 + d]));
+        }
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+        for (int e2 = d; e2 < 3; ++e2) {
+            GG[d * 3 + e2] = fma(G[d], G[e2], fma(G[3 + d], G[3 + e2], G[6 + d] * G[6 + e2]));
+            // no geometric stiffness for the linear elastic material (the reference builds that
+            // assembler without it, AOT_Assembler.py:74-81)
+            GsG[d * 3 + e2] = MAT == LINEARELASTIC ? (T)0 : fma(G[d], sG[e2], fma(G[3 + d], sG[3 + e2], G[6 + d] * sG[6 + e2]));
+            if (MAT == MOONEYRIVLIN) GbG[d * 3 + e2] = fma(G[d], bG[e2], fma(G[3 + d], bG[3 + e2], G[6 + d] * bG[6 + e2]));
+            if (NIMR) GgG[d * 3 + e2] = fma(G[d], gG[e2], fma(G[3 + d], gG[3 + e2], G[6 + d] * gG[6 + e2]));
+        }
+#pragma unroll
+    for (int I = 0; I < 9; ++I)
+#pragma unroll
+        for (int K = I; K < 9; ++K) {
+            const int i = I / 3, d = I % 3, k = K / 3, e2 = K % 3;
+            const int dd = d < e2 ? d : e2, ee = d < e2 ? e2 : d;
+            T v = fma(c1 * G[k * 3 + d], G[i * 3 + e2], c2 * G[i * 3 + d] * G[k * 3 + e2]);
+            if (i == k) v = fma(c1, GG[dd * 3 + ee], v + GsG[dd * 3 + ee]);
+            if (MAT == MOONEYRIVLIN)
+                v = fma(cbb, fma((T)2 * bG[i * 3 + d], bG[k * 3 + e2], -fma(b[s6(i, k)], GbG[dd * 3 + ee], bG[k * 3 + d] * bG[i * 3 + e2])), v);
+            if (NIMR) {
+                // kbI (bG_id G_ke + G_id bG_ke) + kgI (gG_id G_ke + G_id gG_ke) + kgg gG_id gG_ke
+                // + kg4 (g_ik GG_de + gG_ie G_kd + gG_kd G_ie + d_ik GgG_de)
+                v = fma(kbI, fma(bG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * bG[k * 3 + e2]), v);
+                v = fma(kgI, fma(gG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * gG[k * 3 + e2]), v);
+                v = fma(kgg, gG[i * 3 + d] * gG[k * 3 + e2], v);
+                T t4 = fma(g6[s6(i, k)], GG[dd * 3 + ee], fma(gG[i * 3 + e2], G[k * 3 + d], gG[k * 3 + d] * G[i * 3 + e2]));
+                if (i == k) t4 += GgG[dd * 3 + ee];
+                v = fma(kg4, t4, v);
+            }
+            out[sym9(I, K) * ld] = detJ * v;
+        }
+}
+
+// F32T: the tangent part in FP32 into A.Qf [45][ldq] (the split-BF16 Jacobian's input) and the
+// residual part S in FP64 into A.Q [9][ldq]; else both in FP64 into A.Q [54][ldq]
+template <int NPE, int MAT, bool F32T = false>
 __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
     const int64_t t = (int64_t)blockIdx.x * QP_THREADS + threadIdx.x;
     const int nq = A.nq;
@@ -133,58 +201,18 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         ExtraTangent ex;
         material<MAT>(F, mp, sig, b, J, c1, c2, cbb, &ex);
         if (!(J > 0.0)) flag |= FL_FLAG_NONPOSITIVE_J;
-        constexpr bool NIMR = MAT == NEARLYINCOMPRESSIBLEMR;
-        // GG = G^T G, GsG = G^T sigma G, bG = b G, GbG = G^T b G, gG = g G, GgG = G^T g G
-        double GG[9], GsG[9], sG[9], bG[9], GbG[9], gG[9], GgG[9];
+        const int64_t ld = A.ldq;
+        double *q = A.Q + t;
+        // S[i][d] = detJ sum_j sigma_ij G[j][d], the residual's Gauss-point factor, in FP64
+        double *qs = F32T ? q : q + 45 * ld;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                sG[i * 3 + d] = fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
-                if (MAT == MOONEYRIVLIN || NIMR)
-                    bG[i * 3 + d] = fma(b[s6(i, 0)], G[0 * 3 + d], fma(b[s6(i, 1)], G[1 * 3 + d], b[s6(i, 2)] * G[2 * 3 + d]));
-                if (NIMR)
-                    gG[i * 3 + d] = fma(ex.g[s6(i, 0)], G[0 * 3 + d], fma(ex.g[s6(i, 1)], G[1 * 3 + d], ex.g[s6(i, 2)] * G[2 * 3 + d]));
-            }
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-#pragma unroll
-            for (int e2 = d; e2 < 3; ++e2) {
-                GG[d * 3 + e2] = fma(G[d], G[e2], fma(G[3 + d], G[3 + e2], G[6 + d] * G[6 + e2]));
-                // no geometric stiffness for the linear elastic material (the reference builds that
-                // assembler without it, AOT_Assembler.py:74-81)
-                GsG[d * 3 + e2] = MAT == LINEARELASTIC ? 0.0 : fma(G[d], sG[e2], fma(G[3 + d], sG[3 + e2], G[6 + d] * sG[6 + e2]));
-                if (MAT == MOONEYRIVLIN) GbG[d * 3 + e2] = fma(G[d], bG[e2], fma(G[3 + d], bG[3 + e2], G[6 + d] * bG[6 + e2]));
-                if (NIMR) GgG[d * 3 + e2] = fma(G[d], gG[e2], fma(G[3 + d], gG[3 + e2], G[6 + d] * gG[6 + e2]));
-            }
-        // Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
-        //                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ]
-        double *q = A.Q + t;
-        const int64_t ld = A.ldq;
-#pragma unroll
-        for (int I = 0; I < 9; ++I)
-#pragma unroll
-            for (int K = I; K < 9; ++K) {
-                const int i = I / 3, d = I % 3, k = K / 3, e2 = K % 3;
-                const int dd = d < e2 ? d : e2, ee = d < e2 ? e2 : d;
-                double v = fma(c1 * G[k * 3 + d], G[i * 3 + e2], c2 * G[i * 3 + d] * G[k * 3 + e2]);
-                if (i == k) v = fma(c1, GG[dd * 3 + ee], v + GsG[dd * 3 + ee]);
-                if (MAT == MOONEYRIVLIN)
-                    v = fma(cbb, fma(2.0 * bG[i * 3 + d], bG[k * 3 + e2], -fma(b[s6(i, k)], GbG[dd * 3 + ee], bG[k * 3 + d] * bG[i * 3 + e2])), v);
-                if (NIMR) {
-                    // kbI (bG_id G_ke + G_id bG_ke) + kgI (gG_id G_ke + G_id gG_ke) + kgg gG_id gG_ke
-                    // + kg4 (g_ik GG_de + gG_ie G_kd + gG_kd G_ie + d_ik GgG_de)
-                    v = fma(ex.kbI, fma(bG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * bG[k * 3 + e2]), v);
-                    v = fma(ex.kgI, fma(gG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * gG[k * 3 + e2]), v);
-                    v = fma(ex.kgg, gG[i * 3 + d] * gG[k * 3 + e2], v);
-                    double t4 = fma(ex.g[s6(i, k)], GG[dd * 3 + ee], fma(gG[i * 3 + e2], G[k * 3 + d], gG[k * 3 + d] * G[i * 3 + e2]));
-                    if (i == k) t4 += GgG[dd * 3 + ee];
-                    v = fma(ex.kg4, t4, v);
-                }
-                q[sym9(I, K) * ld] = detJ * v;
-            }
-#pragma unroll
-        for (int k = 0; k < 9; ++k) q[(45 + k) * ld] = detJ * sG[k];  // S[i][d]
+            for (int d = 0; d < 3; ++d)
+                qs[(i * 3 + d) * ld] =
+                    detJ * fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
+        if (F32T) pulled_back_tangent<float, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, A.Qf + t, ld);
+        else pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, q, ld);
     }
     if (flag && A.flags) atomicOr(A.flags, flag);
 }
@@ -565,8 +593,6 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.elements = elements;
     A.Eulerx = Eulerx;
     A.Jm = Jm;
-    A.Jmf = nullptr;
-    A.utab = 0;
     A.w = AllGauss;
     A.nelem = nelem;
     A.nnode = nnode;
@@ -581,6 +607,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.eparams = eparams;
     A.flags = flags;
     A.Q = nullptr;
+    A.Qf = nullptr;
     A.e0 = A.ne = A.ldq = 0;
     A.qc = 1;
     if (recompute_sparsity_pattern) {
@@ -625,41 +652,14 @@ static int material_of(int material_number, double mu, double mu1, double mu2, d
 }
 
 // ------------------------------------------------------------------------------------------------
-// C. Mixed-precision contraction on the tensor cores (inexact-Newton Jacobian).
-//
-// Per element, K^T[(i,b,k), a] = sum_{(g,d)} U^T[(i,b,k),(g,d)] L[(g,d), a] with
-// U_g[(i,d),(b,k)] = sum_e Ahat_g[(i,d),(k,e)] Jm[e][b][g] (from the FP64 Gauss-point data, formed
-// in FP32) and L[(g,d), a] = Jm[d][a][g]. Both operands are split into three BF16 terms
-// (x = hi + mid + lo, 24 significant bits together) and multiplied as the six products whose
-// order is at least 2^-16 (hi*hi, hi*mid, mid*hi, hi*lo, lo*hi, mid*mid) with FP32 accumulation
-// (mma.sync m16n8k16 bf16): the tangent to about FP32 accuracy (~1e-7 relative), enough for
-// Newton to keep its FP64 iteration count on ill-conditioned problems (a two-term split, ~1e-5,
-// slows Newton down). The result goes to FP32 CSR values (the Jacobian the PCG applies); the residual is
-// formed in FP64 exactly as in contract_kernel. Rows are processed in chunks of MX_MC and the
-// reduction dimension in chunks of MX_KC, so any element order fits in shared memory.
+// C. Mixed-precision (split-BF16) tangent: shared pieces. The Jacobian is formed on the tensor
+// cores (section D) with both operands split into three BF16 terms (x = hi + mid + lo, 24
+// significant bits together) and multiplied as the six products whose order is at least 2^-16
+// with FP32 accumulation: the tangent to about FP32 accuracy, enough for Newton on
+// ill-conditioned problems (a two-term split, ~1e-5, slows Newton down). The residual is formed
+// in FP64 exactly as in contract_kernel.
 // ------------------------------------------------------------------------------------------------
-constexpr int MX_NT = 128, MX_MC = 64, MX_KC = 96;
-
-// x = hi + mid + lo, three BF16 terms with 8 significant bits each (FP32's 24 bits)
-__device__ __forceinline__ void bf16_split3(float v, __nv_bfloat16 &hi, __nv_bfloat16 &mid, __nv_bfloat16 &lo) {
-    hi = __float2bfloat16_rn(v);
-    const float r1 = v - __bfloat162float(hi);
-    mid = __float2bfloat16_rn(r1);
-    lo = __float2bfloat16_rn(r1 - __bfloat162float(mid));
-}
-
-__device__ __forceinline__ void mma_bf16(float *c, const uint32_t *a, const uint32_t *b) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
-}
-
-__global__ void to_float(const double *a, float *b, int64_t n) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) b[i] = (float)a[i];
-}
+constexpr int MX_KC = 96;  // widest reduction chunk
 
 // reduction-chunk width of the split-BF16 kernel: the padded 3*nq, at most MX_KC (the operand
 // buffers are sized by it, so short reductions leave room for more resident CTAs)
@@ -668,251 +668,180 @@ __host__ __device__ inline int mixed_kc(int nq) {
     return kp < MX_KC ? kp : MX_KC;
 }
 
-// shared memory of the split-BF16 kernel without the U table (16-byte multiple)
-template <int NPE>
-__host__ __device__ inline size_t mixed_base_bytes(int nq) {
-    constexpr int NP = (NPE + 7) / 8 * 8;
-    const int ast = mixed_kc(nq) + 8;
-    const size_t b = sizeof(float) * (((size_t)nq * QSM + 3) / 4 * 4) +
-                     sizeof(__nv_bfloat16) * 3 * ((size_t)MX_MC * ast + (size_t)NP * ast) +
-                     sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
-    return (b + 15) / 16 * 16;
-}
-
-template <int NPE>
-__global__ void __launch_bounds__(MX_NT) contract_mixed_kernel(const AsmArgs A, float *V32) {
-    constexpr int NDOF = 3 * NPE, M = 9 * NPE, NP = (NPE + 7) / 8 * 8, NT8 = NP / 8;
-    const int nq = A.nq, K = 3 * nq;
-    const int KC = mixed_kc(nq), AST = KC + 8;  // chunk width and padded row stride (bf16) of the operands
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *Qs = reinterpret_cast<float *>(smem_raw);                                // [nq][QSM]
-    __nv_bfloat16 *Ah = reinterpret_cast<__nv_bfloat16 *>(Qs + ((size_t)nq * QSM + 3) / 4 * 4);  // [3][MX_MC][AST]
-    __nv_bfloat16 *Am = Ah + MX_MC * AST;
-    __nv_bfloat16 *Al = Am + MX_MC * AST;
-    __nv_bfloat16 *Bh = Al + MX_MC * AST;                                            // [3][NP][AST]
-    __nv_bfloat16 *Bm = Bh + NP * AST;
-    __nv_bfloat16 *Bl = Bm + NP * AST;
-    int *nodes = reinterpret_cast<int *>(Bl + NP * AST);                             // [NPE]
-    int *inv = nodes + NPE;                                                          // [NDOF]
-    int16_t *boff = reinterpret_cast<int16_t *>(inv + NDOF);                         // [NPE][NPE]
-    float *Ut = reinterpret_cast<float *>(smem_raw + mixed_base_bytes<NPE>(nq));      // [nq][NPE][27] if utab
-    __shared__ int s_flag;
-    __shared__ int64_t s_nnz;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
-    const int64_t cap = (int64_t)NDOF * NDOF;
-    int flag = 0;
-    if (tid == 0) {
-        s_flag = 0;
-        s_nnz = (int64_t)A.indptr[3 * A.nnode];
-    }
-    for (int64_t el = blockIdx.x; el < A.ne; el += gridDim.x) {
-        const int64_t e = A.e0 + el;
-        __syncthreads();  // previous element done with the shared buffers
-        for (int a = tid; a < NPE; a += MX_NT) {
-            uint64_t nd = A.elements[e * NPE + a];
-            if (nd >= (uint64_t)A.nnode) {
-                flag |= FL_FLAG_BAD_INDEX;
-                nd = 0;
-            }
-            nodes[a] = (int)nd;
-        }
-        if (A.dl)
-            for (int i = tid; i < NDOF; i += MX_NT) {
-                const int v = A.dl[e * cap + (int64_t)i * NDOF];
-                const int p = v / NDOF;
-                if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
-                else inv[p] = i;
-            }
-        const double *q = A.Q + el * nq;
-        for (int idx = tid; idx < nq * QSM; idx += MX_NT) {
-            const int k = idx / nq, g = idx % nq;
-            Qs[(size_t)g * QSM + k] = (float)q[k * A.ldq + g];
-        }
-        __syncthreads();
-        if (!A.dl)  // offset of column node b in row node a; consecutive threads share a row
-            for (int idx = tid; idx < NPE * NPE; idx += MX_NT) {
-                const int off = row_search(A.indptr, A.indices, 3 * nodes[idx / NPE], 3 * nodes[idx % NPE]);
-                boff[idx] = (int16_t)(off >= 0 && off < 32768 ? off : -1);
-            }
-        // residual in FP64
-        if (A.update) {
-            for (int r = tid; r < NDOF; r += MX_NT) {
-                const int a = r / 3, i = r % 3;
-                double t = 0.0;
-                const double *qs = q + (size_t)(45 + i * 3) * A.ldq;  // S from the L2-resident scratch
-                for (int g = 0; g < nq; ++g) {
-                    t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[g], t);
-                    t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[A.ldq + g], t);
-                    t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2 * A.ldq + g], t);
-                }
-                atomicAdd(A.T + 3 * (int64_t)nodes[a] + i, t);
-            }
-        }
-        if (A.utab)  // U_g[b][(i,d),k] of the whole element: all 27 entries of one (g, b) per work item,
-                     // compile-time tensor indices, no divergence
-            for (int it = tid; it < nq * NPE; it += MX_NT) {
-                const int g = it / NPE, b = it % NPE;
-                const float *qq = Qs + (size_t)g * QSM;
-                const float j0 = __ldg(A.Jmf + (size_t)b * nq + g), j1 = __ldg(A.Jmf + ((size_t)NPE + b) * nq + g),
-                            j2 = __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g);
-                float *uo = Ut + ((size_t)g * NPE + b) * 27;
-#pragma unroll
-                for (int II = 0; II < 9; ++II)
-#pragma unroll
-                    for (int k = 0; k < 3; ++k)
-                        uo[II * 3 + k] = fmaf(qq[sym9(II, k * 3 + 0)], j0,
-                                              fmaf(qq[sym9(II, k * 3 + 1)], j1, qq[sym9(II, k * 3 + 2)] * j2));
-            }
-        for (int m0 = 0; m0 < M; m0 += MX_MC) {
-            float acc[NT8][4];
-#pragma unroll
-            for (int t = 0; t < NT8; ++t) acc[t][0] = acc[t][1] = acc[t][2] = acc[t][3] = 0.f;
-            for (int k0 = 0; k0 < K; k0 += KC) {
-                const int kc = min(KC, K - k0), kcp = (kc + 15) / 16 * 16;
-                __syncthreads();  // previous chunk's MMAs done
-                // A chunk: rows r = m0 + rr -> (i, b, k) with r = (i*NPE + b)*3 + k; cols c = k0 + cc -> (g, d)
-                for (int idx = tid; idx < MX_MC * kcp; idx += MX_NT) {
-                    const int rr = idx / kcp, cc = idx % kcp, r = m0 + rr, c = k0 + cc;
-                    float v = 0.f;
-                    if (r < M && cc < kc) {
-                        const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
-                        const int g = c / 3, d = c % 3, I = i * 3 + d;
-                        if (A.utab) {
-                            v = Ut[((size_t)g * NPE + b) * 27 + I * 3 + k];
-                        } else {
-                            const float *qq = Qs + (size_t)g * QSM;  // U in FP32: the tangent's target accuracy
-                            v = fmaf(qq[sym9(I, k * 3 + 0)], __ldg(A.Jmf + ((size_t)0 * NPE + b) * nq + g),
-                                     fmaf(qq[sym9(I, k * 3 + 1)], __ldg(A.Jmf + ((size_t)1 * NPE + b) * nq + g),
-                                          qq[sym9(I, k * 3 + 2)] * __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g)));
-                        }
-                    }
-                    bf16_split3(v, Ah[rr * AST + cc], Am[rr * AST + cc], Al[rr * AST + cc]);
-                }
-                // B chunk, stored [n][k]: B[(g,d), a] = Jm[d][a][g]
-                for (int idx = tid; idx < NP * kcp; idx += MX_NT) {
-                    const int n = idx / kcp, cc = idx % kcp, c = k0 + cc;
-                    float v = 0.f;
-                    if (n < NPE && cc < kc) v = __ldg(A.Jmf + ((size_t)(c % 3) * NPE + n) * nq + c / 3);
-                    bf16_split3(v, Bh[n * AST + cc], Bm[n * AST + cc], Bl[n * AST + cc]);
-                }
-                __syncthreads();
-                // warp w: m-tile w of the chunk (16 rows), all n-tiles
-                const int mr = warp * 16;
-                for (int ks = 0; ks < kcp; ks += 16) {
-                    uint32_t ah[4], am[4], al[4];
-                    const int c0 = ks + tig * 2;
-                    auto ldA = [&](const __nv_bfloat16 *X, uint32_t *f) {
-                        f[0] = *reinterpret_cast<const uint32_t *>(X + (mr + gid) * AST + c0);
-                        f[1] = *reinterpret_cast<const uint32_t *>(X + (mr + gid + 8) * AST + c0);
-                        f[2] = *reinterpret_cast<const uint32_t *>(X + (mr + gid) * AST + c0 + 8);
-                        f[3] = *reinterpret_cast<const uint32_t *>(X + (mr + gid + 8) * AST + c0 + 8);
-                    };
-                    ldA(Ah, ah);
-                    ldA(Am, am);
-                    ldA(Al, al);
-#pragma unroll
-                    for (int t = 0; t < NT8; ++t) {
-                        uint32_t bh[2], bm[2], bl[2];
-                        const int n = t * 8 + gid;
-                        bh[0] = *reinterpret_cast<const uint32_t *>(Bh + n * AST + c0);
-                        bh[1] = *reinterpret_cast<const uint32_t *>(Bh + n * AST + c0 + 8);
-                        bm[0] = *reinterpret_cast<const uint32_t *>(Bm + n * AST + c0);
-                        bm[1] = *reinterpret_cast<const uint32_t *>(Bm + n * AST + c0 + 8);
-                        bl[0] = *reinterpret_cast<const uint32_t *>(Bl + n * AST + c0);
-                        bl[1] = *reinterpret_cast<const uint32_t *>(Bl + n * AST + c0 + 8);
-                        // smallest terms first
-                        mma_bf16(acc[t], am, bm);
-                        mma_bf16(acc[t], al, bh);
-                        mma_bf16(acc[t], ah, bl);
-                        mma_bf16(acc[t], am, bh);
-                        mma_bf16(acc[t], ah, bm);
-                        mma_bf16(acc[t], ah, bh);
-                    }
-                }
-            }
-            // scatter: C[r, a] = K_e[(a,i),(b,k)]
-#pragma unroll
-            for (int t = 0; t < NT8; ++t)
-#pragma unroll
-                for (int h = 0; h < 4; ++h) {
-                    const int r = m0 + warp * 16 + gid + (h >> 1) * 8, a = t * 8 + tig * 2 + (h & 1);
-                    if (r >= M || a >= NPE) continue;
-                    const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
-                    int64_t pos = -1;
-                    if (A.dl) {
-                        const int ir = inv[3 * a + i], ic = inv[3 * b + k];
-                        if ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
-                            pos = (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic];
-                    } else {
-                        pos = block_entry(A.indptr, A.indices, nodes[a], nodes[b], i, k, boff[a * NPE + b]);
-                    }
-                    if (pos >= 0 && pos < s_nnz) atomicAdd(V32 + pos, acc[t][h]);
-                    else flag |= FL_FLAG_BAD_INDEX;
-                }
-        }
-    }
-    if (flag) atomicOr(&s_flag, flag);
-    __syncthreads();
-    if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
-}
-
 // ------------------------------------------------------------------------------------------------
-// D. The split-BF16 tangent on the fifth-generation tensor cores (tcgen05). Same operands and
-// products as contract_mixed_kernel, organised for the tensor core: per element and 128-row tile
-// of K^T[(i,b,k), a], the three BF16 terms of U (A operand, 128 x KC) and of Jm (B operand,
-// NB x KC, NB = NPE padded to 16) are written to shared memory in the K-major core-matrix layout;
-// one thread issues the six products per 16-wide K step as tcgen05.mma into an FP32 accumulator
-// in tensor memory and commits them to an mbarrier; after the last K chunk each warp reads its 32
-// accumulator rows with tcgen05.ld and scatters them. The B operand depends only on the element
-// type: with a single K chunk it is built once per CTA. Waits are bounded (on expiry the element
-// is skipped and FL_FLAG_BAD_INDEX raised, so the call reports an error).
+// D. The split-BF16 tangent on the fifth-generation tensor cores (tcgen05).
+//
+//    K^T[(i,b,k), a] = sum_(g,d) U[(i,b,k),(g,d)] Jm[d][a][g],
+//    U[(i,b,k),(g,d)] = sum_e Ahat_g[(i,d),(k,e)] Jm[e][b][g]
+//
+// One work item = (element, group of 128-row tiles of K^T). Per reduction chunk of KC columns
+// (g,d), the CTA writes the three BF16 terms of U (A operand, rows of the tile group x KC) and of
+// Jm (B operand, NB x KC, NB = NPE padded to 16) to shared memory in the K-major core-matrix
+// layout; one thread issues, per tile and 16-wide K step, the six products as tcgen05.mma into
+// that tile's FP32 accumulator in tensor memory and commits them to an mbarrier. After the last
+// chunk the eight warps read the accumulators with tcgen05.ld (warps w and w + 4 share tensor-
+// memory lanes 32 (w % 4) .. + 31 and split the tiles between them) and scatter them.
+//
+// The U build is the kernel's main work: each thread forms 8 consecutive columns of one row (one
+// 16-byte row of a core matrix) from float4 rows of the pulled-back tangent
+// Qx[g][(i,d)][k] = (Ahat[(i,d),(k,0..2)], 0) in shared memory and float4 rows
+// J4[g][b] = (Jm[0..2][b][g], 0) (read-only cache), splits them into packed BF16 pairs and stores
+// the three terms as 16-byte words. The B operand depends only on the element type: with one K
+// chunk it is built once per CTA. Waits are bounded (on expiry the CTA stops and raises
+// FL_FLAG_BAD_INDEX, which the call reports as an error).
 // ------------------------------------------------------------------------------------------------
-constexpr int TC_MT = 128;
+constexpr int TC_MT = 128;       // rows per tile (the MMA's M)
+constexpr int TC_THREADS = 256;  // eight warps
 constexpr long long TC_WAIT = 1ll << 22;
 
 template <int NPE>
 __host__ __device__ constexpr int tc_nb() { return (NPE + 15) / 16 * 16; }
-
 template <int NPE>
-__host__ __device__ constexpr int tc_tmem_cols() {
-    const int n = (tc_nb<NPE>() + 31) / 32 * 32;
-    return n <= 32 ? 32 : (n <= 64 ? 64 : (n <= 128 ? 128 : 256));
-}
-
-// shared memory: Qs float [nq][QSM] | A terms 3 x [128][KC] bf16 | B terms 3 x [NB][KC] bf16 |
-// nodes, inv, boff
+__host__ __device__ constexpr int tc_ntiles() { return (9 * NPE + TC_MT - 1) / TC_MT; }
+// tensor-memory columns per tile accumulator (read back 32 at a time)
 template <int NPE>
-__host__ __device__ inline size_t tc_smem_bytes(int nq) {
-    const int kc = mixed_kc(nq);
-    const size_t b = sizeof(float) * (((size_t)nq * QSM + 31) / 32 * 32) +
-                     sizeof(__nv_bfloat16) * 3 * ((size_t)TC_MT * kc + (size_t)tc_nb<NPE>() * kc) +
+__host__ __device__ constexpr int tc_colw() { return (tc_nb<NPE>() + 31) / 32 * 32; }
+
+// valid rows of K^T per (tile, tensor-memory lane quarter): the 9 NPE rows are spread evenly over
+// the 4 lane quarters of every tile, so each warp reads back an equal share
+template <int NPE>
+__host__ __device__ constexpr int tc_rpl() { return (9 * NPE + 4 * tc_ntiles<NPE>() - 1) / (4 * tc_ntiles<NPE>()); }
+
+// Gauss-point values prefetched into registers per thread for the next work item (the 54 nq
+// values of an element when they fit, else loaded when needed)
+constexpr int TC_PF = 4;
+
+// shared memory: Qr double [9][nq] | Qx float4 [nq][27] | A terms 3 x [tg * 128][KC] bf16 |
+// B terms 3 x [NB][KC] bf16 | nodes, inv, boff
+// (with the element's map block [9 NPE^2] int after them when it is staged)
+template <int NPE>
+__host__ __device__ inline size_t tc_map_offset(int nq, int kc, int tg) {
+    const size_t b = (sizeof(double) * 9 * (size_t)nq + 15) / 16 * 16 + sizeof(float4) * 27 * (size_t)nq +
+                     sizeof(__nv_bfloat16) * 3 * ((size_t)tg * TC_MT * kc + (size_t)tc_nb<NPE>() * kc) +
                      sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
+    return (b + 15) / 16 * 16;
+}
+template <int NPE>
+__host__ __device__ inline size_t tc_smem_bytes(int nq, int kc, int tg, bool stage = false) {
+    const size_t b = tc_map_offset<NPE>(nq, kc, tg) + (stage ? sizeof(int) * 9 * (size_t)NPE * NPE : 0);
     return (b + 127) / 128 * 128;
 }
 
+// asynchronous global -> shared copies (cp.async; 16 bytes needs both addresses 16-byte aligned)
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
+// J4[g][b] = (Jm[0][b][g], Jm[1][b][g], Jm[2][b][g], 0) for g < nq, zero rows for nq <= g < nq + 4
+__global__ void jm_float4(const double *Jm, float4 *J4, int npe, int nq) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (nq + 4) * npe) return;
+    const int g = t / npe, b = t % npe;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (g < nq) {
+        v.x = (float)Jm[((size_t)0 * npe + b) * nq + g];
+        v.y = (float)Jm[((size_t)1 * npe + b) * nq + g];
+        v.z = (float)Jm[((size_t)2 * npe + b) * nq + g];
+    }
+    J4[t] = v;
+}
+
+__device__ __forceinline__ float dot3(const float4 &q, const float4 &j) { return fmaf(q.x, j.x, fmaf(q.y, j.y, q.z * j.z)); }
+
+// three-term split of 8 values into packed BF16 pairs (element t in half t % 2 of word t / 2)
+__device__ __forceinline__ void split8(const float (&v)[8], uint4 &H, uint4 &Mi, uint4 &L) {
+    uint32_t h[4], m[4], l[4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        const __nv_bfloat162 h2 = __floats2bfloat162_rn(v[2 * p], v[2 * p + 1]);
+        const float2 hf = __bfloat1622float2(h2);
+        const float r0 = v[2 * p] - hf.x, r1 = v[2 * p + 1] - hf.y;
+        const __nv_bfloat162 m2 = __floats2bfloat162_rn(r0, r1);
+        const float2 mf = __bfloat1622float2(m2);
+        const __nv_bfloat162 l2 = __floats2bfloat162_rn(r0 - mf.x, r1 - mf.y);
+        h[p] = *reinterpret_cast<const uint32_t *>(&h2);
+        m[p] = *reinterpret_cast<const uint32_t *>(&m2);
+        l[p] = *reinterpret_cast<const uint32_t *>(&l2);
+    }
+    H = make_uint4(h[0], h[1], h[2], h[3]);
+    Mi = make_uint4(m[0], m[1], m[2], m[3]);
+    L = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+// U at columns c0 .. c0 + 7 (c = 3 g + d, c0 = 3 g0 + D0) of row (i, b, k), all below K
+template <int NPE, int D0>
+__device__ __forceinline__ void u_row8(const float4 *qx, const float4 *J4, int g0, int i, int b, int k,
+                                       float (&v)[8]) {
+    float4 j[4];
+#pragma unroll
+    for (int s = 0; s < (D0 + 7) / 3 + 1; ++s) j[s] = __ldg(J4 + (size_t)(g0 + s) * NPE + b);
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+        const int gg = (D0 + t) / 3, dd = (D0 + t) % 3;
+        v[t] = dot3(qx[(g0 + gg) * 27 + 9 * i + 3 * dd + k], j[gg]);
+    }
+}
+
+// (I, K), I <= K, of entry p of the packed upper triangle of a symmetric 9x9 (sym9's inverse)
+struct SymPairs {
+    unsigned char I[45], K[45];
+};
+__host__ __device__ constexpr SymPairs make_sym_pairs() {
+    SymPairs t{};
+    int p = 0;
+    for (int I = 0; I < 9; ++I)
+        for (int K = I; K < 9; ++K) {
+            t.I[p] = (unsigned char)I;
+            t.K[p] = (unsigned char)K;
+            ++p;
+        }
+    return t;
+}
+__constant__ SymPairs c_sym = make_sym_pairs();
+
+// n / d for n, d < 2^16 (n d < 2^32) by one high multiply with m = ceil(2^32 / d), d >= 2
+__device__ __forceinline__ int fastdiv(int n, uint32_t m) { return (int)__umulhi((uint32_t)n, m); }
+
 template <int NPE>
-__global__ void __launch_bounds__(128) contract_tc_kernel(const AsmArgs A, float *V32) {
-    constexpr int NDOF = 3 * NPE, M = 9 * NPE, NB = (NPE + 15) / 16 * 16;
-    const int nq = A.nq, K = 3 * nq, KC = mixed_kc(nq);
+__global__ void __launch_bounds__(TC_THREADS, 2)
+    contract_tc_kernel(const AsmArgs A, const float4 *__restrict__ J4, float *V32, int KC, int tg, int tcols,
+                       int stage) {
+    constexpr int NDOF = 3 * NPE, M = 9 * NPE, NB = tc_nb<NPE>(), NT = tc_ntiles<NPE>(), CW = tc_colw<NPE>();
+    constexpr int RPL = tc_rpl<NPE>(), RPL8 = (RPL + 7) / 8 * 8;
+    const int nq = A.nq, K = 3 * nq;
+    const int ngrp = (NT + tg - 1) / tg;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    float *Qs = reinterpret_cast<float *>(smem_raw);  // [nq][QSM]
+    double *Qr = reinterpret_cast<double *>(smem_raw);  // [9][nq] residual part
+    float4 *Qx = reinterpret_cast<float4 *>(smem_raw + (sizeof(double) * 9 * (size_t)nq + 15) / 16 * 16);  // [nq][27]
     __nv_bfloat16 *At[3], *Bt[3];
-    At[0] = reinterpret_cast<__nv_bfloat16 *>(smem_raw + sizeof(float) * (((size_t)nq * QSM + 31) / 32 * 32));
-    At[1] = At[0] + TC_MT * KC;
-    At[2] = At[1] + TC_MT * KC;
-    Bt[0] = At[2] + TC_MT * KC;
+    At[0] = reinterpret_cast<__nv_bfloat16 *>(Qx + 27 * nq);
+    At[1] = At[0] + (size_t)tg * TC_MT * KC;
+    At[2] = At[1] + (size_t)tg * TC_MT * KC;
+    Bt[0] = At[2] + (size_t)tg * TC_MT * KC;
     Bt[1] = Bt[0] + NB * KC;
     Bt[2] = Bt[1] + NB * KC;
     int *nodes = reinterpret_cast<int *>(Bt[2] + NB * KC);  // [NPE]
     int *inv = nodes + NPE;                                 // [NDOF]
     int16_t *boff = reinterpret_cast<int16_t *>(inv + NDOF);  // [NPE][NPE]
+    // the element's block of the local-to-global map [NDOF][NDOF], copied asynchronously
+    int *dgs = reinterpret_cast<int *>(smem_raw + tc_map_offset<NPE>(nq, KC, tg));
     __shared__ __align__(8) uint64_t mbar;
     __shared__ uint32_t taddr_s;
     __shared__ int s_flag;
     __shared__ int64_t s_nnz;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t cap = (int64_t)NDOF * NDOF;
-    constexpr int TCOLS = tc_tmem_cols<NPE>();
+    const int64_t nwork = A.ne * ngrp;
+    const bool staged = stage && A.dg;
+    const bool wide = staged && (cap & 3) == 0 && ((uintptr_t)A.dg & 15) == 0;  // 16-byte copies
+    const bool pf = 54 * nq <= TC_THREADS * TC_PF;  // Gauss-point values fit the prefetch registers
     int flag = 0;
     uint32_t phase = 0;
     if (tid == 0) {
@@ -920,7 +849,7 @@ __global__ void __launch_bounds__(128) contract_tc_kernel(const AsmArgs A, float
         s_nnz = (int64_t)A.indptr[3 * A.nnode];
         tc::mbar_init(&mbar, 1);
     }
-    if (warp == 0) tc::tmem_alloc(&taddr_s, TCOLS);
+    if (warp == 0) tc::tmem_alloc(&taddr_s, (uint32_t)tcols);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
@@ -931,21 +860,62 @@ __global__ void __launch_bounds__(128) contract_tc_kernel(const AsmArgs A, float
     bool b_built = false;
     bool ok = true;
 
-    auto build_b = [&](int k0, int kc) {
-        for (int idx = tid; idx < NB * KC; idx += 128) {
-            const int n = idx / KC, cc = idx % KC, c = k0 + cc;
-            float v = 0.f;
-            if (n < NPE && cc < kc) v = __ldg(A.Jmf + ((size_t)(c % 3) * NPE + n) * nq + c / 3);
-            const uint32_t off = tc::kmajor_offset(n, cc, KC) / 2;
-            bf16_split3(v, Bt[0][off], Bt[1][off], Bt[2][off]);
-        }
+    // per-element inputs of work item w, loaded into registers ahead of use: node tid, entry tid of
+    // the first column of the local-to-sorted map, and the element's Gauss-point values
+    uint64_t pq[TC_PF];  // raw bits: a float (tangent part) or a double (residual part)
+    int pslot[TC_PF];    // (value p << 16) | Gauss point g of register slot j, -1 if unused
+#pragma unroll
+    for (int j = 0; j < TC_PF; ++j) {
+        const int idx = tid + TC_THREADS * j;
+        pslot[j] = pf && idx < 54 * nq ? ((idx / nq) << 16) | (idx % nq) : -1;
+    }
+    uint64_t pnode = 0;
+    int pdl = 0;
+    // Gauss-point value p (0..44 the FP32 tangent part in A.Qf, 45..53 the FP64 residual part in
+    // A.Q) of point g of element el, as raw bits
+    auto load_q = [&](int p, int g, int64_t el) -> uint64_t {
+        const size_t col = (size_t)el * nq + g;
+        return p < 45 ? (uint64_t)__float_as_uint(A.Qf[(size_t)p * A.ldq + col])
+                      : (uint64_t)__double_as_longlong(A.Q[(size_t)(p - 45) * A.ldq + col]);
     };
+    auto prefetch = [&](int64_t w) {
+        if (w >= nwork) return;
+        const int64_t el = w / ngrp, e = A.e0 + el;
+        if (tid < NPE) pnode = A.elements[e * NPE + tid];
+        if (A.dl && tid < NDOF) pdl = A.dl[e * cap + (int64_t)tid * NDOF];
+#pragma unroll
+        for (int j = 0; j < TC_PF; ++j)
+            if (pslot[j] >= 0) pq[j] = load_q(pslot[j] >> 16, pslot[j] & 0xffff, el);
+    };
+    auto put_q = [&](int p, int g, uint64_t bits) {
+        if (p >= 45) {
+            Qr[(p - 45) * nq + g] = __longlong_as_double((long long)bits);
+            return;
+        }
+        const float v = __uint_as_float((uint32_t)bits);
+        const int I = c_sym.I[p], Kc = c_sym.K[p];
+        float *qx = reinterpret_cast<float *>(Qx + (size_t)g * 27);
+        qx[(I * 3 + Kc / 3) * 4 + Kc % 3] = v;
+        if (Kc != I) qx[(Kc * 3 + I / 3) * 4 + I % 3] = v;
+    };
+    // MMA rows whose lane is past RPL8 hold zeros for every work item: written once
+    for (int idx = tid; idx < tg * TC_MT * (KC / 8); idx += TC_THREADS) {
+        const int rr = idx % (tg * TC_MT), cg = idx / (tg * TC_MT);
+        if ((rr & 31) < RPL8) continue;
+        const uint32_t off = tc::kmajor_offset(rr, 8 * cg, KC) / 2;
+        *reinterpret_cast<uint4 *>(At[0] + off) = make_uint4(0, 0, 0, 0);
+        *reinterpret_cast<uint4 *>(At[1] + off) = make_uint4(0, 0, 0, 0);
+        *reinterpret_cast<uint4 *>(At[2] + off) = make_uint4(0, 0, 0, 0);
+    }
+    prefetch(blockIdx.x);
 
-    for (int64_t el = blockIdx.x; el < A.ne && ok; el += gridDim.x) {
-        const int64_t e = A.e0 + el;
-        __syncthreads();  // previous element done with the shared buffers
-        for (int a = tid; a < NPE; a += 128) {
-            uint64_t nd = A.elements[e * NPE + a];
+    for (int64_t w = blockIdx.x; w < nwork && ok; w += gridDim.x) {
+        const int64_t el = w / ngrp, e = A.e0 + el;
+        const int grp = (int)(w % ngrp);
+        const int t0 = grp * tg, tn = min(tg, NT - t0);
+        __syncthreads();  // previous work item done with the shared buffers
+        for (int a = tid; a < NPE; a += TC_THREADS) {  // entry tid was prefetched
+            uint64_t nd = a == tid ? pnode : A.elements[e * NPE + a];
             if (nd >= (uint64_t)A.nnode) {
                 flag |= FL_FLAG_BAD_INDEX;
                 nd = 0;
@@ -953,154 +923,294 @@ __global__ void __launch_bounds__(128) contract_tc_kernel(const AsmArgs A, float
             nodes[a] = (int)nd;
         }
         if (A.dl)
-            for (int i = tid; i < NDOF; i += 128) {
-                const int v = A.dl[e * cap + (int64_t)i * NDOF];
+            for (int i = tid; i < NDOF; i += TC_THREADS) {
+                const int v = i == tid ? pdl : A.dl[e * cap + (int64_t)i * NDOF];
                 const int p = v / NDOF;
                 if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
                 else inv[p] = i;
             }
-        const double *q = A.Q + el * nq;
-        for (int idx = tid; idx < nq * QSM; idx += 128) {
-            const int k = idx / nq, g = idx % nq;
-            Qs[(size_t)g * QSM + k] = (float)q[k * A.ldq + g];
+        if (pf) {
+#pragma unroll
+            for (int j = 0; j < TC_PF; ++j)
+                if (pslot[j] >= 0) put_q(pslot[j] >> 16, pslot[j] & 0xffff, pq[j]);
+        } else {
+            for (int idx = tid; idx < 54 * nq; idx += TC_THREADS) put_q(idx / nq, idx % nq, load_q(idx / nq, idx % nq, el));
         }
         __syncthreads();
+        if (staged) {  // map block of this element, needed at the read-back
+            const int *src = A.dg + e * cap;
+            if (wide)
+                for (int i = 4 * tid; i < cap; i += 4 * TC_THREADS) cp_async16(dgs + i, src + i);
+            else
+                for (int i = tid; i < cap; i += TC_THREADS) cp_async4(dgs + i, src + i);
+            cp_async_commit();
+        }
+        prefetch(w + gridDim.x);  // next item's inputs, in flight during this item
         if (!A.dl)  // offset of column node b in row node a; consecutive threads share a row
-            for (int idx = tid; idx < NPE * NPE; idx += 128) {
+            for (int idx = tid; idx < NPE * NPE; idx += TC_THREADS) {
                 const int off = row_search(A.indptr, A.indices, 3 * nodes[idx / NPE], 3 * nodes[idx % NPE]);
                 boff[idx] = (int16_t)(off >= 0 && off < 32768 ? off : -1);
             }
-        // residual in FP64
-        if (A.update) {
-            for (int r = tid; r < NDOF; r += 128) {
-                const int a = r / 3, i = r % 3;
+        // residual in FP64 (first tile group only): four threads per dof, each a quarter of the
+        // Gauss points, combined by shuffles (the loop trip count is uniform across the CTA)
+        if (A.update && grp == 0) {
+            for (int base = 0; base < 4 * NDOF; base += TC_THREADS) {
+                const int idx = base + tid, r = idx >> 2, part = idx & 3;
                 double t = 0.0;
-                const double *qs = q + (size_t)(45 + i * 3) * A.ldq;
-                for (int g = 0; g < nq; ++g) {
-                    t = fma(__ldg(A.Jm + (size_t)a * nq + g), qs[g], t);
-                    t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), qs[A.ldq + g], t);
-                    t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), qs[2 * A.ldq + g], t);
+                if (r < NDOF) {
+                    const int a = r / 3, i = r % 3;
+                    for (int g = part; g < nq; g += 4) {
+                        t = fma(__ldg(A.Jm + (size_t)a * nq + g), Qr[(i * 3) * nq + g], t);
+                        t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), Qr[(i * 3 + 1) * nq + g], t);
+                        t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), Qr[(i * 3 + 2) * nq + g], t);
+                    }
                 }
-                atomicAdd(A.T + 3 * (int64_t)nodes[a] + i, t);
+                t += __shfl_xor_sync(0xffffffffu, t, 1);
+                t += __shfl_xor_sync(0xffffffffu, t, 2);
+                if (r < NDOF && part == 0) atomicAdd(A.T + 3 * (int64_t)nodes[r / 3] + r % 3, t);
             }
         }
-        for (int m0 = 0; m0 < M; m0 += TC_MT) {
-            for (int k0 = 0; k0 < K; k0 += KC) {
-                const int kc = min(KC, K - k0);
-                // operands of this chunk (the previous chunk's MMAs completed: waited below)
-                for (int idx = tid; idx < TC_MT * KC; idx += 128) {
-                    const int rr = idx / KC, cc = idx % KC, r = m0 + rr, c = k0 + cc;
-                    float v = 0.f;
-                    if (r < M && cc < kc) {
-                        const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
-                        const int g = c / 3, d = c % 3, I = i * 3 + d;
-                        const float *qq = Qs + (size_t)g * QSM;  // U in FP32: the tangent's target accuracy
-                        v = fmaf(qq[sym9(I, k * 3 + 0)], __ldg(A.Jmf + ((size_t)0 * NPE + b) * nq + g),
-                                 fmaf(qq[sym9(I, k * 3 + 1)], __ldg(A.Jmf + ((size_t)1 * NPE + b) * nq + g),
-                                      qq[sym9(I, k * 3 + 2)] * __ldg(A.Jmf + ((size_t)2 * NPE + b) * nq + g)));
+        for (int k0 = 0; k0 < K; k0 += KC) {
+            const int kc = min(KC, K - k0);
+            // A operand: item = (row rl of the tile group, 8-column group cg); consecutive threads
+            // take consecutive rows and each quarter warp stores one 128-byte core matrix. Row
+            // rl = q RPL8 + l (q = 4 t + s, RPL8 = RPL padded to 8) sits at MMA row rr = 32 q + l
+            // (tile t0 + t, lane quarter s, lane l) and holds row r = (4 t0 + q) RPL + l of K^T
+            // when l < RPL and r < M, else zeros; lanes l >= RPL8 were zeroed at the start
+            const int nrg = tn * 4 * RPL8;
+            const uint32_t mg = 0xFFFFFFFFu / (uint32_t)nrg + 1u;
+            for (int idx = tid; idx < nrg * (KC / 8); idx += TC_THREADS) {
+                const int cg = fastdiv(idx, mg), rl = idx - cg * nrg, c0 = k0 + 8 * cg;
+                const int q4 = rl / RPL8, l = rl - q4 * RPL8, rr = 32 * q4 + l, r = (4 * t0 + q4) * RPL + l;
+                const bool live = l < RPL && r < M;
+                float v[8];
+                if (live && c0 + 8 <= K) {
+                    const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+                    const int g0 = c0 / 3;
+                    switch (c0 - 3 * g0) {
+                        case 0: u_row8<NPE, 0>(Qx, J4, g0, i, b, k, v); break;
+                        case 1: u_row8<NPE, 1>(Qx, J4, g0, i, b, k, v); break;
+                        default: u_row8<NPE, 2>(Qx, J4, g0, i, b, k, v); break;
                     }
-                    const uint32_t off = tc::kmajor_offset(rr, cc, KC) / 2;
-                    bf16_split3(v, At[0][off], At[1][off], At[2][off]);
-                }
-                if (!b_once || !b_built) {
-                    build_b(k0, kc);
-                    b_built = true;
-                }
-                tc::fence_async_smem();
-                tc::fence_before_sync();
-                __syncthreads();
-                tc::fence_after_sync();
-                if (tid == 0) {
-                    // the six products of order >= 2^-16, smallest first (term 0 = hi, 1 = mid, 2 = lo)
-                    const int pa[6] = {1, 2, 0, 1, 0, 0}, pb[6] = {1, 0, 2, 0, 1, 0};
-                    for (int ks = 0; ks < KC / 16; ++ks) {
-                        if (16 * ks >= kc) break;
-                        for (int t = 0; t < 6; ++t) {
-                            const uint64_t da = tc::smem_desc(At[pa[t]] + ks * 16 * 8, 128, sbo);
-                            const uint64_t db = tc::smem_desc(Bt[pb[t]] + ks * 16 * 8, 128, sbo);
-                            tc::mma_bf16(taddr, da, db, idesc, k0 > 0 || ks > 0 || t > 0);
+                } else {
+                    const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) {
+                        const int c = c0 + t;
+                        v[t] = 0.f;
+                        if (live && c < K) {
+                            const int g = c / 3, d = c % 3;
+                            v[t] = dot3(Qx[(size_t)g * 27 + 9 * i + 3 * d + k], __ldg(J4 + (size_t)g * NPE + b));
                         }
                     }
-                    tc::mma_commit(&mbar);
                 }
-                ok = __syncthreads_and(tc::mbar_wait(&mbar, phase & 1, TC_WAIT)) != 0;  // uniform in the CTA
-                ++phase;
-                tc::fence_after_sync();
-                if (!ok) break;
+                uint4 h, m, lo;
+                split8(v, h, m, lo);
+                const uint32_t off = tc::kmajor_offset(rr, 8 * cg, KC) / 2;
+                *reinterpret_cast<uint4 *>(At[0] + off) = h;
+                *reinterpret_cast<uint4 *>(At[1] + off) = m;
+                *reinterpret_cast<uint4 *>(At[2] + off) = lo;
             }
-            if (!ok) {
-                flag |= FL_FLAG_BAD_INDEX;  // reported as an error by the caller
-                break;
-            }
-            // read back: warp w holds rows m0 + 32 w + lane of the tile
-            const int r = m0 + 32 * warp + lane;
-            const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
-#pragma unroll 1
-            for (int c0 = 0; c0 < NB; c0 += 32) {
-                float v[32];
-                tc::tmem_ld32(taddr + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0, v);
-                if (r >= M) continue;
+            if (!b_once || !b_built) {  // B operand: Jm[d][n][g] at column c = 3 g + d
+                for (int idx = tid; idx < NB * (KC / 8); idx += TC_THREADS) {
+                    const int n = idx % NB, cg = idx / NB, c0 = k0 + 8 * cg;
+                    float v[8];
 #pragma unroll
-                for (int j = 0; j < 32; ++j) {
+                    for (int t = 0; t < 8; ++t) {
+                        const int c = c0 + t;
+                        v[t] = 0.f;
+                        if (n < NPE && c < K) {
+                            const float4 jj = __ldg(J4 + (size_t)(c / 3) * NPE + n);
+                            const int d = c % 3;
+                            v[t] = d == 0 ? jj.x : (d == 1 ? jj.y : jj.z);
+                        }
+                    }
+                    uint4 h, m, lo;
+                    split8(v, h, m, lo);
+                    const uint32_t off = tc::kmajor_offset(n, 8 * cg, KC) / 2;
+                    *reinterpret_cast<uint4 *>(Bt[0] + off) = h;
+                    *reinterpret_cast<uint4 *>(Bt[1] + off) = m;
+                    *reinterpret_cast<uint4 *>(Bt[2] + off) = lo;
+                }
+                b_built = true;
+            }
+            tc::fence_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
+                // per tile, the six products of order >= 2^-16, smallest first (0 = hi, 1 = mid,
+                // 2 = lo); a descriptor's start-address field counts 16-byte units, so the next
+                // K step (two core matrices, 256 bytes) adds 16 and the next tile (256 KC bytes) 16 KC
+                const int pa[6] = {1, 2, 0, 1, 0, 0}, pb[6] = {1, 0, 2, 0, 1, 0};
+                uint64_t da0[3], db0[3];
+#pragma unroll
+                for (int p = 0; p < 3; ++p) {
+                    da0[p] = tc::smem_desc(At[p], 128, sbo);
+                    db0[p] = tc::smem_desc(Bt[p], 128, sbo);
+                }
+                for (int t = 0; t < tn; ++t)
+                    for (int ks = 0; 16 * ks < kc; ++ks)
+#pragma unroll
+                        for (int p = 0; p < 6; ++p)
+                            tc::mma_bf16(taddr + (uint32_t)(t * CW), da0[pa[p]] + (uint64_t)(t * 16 * KC + 16 * ks),
+                                         db0[pb[p]] + (uint64_t)(16 * ks), idesc, k0 > 0 || ks > 0 || p > 0);
+                tc::mma_commit(&mbar);
+            }
+            if (staged && k0 + KC >= K) cp_async_wait_all();  // own map copies landed
+            // warp 0 polls the barrier, the others wait at the CTA barrier; uniform result
+            ok = __syncthreads_and(warp == 0 ? tc::mbar_wait(&mbar, phase & 1, TC_WAIT) : true) != 0;
+            ++phase;
+            tc::fence_after_sync();
+            if (!ok) break;
+        }
+        if (!ok) {
+            flag |= FL_FLAG_BAD_INDEX;  // reported as an error by the caller
+            break;
+        }
+        // read back: units of (tile, 16 columns), alternating between warps w and w + 4, which
+        // share tensor-memory lane quarter w % 4
+        const int sub = warp & 3, half = warp >> 2;
+        constexpr int CB = NB / 16;
+        for (int u = half; u < tn * CB; u += 2) {
+            const int t = u / CB, c0 = (u % CB) * 16;
+            float v[16];
+            tc::tmem_ld16(taddr + ((uint32_t)(32 * sub) << 16) + (uint32_t)(t * CW + c0), v);
+            const int r = ((t0 + t) * 4 + sub) * RPL + lane;
+            if (lane >= RPL || r >= M) continue;
+            const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+            if (A.dl) {  // positions first (independent loads in flight together), then the adds
+                const int ic = inv[3 * b + k];
+                int64_t pos[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int a = c0 + j;
+                    pos[j] = -1;
+                    if (a < NPE) {
+                        const int ir = inv[3 * a + i];
+                        if ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
+                            pos[j] = staged ? (int64_t)dgs[ir * NDOF + ic] : (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    if (c0 + j >= NPE) continue;
+                    if (pos[j] >= 0 && pos[j] < s_nnz) atomicAdd(V32 + pos[j], v[j]);
+                    else flag |= FL_FLAG_BAD_INDEX;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
                     const int a = c0 + j;  // C[r, a] = K_e[(a,i),(b,k)]
                     if (a >= NPE) continue;
-                    int64_t pos = -1;
-                    if (A.dl) {
-                        const int ir = inv[3 * a + i], ic = inv[3 * b + k];
-                        if ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
-                            pos = (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic];
-                    } else {
-                        pos = block_entry(A.indptr, A.indices, nodes[a], nodes[b], i, k, boff[a * NPE + b]);
-                    }
+                    const int64_t pos = block_entry(A.indptr, A.indices, nodes[a], nodes[b], i, k, boff[a * NPE + b]);
                     if (pos >= 0 && pos < s_nnz) atomicAdd(V32 + pos, v[j]);
                     else flag |= FL_FLAG_BAD_INDEX;
                 }
             }
-            tc::fence_before_sync();
-            __syncthreads();  // every warp has read the accumulator before the next tile's MMAs
-            tc::fence_after_sync();
         }
+        tc::fence_before_sync();
+        __syncthreads();  // every warp has read the accumulators before the next item's MMAs
+        tc::fence_after_sync();
     }
+    cp_async_wait_all();  // no copy outstanding at exit
+    if (!ok)  // give MMAs still in flight a second bounded wait before the tensor memory is freed
+        (void)__syncthreads_and(warp == 0 ? tc::mbar_wait(&mbar, (phase - 1) & 1, TC_WAIT) : true);
     if (flag) atomicOr(&s_flag, flag);
     tc::fence_before_sync();
     __syncthreads();
-    if (warp == 0) tc::tmem_dealloc(taddr, TCOLS);
+    if (warp == 0) tc::tmem_dealloc(taddr, (uint32_t)tcols);
     if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
 }
 
+// Tiling of the split-BF16 kernel (fl_SetTensorCoreTiling): 0 = automatic
+static std::atomic<int> g_tc_tg{0}, g_tc_kc{0};
+
+struct TcPlan {
+    int kc, tg, tcols;
+    size_t smem;
+    int stage;  // the element's map block is staged in shared memory
+};
+
+// Plan: reduction chunk kc (a multiple of 16, at most MX_KC) and tile group tg (tiles per work
+// item, tensor memory tg * CW <= 256 columns). First choice: the padded 3 nq as kc with the most
+// tiles that leave room for two CTAs per SM; else the widest kc, then the most tiles, that fit one
+// CTA. fl_SetTensorCoreTiling fixes either.
 template <int NPE>
-static size_t mixed_smem_bytes(int nq, bool utab) {
-    return mixed_base_bytes<NPE>(nq) + (utab ? sizeof(float) * (size_t)nq * NPE * 27 : 0);
+static TcPlan tc_plan(int nq) {
+    constexpr int NT = tc_ntiles<NPE>(), CW = tc_colw<NPE>();
+    const int kc_req = g_tc_kc.load(), tg_req = g_tc_tg.load();
+    const int kc_nat = kc_req > 0 ? std::min((kc_req + 15) / 16 * 16, MX_KC) : mixed_kc(nq);
+    const size_t limit[2] = {113 * 1024, 227 * 1024};
+    for (int pass = 0; pass < 2; ++pass)
+        for (int kc = kc_nat; kc >= 16; kc -= 16) {
+            if ((pass == 0 || kc_req > 0) && kc != kc_nat) break;
+            for (int tg = tg_req > 0 ? std::min(tg_req, NT) : NT; tg >= 1; --tg) {
+                if (tg_req > 0 && tg != std::min(tg_req, NT)) break;
+                if (tg * CW > 256) continue;
+                const size_t s = tc_smem_bytes<NPE>(nq, kc, tg);
+                if (s > limit[pass]) continue;
+                int cols = 32;
+                while (cols < tg * CW) cols *= 2;
+                const size_t s2 = tc_smem_bytes<NPE>(nq, kc, tg, true);
+                return s2 <= limit[pass] ? TcPlan{kc, tg, cols, s2, 1} : TcPlan{kc, tg, cols, s, 0};
+            }
+        }
+    return TcPlan{0, 0, 0, 0, 0};
+}
+
+// Resident CTAs per SM of the split-BF16 kernel, from its shared memory (with the largest
+// shared-memory carveout requested), registers and tensor-memory columns (512 per SM)
+static int tc_ctas_per_sm(const void *kernel, const TcPlan &P) {
+    int dev = 0, smem_sm = 0, reserved = 0, regs_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, dev);
+    cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess) return 1;
+    const size_t per_cta = P.smem + fa.sharedSizeBytes + (size_t)reserved;
+    int n = (int)((size_t)smem_sm / per_cta);
+    const int regs = (fa.numRegs + 7) / 8 * 8;
+    if (regs > 0) n = std::min(n, regs_sm / (TC_THREADS * regs));
+    n = std::min(n, 512 / P.tcols);
+    return std::max(1, std::min(n, 8));
 }
 
 template <int NPE, int MAT>
 static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
     if (A.nelem == 0) return FL_OK;
-    A.utab = 0;
-    const size_t smem = tc_smem_bytes<NPE>(A.nq);
-    if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    { const int st = ensure_smem<contract_tc_kernel<NPE>>(smem); if (st != FL_OK) return st; }
-    int64_t chunk = chunk_elements(CHUNK_BYTES, A.nq, 1);
+    const TcPlan P = tc_plan<NPE>(A.nq);
+    if (P.tg == 0) return FL_ERR_UNSUPPORTED;
+    { const int st = ensure_smem<contract_tc_kernel<NPE>>(P.smem); if (st != FL_OK) return st; }
+    // Gauss-point scratch per chunk: S [9][ldq] FP64, the tangent part [45][ldq] FP32 (252 bytes
+    // per point, the chunk sized like the FP64 path's to stay in L2), then the float4 table of Jm
+    int64_t chunk = std::max<int64_t>(1, (int64_t)(CHUNK_BYTES / ((9 * sizeof(double) + 45 * sizeof(float)) * (size_t)A.nq)));
     if (chunk > A.nelem) chunk = A.nelem;
-    double *Q = nullptr;  // Gauss-point scratch, then the FP32 copy of Jm
-    const size_t qbytes = (sizeof(double) * QSTRIDE * (size_t)A.nq * chunk + 255) & ~(size_t)255;
-    const int64_t njm = (int64_t)3 * NPE * A.nq;
-    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, qbytes + sizeof(float) * (size_t)njm, stream));
+    const size_t sbytes = (sizeof(double) * 9 * (size_t)A.nq * chunk + 255) & ~(size_t)255;
+    const size_t fbytes = (sizeof(float) * 45 * (size_t)A.nq * chunk + 255) & ~(size_t)255;
+    const int64_t nj4 = (int64_t)(A.nq + 4) * NPE;
+    double *Q = nullptr;
+    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sbytes + fbytes + sizeof(float4) * (size_t)nj4, stream));
     A.Q = Q;
+    A.Qf = reinterpret_cast<float *>(reinterpret_cast<char *>(Q) + sbytes);
     A.ldq = chunk * A.nq;
-    float *Jmf = reinterpret_cast<float *>(reinterpret_cast<char *>(Q) + qbytes);
-    to_float<<<(unsigned)((njm + 255) / 256), 256, 0, stream>>>(A.Jm, Jmf, njm);
-    A.Jmf = Jmf;
+    float4 *J4 = reinterpret_cast<float4 *>(reinterpret_cast<char *>(Q) + sbytes + fbytes);
+    jm_float4<<<(unsigned)((nj4 + 255) / 256), 256, 0, stream>>>(A.Jm, J4, NPE, A.nq);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int occ = tc_ctas_per_sm(reinterpret_cast<const void *>(contract_tc_kernel<NPE>), P);
+    const int ngrp = (tc_ntiles<NPE>() + P.tg - 1) / P.tg;
     for (int64_t e0 = 0; e0 < A.nelem; e0 += chunk) {
         A.e0 = e0;
         A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
         const int64_t nqp = A.ne * A.nq;
-        qp_kernel<NPE, MAT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
-        const int64_t grid = std::min<int64_t>(A.ne, (int64_t)sms * 8);
-        contract_tc_kernel<NPE><<<(unsigned)grid, 128, smem, stream>>>(A, V32);
+        qp_kernel<NPE, MAT, true><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        const int64_t grid = std::min<int64_t>(A.ne * ngrp, (int64_t)sms * occ);
+        contract_tc_kernel<NPE><<<(unsigned)grid, TC_THREADS, P.smem, stream>>>(A, J4, V32, P.kc, P.tg, P.tcols,
+                                                                                 P.stage);
     }
     const int st = launch_status();
     const cudaError_t fe = cudaFreeAsync(Q, stream);
@@ -1195,8 +1305,6 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.elements = elements;
     A.Eulerx = Eulerx;
     A.Jm = Jm;
-    A.Jmf = nullptr;
-    A.utab = 0;
     A.w = AllGauss;
     A.nelem = nelem;
     A.nnode = nnode;
@@ -1214,6 +1322,7 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.eparams = element_params;
     A.flags = flags;
     A.Q = nullptr;
+    A.Qf = nullptr;
     A.e0 = A.ne = A.ldq = 0;
     int mat = 0;
     if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &A.mp) != FL_OK) return FL_ERR_UNSUPPORTED;
@@ -1252,6 +1361,13 @@ int fl_SetAssemblyArithmetic(int arithmetic) {
 }
 
 int fl_GetAssemblyArithmetic(void) { return fl::g_arith.load(); }
+
+int fl_SetTensorCoreTiling(int tile_group, int reduction_chunk) {
+    if (tile_group < 0 || tile_group > 16 || reduction_chunk < 0 || reduction_chunk > fl::MX_KC) return FL_ERR_ARG;
+    fl::g_tc_tg.store(tile_group);
+    fl::g_tc_kc.store(reduction_chunk);
+    return FL_OK;
+}
 
 int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk) {
     std::lock_guard<std::mutex> lock(fl::g_tune_mutex);

@@ -195,6 +195,14 @@ int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
 int fl_SetAssemblyArithmetic(int arithmetic);
 int fl_GetAssemblyArithmetic(void);
 
+/* Tiling of the split-BF16 tensor-core tangent (fl_GlobalAssemblyDF_Mixed; no reference
+ * counterpart) for every later call of the process: tile_group = 128-row tiles of the element's
+ * transposed stiffness per work item (1..16), reduction_chunk = (Gauss point, direction) columns
+ * per tensor-core round (a multiple of 16 up to 96). 0 = automatic (the default). A choice whose
+ * shared or tensor memory does not fit makes later calls return FL_ERR_UNSUPPORTED. FL_ERR_ARG
+ * outside the ranges. */
+int fl_SetTensorCoreTiling(int tile_group, int reduction_chunk);
+
 /* ------------------------------------------------------------------------------------------
  * Explicit (matrix-free) internal force, T[nnode*nvar] += sum_e sum_g detJ (grad N_a . sigma).
  * Argument list of the reference's _GlobalAssemblyExplicit_DF_DPF_ plus flags and stream.

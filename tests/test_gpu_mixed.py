@@ -41,6 +41,29 @@ def test_mixed_tangent_on_config1_cube():
     assert rel_fro(T.cpu().numpy(), T64.cpu().numpy()) < 1e-13
 
 
+@pytest.mark.parametrize("mode", ["csr", "squeeze"])
+@pytest.mark.parametrize("tiling", [(1, 16), (1, 48), (2, 32), (0, 0)])
+@pytest.mark.parametrize("case", ["config1_hex8_p2_q5", "tet_p3_mr_jitter", "hex_p4_nh"])
+def test_mixed_tangent_tilings(case, tiling, mode):
+    """Every tile group / reduction chunk of the tensor-core kernel (one or several 128-row tiles
+    per work item, one or several K chunks per element, scatter through the element-to-nonzero
+    maps or by row search) gives the tangent within the split-BF16 bar of the FP64 one."""
+    import florence_gb300 as fl
+    d = load_golden(case)
+    asm = fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], str(d["material"]),
+                             tuple(d["params"]), mode=mode, requires_geometry_update=int(d["update"]))
+    x = torch.from_numpy(d["Eulerx"]).cuda()
+    V64, T64 = asm.assemble(x)
+    try:
+        fl.set_tensor_core_tiling(*tiling)
+        V32, T = asm.assemble_mixed(x)
+        asm.check_flags()
+    finally:
+        fl.set_tensor_core_tiling(0, 0)
+    assert rel_fro(V32.double().cpu().numpy(), V64.cpu().numpy()) < 5e-6
+    assert rel_fro(T.cpu().numpy(), T64.cpu().numpy()) < 1e-13
+
+
 def test_pcg_with_fp32_values_matches_fp64_values():
     import florence_gb300 as fl
     from florence_gb300.newton import build_beam_problem, pcg
