@@ -329,7 +329,7 @@ def run_ours(args):
                         fp64_equivalent_tflops=achieved, fp64_equivalent_frac=achieved / fp64_peak,
                         instr_per_launch=instr)
     tag = {"fp64": "assemble_df_%s_%s", "float_pair": "contract_float_pair_%s_%s",
-           "mixed": "contract_mixed_%s_%s"}[args.arith] % (W["desc"]["element"], W["desc"]["material"])
+           "mixed": "contract_tc_%s_%s"}[args.arith] % (W["desc"]["element"], W["desc"]["material"])
     roofline.update(traffic=traffic_from_profile(tag), flop_alg_per_launch=f_alg, flop_executed_per_launch=f_exe,
                     kernel_ms=kernel_ms,
                     hbm=dict(bytes_min_per_launch=bmin, achieved_gbs=bmin / (kernel_ms * 1e-3) / 1e9,
@@ -412,6 +412,57 @@ def run_newton(args):
                             nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
                 newton_iters=out["newton_iters"], pcg_iters=out["pcg_iters"], failed=out["failed"],
                 tip_uz=float(u[tip, 2].mean()), increments=incs, **extra)
+    print(json.dumps(line), flush=True)
+
+
+def run_pcg(args):
+    """Block-Jacobi PCG iterations on the FP64 tangent of the tet p=3 beam (the Newton
+    configuration's matrix at the unloaded state, 95 M nonzeros), a fixed count of iterations
+    (no convergence stop), per product mode: float-pair split values on the FP32 pipe (Newton's
+    default) and FP64 products. Reports the time per iteration and the achieved bandwidth by
+    algorithmic bytes against the measured HBM peak."""
+    import torch
+    import florence_gb300 as fl
+    from florence_gb300.newton import build_beam_problem, pcg, pcg_workspace
+    cells = (48, 12, 12) if args.workload != "beam_s" else (24, 6, 6)
+    P, el, Jm, w, fixed, f = build_beam_problem(*cells, traction=0.01)
+    asm = fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
+    V, _ = asm.assemble(torch.from_numpy(P).cuda())
+    fx = torch.from_numpy(fixed.astype(np.int8)).cuda()
+    b = torch.from_numpy(np.where(fixed, 0.0, f)).cuda()
+    n, nnz = asm.nnode * 3, asm.nnz
+    # algorithmic bytes per iteration: values (8 B per nonzero either way: FP64, or the hi + lo
+    # float pair), one column index per 3x3 block, the row pointers, and the vector streams of
+    # the three kernels (K1 reads p and writes q as float pairs, 16 B per dof; K2 reads x, p, q, r
+    # and the 3x3 block inverse, 64 B, and writes x, r, z, 24 B; K3 reads z, p and writes p and
+    # its float pair, 32 B)
+    nbytes = 8 * nnz + 4 * (nnz // 9) + 4 * (n + 1) + 136 * n
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    res = {}
+    for spmv in ("split", "fp64"):
+        ws = pcg_workspace(asm, V, spmv)
+        pcg(asm, V, b, fx, rtol=1e-30, maxiter=args.warmup * 16, workspace=ws, spmv=spmv)  # lanes autotune
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            e0.record()
+            _, it, rel = pcg(asm, V, b, fx, rtol=1e-30, maxiter=args.pcg_iters, workspace=ws, spmv=spmv)
+            e1.record()
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / it
+        res[spmv] = dict(ms_per_iter=ms, iterations=it, achieved_gbs=nbytes / (ms * 1e-3) / 1e9,
+                         frac=nbytes / (ms * 1e-3) / 1e9 / hbm, clocks=clk.summary())
+    line = dict(metric="block-Jacobi PCG time per iteration (float-pair split SpMV)", value=res["split"]["ms_per_iter"],
+                unit="ms", n_gpus=1, steps=args.pcg_iters, warmup=args.warmup * 16, higher_is_better=False,
+                scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice), Mooney-Rivlin FP64 tangent at "
+                                     "the unloaded state, x=0 clamped" % cells, n=n, nnz=nnz,
+                            inputs="larger than L2 (values %.0f MB)" % (8 * nnz / 1e6)),
+                roofline=dict(bound="hbm", achieved=res["split"]["achieved_gbs"], peak=hbm, unit="GB/s",
+                              frac=res["split"]["frac"], bytes_per_iter=nbytes,
+                              peak_source="MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"),
+                split=res["split"], fp64=res["fp64"], clocks=res["split"]["clocks"])
     print(json.dumps(line), flush=True)
 
 
@@ -638,6 +689,8 @@ def main():
                     help="PCG tolerance per Newton step: Eisenstat-Walker, or 0.1 x relative residual")
     ap.add_argument("--spmv", default="split", choices=["split", "fp64"],
                     help="PCG product for FP64 tangents: float-pair split on the FP32 pipe, or FP64")
+    ap.add_argument("--pcg", action="store_true", help="PCG iterations on the beam's tangent instead")
+    ap.add_argument("--pcg-iters", type=int, default=400)
     ap.add_argument("--batched", action="store_true", help="batched uneven instances instead")
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-gb", type=float, default=40.0, help="CSR memory budget per sub-batch")
@@ -653,6 +706,8 @@ def main():
         run_reference(args)
     elif args.newton:
         run_newton(args)
+    elif args.pcg:
+        run_pcg(args)
     elif args.explicit:
         run_explicit(args)
     elif args.batched:
