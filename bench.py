@@ -602,8 +602,9 @@ def e2e_dropin(W, asm, args):
                                    data_local_indices=spa[2], data_global_indices=spa[3])
     fn = getattr(fl, "_LowLevelAssemblyDF__" + mat + "_")
     Ep = np.zeros(W["points"].shape[0])
-    for _ in range(2):
-        fn(solver, fs, form, mesh, material, W["x"], Ep)
+    V = T = None
+    for _ in range(3):  # as in the timed loop, each call runs while the previous result is held
+        V, T = fn(solver, fs, form, mesh, material, W["x"], Ep)
     steps = max(3, min(args.steps, 10))
     torch.cuda.synchronize()
     t0 = time.perf_counter()

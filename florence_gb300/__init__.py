@@ -11,10 +11,12 @@ from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssembl
                        _LowLevelAssemblyDF__MooneyRivlin_, _LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_,
                        _LowLevelAssemblyDF__NeoHookean_, _LowLevelAssemblyExplicit_DF_DPF_,
                        __TotalConstantMassIntegrand__, arithmetic, device_sparsity, fp32_peak_gflops, fp64_peak_gflops,
-                       get_arithmetic, install, material_params, set_arithmetic, set_tensor_core_tiling)
+                       get_arithmetic, install, material_params, release_host_buffers, set_arithmetic,
+                       set_tensor_core_tiling)
 
 __all__ = ["ComputeSparsityPattern", "DeviceAssembler", "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",
            "_LowLevelAssemblyDF__LinearElastic_", "_LowLevelAssemblyExplicit_DF_DPF_",
            "__TotalConstantMassIntegrand__", "arithmetic", "device_sparsity", "fp32_peak_gflops", "fp64_peak_gflops", "get_arithmetic",
-           "install", "material_params", "set_arithmetic", "set_tensor_core_tiling"]
+           "install", "material_params", "release_host_buffers", "set_arithmetic",
+           "set_tensor_core_tiling"]

@@ -21,7 +21,9 @@ Every call goes through the CUDA library; there is no CPU path.
 """
 import contextlib
 import ctypes
+import threading
 import warnings
+import weakref
 
 import numpy as np
 import torch
@@ -30,7 +32,8 @@ from . import _native as N
 
 __all__ = ["DeviceAssembler", "ComputeSparsityPattern", "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
-           "__TotalConstantMassIntegrand__", "install", "material_params", "fp64_peak_gflops"]
+           "__TotalConstantMassIntegrand__", "install", "material_params", "fp64_peak_gflops",
+           "release_host_buffers"]
 
 MATERIALS = {"NeoHookean": N.FL_MATERIAL_NEOHOOKEAN, "MooneyRivlin": N.FL_MATERIAL_MOONEYRIVLIN,
              "NearlyIncompressibleMooneyRivlin": N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
@@ -57,6 +60,56 @@ class NonPositiveJacobianWarning(RuntimeWarning):
 
 def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+class _HostPool:
+    """Host buffers for the drop-ins' outputs, reused once the caller has dropped the array a
+    buffer was last returned as (tracked by a weak reference; a live view or a matrix built on the
+    array keeps it alive). Fresh host memory costs a page fault per page on its first write, which
+    made the device-to-host copy of a 761 MB tangent run at 27 GB/s; into memory written before,
+    the same copy runs at ~190 GB/s over the Grace-GPU link. At most `keep` idle buffers per size
+    are held; ``release_host_buffers()`` frees them."""
+
+    def __init__(self, keep=2):
+        self.keep = keep
+        self.slots = []  # [tensor, weakref to the array last handed out]
+        self.lock = threading.Lock()
+
+    def take(self, shape, dtype):
+        n = int(np.prod(shape))
+        with self.lock:
+            same = [sl for sl in self.slots if sl[0].numel() == n and sl[0].dtype == dtype]
+            idle = [sl for sl in same if sl[1]() is None]
+            if idle:
+                slot = idle.pop(0)
+            else:
+                slot = [torch.empty(n, dtype=dtype), None]
+                self.slots.append(slot)
+            drop = {id(sl) for sl in idle[self.keep:]}
+            self.slots = [sl for sl in self.slots if id(sl) not in drop]
+            # the weak reference is to the array that every view of the returned one has as its
+            # base (numpy collapses view chains onto it), so it dies only with the last view
+            base = slot[0].numpy()
+            slot[1] = weakref.ref(base)
+            return slot[0], base.reshape(shape)
+
+    def to_host(self, dev):
+        """Copy of a device tensor into a pooled host array (synchronous)."""
+        t, arr = self.take(tuple(dev.shape), dev.dtype)
+        t.copy_(dev.reshape(-1))
+        return arr
+
+    def release(self):
+        with self.lock:
+            self.slots = [sl for sl in self.slots if sl[1]() is not None]
+
+
+_HOST = _HostPool()
+
+
+def release_host_buffers():
+    """Frees the idle host buffers of the drop-ins' outputs (arrays still held are unaffected)."""
+    _HOST.release()
 
 
 def _ptr(t):
@@ -291,7 +344,7 @@ def _low_level_df(name, fem_solver, function_space, formulation, mesh, material,
                           mode=mode, requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity)
     x = _to_dev(Eulerx, torch.float64, asm.device)
     out = asm.assemble(x)
-    host = [t.cpu().numpy() for t in out]
+    host = [_HOST.to_host(t) for t in out]
     asm.check_flags("_LowLevelAssemblyDF_" + name)
     return tuple(host)
 
@@ -331,7 +384,7 @@ def _LowLevelAssemblyExplicit_DF_DPF_(function_space, formulation, mesh, materia
     asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, name, params,
                           mode="triplet")
     T = asm.internal_force(_to_dev(Eulerx, torch.float64, asm.device))
-    out = T.cpu().numpy()
+    out = _HOST.to_host(T)
     asm.check_flags("_LowLevelAssemblyExplicit_DF_DPF_")
     return out
 
