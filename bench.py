@@ -110,6 +110,14 @@ def mixed_launches(nelem, nq):
     return 1 + 2 * ((nelem + ce - 1) // ce)
 
 
+def tensor_launches(nelem, nq):
+    """Kernels one FP64 tensor-core assembly call launches: the float-pair table of the
+    shape-function gradients, then (Gauss-point kernel + contraction) per chunk of the 64 MiB
+    Gauss-point scratch (9 doubles + 90 floats per Gauss point)."""
+    ce = max(1, (64 << 20) // ((9 * 8 + 90 * 4) * nq))
+    return 1 + 2 * ((nelem + ce - 1) // ce)
+
+
 def pair_macs(npe, nq):
     """Multiply-adds of the contraction per element (stiffness node blocks a <= b and the U
     build), each 12 FP32-pipe instructions in the float-pair arithmetic."""
@@ -320,6 +328,17 @@ def run_ours(args):
                         peak_source="MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
                         note="the tensor work per element is small; the FP64 Gauss-point kernel and the scatter "
                              "bound the step", fp64_equivalent_tflops=achieved)
+    elif args.arith == "tensor":  # FP64 tangent on the tensor cores: 21 digit-pair products per K step
+        npad = (npe + 15) // 16 * 16
+        mpad = (9 * npe + 127) // 128 * 128
+        kpad = (3 * nq + 15) // 16 * 16
+        tflop = 21 * 2.0 * mpad * npad * kpad * nelem / (kernel_ms * 1e-3) / 1e12
+        peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+        bf16_peak = peaks.get("bf16_tflops", 1900.0)
+        roofline = dict(bound="tensor", achieved=tflop, peak=bf16_peak, unit="TFLOP/s", frac=tflop / bf16_peak,
+                        peak_source="MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
+                        note="BF16 digit products; the operand build and the scatter bound the step",
+                        fp64_equivalent_tflops=achieved, fp64_equivalent_frac=achieved / fp64_peak)
     else:  # the contraction runs as float pairs on the FP32 pipe
         instr = 12.0 * pair_macs(npe, nq) * nelem
         ach_i = instr / (kernel_ms * 1e-3) / 1e12
@@ -328,7 +347,7 @@ def run_ours(args):
                         peak_source="FP32 FMA microkernel measured in this run (instructions/s = FLOP/s / 2)",
                         fp64_equivalent_tflops=achieved, fp64_equivalent_frac=achieved / fp64_peak,
                         instr_per_launch=instr)
-    tag = {"fp64": "assemble_df_%s_%s", "float_pair": "contract_float_pair_%s_%s",
+    tag = {"fp64": "assemble_df_%s_%s", "float_pair": "contract_float_pair_%s_%s", "tensor": "contract_oz_%s_%s",
            "mixed": "contract_tc_%s_%s"}[args.arith] % (W["desc"]["element"], W["desc"]["material"])
     roofline.update(traffic=traffic_from_profile(tag), flop_alg_per_launch=f_alg, flop_executed_per_launch=f_exe,
                     kernel_ms=kernel_ms,
@@ -355,13 +374,16 @@ def run_ours(args):
                     n_gpus=world, steps=args.steps, warmup=args.warmup, ms_per_step=ms / args.steps,
                     higher_is_better=True, scaling="weak", vs_baseline=None,
                     dtype={"fp64": "f64", "float_pair": "f64 (float-pair contraction)",
+                           "tensor": "f64 (six-digit BF16 products, exact f32 levels, float-pair recombination)",
                            "mixed": "bf16x3 products, f32 accumulate; f64 residual"}[args.arith], data="synthetic",
                     config=dict(W["desc"], nelem=int(nelem), nnode=int(nnode), nnz=int(asm.nnz), gauss_points=nq,
                                 parallelism="replicas" if world > 1 else "single GPU",
                                 l2="inputs larger than L2: CSR values %.0f MB and element-to-nonzero map %.0f MB "
                                    "per step" % (asm.nnz * 8 / 1e6, asm.data_global.numel() * 4 / 1e6)),
                     roofline=roofline, cpu_baseline=cpu, e2e=e2e, clocks=clocks,
-                    gpu_launches=args.steps * (mixed_launches(nelem, nq) if mixed else assembly_launches(nelem, npe, nq)))
+                    gpu_launches=args.steps * (mixed_launches(nelem, nq) if mixed else
+                                               tensor_launches(nelem, nq) if args.arith == "tensor" else
+                                               assembly_launches(nelem, npe, nq)))
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
@@ -671,7 +693,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
-    ap.add_argument("--arith", default="float_pair", choices=["fp64", "float_pair", "mixed"],
+    ap.add_argument("--arith", default="float_pair", choices=["fp64", "float_pair", "tensor", "mixed"],
                     help="arithmetic of the stiffness contraction (FP64, float pairs on the FP32 pipe, or the "
                          "split-BF16 tensor-core tangent with FP32 values)")
     ap.add_argument("--tc-tiling", default="0,0",

@@ -23,6 +23,7 @@ FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN = 3
 FL_MATERIAL_LINEARELASTIC = 10
 FL_ARITH_FP64 = 0
 FL_ARITH_FLOAT_PAIR = 1
+FL_ARITH_TENSOR = 2
 FL_PCG_F64 = 64
 FL_PCG_F32 = 32
 FL_PCG_F64_SPLIT = 6432

@@ -449,13 +449,15 @@ def fp32_peak_gflops():
     return g.value
 
 
-ARITHMETIC = {"fp64": N.FL_ARITH_FP64, "float_pair": N.FL_ARITH_FLOAT_PAIR}
+ARITHMETIC = {"fp64": N.FL_ARITH_FP64, "float_pair": N.FL_ARITH_FLOAT_PAIR, "tensor": N.FL_ARITH_TENSOR}
 
 
 def set_arithmetic(name):
     """Arithmetic of the stiffness contraction for every later FP64 assembly in the process:
-    'float_pair' (the default: hi + lo float pairs on the FP32 pipe, ~1e-14 relative to FP64) or
-    'fp64' (FP64 multiply-adds). Kinematics, material, residual and scatter are FP64 in both."""
+    'float_pair' (the default: hi + lo float pairs on the FP32 pipe, ~1e-14 relative to FP64),
+    'fp64' (FP64 multiply-adds) or 'tensor' (tensor cores on operands split into six exact BF16
+    digits, ~1e-13; CSR outputs of supported element types, else float pairs). Kinematics,
+    material, residual and scatter are FP64 in all three."""
     N.check(N.lib().fl_SetAssemblyArithmetic(ARITHMETIC[name]), "fl_SetAssemblyArithmetic")
 
 

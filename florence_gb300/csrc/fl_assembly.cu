@@ -108,11 +108,12 @@ __host__ __device__ __forceinline__ constexpr int sym9(int I, int K) {
 // Pulled-back tangent of one Gauss point in arithmetic T from the FP64 kinematics and material:
 // Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
 //                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ] (+ the
-// nearly incompressible material's terms), written as out[sym9(I, K) * ld], I = 3 i + d, K = 3 k + e
-template <typename T, int MAT>
+// nearly incompressible material's terms), handed to out.put(sym9(I, K), value), I = 3 i + d,
+// K = 3 k + e
+template <typename T, int MAT, class OUT>
 __device__ __forceinline__ void pulled_back_tangent(const double *Gd, const double *sigd, const double *bd,
                                                     const ExtraTangent &exd, double c1d, double c2d, double cbbd,
-                                                    double detJd, T *out, int64_t ld) {
+                                                    double detJd, const OUT &out) {
     constexpr bool NIMR = MAT == NEARLYINCOMPRESSIBLEMR;
     T G[9], sig[6], b[6], g6[6];
 #pragma unroll
@@ -168,13 +169,38 @@ __device__ __forceinline__ void pulled_back_tangent(const double *Gd, const doub
                 if (i == k) t4 += GgG[dd * 3 + ee];
                 v = fma(kg4, t4, v);
             }
-            out[sym9(I, K) * ld] = detJ * v;
+            out.put(sym9(I, K), detJ * v);
         }
 }
 
-// F32T: the tangent part in FP32 into A.Qf [45][ldq] (the split-BF16 Jacobian's input) and the
-// residual part S in FP64 into A.Q [9][ldq]; else both in FP64 into A.Q [54][ldq]
-template <int NPE, int MAT, bool F32T = false>
+// Gauss-point tangent writers: FP64, FP32, or an FP64 value as the float pair hi + lo
+struct QOutF64 {
+    double *q;
+    int64_t ld;
+    __device__ void put(int p, double v) const { q[p * ld] = v; }
+};
+struct QOutF32 {
+    float *q;
+    int64_t ld;
+    __device__ void put(int p, float v) const { q[p * ld] = v; }
+};
+struct QOutPair {
+    float *h, *l;
+    int64_t ld;
+    __device__ void put(int p, double v) const {
+        const float hi = (float)v;
+        h[p * ld] = hi;
+        l[p * ld] = (float)(v - (double)hi);
+    }
+};
+
+// Gauss-point output layout: FP64 [54][ldq] in Q; FP32 tangent [45][ldq] in Qf with S [9][ldq]
+// in Q; float-pair tangent (hi [45][ldq] then lo [45][ldq]) in Qf with S [9][ldq] in Q
+enum { QOUT_F64 = 0, QOUT_F32 = 1, QOUT_PAIR = 2 };
+
+// QOUT: layout of the Gauss-point data (QOUT_F64, QOUT_F32 for the split-BF16 Jacobian,
+// QOUT_PAIR for the FP64 tangent on the tensor cores); S is FP64 in every layout
+template <int NPE, int MAT, int QOUT = QOUT_F64>
 __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
     const int64_t t = (int64_t)blockIdx.x * QP_THREADS + threadIdx.x;
     const int nq = A.nq;
@@ -204,15 +230,19 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         const int64_t ld = A.ldq;
         double *q = A.Q + t;
         // S[i][d] = detJ sum_j sigma_ij G[j][d], the residual's Gauss-point factor, in FP64
-        double *qs = F32T ? q : q + 45 * ld;
+        double *qs = QOUT != QOUT_F64 ? q : q + 45 * ld;
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int d = 0; d < 3; ++d)
                 qs[(i * 3 + d) * ld] =
                     detJ * fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
-        if (F32T) pulled_back_tangent<float, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, A.Qf + t, ld);
-        else pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, q, ld);
+        if constexpr (QOUT == QOUT_F32)
+            pulled_back_tangent<float, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF32{A.Qf + t, ld});
+        else if constexpr (QOUT == QOUT_PAIR)
+            pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutPair{A.Qf + t, A.Qf + 45 * ld + t, ld});
+        else
+            pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF64{q, ld});
     }
     if (flag && A.flags) atomicOr(A.flags, flag);
 }
@@ -537,9 +567,17 @@ static int run_chunks(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) 
 }
 
 template <int NPE, int MAT>
+static int launch_oz(AsmArgs A, cudaStream_t stream);
+template <int NPE>
+static bool oz_supported(int nq);
+
+template <int NPE, int MAT>
 static int launch_asm(AsmArgs A, double *scratch, size_t scratch_bytes, cudaStream_t stream) {
     constexpr int EPC = AsmCfg<NPE>::EPC;
     if (A.nelem == 0) return FL_OK;
+    // FP64 tangent on the tensor cores: CSR output, its own scratch, elements it supports
+    if (g_arith.load() == FL_ARITH_TENSOR && !scratch && A.mode != 0 && oz_supported<NPE>(A.nq))
+        return launch_oz<NPE, MAT>(A, stream);
     if (scratch) {  // caller-provided scratch
         const int64_t chunk = chunk_elements(scratch_bytes, A.nq, EPC);
         if (chunk < EPC) return FL_ERR_CAPACITY;
@@ -1207,10 +1245,569 @@ static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
         A.e0 = e0;
         A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
         const int64_t nqp = A.ne * A.nq;
-        qp_kernel<NPE, MAT, true><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        qp_kernel<NPE, MAT, QOUT_F32><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
         const int64_t grid = std::min<int64_t>(A.ne * ngrp, (int64_t)sms * occ);
         contract_tc_kernel<NPE><<<(unsigned)grid, TC_THREADS, P.smem, stream>>>(A, J4, V32, P.kc, P.tg, P.tcols,
                                                                                  P.stage);
+    }
+    const int st = launch_status();
+    const cudaError_t fe = cudaFreeAsync(Q, stream);
+    if (st != FL_OK) return st;
+    return fe == cudaSuccess ? FL_OK : FL_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------------------------------------
+// E. The FP64 tangent on the tensor cores (FL_ARITH_TENSOR).
+//
+// The same contraction as section D, to FP64 accuracy: both operands are scaled by a power of two
+// (per element for U, from max|Ahat| times the largest column sum of |Jm|; per element type for Jm)
+// and written as six signed base-256 digits, x = 2^e (d0 + d1 2^-8 + ... + d5 2^-40) / 128, every
+// digit an integer of at most 8 bits, held exactly in BF16. The products of digit pairs (i, j)
+// are summed per level w = i + j < 6 in an FP32 tensor-memory accumulator of their own: 21 MMAs
+// per tile and 16-wide K step. Digits 0-2 are at most 128 in magnitude, so a product is at most
+// 2^14 and the levels 0-2 (the ones whose rounding would show at 1e-12) sum exactly as long as
+// 3 K 2^14 < 2^24; the levels 3-5 weigh 2^-24 and less. The read-back recombines the levels in
+// float-pair arithmetic (Horner in 2^-8 from level 5), scales by 2^(eU + eJ - 14) and adds the
+// FP64 value into V. U itself is formed in float-pair arithmetic from Ahat and Jm as float pairs
+// (the Gauss-point kernel writes Ahat as hi + lo), ~2^-46 relative; the residual is FP64.
+// One tile per work item (the six accumulators of a 32-column tile take 192 tensor-memory
+// columns), reduction chunks of KC columns, the Jm digits built once per CTA for the whole K.
+// ------------------------------------------------------------------------------------------------
+constexpr int OZ_DIG = 6;
+constexpr int OZ_THREADS = 256;
+
+__device__ __forceinline__ void oz_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// six signed digits of the float pair (h, l), |h + l| <= 128: h + l = d0 + d1/256 + ... + d5/256^5
+// up to ~2^-40 (digits 0-2 within [-128, 128], digits 3-5 within [-193, 193])
+__device__ __forceinline__ void oz_digits(float h, float l, float (&d)[OZ_DIG]) {
+    d[0] = rintf(h);
+    float r = h - d[0];  // exact: |r| <= 1/2 and a multiple of ulp(h)
+    d[1] = rintf(r * 256.f);
+    r = r * 256.f - d[1];
+    d[2] = rintf(r * 256.f);
+    r = r * 256.f - d[2];
+    float t, te;
+    oz_two_sum(r * 256.f, l * 16777216.f, t, te);  // the rest of h and all of l, in units of digit 3
+    d[3] = rintf(t);
+    r = t - d[3];
+    d[4] = rintf(r * 256.f);
+    r = r * 256.f - d[4];
+    d[5] = rintf(r * 256.f + te * 256.f);
+}
+
+// U entry sum_l (qh_l + ql_l)(jh_l + jl_l) as a float pair (ql jl dropped, ~2^-48 relative)
+__device__ __forceinline__ void oz_dot3(const float4 &qh, const float4 &ql, const float4 &jh, const float4 &jl,
+                                        float &h, float &l) {
+    const float p0 = qh.x * jh.x, e0 = fmaf(qh.x, jh.x, -p0) + fmaf(qh.x, jl.x, ql.x * jh.x);
+    const float p1 = qh.y * jh.y, e1 = fmaf(qh.y, jh.y, -p1) + fmaf(qh.y, jl.y, ql.y * jh.y);
+    const float p2 = qh.z * jh.z, e2 = fmaf(qh.z, jh.z, -p2) + fmaf(qh.z, jl.z, ql.z * jh.z);
+    float s, es, s2, es2;
+    oz_two_sum(p0, p1, s, es);
+    oz_two_sum(s, p2, s2, es2);
+    const float err = (e0 + e1) + (e2 + es) + es2;
+    oz_two_sum(s2, err, h, l);
+}
+
+// digit planes of 8 values (element t in half t % 2 of word t / 2): 8 x 6 digits -> 6 uint4
+__device__ __forceinline__ void oz_pack8(const float (&d)[8][OZ_DIG], uint4 (&out)[OZ_DIG]) {
+#pragma unroll
+    for (int s = 0; s < OZ_DIG; ++s) {
+        uint32_t w[4];
+#pragma unroll
+        for (int p = 0; p < 4; ++p) {
+            const __nv_bfloat162 b2 = __floats2bfloat162_rn(d[2 * p][s], d[2 * p + 1][s]);
+            w[p] = *reinterpret_cast<const uint32_t *>(&b2);
+        }
+        out[s] = make_uint4(w[0], w[1], w[2], w[3]);
+    }
+}
+
+// digits of U at columns c0 .. c0 + 7 (c = 3 g + d, c0 = 3 g0 + D0, all below K) of row (i, b, k),
+// scaled by su, packed per digit plane: w[s] holds plane s of the 8 values
+template <int NPE, int D0>
+__device__ __forceinline__ void oz_row8(const float4 *Qxh, const float4 *Qxl, const float4 *J4h, const float4 *J4l,
+                                        int g0, int i, int b, int k, float su, uint4 (&w)[OZ_DIG]) {
+    constexpr int NG = (D0 + 7) / 3 + 1;
+    float4 jh[NG], jl[NG];
+#pragma unroll
+    for (int s = 0; s < NG; ++s) {
+        jh[s] = __ldg(J4h + (size_t)(g0 + s) * NPE + b);
+        jl[s] = __ldg(J4l + (size_t)(g0 + s) * NPE + b);
+    }
+    uint32_t pw[OZ_DIG][4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p) {
+        float da[OZ_DIG], db[OZ_DIG];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int t = 2 * p + q, gg = (D0 + t) / 3, dd = (D0 + t) % 3;
+            const int o = (g0 + gg) * 27 + 9 * i + 3 * dd + k;
+            float h, l;
+            oz_dot3(Qxh[o], Qxl[o], jh[gg], jl[gg], h, l);
+            oz_digits(h * su, l * su, q == 0 ? da : db);
+        }
+#pragma unroll
+        for (int s = 0; s < OZ_DIG; ++s) {
+            const __nv_bfloat162 b2 = __floats2bfloat162_rn(da[s], db[s]);
+            pw[s][p] = *reinterpret_cast<const uint32_t *>(&b2);
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < OZ_DIG; ++s) w[s] = make_uint4(pw[s][0], pw[s][1], pw[s][2], pw[s][3]);
+}
+
+// Jm as float4 pairs: J4h/J4l[g][b] = (Jm[0..2][b][g] hi / lo, 0), zero rows for nq <= g < nq + 4
+__global__ void jm_float4_pair(const double *Jm, float4 *J4h, float4 *J4l, int npe, int nq) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (nq + 4) * npe) return;
+    const int g = t / npe, b = t % npe;
+    float hv[3] = {0.f, 0.f, 0.f}, lv[3] = {0.f, 0.f, 0.f};
+    if (g < nq)
+        for (int d = 0; d < 3; ++d) {
+            const double x = Jm[((size_t)d * npe + b) * nq + g];
+            hv[d] = (float)x;
+            lv[d] = (float)(x - (double)hv[d]);
+        }
+    J4h[t] = make_float4(hv[0], hv[1], hv[2], 0.f);
+    J4l[t] = make_float4(lv[0], lv[1], lv[2], 0.f);
+}
+
+// power-of-two exponent e with 2^e > |x| (x >= 0 finite), 0 for x == 0
+__device__ __forceinline__ int oz_exp_above(float x) {
+    if (!(x > 0.f)) return 0;
+    return ((__float_as_int(x) >> 23) & 0xff) - 127 + 1;
+}
+__device__ __forceinline__ float oz_pow2(int e) { return __int_as_float((127 + e) << 23); }  // |e| < 127
+
+// shared memory: Qr double [9][nq] | Qxh, Qxl float4 [nq][27] | A digits 6 x [128][KC] bf16 |
+// B digits 6 x [NB][KB] bf16 (KB = the reduction padded to whole chunks) | nodes, inv, boff | map
+template <int NPE>
+__host__ __device__ inline size_t oz_map_offset(int nq, int kc) {
+    const int kb = (3 * nq + kc - 1) / kc * kc;
+    const size_t b = (sizeof(double) * 9 * (size_t)nq + 15) / 16 * 16 + 2 * sizeof(float4) * 27 * (size_t)nq +
+                     sizeof(__nv_bfloat16) * OZ_DIG * ((size_t)TC_MT * kc + (size_t)tc_nb<NPE>() * kb) +
+                     sizeof(int) * (NPE + 3 * NPE) + sizeof(int16_t) * NPE * NPE;
+    return (b + 15) / 16 * 16;
+}
+template <int NPE>
+__host__ __device__ inline size_t oz_smem_bytes(int nq, int kc, bool stage) {
+    const size_t b = oz_map_offset<NPE>(nq, kc) + (stage ? sizeof(int) * 9 * (size_t)NPE * NPE : 0);
+    return (b + 127) / 128 * 128;
+}
+
+template <int NPE>
+__global__ void __launch_bounds__(OZ_THREADS, 2)
+    contract_oz_kernel(const AsmArgs A, const float4 *__restrict__ J4h, const float4 *__restrict__ J4l, int KC,
+                       int tcols, int stage) {
+    constexpr int NDOF = 3 * NPE, M = 9 * NPE, NB = tc_nb<NPE>(), NT = tc_ntiles<NPE>(), CW = tc_colw<NPE>();
+    constexpr int RPL = tc_rpl<NPE>(), RPL8 = (RPL + 7) / 8 * 8;
+    const int nq = A.nq, K = 3 * nq, KB = (K + KC - 1) / KC * KC;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *Qr = reinterpret_cast<double *>(smem_raw);  // [9][nq]
+    float4 *Qxh = reinterpret_cast<float4 *>(smem_raw + (sizeof(double) * 9 * (size_t)nq + 15) / 16 * 16);
+    float4 *Qxl = Qxh + 27 * nq;
+    __nv_bfloat16 *Ad = reinterpret_cast<__nv_bfloat16 *>(Qxl + 27 * nq);  // plane s at s * 128 * KC
+    __nv_bfloat16 *Bd = Ad + (size_t)OZ_DIG * TC_MT * KC;                   // plane s at s * NB * KB
+    int *nodes = reinterpret_cast<int *>(Bd + (size_t)OZ_DIG * NB * KB);
+    int *inv = nodes + NPE;
+    int16_t *boff = reinterpret_cast<int16_t *>(inv + NDOF);
+    int *dgs = reinterpret_cast<int *>(smem_raw + oz_map_offset<NPE>(nq, KC));
+    __shared__ __align__(8) uint64_t mbar;
+    __shared__ uint32_t taddr_s;
+    __shared__ int s_flag, s_amax[2], s_jmax, s_jsum;
+    __shared__ int64_t s_nnz;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int64_t cap = (int64_t)NDOF * NDOF;
+    const int64_t nwork = A.ne * NT;
+    const bool staged = stage && A.dg;
+    const bool wide = staged && (cap & 3) == 0 && ((uintptr_t)A.dg & 15) == 0;
+    const bool pf = 54 * nq <= OZ_THREADS * TC_PF;
+    int flag = 0;
+    uint32_t phase = 0;
+    if (tid == 0) {
+        s_flag = 0;
+        s_amax[0] = s_amax[1] = 0;
+        s_jmax = s_jsum = 0;
+        s_nnz = (int64_t)A.indptr[3 * A.nnode];
+        tc::mbar_init(&mbar, 1);
+    }
+    if (warp == 0) tc::tmem_alloc(&taddr_s, (uint32_t)tcols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t taddr = taddr_s;
+    const uint32_t idesc = tc::idesc_bf16_f32(TC_MT, NB);
+    const uint32_t sbo_a = (uint32_t)(KC / 8) * 128, sbo_b = (uint32_t)(KB / 8) * 128;
+
+    // Jm scale (element type): max |Jm| and the largest sum over l of |Jm[l][b][g]| (hi parts)
+    for (int idx = tid; idx < nq * NPE; idx += OZ_THREADS) {
+        const float4 j = __ldg(J4h + idx);
+        const float ax = fabsf(j.x), ay = fabsf(j.y), az = fabsf(j.z);
+        atomicMax(&s_jmax, __float_as_int(fmaxf(ax, fmaxf(ay, az))));
+        atomicMax(&s_jsum, __float_as_int(ax + ay + az));
+    }
+    // lanes past RPL8 are zero rows of every A plane, written once
+    for (int idx = tid; idx < TC_MT * (KC / 8); idx += OZ_THREADS) {
+        const int rr = idx % TC_MT, cg = idx / TC_MT;
+        if ((rr & 31) < RPL8) continue;
+        const uint32_t off = tc::kmajor_offset(rr, 8 * cg, KC) / 2;
+#pragma unroll
+        for (int s = 0; s < OZ_DIG; ++s)
+            *reinterpret_cast<uint4 *>(Ad + (size_t)s * TC_MT * KC + off) = make_uint4(0, 0, 0, 0);
+    }
+    __syncthreads();
+    const float jsum = __int_as_float(s_jsum) * (1.f + 1.f / 1048576.f);
+    const int eJ = oz_exp_above(__int_as_float(s_jmax) * (1.f + 1.f / 1048576.f));
+    {  // B digits for the whole reduction: row n = node, column c = 3 g + d
+        const float sj = oz_pow2(7 - eJ);
+        for (int idx = tid; idx < NB * (KB / 8); idx += OZ_THREADS) {
+            const int n = idx % NB, cg = idx / NB;
+            float d[8][OZ_DIG];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int c = 8 * cg + t;
+                float h = 0.f, l = 0.f;
+                if (n < NPE && c < K) {
+                    const float4 jh = __ldg(J4h + (size_t)(c / 3) * NPE + n), jl = __ldg(J4l + (size_t)(c / 3) * NPE + n);
+                    const int dd = c % 3;
+                    h = (dd == 0 ? jh.x : (dd == 1 ? jh.y : jh.z)) * sj;
+                    l = (dd == 0 ? jl.x : (dd == 1 ? jl.y : jl.z)) * sj;
+                }
+                oz_digits(h, l, d[t]);
+            }
+            uint4 w[OZ_DIG];
+            oz_pack8(d, w);
+            const uint32_t off = tc::kmajor_offset(n, 8 * cg, KB) / 2;
+#pragma unroll
+            for (int s = 0; s < OZ_DIG; ++s) *reinterpret_cast<uint4 *>(Bd + (size_t)s * NB * KB + off) = w[s];
+        }
+    }
+    bool ok = true;
+
+    uint64_t pq[TC_PF];  // prefetched Gauss-point values: (lo << 32 | hi) of a tangent entry, or an S double
+    int pslot[TC_PF];
+#pragma unroll
+    for (int j = 0; j < TC_PF; ++j) {
+        const int idx = tid + OZ_THREADS * j;
+        pslot[j] = pf && idx < 54 * nq ? ((idx / nq) << 16) | (idx % nq) : -1;
+    }
+    uint64_t pnode = 0;
+    int pdl = 0;
+    auto load_q = [&](int p, int g, int64_t el) -> uint64_t {
+        const size_t col = (size_t)el * nq + g;
+        if (p < 45)
+            return ((uint64_t)__float_as_uint(A.Qf[(size_t)(45 + p) * A.ldq + col]) << 32) |
+                   (uint64_t)__float_as_uint(A.Qf[(size_t)p * A.ldq + col]);
+        return (uint64_t)__double_as_longlong(A.Q[(size_t)(p - 45) * A.ldq + col]);
+    };
+    auto prefetch = [&](int64_t w) {
+        if (w >= nwork) return;
+        const int64_t el = w / NT, e = A.e0 + el;
+        if (tid < NPE) pnode = A.elements[e * NPE + tid];
+        if (A.dl && tid < NDOF) pdl = A.dl[e * cap + (int64_t)tid * NDOF];
+#pragma unroll
+        for (int j = 0; j < TC_PF; ++j)
+            if (pslot[j] >= 0) pq[j] = load_q(pslot[j] >> 16, pslot[j] & 0xffff, el);
+    };
+    auto put_q = [&](int p, int g, uint64_t bits, int *amax) {
+        if (p >= 45) {
+            Qr[(p - 45) * nq + g] = __longlong_as_double((long long)bits);
+            return;
+        }
+        const float h = __uint_as_float((uint32_t)bits), l = __uint_as_float((uint32_t)(bits >> 32));
+        atomicMax(amax, __float_as_int(fabsf(h)));
+        const int I = c_sym.I[p], Kc = c_sym.K[p];
+        float *qh = reinterpret_cast<float *>(Qxh + (size_t)g * 27), *ql = reinterpret_cast<float *>(Qxl + (size_t)g * 27);
+        qh[(I * 3 + Kc / 3) * 4 + Kc % 3] = h;
+        ql[(I * 3 + Kc / 3) * 4 + Kc % 3] = l;
+        if (Kc != I) {
+            qh[(Kc * 3 + I / 3) * 4 + I % 3] = h;
+            ql[(Kc * 3 + I / 3) * 4 + I % 3] = l;
+        }
+    };
+    prefetch(blockIdx.x);
+
+    int it = 0;
+    for (int64_t w = blockIdx.x; w < nwork && ok; w += gridDim.x, ++it) {
+        const int64_t el = w / NT, e = A.e0 + el;
+        const int t0 = (int)(w % NT);
+        int *amax = &s_amax[it & 1];
+        __syncthreads();  // previous work item done with the shared buffers
+        if (tid == 0) s_amax[(it + 1) & 1] = 0;  // for the next item (read by nobody until then)
+        for (int a = tid; a < NPE; a += OZ_THREADS) {
+            uint64_t nd = a == tid ? pnode : A.elements[e * NPE + a];
+            if (nd >= (uint64_t)A.nnode) {
+                flag |= FL_FLAG_BAD_INDEX;
+                nd = 0;
+            }
+            nodes[a] = (int)nd;
+        }
+        if (A.dl)
+            for (int i = tid; i < NDOF; i += OZ_THREADS) {
+                const int v = i == tid ? pdl : A.dl[e * cap + (int64_t)i * NDOF];
+                const int p = v / NDOF;
+                if (v < 0 || p >= NDOF) flag |= FL_FLAG_BAD_INDEX;
+                else inv[p] = i;
+            }
+        if (pf) {
+#pragma unroll
+            for (int j = 0; j < TC_PF; ++j)
+                if (pslot[j] >= 0) put_q(pslot[j] >> 16, pslot[j] & 0xffff, pq[j], amax);
+        } else {
+            for (int idx = tid; idx < 54 * nq; idx += OZ_THREADS)
+                put_q(idx / nq, idx % nq, load_q(idx / nq, idx % nq, el), amax);
+        }
+        __syncthreads();
+        if (staged) {
+            const int *src = A.dg + e * cap;
+            if (wide)
+                for (int i = 4 * tid; i < cap; i += 4 * OZ_THREADS) cp_async16(dgs + i, src + i);
+            else
+                for (int i = tid; i < cap; i += OZ_THREADS) cp_async4(dgs + i, src + i);
+            cp_async_commit();
+        }
+        prefetch(w + gridDim.x);
+        if (!A.dl)
+            for (int idx = tid; idx < NPE * NPE; idx += OZ_THREADS) {
+                const int off = row_search(A.indptr, A.indices, 3 * nodes[idx / NPE], 3 * nodes[idx % NPE]);
+                boff[idx] = (int16_t)(off >= 0 && off < 32768 ? off : -1);
+            }
+        if (A.update && t0 == 0) {  // residual in FP64, four threads per dof
+            for (int base = 0; base < 4 * NDOF; base += OZ_THREADS) {
+                const int idx = base + tid, r = idx >> 2, part = idx & 3;
+                double t = 0.0;
+                if (r < NDOF) {
+                    const int a = r / 3, i = r % 3;
+                    for (int g = part; g < nq; g += 4) {
+                        t = fma(__ldg(A.Jm + (size_t)a * nq + g), Qr[(i * 3) * nq + g], t);
+                        t = fma(__ldg(A.Jm + ((size_t)NPE + a) * nq + g), Qr[(i * 3 + 1) * nq + g], t);
+                        t = fma(__ldg(A.Jm + ((size_t)2 * NPE + a) * nq + g), Qr[(i * 3 + 2) * nq + g], t);
+                    }
+                }
+                t += __shfl_xor_sync(0xffffffffu, t, 1);
+                t += __shfl_xor_sync(0xffffffffu, t, 2);
+                if (r < NDOF && part == 0) atomicAdd(A.T + 3 * (int64_t)nodes[r / 3] + r % 3, t);
+            }
+        }
+        const int eU = oz_exp_above(__int_as_float(*amax) * jsum);
+        const float su = oz_pow2(7 - eU);
+        for (int k0 = 0; k0 < K; k0 += KC) {
+            const int kc = min(KC, K - k0);
+            // A digits: item = (row rl of the tile, 8-column group cg), rows as in section D
+            constexpr int NRG = 4 * RPL8;
+            for (int idx = tid; idx < NRG * (KC / 8); idx += OZ_THREADS) {
+                const int cg = idx / NRG, rl = idx - cg * NRG, c0 = k0 + 8 * cg;
+                const int q4 = rl / RPL8, l8 = rl - q4 * RPL8, rr = 32 * q4 + l8, r = (4 * t0 + q4) * RPL + l8;
+                const bool live = l8 < RPL && r < M;
+                const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+                uint4 wv[OZ_DIG];
+                if (live && c0 + 8 <= K) {
+                    const int g0 = c0 / 3;
+                    switch (c0 - 3 * g0) {
+                        case 0: oz_row8<NPE, 0>(Qxh, Qxl, J4h, J4l, g0, i, b, k, su, wv); break;
+                        case 1: oz_row8<NPE, 1>(Qxh, Qxl, J4h, J4l, g0, i, b, k, su, wv); break;
+                        default: oz_row8<NPE, 2>(Qxh, Qxl, J4h, J4l, g0, i, b, k, su, wv); break;
+                    }
+                } else {
+                    float d[8][OZ_DIG];
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) {
+                        const int c = c0 + t;
+                        float h = 0.f, l = 0.f;
+                        if (live && c < K) {
+                            const int g = c / 3, dd = c % 3;
+                            oz_dot3(Qxh[(size_t)g * 27 + 9 * i + 3 * dd + k], Qxl[(size_t)g * 27 + 9 * i + 3 * dd + k],
+                                    __ldg(J4h + (size_t)g * NPE + b), __ldg(J4l + (size_t)g * NPE + b), h, l);
+                            h *= su;
+                            l *= su;
+                        }
+                        oz_digits(h, l, d[t]);
+                    }
+                    oz_pack8(d, wv);
+                }
+                const uint32_t off = tc::kmajor_offset(rr, 8 * cg, KC) / 2;
+#pragma unroll
+                for (int s = 0; s < OZ_DIG; ++s) *reinterpret_cast<uint4 *>(Ad + (size_t)s * TC_MT * KC + off) = wv[s];
+            }
+            tc::fence_async_smem();
+            tc::fence_before_sync();
+            __syncthreads();
+            tc::fence_after_sync();
+            if (tid == 0) {
+                // level w = i + j into accumulator w (columns w CW); the first product of a level
+                // overwrites it
+                uint64_t da0[OZ_DIG], db0[OZ_DIG];
+#pragma unroll
+                for (int s = 0; s < OZ_DIG; ++s) {
+                    da0[s] = tc::smem_desc(Ad + (size_t)s * TC_MT * KC, 128, sbo_a);
+                    db0[s] = tc::smem_desc(Bd + (size_t)s * NB * KB, 128, sbo_b);
+                }
+                for (int ks = 0; 16 * ks < kc; ++ks)
+#pragma unroll
+                    for (int lv = 0; lv < OZ_DIG; ++lv)
+#pragma unroll
+                        for (int i = 0; i <= lv; ++i)
+                            tc::mma_bf16(taddr + (uint32_t)(lv * CW), da0[i] + (uint64_t)(16 * ks),
+                                         db0[lv - i] + (uint64_t)(k0 + 16 * ks), idesc, k0 > 0 || ks > 0 || i > 0);
+                tc::mma_commit(&mbar);
+            }
+            if (staged && k0 + KC >= K) cp_async_wait_all();
+            ok = __syncthreads_and(warp == 0 ? tc::mbar_wait(&mbar, phase & 1, TC_WAIT) : true) != 0;
+            ++phase;
+            tc::fence_after_sync();
+            if (!ok) break;
+        }
+        if (!ok) {
+            flag |= FL_FLAG_BAD_INDEX;
+            break;
+        }
+        // read back: 16-column blocks alternating between warps w and w + 4. Levels 5..3 (weights
+        // 2^-40..2^-24) are combined in FP32; levels 2, 1, 0, whose sums are exact integers, join
+        // as float pairs; then the scale and the FP64 add
+        const int sub = warp & 3, half = warp >> 2;
+        constexpr int CB = NB / 16;
+        const float scale = oz_pow2(eU + eJ - 14);
+        const int r = (4 * t0 + sub) * RPL + lane;
+        const bool row_ok = lane < RPL && r < M;
+        const int k = r % 3, b = (r / 3) % NPE, i = r / (3 * NPE);
+        const int ic = A.dl && row_ok ? inv[3 * b + k] : 0;
+        const uint32_t tl = taddr + ((uint32_t)(32 * sub) << 16);
+#pragma unroll
+        for (int u = 0; u < CB; ++u) {
+            if ((u & 1) != half) continue;  // warp-uniform
+            const int c0 = u * 16;
+            constexpr int NV = 16;
+            float hh[NV], ll[NV], v[NV];
+            tc::tmem_ld16(tl + (uint32_t)(5 * CW + c0), v);
+#pragma unroll
+            for (int j = 0; j < NV; ++j) hh[j] = v[j];
+            tc::tmem_ld16(tl + (uint32_t)(4 * CW + c0), v);
+#pragma unroll
+            for (int j = 0; j < NV; ++j) hh[j] = fmaf(hh[j], 1.f / 256.f, v[j]);
+            tc::tmem_ld16(tl + (uint32_t)(3 * CW + c0), v);
+#pragma unroll
+            for (int j = 0; j < NV; ++j) {
+                hh[j] = fmaf(hh[j], 1.f / 256.f, v[j]);
+                ll[j] = 0.f;
+            }
+#pragma unroll 1
+            for (int lv = 2; lv >= 0; --lv) {
+                tc::tmem_ld16(tl + (uint32_t)(lv * CW + c0), v);
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    float sh, e2;
+                    oz_two_sum(v[j], hh[j] * (1.f / 256.f), sh, e2);
+                    ll[j] = fmaf(ll[j], 1.f / 256.f, e2);
+                    hh[j] = sh;
+                }
+            }
+            if (!row_ok) continue;
+            if (A.dl) {
+                int64_t pos[NV];
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    const int a = c0 + j;
+                    pos[j] = -1;
+                    if (a < NPE) {
+                        const int ir = inv[3 * a + i];
+                        if ((unsigned)ir < (unsigned)NDOF && (unsigned)ic < (unsigned)NDOF)
+                            pos[j] = staged ? (int64_t)dgs[ir * NDOF + ic] : (int64_t)A.dg[e * cap + (int64_t)ir * NDOF + ic];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    if (c0 + j >= NPE) continue;
+                    const double vv = (double)(hh[j] * scale) + (double)(ll[j] * scale);
+                    if (pos[j] >= 0 && pos[j] < s_nnz) atomicAdd(A.V + pos[j], vv);
+                    else flag |= FL_FLAG_BAD_INDEX;
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < NV; ++j) {
+                    const int a = c0 + j;
+                    if (a >= NPE) continue;
+                    const double vv = (double)(hh[j] * scale) + (double)(ll[j] * scale);
+                    const int64_t pos = block_entry(A.indptr, A.indices, nodes[a], nodes[b], i, k, boff[a * NPE + b]);
+                    if (pos >= 0 && pos < s_nnz) atomicAdd(A.V + pos, vv);
+                    else flag |= FL_FLAG_BAD_INDEX;
+                }
+            }
+        }
+        tc::fence_before_sync();
+        __syncthreads();
+        tc::fence_after_sync();
+    }
+    cp_async_wait_all();
+    if (!ok) (void)__syncthreads_and(warp == 0 ? tc::mbar_wait(&mbar, (phase - 1) & 1, TC_WAIT) : true);
+    if (flag) atomicOr(&s_flag, flag);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(taddr, (uint32_t)tcols);
+    if (tid == 0 && s_flag && A.flags) atomicOr(A.flags, s_flag);
+}
+
+// Plan of the FP64 tensor-core kernel: one tile per item (6 accumulators of CW columns); the
+// element map staged in shared memory if possible, with the widest reduction chunk (multiple of
+// 16) that leaves room for two CTAs per SM, else for one.
+// Unsupported (0) when the exact levels could overflow FP32 (3 K 2^14 >= 2^24) or nothing fits.
+template <int NPE>
+static TcPlan oz_plan(int nq) {
+    constexpr int CW = tc_colw<NPE>();
+    if (3 * 3 * nq * 16384.0 >= 16777216.0 || OZ_DIG * CW > 512) return TcPlan{0, 0, 0, 0, 0};
+    const int kmax = std::min(MX_KC, (3 * nq + 15) / 16 * 16);
+    const size_t limit[2] = {113 * 1024, 227 * 1024};
+    int cols = 32;
+    while (cols < OZ_DIG * CW) cols *= 2;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int stage = 1; stage >= 0; --stage)  // the staged map first (the scatter's latency)
+            for (int kc = kmax; kc >= 16; kc -= 16) {
+                const size_t s = oz_smem_bytes<NPE>(nq, kc, stage != 0);
+                if (s <= limit[pass]) return TcPlan{kc, 1, cols, s, stage};
+            }
+    return TcPlan{0, 0, 0, 0, 0};
+}
+
+template <int NPE>
+static bool oz_supported(int nq) { return oz_plan<NPE>(nq).tg > 0; }
+
+template <int NPE, int MAT>
+static int launch_oz(AsmArgs A, cudaStream_t stream) {
+    if (A.nelem == 0) return FL_OK;
+    const TcPlan P = oz_plan<NPE>(A.nq);
+    if (P.tg == 0) return FL_ERR_UNSUPPORTED;
+    { const int st = ensure_smem<contract_oz_kernel<NPE>>(P.smem); if (st != FL_OK) return st; }
+    // Gauss-point scratch per chunk: S [9][ldq] FP64, the tangent as float pairs [90][ldq]
+    // (288 bytes per point), then the float4 pair tables of Jm
+    int64_t chunk = std::max<int64_t>(1, (int64_t)(CHUNK_BYTES / ((9 * sizeof(double) + 90 * sizeof(float)) * (size_t)A.nq)));
+    if (chunk > A.nelem) chunk = A.nelem;
+    const size_t sbytes = (sizeof(double) * 9 * (size_t)A.nq * chunk + 255) & ~(size_t)255;
+    const size_t fbytes = (sizeof(float) * 90 * (size_t)A.nq * chunk + 255) & ~(size_t)255;
+    const int64_t nj4 = (int64_t)(A.nq + 4) * NPE;
+    const size_t jbytes = (sizeof(float4) * (size_t)nj4 + 255) & ~(size_t)255;
+    double *Q = nullptr;
+    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sbytes + fbytes + 2 * jbytes, stream));
+    A.Q = Q;
+    A.Qf = reinterpret_cast<float *>(reinterpret_cast<char *>(Q) + sbytes);
+    A.ldq = chunk * A.nq;
+    float4 *J4h = reinterpret_cast<float4 *>(reinterpret_cast<char *>(Q) + sbytes + fbytes);
+    float4 *J4l = reinterpret_cast<float4 *>(reinterpret_cast<char *>(J4h) + jbytes);
+    jm_float4_pair<<<(unsigned)((nj4 + 255) / 256), 256, 0, stream>>>(A.Jm, J4h, J4l, NPE, A.nq);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int occ = tc_ctas_per_sm(reinterpret_cast<const void *>(contract_oz_kernel<NPE>), P);
+    for (int64_t e0 = 0; e0 < A.nelem; e0 += chunk) {
+        A.e0 = e0;
+        A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
+        const int64_t nqp = A.ne * A.nq;
+        qp_kernel<NPE, MAT, QOUT_PAIR><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        const int64_t grid = std::min<int64_t>(A.ne * tc_ntiles<NPE>(), (int64_t)sms * occ);
+        contract_oz_kernel<NPE><<<(unsigned)grid, OZ_THREADS, P.smem, stream>>>(A, J4h, J4l, P.kc, P.tcols, P.stage);
     }
     const int st = launch_status();
     const cudaError_t fe = cudaFreeAsync(Q, stream);
@@ -1355,7 +1952,8 @@ int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const
 }
 
 int fl_SetAssemblyArithmetic(int arithmetic) {
-    if (arithmetic != FL_ARITH_FP64 && arithmetic != FL_ARITH_FLOAT_PAIR) return FL_ERR_ARG;
+    if (arithmetic != FL_ARITH_FP64 && arithmetic != FL_ARITH_FLOAT_PAIR && arithmetic != FL_ARITH_TENSOR)
+        return FL_ERR_ARG;
     fl::g_arith.store(arithmetic);
     return FL_OK;
 }

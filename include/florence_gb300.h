@@ -192,6 +192,13 @@ int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
  * in both. FL_ERR_ARG for other values. */
 #define FL_ARITH_FP64 0
 #define FL_ARITH_FLOAT_PAIR 1
+/* FL_ARITH_TENSOR: the contraction on the tensor cores with both operands scaled and split into
+ * six signed 8-bit digits held exactly in BF16, digit products summed per weight level in FP32
+ * (the three leading levels exactly), recombined as float pairs and added in FP64: element
+ * matrices within ~1e-13 of FP64. Applies to CSR outputs (maps or squeeze) without a
+ * caller-provided scratch, for element types whose reduction fits (3 * 3 * ngauss * 2^14 < 2^24);
+ * other calls use the float-pair contraction. */
+#define FL_ARITH_TENSOR 2
 int fl_SetAssemblyArithmetic(int arithmetic);
 int fl_GetAssemblyArithmetic(void);
 

@@ -102,6 +102,25 @@ def test_both_contraction_arithmetics_match_reference(fl, case, mode):
         assert rel_fro(V.cpu().numpy(), d["K_data"]) < TOL
 
 
+@pytest.mark.parametrize("case", golden_cases())
+@pytest.mark.parametrize("mode", ["csr", "squeeze"])
+def test_tensor_core_fp64_tangent_matches_reference(fl, case, mode):
+    """The contraction on the tensor cores (operands split into six exact BF16 digits, the three
+    leading digit levels summed exactly in FP32) meets the FP64 bar against the reference in both
+    CSR scatter modes; element types whose reduction does not fit fall back to float pairs and
+    meet it too."""
+    d = load_golden(case)
+    asm = _asm(fl, d, mode)
+    x = torch.from_numpy(d["Eulerx"]).cuda()
+    with fl.arithmetic("tensor"):
+        assert fl.get_arithmetic() == "tensor"
+        V, T = asm.assemble(x)
+        asm.check_flags()
+    assert fl.get_arithmetic() == "float_pair"
+    assert rel_fro(V.cpu().numpy(), d["K_data"]) < TOL
+    assert rel_fro(T.cpu().numpy(), d["T"]) < TOL
+
+
 def _padded_csr(indptr, indices, every=3, phase=1):
     """The CSR pattern with one extra column in every `every`-th row (the smallest column absent
     from the row): the rows of a node no longer share a column pattern. Returns the padded
