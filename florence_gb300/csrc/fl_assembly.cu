@@ -105,6 +105,45 @@ __host__ __device__ __forceinline__ constexpr int sym9(int I, int K) {
 // ------------------------------------------------------------------------------------------------
 // A. Gauss-point data
 // ------------------------------------------------------------------------------------------------
+// Float-pair number hi + lo (|lo| <= ulp(hi) / 2) with FP32-pipe arithmetic: products error-free
+// in their leading part (fma), sums by Knuth's two-sum, ~2^-46 relative per operation. Used for
+// the Gauss-point tangent of the FP64 path, whose FP64 form would hold GB300's FP64 pipe.
+namespace fpair {  // its own namespace: the overloads are found by argument lookup only, so they
+                  // do not hide the FP64 fma of namespace fl's callers
+struct FloatPair {
+    float h, l;
+    FloatPair() = default;
+    __device__ constexpr FloatPair(float h_, float l_) : h(h_), l(l_) {}
+    __device__ explicit FloatPair(double x) : h((float)x), l((float)(x - (double)(float)x)) {}
+    __device__ explicit FloatPair(int x) : h((float)x), l(0.f) {}
+};
+__device__ __forceinline__ FloatPair df_renorm(float s, float e) {
+    const float h = s + e;
+    return FloatPair(h, e - (h - s));
+}
+__device__ __forceinline__ FloatPair operator+(FloatPair a, FloatPair b) {
+    const float s = a.h + b.h, bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb) + (a.l + b.l);
+    return df_renorm(s, e);
+}
+__device__ __forceinline__ FloatPair operator-(FloatPair a) { return FloatPair(-a.h, -a.l); }
+__device__ __forceinline__ FloatPair operator-(FloatPair a, FloatPair b) { return a + (-b); }
+__device__ __forceinline__ FloatPair &operator+=(FloatPair &a, FloatPair b) { return a = a + b; }
+__device__ __forceinline__ FloatPair operator*(FloatPair a, FloatPair b) {
+    const float p = a.h * b.h;
+    const float e = fmaf(a.h, b.h, -p) + fmaf(a.h, b.l, a.l * b.h);
+    return df_renorm(p, e);
+}
+__device__ __forceinline__ FloatPair fma(FloatPair a, FloatPair b, FloatPair c) {  // a b + c
+    const float p = a.h * b.h;
+    const float pe = fmaf(a.h, b.h, -p) + fmaf(a.h, b.l, a.l * b.h);
+    const float s = p + c.h, bb = s - p;
+    const float e = (p - (s - bb)) + (c.h - bb) + (pe + c.l);
+    return df_renorm(s, e);
+}
+}  // namespace fpair
+using fpair::FloatPair;
+
 // Pulled-back tangent of one Gauss point in arithmetic T from the FP64 kinematics and material:
 // Ahat[(i,d),(k,e)] = detJ [ d_ik (c1 GG + GsG)[d][e] + c1 G[k][d] G[i][e] + c2 G[i][d] G[k][e]
 //                          + cbb (2 bG[i][d] bG[k][e] - b_ik GbG[d][e] - bG[k][d] bG[i][e]) ] (+ the
@@ -173,7 +212,7 @@ __device__ __forceinline__ void pulled_back_tangent(const double *Gd, const doub
         }
 }
 
-// Gauss-point tangent writers: FP64, FP32, or an FP64 value as the float pair hi + lo
+// Gauss-point tangent writers: FP64, FP32, or a float pair hi + lo
 struct QOutF64 {
     double *q;
     int64_t ld;
@@ -184,22 +223,23 @@ struct QOutF32 {
     int64_t ld;
     __device__ void put(int p, float v) const { q[p * ld] = v; }
 };
-struct QOutPair {
+struct QOutDF {
     float *h, *l;
     int64_t ld;
-    __device__ void put(int p, double v) const {
-        const float hi = (float)v;
-        h[p * ld] = hi;
-        l[p * ld] = (float)(v - (double)hi);
+    __device__ void put(int p, FloatPair v) const {
+        h[p * ld] = v.h;
+        l[p * ld] = v.l;
     }
 };
 
 // Gauss-point output layout: FP64 [54][ldq] in Q; FP32 tangent [45][ldq] in Qf with S [9][ldq]
-// in Q; float-pair tangent (hi [45][ldq] then lo [45][ldq]) in Qf with S [9][ldq] in Q
-enum { QOUT_F64 = 0, QOUT_F32 = 1, QOUT_PAIR = 2 };
+// in Q; the tangent formed in float-pair arithmetic (hi [45][ldq] then lo [45][ldq]) in Qf with
+// S [9][ldq] in Q
+enum { QOUT_F64 = 0, QOUT_F32 = 1, QOUT_DF = 2 };
 
-// QOUT: layout of the Gauss-point data (QOUT_F64, QOUT_F32 for the split-BF16 Jacobian,
-// QOUT_PAIR for the FP64 tangent on the tensor cores); S is FP64 in every layout
+// QOUT: layout of the Gauss-point data (QOUT_F64 for the FP64 contraction, QOUT_F32 for the
+// split-BF16 Jacobian, QOUT_DF for the float-pair and tensor-core contractions); the kinematics,
+// the material law and S are FP64 in every layout
 template <int NPE, int MAT, int QOUT = QOUT_F64>
 __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
     const int64_t t = (int64_t)blockIdx.x * QP_THREADS + threadIdx.x;
@@ -239,8 +279,8 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
                     detJ * fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
         if constexpr (QOUT == QOUT_F32)
             pulled_back_tangent<float, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF32{A.Qf + t, ld});
-        else if constexpr (QOUT == QOUT_PAIR)
-            pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutPair{A.Qf + t, A.Qf + 45 * ld + t, ld});
+        else if constexpr (QOUT == QOUT_DF)
+            pulled_back_tangent<FloatPair, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutDF{A.Qf + t, A.Qf + 45 * ld + t, ld});
         else
             pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF64{q, ld});
     }
@@ -361,6 +401,17 @@ __global__ void __launch_bounds__(AsmCfg<NPE>::TPE * AsmCfg<NPE>::EPC, DF ? AsmC
         // Ss[slot][g][k] (FP64)
         for (int idx = lt; idx < nq * QSTRIDE; idx += TPE) {
             const int k = idx / nq, g = idx % nq;
+            if constexpr (DF) {
+                if (A.Qf) {  // the Gauss-point kernel wrote the tangent as float pairs
+                    const size_t col = (size_t)el * nq + g;
+                    if (k < QSM)
+                        Qs[((size_t)slot * nq + g) * QSM + k] =
+                            make_float2(A.Qf[(size_t)k * A.ldq + col], A.Qf[(size_t)(QSM + k) * A.ldq + col]);
+                    else
+                        Ss[((size_t)slot * nq + g) * 9 + (k - QSM)] = A.Q[(size_t)(k - QSM) * A.ldq + col];
+                    continue;
+                }
+            }
             const double v = qg[k * A.ldq + g];
             if (k < QSM) Qs[((size_t)slot * nq + g) * QSM + k] = AR::split(v);
             else Ss[((size_t)slot * nq + g) * 9 + (k - QSM)] = v;
@@ -550,11 +601,17 @@ static int run_chunks_t(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream
     { const int st = ensure_smem<contract_kernel<NPE, DF>>(smem); if (st != FL_OK) return st; }
     A.Q = Q;
     A.ldq = chunk * A.nq;
+    // float pairs: the Gauss-point kernel forms the tangent in float-pair arithmetic and writes it
+    // as hi [45][ldq] + lo [45][ldq] after S [9][ldq] (the same 432 bytes per Gauss point)
+    A.Qf = DF ? reinterpret_cast<float *>(Q + (size_t)9 * A.ldq) : nullptr;
     for (int64_t e0 = 0; e0 < A.nelem; e0 += chunk) {
         A.e0 = e0;
         A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
         const int64_t nqp = A.ne * A.nq;
-        qp_kernel<NPE, MAT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        if (DF)
+            qp_kernel<NPE, MAT, QOUT_DF><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        else
+            qp_kernel<NPE, MAT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
         contract_kernel<NPE, DF><<<(unsigned)((A.ne + EPC - 1) / EPC), NT, smem, stream>>>(A);
     }
     return launch_status();
@@ -1805,7 +1862,7 @@ static int launch_oz(AsmArgs A, cudaStream_t stream) {
         A.e0 = e0;
         A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
         const int64_t nqp = A.ne * A.nq;
-        qp_kernel<NPE, MAT, QOUT_PAIR><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+        qp_kernel<NPE, MAT, QOUT_DF><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
         const int64_t grid = std::min<int64_t>(A.ne * tc_ntiles<NPE>(), (int64_t)sms * occ);
         contract_oz_kernel<NPE><<<(unsigned)grid, OZ_THREADS, P.smem, stream>>>(A, J4h, J4l, P.kc, P.tcols, P.stage);
     }
