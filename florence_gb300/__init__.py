@@ -7,7 +7,8 @@ The CUDA library (libflorence_gb300.so, built in-tree) is required: nothing here
 the CPU.
 """
 from . import _native
-from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssemblyDF__LinearElastic_,
+from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_,
+                       _LowLevelAssemblyDF__LinearElastic_,
                        _LowLevelAssemblyDF__MooneyRivlin_, _LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_,
                        _LowLevelAssemblyDF__NeoHookean_, _LowLevelAssemblyExplicit_DF_DPF_,
                        __TotalConstantMassIntegrand__, arithmetic, device_sparsity, fp32_peak_gflops, fp64_peak_gflops,
@@ -15,6 +16,7 @@ from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssembl
                        set_tensor_core_tiling)
 
 __all__ = ["ComputeSparsityPattern", "DeviceAssembler", "_LowLevelAssemblyDF__NeoHookean_",
+           "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",
            "_LowLevelAssemblyDF__LinearElastic_", "_LowLevelAssemblyExplicit_DF_DPF_",
            "__TotalConstantMassIntegrand__", "arithmetic", "device_sparsity", "fp32_peak_gflops", "fp64_peak_gflops", "get_arithmetic",

@@ -21,6 +21,7 @@ FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
 FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN = 3
 FL_MATERIAL_LINEARELASTIC = 10
+FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1 = 11
 FL_ARITH_FP64 = 0
 FL_ARITH_FLOAT_PAIR = 1
 FL_ARITH_TENSOR = 2
@@ -63,7 +64,8 @@ def lib():
         L.fl_ComputeSparsityPattern.argtypes = [P, I64, I64, I64, I64, P, P, I64, ctypes.POINTER(I64), P, P, P,
                                                 ctypes.c_size_t, P]
         for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
-                     "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_"):
+                     "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
+                     "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_"):
             getattr(L, name).argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_noalloc.argtypes = [INT] + _DF_ARGS
         L.fl_GlobalAssemblyDF_Batched.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, P, P,
@@ -73,7 +75,7 @@ def lib():
         L.fl_GetAssemblyArithmetic.argtypes = []
         L.fl_SetTensorCoreTiling.argtypes = [INT, INT]
         L.fl_GlobalAssemblyDF_Mixed.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, D, D, D,
-                                                D, P, P, P]
+                                                D, D, P, P, P, P]
         L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
                                                         D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
         L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
@@ -109,7 +111,7 @@ def check(status, what=""):
 EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_ComputeSparsityPattern",
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
            "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
-           "fl_GlobalAssemblyDF_noalloc",
+           "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_", "fl_GlobalAssemblyDF_noalloc",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak", "fl_TensorCoreSelfTest",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",

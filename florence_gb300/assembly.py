@@ -31,27 +31,35 @@ import torch
 from . import _native as N
 
 __all__ = ["DeviceAssembler", "ComputeSparsityPattern", "_LowLevelAssemblyDF__NeoHookean_",
+           "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
            "__TotalConstantMassIntegrand__", "install", "material_params", "fp64_peak_gflops",
            "release_host_buffers"]
 
 MATERIALS = {"NeoHookean": N.FL_MATERIAL_NEOHOOKEAN, "MooneyRivlin": N.FL_MATERIAL_MOONEYRIVLIN,
              "NearlyIncompressibleMooneyRivlin": N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
-             "LinearElastic": N.FL_MATERIAL_LINEARELASTIC}
+             "LinearElastic": N.FL_MATERIAL_LINEARELASTIC,
+             "AnisotropicMooneyRivlin_1": N.FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1}
+# the reference's explicit dispatcher has no transversely isotropic material
+# (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-109)
+EXPLICIT_MATERIALS = {k: v for k, v in MATERIALS.items() if k != "AnisotropicMooneyRivlin_1"}
 _DF_ENTRY = {N.FL_MATERIAL_NEOHOOKEAN: "fl_GlobalAssemblyDF__NeoHookean_",
              N.FL_MATERIAL_MOONEYRIVLIN: "fl_GlobalAssemblyDF__MooneyRivlin_",
              N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN: "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_",
-             N.FL_MATERIAL_LINEARELASTIC: "fl_GlobalAssemblyDF__LinearElastic_"}
+             N.FL_MATERIAL_LINEARELASTIC: "fl_GlobalAssemblyDF__LinearElastic_",
+             N.FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1: "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_"}
 
 
 def _abi_params(mat_id, params):
-    """(mu, mu1, mu2, lamb) of the reference's argument list for kernel parameters (p0, p1, p2):
-    neo-Hookean and linear elastic (mu, lamb); Mooney-Rivlin (mu1, mu2, lamb); nearly
-    incompressible Mooney-Rivlin (alpha, beta, kappa) passed as (mu1, mu2, lamb)."""
-    p0, p1, p2 = params
+    """(mu, mu1, mu2, lamb, mu3) of the reference's argument list for kernel parameters
+    (p0, p1, p2[, p3]): neo-Hookean and linear elastic (mu, lamb); Mooney-Rivlin (mu1, mu2, lamb);
+    nearly incompressible Mooney-Rivlin (alpha, beta, kappa) passed as (mu1, mu2, lamb); the
+    transversely isotropic Mooney-Rivlin (mu1, mu2, lamb, mu3)."""
+    p0, p1, p2 = params[:3]
+    p3 = params[3] if len(params) > 3 else 0.0
     if mat_id in (N.FL_MATERIAL_NEOHOOKEAN, N.FL_MATERIAL_LINEARELASTIC):
-        return p0, 0.0, 0.0, p1
-    return 0.0, p0, p1, p2
+        return p0, 0.0, 0.0, p1, 0.0
+    return 0.0, p0, p1, p2, p3
 
 
 class NonPositiveJacobianWarning(RuntimeWarning):
@@ -143,6 +151,9 @@ def material_params(material, name=None, explicit=False):
         # the low-level path constructs the material from (mu1, mu2, lamb) (AOT_Assembler.py:68-69, 110-111)
         return (N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
                 (float(material.mu1), float(material.mu2), float(material.lamb)))
+    if name == "AnisotropicMooneyRivlin_1" and not explicit:  # AOT_Assembler.py:72-75, 113-114
+        return (N.FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1,
+                (float(material.mu1), float(material.mu2), float(material.lamb), float(material.mu3)))
     raise NotImplementedError("Turning optimise option on for {} material is not supported yet. "
                               "Consider 'optimise=False' for now".format(name))
 
@@ -187,13 +198,15 @@ class DeviceAssembler:
     """Mesh + function space + material resident on the GPU; assembles from device coordinates.
 
     points [N,3] f64, elements [E,npe] (any integer dtype), Jm [3,npe,nq], AllGauss [nq] or [nq,1],
-    material: 'NeoHookean' (mu, lamb) or 'MooneyRivlin' (mu1, mu2, lamb).
+    material: 'NeoHookean' (mu, lamb), 'MooneyRivlin' (mu1, mu2, lamb), 'LinearElastic' (mu, lamb),
+    'NearlyIncompressibleMooneyRivlin' (alpha, beta, kappa) or 'AnisotropicMooneyRivlin_1'
+    (mu1, mu2, lamb, mu3, with `orientations` [E,3], one fibre direction per element).
     mode: 'csr' (the reference's element-to-nonzero maps), 'squeeze' (binary search in each row)
     or 'triplet' (I, J, V per element entry).
     """
 
     def __init__(self, points, elements, Jm, AllGauss, material, params, mode="csr", device="cuda",
-                 requires_geometry_update=1, Bases=None, sparsity=None):
+                 requires_geometry_update=1, Bases=None, sparsity=None, orientations=None):
         self.device = torch.device(device)
         self.points = _to_dev(points, torch.float64, self.device)
         self.elements = _to_dev(elements, torch.int64, self.device)
@@ -207,6 +220,15 @@ class DeviceAssembler:
         self.ndof = 3 * self.npe
         self.material = material
         self.mat_id = MATERIALS[material]
+        self.orient = None
+        if self.mat_id == N.FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1:
+            if orientations is None:
+                raise ValueError("AnisotropicMooneyRivlin_1 needs the fibre direction of every element (orientations)")
+            self.orient = _to_dev(np.asarray(orientations, np.float64).reshape(-1, 3)
+                                  if not isinstance(orientations, torch.Tensor) else orientations.reshape(-1, 3),
+                                  torch.float64, self.device)
+            if self.orient.shape[0] != self.elements.shape[0]:
+                raise ValueError("orientations must hold one direction per element")
         self.params = tuple(float(p) for p in params) + (0.0,) * (3 - len(params))
         self.mode = mode
         self.update = int(requires_geometry_update)
@@ -241,12 +263,13 @@ class DeviceAssembler:
             V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
             Ip, Jp, dl, dg = self.indptr, self.indices, self.data_local, self.data_global
         fn = getattr(L, _DF_ENTRY[self.mat_id])
-        mu, mu1, mu2, lamb = _abi_params(self.mat_id, self.params)
+        mu, mu1, mu2, lamb, mu3 = _abi_params(self.mat_id, self.params)
         st = fn(_ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
                 3, 3, self.nq, self.nelem, self.npe, self.nnode, 6, self.update, None, None,
                 _ptr(Ip), _ptr(Jp), _ptr(V), _ptr(T), 1 if self.mode == "triplet" else 0,
                 1 if self.mode == "squeeze" else 0, _ptr(dl), _ptr(dg), None, None,
-                1.0, mu, mu1, mu2, 0.0, 0.0, lamb, 0.0, 0.0, 0.0, 0.0, None, _ptr(self.flags), stream or _stream())
+                1.0, mu, mu1, mu2, mu3, 0.0, lamb, 0.0, 0.0, 0.0, 0.0, _ptr(self.orient), _ptr(self.flags),
+                stream or _stream())
         N.check(st, "fl_GlobalAssemblyDF")
         if self.mode == "triplet":
             return I, J, V, T
@@ -263,12 +286,12 @@ class DeviceAssembler:
             V32 = torch.zeros(self.nnz, dtype=torch.float32, device=self.device)
         if T is None:
             T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
-        mu, mu1, mu2, lamb = _abi_params(self.mat_id, self.params)
+        mu, mu1, mu2, lamb, mu3 = _abi_params(self.mat_id, self.params)
         st = L.fl_GlobalAssemblyDF_Mixed(self.mat_id, _ptr(self.points), _ptr(self.elements), _ptr(x), _ptr(self.Jm),
                                          _ptr(self.w), self.nq, self.nelem, self.npe, self.nnode, self.update,
                                          _ptr(self.indptr), _ptr(self.indices), _ptr(self.data_local),
-                                         _ptr(self.data_global), _ptr(V32), _ptr(T), mu, mu1, mu2, lamb, None,
-                                         _ptr(self.flags), stream or _stream())
+                                         _ptr(self.data_global), _ptr(V32), _ptr(T), mu, mu1, mu2, lamb, mu3,
+                                         _ptr(self.orient), None, _ptr(self.flags), stream or _stream())
         N.check(st, "fl_GlobalAssemblyDF_Mixed")
         return V32, T
 
@@ -278,7 +301,10 @@ class DeviceAssembler:
         x = Eulerx if Eulerx.is_contiguous() else Eulerx.contiguous()
         if T is None:
             T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
-        mu, mu1, mu2, lamb = _abi_params(self.mat_id, self.params)
+        if self.mat_id not in EXPLICIT_MATERIALS.values():
+            raise NotImplementedError("the explicit internal force has no transversely isotropic material "
+                                      "(as in the reference's explicit dispatcher)")
+        mu, mu1, mu2, lamb, _ = _abi_params(self.mat_id, self.params)
         # the explicit entry takes the nearly incompressible material's (alpha, beta, kappa) as
         # (mu1, mu2, mu3) (_LowLevelAssemblyExplicit_DF_DPF_.pyx:82-84)
         mu3 = self.params[2] if self.mat_id == N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN else 0.0
@@ -340,8 +366,11 @@ def _low_level_df(name, fem_solver, function_space, formulation, mesh, material,
     sparsity = None
     if not recompute:
         sparsity = (fem_solver.indices, fem_solver.indptr, None, None)
+    orient = getattr(material, "anisotropic_orientations", None) if mat_id == N.FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1 \
+        else None
     asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, name, params,
-                          mode=mode, requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity)
+                          mode=mode, requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity,
+                          orientations=orient)
     x = _to_dev(Eulerx, torch.float64, asm.device)
     out = asm.assemble(x)
     host = [_HOST.to_host(t) for t in out]
@@ -371,13 +400,22 @@ def _LowLevelAssemblyDF__LinearElastic_(fem_solver, function_space, formulation,
     return _low_level_df("LinearElastic", fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp)
 
 
+def _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_(fem_solver, function_space, formulation, mesh, material, Eulerx,
+                                                     Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDF_.pyx:53-160 as
+    AOT_Assembler.py builds it for _AnisotropicMooneyRivlin_1_ (mu1, mu2, mu3, lamb and the
+    material's anisotropic_orientations, one fibre direction per element)."""
+    return _low_level_df("AnisotropicMooneyRivlin_1", fem_solver, function_space, formulation, mesh, material, Eulerx,
+                         Eulerp)
+
+
 def _LowLevelAssemblyExplicit_DF_DPF_(function_space, formulation, mesh, material, Eulerx, Eulerp):
     """Internal force T [nnode*nvar] -- _LowLevelAssemblyExplicit_DF_DPF_.pyx:44-152 (mechanics)."""
     if formulation.fields != "mechanics":
         raise NotImplementedError("the GB300 explicit assembly covers the displacement formulation")
     _check_formulation(formulation, material)
     name = getattr(material, "mtype", type(material).__name__)
-    if name not in MATERIALS:
+    if name not in EXPLICIT_MATERIALS:
         raise NotImplementedError("Low level assembly for material {} not available for explicit analysis."
                                   " Consider 'optimise=False' for now".format(name))
     _, params = material_params(material, name, explicit=True)
@@ -422,6 +460,7 @@ def install(florence):
     ll._LowLevelAssemblyDF__MooneyRivlin_ = _LowLevelAssemblyDF__MooneyRivlin_
     ll._LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_ = _LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_
     ll._LowLevelAssemblyDF__LinearElastic_ = _LowLevelAssemblyDF__LinearElastic_
+    ll._LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_ = _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_
     ll._LowLevelAssemblyExplicit_DF_DPF_ = _LowLevelAssemblyExplicit_DF_DPF_
     ll.has_low_level_dispatcher = True
     try:

@@ -62,7 +62,7 @@ class BatchedAssembler:
             st = L.fl_GlobalAssemblyDF_Mixed(self.mat_id, _ptr(self.points), _ptr(self.elements), _ptr(self.x),
                                              _ptr(self.Jm), _ptr(self.w), self.nq, self.nelem, self.npe, self.nnode, 1,
                                              _ptr(self.indptr), _ptr(self.indices), _ptr(self.dl), _ptr(self.dg),
-                                             _ptr(V), _ptr(T), 0.0, 0.0, 0.0, 0.0, _ptr(self.eparams),
+                                             _ptr(V), _ptr(T), 0.0, 0.0, 0.0, 0.0, 0.0, None, _ptr(self.eparams),
                                              _ptr(self.flags), stream or _stream())
             N.check(st, "fl_GlobalAssemblyDF_Mixed")
         else:

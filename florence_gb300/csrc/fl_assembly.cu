@@ -64,6 +64,7 @@ struct AsmArgs {
     const int32_t *indptr, *indices, *dl, *dg;
     MatParams mp;
     const double *eparams;  // optional per-element material parameters [nelem][3] (overrides mp)
+    const double *orient;   // fibre direction per element [nelem][3] (transversely isotropic material)
     int *flags;
     double *Q;       // scratch [QSTRIDE][ldq]
     float *Qf;       // split-BF16 path: FP32 tangent part [45][ldq] (Q then holds S [9][ldq])
@@ -154,6 +155,8 @@ __device__ __forceinline__ void pulled_back_tangent(const double *Gd, const doub
                                                     const ExtraTangent &exd, double c1d, double c2d, double cbbd,
                                                     double detJd, const OUT &out) {
     constexpr bool NIMR = MAT == NEARLYINCOMPRESSIBLEMR;
+    constexpr bool BB = MAT == MOONEYRIVLIN || MAT == ANISOTROPICMR1;    // the cbb (b b) terms
+    constexpr bool GT = NIMR || MAT == ANISOTROPICMR1;                    // the g terms (kgI, kg4)
     T G[9], sig[6], b[6], g6[6];
 #pragma unroll
     for (int i = 0; i < 9; ++i) G[i] = (T)Gd[i];
@@ -172,9 +175,9 @@ __device__ __forceinline__ void pulled_back_tangent(const double *Gd, const doub
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             sG[i * 3 + d] = fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
-            if (MAT == MOONEYRIVLIN || NIMR)
+            if (BB || NIMR)
                 bG[i * 3 + d] = fma(b[s6(i, 0)], G[0 * 3 + d], fma(b[s6(i, 1)], G[1 * 3 + d], b[s6(i, 2)] * G[2 * 3 + d]));
-            if (NIMR)
+            if (GT)
                 gG[i * 3 + d] = fma(g6[s6(i, 0)], G[0 * 3 + d], fma(g6[s6(i, 1)], G[1 * 3 + d], g6[s6(i, 2)] * G[2 * 3 + d]));
         }
 #pragma unroll
@@ -185,8 +188,8 @@ __device__ __forceinline__ void pulled_back_tangent(const double *Gd, const doub
             // no geometric stiffness for the linear elastic material (the reference builds that
             // assembler without it, AOT_Assembler.py:74-81)
             GsG[d * 3 + e2] = MAT == LINEARELASTIC ? (T)0 : fma(G[d], sG[e2], fma(G[3 + d], sG[3 + e2], G[6 + d] * sG[6 + e2]));
-            if (MAT == MOONEYRIVLIN) GbG[d * 3 + e2] = fma(G[d], bG[e2], fma(G[3 + d], bG[3 + e2], G[6 + d] * bG[6 + e2]));
-            if (NIMR) GgG[d * 3 + e2] = fma(G[d], gG[e2], fma(G[3 + d], gG[3 + e2], G[6 + d] * gG[6 + e2]));
+            if (BB) GbG[d * 3 + e2] = fma(G[d], bG[e2], fma(G[3 + d], bG[3 + e2], G[6 + d] * bG[6 + e2]));
+            if (GT) GgG[d * 3 + e2] = fma(G[d], gG[e2], fma(G[3 + d], gG[3 + e2], G[6 + d] * gG[6 + e2]));
         }
 #pragma unroll
     for (int I = 0; I < 9; ++I)
@@ -196,14 +199,14 @@ __device__ __forceinline__ void pulled_back_tangent(const double *Gd, const doub
             const int dd = d < e2 ? d : e2, ee = d < e2 ? e2 : d;
             T v = fma(c1 * G[k * 3 + d], G[i * 3 + e2], c2 * G[i * 3 + d] * G[k * 3 + e2]);
             if (i == k) v = fma(c1, GG[dd * 3 + ee], v + GsG[dd * 3 + ee]);
-            if (MAT == MOONEYRIVLIN)
+            if (BB)
                 v = fma(cbb, fma((T)2 * bG[i * 3 + d], bG[k * 3 + e2], -fma(b[s6(i, k)], GbG[dd * 3 + ee], bG[k * 3 + d] * bG[i * 3 + e2])), v);
-            if (NIMR) {
+            if (GT) {
                 // kbI (bG_id G_ke + G_id bG_ke) + kgI (gG_id G_ke + G_id gG_ke) + kgg gG_id gG_ke
                 // + kg4 (g_ik GG_de + gG_ie G_kd + gG_kd G_ie + d_ik GgG_de)
-                v = fma(kbI, fma(bG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * bG[k * 3 + e2]), v);
+                if (NIMR) v = fma(kbI, fma(bG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * bG[k * 3 + e2]), v);
                 v = fma(kgI, fma(gG[i * 3 + d], G[k * 3 + e2], G[i * 3 + d] * gG[k * 3 + e2]), v);
-                v = fma(kgg, gG[i * 3 + d] * gG[k * 3 + e2], v);
+                if (NIMR) v = fma(kgg, gG[i * 3 + d] * gG[k * 3 + e2], v);
                 T t4 = fma(g6[s6(i, k)], GG[dd * 3 + ee], fma(gG[i * 3 + e2], G[k * 3 + d], gG[k * 3 + d] * G[i * 3 + e2]));
                 if (i == k) t4 += GgG[dd * 3 + ee];
                 v = fma(kg4, t4, v);
@@ -263,9 +266,9 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         const double detJ = kinematics_fn<NPE>(jm, coords, __ldg(A.w + g), A.update, G, F);
         double sig[6], b[6], J, c1, c2, cbb;
         MatParams mp = A.mp;
-        if (A.eparams) mp = MatParams{__ldg(A.eparams + e * 3), __ldg(A.eparams + e * 3 + 1), __ldg(A.eparams + e * 3 + 2)};
+        if (A.eparams) mp = MatParams{__ldg(A.eparams + e * 3), __ldg(A.eparams + e * 3 + 1), __ldg(A.eparams + e * 3 + 2), 0.0};
         ExtraTangent ex;
-        material<MAT>(F, mp, sig, b, J, c1, c2, cbb, &ex);
+        material<MAT>(F, mp, sig, b, J, c1, c2, cbb, &ex, A.orient ? A.orient + e * 3 : nullptr);
         if (!(J > 0.0)) flag |= FL_FLAG_NONPOSITIVE_J;
         const int64_t ld = A.ldq;
         double *q = A.Q + t;
@@ -674,15 +677,18 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
                        double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
                        const int32_t *data_local_indices, const int32_t *data_global_indices, MatParams mp,
                        int *flags, double *scratch, size_t scratch_bytes, cudaStream_t stream,
-                       const double *eparams = nullptr) {
+                       const double *eparams = nullptr, const double *orient = nullptr) {
     if (ndim != 3 || nvar != 3 || H_VoigtSize != 6) return FL_ERR_ARG;
     if (nelem < 0 || nnode <= 0) return FL_ERR_ARG;
     if (ngauss <= 0 || ngauss > 343) return FL_ERR_UNSUPPORTED;
     if (3 * nnode + 2 > INT32_MAX) return FL_ERR_UNSUPPORTED;
-    if (mat != NEOHOOKEAN && mat != MOONEYRIVLIN && mat != NEARLYINCOMPRESSIBLEMR && mat != LINEARELASTIC)
+    if (mat != NEOHOOKEAN && mat != MOONEYRIVLIN && mat != NEARLYINCOMPRESSIBLEMR && mat != LINEARELASTIC &&
+        mat != ANISOTROPICMR1)
         return FL_ERR_UNSUPPORTED;
+    if (mat == ANISOTROPICMR1 && eparams) return FL_ERR_UNSUPPORTED;  // per-element parameters: 3 values
     if (nelem == 0) return FL_OK;  // nothing is read or written
     if (!points || !elements || !Eulerx || !Jm || !AllGauss || !V_stiff || !T) return FL_ERR_ARG;
+    if (mat == ANISOTROPICMR1 && !orient) return FL_ERR_ARG;  // the fibre directions are required
     AsmArgs A;
     A.points = points;
     A.elements = elements;
@@ -703,6 +709,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.flags = flags;
     A.Q = nullptr;
     A.Qf = nullptr;
+    A.orient = mat == ANISOTROPICMR1 ? orient : nullptr;
     A.e0 = A.ne = A.ldq = 0;
     A.qc = 1;
     if (recompute_sparsity_pattern) {
@@ -729,19 +736,23 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
         case MOONEYRIVLIN: return dispatch_asm<MOONEYRIVLIN>((int)nodeperelem, A, scratch, scratch_bytes, stream);
         case NEARLYINCOMPRESSIBLEMR:
             return dispatch_asm<NEARLYINCOMPRESSIBLEMR>((int)nodeperelem, A, scratch, scratch_bytes, stream);
+        case ANISOTROPICMR1: return dispatch_asm<ANISOTROPICMR1>((int)nodeperelem, A, scratch, scratch_bytes, stream);
         default: return dispatch_asm<LINEARELASTIC>((int)nodeperelem, A, scratch, scratch_bytes, stream);
     }
 }
 
 // Material of a C-ABI material number and its parameters from the reference's argument names:
 // neo-Hookean and linear elastic (mu, lamb), Mooney-Rivlin (mu1, mu2, lamb), nearly incompressible
-// Mooney-Rivlin (alpha, beta, kappa) = (mu1, mu2, lamb) (AOT_Assembler.py:62-71).
-static int material_of(int material_number, double mu, double mu1, double mu2, double lamb, int *mat, MatParams *mp) {
+// Mooney-Rivlin (alpha, beta, kappa) = (mu1, mu2, lamb), transversely isotropic Mooney-Rivlin
+// (mu1, mu2, lamb, mu3) (AOT_Assembler.py:62-75, 110-115).
+static int material_of(int material_number, double mu, double mu1, double mu2, double lamb, int *mat, MatParams *mp,
+                       double mu3 = 0.0) {
     switch (material_number) {
         case FL_MATERIAL_NEOHOOKEAN: *mat = NEOHOOKEAN; *mp = {mu, lamb, 0.0}; return FL_OK;
         case FL_MATERIAL_MOONEYRIVLIN: *mat = MOONEYRIVLIN; *mp = {mu1, mu2, lamb}; return FL_OK;
         case FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN: *mat = NEARLYINCOMPRESSIBLEMR; *mp = {mu1, mu2, lamb}; return FL_OK;
         case FL_MATERIAL_LINEARELASTIC: *mat = LINEARELASTIC; *mp = {mu, lamb, 0.0}; return FL_OK;
+        case FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1: *mat = ANISOTROPICMR1; *mp = {mu1, mu2, lamb, mu3}; return FL_OK;
         default: return FL_ERR_UNSUPPORTED;
     }
 }
@@ -1921,11 +1932,10 @@ extern "C" {
 
 int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS) {
     (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
-    (void)sorter; (void)rho; (void)mu3; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
-    (void)anisotropic_orientations;
+    (void)sorter; (void)rho; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
     fl::MatParams mp;
     int mat = 0;
-    if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &mp) != FL_OK) return FL_ERR_UNSUPPORTED;
+    if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &mp, mu3) != FL_OK) return FL_ERR_UNSUPPORTED;
     if (ngauss <= 0 || ngauss > 343 || nelem < 0) return FL_ERR_ARG;
     // the whole mesh must fit the array in one pass: nelem * ngauss Gauss points of 54 doubles
     if ((double)nelem * (double)ngauss * fl::QSTRIDE * sizeof(double) > (double)FL_NOALLOC_SCRATCH_BYTES)
@@ -1938,7 +1948,7 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
                                   nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
                                   recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
                                   data_global_indices, mp, flags, scratch, FL_NOALLOC_SCRATCH_BYTES,
-                                  (cudaStream_t)stream);
+                                  (cudaStream_t)stream, nullptr, anisotropic_orientations);
 }
 
 int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const uint64_t *elements,
@@ -1946,8 +1956,8 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
                               int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
                               const int32_t *indptr, const int32_t *indices, const int32_t *data_local_indices,
                               const int32_t *data_global_indices, float *V_stiff, double *T, double mu, double mu1,
-                              double mu2, double lamb, const double *element_params, int *flags,
-                              fl_stream_t stream) {
+                              double mu2, double lamb, double mu3, const double *anisotropic_orientations,
+                              const double *element_params, int *flags, fl_stream_t stream) {
     if (nelem < 0 || nnode <= 0 || ngauss <= 0 || ngauss > 343) return FL_ERR_ARG;
     if (nelem == 0) return FL_OK;
     const bool maps = data_local_indices && data_global_indices;
@@ -1977,13 +1987,20 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.flags = flags;
     A.Q = nullptr;
     A.Qf = nullptr;
+    A.orient = nullptr;
     A.e0 = A.ne = A.ldq = 0;
     int mat = 0;
-    if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &A.mp) != FL_OK) return FL_ERR_UNSUPPORTED;
+    if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &A.mp, mu3) != FL_OK) return FL_ERR_UNSUPPORTED;
+    if (mat == fl::ANISOTROPICMR1) {
+        if (!anisotropic_orientations) return FL_ERR_ARG;
+        if (element_params) return FL_ERR_UNSUPPORTED;
+        A.orient = anisotropic_orientations;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     switch (mat) {
         case fl::NEOHOOKEAN: return fl::mixed_dispatch<fl::NEOHOOKEAN>((int)nodeperelem, A, V_stiff, s);
         case fl::MOONEYRIVLIN: return fl::mixed_dispatch<fl::MOONEYRIVLIN>((int)nodeperelem, A, V_stiff, s);
+        case fl::ANISOTROPICMR1: return fl::mixed_dispatch<fl::ANISOTROPICMR1>((int)nodeperelem, A, V_stiff, s);
         case fl::NEARLYINCOMPRESSIBLEMR:
             return fl::mixed_dispatch<fl::NEARLYINCOMPRESSIBLEMR>((int)nodeperelem, A, V_stiff, s);
         default: return fl::mixed_dispatch<fl::LINEARELASTIC>((int)nodeperelem, A, V_stiff, s);
@@ -2082,6 +2099,17 @@ int fl_GlobalAssemblyDF__LinearElastic_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
                                   nelem, nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff,
                                   V_stiff, T, recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
                                   data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream);
+}
+
+int fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
+    (void)sorter; (void)rho; (void)mu; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
+    fl::MatParams mp{mu1, mu2, lamb, mu3};
+    return fl::global_assembly_df(fl::ANISOTROPICMR1, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss,
+                                  nelem, nodeperelem, nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff,
+                                  V_stiff, T, recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
+                                  data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream, nullptr,
+                                  anisotropic_orientations);
 }
 
 int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {

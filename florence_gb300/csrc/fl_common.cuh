@@ -38,7 +38,7 @@ inline int ensure_smem(size_t bytes) {
 
 // Material numbers (FL_MATERIAL_*), as the reference's explicit dispatcher numbers them
 // (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-106)
-enum { NEOHOOKEAN = 1, MOONEYRIVLIN = 2, NEARLYINCOMPRESSIBLEMR = 3, LINEARELASTIC = 10 };
+enum { NEOHOOKEAN = 1, MOONEYRIVLIN = 2, NEARLYINCOMPRESSIBLEMR = 3, LINEARELASTIC = 10, ANISOTROPICMR1 = 11 };
 
 // Extra elasticity terms of the nearly incompressible Mooney-Rivlin material:
 //   c += kbI (b_ij d_kl + d_ij b_kl) + kgI (g_ij d_kl + d_ij g_kl)
@@ -50,6 +50,7 @@ struct ExtraTangent {
 
 struct MatParams {
     double p0, p1, p2;  // neo-Hookean: mu, lamb; Mooney-Rivlin: mu1, mu2, lamb
+    double p3 = 0.0;    // transversely isotropic Mooney-Rivlin: mu3 (p0..p2 as Mooney-Rivlin)
 };
 
 // Inverse of a row-major 3x3 by adjugate over determinant; returns the determinant.
@@ -88,7 +89,8 @@ __device__ __forceinline__ int s6(int i, int j) {
 //   + lamb (J-1) I, c1 = 2(mu1+2mu2)/J - lamb (J-1), c2 = lamb (2J-1), cbb = 2 mu2/J.
 template <int MAT>
 __device__ __forceinline__ void material(const double *F, const MatParams &mp, double *sig, double *b, double &J,
-                                         double &c1, double &c2, double &cbb, ExtraTangent *ex = nullptr) {
+                                         double &c1, double &c2, double &cbb, ExtraTangent *ex = nullptr,
+                                         const double *N = nullptr) {
     J = det3(F);
     if constexpr (MAT == LINEARELASTIC) {  // _LinearElastic_.h:26-60: sigma = 2 mu eps + lamb tr(eps) I, eps = sym(F - I)
         const double mu = mp.p0, lamb = mp.p1;
@@ -151,6 +153,49 @@ __device__ __forceinline__ void material(const double *F, const MatParams &mp, d
             ex->kgg = B1 / trg;
 #pragma unroll
             for (int k = 0; k < 6; ++k) ex->g[k] = g[k];
+        }
+    } else if (MAT == ANISOTROPICMR1) {
+        // _AnisotropicMooneyRivlin_1_.h:31-88, parameters (mu1, mu2, lamb, mu3) and the element's
+        // fibre direction N; with HN = cof(F) N = J F^-T N and m = HN HN^T:
+        // sigma = 2mu1/J b + 2mu2/J (tr b b - b b) - 2(mu1+2mu2+mu3)/J I + lamb (J-1) I
+        //       + 2mu3/J (FN FN^T + |HN|^2 I - m);
+        // elasticity = the Mooney-Rivlin terms with mu1+2mu2+mu3, -4mu3/J (I m + m I),
+        // 2mu3/J |HN|^2 (2 II - I_ik I_jl - I_il I_jk), 2mu3/J (I_ik m_jl + I_il m_jk + m_ik I_jl + m_il I_jk):
+        // the last two fold into c1, c2 and the g-terms (kgI, kg4) of the shared tangent form
+        const double mu1 = mp.p0, mu2 = mp.p1, lamb = mp.p2, mu3 = mp.p3;
+        const double n0 = N ? N[0] : 0.0, n1 = N ? N[1] : 0.0, n2 = N ? N[2] : 0.0;
+        double iF[9], FN[3], HN[3], m[6], bb[6];
+        inv3(F, iF);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            FN[i] = fma(F[i * 3], n0, fma(F[i * 3 + 1], n1, F[i * 3 + 2] * n2));
+            HN[i] = J * fma(iF[0 * 3 + i], n0, fma(iF[1 * 3 + i], n1, iF[2 * 3 + i] * n2));
+        }
+        const double inHN = HN[0] * HN[0] + HN[1] * HN[1] + HN[2] * HN[2];
+        const double trb = b[0] + b[1] + b[2];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = i; j < 3; ++j) {
+                m[s6(i, j)] = HN[i] * HN[j];
+                bb[s6(i, j)] = b[s6(i, 0)] * b[s6(0, j)] + b[s6(i, 1)] * b[s6(1, j)] + b[s6(i, 2)] * b[s6(2, j)];
+                sig[s6(i, j)] = 2.0 * mu1 * iJ * b[s6(i, j)] + 2.0 * mu2 * iJ * (trb * b[s6(i, j)] - bb[s6(i, j)]) +
+                                2.0 * mu3 * iJ * (FN[i] * FN[j] - HN[i] * HN[j]);
+            }
+        const double C = 2.0 * (mu1 + 2.0 * mu2 + mu3) * iJ, dv = lamb * (J - 1.0), a3 = 2.0 * mu3 * iJ;
+        sig[0] += dv - C + a3 * inHN;
+        sig[1] += dv - C + a3 * inHN;
+        sig[2] += dv - C + a3 * inHN;
+        c1 = C - dv - a3 * inHN;
+        c2 = lamb * (2.0 * J - 1.0) + 2.0 * a3 * inHN;
+        cbb = 2.0 * mu2 * iJ;
+        if (ex) {
+            ex->kbI = 0.0;
+            ex->kgI = -2.0 * a3;
+            ex->kg4 = a3;
+            ex->kgg = 0.0;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) ex->g[k] = m[k];
         }
     } else {
         const double mu1 = mp.p0, mu2 = mp.p1, lamb = mp.p2;

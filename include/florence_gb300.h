@@ -47,6 +47,9 @@ typedef struct CUstream_st *fl_stream_t;
 #define FL_MATERIAL_MOONEYRIVLIN 2
 #define FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN 3
 #define FL_MATERIAL_LINEARELASTIC 10
+/* the transversely isotropic Mooney-Rivlin law (implicit entry points only; the reference's
+ * explicit dispatcher has no number for it) */
+#define FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1 11
 
 const char *fl_status_string(int status);
 
@@ -108,6 +111,11 @@ int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu1, mu2,
  * stiffness, AOT_Assembler.py:74-81). */
 int fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS);
 int fl_GlobalAssemblyDF__LinearElastic_(FL_GLOBAL_ASSEMBLY_DF_ARGS);
+/* _GlobalAssemblyDF__AnisotropicMooneyRivlin_1_ (AOT_Assembler.py:8-14, 72-75, 113-114): the
+ * transversely isotropic Mooney-Rivlin law of _AnisotropicMooneyRivlin_1_.h:31-88 with parameters
+ * mu1, mu2, mu3, lamb and one fibre direction per element, anisotropic_orientations [nelem][3]
+ * (device, required: FL_ERR_ARG if null). */
+int fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_(FL_GLOBAL_ASSEMBLY_DF_ARGS);
 
 /* ------------------------------------------------------------------------------------------
  * Allocation-free tangent + residual assembly. No counterpart in the reference (its assembly
@@ -149,16 +157,20 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
  * (_LowLevelAssemblyDF_.h:8-176); this is the Jacobian fl_BlockJacobiPCG applies with
  * value_bits = 32. CSR through the reference's element-to-nonzero maps, or, with both map
  * pointers NULL, by binary search in the rows of indptr/indices.
- * material_number: FL_MATERIAL_NEOHOOKEAN (mu, lamb) or FL_MATERIAL_MOONEYRIVLIN (mu1, mu2, lamb);
- * element_params [nelem][3] (optional) overrides them per element, as in fl_GlobalAssemblyDF_Batched.
+ * material_number: FL_MATERIAL_NEOHOOKEAN (mu, lamb), FL_MATERIAL_MOONEYRIVLIN (mu1, mu2, lamb),
+ * FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN (alpha, beta, kappa as mu1, mu2, lamb),
+ * FL_MATERIAL_LINEARELASTIC (mu, lamb) or FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1 (mu1, mu2, lamb, mu3
+ * and anisotropic_orientations [nelem][3], required for it and ignored otherwise);
+ * element_params [nelem][3] (optional) overrides (p0, p1, p2) per element, as in
+ * fl_GlobalAssemblyDF_Batched (not for the transversely isotropic law).
  * ------------------------------------------------------------------------------------------ */
 int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const uint64_t *elements,
                               const double *Eulerx, const double *Jm, const double *AllGauss, int64_t ngauss,
                               int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t requires_geometry_update,
                               const int32_t *indptr, const int32_t *indices, const int32_t *data_local_indices,
                               const int32_t *data_global_indices, float *V_stiff, double *T, double mu, double mu1,
-                              double mu2, double lamb, const double *element_params, int *flags,
-                              fl_stream_t stream);
+                              double mu2, double lamb, double mu3, const double *anisotropic_orientations,
+                              const double *element_params, int *flags, fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
  * Batched assembly of many independent meshes: the caller concatenates the instances of one

@@ -41,6 +41,13 @@
 #define ORC_MOONEYRIVLIN 2
 #define ORC_NEARLYINCOMPRESSIBLEMOONEYRIVLIN 3
 #define ORC_LINEARELASTIC 10
+#define ORC_ANISOTROPICMOONEYRIVLIN_1 11
+
+/* Fibre direction N per element [nelem][3] for the transversely isotropic material (the
+ * reference's anisotropic_orientations, read as &anisotropic_orientations[elem*ndim],
+ * AOT_Assembler.py:72-75); set before an assembly call, NULL otherwise. */
+static const double *g_orient = NULL;
+void orc_set_orientations(const double *orient) { g_orient = orient; }
 
 /* Voigt pairs in the reference's order xx,yy,zz,xy,xz,yz (_ConstitutiveStiffnessDF_.h:17-22). */
 static const int VI[6] = {0, 1, 2, 0, 0, 1};
@@ -105,8 +112,9 @@ static double kinematics_qp(const double *Jm, const double *w, const double *X, 
     return detJ;
 }
 
-/* Cauchy stress (row-major 3x3) and the Voigt elasticity H (6x6) of the material at F. */
-static void material_qp(int mat, const double *prm, const double *F, double *sig, double *H) {
+/* Cauchy stress (row-major 3x3) and the Voigt elasticity H (6x6) of the material at F (N: the
+ * element's fibre direction, transversely isotropic material only). */
+static void material_qp(int mat, const double *prm, const double *F, const double *N, double *sig, double *H) {
     double J = det3(F);
     double b[9];
     for (int i = 0; i < 3; ++i)
@@ -155,6 +163,41 @@ static void material_qp(int mat, const double *prm, const double *F, double *sig
         kgI = -B1;
         kg4 = B1;
         kgg = B1 / trg;
+    } else if (mat == ORC_ANISOTROPICMOONEYRIVLIN_1) {
+        /* _AnisotropicMooneyRivlin_1_.h:31-88 (parameters mu1, mu2, lamb, mu3), with HN = cof(F) N:
+         * sigma = 2mu1/J b + 2mu2/J (tr b b - b b) - 2(mu1+2mu2+mu3)/J I + lamb (J-1) I
+         *       + 2mu3/J (FN FN^T + |HN|^2 I - HN HN^T);
+         * elasticity: the Mooney-Rivlin terms with mu1+2mu2+mu3, and with m = HN HN^T
+         * -4mu3/J (I m + m I) + 2mu3/J |HN|^2 (2 II - I_ik I_jl - I_il I_jk)
+         * + 2mu3/J (I_ik m_jl + I_il m_jk + m_ik I_jl + m_il I_jk) */
+        static const double N0[3] = {0.0, 0.0, 0.0};
+        double mu1 = prm[0], mu2 = prm[1], lamb = prm[2], mu3 = prm[3];
+        double iF[9], Hc[9], FN[3], HN[3];
+        if (!N) N = N0; /* no fibre directions given */
+        inv3(F, iF);
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) Hc[i * 3 + j] = J * iF[j * 3 + i];
+        for (int i = 0; i < 3; ++i) {
+            FN[i] = F[i * 3] * N[0] + F[i * 3 + 1] * N[1] + F[i * 3 + 2] * N[2];
+            HN[i] = Hc[i * 3] * N[0] + Hc[i * 3 + 1] * N[1] + Hc[i * 3 + 2] * N[2];
+        }
+        double inHN = HN[0] * HN[0] + HN[1] * HN[1] + HN[2] * HN[2];
+        double trb = b[0] + b[4] + b[8];
+        for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j) {
+                double bb = 0.0;
+                for (int k = 0; k < 3; ++k) bb += b[i * 3 + k] * b[k * 3 + j];
+                double d = (i == j) ? 1.0 : 0.0;
+                g[i * 3 + j] = HN[i] * HN[j];
+                sig[i * 3 + j] = 2.0 * mu1 / J * b[i * 3 + j] + 2.0 * mu2 / J * (trb * b[i * 3 + j] - bb) -
+                                 2.0 * (mu1 + 2.0 * mu2 + mu3) / J * d + lamb * (J - 1.0) * d +
+                                 2.0 * mu3 / J * (FN[i] * FN[j] + inHN * d - HN[i] * HN[j]);
+            }
+        c1 = 2.0 * (mu1 + 2.0 * mu2 + mu3) / J - lamb * (J - 1.0) - 2.0 * mu3 / J * inHN;
+        c2 = lamb * (2.0 * J - 1.0) + 4.0 * mu3 / J * inHN;
+        cbb = 2.0 * mu2 / J;
+        kgI = -4.0 * mu3 / J;
+        kg4 = 2.0 * mu3 / J;
     } else if (mat == ORC_NEOHOOKEAN) {
         double mu = prm[0], lamb = prm[1];
         for (int i = 0; i < 3; ++i)
@@ -182,7 +225,7 @@ static void material_qp(int mat, const double *prm, const double *F, double *sig
             int i = VI[I], j = VJ[I], k = VI[K], l = VJ[K];
             double v = c1 * ((i == k) * (j == l) + (i == l) * (j == k)) + c2 * (i == j) * (k == l);
             if (cbb != 0.0) v += cbb * (2.0 * b[i * 3 + j] * b[k * 3 + l] - b[i * 3 + k] * b[j * 3 + l] - b[i * 3 + l] * b[j * 3 + k]);
-            if (mat == ORC_NEARLYINCOMPRESSIBLEMOONEYRIVLIN) {
+            if (mat == ORC_NEARLYINCOMPRESSIBLEMOONEYRIVLIN || mat == ORC_ANISOTROPICMOONEYRIVLIN_1) {
                 double dij = (i == j), dkl = (k == l), dik = (i == k), djl = (j == l), dil = (i == l), djk = (j == k);
                 v += kbI * (b[i * 3 + j] * dkl + dij * b[k * 3 + l]) + kgI * (g[i * 3 + j] * dkl + dij * g[k * 3 + l]) +
                      kg4 * (g[i * 3 + k] * djl + g[i * 3 + l] * djk + dik * g[j * 3 + l] + dil * g[j * 3 + k]) +
@@ -195,8 +238,9 @@ static void material_qp(int mat, const double *prm, const double *F, double *sig
 /* Element tangent K_e (row-major ndof x ndof, dofs interleaved a*3+i) and residual t_e.
  * Dense B*H*B^T per Gauss point plus geometric stiffness, as in the reference. Work arrays:
  * B[ndof*6], HBT[6*ndof]. */
-static void element_df(int mat, const double *prm, const double *Jm, const double *w, const double *X, const double *x,
-                       int npe, int nq, int update, double *Ke, double *te, double *sp, double *B, double *HBT) {
+static void element_df(int mat, const double *prm, const double *N, const double *Jm, const double *w, const double *X,
+                       const double *x, int npe, int nq, int update, double *Ke, double *te, double *sp, double *B,
+                       double *HBT) {
     int ndof = 3 * npe;
     memset(Ke, 0, sizeof(double) * ndof * ndof);
     memset(te, 0, sizeof(double) * ndof);
@@ -204,7 +248,7 @@ static void element_df(int mat, const double *prm, const double *Jm, const doubl
     for (int g = 0; g < nq; ++g) {
         double F[9], sig[9], H[36];
         double detJ = kinematics_qp(Jm, w, X, x, npe, nq, g, update, sp, F);
-        material_qp(mat, prm, F, sig, H);
+        material_qp(mat, prm, F, N, sig, H);
         /* FillConstitutiveB_: rows (a,x),(a,y),(a,z) */
         for (int a = 0; a < npe; ++a) {
             double a0 = sp[a * 3], a1 = sp[a * 3 + 1], a2 = sp[a * 3 + 2];
@@ -290,7 +334,8 @@ void orc_element_matrices(int mat, const double *prm, const double *points, cons
         const int64_t *el = elements + elem_ids[n] * npe;
         gather(points, el, (int)npe, X);
         gather(Eulerx, el, (int)npe, x);
-        element_df(mat, prm, Jm, w, X, x, (int)npe, (int)nq, update, Ke_out + n * ndof * ndof, te_out + n * ndof, sp, B, HBT);
+        element_df(mat, prm, g_orient ? g_orient + elem_ids[n] * 3 : NULL, Jm, w, X, x, (int)npe, (int)nq, update,
+                   Ke_out + n * ndof * ndof, te_out + n * ndof, sp, B, HBT);
     }
     free(X); free(x); free(sp); free(B); free(HBT);
 }
@@ -316,7 +361,8 @@ int orc_assemble_df(int mat, const double *prm, const double *points, const int6
             const int64_t *el = elements + e * npe;
             gather(points, el, (int)npe, X);
             gather(Eulerx, el, (int)npe, x);
-            element_df(mat, prm, Jm, w, X, x, (int)npe, (int)nq, update, Ke, te, sp, B, HBT);
+            element_df(mat, prm, g_orient ? g_orient + e * 3 : NULL, Jm, w, X, x, (int)npe, (int)nq, update, Ke, te, sp,
+                       B, HBT);
             for (int a = 0; a < npe; ++a)
                 for (int c = 0; c < 3; ++c) dofs[a * 3 + c] = el[a] * 3 + c;
             if (mode == 0) {
@@ -364,7 +410,7 @@ int orc_internal_force(int mat, const double *prm, const double *points, const i
             for (int g = 0; g < nq; ++g) {
                 double F[9], sig[9], H[36];
                 double detJ = kinematics_qp(Jm, w, X, x, (int)npe, (int)nq, g, 1, sp, F);
-                material_qp(mat, prm, F, sig, H);
+                material_qp(mat, prm, F, g_orient ? g_orient + e * 3 : NULL, sig, H);
                 for (int a = 0; a < npe; ++a) {
                     double a0 = sp[a * 3], a1 = sp[a * 3 + 1], a2 = sp[a * 3 + 2];
                     tr[a * 3 + 0] += (a0 * sig[0] + a1 * sig[1] + a2 * sig[2]) * detJ;

@@ -16,7 +16,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 FAST_PATH = os.path.join(HERE, "liboracle_fast.so")
-MATERIALS = {"NeoHookean": 1, "MooneyRivlin": 2, "NearlyIncompressibleMooneyRivlin": 3, "LinearElastic": 10}
+MATERIALS = {"NeoHookean": 1, "MooneyRivlin": 2, "NearlyIncompressibleMooneyRivlin": 3, "LinearElastic": 10,
+             "AnisotropicMooneyRivlin_1": 11}
 
 _libs = {}
 
@@ -46,6 +47,7 @@ def lib(fast=False):
         L.orc_sparsity_nnz.argtypes = [P, i64, i64, i64, i64]
         L.orc_sparsity_nnz.restype = i64
         L.orc_sparsity.argtypes = [P, i64, i64, i64, i64, P, P, P, P]
+        L.orc_set_orientations.argtypes = [P]
         _libs[key] = L
     return _libs[key]
 
@@ -56,6 +58,21 @@ def _p(a):
 
 def _c(a, dt):
     return np.ascontiguousarray(a, dtype=dt)
+
+
+class _orientations:
+    """Per-element fibre directions [nelem][3] (AnisotropicMooneyRivlin_1) for the calls made
+    within the block; the array is kept alive and the pointer cleared afterwards."""
+
+    def __init__(self, L, orientations):
+        self.L = L
+        self.a = None if orientations is None else _c(orientations, np.float64)
+
+    def __enter__(self):
+        self.L.orc_set_orientations(_p(self.a))
+
+    def __exit__(self, *exc):
+        self.L.orc_set_orientations(None)
 
 
 def max_threads():
@@ -79,7 +96,7 @@ def sparsity(elements, nnode, nvar=3, maps=True):
 
 
 def assemble_df(material, params, points, elements, Eulerx, Jm, AllGauss, mode="csr", sparsity_arrays=None,
-                requires_geometry_update=1, nthreads=1, fast=False):
+                requires_geometry_update=1, nthreads=1, fast=False, orientations=None):
     """Global tangent and residual. mode: 'triplet' -> (I, J, V, T); 'csr'/'squeeze' -> (V, T)."""
     mat = MATERIALS[material]
     prm = _c(params, np.float64)
@@ -96,21 +113,26 @@ def assemble_df(material, params, points, elements, Eulerx, Jm, AllGauss, mode="
         I = np.zeros(nelem * ndof * ndof, np.int32)
         J = np.zeros_like(I)
         V = np.zeros(nelem * ndof * ndof)
-        lib(fast).orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
-                                  requires_geometry_update, 0, _p(I), _p(J), _p(V), _p(T), None, None, None, None, nthreads)
+        with _orientations(lib(fast), orientations):
+            lib(fast).orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
+                                      requires_geometry_update, 0, _p(I), _p(J), _p(V), _p(T), None, None, None, None,
+                                      nthreads)
         return I, J, V, T
     indices, indptr, dl, dg = sparsity_arrays
     indices = _c(indices, np.int32)
     indptr = _c(indptr, np.int32)
     V = np.zeros(indices.shape[0])
     m = 1 if mode == "csr" else 2
-    lib(fast).orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
-                              requires_geometry_update, m, None, None, _p(V), _p(T), _p(indptr), _p(indices),
-                          _p(_c(dl, np.int32) if m == 1 else None), _p(_c(dg, np.int32) if m == 1 else None), nthreads)
+    with _orientations(lib(fast), orientations):
+        lib(fast).orc_assemble_df(mat, _p(prm), _p(X), _p(el), _p(x), _p(jm), _p(w), nelem, npe, nq,
+                                  requires_geometry_update, m, None, None, _p(V), _p(T), _p(indptr), _p(indices),
+                                  _p(_c(dl, np.int32) if m == 1 else None), _p(_c(dg, np.int32) if m == 1 else None),
+                                  nthreads)
     return V, T
 
 
-def element_matrices(material, params, points, elements, Eulerx, Jm, AllGauss, elem_ids, requires_geometry_update=1):
+def element_matrices(material, params, points, elements, Eulerx, Jm, AllGauss, elem_ids, requires_geometry_update=1,
+                     orientations=None):
     mat = MATERIALS[material]
     el = _c(elements, np.int64)
     npe = el.shape[1]
@@ -119,20 +141,22 @@ def element_matrices(material, params, points, elements, Eulerx, Jm, AllGauss, e
     ndof = 3 * npe
     Ke = np.zeros((ids.shape[0], ndof, ndof))
     te = np.zeros((ids.shape[0], ndof))
-    lib().orc_element_matrices(mat, _p(_c(params, np.float64)), _p(_c(points, np.float64)), _p(el),
-                               _p(_c(Eulerx, np.float64)), _p(_c(Jm, np.float64)), _p(w), npe, w.shape[0],
-                               requires_geometry_update, _p(ids), ids.shape[0], _p(Ke), _p(te))
+    with _orientations(lib(), orientations):
+        lib().orc_element_matrices(mat, _p(_c(params, np.float64)), _p(_c(points, np.float64)), _p(el),
+                                   _p(_c(Eulerx, np.float64)), _p(_c(Jm, np.float64)), _p(w), npe, w.shape[0],
+                                   requires_geometry_update, _p(ids), ids.shape[0], _p(Ke), _p(te))
     return Ke, te
 
 
-def internal_force(material, params, points, elements, Eulerx, Jm, AllGauss, nthreads=1):
+def internal_force(material, params, points, elements, Eulerx, Jm, AllGauss, nthreads=1, orientations=None):
     mat = MATERIALS[material]
     el = _c(elements, np.int64)
     w = _c(np.ravel(AllGauss), np.float64)
     T = np.zeros(np.shape(points)[0] * 3)
-    lib().orc_internal_force(mat, _p(_c(params, np.float64)), _p(_c(points, np.float64)), _p(el),
-                             _p(_c(Eulerx, np.float64)), _p(_c(Jm, np.float64)), _p(w), el.shape[0], el.shape[1],
-                             w.shape[0], _p(T), nthreads)
+    with _orientations(lib(), orientations):
+        lib().orc_internal_force(mat, _p(_c(params, np.float64)), _p(_c(points, np.float64)), _p(el),
+                                 _p(_c(Eulerx, np.float64)), _p(_c(Jm, np.float64)), _p(w), el.shape[0], el.shape[1],
+                                 w.shape[0], _p(T), nthreads)
     return T
 
 

@@ -44,10 +44,19 @@ def make_material(F, name, params):
         m = F.NearlyIncompressibleMooneyRivlin(3, mu=2.0 * params[0], lamb=params[2], rho=1.0)
         m.alpha, m.beta, m.kappa = params
         m.mu1, m.mu2, m.lamb = params
+    elif name == "AnisotropicMooneyRivlin_1":
+        # params (mu1, mu2, lamb, mu3); fibre directions set per element by make_case
+        m = F.AnisotropicMooneyRivlin_1(3, mu1=params[0], mu2=params[1], lamb=params[2], mu3=params[3], rho=1.0)
     else:
         raise ValueError(name)
     m.has_low_level_dispatcher = False
     return m
+
+
+def fibre_directions(nelem, seed):
+    """Seeded unit fibre directions per element (the reference's anisotropic_orientations)."""
+    v = np.random.default_rng(seed).standard_normal((nelem, 3))
+    return v / np.linalg.norm(v, axis=1, keepdims=True)
 
 
 def jittered_tet_mesh(F, nx, ny, nz, L, seed, jitter=0.15):
@@ -114,6 +123,8 @@ def build_mesh(F, spec):
 def reference_assembly(F, spec, mesh, x, recompute):
     """K (CSR) and T from the reference's AssembleForm, pure-numpy element path."""
     mat = make_material(F, spec["material"], spec["params"])
+    if spec.get("fibre_seed") is not None:
+        mat.anisotropic_orientations = fibre_directions(mesh.nelem, spec["fibre_seed"])
     kw = {} if spec.get("qdeg") is None else {"quadrature_degree": spec["qdeg"]}
     form = F.DisplacementFormulation(mesh, **kw)
     solver = F.FEMSolver(optimise=False, recompute_sparsity_pattern=recompute,
@@ -168,6 +179,11 @@ CASES = [
          amp=0.0, qdeg=None, emat=(0, 2), mass=False, nature="linear"),
     dict(name="tet_p2_nimr", mesh="cube_tet", n=(1, 1, 1), p=2, material="NearlyIncompressibleMooneyRivlin",
          params=(0.4, 0.1, 15.0), seed=20, amp=0.03, qdeg=None, emat=(0, 3), mass=False, triplet=True),
+    dict(name="hex_p2_amr", mesh="cube_hex", n=(2, 1, 1), p=2, material="AnisotropicMooneyRivlin_1",
+         params=(0.5, 0.3, 20.0, 0.7), fibre_seed=21, seed=22, amp=0.04, qdeg=None, emat=(0, 1), mass=False),
+    dict(name="tet_p2_amr", mesh="cube_tet", n=(1, 1, 1), p=2, material="AnisotropicMooneyRivlin_1",
+         params=(0.4, 0.2, 10.0, 1.1), fibre_seed=23, seed=24, amp=0.03, qdeg=None, emat=(0, 3), mass=False,
+         triplet=True),
     dict(name="tet_p3_mr_jitter", mesh="jitter_tet", L=(4.0, 1.0, 1.0), n=(4, 1, 1), mesh_seed=1, p=3,
          material="MooneyRivlin", params=(0.5, 0.5, 20.0), seed=18, amp=0.01, qdeg=None, emat=(0, 4), mass=True,
          triplet=True),
@@ -186,6 +202,8 @@ def make_case(F, spec):
         Jm=fs.Jm, AllGauss=fs.AllGauss.ravel(), Bases=fs.Bases,
         material=np.array(spec["material"]), params=np.array(spec["params"], np.float64),
         update=np.array(int(solver.requires_geometry_update)),
+        **({"orientations": np.asarray(mat.anisotropic_orientations, np.float64)}
+           if spec.get("fibre_seed") is not None else {}),
         K_indptr=K.indptr.astype(np.int32), K_indices=K.indices.astype(np.int32), K_data=K.data, T=T,
         sp_indices=solver.indices.astype(np.int32), sp_indptr=solver.indptr.astype(np.int32),
         sp_data_local=solver.data_local_indices.astype(np.int32),

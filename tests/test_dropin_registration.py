@@ -23,7 +23,8 @@ def test_install_registers_callables_in_reference_namespaces():
     ll = florence_gb300.install(F)
     from Florence.FiniteElements.Assembly import _LowLevelAssembly_ as mod
     assert mod is ll
-    for mat in ("NeoHookean", "MooneyRivlin"):
+    for mat in ("NeoHookean", "MooneyRivlin", "NearlyIncompressibleMooneyRivlin", "LinearElastic",
+                "AnisotropicMooneyRivlin_1"):
         name = "_LowLevelAssemblyDF__" + mat + "_"
         assert getattr(mod, name) is getattr(florence_gb300, name)
     assert mod._LowLevelAssemblyExplicit_DF_DPF_ is florence_gb300._LowLevelAssemblyExplicit_DF_DPF_

@@ -31,6 +31,8 @@ def fl():
 
 def _asm(fl, d, mode, **kw):
     kw.setdefault("requires_geometry_update", int(d["update"]))
+    if "orientations" in d:  # fibre directions of the transversely isotropic material
+        kw.setdefault("orientations", d["orientations"])
     return fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], str(d["material"]),
                               tuple(d["params"]), mode=mode, **kw)
 
@@ -187,15 +189,17 @@ def test_element_residual(fl, case):
     d = load_golden(case)
     for k, e in enumerate(d["emat_ids"]):
         el = d["elements"][int(e):int(e) + 1]
+        orient = d["orientations"][int(e):int(e) + 1] if "orientations" in d else None
         asm = fl.DeviceAssembler(d["points"], el, d["Jm"], d["AllGauss"], str(d["material"]), tuple(d["params"]),
-                                 mode="triplet")
+                                 mode="triplet", orientations=orient)
         _, _, _, T = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda())
         dofs = (3 * el[0][:, None] + np.arange(3)).ravel()
         assert rel_fro(T.cpu().numpy()[dofs], d["emat_t"][k]) < TOL
 
 
-@pytest.mark.parametrize("case", golden_cases())
+@pytest.mark.parametrize("case", [c for c in golden_cases() if "orientations" not in load_golden(c)])
 def test_internal_force(fl, case):
+    # (the reference's explicit path has no transversely isotropic material)
     d = load_golden(case)
     asm = _asm(fl, d, "triplet")
     T = asm.internal_force(torch.from_numpy(d["Eulerx"]).cuda())
@@ -330,6 +334,10 @@ def _fake_florence_objects(d, recompute, squeeze=False):
         material.mu, material.lamb = p[0], p[1]
     else:
         material.mu1, material.mu2, material.lamb = p[0], p[1], p[2]
+    if mat_name == "AnisotropicMooneyRivlin_1":
+        material.mu3 = p[3]
+        material.is_transversely_isotropic = True
+        material.anisotropic_orientations = d["orientations"]
     fs = types.SimpleNamespace(Jm=d["Jm"], AllGauss=d["AllGauss"][:, None], Bases=d["Bases"])
     form = types.SimpleNamespace(ndim=3, nvar=3, fields="mechanics")
     mesh = types.SimpleNamespace(points=d["points"], elements=d["elements"].astype(np.uint64),
@@ -340,7 +348,7 @@ def _fake_florence_objects(d, recompute, squeeze=False):
     return solver, fs, form, mesh, material
 
 
-@pytest.mark.parametrize("case", ["hex_p2_nh_q5", "tet_p3_mr_jitter"])
+@pytest.mark.parametrize("case", ["hex_p2_nh_q5", "tet_p3_mr_jitter", "tet_p2_amr"])
 @pytest.mark.parametrize("recompute,squeeze", [(True, False), (False, False), (False, True)])
 def test_drop_in_callables(fl, case, recompute, squeeze):
     d = load_golden(case)
@@ -357,6 +365,10 @@ def test_drop_in_callables(fl, case, recompute, squeeze):
         K = sp.csr_matrix((V, d["sp_indices"], d["sp_indptr"]), shape=(n, n))
     assert T.shape == (n,) and T.dtype == np.float64
     assert rel_fro(K.data, d["K_data"]) < TOL and rel_fro(T, d["T"]) < TOL
+    if "orientations" in d:  # no explicit path for the transversely isotropic material, as in the reference
+        with pytest.raises(NotImplementedError):
+            fl._LowLevelAssemblyExplicit_DF_DPF_(fs, form, mesh, material, d["Eulerx"], np.zeros(d["points"].shape[0]))
+        return
     Ti = fl._LowLevelAssemblyExplicit_DF_DPF_(fs, form, mesh, material, d["Eulerx"], np.zeros(d["points"].shape[0]))
     assert rel_fro(Ti, d["T"]) < TOL
 
@@ -375,9 +387,26 @@ def test_unsupported_material_raises(fl):
     d = load_golden("hex_p1_nh")
     solver, fs, form, mesh, material = _fake_florence_objects(d, True)
     with pytest.raises(NotImplementedError):
-        fl.material_params(material, "AnisotropicMooneyRivlin_1")
+        fl.material_params(material, "AnisotropicMooneyRivlin_0")
 
 
 def test_fp64_peak_is_measured(fl):
     g = fl.fp64_peak_gflops()
     assert 100.0 < g < 200000.0
+
+
+def test_transversely_isotropic_material_needs_fibre_directions(fl):
+    """AnisotropicMooneyRivlin_1 takes one fibre direction per element (the reference's
+    anisotropic_orientations); without them, or through the explicit path, it is refused."""
+    d = load_golden("tet_p2_amr")
+    with pytest.raises(ValueError):
+        fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], "AnisotropicMooneyRivlin_1",
+                           tuple(d["params"]), mode="csr")
+    asm = _asm(fl, d, "csr")
+    with pytest.raises(NotImplementedError):
+        asm.internal_force(torch.from_numpy(d["Eulerx"]).cuda())
+    # the fibre direction matters: rotating it changes the tangent
+    asm2 = fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], "AnisotropicMooneyRivlin_1",
+                              tuple(d["params"]), mode="csr", orientations=d["orientations"][:, [1, 2, 0]])
+    x = torch.from_numpy(d["Eulerx"]).cuda()
+    assert rel_fro(asm2.assemble(x)[0].cpu().numpy(), d["K_data"]) > 1e-3

@@ -20,7 +20,8 @@ def test_mixed_tangent_close_to_fp64(case):
     import florence_gb300 as fl
     d = load_golden(case)
     asm = fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], str(d["material"]),
-                             tuple(d["params"]), mode="csr", requires_geometry_update=int(d["update"]))
+                             tuple(d["params"]), mode="csr", requires_geometry_update=int(d["update"]),
+                             orientations=d.get("orientations"))
     x = torch.from_numpy(d["Eulerx"]).cuda()
     V32, T = asm.assemble_mixed(x)
     asm.check_flags()

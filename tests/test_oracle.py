@@ -34,14 +34,15 @@ def test_assembly_matches_reference(oracle, case, mode):
     mat, prm = str(d["material"]), d["params"]
     args = (mat, prm, d["points"], d["elements"], d["Eulerx"], d["Jm"], d["AllGauss"])
     nn = d["points"].shape[0] * 3
+    orient = d.get("orientations")
     if mode == "triplet":
-        I, J, V, T = oracle.assemble_df(*args, mode="triplet")
+        I, J, V, T = oracle.assemble_df(*args, mode="triplet", orientations=orient)
         K = sp.csr_matrix((V, (I, J)), shape=(nn, nn))
         assert np.array_equal(K.indptr, d["K_indptr"]) and np.array_equal(K.indices, d["K_indices"])
         V = K.data
     else:
         spa = oracle.sparsity(d["elements"], d["points"].shape[0])
-        V, T = oracle.assemble_df(*args, mode=mode, sparsity_arrays=spa)
+        V, T = oracle.assemble_df(*args, mode=mode, sparsity_arrays=spa, orientations=orient)
     assert rel_fro(V, d["K_data"]) < TOL
     assert rel_fro(T, d["T"]) < 1e-12
     if "K_triplet_data" in d:
@@ -52,7 +53,7 @@ def test_assembly_matches_reference(oracle, case, mode):
 def test_element_matrices(oracle, case):
     d = load_golden(case)
     Ke, te = oracle.element_matrices(str(d["material"]), d["params"], d["points"], d["elements"], d["Eulerx"],
-                                     d["Jm"], d["AllGauss"], d["emat_ids"])
+                                     d["Jm"], d["AllGauss"], d["emat_ids"], orientations=d.get("orientations"))
     assert rel_fro(Ke, d["emat_K"]) < TOL
     assert rel_fro(te, d["emat_t"]) < 1e-12
 
@@ -62,7 +63,7 @@ def test_internal_force_matches_residual(oracle, case):
     # the explicit internal force is the implicit residual without the tangent
     d = load_golden(case)
     T = oracle.internal_force(str(d["material"]), d["params"], d["points"], d["elements"], d["Eulerx"], d["Jm"],
-                              d["AllGauss"])
+                              d["AllGauss"], orientations=d.get("orientations"))
     assert rel_fro(T, d["T"]) < 1e-12
 
 
