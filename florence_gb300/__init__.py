@@ -7,7 +7,7 @@ The CUDA library (libflorence_gb300.so, built in-tree) is required: nothing here
 the CPU.
 """
 from . import _native
-from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_,
+from .assembly import (AssembleBodyForces, AssembleExternalTractionForces, ComputeSparsityPattern, DeviceAssembler, _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_,
                        _LowLevelAssemblyDF__LinearElastic_,
                        _LowLevelAssemblyDF__MooneyRivlin_, _LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_,
                        _LowLevelAssemblyDF__NeoHookean_, _LowLevelAssemblyExplicit_DF_DPF_,
@@ -15,7 +15,7 @@ from .assembly import (ComputeSparsityPattern, DeviceAssembler, _LowLevelAssembl
                        get_arithmetic, install, material_params, release_host_buffers, set_arithmetic,
                        set_tensor_core_tiling)
 
-__all__ = ["ComputeSparsityPattern", "DeviceAssembler", "_LowLevelAssemblyDF__NeoHookean_",
+__all__ = ["AssembleBodyForces", "AssembleExternalTractionForces", "ComputeSparsityPattern", "DeviceAssembler", "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",
            "_LowLevelAssemblyDF__LinearElastic_", "_LowLevelAssemblyExplicit_DF_DPF_",

@@ -74,6 +74,8 @@ def lib():
         L.fl_SetAssemblyArithmetic.argtypes = [INT]
         L.fl_GetAssemblyArithmetic.argtypes = []
         L.fl_SetTensorCoreTiling.argtypes = [INT, INT]
+        L.fl_AssembleExternalTractionForces.argtypes = [P, I64, I64, P, P, P, P, I64, P, P, I64, P, P, P]
+        L.fl_AssembleBodyForces.argtypes = [P, I64, I64, P, P, I64, D, I64, P, P, P]
         L.fl_GlobalAssemblyDF_Mixed.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, D, D, D,
                                                 D, D, P, P, P, P]
         L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
@@ -115,5 +117,5 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak", "fl_TensorCoreSelfTest",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
-           "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_MLP_num_params", "fl_MLP_workspace_size",
+           "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_AssembleExternalTractionForces", "fl_AssembleBodyForces", "fl_MLP_num_params", "fl_MLP_workspace_size",
            "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep"]

@@ -31,6 +31,7 @@ import torch
 from . import _native as N
 
 __all__ = ["DeviceAssembler", "ComputeSparsityPattern", "_LowLevelAssemblyDF__NeoHookean_",
+           "AssembleExternalTractionForces", "AssembleBodyForces",
            "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
            "__TotalConstantMassIntegrand__", "install", "material_params", "fp64_peak_gflops",
@@ -409,6 +410,54 @@ def _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_(fem_solver, function_space, 
                          Eulerp)
 
 
+def AssembleExternalTractionForces(boundary_condition, mesh, material, function_space, physical_faces=False):
+    """F [nnode*nvar, 1] -- Assembly.py:451-514 on the device: for every face with
+    boundary_condition.neumann_flags set, F[(a, i)] += applied_neumann[face, i] sum_g N_a(g) w_g
+    with the face function space's parent weights, as the reference integrates it. With
+    physical_faces=True the weights carry |dX/dxi x dX/deta| of the face (no reference
+    counterpart)."""
+    if material.ndim != 3 or material.nvar != 3:
+        raise NotImplementedError("the GB300 force assembly covers three-dimensional mechanics")
+    dev = torch.device("cuda")
+    faces = _to_dev(mesh.faces, torch.int64, dev)
+    nnode = mesh.points.shape[0]
+    F = torch.zeros(nnode * 3, dtype=torch.float64, device=dev)
+    flags_dev = torch.zeros(1, dtype=torch.int32, device=dev)
+    nf = _to_dev(np.asarray(boundary_condition.neumann_flags).astype(np.uint8).ravel(), torch.uint8, dev)
+    tr = _to_dev(np.nan_to_num(np.asarray(boundary_condition.applied_neumann, np.float64).reshape(faces.shape[0], -1)
+                               [:, :3]), torch.float64, dev)
+    B = _to_dev(function_space.Bases, torch.float64, dev)
+    w = _to_dev(np.ravel(function_space.AllGauss), torch.float64, dev)
+    P = _to_dev(mesh.points, torch.float64, dev) if physical_faces else None
+    Jf = _to_dev(function_space.Jm, torch.float64, dev) if physical_faces else None
+    st = N.lib().fl_AssembleExternalTractionForces(_ptr(faces), faces.shape[0], faces.shape[1], _ptr(nf), _ptr(tr),
+                                                   _ptr(B), _ptr(w), w.shape[0], _ptr(P), _ptr(Jf), nnode, _ptr(F),
+                                                   _ptr(flags_dev), _stream())
+    N.check(st, "fl_AssembleExternalTractionForces")
+    _check_flags(flags_dev, "AssembleExternalTractionForces")
+    return F.cpu().numpy()[:, None]
+
+
+def AssembleBodyForces(boundary_condition, mesh, material, function_space):
+    """F [nnode*nvar, 1] -- Assembly.py:516-560 on the device: the body force -rho in z,
+    F[(a, z)] -= rho sum_g N_a(g) w_g for every element, with the parent weights as the reference
+    integrates it."""
+    if material.ndim != 3 or material.nvar != 3:
+        raise NotImplementedError("the GB300 force assembly covers three-dimensional mechanics")
+    dev = torch.device("cuda")
+    el = _to_dev(mesh.elements, torch.int64, dev)
+    nnode = mesh.points.shape[0]
+    F = torch.zeros(nnode * 3, dtype=torch.float64, device=dev)
+    flags_dev = torch.zeros(1, dtype=torch.int32, device=dev)
+    B = _to_dev(function_space.Bases, torch.float64, dev)
+    w = _to_dev(np.ravel(function_space.AllGauss), torch.float64, dev)
+    st = N.lib().fl_AssembleBodyForces(_ptr(el), el.shape[0], el.shape[1], _ptr(B), _ptr(w), w.shape[0],
+                                       float(material.rho), nnode, _ptr(F), _ptr(flags_dev), _stream())
+    N.check(st, "fl_AssembleBodyForces")
+    _check_flags(flags_dev, "AssembleBodyForces")
+    return F.cpu().numpy()[:, None]
+
+
 def _LowLevelAssemblyExplicit_DF_DPF_(function_space, formulation, mesh, material, Eulerx, Eulerp):
     """Internal force T [nnode*nvar] -- _LowLevelAssemblyExplicit_DF_DPF_.pyx:44-152 (mechanics)."""
     if formulation.fields != "mechanics":
@@ -463,6 +512,9 @@ def install(florence):
     ll._LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_ = _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_
     ll._LowLevelAssemblyExplicit_DF_DPF_ = _LowLevelAssemblyExplicit_DF_DPF_
     ll.has_low_level_dispatcher = True
+    asm_mod = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly.Assembly")
+    asm_mod.AssembleExternalTractionForces = AssembleExternalTractionForces
+    asm_mod.AssembleBodyForces = AssembleBodyForces
     try:
         sp = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly.ComputeSparsityPattern")
     except ImportError:

@@ -337,6 +337,24 @@ int fl_MLPAdamStep(float *params, const float *grads, float *m, float *v, int64_
 int fl_measure_fp64_peak(double *gflops, fl_stream_t stream);
 int fl_measure_fp32_peak(double *gflops, fl_stream_t stream);
 
+/* ------------------------------------------------------------------------------------------
+ * External forces, F[nnode*3] += (device arrays). AssembleExternalTractionForces
+ * (Assembly.py:451-514): for every face f with neumann_flags[f] != 0 (all faces if the flags are
+ * NULL), F[(faces[f][a], i)] += applied_neumann[f][i] * sum_g Bases[a][g] w_g, the reference's
+ * parent-face weights; with Jm_face [2][nodeperface][ngauss] (the face basis gradients) and the
+ * points, w_g is multiplied by |dX/dxi x dX/deta| (the physical face). AssembleBodyForces
+ * (Assembly.py:516-560): F[(elements[e][a], z)] -= rho * sum_g Bases[a][g] w_g for every element.
+ * flags: device int, FL_FLAG_BAD_INDEX when a node id is out of range. No synchronisation.
+ * ------------------------------------------------------------------------------------------ */
+int fl_AssembleExternalTractionForces(const uint64_t *faces, int64_t nface, int64_t nodeperface,
+                                      const uint8_t *neumann_flags, const double *applied_neumann,
+                                      const double *Bases, const double *AllGauss, int64_t ngauss,
+                                      const double *points, const double *Jm_face, int64_t nnode, double *F,
+                                      int *flags, fl_stream_t stream);
+int fl_AssembleBodyForces(const uint64_t *elements, int64_t nelem, int64_t nodeperelem, const double *Bases,
+                          const double *AllGauss, int64_t ngauss, double rho, int64_t nnode, double *F, int *flags,
+                          fl_stream_t stream);
+
 /* Self-test of the tcgen05 tensor-core path (no reference counterpart): D [128 x 32] (FP32,
  * row-major) = A [128 x 48] * B [32 x 48]^T with BF16 A and B (row-major, device pointers), one
  * CTA, operands in shared memory, accumulator in tensor memory. *status (device) gets bit 1 if

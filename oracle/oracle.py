@@ -167,3 +167,25 @@ def lumped_mass(rho, points, elements, Jm, AllGauss, Bases):
     lib().orc_lumped_mass(float(rho), _p(_c(points, np.float64)), _p(el), _p(_c(Jm, np.float64)), _p(w),
                           _p(_c(Bases, np.float64)), el.shape[0], el.shape[1], w.shape[0], _p(M))
     return M
+
+
+def external_traction(faces, neumann_flags, applied_neumann, Bases, AllGauss, nnode):
+    """F [nnode*3] of AssembleExternalTractionForces (Assembly.py:451-514): every flagged face adds
+    applied_neumann[face, i] * sum_g Bases[a, g] w_g to its node a, component i (parent weights)."""
+    faces = np.asarray(faces, np.int64)
+    s = np.asarray(Bases, np.float64) @ np.ravel(AllGauss).astype(np.float64)  # sum_g N_a(g) w_g
+    F = np.zeros(nnode * 3)
+    for f in np.nonzero(np.ravel(neumann_flags))[0]:
+        for a, nd in enumerate(faces[f]):
+            F[3 * nd:3 * nd + 3] += np.asarray(applied_neumann[f], np.float64)[:3] * s[a]
+    return F
+
+
+def body_forces(elements, Bases, AllGauss, rho, nnode):
+    """F [nnode*3] of AssembleBodyForces (Assembly.py:516-560): -rho * sum_g Bases[a, g] w_g on the z
+    component of every element node."""
+    el = np.asarray(elements, np.int64)
+    s = np.asarray(Bases, np.float64) @ np.ravel(AllGauss).astype(np.float64)
+    F = np.zeros(nnode * 3)
+    np.add.at(F, 3 * el.ravel() + 2, np.tile(-rho * s, el.shape[0]))
+    return F

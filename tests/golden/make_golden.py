@@ -145,6 +145,26 @@ def element_matrices(F, form, mat, solver, mesh, x, elems):
     return np.array(Ks), np.array(ts)
 
 
+def reference_forces(F, spec, mesh, form, mat):
+    """Traction on the faces of the x = max plane (seeded traction per face) and the body force,
+    from the reference's AssembleExternalTractionForces / AssembleBodyForces (Assembly.py:451-560)."""
+    import types
+    from Florence.FiniteElements.Assembly.Assembly import AssembleBodyForces, AssembleExternalTractionForces
+    faces = np.asarray(mesh.faces).astype(np.int64)
+    xmax = mesh.points[:, 0].max()
+    flags = np.all(np.abs(mesh.points[faces][:, :, 0] - xmax) < 1e-9, axis=1)
+    traction = np.random.default_rng(spec["seed"] + 100).uniform(-1, 1, (faces.shape[0], 3))
+    bc = types.SimpleNamespace(is_applied_neumann_shape_functions_computed=False, neumann_flags=flags,
+                               applied_neumann=traction, is_body_force_shape_functions_computed=False)
+    mat.nvar, mat.ndim = 3, 3
+    fsf = form.function_spaces[-1]
+    Ft = AssembleExternalTractionForces(bc, mesh, mat, fsf)
+    Fb = AssembleBodyForces(bc, mesh, mat, form.function_spaces[0])
+    return dict(faces=faces, neumann_flags=flags, applied_neumann=traction, face_Bases=fsf.Bases,
+                face_AllGauss=np.ravel(fsf.AllGauss), face_Jm=fsf.Jm, F_traction=np.ravel(Ft), F_body=np.ravel(Fb),
+                rho_body=np.array(float(mat.rho)))
+
+
 def lumped_mass(F, form, mat, mesh, x):
     from Florence.FiniteElements.Assembly.Assembly import AssembleExplicit_NoLLD_Mass
     fs = form.function_spaces[0]
@@ -161,7 +181,7 @@ CASES = [
     dict(name="hex_p2_nh_q5", mesh="cube_hex", n=(2, 2, 2), p=2, material="NeoHookean", params=(1.0, 10.0), seed=11,
          amp=0.01, qdeg=5, emat=(0, 3, 7), mass=True, triplet=True),
     dict(name="hex_p2_mr", mesh="cube_hex", n=(2, 2, 1), p=2, material="MooneyRivlin", params=(0.5, 0.5, 20.0),
-         seed=12, amp=0.05, qdeg=None, emat=(0, 3), mass=False),
+         seed=12, amp=0.05, qdeg=None, emat=(0, 3), mass=False, forces=True),
     dict(name="box_hex_p2_nh_big", mesh="box_hex", L=(4.0, 1.0, 1.0), n=(4, 2, 2), p=2, material="NeoHookean",
          params=(1.0, 1000.0), seed=13, amp=0.02, qdeg=None, emat=(1,), mass=True),
     dict(name="hex_p3_nh", mesh="cube_hex", n=(1, 1, 2), p=3, material="NeoHookean", params=(1.3, 7.0), seed=14,
@@ -171,7 +191,7 @@ CASES = [
     dict(name="tet_p1_nh", mesh="cube_tet", n=(2, 2, 2), p=1, material="NeoHookean", params=(1.0, 10.0), seed=16,
          amp=0.01, qdeg=None, emat=(0, 5), mass=True),
     dict(name="tet_p2_mr", mesh="cube_tet", n=(1, 1, 1), p=2, material="MooneyRivlin", params=(0.5, 0.5, 20.0),
-         seed=17, amp=0.02, qdeg=None, emat=(0, 2), mass=True),
+         seed=17, amp=0.02, qdeg=None, emat=(0, 2), mass=True, forces=True),
     # linear analysis (no geometry update, no residual): at x = X the low-level and numpy paths agree
     # (the low-level kinematics take spatial gradients from x even without the update,
     # _KinematicMeasures_.h:95-103; the numpy path then takes material gradients)
@@ -218,6 +238,8 @@ def make_case(F, spec):
     out["emat_ids"] = np.array(emat, np.int64)
     out["emat_K"] = Ke
     out["emat_t"] = te
+    if spec.get("forces"):
+        out.update(reference_forces(F, spec, mesh, form, mat))
     if spec.get("mass"):
         rho = 1.0
         out["M_lumped"] = lumped_mass(F, form, mat, mesh, x)

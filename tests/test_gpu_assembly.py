@@ -410,3 +410,34 @@ def test_transversely_isotropic_material_needs_fibre_directions(fl):
                               tuple(d["params"]), mode="csr", orientations=d["orientations"][:, [1, 2, 0]])
     x = torch.from_numpy(d["Eulerx"]).cuda()
     assert rel_fro(asm2.assemble(x)[0].cpu().numpy(), d["K_data"]) > 1e-3
+
+
+@pytest.mark.parametrize("case", [c for c in golden_cases() if "F_traction" in load_golden(c)])
+def test_external_forces_match_reference(fl, case):
+    """AssembleExternalTractionForces / AssembleBodyForces on the device against the reference's
+    (parent-face weights, Assembly.py:451-560), and the physical-face option against a numpy
+    integral of the same faces."""
+    d = load_golden(case)
+    bc = types.SimpleNamespace(neumann_flags=d["neumann_flags"], applied_neumann=d["applied_neumann"])
+    mat = types.SimpleNamespace(ndim=3, nvar=3, rho=float(d["rho_body"]))
+    mesh = types.SimpleNamespace(points=d["points"], faces=d["faces"].astype(np.uint64),
+                                 elements=d["elements"].astype(np.uint64))
+    fsf = types.SimpleNamespace(Bases=d["face_Bases"], AllGauss=d["face_AllGauss"][:, None], Jm=d["face_Jm"])
+    fse = types.SimpleNamespace(Bases=d["Bases"], AllGauss=d["AllGauss"][:, None])
+    Ft = fl.AssembleExternalTractionForces(bc, mesh, mat, fsf)
+    Fb = fl.AssembleBodyForces(bc, mesh, mat, fse)
+    assert Ft.shape == (d["points"].shape[0] * 3, 1) and Fb.shape == Ft.shape
+    assert rel_fro(Ft.ravel(), d["F_traction"]) < 1e-14
+    assert rel_fro(Fb.ravel(), d["F_body"]) < 1e-14
+    # physical faces: w_g |dX/dxi x dX/deta|
+    Fp = fl.AssembleExternalTractionForces(bc, mesh, mat, fsf, physical_faces=True).ravel()
+    ref = np.zeros_like(Fp)
+    for f in np.nonzero(d["neumann_flags"])[0]:
+        X = d["points"][d["faces"][f]]
+        d0 = np.einsum("ag,ak->gk", d["face_Jm"][0], X)
+        d1 = np.einsum("ag,ak->gk", d["face_Jm"][1], X)
+        area = np.linalg.norm(np.cross(d0, d1), axis=1)
+        s = d["face_Bases"] @ (d["face_AllGauss"] * area)
+        for a, nd in enumerate(d["faces"][f]):
+            ref[3 * nd:3 * nd + 3] += d["applied_neumann"][f] * s[a]
+    assert rel_fro(Fp, ref) < 1e-13

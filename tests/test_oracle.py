@@ -127,3 +127,15 @@ def test_mlp_oracle_bf16_rounding_matches_torch():
     x = np.random.default_rng(1).normal(0, 3, 10000).astype(np.float32)
     ref = torch.from_numpy(x).to(torch.bfloat16).double().numpy()
     assert np.array_equal(M._bf16(x), ref)
+
+
+@pytest.mark.parametrize("case", [c for c in golden_cases() if "F_traction" in load_golden(c)])
+def test_external_forces(oracle, case):
+    """Surface traction and body force as the reference assembles them (Assembly.py:451-560)."""
+    d = load_golden(case)
+    n = d["points"].shape[0]
+    Ft = oracle.external_traction(d["faces"], d["neumann_flags"], d["applied_neumann"], d["face_Bases"],
+                                  d["face_AllGauss"], n)
+    Fb = oracle.body_forces(d["elements"], d["Bases"], d["AllGauss"], float(d["rho_body"]), n)
+    assert rel_fro(Ft, d["F_traction"]) < 1e-14
+    assert rel_fro(Fb, d["F_body"]) < 1e-14
