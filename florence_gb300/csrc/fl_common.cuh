@@ -263,4 +263,52 @@ __device__ __forceinline__ double kinematics(JmFn jm, const double *X, const dou
     return kinematics_fn<NPE>(jm, coords, w, update, G, F);
 }
 
+// Float-pair number hi + lo (|lo| <= ulp(hi) / 2) with FP32-pipe arithmetic: products error-free
+// in their leading part (fma), sums by Knuth's two-sum, ~2^-46 relative per operation. Used for
+// the Gauss-point tangent of the FP64 path and the float-pair explicit internal force, whose
+// FP64 forms would hold GB300's FP64 pipe.
+namespace fpair {  // its own namespace: the overloads are found by argument lookup only, so they
+                  // do not hide the FP64 fma of namespace fl's callers
+struct FloatPair {
+    float h, l;
+    FloatPair() = default;
+    __device__ constexpr FloatPair(float h_, float l_) : h(h_), l(l_) {}
+    __device__ explicit FloatPair(double x) : h((float)x), l((float)(x - (double)(float)x)) {}
+    __device__ explicit FloatPair(int x) : h((float)x), l(0.f) {}
+};
+__device__ __forceinline__ FloatPair df_renorm(float s, float e) {
+    const float h = s + e;
+    return FloatPair(h, e - (h - s));
+}
+__device__ __forceinline__ FloatPair operator+(FloatPair a, FloatPair b) {
+    const float s = a.h + b.h, bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb) + (a.l + b.l);
+    return df_renorm(s, e);
+}
+__device__ __forceinline__ FloatPair operator-(FloatPair a) { return FloatPair(-a.h, -a.l); }
+__device__ __forceinline__ FloatPair operator-(FloatPair a, FloatPair b) { return a + (-b); }
+__device__ __forceinline__ FloatPair &operator+=(FloatPair &a, FloatPair b) { return a = a + b; }
+__device__ __forceinline__ FloatPair operator*(FloatPair a, FloatPair b) {
+    const float p = a.h * b.h;
+    const float e = fmaf(a.h, b.h, -p) + fmaf(a.h, b.l, a.l * b.h);
+    return df_renorm(p, e);
+}
+__device__ __forceinline__ FloatPair fma(FloatPair a, FloatPair b, FloatPair c) {  // a b + c
+    const float p = a.h * b.h;
+    const float pe = fmaf(a.h, b.h, -p) + fmaf(a.h, b.l, a.l * b.h);
+    const float s = p + c.h, bb = s - p;
+    const float e = (p - (s - bb)) + (c.h - bb) + (pe + c.l);
+    return df_renorm(s, e);
+}
+}  // namespace fpair
+using fpair::FloatPair;
+namespace fpair {
+__device__ __forceinline__ FloatPair operator/(FloatPair a, FloatPair b) {  // a / b, one correction step
+    const float q1 = a.h / b.h;
+    const FloatPair r = a - FloatPair(q1, 0.f) * b;
+    return df_renorm(q1, r.h / b.h);
+}
+__device__ __forceinline__ double to_double(FloatPair a) { return (double)a.h + (double)a.l; }
+}  // namespace fpair
+
 }  // namespace fl

@@ -363,6 +363,144 @@ __global__ void __launch_bounds__(F32_NT) internal_force_f32_kernel(const uint64
     if (flag && flags) atomicOr(flags, flag);
 }
 
+// Float-pair internal force: the FP32 kernel's total-Lagrangian neo-Hookean force with every
+// quantity an unevaluated float pair (FloatPair, ~2^-46 relative per operation) on the FP32 pipe:
+// FP64-level results without FP64 instructions in the loops. Reference gradients come as hi / lo
+// float arrays and dV in FP64 (ref_grad_pair_kernel); T is accumulated in FP64.
+constexpr int PF_EPC = 4, PF_NT = 128;
+
+template <int NPE>
+__global__ void __launch_bounds__(128) ref_grad_pair_kernel(const double *points, const uint64_t *elements,
+                                                            const double *Jm, const double *w, int64_t nelem, int nq,
+                                                            int64_t nnode, float *gh, float *gl, double *dV,
+                                                            int *flags) {
+    const int64_t t = (int64_t)blockIdx.x * 128 + threadIdx.x;
+    if (t >= nelem * nq) return;
+    const int64_t e = t / nq;
+    const int g = (int)(t % nq);
+    double PX[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < NPE; ++a) {
+        uint64_t nd = elements[e * NPE + a];
+        if (nd >= (uint64_t)nnode) {
+            if (flags) atomicOr(flags, FL_FLAG_BAD_INDEX);
+            nd = 0;
+        }
+        for (int d = 0; d < 3; ++d) {
+            const double j = Jm[((size_t)d * NPE + a) * nq + g];
+            PX[d * 3] = fma(j, points[nd * 3], PX[d * 3]);
+            PX[d * 3 + 1] = fma(j, points[nd * 3 + 1], PX[d * 3 + 1]);
+            PX[d * 3 + 2] = fma(j, points[nd * 3 + 2], PX[d * 3 + 2]);
+        }
+    }
+    double iPX[9];
+    const double det = inv3(PX, iPX);
+    dV[t] = w[g] * fabs(det);
+    for (int a = 0; a < NPE; ++a) {
+        const double j0 = Jm[((size_t)0 * NPE + a) * nq + g], j1 = Jm[((size_t)1 * NPE + a) * nq + g],
+                     j2 = Jm[((size_t)2 * NPE + a) * nq + g];
+        for (int d = 0; d < 3; ++d) {
+            const double v = fma(iPX[d * 3], j0, fma(iPX[d * 3 + 1], j1, iPX[d * 3 + 2] * j2));
+            const float h = (float)v;
+            gh[((size_t)t * NPE + a) * 3 + d] = h;
+            gl[((size_t)t * NPE + a) * 3 + d] = (float)(v - (double)h);
+        }
+    }
+}
+
+template <int NPE>
+__global__ void __launch_bounds__(PF_NT) internal_force_pair_kernel(const uint64_t *elements, const double *u,
+                                                                     const float *gh, const float *gl,
+                                                                     const double *dV, int64_t nelem, int nq,
+                                                                     int64_t nnode, double mu_d, double lamb_d,
+                                                                     double *T, int *flags) {
+    using fpair::to_double;
+    __shared__ FloatPair us[PF_EPC][NPE * 3];
+    __shared__ FloatPair Ps[PF_EPC][32][9];  // first Piola stress x dV per Gauss point (nq <= 32)
+    __shared__ int nodes[PF_EPC][NPE];
+    const int64_t e0 = (int64_t)blockIdx.x * PF_EPC;
+    int flag = 0;
+    for (int idx = threadIdx.x; idx < PF_EPC * NPE; idx += PF_NT) {
+        const int s = idx / NPE, a = idx % NPE;
+        if (e0 + s >= nelem) continue;
+        uint64_t nd = elements[(e0 + s) * NPE + a];
+        if (nd >= (uint64_t)nnode) {
+            flag |= FL_FLAG_BAD_INDEX;
+            nd = 0;
+        }
+        nodes[s][a] = (int)nd;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) us[s][a * 3 + i] = FloatPair(u[nd * 3 + i]);
+    }
+    __syncthreads();
+    const FloatPair mu(mu_d), lamb(lamb_d), one(1), half(0.5), two(2);
+    for (int idx = threadIdx.x; idx < PF_EPC * nq; idx += PF_NT) {
+        const int s = idx / nq, g = idx % nq;
+        const int64_t e = e0 + s;
+        if (e >= nelem) continue;
+        const size_t base = ((size_t)(e * nq + g) * NPE) * 3;
+        FloatPair H[9];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) H[k] = FloatPair(0.f, 0.f);
+        for (int a = 0; a < NPE; ++a) {
+            const FloatPair g0(gh[base + a * 3], gl[base + a * 3]), g1(gh[base + a * 3 + 1], gl[base + a * 3 + 1]),
+                g2(gh[base + a * 3 + 2], gl[base + a * 3 + 2]);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const FloatPair ui = us[s][a * 3 + i];
+                H[i * 3] = fma(ui, g0, H[i * 3]);
+                H[i * 3 + 1] = fma(ui, g1, H[i * 3 + 1]);
+                H[i * 3 + 2] = fma(ui, g2, H[i * 3 + 2]);
+            }
+        }
+        const FloatPair trH = H[0] + H[4] + H[8];
+        const FloatPair trH2 = H[0] * H[0] + H[4] * H[4] + H[8] * H[8] + two * (H[1] * H[3] + H[2] * H[6] + H[5] * H[7]);
+        FloatPair cH[9];  // cofactor of H
+        cH[0] = H[4] * H[8] - H[5] * H[7];
+        cH[1] = H[5] * H[6] - H[3] * H[8];
+        cH[2] = H[3] * H[7] - H[4] * H[6];
+        cH[3] = H[2] * H[7] - H[1] * H[8];
+        cH[4] = H[0] * H[8] - H[2] * H[6];
+        cH[5] = H[1] * H[6] - H[0] * H[7];
+        cH[6] = H[1] * H[5] - H[2] * H[4];
+        cH[7] = H[2] * H[3] - H[0] * H[5];
+        cH[8] = H[0] * H[4] - H[1] * H[3];
+        const FloatPair detH = H[0] * cH[0] + H[1] * cH[1] + H[2] * cH[2];
+        const FloatPair q = half * (trH * trH - trH2) + detH;
+        const FloatPair j = trH + q;
+        const FloatPair J = one + j;
+        if (!(J.h > 0.f)) flag |= FL_FLAG_NONPOSITIVE_J;
+        const FloatPair a1 = mu / J, a2 = lamb * j;
+        const FloatPair dv(dV[e * nq + g]);
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                FloatPair A = H[r * 3 + c] + H[c * 3 + r] + j * H[r * 3 + c] - cH[r * 3 + c];
+                FloatPair cofF = cH[r * 3 + c] - H[c * 3 + r];
+                if (r == c) {
+                    A = A + q;
+                    cofF = cofF + one + trH;
+                }
+                Ps[s][g][r * 3 + c] = (a1 * A + a2 * cofF) * dv;
+            }
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < PF_EPC * NPE * 3; idx += PF_NT) {
+        const int s = idx / (NPE * 3), r = idx % (NPE * 3), a = r / 3, i = r % 3;
+        const int64_t e = e0 + s;
+        if (e >= nelem) continue;
+        FloatPair t(0.f, 0.f);
+        for (int g = 0; g < nq; ++g) {
+            const size_t o = ((size_t)(e * nq + g) * NPE + a) * 3;
+            t = fma(Ps[s][g][i * 3], FloatPair(gh[o], gl[o]), t);
+            t = fma(Ps[s][g][i * 3 + 1], FloatPair(gh[o + 1], gl[o + 1]), t);
+            t = fma(Ps[s][g][i * 3 + 2], FloatPair(gh[o + 2], gl[o + 2]), t);
+        }
+        atomicAdd(T + 3 * (int64_t)nodes[s][a] + i, to_double(t));
+    }
+    if (flag && flags) atomicOr(flags, flag);
+}
+
 // leapfrog central difference: a = (F - T)/M on free dofs, v += dt a, u += dt v
 template <class TT>
 __global__ void cd_update_kernel(int64_t n, double dt, const TT *T, const double *Fext, const double *Minv,
@@ -453,6 +591,51 @@ int fl_InternalForceF32(const uint64_t *elements, const double *u, const float *
         fl::internal_force_f32_kernel<N><<<grid, fl::F32_NT, 0, s>>>(elements, u, grad0, dV, nelem,         \
                                                                      (int)ngauss, nnode, (float)mu,         \
                                                                      (float)lamb, T, flags);                \
+        break;
+        FL_NPE_CASES(FL_CASE)
+#undef FL_CASE
+        default: return FL_ERR_UNSUPPORTED;
+    }
+    return fl::launch_status();
+}
+
+int fl_ReferenceGradientsPair(const double *points, const uint64_t *elements, const double *Jm,
+                              const double *AllGauss, int64_t ngauss, int64_t nelem, int64_t nodeperelem,
+                              int64_t nnode, float *grad0_hi, float *grad0_lo, double *dV, int *flags,
+                              fl_stream_t stream) {
+    if (nelem < 0 || ngauss <= 0 || nnode <= 0) return FL_ERR_ARG;
+    if (nelem == 0) return FL_OK;
+    if (!points || !elements || !Jm || !AllGauss || !grad0_hi || !grad0_lo || !dV) return FL_ERR_ARG;
+    const unsigned grid = (unsigned)((nelem * ngauss + 127) / 128);
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (nodeperelem) {
+#define FL_CASE(N)                                                                                             \
+    case N:                                                                                                    \
+        fl::ref_grad_pair_kernel<N><<<grid, 128, 0, s>>>(points, elements, Jm, AllGauss, nelem, (int)ngauss,  \
+                                                         nnode, grad0_hi, grad0_lo, dV, flags);                \
+        break;
+        FL_NPE_CASES(FL_CASE)
+#undef FL_CASE
+        default: return FL_ERR_UNSUPPORTED;
+    }
+    return fl::launch_status();
+}
+
+int fl_InternalForcePair(const uint64_t *elements, const double *u, const float *grad0_hi, const float *grad0_lo,
+                         const double *dV, int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode,
+                         int material_number, double mu, double lamb, double *T, int *flags, fl_stream_t stream) {
+    if (material_number != FL_MATERIAL_NEOHOOKEAN) return FL_ERR_UNSUPPORTED;
+    if (nelem < 0 || ngauss <= 0 || ngauss > 32 || nnode <= 0) return ngauss > 32 ? FL_ERR_UNSUPPORTED : FL_ERR_ARG;
+    if (nelem == 0) return FL_OK;
+    if (!elements || !u || !grad0_hi || !grad0_lo || !dV || !T) return FL_ERR_ARG;
+    const unsigned grid = (unsigned)((nelem + fl::PF_EPC - 1) / fl::PF_EPC);
+    cudaStream_t s = (cudaStream_t)stream;
+    switch (nodeperelem) {
+#define FL_CASE(N)                                                                                          \
+    case N:                                                                                                 \
+        fl::internal_force_pair_kernel<N><<<grid, fl::PF_NT, 0, s>>>(elements, u, grad0_hi, grad0_lo, dV,   \
+                                                                     nelem, (int)ngauss, nnode, mu, lamb,   \
+                                                                     T, flags);                             \
         break;
         FL_NPE_CASES(FL_CASE)
 #undef FL_CASE

@@ -12,9 +12,11 @@ the internal-force kernel (the reference has no CFL estimate), and energy bookke
 textbook central-difference velocity v_n = (u_{n+1} - u_{n-1}) / (2 dt) (the reference computes
 (U + U0)/(2 dt) at :152, which only feeds its own energy output).
 
-Internal force per step: FP64 (fl_GlobalAssemblyExplicit_DF_DPF_, the reference's algorithm) or
-FP32 (fl_InternalForceF32, total-Lagrangian form with precomputed FP32 reference gradients,
-FP32 accumulation); the state u, v stays FP64 in both. Steps are captured in CUDA graphs.
+Internal force per step: FP64 (fl_GlobalAssemblyExplicit_DF_DPF_, the reference's algorithm),
+float pairs (fl_InternalForcePair: the total-Lagrangian form in float-pair arithmetic on the FP32
+pipe, FP64-level results) or FP32 (fl_InternalForceF32, the same form with FP32 reference
+gradients and accumulation); the state u, v stays FP64 in all three. Steps are captured in CUDA
+graphs.
 """
 import ctypes
 import time
@@ -44,6 +46,12 @@ class ExplicitSolver:
         N.check(L.fl_ReferenceGradients(_ptr(a.points), _ptr(a.elements), _ptr(a.Jm), _ptr(a.w), a.nq, a.nelem,
                                         a.npe, a.nnode, _ptr(self.grad0), _ptr(self.dV), _ptr(a.flags), _stream()),
                 "fl_ReferenceGradients")
+        self.gh = torch.empty(a.nelem * a.nq * a.npe * 3, dtype=torch.float32, device=a.device)
+        self.gl = torch.empty_like(self.gh)
+        self.dV64 = torch.empty(a.nelem * a.nq, dtype=torch.float64, device=a.device)
+        N.check(L.fl_ReferenceGradientsPair(_ptr(a.points), _ptr(a.elements), _ptr(a.Jm), _ptr(a.w), a.nq, a.nelem,
+                                            a.npe, a.nnode, _ptr(self.gh), _ptr(self.gl), _ptr(self.dV64),
+                                            _ptr(a.flags), _stream()), "fl_ReferenceGradientsPair")
         self.T64 = torch.zeros(self.n, dtype=torch.float64, device=a.device)
         self.T32 = torch.zeros(self.n, dtype=torch.float32, device=a.device)
         self.energy = torch.zeros(1, dtype=torch.float64, device=a.device)
@@ -54,6 +62,13 @@ class ExplicitSolver:
         if mode == "fp64":
             self.T64.zero_()
             a.internal_force((self.X + u).reshape(-1, 3), T=self.T64)
+            return self.T64
+        if mode == "pair":
+            self.T64.zero_()
+            N.check(N.lib().fl_InternalForcePair(_ptr(a.elements), _ptr(u), _ptr(self.gh), _ptr(self.gl),
+                                                 _ptr(self.dV64), a.nq, a.nelem, a.npe, a.nnode,
+                                                 N.FL_MATERIAL_NEOHOOKEAN, self.mu, self.lamb, _ptr(self.T64),
+                                                 _ptr(a.flags), _stream()), "fl_InternalForcePair")
             return self.T64
         self.T32.zero_()
         N.check(N.lib().fl_InternalForceF32(_ptr(a.elements), _ptr(u), _ptr(self.grad0), _ptr(self.dV), a.nq,

@@ -270,6 +270,18 @@ int fl_ReferenceGradients(const double *points, const uint64_t *elements, const 
 int fl_InternalForceF32(const uint64_t *elements, const double *u, const float *grad0, const float *dV,
                         int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode, int material_number,
                         double mu, double lamb, float *T, int *flags, fl_stream_t stream);
+/* Float-pair variant (no reference counterpart): the same total-Lagrangian neo-Hookean force with
+ * every quantity carried as an unevaluated pair of floats on the FP32 pipe (~2^-46 relative per
+ * operation, FP64-level results). fl_ReferenceGradientsPair writes dN_a/dX as grad0_hi + grad0_lo
+ * (FP32 arrays, layout of grad0 above) and dV in FP64; fl_InternalForcePair accumulates
+ * T [nnode*3] (FP64) +=. ngauss <= 32. */
+int fl_ReferenceGradientsPair(const double *points, const uint64_t *elements, const double *Jm,
+                              const double *AllGauss, int64_t ngauss, int64_t nelem, int64_t nodeperelem,
+                              int64_t nnode, float *grad0_hi, float *grad0_lo, double *dV, int *flags,
+                              fl_stream_t stream);
+int fl_InternalForcePair(const uint64_t *elements, const double *u, const float *grad0_hi, const float *grad0_lo,
+                         const double *dV, int64_t ngauss, int64_t nelem, int64_t nodeperelem, int64_t nnode,
+                         int material_number, double mu, double lamb, double *T, int *flags, fl_stream_t stream);
 int fl_CentralDifferenceUpdate(int64_t n, double dt, const void *T, int T_is_f32, const double *Fext,
                                const double *Minv, const int8_t *fixed, double *u, double *v, fl_stream_t stream);
 int fl_StrainEnergy(const double *points, const uint64_t *elements, const double *Eulerx, const double *Jm,

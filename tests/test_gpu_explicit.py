@@ -1,7 +1,8 @@
 """GPU tests of the explicit-dynamics building blocks and the time loop.
 
 * FP32 internal force (total-Lagrangian, FP32 accumulation) against the reference's residual:
-  within 2e-6 relative (FP32 arithmetic);
+  within 2e-6 relative (FP32 arithmetic); the float-pair variant of the same form within 1e-12
+  (the FP64 bar);
 * reference gradients and the strain energy against numpy restatements;
 * the FP64 time loop (CUDA graphs) against a CPU leapfrog built on the oracle's internal force
   and lumped mass: within 1e-10 relative after 200 steps;
@@ -42,6 +43,8 @@ def test_f32_internal_force_matches_reference(box):
     assert rel_fro(T32, d["T"]) < 2e-6
     T64 = s.internal_force(u, "fp64").cpu().numpy()
     assert rel_fro(T64, d["T"]) < 1e-12
+    Tp = s.internal_force(u, "pair").cpu().numpy()
+    assert rel_fro(Tp, d["T"]) < 1e-12
     s.asm.check_flags()
 
 
@@ -122,7 +125,10 @@ def test_energy_and_fp32_trajectory(small_beam):
     v0[:, 2] = 0.1 * np.sin(np.pi * P[:, 0] / 2.0)
     r64 = s.run(v0.ravel(), dt, 2000, mode="fp64", energy_every=100)
     r32 = s.run(v0.ravel(), dt, 2000, mode="fp32", energy_every=100)
-    for r in (r64, r32):
+    rp = s.run(v0.ravel(), dt, 2000, mode="pair", energy_every=100)
+    # the float-pair trajectory stays on the FP64 one
+    assert rel_fro(rp["u"].cpu().numpy(), r64["u"].cpu().numpy()) < 1e-9
+    for r in (r64, r32, rp):
         assert not r["blowup"]
         E = np.array([k + i for _, k, i in r["energy"]])
         assert np.abs(E / E[0] - 1.0).max() < 5e-3          # central difference: bounded oscillation
