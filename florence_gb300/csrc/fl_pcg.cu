@@ -9,6 +9,10 @@
 // rows and columns replaced by the identity. This is CG on the reduced system K_ff, with the
 // matrix left as assembled.
 //
+// With the float-pair products (split FP64 values, or FP32 values) the iteration vectors x, r, z, p
+// and the block inverses are float pairs as well (pcg_k2_pair, pcg_k3_pair), converted from and
+// to FP64 once per solve.
+//
 // One iteration = three kernels:
 //   K1  q = K p, p.q
 //   K2  alpha = rz_k / p.q;  x += alpha p;  r -= alpha q;  z = B^-1 r;  r.z and r.r
@@ -43,6 +47,9 @@ struct PcgState {
     float *qh, *ql;                // q = K p as a float pair, written by the float-pair products
     double *acc;                   // [0] p.q, [1],[2] r.z of even/odd iterates, [3] r.r, [4] |b|^2
     int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
+    // float-pair iteration vectors (with the float-pair products): x, r, z as hi/lo floats [n],
+    // the block inverses as hi/lo floats [n/3][9]
+    float *xh, *xl, *rh, *rl, *zh, *zl, *Bh, *Bl;
 };
 
 static size_t pcg_layout(int64_t n, int64_t nnz, PcgState *s, char *base, float2 **vsplit = nullptr) {
@@ -62,6 +69,14 @@ static size_t pcg_layout(int64_t n, int64_t nnz, PcgState *s, char *base, float2
     t.pl = (float *)take(sizeof(float) * n);
     t.qh = (float *)take(sizeof(float) * n);
     t.ql = (float *)take(sizeof(float) * n);
+    t.xh = (float *)take(sizeof(float) * n);
+    t.xl = (float *)take(sizeof(float) * n);
+    t.rh = (float *)take(sizeof(float) * n);
+    t.rl = (float *)take(sizeof(float) * n);
+    t.zh = (float *)take(sizeof(float) * n);
+    t.zl = (float *)take(sizeof(float) * n);
+    t.Bh = (float *)take(sizeof(float) * (n / 3) * 9);
+    t.Bl = (float *)take(sizeof(float) * (n / 3) * 9);
     t.acc = (double *)take(sizeof(double) * 8);
     t.done = (int *)take(sizeof(int) * 4);
     float2 *vs = (float2 *)take(sizeof(float2) * (size_t)nnz);
@@ -460,6 +475,109 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, 
     }
 }
 
+// Float-pair iteration (with the float-pair products): x, r, z, p and the block inverses as
+// unevaluated float pairs, every update on the FP32 pipe (~2^-46 relative per operation); the
+// FP64 pipe, which bounds pcg_k2 / pcg_k3 on GB300, only forms one partial dot product per thread.
+
+// x, r, z (FP64, from pcg_init / pcg_init2) and B^-1 -> float pairs
+__global__ void __launch_bounds__(PCG_NT) pcg_to_pairs(int64_t n, const double *x, PcgState s) {
+    for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT) {
+        const FloatPair xv(x[d]), rv(s.r[d]), zv(s.z[d]);
+        s.xh[d] = xv.h; s.xl[d] = xv.l;
+        s.rh[d] = rv.h; s.rl[d] = rv.l;
+        s.zh[d] = zv.h; s.zl[d] = zv.l;
+        for (int k = 0; k < 3; ++k) {
+            const FloatPair bv(s.Binv[d * 3 + k]);
+            s.Bh[d * 3 + k] = bv.h;
+            s.Bl[d * 3 + k] = bv.l;
+        }
+    }
+}
+
+// x (float pairs) -> x (FP64), at the end of a solve
+__global__ void __launch_bounds__(PCG_NT) pcg_from_pairs(int64_t n, double *x, PcgState s) {
+    for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT)
+        x[d] = (double)s.xh[d] + (double)s.xl[d];
+}
+
+// K2 in float pairs: x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r (layout as pcg_k2)
+__global__ void __launch_bounds__(PCG_NT) pcg_k2_pair(int64_t nnode, int k, PcgState s) {
+    __shared__ double s_alpha;
+    __shared__ int s_done;
+    if (threadIdx.x == 0) {
+        s_done = s.done[0];
+        s_alpha = s_done ? 0.0 : s.acc[1 + (k & 1)] / s.acc[0];
+    }
+    __syncthreads();
+    if (s_done) return;
+    const FloatPair alpha(s_alpha), nalpha(-s_alpha);
+    const int lane = threadIdx.x & 31, ln = lane / 3, i = lane % 3, l0 = 3 * ln;
+    const int64_t warp = (blockIdx.x * (int64_t)PCG_NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * PCG_NT) >> 5;
+    FloatPair rz(0.f, 0.f), rr(0.f, 0.f);
+    for (int64_t base = warp * 10; base < nnode; base += nwarps * 10) {  // warp-uniform trip count
+        const int64_t m = base + ln;
+        const bool valid = lane < 30 && m < nnode;
+        const int64_t d = 3 * m + i;
+        FloatPair rv(0.f, 0.f);
+        if (valid) {
+            const FloatPair p(s.ph[d], s.pl[d]), q(s.qh[d], s.ql[d]);
+            const FloatPair xv = fma(alpha, p, FloatPair(s.xh[d], s.xl[d]));
+            s.xh[d] = xv.h;
+            s.xl[d] = xv.l;
+            rv = fma(nalpha, q, FloatPair(s.rh[d], s.rl[d]));
+            s.rh[d] = rv.h;
+            s.rl[d] = rv.l;
+        }
+        FloatPair r3[3];
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            r3[j] = FloatPair(__shfl_sync(0xffffffffu, rv.h, (l0 + j) & 31), __shfl_sync(0xffffffffu, rv.l, (l0 + j) & 31));
+        if (valid) {
+            const int64_t b = m * 9 + i * 3;
+            FloatPair z = FloatPair(s.Bh[b], s.Bl[b]) * r3[0];
+            z = fma(FloatPair(s.Bh[b + 1], s.Bl[b + 1]), r3[1], z);
+            z = fma(FloatPair(s.Bh[b + 2], s.Bl[b + 2]), r3[2], z);
+            s.zh[d] = z.h;
+            s.zl[d] = z.l;
+            rz = fma(rv, z, rz);
+            rr = fma(rv, rv, rr);
+        }
+    }
+    block_atomic_add(fpair::to_double(rz), s.acc + 1 + ((k + 1) & 1));
+    block_atomic_add(fpair::to_double(rr), s.acc + 3);
+}
+
+// K3 in float pairs: p = z + beta p (written straight as the product's float pair), convergence
+__global__ void __launch_bounds__(PCG_NT) pcg_k3_pair(int64_t n, int k, double tol2, PcgState s) {
+    __shared__ double s_beta;
+    __shared__ int s_done;
+    if (threadIdx.x == 0) {
+        s_done = s.done[0];
+        s_beta = s_done ? 0.0 : s.acc[1 + ((k + 1) & 1)] / s.acc[1 + (k & 1)];
+    }
+    __syncthreads();
+    if (s_done) return;
+    const FloatPair beta(s_beta);
+    const double rr = s.acc[3];
+    for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT) {
+        const FloatPair pv = fma(beta, FloatPair(s.ph[d], s.pl[d]), FloatPair(s.zh[d], s.zl[d]));
+        s.ph[d] = pv.h;
+        s.pl[d] = pv.l;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        s.acc[0] = 0.0;  // p.q of the next iterate (K2, the only reader, has finished)
+        if (rr <= tol2) {
+            s.done[0] = 1;
+            s.done[1] = k + 1;
+        } else if (!isfinite(rr)) {
+            s.done[0] = 1;
+            s.done[1] = k + 1;
+            s.done[2] |= 4;
+        }
+    }
+}
+
 // Resident blocks of a kernel over the whole GPU (one wave), for grid sizes of the grid-stride
 // kernels.
 template <auto Kernel>
@@ -597,6 +715,9 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
         FL_CUDA_TRY(cudaMemsetAsync(s.acc, 0, sizeof(double), st));  // p.q of the timed products
     }
     const double tol2 = rtol * rtol * b2;
+    // with the float-pair products the iteration vectors are float pairs too
+    const bool pairs = nodeblk && (split || sizeof(VT) == 4);
+    if (pairs) pcg_to_pairs<<<g_dofs, PCG_NT, 0, st>>>(n, x, s);
     int hd[4] = {0, 0, 0, 0};
     int64_t k = 0;
     while (k < maxiter) {
@@ -605,14 +726,20 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
             if (split) launch_k1_nb<float2>(nb, indptr, indices, vsplit, fixed, n, (int)k, s, st);
             else if (nodeblk) launch_k1_nb<VT>(nb, indptr, indices, vals, fixed, n, (int)k, s, st);
             else pcg_k1<VT, false><<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
-            pcg_k2<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, x, s, (nodeblk && (split || sizeof(VT) == 4)) ? 1 : 0);
-            pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, (sizeof(VT) == 4 || split) ? 1 : 0, s);
+            if (pairs) {
+                pcg_k2_pair<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, s);
+                pcg_k3_pair<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, s);
+            } else {
+                pcg_k2<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, x, s, 0);
+                pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, 0, s);
+            }
         }
         FL_CUDA_TRY(cudaGetLastError());
         FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
         FL_CUDA_TRY(cudaStreamSynchronize(st));
         if (hd[0]) break;
     }
+    if (pairs) pcg_from_pairs<<<g_dofs, PCG_NT, 0, st>>>(n, x, s);
     FL_CUDA_TRY(cudaMemcpyAsync(hacc, s.acc, sizeof(hacc), cudaMemcpyDeviceToHost, st));
     FL_CUDA_TRY(cudaStreamSynchronize(st));
     *iters = hd[0] ? hd[1] : maxiter;
