@@ -65,6 +65,10 @@ struct AsmArgs {
     MatParams mp;
     const double *eparams;  // optional per-element material parameters [nelem][3] (overrides mp)
     const double *orient;   // fibre direction per element [nelem][3] (transversely isotropic material)
+    // float-pair kinematics (optional): per node X hi, X lo, u hi, u lo [nnode][12] floats, and
+    // the shape-function gradients as pairs [3][npe][nq]
+    const float *npair;
+    const float2 *jmp;
     int *flags;
     double *Q;       // scratch [QSTRIDE][ldq]
     float *Qf;       // split-BF16 path: FP32 tangent part [45][ldq] (Q then holds S [9][ldq])
@@ -225,7 +229,27 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
             x0 = __ldg(A.Eulerx + nd * 3); x1 = __ldg(A.Eulerx + nd * 3 + 1); x2 = __ldg(A.Eulerx + nd * 3 + 2);
         };
         double G[9], F[9];
-        const double detJ = kinematics_fn<NPE>(jm, coords, __ldg(A.w + g), A.update, G, F);
+        double detJ;
+        if (A.npair) {  // coordinate sums as float pairs (FP32 pipe)
+            auto jp = [&](int d, int a) {
+                const float2 v = __ldg(A.jmp + ((size_t)d * NPE + a) * nq + g);
+                return FloatPair(v.x, v.y);
+            };
+            auto nodep = [&](int a, FloatPair *X, FloatPair *U) {
+                uint64_t nd = __ldg(el + a);
+                if (nd >= (uint64_t)A.nnode) {
+                    flag |= FL_FLAG_BAD_INDEX;
+                    nd = 0;
+                }
+                const float4 *q = reinterpret_cast<const float4 *>(A.npair + nd * 12);
+                const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
+                X[0] = FloatPair(q0.x, q1.y); X[1] = FloatPair(q0.y, q1.z); X[2] = FloatPair(q0.z, q1.w);
+                U[0] = FloatPair(q0.w, q2.y); U[1] = FloatPair(q1.x, q2.z); U[2] = FloatPair(q2.x, q2.w);
+            };
+            detJ = kinematics_pair<NPE>(jp, nodep, __ldg(A.w + g), A.update, G, F);
+        } else {
+            detJ = kinematics_fn<NPE>(jm, coords, __ldg(A.w + g), A.update, G, F);
+        }
         double sig[6], b[6], J, c1, c2, cbb;
         MatParams mp = A.mp;
         if (A.eparams) mp = MatParams{__ldg(A.eparams + e * 3), __ldg(A.eparams + e * 3 + 1), __ldg(A.eparams + e * 3 + 2), 0.0};
@@ -556,6 +580,49 @@ static int64_t chunk_elements(size_t bytes, int nq, int epc) {
 // faster of the two on GB300, within the FP64 path's accuracy bar
 static std::atomic<int> g_arith{FL_ARITH_FLOAT_PAIR};
 
+// Float-pair kinematics inputs, once per assembly call: per node the reference coordinates X and
+// the displacement u = x - X (formed in FP64) as float pairs, 12 floats in three float4 words
+// (Xh0 Xh1 Xh2 Uh0 | Uh1 Xl0 Xl1 Xl2 | Uh2 Ul0 Ul1 Ul2), and the shape-function gradients as
+// (hi, lo) pairs.
+__global__ void node_pairs_kernel(const double *points, const double *Eulerx, int64_t nnode, float *out) {
+    const int64_t n = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (n >= nnode) return;
+    FloatPair X[3], U[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const double xv = points[n * 3 + k];
+        X[k] = FloatPair(xv);
+        U[k] = FloatPair(Eulerx[n * 3 + k] - xv);
+    }
+    float4 *o = reinterpret_cast<float4 *>(out + n * 12);
+    o[0] = make_float4(X[0].h, X[1].h, X[2].h, U[0].h);
+    o[1] = make_float4(U[1].h, X[0].l, X[1].l, X[2].l);
+    o[2] = make_float4(U[2].h, U[0].l, U[1].l, U[2].l);
+}
+
+__global__ void jm_pairs_kernel(const double *Jm, float2 *out, int64_t n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const FloatPair v(Jm[i]);
+    out[i] = make_float2(v.h, v.l);
+}
+
+static size_t pair_prep_bytes(int64_t nnode, int npe, int nq) {
+    return ((sizeof(float) * 12 * (size_t)nnode + 255) & ~(size_t)255) +
+           ((sizeof(float2) * 3 * (size_t)npe * nq + 255) & ~(size_t)255);
+}
+
+// fills the float-pair kinematics inputs at `base` (pair_prep_bytes long) and points A at them
+static void pair_prep(AsmArgs &A, int npe, char *base, cudaStream_t stream) {
+    float *np = reinterpret_cast<float *>(base);
+    float2 *jp = reinterpret_cast<float2 *>(base + ((sizeof(float) * 12 * (size_t)A.nnode + 255) & ~(size_t)255));
+    const int64_t nj = (int64_t)3 * npe * A.nq;
+    node_pairs_kernel<<<(unsigned)((A.nnode + 255) / 256), 256, 0, stream>>>(A.points, A.Eulerx, A.nnode, np);
+    jm_pairs_kernel<<<(unsigned)((nj + 255) / 256), 256, 0, stream>>>(A.Jm, jp, nj);
+    A.npair = np;
+    A.jmp = jp;
+}
+
 // Runs A and B over [0, nelem) in chunks of at most `chunk` elements through scratch Q.
 template <int NPE, int MAT, bool DF>
 static int run_chunks_t(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) {
@@ -672,6 +739,8 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.Q = nullptr;
     A.Qf = nullptr;
     A.orient = mat == ANISOTROPICMR1 ? orient : nullptr;
+    A.npair = nullptr;
+    A.jmp = nullptr;
     A.e0 = A.ne = A.ldq = 0;
     A.qc = 1;
     if (recompute_sparsity_pattern) {
@@ -1260,11 +1329,13 @@ static int launch_mixed(AsmArgs A, float *V32, cudaStream_t stream) {
     const size_t fbytes = (sizeof(float) * 45 * (size_t)A.nq * chunk + 255) & ~(size_t)255;
     const int64_t nj4 = (int64_t)(A.nq + 4) * NPE;
     double *Q = nullptr;
-    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sbytes + fbytes + sizeof(float4) * (size_t)nj4, stream));
+    const size_t j4bytes = (sizeof(float4) * (size_t)nj4 + 255) & ~(size_t)255;
+    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sbytes + fbytes + j4bytes + pair_prep_bytes(A.nnode, NPE, A.nq), stream));
     A.Q = Q;
     A.Qf = reinterpret_cast<float *>(reinterpret_cast<char *>(Q) + sbytes);
     A.ldq = chunk * A.nq;
     float4 *J4 = reinterpret_cast<float4 *>(reinterpret_cast<char *>(Q) + sbytes + fbytes);
+    pair_prep(A, NPE, reinterpret_cast<char *>(Q) + sbytes + fbytes + j4bytes, stream);
     jm_float4<<<(unsigned)((nj4 + 255) / 256), 256, 0, stream>>>(A.Jm, J4, NPE, A.nq);
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -1820,7 +1891,8 @@ static int launch_oz(AsmArgs A, cudaStream_t stream) {
     const int64_t nj4 = (int64_t)(A.nq + 4) * NPE;
     const size_t jbytes = (sizeof(float4) * (size_t)nj4 + 255) & ~(size_t)255;
     double *Q = nullptr;
-    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sbytes + fbytes + 2 * jbytes, stream));
+    FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sbytes + fbytes + 2 * jbytes + pair_prep_bytes(A.nnode, NPE, A.nq), stream));
+    pair_prep(A, NPE, reinterpret_cast<char *>(Q) + sbytes + fbytes + 2 * jbytes, stream);
     A.Q = Q;
     A.Qf = reinterpret_cast<float *>(reinterpret_cast<char *>(Q) + sbytes);
     A.ldq = chunk * A.nq;
@@ -1950,6 +2022,8 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.Q = nullptr;
     A.Qf = nullptr;
     A.orient = nullptr;
+    A.npair = nullptr;
+    A.jmp = nullptr;
     A.e0 = A.ne = A.ldq = 0;
     int mat = 0;
     if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &A.mp, mu3) != FL_OK) return FL_ERR_UNSUPPORTED;

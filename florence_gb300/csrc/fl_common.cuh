@@ -302,6 +302,46 @@ __device__ __forceinline__ FloatPair fma(FloatPair a, FloatPair b, FloatPair c) 
 }
 }  // namespace fpair
 using fpair::FloatPair;
+// kinematics_fn with the coordinate sums in float-pair arithmetic on the FP32 pipe: PX = sum_a
+// dN_a/dxi X_a and Pu = sum_a dN_a/dxi u_a (u = x - X, so small strains keep their relative
+// precision) from float-pair gradients jp(d, a) and node data nodep(a, X, u); both sums are then
+// taken to FP64 (Px = PX + Pu) and the rest is kinematics_fn's FP64 code.
+template <int NPE, class JpFn, class NodeFn>
+__device__ __forceinline__ double kinematics_pair(JpFn jp, NodeFn nodep, double w, int update, double *G, double *F) {
+    FloatPair PXp[9], Pup[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) PXp[k] = Pup[k] = FloatPair(0.f, 0.f);
+#pragma unroll 2
+    for (int a = 0; a < NPE; ++a) {
+        FloatPair X[3], U[3];
+        nodep(a, X, U);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const FloatPair j = jp(d, a);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                PXp[d * 3 + k] = fma(j, X[k], PXp[d * 3 + k]);
+                Pup[d * 3 + k] = fma(j, U[k], Pup[d * 3 + k]);
+            }
+        }
+    }
+    double PX[9], Px[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+        PX[k] = (double)PXp[k].h + (double)PXp[k].l;
+        Px[k] = PX[k] + ((double)Pup[k].h + (double)Pup[k].l);
+    }
+    double iPX[9];
+    const double detX = inv3(PX, iPX);
+    const double detx = inv3(Px, G);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            F[i * 3 + j] = Px[0 * 3 + i] * iPX[j * 3 + 0] + Px[1 * 3 + i] * iPX[j * 3 + 1] + Px[2 * 3 + i] * iPX[j * 3 + 2];
+    return update ? w * fabs(detx) : w * fabs(detX);
+}
+
 namespace fpair {
 __device__ __forceinline__ FloatPair operator/(FloatPair a, FloatPair b) {  // a / b, one correction step
     const float q1 = a.h / b.h;

@@ -70,8 +70,8 @@ def test_csr_assembly_matches_reference(fl, case, mode):
 def test_both_contraction_arithmetics_match_reference(fl, case, mode):
     """The contraction in FP64 multiply-adds and in float-pair arithmetic on the FP32 pipe (the
     default; every other test runs it) both meet the FP64 path's bar (1e-12 relative Frobenius
-    against the reference) in every scatter mode; the residual is formed in FP64 either way (the
-    two agree up to the order of the atomic sums)."""
+    against the reference) in every scatter mode; the residual is formed in FP64 either way from
+    kinematics summed in FP64 or in float pairs (the two agree to ~1e-14)."""
     d = load_golden(case)
     asm = _asm(fl, d, mode)
     x = torch.from_numpy(d["Eulerx"]).cuda()
@@ -90,7 +90,7 @@ def test_both_contraction_arithmetics_match_reference(fl, case, mode):
         assert rel_fro(out64[0].cpu().numpy(), d["K_data"]) < TOL
     asm.check_flags()
     V, T = out[-2], out[-1]
-    assert rel_fro(T.cpu().numpy(), out64[-1].cpu().numpy()) < 1e-14
+    assert rel_fro(T.cpu().numpy(), out64[-1].cpu().numpy()) < 1e-13
     assert rel_fro(T.cpu().numpy(), d["T"]) < TOL
     if mode == "triplet":
         I, J = out[0].cpu().numpy(), out[1].cpu().numpy()
