@@ -689,6 +689,79 @@ def run_warmstart(args):
     print(json.dumps(line), flush=True)
 
 
+def run_meshing(args):
+    """High-order tet mesh generation on the device (fl_RaiseTetOrder): a box of Kuhn-split cubes
+    (10.6 M linear tets, 1.8 M vertices) raised to p=3 with the equispaced 20-node layout. One
+    step = one call with preallocated outputs (counting, entity numbering, node numbers and
+    positions, two host synchronisations). value = linear tets per second; e2e = the same call from host
+    numpy arrays with the mesh copied back; cpu_baseline = the host builder (numpy, one thread)
+    on a 24 x 24 x 24 box."""
+    import itertools
+    import torch
+    from florence_gb300 import meshes
+    cells = (192, 96, 96) if args.workload != "beam_s" else (48, 24, 24)
+    rows = sorted((c for c in itertools.product(range(4), repeat=4) if sum(c) == 3),
+                  key=lambda c: (-max(c), [-x for x in c]))
+    lam = np.array(rows, np.float64) / 3.0
+    P, el = meshes.kuhn_tet_box(cells, (2.0, 1.0, 1.0))
+    nelem, nvert = el.shape[0], P.shape[0]
+    Pd, eld = torch.from_numpy(P).cuda(), torch.from_numpy(el).cuda()
+    X3, E3 = meshes.raise_tet_order_device(Pd, eld, lam)
+    nnode = X3.shape[0]
+    out_p, out_e = torch.empty((nnode, 3), dtype=torch.float64, device="cuda"), E3
+    del X3
+    for _ in range(args.warmup):
+        meshes.raise_tet_order_device(Pd, eld, lam, out_points=out_p, out_elements=out_e)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    steps = max(1, args.steps)
+    with ClockSampler(0) as clk:
+        e0.record()
+        for _ in range(steps):
+            meshes.raise_tet_order_device(Pd, eld, lam, out_points=out_p, out_elements=out_e)
+        e1.record()
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    value = nelem / (ms * 1e-3) / 1e6
+    # compulsory bytes: linear tets and vertices read once, the high-order mesh written once
+    npe = lam.shape[0]
+    nbytes = 32 * nelem + 24 * nvert + 8 * npe * nelem + 24 * nnode
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    # end to end: host arrays in, host mesh out
+    e2e = None
+    if not args.no_e2e:
+        t_h = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            Xh, Eh = meshes.raise_tet_order_device(P, el, lam)
+            Xh, Eh = Xh.cpu().numpy(), Eh.cpu().numpy()
+            t_h.append(time.perf_counter() - t0)
+        e2e = dict(value=nelem / min(t_h[1:]) / 1e6, unit="Melem/s", h2d_bytes_per_step=P.nbytes + el.nbytes,
+                   d2h_bytes_per_step=Xh.nbytes + Eh.nbytes)
+    cpu = None
+    if not args.no_cpu:
+        Ps, els = meshes.kuhn_tet_box((24, 24, 24), (2.0, 1.0, 1.0))
+        t0 = time.perf_counter()
+        meshes.raise_tet_order(Ps, els, lam)
+        dt = time.perf_counter() - t0
+        cpu = dict(value=els.shape[0] / dt / 1e6, unit="Melem/s", cores=1, kind="port",
+                   sample="host builder (numpy np.unique of entity keys) on a 24x24x24 Kuhn box, %d tets" % els.shape[0])
+    launches = 18  # count, degree, fill, entities (count and write), nodes, four 3-kernel scans
+    line = dict(metric="high-order tet mesh generation rate (linear tets raised to p=3 per second)", value=value,
+                unit="Melem/s", n_gpus=1, steps=steps, warmup=args.warmup, ms_per_step=ms, higher_is_better=True,
+                scaling="weak", vs_baseline=None, dtype="int64+f64", data="synthetic",
+                config=dict(workload="Kuhn-split box %dx%dx%d cubes on 2x1x1, %d tets, %d vertices -> %d nodes "
+                                     "(equispaced p=3, 20 nodes per tet)" % (cells + (nelem, nvert, nnode)),
+                            inputs="larger than L2 (outputs %.2f GB)" % ((8 * npe * nelem + 24 * nnode) / 1e9)),
+                roofline=dict(bound="hbm", achieved=nbytes / (ms * 1e-3) / 1e9, peak=hbm, unit="GB/s",
+                              frac=nbytes / (ms * 1e-3) / 1e9 / hbm, traffic=None, bytes_min_per_step=nbytes,
+                              peak_source="MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"),
+                e2e=e2e, cpu_baseline=cpu, gpu_launches=launches * steps, clocks=clk.summary())
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -721,6 +794,7 @@ def main():
     ap.add_argument("--instances", type=int, default=512)
     ap.add_argument("--batch-gb", type=float, default=40.0, help="CSR memory budget per sub-batch")
     ap.add_argument("--warmstart", action="store_true", help="learned warm start on the plate instead")
+    ap.add_argument("--meshing", action="store_true", help="device high-order tet mesh generation instead")
     ap.add_argument("--ws-train", type=int, default=2000, help="training solves")
     ap.add_argument("--ws-test", type=int, default=200, help="held-out solves")
     ap.add_argument("--ws-increments", type=int, default=5)
@@ -740,6 +814,8 @@ def main():
         run_batched(args)
     elif args.warmstart:
         run_warmstart(args)
+    elif args.meshing:
+        run_meshing(args)
     else:
         run_ours(args)
 

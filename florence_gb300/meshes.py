@@ -11,7 +11,9 @@ replicate it over larger meshes:
   positive volume, raised to order p with the pattern's barycentric node positions.
 
 Global node numbering differs from Florence's; the assembled operator is the same up to that
-permutation.
+permutation. ``raise_tet_order_device`` is the GPU form of ``raise_tet_order`` (``fl_RaiseTetOrder``):
+the same node numbering and the same weighted sums for the positions, for meshes too large to
+raise on the host.
 """
 import numpy as np
 
@@ -104,3 +106,87 @@ def raise_tet_order(P, el, pattern):
     pos = np.einsum("ak,ekd->ead", lam, P[el]).reshape(-1, 3)
     points = pos[first]
     return points, elements
+
+
+def tet_node_layout(pattern):
+    """(nodes inside one edge, inside one face, inside the element) of the barycentric layout
+    `pattern` [npe,4], as the device mesher classifies it; ValueError for a layout it rejects."""
+    import ctypes
+    from . import _native as N
+    lam = np.ascontiguousarray(pattern, dtype=np.float64)
+    counts = (ctypes.c_int64 * 3)()
+    st = N.lib().fl_TetNodeLayout(lam.ctypes.data, lam.shape[0], ctypes.cast(counts, ctypes.c_void_p))
+    if st != N.FL_OK:
+        raise ValueError("node layout rejected: " + N.lib().fl_status_string(st).decode())
+    return tuple(int(c) for c in counts)
+
+
+def raise_tet_order_device(points, elements, pattern, device="cuda", out_points=None, out_elements=None):
+    """High-order tet mesh built on the GPU from linear tets (``fl_RaiseTetOrder``): node numbers
+    identical to ``raise_tet_order``, positions the same weighted vertex sums. points [nvert,3],
+    elements [E,4] (numpy or tensors); returns (points [nnode,3] float64, elements [E,npe] int64)
+    as device tensors on the current stream. Optional preallocated outputs (out_points [cap,3]
+    float64, out_elements [E,npe] int64) save the counting call when cap is large enough."""
+    import ctypes
+    import torch
+    from . import _native as N
+    L = N.lib()
+    dev = torch.device(device)
+    lam = np.ascontiguousarray(pattern, dtype=np.float64)
+    X = torch.as_tensor(points, dtype=torch.float64).to(dev).contiguous()
+    el = torch.as_tensor(np.asarray(elements).astype(np.int64) if not isinstance(elements, torch.Tensor)
+                         else elements, dtype=torch.int64).to(dev).contiguous()
+    nvert, nelem, npe = X.shape[0], el.shape[0], lam.shape[0]
+    ws_bytes = L.fl_RaiseTetOrder_workspace_size(nelem, nvert)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    out_el = out_elements if out_elements is not None else torch.empty((nelem, npe), dtype=torch.int64, device=dev)
+    if out_el.shape != (nelem, npe) or out_el.dtype != torch.int64 or not out_el.is_contiguous():
+        raise ValueError("out_elements must be a contiguous int64 tensor of shape (nelem, npe)")
+    if out_points is not None and (out_points.dtype != torch.float64 or out_points.dim() != 2
+                                   or out_points.shape[1] != 3 or not out_points.is_contiguous()):
+        raise ValueError("out_points must be a contiguous float64 tensor of shape (capacity, 3)")
+    nnode = ctypes.c_int64(0)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def call(out_pts):
+        return L.fl_RaiseTetOrder(ctypes.c_void_p(X.data_ptr()), nvert, ctypes.c_void_p(el.data_ptr()), nelem,
+                                  lam.ctypes.data, npe,
+                                  ctypes.c_void_p(out_pts.data_ptr()) if out_pts is not None else None,
+                                  out_pts.shape[0] if out_pts is not None else 0, ctypes.byref(nnode),
+                                  ctypes.c_void_p(out_el.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ws_bytes, stream)
+
+    out_pts = out_points
+    st = call(out_pts)  # without a large enough buffer: counts the nodes only
+    if st == N.FL_ERR_CAPACITY:
+        out_pts = torch.empty((max(nnode.value, 1), 3), dtype=torch.float64, device=dev)
+        st = call(out_pts)
+    if st == N.FL_ERR_MESH:
+        raise ValueError("an element repeats a vertex")
+    N.check(st, "fl_RaiseTetOrder")
+    return out_pts[:nnode.value], out_el
+
+
+def kuhn_tet_box(n, L=(1.0, 1.0, 1.0)):
+    """Linear tets of an nx x ny x nz box of cubes, each cube split into the six tets around its
+    main diagonal (the Kuhn split, conforming across cubes), all positively oriented."""
+    nx, ny, nz = n
+    xs = [np.linspace(0, L[i], m + 1) for i, m in enumerate((nx, ny, nz))]
+    P = np.stack(np.meshgrid(*xs, indexing="ij"), -1).reshape(-1, 3)
+    ci, cj, ck = [c.ravel() for c in np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")]
+
+    def vid(i, j, k):
+        return (i * (ny + 1) + j) * (nz + 1) + k
+
+    tets = []
+    for perm in ((0, 1, 2), (0, 2, 1), (1, 0, 2), (1, 2, 0), (2, 0, 1), (2, 1, 0)):
+        c = [ci.copy(), cj.copy(), ck.copy()]
+        t = [vid(*c)]
+        for axis in perm:
+            c[axis] = c[axis] + 1
+            t.append(vid(*c))
+        t = np.stack(t, 1)
+        if perm in ((0, 2, 1), (1, 0, 2), (2, 1, 0)):  # odd permutations: negative volume as walked
+            t[:, [1, 2]] = t[:, [2, 1]]
+        tets.append(t)
+    el = np.stack(tets, 1).reshape(-1, 4).astype(np.int64)
+    return P, el

@@ -17,6 +17,8 @@
  *                                      (signature), called from _LowLevelAssemblyExplicit_DF_DPF_.pyx:123-152
  *   fl_LumpedMass                      VariationalPrinciple/_Mass_/_MassIntegrand_.h:249-400 (mass_type 0),
  *                                      called from _MassIntegrand_.pyx:192-348 (__TotalConstantMassIntegrand__)
+ *   fl_RaiseTetOrder                   the tet branch of Mesh.GetHighOrderMesh (MeshGeneration/Mesh.py:1339-1410),
+ *                                      HighOrderMeshTet_SEMISTABLE (HigherOrderMeshing/HigherOrderMeshingTet.py:19-135)
  */
 #ifndef FLORENCE_GB300_H
 #define FLORENCE_GB300_H
@@ -71,6 +73,38 @@ int fl_ComputeSparsityPattern(const int64_t *elements, int64_t nelem, int64_t no
                               int64_t nvar, int32_t *indptr, int32_t *indices, int64_t indices_capacity,
                               int64_t *nnz, int32_t *data_local_indices, int32_t *data_global_indices,
                               void *workspace, size_t workspace_bytes, fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * High-order tet mesh from a linear one (the tet branch of GetHighOrderMesh). `pattern` (HOST,
+ * [nodeperelem * 4]) holds the barycentric coordinates of the high-order element's local nodes
+ * with respect to its four vertices, e.g. the reference element's node layout. A local node
+ * belongs to the vertices whose weight exceeds 1e-10 (a vertex, an edge, a face or the
+ * interior); nodes of shared edges and faces are merged when their weights, read in increasing
+ * global-vertex order and rounded to 1e-6, agree. Output: the same mesh as the reference's up to
+ * a permutation of node numbers; the numbering is the lexicographic order of (entity size,
+ * global vertex ids ascending, weights in that order): used vertices first (in id order), then
+ * edge, face and interior nodes. Positions are the weighted sums of the vertex coordinates.
+ *   points          [nvert * 3] linear vertices
+ *   elements        [nelem * 4] linear tets (int64 vertex ids)
+ *   out_points      out [points_capacity * 3]
+ *   nnode           host out: number of nodes of the high-order mesh
+ *   out_elements    out [nelem * nodeperelem] (int64 node ids)
+ *   workspace       device scratch of fl_RaiseTetOrder_workspace_size() bytes (about 96 B per
+ *                   element + 40 B per vertex)
+ * Synchronises `stream` twice. Returns FL_ERR_CAPACITY with *nnode set when
+ * points_capacity < nnode (or out_points is NULL): call again with a larger buffer.
+ * FL_ERR_ARG for a vertex id out of range, FL_ERR_MESH for an element that repeats a vertex,
+ * FL_ERR_UNSUPPORTED for a layout whose shared nodes cannot be matched from both sides (weights
+ * not symmetric under the permutations of an edge's or face's vertices) or nodeperelem > 35.
+ * fl_TetNodeLayout (host only, no CUDA call) classifies a pattern the same way and returns
+ * counts[0..2] = nodes inside one edge, inside one face, inside the element.
+ * ------------------------------------------------------------------------------------------ */
+int fl_TetNodeLayout(const double *pattern, int64_t nodeperelem, int64_t *counts);
+size_t fl_RaiseTetOrder_workspace_size(int64_t nelem, int64_t nvert);
+int fl_RaiseTetOrder(const double *points, int64_t nvert, const int64_t *elements, int64_t nelem,
+                     const double *pattern, int64_t nodeperelem, double *out_points, int64_t points_capacity,
+                     int64_t *nnode, int64_t *out_elements, void *workspace, size_t workspace_bytes,
+                     fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
  * Implicit assembly of the tangent stiffness and the internal-force residual (FP64), one
