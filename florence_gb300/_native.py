@@ -85,6 +85,8 @@ def lib():
         L.fl_GlobalAssemblyExplicit_DF_DPF_.argtypes = [P, P, P, P, P, P, P, I64, I64, I64, I64, I64, I64, I64, I64, P,
                                                         D, D, D, D, D, D, D, D, D, D, D, P, INT, INT, P, P]
         L.fl_LumpedMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, P, P, P]
+        L.fl_ConsistentMass.argtypes = [P, P, P, P, P, I64, I64, I64, I64, I64, I64, D, INT, INT, P, P, I64, P, P, P,
+                                        P, P, P, P]
         L.fl_measure_fp64_peak.argtypes = [ctypes.POINTER(D), P]
         L.fl_measure_fp32_peak.argtypes = [ctypes.POINTER(D), P]
         L.fl_TensorCoreSelfTest.argtypes = [P, P, P, P, P]
@@ -121,7 +123,7 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
            "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
            "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_", "fl_GlobalAssemblyDF_noalloc",
-           "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak", "fl_TensorCoreSelfTest",
+           "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_ConsistentMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak", "fl_TensorCoreSelfTest",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
            "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_AssembleExternalTractionForces", "fl_AssembleBodyForces", "fl_MLP_num_params", "fl_MLP_workspace_size",

@@ -13,7 +13,7 @@ Two layers:
     AOT_Assembler.py:36-118, looked up by _LowLevelAssembly_.py:45-83);
   - ``_LowLevelAssemblyExplicit_DF_DPF_`` (_LowLevelAssemblyExplicit_DF_DPF_.pyx:44-152);
   - ``ComputeSparsityPattern`` (_Assembly_/ComputeSparsityPattern.pyx:44-112);
-  - ``__TotalConstantMassIntegrand__`` for lumped mass (VariationalPrinciple/_Mass_/_MassIntegrand_.pyx:192-348).
+  - ``__TotalConstantMassIntegrand__`` for lumped and consistent mass (VariationalPrinciple/_Mass_/_MassIntegrand_.pyx:192-348).
 
   ``install(Florence)`` registers them in Florence's module namespaces.
 
@@ -330,6 +330,35 @@ class DeviceAssembler:
         N.check(st, "fl_LumpedMass")
         return M
 
+    # -- consistent mass -------------------------------------------------------------------------
+    def consistent_mass(self, rho, Bases=None, V=None, I=None, J=None, stream=None):
+        """Consistent mass sum_g rho N_a N_b w |det dX/dxi| on the nvar diagonal, in the
+        assembler's scatter mode: CSR values [nnz] (accumulated into V when given), or in triplet
+        mode (I, J, V) in element-local order."""
+        L = N.lib()
+        B = self.Bases if Bases is None else _to_dev(Bases, torch.float64, self.device)
+        if B is None:
+            raise ValueError("the mass needs the basis values (Bases [npe, nq])")
+        cap = self.nelem * self.ndof * self.ndof
+        if self.mode == "triplet":
+            I = torch.empty(cap, dtype=torch.int32, device=self.device) if I is None else I
+            J = torch.empty(cap, dtype=torch.int32, device=self.device) if J is None else J
+            V = torch.empty(cap, dtype=torch.float64, device=self.device) if V is None else V
+            ptr, ind, nnz = None, None, cap
+        else:
+            V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
+            ptr, ind, nnz = self.indptr, self.indices, self.nnz
+        st = L.fl_ConsistentMass(_ptr(self.points), _ptr(self.elements), _ptr(B), _ptr(self.Jm), _ptr(self.w), 3, 3,
+                                 self.nq, self.nelem, self.npe, self.nnode, float(rho),
+                                 1 if self.mode == "triplet" else 0, 1 if self.mode == "squeeze" else 0, _ptr(ptr),
+                                 _ptr(ind), nnz, _ptr(self.data_local if self.mode == "csr" else None),
+                                 _ptr(self.data_global if self.mode == "csr" else None), _ptr(I), _ptr(J), _ptr(V),
+                                 _ptr(self.flags), stream or _stream())
+        N.check(st, "fl_ConsistentMass")
+        if self.mode == "triplet":
+            return I, J, V
+        return V
+
     def check_flags(self, what="assembly"):
         _check_flags(self.flags, what)
         self.flags.zero_()
@@ -479,10 +508,13 @@ def _LowLevelAssemblyExplicit_DF_DPF_(function_space, formulation, mesh, materia
 def __TotalConstantMassIntegrand__(mesh, function_space, formulation, mass_type="lumped",
                                    recompute_sparsity_pattern=True, squeeze_sparsity_pattern=False,
                                    indices=None, indptr=None, data_global_indices=None, data_local_indices=None):
-    """Lumped mass of _MassIntegrand_.pyx:192-348: returns (mass [nvar*N,1], I, J, V) or (mass, V),
-    with the 1-element placeholder I/J/V the reference returns for lumped mass."""
-    if mass_type != "lumped":
-        raise NotImplementedError("the GB300 mass assembly provides the lumped (row-sum) mass")
+    """_MassIntegrand_.pyx:192-348 on the device. Lumped: (mass [nvar*N,1], I, J, V) or (mass, V)
+    with the 1-element placeholder I/J/V the reference returns. Consistent: (mass placeholder
+    [1,1], I_mass, J_mass, V_mass) triplets in element-local order when
+    recompute_sparsity_pattern, else (mass placeholder, V_mass) on the given CSR pattern (through
+    the element-to-nonzero maps, or by row search when squeeze_sparsity_pattern)."""
+    if mass_type not in ("lumped", "consistent"):
+        raise ValueError("mass_type must be 'lumped' or 'consistent'")
     if formulation.nvar != 3 or mesh.points.shape[1] != 3:
         raise NotImplementedError("the GB300 mass assembly covers three-dimensional mechanics")
     # constant_mass_integrand[g] = rho N N^T (x) I3 (VariationalPrinciple.py:269-290): its entries sum
@@ -490,6 +522,25 @@ def __TotalConstantMassIntegrand__(mesh, function_space, formulation, mass_type=
     cmi = np.asarray(formulation.constant_mass_integrand)
     nsum = float(np.asarray(function_space.Bases)[:, 0].sum())
     rho = float(cmi[0].sum()) / (3.0 * nsum * nsum)
+    if mass_type == "consistent":
+        if recompute_sparsity_pattern:
+            asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss,
+                                  "NeoHookean", (1.0, 1.0), mode="triplet", Bases=function_space.Bases)
+            I, J, V = asm.consistent_mass(rho)
+            asm.check_flags("__TotalConstantMassIntegrand__")
+            return np.zeros((1, 1)), I.cpu().numpy(), J.cpu().numpy(), V.cpu().numpy()
+        squeeze = bool(squeeze_sparsity_pattern)
+        if indices is None or indptr is None or (not squeeze and (data_global_indices is None
+                                                                  or data_local_indices is None)):
+            raise ValueError("the CSR consistent mass needs indices, indptr and (unless squeezed) the maps")
+        sparsity = (indices, indptr, None if squeeze else data_local_indices,
+                    None if squeeze else data_global_indices)
+        asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, "NeoHookean",
+                              (1.0, 1.0), mode="squeeze" if squeeze else "csr", Bases=function_space.Bases,
+                              sparsity=sparsity)
+        V = asm.consistent_mass(rho)
+        asm.check_flags("__TotalConstantMassIntegrand__")
+        return np.zeros((1, 1)), V.cpu().numpy()
     asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, "NeoHookean",
                           (1.0, 1.0), mode="triplet", Bases=function_space.Bases)
     M = asm.lumped_mass(rho).cpu().numpy()[:, None]

@@ -15,7 +15,7 @@
  *                                      called from _LowLevelAssemblyDF_.pyx:115-154
  *   fl_GlobalAssemblyExplicit_DF_DPF_  FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyExplicit_DF_DPF_.h:728-829
  *                                      (signature), called from _LowLevelAssemblyExplicit_DF_DPF_.pyx:123-152
- *   fl_LumpedMass                      VariationalPrinciple/_Mass_/_MassIntegrand_.h:249-400 (mass_type 0),
+ *   fl_LumpedMass, fl_ConsistentMass   VariationalPrinciple/_Mass_/_MassIntegrand_.h:249-400 (mass_type 0 / 1),
  *                                      called from _MassIntegrand_.pyx:192-348 (__TotalConstantMassIntegrand__)
  *   fl_RaiseTetOrder                   the tet branch of Mesh.GetHighOrderMesh (MeshGeneration/Mesh.py:1339-1410),
  *                                      HighOrderMeshTet_SEMISTABLE (HigherOrderMeshing/HigherOrderMeshingTet.py:19-135)
@@ -279,6 +279,25 @@ int fl_GlobalAssemblyExplicit_DF_DPF_(const double *points, const uint64_t *elem
 int fl_LumpedMass(const double *points, const uint64_t *elements, const double *bases, const double *Jm,
                   const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss, int64_t nelem,
                   int64_t nodeperelem, int64_t nnode, double rho, double *M, int *flags, fl_stream_t stream);
+
+/* ------------------------------------------------------------------------------------------
+ * Consistent mass (mass_type 1 of _GenericConstantMassIntegrand_, _MassIntegrand_.h:249-400,
+ * scattered as its fill_global_data, :68-178): element mass sum_g rho N_a N_b w_g |det dX/dxi|
+ * on the nvar diagonal of every node pair.
+ *   recompute_sparsity_pattern != 0: triplets I_mass, J_mass, V_mass [nelem*(nvar*nodeperelem)^2]
+ *     written in element-local order (entry e*ndof^2 + r*ndof + c, zeros off the nvar diagonal);
+ *   else squeeze_sparsity_pattern != 0: V_mass[nnz] += by searching each CSR row (indptr, indices);
+ *   else: V_mass[nnz] += through the element-to-nonzero maps (data_local_indices,
+ *     data_global_indices, [nelem*(nvar*nodeperelem)^2] each).
+ * nvar 1..4 (the mass acts on every field, as in the reference). flags: optional device int,
+ * FL_FLAG_BAD_INDEX when a node id or map entry is out of range (the entry is skipped).
+ * ------------------------------------------------------------------------------------------ */
+int fl_ConsistentMass(const double *points, const uint64_t *elements, const double *bases, const double *Jm,
+                      const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss, int64_t nelem,
+                      int64_t nodeperelem, int64_t nnode, double rho, int recompute_sparsity_pattern,
+                      int squeeze_sparsity_pattern, const int32_t *indptr, const int32_t *indices, int64_t nnz,
+                      const int32_t *data_local_indices, const int32_t *data_global_indices, int32_t *I_mass,
+                      int32_t *J_mass, double *V_mass, int *flags, fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
  * Explicit central-difference dynamics (the lumped-mass loop of

@@ -169,6 +169,28 @@ def lumped_mass(rho, points, elements, Jm, AllGauss, Bases):
     return M
 
 
+def consistent_mass(rho, points, elements, Jm, AllGauss, Bases, nvar=3):
+    """Dense [nvar*N, nvar*N] consistent mass (mass_type 1 of _GenericConstantMassIntegrand_,
+    VariationalPrinciple/_Mass_/_MassIntegrand_.h:249-400, with the constant integrand
+    rho N N^T of VariationalPrinciple.py:255-290): per element sum_g rho N_a N_b w_g |det dX/dxi|
+    on the nvar diagonal of every node pair. numpy, for small meshes."""
+    P = np.asarray(points, np.float64)
+    el = np.asarray(elements, np.int64)
+    Jm = np.asarray(Jm, np.float64)                     # [3, npe, nq]
+    w = np.ravel(AllGauss).astype(np.float64)
+    B = np.asarray(Bases, np.float64)                   # [npe, nq]
+    n = P.shape[0] * nvar
+    M = np.zeros((n, n))
+    for e in range(el.shape[0]):
+        X = P[el[e]]                                    # [npe, 3]
+        G = np.einsum("dag,ak->gdk", Jm, X)             # dX/dxi per Gauss point
+        wdet = w * np.abs(np.linalg.det(G))
+        m = np.einsum("ag,bg,g->ab", B, B, wdet) * rho
+        for i in range(nvar):
+            M[np.ix_(nvar * el[e] + i, nvar * el[e] + i)] += m
+    return M
+
+
 def external_traction(faces, neumann_flags, applied_neumann, Bases, AllGauss, nnode):
     """F [nnode*3] of AssembleExternalTractionForces (Assembly.py:451-514): every flagged face adds
     applied_neumann[face, i] * sum_g Bases[a, g] w_g to its node a, component i (parent weights)."""

@@ -11,7 +11,7 @@ Every output is produced by the reference's own pure-numpy assembly path
 Florence/FiniteElements/Assembly/Assembly.py:1454-1495, :99-252 and
 Florence/VariationalPrinciple/DisplacementFormulation.py:110-188), by its compiled
 ``ComputeSparsityPattern`` (Florence/FiniteElements/Assembly/_Assembly_/ComputeSparsityPattern.pyx:44-112)
-and by its Python lumped-mass path (Florence/FiniteElements/Assembly/Assembly.py:608-657).
+and by its Python lumped and consistent mass path (Florence/FiniteElements/Assembly/Assembly.py:608-657).
 Meshes come from the reference's own generators (``Mesh.Cube``, ``Mesh.Parallelepiped``,
 ``GetHighOrderMesh``) or from a seeded jittered lattice split by ``scipy.spatial.Delaunay``.
 """
@@ -175,6 +175,20 @@ def lumped_mass(F, form, mat, mesh, x):
     return np.asarray(M).ravel()
 
 
+def consistent_mass(F, form, mat, mesh, x):
+    """The reference's consistent mass (Assembly.py:608-657 with mass_type="consistent") as a
+    canonical CSR: (indptr, indices, data), duplicates summed, columns sorted."""
+    from Florence.FiniteElements.Assembly.Assembly import AssembleExplicit_NoLLD_Mass
+    fs = form.function_spaces[0]
+    form.GetConstantMassIntegrand(fs, mat)
+    solver = F.FEMSolver(optimise=False, analysis_type="dynamic", analysis_subtype="explicit", mass_type="consistent")
+    solver.is_mass_computed = False
+    M = AssembleExplicit_NoLLD_Mass(solver, fs, form, mesh, mat, x, np.zeros(mesh.points.shape[0])).tocsr()
+    M.sum_duplicates()
+    M.sort_indices()
+    return M.indptr.astype(np.int32), M.indices.astype(np.int32), M.data
+
+
 CASES = [
     dict(name="hex_p1_nh", mesh="cube_hex", n=(2, 2, 2), p=1, material="NeoHookean", params=(1.0, 10.0), seed=10,
          amp=0.01, qdeg=None, emat=(0, 7), mass=True),
@@ -244,6 +258,7 @@ def make_case(F, spec):
         rho = 1.0
         out["M_lumped"] = lumped_mass(F, form, mat, mesh, x)
         out["rho"] = np.array(rho)
+        out["Mc_indptr"], out["Mc_indices"], out["Mc_data"] = consistent_mass(F, form, mat, mesh, x)
     np.savez_compressed(os.path.join(HERE, spec["name"] + ".npz"), **out)
     print("%-22s E=%-4d npe=%-3d nq=%-3d nnz=%-8d %.1fs" % (spec["name"], mesh.nelem, mesh.elements.shape[1],
           fs.AllGauss.shape[0], K.nnz, time.time() - t0), flush=True)

@@ -216,6 +216,54 @@ def test_lumped_mass(fl, case):
     assert rel_fro(M.cpu().numpy(), d["M_lumped"]) < TOL
 
 
+def _golden_consistent_mass(d):
+    n = d["points"].shape[0] * 3
+    return sp.csr_matrix((d["Mc_data"], d["Mc_indices"], d["Mc_indptr"]), shape=(n, n))
+
+
+@pytest.mark.parametrize("mode", ["csr", "squeeze", "triplet"])
+@pytest.mark.parametrize("case", [c for c in golden_cases() if "Mc_data" in load_golden(c)])
+def test_consistent_mass(fl, case, mode):
+    """Consistent mass against the reference's (golden CSR), in each scatter mode; values off the
+    nvar diagonal of the tangent's pattern stay zero."""
+    d = load_golden(case)
+    n = d["points"].shape[0] * 3
+    asm = fl.DeviceAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], "NeoHookean", (1.0, 1.0),
+                             mode=mode, Bases=d["Bases"])
+    out = asm.consistent_mass(float(d["rho"]))
+    asm.check_flags()
+    if mode == "triplet":
+        I, J, V = (t.cpu().numpy() for t in out)
+        M = sp.csr_matrix((V, (I, J)), shape=(n, n))
+    else:
+        M = sp.csr_matrix((out.cpu().numpy(), asm.indices.cpu().numpy(), asm.indptr.cpu().numpy()), shape=(n, n))
+    ref = _golden_consistent_mass(d)
+    assert spla.norm(M - ref) <= TOL * spla.norm(ref)
+
+
+@pytest.mark.parametrize("recompute,squeeze", [(True, False), (False, False), (False, True)])
+def test_drop_in_consistent_mass(fl, recompute, squeeze):
+    d = load_golden("tet_p3_mr_jitter")
+    n = d["points"].shape[0] * 3
+    rho = float(d["rho"])
+    mesh = types.SimpleNamespace(points=d["points"], elements=d["elements"].astype(np.uint64))
+    fs = types.SimpleNamespace(Jm=d["Jm"], AllGauss=np.ravel(d["AllGauss"])[:, None], Bases=d["Bases"])
+    B = d["Bases"]
+    cmi = np.zeros((B.shape[1], 3 * B.shape[0], 3 * B.shape[0]))
+    for g in range(B.shape[1]):  # rho N N^T (x) I3, VariationalPrinciple.py:255-290
+        cmi[g] = rho * np.kron(np.outer(B[:, g], B[:, g]), np.eye(3))
+    form = types.SimpleNamespace(nvar=3, ndim=3, constant_mass_integrand=cmi)
+    ref = _golden_consistent_mass(d)
+    if recompute:
+        _, I, J, V = fl.__TotalConstantMassIntegrand__(mesh, fs, form, "consistent", True)
+        M = sp.csr_matrix((V, (I, J)), shape=(n, n))
+    else:
+        args = (d["sp_indices"], d["sp_indptr"], d["sp_data_global"], d["sp_data_local"])
+        _, V = fl.__TotalConstantMassIntegrand__(mesh, fs, form, "consistent", False, squeeze, *args)
+        M = sp.csr_matrix((V, d["sp_indices"], d["sp_indptr"]), shape=(n, n))
+    assert spla.norm(M - ref) <= TOL * spla.norm(ref)
+
+
 def test_config1_full_size(fl, oracle):
     """Structured 8x8x8 p=2 hex cube, 125 Gauss points, neo-Hookean: exact structure hashes from the
     reference, value probes from the reference, full CSR values against the oracle."""

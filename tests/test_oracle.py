@@ -74,6 +74,21 @@ def test_lumped_mass(oracle, case):
     assert rel_fro(M, d["M_lumped"]) < TOL
 
 
+def golden_consistent_mass(d):
+    n = d["points"].shape[0] * 3
+    return sp.csr_matrix((d["Mc_data"], d["Mc_indices"], d["Mc_indptr"]), shape=(n, n))
+
+
+@pytest.mark.parametrize("case", [c for c in golden_cases() if "Mc_data" in load_golden(c)])
+def test_consistent_mass(oracle, case):
+    d = load_golden(case)
+    M = oracle.consistent_mass(float(d["rho"]), d["points"], d["elements"], d["Jm"], d["AllGauss"], d["Bases"])
+    ref = golden_consistent_mass(d).toarray()
+    assert rel_fro(M, ref) < TOL
+    # its row sums are the lumped mass, the reference's own lumping
+    assert rel_fro(M.sum(1), d["M_lumped"]) < TOL
+
+
 def test_config1_structure_and_values(oracle):
     """Full-size structured 8x8x8 p=2 hex cube, 125 Gauss points: exact structure hashes and value probes."""
     d = load_golden("config1_hex8_p2_q5")
