@@ -1,0 +1,155 @@
+"""numpy restatement of the displacement-potential (electromechanics) assembly.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/ as the checker, never by the product path. Pinned
+against golden vectors made by the reference's own code (tests/golden/make_golden.py,
+``DPF_CASES``; tests/test_dpf_oracle.py).
+
+What it restates (paths inside the Florence repository):
+* the element integral of DisplacementPotentialFormulation.GetLocalStiffness
+  (VariationalPrinciple/DisplacementPotentialFormulation.py:108-200): per Gauss point the
+  kinematics, the spatial electric field E = -grad(phi), the material's electric displacement,
+  Cauchy stress and 9x9 Hessian, the constitutive term B H B^T and the residual B [sigma; D], the
+  geometric term on the displacement dofs; weights w |det dX/dxi| |J|;
+* the DPF strain-displacement matrix and total traction (Voigt order xx, yy, zz, xy, xz, yz;
+  electric rows carry grad N; VariationalPrinciple/_ConstitutiveStiffness_/
+  DisplacementPotentialApproachIndices.pyx:1-50, :203-230);
+* IsotropicElectroMechanics_108, an internal-energy model (MaterialLibrary/
+  IsotropicElectroMechanics_108.py:36-113, LLDispatch/CythonSource/_IsotropicElectroMechanics_108_.h):
+  D = eps_2 E, the internal-energy elasticity, coupling and dielectric tensors turned into the
+  electric-enthalpy Hessian by the Legendre transform (LegendreTransform/LegendreTransform.py:22-40);
+* symmetric Voigt reduction of 4th- and 3rd-order tensors (Tensor/Numeric.pyx:166-270): the
+  average over the last pair's (4th order) or first pair's (3rd order) index swap.
+Global dof of (node n, field v) is 4 n + v (v = 3: the electric potential).
+"""
+import numpy as np
+
+NVAR = 4
+VOIGT_PAIRS = ((0, 0), (1, 1), (2, 2), (0, 1), (0, 2), (1, 2))
+
+
+def voigt4(C):
+    """6x6 symmetric Voigt form: V[I, J] = (C[i,j,k,l] + C[i,j,l,k]) / 2 for I <= J, mirrored."""
+    V = np.zeros((6, 6))
+    for I, (i, j) in enumerate(VOIGT_PAIRS):
+        for J in range(I, 6):
+            k, l = VOIGT_PAIRS[J]
+            V[I, J] = 0.5 * (C[i, j, k, l] + C[i, j, l, k])
+            V[J, I] = V[I, J]
+    return V
+
+
+def voigt3(e):
+    """6x3 Voigt form of a 3rd-order tensor: V[I, k] = (e[i,j,k] + e[j,i,k]) / 2."""
+    V = np.zeros((6, 3))
+    for I, (i, j) in enumerate(VOIGT_PAIRS):
+        V[I] = 0.5 * (e[i, j] + e[j, i])
+    return V
+
+
+def em108(F, E, mu1, mu2, lamb, eps_2):
+    """(D, sigma, H[9x9]) of IsotropicElectroMechanics_108 at deformation gradient F and spatial
+    electric field E."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    D = eps_2 * E
+    DD = D @ D
+    sigma = (2.0 * mu1 / J) * b + (2.0 * mu2 / J) * (np.trace(b) * b - b @ b) \
+        - (2.0 * (mu1 + 2.0 * mu2) / J) * d + lamb * (J - 1.0) * d \
+        + (np.outer(D, D) - 0.5 * DD * d) / eps_2
+    # 4th-order identities and b products, index order (i, j, k, l)
+    dd_ij_kl = d[:, :, None, None] * d[None, None, :, :]
+    dd_ik_jl = d[:, None, :, None] * d[None, :, None, :]
+    dd_il_jk = d[:, None, None, :] * d[None, :, :, None]
+    bb_ij_kl = b[:, :, None, None] * b[None, None, :, :]
+    bb_ik_jl = b[:, None, :, None] * b[None, :, None, :]
+    bb_il_jk = b[:, None, None, :] * b[None, :, :, None]
+    sym = dd_ik_jl + dd_il_jk
+    W_el = (2.0 * mu2 / J) * (2.0 * bb_ij_kl - bb_ik_jl - bb_il_jk) + (2.0 * (mu1 + 2.0 * mu2) / J) * sym \
+        + lamb * (2.0 * J - 1.0) * dd_ij_kl - lamb * (J - 1.0) * sym \
+        + (0.5 * DD * (sym + dd_ij_kl) - d[:, :, None, None] * np.outer(D, D)[None, None]
+           - np.outer(D, D)[:, :, None, None] * d[None, None]) / eps_2
+    # coupling W_cp[i,j,k] = (delta_ik D_j + D_i delta_jk - delta_ij D_k) / eps_2
+    W_cp = (d[:, None, :] * D[None, :, None] + D[:, None, None] * d[None, :, :]
+            - d[:, :, None] * D[None, None, :]) / eps_2
+    W_di = d / eps_2
+    # Legendre transform to the electric enthalpy
+    H_di = -np.linalg.inv(W_di)
+    H_cp = -np.tensordot(W_cp, H_di, axes=([2], [0]))         # H_cp[k,l,j] = -sum_i W_cp[k,l,i] H_di[i,j]
+    H_el = W_el - np.einsum("ijk,mlk->ijlm", W_cp, H_cp)     # sum_k W_cp[i,j,k] H_cp[m,l,k]
+    C_V, P_V = voigt4(H_el), voigt3(H_cp)
+    H = np.zeros((9, 9))
+    H[:6, :6] = C_V
+    H[:6, 6:] = -P_V
+    H[6:, :6] = -P_V.T
+    H[6:, 6:] = H_di
+    return D, sigma, H
+
+
+MATERIALS = {"IsotropicElectroMechanics_108": em108}
+
+
+def b_matrix(SG):
+    """DPF strain-displacement matrix [4 npe, 9] from spatial gradients SG [3, npe]."""
+    npe = SG.shape[1]
+    B = np.zeros((NVAR * npe, 9))
+    for a in range(npe):
+        gx, gy, gz = SG[:, a]
+        r = NVAR * a
+        B[r + 0, 0], B[r + 1, 1], B[r + 2, 2] = gx, gy, gz
+        B[r + 0, 3], B[r + 1, 3] = gy, gx
+        B[r + 0, 4], B[r + 2, 4] = gz, gx
+        B[r + 1, 5], B[r + 2, 5] = gz, gy
+        B[r + 3, 6:9] = SG[:, a]
+    return B
+
+
+def element(material, params, X, x, phi, Jm, w, update=1):
+    """(K_e [4 npe, 4 npe], t_e [4 npe]) of one element."""
+    kin = MATERIALS[material]
+    npe = X.shape[0]
+    K = np.zeros((NVAR * npe, NVAR * npe))
+    t = np.zeros(NVAR * npe)
+    for g in range(w.shape[0]):
+        dN = Jm[:, :, g]                      # [3, npe] parent gradients
+        GX = dN @ X                           # dX/dxi
+        MG = np.linalg.solve(GX, dN)          # material gradients [3, npe]
+        F = x.T @ MG.T
+        if update:
+            SG = np.linalg.solve(dN @ x, dN)  # spatial gradients
+            dv = w[g] * abs(np.linalg.det(GX)) * abs(np.linalg.det(F))
+        else:
+            SG = MG
+            dv = w[g] * abs(np.linalg.det(GX))
+        E = -SG @ phi
+        D, sigma, H = kin(F, E, *params)
+        B = b_matrix(SG)
+        Kg = B @ H @ B.T
+        geo = SG.T @ sigma @ SG               # grad N_a . sigma . grad N_b
+        for v in range(3):
+            Kg[v::NVAR, v::NVAR] += geo
+        K += Kg * dv
+        if update:
+            tt = np.array([sigma[0, 0], sigma[1, 1], sigma[2, 2], sigma[0, 1], sigma[0, 2], sigma[1, 2], *D])
+            t += (B @ tt) * dv
+    return K, t
+
+
+def assemble(material, params, points, elements, Eulerx, Eulerp, Jm, AllGauss, update=1):
+    """Dense global tangent [4N, 4N] and residual [4N]. For small meshes."""
+    P = np.asarray(points, np.float64)
+    x = np.asarray(Eulerx, np.float64)
+    phi = np.asarray(Eulerp, np.float64)
+    el = np.asarray(elements, np.int64)
+    Jm = np.asarray(Jm, np.float64)
+    w = np.ravel(AllGauss).astype(np.float64)
+    n = NVAR * P.shape[0]
+    K = np.zeros((n, n))
+    T = np.zeros(n)
+    for e in range(el.shape[0]):
+        nodes = el[e]
+        Ke, te = element(material, params, P[nodes], x[nodes], phi[nodes], Jm, w, update)
+        dofs = (NVAR * nodes[:, None] + np.arange(NVAR)[None, :]).ravel()
+        K[np.ix_(dofs, dofs)] += Ke
+        T[dofs] += te
+    return K, T

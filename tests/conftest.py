@@ -22,7 +22,14 @@ def load_golden(name):
 
 
 def golden_cases():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("config1"))
+    """Displacement-formulation cases (nvar 3)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and not f.startswith("config1") and not f.startswith("dpf_"))
+
+
+def dpf_cases():
+    """Displacement-potential (electromechanics, nvar 4) cases."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and f.startswith("dpf_"))
 
 
 def rel_fro(a, b):

@@ -47,6 +47,9 @@ def make_material(F, name, params):
     elif name == "AnisotropicMooneyRivlin_1":
         # params (mu1, mu2, lamb, mu3); fibre directions set per element by make_case
         m = F.AnisotropicMooneyRivlin_1(3, mu1=params[0], mu2=params[1], lamb=params[2], mu3=params[3], rho=1.0)
+    elif name == "IsotropicElectroMechanics_108":
+        # params (mu1, mu2, lamb, eps_2): internal-energy electromechanics, displacement-potential form
+        m = F.IsotropicElectroMechanics_108(3, mu1=params[0], mu2=params[1], lamb=params[2], eps_2=params[3], rho=1.0)
     else:
         raise ValueError(name)
     m.has_low_level_dispatcher = False
@@ -264,6 +267,54 @@ def make_case(F, spec):
           fs.AllGauss.shape[0], K.nnz, time.time() - t0), flush=True)
 
 
+DPF_CASES = [
+    dict(name="dpf_tet_p2_em108", mesh="cube_tet", n=(1, 1, 1), p=2, material="IsotropicElectroMechanics_108",
+         params=(0.5, 0.3, 10.0, 2.0), seed=30, amp=0.02, phi_amp=0.1, emat=(0, 4)),
+    dict(name="dpf_hex_p2_em108", mesh="box_hex", n=(2, 1, 1), L=(2.0, 1.0, 1.0), p=2,
+         material="IsotropicElectroMechanics_108", params=(0.4, 0.2, 15.0, 1.5), seed=31, amp=0.03, phi_amp=0.2,
+         emat=(0, 1)),
+]
+
+
+def make_dpf_case(F, spec):
+    """Displacement-potential formulation (nvar 4: three displacements and the electric potential)
+    through the reference's numpy element path (DisplacementPotentialFormulation.GetLocalStiffness,
+    Florence/VariationalPrinciple/DisplacementPotentialFormulation.py:108-200): tangent CSR and
+    residual at seeded displacements and potentials, with the reference's nvar=4 sparsity."""
+    t0 = time.time()
+    mesh = build_mesh(F, spec)
+    rng = np.random.default_rng(spec["seed"])
+    x = mesh.points + rng.uniform(-spec["amp"], spec["amp"], size=mesh.points.shape)
+    phi = rng.uniform(-spec["phi_amp"], spec["phi_amp"], size=mesh.points.shape[0])
+    mat = make_material(F, spec["material"], spec["params"])
+    form = F.DisplacementPotentialFormulation(mesh)
+    solver = F.FEMSolver(optimise=False, recompute_sparsity_pattern=False)
+    K, T = F.AssembleForm(form, mesh, mat, solver, Eulerx=x, Eulerp=phi)
+    K = K.tocsr()
+    fs = form.function_spaces[0]
+    Ks, ts = [], []
+    for e in spec["emat"]:
+        nodes = mesh.elements[e].astype(np.int64)
+        K_e, t_e = form.GetLocalStiffness(fs, mat, mesh.points[nodes], x[nodes], phi[nodes], solver, e)
+        Ks.append(K_e)
+        ts.append(np.asarray(t_e).ravel())
+    out = dict(
+        points=mesh.points, elements=mesh.elements.astype(np.int64), Eulerx=x, Eulerp=phi,
+        Jm=fs.Jm, AllGauss=fs.AllGauss.ravel(), Bases=fs.Bases, nvar=np.array(4),
+        material=np.array(spec["material"]), params=np.array(spec["params"], np.float64),
+        update=np.array(int(solver.requires_geometry_update)),
+        K_indptr=K.indptr.astype(np.int32), K_indices=K.indices.astype(np.int32), K_data=K.data,
+        T=np.asarray(T).ravel(),
+        sp_indices=solver.indices.astype(np.int32), sp_indptr=solver.indptr.astype(np.int32),
+        sp_data_local=solver.data_local_indices.astype(np.int32),
+        sp_data_global=solver.data_global_indices.astype(np.int32),
+        emat_ids=np.array(spec["emat"], np.int64), emat_K=np.array(Ks), emat_t=np.array(ts),
+    )
+    np.savez_compressed(os.path.join(HERE, spec["name"] + ".npz"), **out)
+    print("%-22s E=%-4d npe=%-3d nq=%-3d nnz=%-8d %.1fs" % (spec["name"], mesh.nelem, mesh.elements.shape[1],
+          fs.AllGauss.shape[0], K.nnz, time.time() - t0), flush=True)
+
+
 def make_config1(F):
     """Structured 8x8x8 p=2 hex cube, Gauss order 5 (125 points), neo-Hookean mu=1, lambda=10,
     u ~ U(-0.01, 0.01) per dof from default_rng(0). The full CSR is too large to commit, so the
@@ -300,5 +351,8 @@ if __name__ == "__main__":
     for spec in CASES:
         if not only or spec["name"] in only:
             make_case(F, spec)
+    for spec in DPF_CASES:
+        if not only or spec["name"] in only:
+            make_dpf_case(F, spec)
     if not only or "config1" in only:
         make_config1(F)

@@ -1,0 +1,44 @@
+"""The displacement-potential (electromechanics) oracle against golden vectors made by the
+reference's own numpy DPF path (DisplacementPotentialFormulation.py:108-200 with
+IsotropicElectroMechanics_108): element matrices, the global tangent and the residual; and the
+reference's nvar=4 sparsity pattern reproduced by the CPU sparsity oracle."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from conftest import dpf_cases, load_golden, rel_fro
+from oracle import dpf_oracle
+
+TOL = 1e-12
+
+
+@pytest.mark.parametrize("case", dpf_cases())
+def test_dpf_element_matrices(case):
+    d = load_golden(case)
+    for k, e in enumerate(d["emat_ids"]):
+        nodes = d["elements"][e]
+        K, t = dpf_oracle.element(str(d["material"]), tuple(d["params"]), d["points"][nodes], d["Eulerx"][nodes],
+                                  d["Eulerp"][nodes], d["Jm"], np.ravel(d["AllGauss"]), int(d["update"]))
+        assert rel_fro(K, d["emat_K"][k]) < TOL
+        assert rel_fro(t, d["emat_t"][k]) < TOL
+
+
+@pytest.mark.parametrize("case", dpf_cases())
+def test_dpf_global_tangent_and_residual(case):
+    d = load_golden(case)
+    K, T = dpf_oracle.assemble(str(d["material"]), tuple(d["params"]), d["points"], d["elements"], d["Eulerx"],
+                               d["Eulerp"], d["Jm"], d["AllGauss"], int(d["update"]))
+    n = K.shape[0]
+    ref = sp.csr_matrix((d["K_data"], d["K_indices"], d["K_indptr"]), shape=(n, n)).toarray()
+    assert rel_fro(K, ref) < TOL
+    assert rel_fro(T, d["T"]) < TOL
+    # the tangent is symmetric (an enthalpy Hessian); the electric block is negative definite
+    assert np.abs(K - K.T).max() <= 1e-12 * np.abs(K).max()
+
+
+@pytest.mark.parametrize("case", dpf_cases())
+def test_dpf_sparsity_pattern_nvar4(oracle, case):
+    d = load_golden(case)
+    ind, ptr, dl, dg = oracle.sparsity(d["elements"], d["points"].shape[0], nvar=4)
+    assert np.array_equal(ind, d["sp_indices"]) and np.array_equal(ptr, d["sp_indptr"])
+    assert np.array_equal(dl, d["sp_data_local"]) and np.array_equal(dg, d["sp_data_global"])
