@@ -1,7 +1,8 @@
 """florence_gb300 -- GB300-native (sm_103a) low-level finite-element assembly for Florence's
 displacement formulation: fused FP64 tangent + residual kernels, a device-built CSR pattern
-with the reference's element-to-nonzero maps, a matrix-free explicit internal force and the
-lumped mass, behind Florence's own low-level assembly interface.
+with the reference's element-to-nonzero maps, a matrix-free explicit internal force, lumped and
+consistent mass, external forces, the displacement-potential (electromechanics) assembly and
+high-order tet meshing, behind Florence's own low-level assembly interface.
 
 The CUDA library (libflorence_gb300.so, built in-tree) is required: nothing here falls back to
 the CPU.
@@ -14,8 +15,10 @@ from .assembly import (AssembleBodyForces, AssembleExternalTractionForces, Compu
                        __TotalConstantMassIntegrand__, arithmetic, device_sparsity, fp32_peak_gflops, fp64_peak_gflops,
                        get_arithmetic, install, material_params, release_host_buffers, set_arithmetic,
                        set_tensor_core_tiling)
+from .electromechanics import DPFAssembler, _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_
 
-__all__ = ["AssembleBodyForces", "AssembleExternalTractionForces", "ComputeSparsityPattern", "DeviceAssembler", "_LowLevelAssemblyDF__NeoHookean_",
+__all__ = ["AssembleBodyForces", "AssembleExternalTractionForces", "ComputeSparsityPattern", "DeviceAssembler", "DPFAssembler",
+           "_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_", "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",
            "_LowLevelAssemblyDF__LinearElastic_", "_LowLevelAssemblyExplicit_DF_DPF_",

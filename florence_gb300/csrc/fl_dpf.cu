@@ -1,0 +1,173 @@
+// fl_dpf.cu -- global displacement-potential (electromechanics) assembly: the reference's
+// _GlobalAssemblyDPF_ (FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.h:8-198),
+// monomorphised for IsotropicElectroMechanics_108 as AOT_Assembler.py:125-175 does it, with its
+// tangent scattered like fill_global_data (triplets in element-local order, CSR through the
+// element-to-nonzero maps, or CSR by row search) and its residual accumulated into T[4 N].
+//
+// One CTA per element (grid-stride): the element's coordinates and potentials are staged in
+// shared memory; a thread per Gauss point computes the spatial gradients, weight, electric
+// displacement, stress and 9x9 Hessian (fl_dpf.cuh) into shared memory; then a thread per tangent
+// entry sums its Gauss-point contributions and scatters it, and a thread per dof its residual.
+// Node ids and map entries are range-checked (FL_FLAG_BAD_INDEX, the entry is skipped);
+// det F <= 0 sets FL_FLAG_NONPOSITIVE_J.
+#include <algorithm>
+
+#include "fl_common.cuh"
+#include "fl_dpf.cuh"
+
+namespace fl {
+
+constexpr int DP_NT = 128;
+
+struct DpfArgs {
+    const double *points, *Eulerx, *Eulerp, *Jm, *w;
+    const uint64_t *elements;
+    int64_t nelem, nnode;
+    int npe, nq, update, mode;  // mode 0 CSR through maps, 1 triplets, 2 CSR by row search
+    const int32_t *indptr, *indices, *dl, *dg;
+    int64_t nnz;
+    int32_t *I, *J;
+    double *V, *T;
+    dpf::Em108 mat;
+    int *err;
+};
+
+// shared-memory doubles per element: X, x [3 npe], phi [npe], node ids [npe], SG [3 npe nq],
+// H [81 nq], sigma [9 nq], D [3 nq], dv [nq]
+__host__ __device__ inline size_t dpf_smem_doubles(int npe, int nq) {
+    return (size_t)8 * npe + (size_t)3 * npe * nq + (size_t)94 * nq;
+}
+
+__global__ void __launch_bounds__(DP_NT) dpf_kernel(const DpfArgs A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int npe = A.npe, nq = A.nq;
+    double *X = reinterpret_cast<double *>(smem_raw);
+    double *x = X + 3 * npe;
+    double *phi = x + 3 * npe;
+    int64_t *node = reinterpret_cast<int64_t *>(phi + npe);
+    double *SG = reinterpret_cast<double *>(node + npe);
+    double *H = SG + (size_t)3 * npe * nq;
+    double *sig = H + (size_t)81 * nq;
+    double *D = sig + (size_t)9 * nq;
+    double *dv = D + (size_t)3 * nq;
+    const int ndof = dpf::NV * npe;
+    const int64_t cap = (int64_t)ndof * ndof;
+    for (int64_t e = blockIdx.x; e < A.nelem; e += gridDim.x) {
+        for (int a = threadIdx.x; a < npe; a += DP_NT) {
+            const uint64_t nd = A.elements[e * npe + a];
+            const bool ok = nd < (uint64_t)A.nnode;
+            if (!ok && A.err) atomicOr(A.err, FL_FLAG_BAD_INDEX);
+            node[a] = ok ? (int64_t)nd : -1;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                X[a * 3 + d] = ok ? A.points[nd * 3 + d] : 0.0;
+                x[a * 3 + d] = ok ? A.Eulerx[nd * 3 + d] : 0.0;
+            }
+            phi[a] = ok ? A.Eulerp[nd] : 0.0;
+        }
+        __syncthreads();
+        for (int g = threadIdx.x; g < nq; g += DP_NT) {
+            const double J = dpf::gauss_point(npe, nq, g, A.Jm, A.w[g], X, x, phi, A.update, A.mat,
+                                              SG + (size_t)3 * npe * g, dv + g, D + 3 * g, sig + 9 * g, H + 81 * g);
+            if (!(J > 0.0) && A.err) atomicOr(A.err, FL_FLAG_NONPOSITIVE_J);
+        }
+        __syncthreads();
+        if (A.mode == 1) {  // triplets, entry e*ndof^2 + r*ndof + c
+            for (int64_t k = threadIdx.x; k < cap; k += DP_NT) {
+                const int r = (int)(k / ndof), c = (int)(k % ndof);
+                const int a = r / dpf::NV, v = r % dpf::NV, b = c / dpf::NV, u = c % dpf::NV;
+                double s = 0.0;
+                for (int g = 0; g < nq; ++g)
+                    s += dv[g] * dpf::entry(a, v, b, u, npe, SG + (size_t)3 * npe * g, H + 81 * g, sig + 9 * g);
+                const int64_t na = node[a] < 0 ? 0 : node[a], nb = node[b] < 0 ? 0 : node[b];
+                A.I[e * cap + k] = (int32_t)(dpf::NV * na + v);
+                A.J[e * cap + k] = (int32_t)(dpf::NV * nb + u);
+                A.V[e * cap + k] = s;
+            }
+        } else if (A.mode == 0) {  // CSR through the element-to-nonzero maps
+            for (int64_t k = threadIdx.x; k < cap; k += DP_NT) {
+                const int32_t lk = A.dl[e * cap + k], pos = A.dg[e * cap + k];
+                if (lk < 0 || lk >= cap || pos < 0 || pos >= A.nnz) {
+                    if (A.err) atomicOr(A.err, FL_FLAG_BAD_INDEX);
+                    continue;
+                }
+                const int r = lk / ndof, c = lk % ndof;
+                const int a = r / dpf::NV, v = r % dpf::NV, b = c / dpf::NV, u = c % dpf::NV;
+                double s = 0.0;
+                for (int g = 0; g < nq; ++g)
+                    s += dv[g] * dpf::entry(a, v, b, u, npe, SG + (size_t)3 * npe * g, H + 81 * g, sig + 9 * g);
+                atomicAdd(A.V + pos, s);
+            }
+        } else {  // CSR, the column searched in each row
+            for (int64_t k = threadIdx.x; k < cap; k += DP_NT) {
+                const int r = (int)(k / ndof), c = (int)(k % ndof);
+                const int a = r / dpf::NV, v = r % dpf::NV, b = c / dpf::NV, u = c % dpf::NV;
+                if (node[a] < 0 || node[b] < 0) continue;
+                double s = 0.0;
+                for (int g = 0; g < nq; ++g)
+                    s += dv[g] * dpf::entry(a, v, b, u, npe, SG + (size_t)3 * npe * g, H + 81 * g, sig + 9 * g);
+                const int64_t row = dpf::NV * node[a] + v;
+                const int32_t col = (int32_t)(dpf::NV * node[b] + u);
+                int lo = A.indptr[row], hi = A.indptr[row + 1];
+                while (lo < hi) {
+                    const int mid = lo + (hi - lo) / 2;
+                    if (A.indices[mid] < col) lo = mid + 1;
+                    else hi = mid;
+                }
+                if (lo < A.indptr[row + 1] && A.indices[lo] == col) atomicAdd(A.V + lo, s);
+                else if (A.err) atomicOr(A.err, FL_FLAG_BAD_INDEX);
+            }
+        }
+        if (A.update)
+            for (int r = threadIdx.x; r < ndof; r += DP_NT) {
+                const int a = r / dpf::NV, v = r % dpf::NV;
+                if (node[a] < 0) continue;
+                double s = 0.0;
+                for (int g = 0; g < nq; ++g)
+                    s += dv[g] * dpf::residual(a, v, npe, SG + (size_t)3 * npe * g, D + 3 * g, sig + 9 * g);
+                atomicAdd(A.T + dpf::NV * node[a] + v, s);
+            }
+        __syncthreads();  // shared memory is reused by the next element
+    }
+}
+
+}  // namespace fl
+
+extern "C" int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements; (void)sorter;
+    (void)rho; (void)mu; (void)mu3; (void)mue; (void)eps_1; (void)eps_3; (void)eps_e; (void)anisotropic_orientations;
+    if (ndim != 3 || nvar != 4 || H_VoigtSize != 9) return FL_ERR_ARG;
+    if (nelem == 0 && nnode > 0 && ngauss > 0) return FL_OK;  // nothing is read or written
+    if (!points || !elements || !Eulerx || !Eulerp || !Jm || !AllGauss || !V_stiff || !T || nelem < 0 ||
+        nnode <= 0 || ngauss <= 0 || nodeperelem <= 0 || !(eps_2 != 0.0))
+        return FL_ERR_ARG;
+    fl::DpfArgs A{};
+    A.points = points; A.Eulerx = Eulerx; A.Eulerp = Eulerp; A.Jm = Jm; A.w = AllGauss; A.elements = elements;
+    A.nelem = nelem; A.nnode = nnode; A.npe = (int)nodeperelem; A.nq = (int)ngauss;
+    A.update = requires_geometry_update ? 1 : 0;
+    A.V = V_stiff; A.T = T; A.err = flags;
+    A.mat = fl::dpf::Em108{mu1, mu2, lamb, eps_2};
+    const int64_t ndof = 4 * nodeperelem;
+    if (recompute_sparsity_pattern) {
+        if (!I_stiff || !J_stiff) return FL_ERR_ARG;
+        if (nnode * 4 > INT32_MAX || ndof * ndof * nelem > ((int64_t)1 << 62)) return FL_ERR_UNSUPPORTED;
+        A.mode = 1; A.I = I_stiff; A.J = J_stiff;
+    } else if (squeeze_sparsity_pattern) {
+        if (!I_stiff || !J_stiff) return FL_ERR_ARG;  // indptr, indices (the reference's I/J slots)
+        A.mode = 2; A.indptr = I_stiff; A.indices = J_stiff;
+    } else {
+        if (!I_stiff || !data_local_indices || !data_global_indices) return FL_ERR_ARG;
+        A.mode = 0; A.dl = data_local_indices; A.dg = data_global_indices;
+        int32_t nnz32 = 0;  // indptr[4 N]: the pattern's size, read once
+        FL_CUDA_TRY(cudaMemcpyAsync(&nnz32, I_stiff + 4 * nnode, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                    (cudaStream_t)stream));
+        FL_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+        A.nnz = nnz32;
+    }
+    const size_t smem = sizeof(double) * fl::dpf_smem_doubles((int)nodeperelem, (int)ngauss);
+    if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
+    { const int st = fl::ensure_smem<fl::dpf_kernel>(smem); if (st != FL_OK) return st; }
+    const unsigned grid = (unsigned)std::min<int64_t>(nelem, 152 * 16);
+    fl::dpf_kernel<<<grid, fl::DP_NT, smem, (cudaStream_t)stream>>>(A);
+    return fl::launch_status();
+}

@@ -1,0 +1,213 @@
+// fl_dpf.cuh -- Gauss-point and matrix-entry arithmetic of the displacement-potential
+// (electromechanics) assembly: three displacements and the electric potential per node (nvar 4),
+// a 9x9 Hessian (6 Voigt stresses + 3 electric displacements). Plain C++ so that the device kernel
+// (fl_dpf.cu) and a host build of the same source use identical arithmetic.
+//
+// Reference (paths inside the Florence repository):
+//   the element integral     FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.h:8-198,
+//                            VariationalPrinciple/DisplacementPotentialFormulation.py:108-200
+//   B rows and traction      VariationalPrinciple/_ConstitutiveStiffness_/DisplacementPotentialApproachIndices.pyx:1-50, :203-230
+//                            (Voigt order xx, yy, zz, xy, xz, yz; the potential's row carries grad N)
+//   material 108             MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_108_.h:32-112
+//   Legendre transform       MaterialLibrary/LLDispatch/CythonSource/_LegendreTransform_.h (InternalEnergyToEnthalpy)
+//   symmetric Voigt forms    Tensor/Numeric.pyx:166-270
+#pragma once
+#include <cmath>
+
+#ifdef __CUDACC__
+#define FL_HD __host__ __device__ __forceinline__
+#else
+#define FL_HD inline
+#endif
+
+namespace fl {
+namespace dpf {
+
+constexpr int NV = 4;  // fields per node
+constexpr int HV = 9;  // Hessian size
+
+// Voigt index I -> tensor index pair: 0 xx, 1 yy, 2 zz, 3 xy, 4 xz, 5 yz
+FL_HD int vp0(int I) { return I < 3 ? I : (I == 5 ? 1 : 0); }
+FL_HD int vp1(int I) { return I < 3 ? I : (I == 3 ? 1 : 2); }
+FL_HD double kd(int i, int j) { return i == j ? 1.0 : 0.0; }
+
+FL_HD double det3(const double *m) {
+    return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
+}
+
+// inverse of a 3x3 matrix (row-major) by cofactors; returns the determinant
+FL_HD double inv3(const double *m, double *r) {
+    const double d = det3(m);
+    const double id = 1.0 / d;
+    r[0] = (m[4] * m[8] - m[5] * m[7]) * id;
+    r[1] = (m[2] * m[7] - m[1] * m[8]) * id;
+    r[2] = (m[1] * m[5] - m[2] * m[4]) * id;
+    r[3] = (m[5] * m[6] - m[3] * m[8]) * id;
+    r[4] = (m[0] * m[8] - m[2] * m[6]) * id;
+    r[5] = (m[2] * m[3] - m[0] * m[5]) * id;
+    r[6] = (m[3] * m[7] - m[4] * m[6]) * id;
+    r[7] = (m[1] * m[6] - m[0] * m[7]) * id;
+    r[8] = (m[0] * m[4] - m[1] * m[3]) * id;
+    return d;
+}
+
+// IsotropicElectroMechanics_108: internal energy
+//   W(C, D) = mu1 C:I + mu2 G:I - 2 (mu1 + 2 mu2) ln J + lamb/2 (J - 1)^2 + |F D0|^2 / (2 eps_2 J)
+struct Em108 {
+    double mu1, mu2, lamb, eps2;
+};
+
+// coupling tensor of the internal energy, (delta_ik D_j + D_i delta_jk - delta_ij D_k) / eps_2
+FL_HD double em108_wcp(int i, int j, int k, const double *D, double ie) {
+    return ie * (kd(i, k) * D[j] + D[i] * kd(j, k) - kd(i, j) * D[k]);
+}
+
+// elasticity tensor of the internal energy at (i, j, k, l)
+FL_HD double em108_wel(int i, int j, int k, int l, const double *b, const double *D, double J, double DD,
+                       const Em108 &m) {
+    const double ie = 1.0 / m.eps2;
+    const double sym = kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k);
+    const double dd = kd(i, j) * kd(k, l);
+    return 2.0 * m.mu2 / J * (2.0 * b[i * 3 + j] * b[k * 3 + l] - b[i * 3 + k] * b[j * 3 + l] - b[i * 3 + l] * b[j * 3 + k]) +
+           (2.0 * (m.mu1 + 2.0 * m.mu2) / J - m.lamb * (J - 1.0)) * sym + m.lamb * (2.0 * J - 1.0) * dd +
+           ie * (0.5 * DD * (sym + dd) - kd(i, j) * D[k] * D[l] - D[i] * D[j] * kd(k, l));
+}
+
+// electric displacement D = eps_2 E, Cauchy stress sigma[9], and the electric-enthalpy Hessian
+// H[9x9] = [[C, -P], [-P^T, -eps_2 I]]: the internal energy's dielectric tensor I / eps_2 inverts
+// to eps_2 I, the enthalpy coupling is eps_2 times the internal one, and the enthalpy elasticity
+// subtracts eps_2 sum_n W_cp(i,j,n) W_cp(k,l,n); C and P are their symmetric Voigt forms
+FL_HD void em108_point(const double *F, const double *E, const Em108 &m, double *D, double *sigma, double *H) {
+    const double J = det3(F);
+    double b[9];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) b[i * 3 + j] = F[i * 3] * F[j * 3] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
+    for (int k = 0; k < 3; ++k) D[k] = m.eps2 * E[k];
+    const double DD = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    const double trb = b[0] + b[4] + b[8];
+    const double ie = 1.0 / m.eps2;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const double bb = b[i * 3] * b[j] + b[i * 3 + 1] * b[3 + j] + b[i * 3 + 2] * b[6 + j];
+            sigma[i * 3 + j] = 2.0 * m.mu1 / J * b[i * 3 + j] + 2.0 * m.mu2 / J * (trb * b[i * 3 + j] - bb) -
+                               2.0 * (m.mu1 + 2.0 * m.mu2) / J * kd(i, j) + m.lamb * (J - 1.0) * kd(i, j) +
+                               ie * (D[i] * D[j] - 0.5 * DD * kd(i, j));
+        }
+    for (int I = 0; I < 6; ++I) {
+        const int i = vp0(I), j = vp1(I);
+        for (int K = I; K < 6; ++K) {
+            const int k = vp0(K), l = vp1(K);
+            double h1 = em108_wel(i, j, k, l, b, D, J, DD, m), h2 = em108_wel(i, j, l, k, b, D, J, DD, m);
+            for (int n = 0; n < 3; ++n) {
+                h1 -= m.eps2 * em108_wcp(i, j, n, D, ie) * em108_wcp(k, l, n, D, ie);
+                h2 -= m.eps2 * em108_wcp(i, j, n, D, ie) * em108_wcp(l, k, n, D, ie);
+            }
+            H[I * HV + K] = H[K * HV + I] = 0.5 * (h1 + h2);
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double P = 0.5 * m.eps2 * (em108_wcp(i, j, k, D, ie) + em108_wcp(j, i, k, D, ie));
+            H[I * HV + 6 + k] = H[(6 + k) * HV + I] = -P;
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) H[(6 + k) * HV + 6 + l] = -m.eps2 * kd(k, l);
+}
+
+// Gauss point g of one element: spatial gradients SG[d * npe + a] (material gradients when the
+// geometry is not updated), the weight dv = w |det dX/dxi| (|J| too with the update), the spatial
+// electric field E = -grad phi, and the material's D, sigma and H. X, x [npe * 3], phi [npe];
+// Jm [3 * npe * nq] (d-major, then node, then point). Returns det F.
+FL_HD double gauss_point(int npe, int nq, int g, const double *Jm, double w, const double *X, const double *x,
+                         const double *phi, int update, const Em108 &m, double *SG, double *dv, double *D,
+                         double *sigma, double *H) {
+    double GX[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, iGX[9];
+    for (int a = 0; a < npe; ++a)
+        for (int d = 0; d < 3; ++d) {
+            const double j = Jm[(d * npe + a) * nq + g];
+            for (int k = 0; k < 3; ++k) GX[d * 3 + k] += j * X[a * 3 + k];
+        }
+    const double detX = inv3(GX, iGX);
+    double F[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < npe; ++a) {
+        double mg[3];
+        for (int J = 0; J < 3; ++J)
+            mg[J] = iGX[J * 3] * Jm[a * nq + g] + iGX[J * 3 + 1] * Jm[(npe + a) * nq + g] +
+                    iGX[J * 3 + 2] * Jm[(2 * npe + a) * nq + g];
+        for (int i = 0; i < 3; ++i)
+            for (int J = 0; J < 3; ++J) F[i * 3 + J] += x[a * 3 + i] * mg[J];
+        if (!update)
+            for (int d = 0; d < 3; ++d) SG[d * npe + a] = mg[d];
+    }
+    const double detF = det3(F);
+    if (update) {
+        double Gx[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, iGx[9];
+        for (int a = 0; a < npe; ++a)
+            for (int d = 0; d < 3; ++d) {
+                const double j = Jm[(d * npe + a) * nq + g];
+                for (int k = 0; k < 3; ++k) Gx[d * 3 + k] += j * x[a * 3 + k];
+            }
+        inv3(Gx, iGx);
+        for (int a = 0; a < npe; ++a)
+            for (int l = 0; l < 3; ++l)
+                SG[l * npe + a] = iGx[l * 3] * Jm[a * nq + g] + iGx[l * 3 + 1] * Jm[(npe + a) * nq + g] +
+                                  iGx[l * 3 + 2] * Jm[(2 * npe + a) * nq + g];
+        *dv = w * std::fabs(detX) * std::fabs(detF);
+    } else {
+        *dv = w * std::fabs(detX);
+    }
+    double E[3] = {0, 0, 0};
+    for (int a = 0; a < npe; ++a)
+        for (int k = 0; k < 3; ++k) E[k] -= SG[k * npe + a] * phi[a];
+    em108_point(F, E, m, D, sigma, H);
+    return detF;
+}
+
+// nonzero columns and values of the B row of field v (0-2 displacement, 3 potential) of a node
+// with spatial gradient (gx, gy, gz)
+FL_HD void brow(int v, double gx, double gy, double gz, int *c, double *s) {
+    if (v == 0) {
+        c[0] = 0; c[1] = 3; c[2] = 4;
+        s[0] = gx; s[1] = gy; s[2] = gz;
+    } else if (v == 1) {
+        c[0] = 1; c[1] = 3; c[2] = 5;
+        s[0] = gy; s[1] = gx; s[2] = gz;
+    } else if (v == 2) {
+        c[0] = 2; c[1] = 4; c[2] = 5;
+        s[0] = gz; s[1] = gx; s[2] = gy;
+    } else {
+        c[0] = 6; c[1] = 7; c[2] = 8;
+        s[0] = gx; s[1] = gy; s[2] = gz;
+    }
+}
+
+// one Gauss point's contribution (without dv) to the tangent entry of (node a, field v) x
+// (node b, field u): B H B^T plus the geometric term grad N_a . sigma . grad N_b on equal
+// displacement fields
+FL_HD double entry(int a, int v, int b, int u, int npe, const double *SG, const double *H, const double *sigma) {
+    const double ga[3] = {SG[a], SG[npe + a], SG[2 * npe + a]};
+    const double gb[3] = {SG[b], SG[npe + b], SG[2 * npe + b]};
+    int ca[3], cb[3];
+    double sa[3], sb[3];
+    brow(v, ga[0], ga[1], ga[2], ca, sa);
+    brow(u, gb[0], gb[1], gb[2], cb, sb);
+    double r = 0.0;
+    for (int p = 0; p < 3; ++p)
+        for (int q = 0; q < 3; ++q) r += sa[p] * H[ca[p] * HV + cb[q]] * sb[q];
+    if (v == u && v < 3)
+        for (int k = 0; k < 3; ++k)
+            for (int l = 0; l < 3; ++l) r += ga[k] * sigma[k * 3 + l] * gb[l];
+    return r;
+}
+
+// one Gauss point's contribution (without dv) to the residual of (node a, field v): the B row
+// against (sigma_xx, sigma_yy, sigma_zz, sigma_xy, sigma_xz, sigma_yz, D)
+FL_HD double residual(int a, int v, int npe, const double *SG, const double *D, const double *sigma) {
+    const double tt[9] = {sigma[0], sigma[4], sigma[8], sigma[1], sigma[2], sigma[5], D[0], D[1], D[2]};
+    int c[3];
+    double s[3];
+    brow(v, SG[a], SG[npe + a], SG[2 * npe + a], c, s);
+    return s[0] * tt[c[0]] + s[1] * tt[c[1]] + s[2] * tt[c[2]];
+}
+
+}  // namespace dpf
+}  // namespace fl

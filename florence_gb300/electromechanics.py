@@ -1,0 +1,114 @@
+"""Displacement-potential (electromechanics) assembly on the GPU: three displacements and the
+electric potential per node (nvar 4, global dof 4 n + v), IsotropicElectroMechanics_108.
+
+* ``DPFAssembler`` keeps the mesh, function-space tables and the nvar=4 CSR pattern on the device
+  and assembles the tangent and residual from device coordinates and potentials
+  (``fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_``).
+* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_`` is the drop-in for the reference's
+  Cython wrapper (Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.pyx:53-160):
+  the reference's dispatcher (_LowLevelAssembly_.py:45-83) finds it by name when
+  ``formulation.fields == "electro_mechanics"``; ``florence_gb300.install`` registers it.
+
+There is no CPU path: a missing library raises.
+"""
+import numpy as np
+import torch
+
+from . import _native as N
+from .assembly import _HOST, _check_flags, _ptr, _stream, _to_dev, device_sparsity
+
+NVAR = 4
+MATERIALS = {"IsotropicElectroMechanics_108": "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_"}
+
+
+class DPFAssembler:
+    """points [N,3], elements [E,npe], Jm [3,npe,nq], AllGauss [nq]; params (mu1, mu2, lamb, eps_2);
+    mode 'csr' (element-to-nonzero maps), 'squeeze' (row search) or 'triplet'."""
+
+    def __init__(self, points, elements, Jm, AllGauss, params, material="IsotropicElectroMechanics_108",
+                 mode="csr", device="cuda", requires_geometry_update=1, sparsity=None):
+        if material not in MATERIALS:
+            raise NotImplementedError("the GB300 DPF assembly provides " + ", ".join(MATERIALS))
+        self.device = torch.device(device)
+        self.points = _to_dev(points, torch.float64, self.device)
+        self.elements = _to_dev(elements, torch.int64, self.device)
+        self.Jm = _to_dev(Jm, torch.float64, self.device)
+        self.w = _to_dev(np.ravel(AllGauss) if not isinstance(AllGauss, torch.Tensor) else AllGauss.reshape(-1),
+                         torch.float64, self.device)
+        self.nnode = self.points.shape[0]
+        self.nelem, self.npe = self.elements.shape
+        self.nq = self.w.shape[0]
+        self.ndof = NVAR * self.npe
+        self.entry = MATERIALS[material]
+        self.params = tuple(float(p) for p in params)
+        if len(self.params) != 4:
+            raise ValueError("IsotropicElectroMechanics_108 takes (mu1, mu2, lamb, eps_2)")
+        self.mode = mode
+        self.update = int(requires_geometry_update)
+        self.flags = torch.zeros(1, dtype=torch.int32, device=self.device)
+        if mode in ("csr", "squeeze"):
+            if sparsity is None:
+                sparsity = device_sparsity(self.elements, self.nnode, NVAR, maps=(mode == "csr"))
+            ind, ptr, dl, dg = sparsity
+            self.indices = _to_dev(ind, torch.int32, self.device)
+            self.indptr = _to_dev(ptr, torch.int32, self.device)
+            self.data_local = _to_dev(dl, torch.int32, self.device) if mode == "csr" else None
+            self.data_global = _to_dev(dg, torch.int32, self.device) if mode == "csr" else None
+            self.nnz = self.indices.shape[0]
+        elif mode != "triplet":
+            raise ValueError("mode must be 'csr', 'squeeze' or 'triplet'")
+
+    def assemble(self, Eulerx, Eulerp, V=None, T=None, stream=None):
+        """Tangent and residual at device coordinates Eulerx [N,3] and potentials Eulerp [N].
+        Returns (V, T), or (I, J, V, T) in triplet mode; accumulates into V/T when given."""
+        L = N.lib()
+        x = Eulerx.contiguous()
+        p = Eulerp.reshape(-1).contiguous()
+        if T is None:
+            T = torch.zeros(self.nnode * NVAR, dtype=torch.float64, device=self.device)
+        if self.mode == "triplet":
+            cap = self.nelem * self.ndof * self.ndof
+            I = torch.empty(cap, dtype=torch.int32, device=self.device)
+            J = torch.empty(cap, dtype=torch.int32, device=self.device)
+            V = torch.empty(cap, dtype=torch.float64, device=self.device) if V is None else V
+            Ip, Jp, dl, dg = I, J, None, None
+        else:
+            V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
+            Ip, Jp, dl, dg = self.indptr, self.indices, self.data_local, self.data_global
+        mu1, mu2, lamb, eps_2 = self.params
+        st = getattr(L, self.entry)(
+            _ptr(self.points), _ptr(self.elements), _ptr(x), _ptr(p), None, _ptr(self.Jm), _ptr(self.w), 3, NVAR,
+            self.nq, self.nelem, self.npe, self.nnode, 9, self.update, None, None, _ptr(Ip), _ptr(Jp), _ptr(V),
+            _ptr(T), 1 if self.mode == "triplet" else 0, 1 if self.mode == "squeeze" else 0, _ptr(dl), _ptr(dg),
+            None, None, 1.0, 0.0, mu1, mu2, 0.0, 0.0, lamb, 0.0, eps_2, 0.0, 0.0, None, _ptr(self.flags),
+            stream or _stream())
+        N.check(st, self.entry)
+        if self.mode == "triplet":
+            return I, J, V, T
+        return V, T
+
+    def check_flags(self, what="DPF assembly"):
+        _check_flags(self.flags, what)
+        self.flags.zero_()
+
+
+def _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_(fem_solver, function_space, formulation, mesh, material,
+                                                         Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
+    as AOT_Assembler.py builds it for _IsotropicElectroMechanics_108_ (mu1, mu2, lamb, eps_2)."""
+    if formulation.ndim != 3 or formulation.nvar != NVAR:
+        raise NotImplementedError("the GB300 DPF assembly covers three-dimensional electromechanics (nvar 4)")
+    params = (material.mu1, material.mu2, material.lamb, material.eps_2)
+    recompute = bool(fem_solver.recompute_sparsity_pattern)
+    # CSR output without uploading the two E*ndof^2 maps: each entry's position is found by row
+    # search, which lands it where the maps would
+    mode = "triplet" if recompute else "squeeze"
+    sparsity = None if recompute else (fem_solver.indices, fem_solver.indptr, None, None)
+    asm = DPFAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, params, mode=mode,
+                       requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity)
+    x = _to_dev(Eulerx, torch.float64, asm.device)
+    p = _to_dev(np.ravel(Eulerp), torch.float64, asm.device)
+    out = asm.assemble(x, p)
+    host = [_HOST.to_host(t) for t in out]
+    asm.check_flags("_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_")
+    return tuple(host)

@@ -1,0 +1,34 @@
+// Host build of the device DPF arithmetic (florence_gb300/csrc/fl_dpf.cuh), test infrastructure:
+// the element tangent and residual of one element, summed over its Gauss points exactly as the
+// kernel sums them, for comparison with the reference's golden element matrices.
+#include <vector>
+
+#include "../florence_gb300/csrc/fl_dpf.cuh"
+
+extern "C" double dpf_element(int npe, int nq, const double *Jm, const double *w, const double *X, const double *x,
+                              const double *phi, int update, double mu1, double mu2, double lamb, double eps2,
+                              double *K, double *t) {
+    using namespace fl::dpf;
+    const Em108 m{mu1, mu2, lamb, eps2};
+    const int ndof = NV * npe;
+    std::vector<double> SG(3 * npe * nq), H(HV * HV * nq), sig(9 * nq), D(3 * nq), dv(nq);
+    double minJ = 1e300;
+    for (int g = 0; g < nq; ++g) {
+        const double J = gauss_point(npe, nq, g, Jm, w[g], X, x, phi, update, m, &SG[3 * npe * g], &dv[g], &D[3 * g],
+                                     &sig[9 * g], &H[HV * HV * g]);
+        minJ = J < minJ ? J : minJ;
+    }
+    for (int r = 0; r < ndof; ++r) {
+        for (int c = 0; c < ndof; ++c) {
+            double s = 0.0;
+            for (int g = 0; g < nq; ++g)
+                s += dv[g] * entry(r / NV, r % NV, c / NV, c % NV, npe, &SG[3 * npe * g], &H[HV * HV * g], &sig[9 * g]);
+            K[r * ndof + c] = s;
+        }
+        double s = 0.0;
+        if (update)
+            for (int g = 0; g < nq; ++g) s += dv[g] * residual(r / NV, r % NV, npe, &SG[3 * npe * g], &D[3 * g], &sig[9 * g]);
+        t[r] = s;
+    }
+    return minJ;
+}

@@ -42,3 +42,42 @@ def test_dpf_sparsity_pattern_nvar4(oracle, case):
     ind, ptr, dl, dg = oracle.sparsity(d["elements"], d["points"].shape[0], nvar=4)
     assert np.array_equal(ind, d["sp_indices"]) and np.array_equal(ptr, d["sp_indptr"])
     assert np.array_equal(dl, d["sp_data_local"]) and np.array_equal(dg, d["sp_data_global"])
+
+
+@pytest.fixture(scope="module")
+def dpf_host(tmp_path_factory):
+    """Host build of the device kernel's DPF arithmetic (florence_gb300/csrc/fl_dpf.cuh)."""
+    import ctypes
+    import os
+    import subprocess
+    here = os.path.dirname(os.path.abspath(__file__))
+    so = str(tmp_path_factory.mktemp("dpf") / "dpf_shim.so")
+    subprocess.check_call(["g++", "-O2", "-shared", "-fPIC", "-o", so, os.path.join(here, "dpf_host_shim.cpp")])
+    L = ctypes.CDLL(so)
+    P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.dpf_element.argtypes = [I, I, P, P, P, P, P, I, D, D, D, D, P, P]
+    L.dpf_element.restype = D
+    return L
+
+
+@pytest.mark.parametrize("case", dpf_cases())
+def test_device_dpf_arithmetic_on_host(dpf_host, case):
+    """The Gauss-point and entry functions the device kernel runs, built for the host, give the
+    reference's element tangents and residuals."""
+    d = load_golden(case)
+    Jm = np.ascontiguousarray(d["Jm"], np.float64)
+    w = np.ascontiguousarray(np.ravel(d["AllGauss"]), np.float64)
+    npe, nq = Jm.shape[1], Jm.shape[2]
+    for k, e in enumerate(d["emat_ids"]):
+        nodes = d["elements"][e]
+        X = np.ascontiguousarray(d["points"][nodes], np.float64)
+        x = np.ascontiguousarray(d["Eulerx"][nodes], np.float64)
+        phi = np.ascontiguousarray(d["Eulerp"][nodes], np.float64)
+        K = np.zeros((4 * npe, 4 * npe))
+        t = np.zeros(4 * npe)
+        minJ = dpf_host.dpf_element(npe, nq, Jm.ctypes.data, w.ctypes.data, X.ctypes.data, x.ctypes.data,
+                                    phi.ctypes.data, int(d["update"]), *map(float, d["params"]), K.ctypes.data,
+                                    t.ctypes.data)
+        assert minJ > 0
+        assert rel_fro(K, d["emat_K"][k]) < TOL
+        assert rel_fro(t, d["emat_t"][k]) < TOL

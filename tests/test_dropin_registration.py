@@ -28,6 +28,11 @@ def test_install_registers_callables_in_reference_namespaces():
         name = "_LowLevelAssemblyDF__" + mat + "_"
         assert getattr(mod, name) is getattr(florence_gb300, name)
     assert mod._LowLevelAssemblyExplicit_DF_DPF_ is florence_gb300._LowLevelAssemblyExplicit_DF_DPF_
+    # the electromechanics (displacement-potential) entry, found by the dispatcher's "DPF" prefix
+    assert (mod._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_
+            is florence_gb300._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_)
+    em = F.IsotropicElectroMechanics_108(3, mu1=0.5, mu2=0.3, lamb=10.0, eps_2=2.0)
+    assert ("_LowLevelAssemblyDPF__" + type(em).__name__ + "_") in vars(mod)
     from Florence.FiniteElements.Assembly.ComputeSparsityPattern import ComputeSparsityPattern
     assert ComputeSparsityPattern is florence_gb300.ComputeSparsityPattern
     # the dispatcher's own name lookup now finds the GPU callable
