@@ -562,8 +562,9 @@ def install(florence):
     ll._LowLevelAssemblyDF__LinearElastic_ = _LowLevelAssemblyDF__LinearElastic_
     ll._LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_ = _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_
     ll._LowLevelAssemblyExplicit_DF_DPF_ = _LowLevelAssemblyExplicit_DF_DPF_
-    from .electromechanics import _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_
-    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_ = _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_
+    from . import electromechanics as em
+    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_
+    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_101_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_101_
     ll.has_low_level_dispatcher = True
     asm_mod = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly.Assembly")
     asm_mod.AssembleExternalTractionForces = AssembleExternalTractionForces

@@ -1,6 +1,6 @@
 // fl_dpf.cu -- global displacement-potential (electromechanics) assembly: the reference's
 // _GlobalAssemblyDPF_ (FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.h:8-198),
-// monomorphised for IsotropicElectroMechanics_108 as AOT_Assembler.py:125-175 does it, with its
+// monomorphised for IsotropicElectroMechanics_101 and _108 as AOT_Assembler.py:125-220 does it, with its
 // tangent scattered like fill_global_data (triplets in element-local order, CSR through the
 // element-to-nonzero maps, or CSR by row search) and its residual accumulated into T[4 N].
 //
@@ -28,7 +28,6 @@ struct DpfArgs {
     int64_t nnz;
     int32_t *I, *J;
     double *V, *T;
-    dpf::Em108 mat;
     int *err;
 };
 
@@ -38,7 +37,8 @@ __host__ __device__ inline size_t dpf_smem_doubles(int npe, int nq) {
     return (size_t)8 * npe + (size_t)3 * npe * nq + (size_t)94 * nq;
 }
 
-__global__ void __launch_bounds__(DP_NT) dpf_kernel(const DpfArgs A) {
+template <class MAT>
+__global__ void __launch_bounds__(DP_NT) dpf_kernel(const DpfArgs A, const MAT mat) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int npe = A.npe, nq = A.nq;
     double *X = reinterpret_cast<double *>(smem_raw);
@@ -67,7 +67,7 @@ __global__ void __launch_bounds__(DP_NT) dpf_kernel(const DpfArgs A) {
         }
         __syncthreads();
         for (int g = threadIdx.x; g < nq; g += DP_NT) {
-            const double J = dpf::gauss_point(npe, nq, g, A.Jm, A.w[g], X, x, phi, A.update, A.mat,
+            const double J = dpf::gauss_point(npe, nq, g, A.Jm, A.w[g], X, x, phi, A.update, mat,
                                               SG + (size_t)3 * npe * g, dv + g, D + 3 * g, sig + 9 * g, H + 81 * g);
             if (!(J > 0.0) && A.err) atomicOr(A.err, FL_FLAG_NONPOSITIVE_J);
         }
@@ -131,22 +131,25 @@ __global__ void __launch_bounds__(DP_NT) dpf_kernel(const DpfArgs A) {
     }
 }
 
-}  // namespace fl
-
-extern "C" int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
-    (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements; (void)sorter;
-    (void)rho; (void)mu; (void)mu3; (void)mue; (void)eps_1; (void)eps_3; (void)eps_e; (void)anisotropic_orientations;
+// the reference's argument list with the material's parameters already taken out of it
+template <class MAT>
+static int dpf_assemble(const double *points, const uint64_t *elements, const double *Eulerx, const double *Eulerp,
+                        const double *Jm, const double *AllGauss, int64_t ndim, int64_t nvar, int64_t ngauss,
+                        int64_t nelem, int64_t nodeperelem, int64_t nnode, int64_t H_VoigtSize,
+                        int64_t requires_geometry_update, int32_t *I_stiff, int32_t *J_stiff, double *V_stiff,
+                        double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
+                        const int32_t *data_local_indices, const int32_t *data_global_indices, const MAT &mat,
+                        int *flags, cudaStream_t stream) {
     if (ndim != 3 || nvar != 4 || H_VoigtSize != 9) return FL_ERR_ARG;
     if (nelem == 0 && nnode > 0 && ngauss > 0) return FL_OK;  // nothing is read or written
     if (!points || !elements || !Eulerx || !Eulerp || !Jm || !AllGauss || !V_stiff || !T || nelem < 0 ||
-        nnode <= 0 || ngauss <= 0 || nodeperelem <= 0 || !(eps_2 != 0.0))
+        nnode <= 0 || ngauss <= 0 || nodeperelem <= 0)
         return FL_ERR_ARG;
-    fl::DpfArgs A{};
+    DpfArgs A{};
     A.points = points; A.Eulerx = Eulerx; A.Eulerp = Eulerp; A.Jm = Jm; A.w = AllGauss; A.elements = elements;
     A.nelem = nelem; A.nnode = nnode; A.npe = (int)nodeperelem; A.nq = (int)ngauss;
     A.update = requires_geometry_update ? 1 : 0;
     A.V = V_stiff; A.T = T; A.err = flags;
-    A.mat = fl::dpf::Em108{mu1, mu2, lamb, eps_2};
     const int64_t ndof = 4 * nodeperelem;
     if (recompute_sparsity_pattern) {
         if (!I_stiff || !J_stiff) return FL_ERR_ARG;
@@ -159,15 +162,39 @@ extern "C" int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_(FL_GLOBAL_AS
         if (!I_stiff || !data_local_indices || !data_global_indices) return FL_ERR_ARG;
         A.mode = 0; A.dl = data_local_indices; A.dg = data_global_indices;
         int32_t nnz32 = 0;  // indptr[4 N]: the pattern's size, read once
-        FL_CUDA_TRY(cudaMemcpyAsync(&nnz32, I_stiff + 4 * nnode, sizeof(int32_t), cudaMemcpyDeviceToHost,
-                                    (cudaStream_t)stream));
-        FL_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+        FL_CUDA_TRY(cudaMemcpyAsync(&nnz32, I_stiff + 4 * nnode, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+        FL_CUDA_TRY(cudaStreamSynchronize(stream));
         A.nnz = nnz32;
     }
-    const size_t smem = sizeof(double) * fl::dpf_smem_doubles((int)nodeperelem, (int)ngauss);
+    const size_t smem = sizeof(double) * dpf_smem_doubles((int)nodeperelem, (int)ngauss);
     if (smem > 227 * 1024) return FL_ERR_UNSUPPORTED;
-    { const int st = fl::ensure_smem<fl::dpf_kernel>(smem); if (st != FL_OK) return st; }
+    { const int st = ensure_smem<dpf_kernel<MAT>>(smem); if (st != FL_OK) return st; }
     const unsigned grid = (unsigned)std::min<int64_t>(nelem, 152 * 16);
-    fl::dpf_kernel<<<grid, fl::DP_NT, smem, (cudaStream_t)stream>>>(A);
-    return fl::launch_status();
+    dpf_kernel<MAT><<<grid, DP_NT, smem, stream>>>(A, mat);
+    return launch_status();
+}
+
+}  // namespace fl
+
+#define FL_DPF_FORWARD(MAT_VALUE)                                                                              \
+    fl::dpf_assemble(points, elements, Eulerx, Eulerp, Jm, AllGauss, ndim, nvar, ngauss, nelem, nodeperelem, nnode, \
+                     H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T, recompute_sparsity_pattern, \
+                     squeeze_sparsity_pattern, data_local_indices, data_global_indices, MAT_VALUE, flags,           \
+                     (cudaStream_t)stream)
+
+// mu1, mu2, lamb, eps_2 (AOT_Assembler.py:167-168, 213-214)
+extern "C" int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements; (void)sorter;
+    (void)rho; (void)mu; (void)mu3; (void)mue; (void)eps_1; (void)eps_3; (void)eps_e; (void)anisotropic_orientations;
+    if (!(eps_2 != 0.0)) return FL_ERR_ARG;
+    return FL_DPF_FORWARD((fl::dpf::Em108{mu1, mu2, lamb, eps_2}));
+}
+
+// mu, lamb, eps_1 (AOT_Assembler.py:159-160, 204-205)
+extern "C" int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements; (void)sorter;
+    (void)rho; (void)mu1; (void)mu2; (void)mu3; (void)mue; (void)eps_2; (void)eps_3; (void)eps_e;
+    (void)anisotropic_orientations;
+    if (!(eps_1 != 0.0)) return FL_ERR_ARG;
+    return FL_DPF_FORWARD((fl::dpf::Em101{mu, lamb, eps_1}));
 }

@@ -8,7 +8,8 @@
 //                            VariationalPrinciple/DisplacementPotentialFormulation.py:108-200
 //   B rows and traction      VariationalPrinciple/_ConstitutiveStiffness_/DisplacementPotentialApproachIndices.pyx:1-50, :203-230
 //                            (Voigt order xx, yy, zz, xy, xz, yz; the potential's row carries grad N)
-//   material 108             MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_108_.h:32-112
+//   materials 101, 108       MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_101_.h,
+//                            _IsotropicElectroMechanics_108_.h:32-112
 //   Legendre transform       MaterialLibrary/LLDispatch/CythonSource/_LegendreTransform_.h (InternalEnergyToEnthalpy)
 //   symmetric Voigt forms    Tensor/Numeric.pyx:166-270
 #pragma once
@@ -51,37 +52,65 @@ FL_HD double inv3(const double *m, double *r) {
     return d;
 }
 
+// Electric-enthalpy Hessian H[9x9] = [[C, -P], [-P^T, -eps I]] of an internal-energy model whose
+// dielectric tensor is isotropic, W_di = I / eps: the Legendre transform inverts it to -eps I,
+// the enthalpy coupling is eps times the internal one, and the enthalpy elasticity subtracts
+// eps sum_n W_cp(i,j,n) W_cp(k,l,n); C and P are their symmetric Voigt forms. Pt supplies the
+// internal energy's elasticity wel(i,j,k,l) and coupling wcp(i,j,k) (symmetric in i, j).
+template <class Pt>
+FL_HD void enthalpy_hessian(const Pt &pt, double eps, double *H) {
+    for (int I = 0; I < 6; ++I) {
+        const int i = vp0(I), j = vp1(I);
+        for (int K = I; K < 6; ++K) {
+            const int k = vp0(K), l = vp1(K);
+            double h1 = pt.wel(i, j, k, l), h2 = pt.wel(i, j, l, k);
+            for (int n = 0; n < 3; ++n) {
+                h1 -= eps * pt.wcp(i, j, n) * pt.wcp(k, l, n);
+                h2 -= eps * pt.wcp(i, j, n) * pt.wcp(l, k, n);
+            }
+            H[I * HV + K] = H[K * HV + I] = 0.5 * (h1 + h2);
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double P = 0.5 * eps * (pt.wcp(i, j, k) + pt.wcp(j, i, k));
+            H[I * HV + 6 + k] = H[(6 + k) * HV + I] = -P;
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) H[(6 + k) * HV + 6 + l] = -eps * kd(k, l);
+}
+
+FL_HD void left_cauchy_green(const double *F, double *b) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) b[i * 3 + j] = F[i * 3] * F[j * 3] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
+}
+
 // IsotropicElectroMechanics_108: internal energy
 //   W(C, D) = mu1 C:I + mu2 G:I - 2 (mu1 + 2 mu2) ln J + lamb/2 (J - 1)^2 + |F D0|^2 / (2 eps_2 J)
 struct Em108 {
     double mu1, mu2, lamb, eps2;
 };
 
-// coupling tensor of the internal energy, (delta_ik D_j + D_i delta_jk - delta_ij D_k) / eps_2
-FL_HD double em108_wcp(int i, int j, int k, const double *D, double ie) {
-    return ie * (kd(i, k) * D[j] + D[i] * kd(j, k) - kd(i, j) * D[k]);
-}
+struct Em108Point {
+    const double *b, *D;
+    double J, DD, ie;
+    Em108 m;
+    // elasticity tensor of the internal energy
+    FL_HD double wel(int i, int j, int k, int l) const {
+        const double sym = kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k);
+        const double dd = kd(i, j) * kd(k, l);
+        return 2.0 * m.mu2 / J * (2.0 * b[i * 3 + j] * b[k * 3 + l] - b[i * 3 + k] * b[j * 3 + l] - b[i * 3 + l] * b[j * 3 + k]) +
+               (2.0 * (m.mu1 + 2.0 * m.mu2) / J - m.lamb * (J - 1.0)) * sym + m.lamb * (2.0 * J - 1.0) * dd +
+               ie * (0.5 * DD * (sym + dd) - kd(i, j) * D[k] * D[l] - D[i] * D[j] * kd(k, l));
+    }
+    // coupling tensor, (delta_ik D_j + D_i delta_jk - delta_ij D_k) / eps_2
+    FL_HD double wcp(int i, int j, int k) const { return ie * (kd(i, k) * D[j] + D[i] * kd(j, k) - kd(i, j) * D[k]); }
+};
 
-// elasticity tensor of the internal energy at (i, j, k, l)
-FL_HD double em108_wel(int i, int j, int k, int l, const double *b, const double *D, double J, double DD,
-                       const Em108 &m) {
-    const double ie = 1.0 / m.eps2;
-    const double sym = kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k);
-    const double dd = kd(i, j) * kd(k, l);
-    return 2.0 * m.mu2 / J * (2.0 * b[i * 3 + j] * b[k * 3 + l] - b[i * 3 + k] * b[j * 3 + l] - b[i * 3 + l] * b[j * 3 + k]) +
-           (2.0 * (m.mu1 + 2.0 * m.mu2) / J - m.lamb * (J - 1.0)) * sym + m.lamb * (2.0 * J - 1.0) * dd +
-           ie * (0.5 * DD * (sym + dd) - kd(i, j) * D[k] * D[l] - D[i] * D[j] * kd(k, l));
-}
-
-// electric displacement D = eps_2 E, Cauchy stress sigma[9], and the electric-enthalpy Hessian
-// H[9x9] = [[C, -P], [-P^T, -eps_2 I]]: the internal energy's dielectric tensor I / eps_2 inverts
-// to eps_2 I, the enthalpy coupling is eps_2 times the internal one, and the enthalpy elasticity
-// subtracts eps_2 sum_n W_cp(i,j,n) W_cp(k,l,n); C and P are their symmetric Voigt forms
-FL_HD void em108_point(const double *F, const double *E, const Em108 &m, double *D, double *sigma, double *H) {
+// D = eps_2 E, Cauchy stress sigma[9] and the enthalpy Hessian; dielectric tensor I / eps_2
+FL_HD void material_point(const Em108 &m, const double *F, const double *E, double *D, double *sigma, double *H) {
     const double J = det3(F);
     double b[9];
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j) b[i * 3 + j] = F[i * 3] * F[j * 3] + F[i * 3 + 1] * F[j * 3 + 1] + F[i * 3 + 2] * F[j * 3 + 2];
+    left_cauchy_green(F, b);
     for (int k = 0; k < 3; ++k) D[k] = m.eps2 * E[k];
     const double DD = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
     const double trb = b[0] + b[4] + b[8];
@@ -93,32 +122,50 @@ FL_HD void em108_point(const double *F, const double *E, const Em108 &m, double 
                                2.0 * (m.mu1 + 2.0 * m.mu2) / J * kd(i, j) + m.lamb * (J - 1.0) * kd(i, j) +
                                ie * (D[i] * D[j] - 0.5 * DD * kd(i, j));
         }
-    for (int I = 0; I < 6; ++I) {
-        const int i = vp0(I), j = vp1(I);
-        for (int K = I; K < 6; ++K) {
-            const int k = vp0(K), l = vp1(K);
-            double h1 = em108_wel(i, j, k, l, b, D, J, DD, m), h2 = em108_wel(i, j, l, k, b, D, J, DD, m);
-            for (int n = 0; n < 3; ++n) {
-                h1 -= m.eps2 * em108_wcp(i, j, n, D, ie) * em108_wcp(k, l, n, D, ie);
-                h2 -= m.eps2 * em108_wcp(i, j, n, D, ie) * em108_wcp(l, k, n, D, ie);
-            }
-            H[I * HV + K] = H[K * HV + I] = 0.5 * (h1 + h2);
-        }
-        for (int k = 0; k < 3; ++k) {
-            const double P = 0.5 * m.eps2 * (em108_wcp(i, j, k, D, ie) + em108_wcp(j, i, k, D, ie));
-            H[I * HV + 6 + k] = H[(6 + k) * HV + I] = -P;
-        }
+    const Em108Point pt{b, D, J, DD, ie, m};
+    enthalpy_hessian(pt, m.eps2, H);
+}
+
+// IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94,
+// LLDispatch/CythonSource/_IsotropicElectroMechanics_101_.h): internal energy
+//   W(C, D0) = W_neo-Hookean(C) + |F D0|^2 / (2 eps_1)
+struct Em101 {
+    double mu, lamb, eps1;
+};
+
+struct Em101Point {
+    const double *D;
+    double J, c;  // c = J / eps_1
+    Em101 m;
+    FL_HD double wel(int i, int j, int k, int l) const {
+        return m.lamb * (2.0 * J - 1.0) * kd(i, j) * kd(k, l) +
+               (m.mu / J - m.lamb * (J - 1.0)) * (kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k));
     }
-    for (int k = 0; k < 3; ++k)
-        for (int l = 0; l < 3; ++l) H[(6 + k) * HV + 6 + l] = -m.eps2 * kd(k, l);
+    // J / eps_1 (delta_ik D_j + D_i delta_jk)
+    FL_HD double wcp(int i, int j, int k) const { return c * (kd(i, k) * D[j] + D[i] * kd(j, k)); }
+};
+
+// D = eps_1 / J E, Cauchy stress and the enthalpy Hessian; dielectric tensor J / eps_1 I
+FL_HD void material_point(const Em101 &m, const double *F, const double *E, double *D, double *sigma, double *H) {
+    const double J = det3(F);
+    double b[9];
+    left_cauchy_green(F, b);
+    for (int k = 0; k < 3; ++k) D[k] = m.eps1 / J * E[k];
+    const double c = J / m.eps1;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            sigma[i * 3 + j] = m.mu / J * (b[i * 3 + j] - kd(i, j)) + m.lamb * (J - 1.0) * kd(i, j) + c * D[i] * D[j];
+    const Em101Point pt{D, J, c, m};
+    enthalpy_hessian(pt, m.eps1 / J, H);
 }
 
 // Gauss point g of one element: spatial gradients SG[d * npe + a] (material gradients when the
 // geometry is not updated), the weight dv = w |det dX/dxi| (|J| too with the update), the spatial
 // electric field E = -grad phi, and the material's D, sigma and H. X, x [npe * 3], phi [npe];
 // Jm [3 * npe * nq] (d-major, then node, then point). Returns det F.
+template <class MAT>
 FL_HD double gauss_point(int npe, int nq, int g, const double *Jm, double w, const double *X, const double *x,
-                         const double *phi, int update, const Em108 &m, double *SG, double *dv, double *D,
+                         const double *phi, int update, const MAT &m, double *SG, double *dv, double *D,
                          double *sigma, double *H) {
     double GX[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, iGX[9];
     for (int a = 0; a < npe; ++a)
@@ -158,7 +205,7 @@ FL_HD double gauss_point(int npe, int nq, int g, const double *Jm, double w, con
     double E[3] = {0, 0, 0};
     for (int a = 0; a < npe; ++a)
         for (int k = 0; k < 3; ++k) E[k] -= SG[k * npe + a] * phi[a];
-    em108_point(F, E, m, D, sigma, H);
+    material_point(m, F, E, D, sigma, H);
     return detF;
 }
 

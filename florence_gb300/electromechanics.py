@@ -1,13 +1,13 @@
 """Displacement-potential (electromechanics) assembly on the GPU: three displacements and the
-electric potential per node (nvar 4, global dof 4 n + v), IsotropicElectroMechanics_108.
+electric potential per node (nvar 4, global dof 4 n + v), IsotropicElectroMechanics_108 and _101.
 
 * ``DPFAssembler`` keeps the mesh, function-space tables and the nvar=4 CSR pattern on the device
   and assembles the tangent and residual from device coordinates and potentials
   (``fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_``).
-* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_`` is the drop-in for the reference's
+* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_`` / ``_101_`` are the drop-ins for the reference's
   Cython wrapper (Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.pyx:53-160):
   the reference's dispatcher (_LowLevelAssembly_.py:45-83) finds it by name when
-  ``formulation.fields == "electro_mechanics"``; ``florence_gb300.install`` registers it.
+  ``formulation.fields == "electro_mechanics"``; ``florence_gb300.install`` registers them.
 
 There is no CPU path: a missing library raises.
 """
@@ -18,12 +18,18 @@ from . import _native as N
 from .assembly import _HOST, _check_flags, _ptr, _stream, _to_dev, device_sparsity
 
 NVAR = 4
-MATERIALS = {"IsotropicElectroMechanics_108": "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_"}
+# material -> (entry point, parameter names in the reference's order, AOT_Assembler.py:159-168)
+MATERIALS = {"IsotropicElectroMechanics_108": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_",
+                                               ("mu1", "mu2", "lamb", "eps_2")),
+             "IsotropicElectroMechanics_101": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_",
+                                               ("mu", "lamb", "eps_1"))}
+_ABI_SCALARS = ("rho", "mu", "mu1", "mu2", "mu3", "mue", "lamb", "eps_1", "eps_2", "eps_3", "eps_e")
 
 
 class DPFAssembler:
-    """points [N,3], elements [E,npe], Jm [3,npe,nq], AllGauss [nq]; params (mu1, mu2, lamb, eps_2);
-    mode 'csr' (element-to-nonzero maps), 'squeeze' (row search) or 'triplet'."""
+    """points [N,3], elements [E,npe], Jm [3,npe,nq], AllGauss [nq]; params (mu1, mu2, lamb, eps_2)
+    for IsotropicElectroMechanics_108, (mu, lamb, eps_1) for _101; mode 'csr' (element-to-nonzero
+    maps), 'squeeze' (row search) or 'triplet'."""
 
     def __init__(self, points, elements, Jm, AllGauss, params, material="IsotropicElectroMechanics_108",
                  mode="csr", device="cuda", requires_geometry_update=1, sparsity=None):
@@ -39,10 +45,12 @@ class DPFAssembler:
         self.nelem, self.npe = self.elements.shape
         self.nq = self.w.shape[0]
         self.ndof = NVAR * self.npe
-        self.entry = MATERIALS[material]
+        self.entry, names = MATERIALS[material]
         self.params = tuple(float(p) for p in params)
-        if len(self.params) != 4:
-            raise ValueError("IsotropicElectroMechanics_108 takes (mu1, mu2, lamb, eps_2)")
+        if len(self.params) != len(names):
+            raise ValueError("%s takes (%s)" % (material, ", ".join(names)))
+        given = dict(zip(names, self.params))
+        self.scalars = tuple(given.get(k, 1.0 if k == "rho" else 0.0) for k in _ABI_SCALARS)
         self.mode = mode
         self.update = int(requires_geometry_update)
         self.flags = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -75,13 +83,11 @@ class DPFAssembler:
         else:
             V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
             Ip, Jp, dl, dg = self.indptr, self.indices, self.data_local, self.data_global
-        mu1, mu2, lamb, eps_2 = self.params
         st = getattr(L, self.entry)(
             _ptr(self.points), _ptr(self.elements), _ptr(x), _ptr(p), None, _ptr(self.Jm), _ptr(self.w), 3, NVAR,
             self.nq, self.nelem, self.npe, self.nnode, 9, self.update, None, None, _ptr(Ip), _ptr(Jp), _ptr(V),
             _ptr(T), 1 if self.mode == "triplet" else 0, 1 if self.mode == "squeeze" else 0, _ptr(dl), _ptr(dg),
-            None, None, 1.0, 0.0, mu1, mu2, 0.0, 0.0, lamb, 0.0, eps_2, 0.0, 0.0, None, _ptr(self.flags),
-            stream or _stream())
+            None, None, *self.scalars, None, _ptr(self.flags), stream or _stream())
         N.check(st, self.entry)
         if self.mode == "triplet":
             return I, J, V, T
@@ -92,23 +98,37 @@ class DPFAssembler:
         self.flags.zero_()
 
 
-def _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_(fem_solver, function_space, formulation, mesh, material,
-                                                         Eulerx, Eulerp):
-    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
-    as AOT_Assembler.py builds it for _IsotropicElectroMechanics_108_ (mu1, mu2, lamb, eps_2)."""
+def _low_level_dpf(name, fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
     if formulation.ndim != 3 or formulation.nvar != NVAR:
         raise NotImplementedError("the GB300 DPF assembly covers three-dimensional electromechanics (nvar 4)")
-    params = (material.mu1, material.mu2, material.lamb, material.eps_2)
+    params = tuple(float(getattr(material, k)) for k in MATERIALS[name][1])
     recompute = bool(fem_solver.recompute_sparsity_pattern)
     # CSR output without uploading the two E*ndof^2 maps: each entry's position is found by row
     # search, which lands it where the maps would
     mode = "triplet" if recompute else "squeeze"
     sparsity = None if recompute else (fem_solver.indices, fem_solver.indptr, None, None)
-    asm = DPFAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, params, mode=mode,
-                       requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity)
+    asm = DPFAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, params,
+                       material=name, mode=mode, requires_geometry_update=fem_solver.requires_geometry_update,
+                       sparsity=sparsity)
     x = _to_dev(Eulerx, torch.float64, asm.device)
     p = _to_dev(np.ravel(Eulerp), torch.float64, asm.device)
     out = asm.assemble(x, p)
     host = [_HOST.to_host(t) for t in out]
-    asm.check_flags("_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_")
+    asm.check_flags("_LowLevelAssemblyDPF__" + name + "_")
     return tuple(host)
+
+
+def _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_(fem_solver, function_space, formulation, mesh, material,
+                                                         Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
+    as AOT_Assembler.py builds it for _IsotropicElectroMechanics_108_ (mu1, mu2, lamb, eps_2)."""
+    return _low_level_dpf("IsotropicElectroMechanics_108", fem_solver, function_space, formulation, mesh, material,
+                          Eulerx, Eulerp)
+
+
+def _LowLevelAssemblyDPF__IsotropicElectroMechanics_101_(fem_solver, function_space, formulation, mesh, material,
+                                                         Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
+    as AOT_Assembler.py builds it for _IsotropicElectroMechanics_101_ (mu, lamb, eps_1)."""
+    return _low_level_dpf("IsotropicElectroMechanics_101", fem_solver, function_space, formulation, mesh, material,
+                          Eulerx, Eulerp)

@@ -13,7 +13,8 @@ What it restates (paths inside the Florence repository):
 * the DPF strain-displacement matrix and total traction (Voigt order xx, yy, zz, xy, xz, yz;
   electric rows carry grad N; VariationalPrinciple/_ConstitutiveStiffness_/
   DisplacementPotentialApproachIndices.pyx:1-50, :203-230);
-* IsotropicElectroMechanics_108, an internal-energy model (MaterialLibrary/
+* IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94) and
+  IsotropicElectroMechanics_108, internal-energy models (MaterialLibrary/
   IsotropicElectroMechanics_108.py:36-113, LLDispatch/CythonSource/_IsotropicElectroMechanics_108_.h):
   D = eps_2 E, the internal-energy elasticity, coupling and dielectric tensors turned into the
   electric-enthalpy Hessian by the Legendre transform (LegendreTransform/LegendreTransform.py:22-40);
@@ -73,7 +74,12 @@ def em108(F, E, mu1, mu2, lamb, eps_2):
     W_cp = (d[:, None, :] * D[None, :, None] + D[:, None, None] * d[None, :, :]
             - d[:, :, None] * D[None, None, :]) / eps_2
     W_di = d / eps_2
-    # Legendre transform to the electric enthalpy
+    return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
+
+
+def enthalpy_hessian(W_el, W_cp, W_di):
+    """9x9 electric-enthalpy Hessian [[C, -P], [-P^T, H_di]] from the internal energy's
+    elasticity, coupling and dielectric tensors (the Legendre transform)."""
     H_di = -np.linalg.inv(W_di)
     H_cp = -np.tensordot(W_cp, H_di, axes=([2], [0]))         # H_cp[k,l,j] = -sum_i W_cp[k,l,i] H_di[i,j]
     H_el = W_el - np.einsum("ijk,mlk->ijlm", W_cp, H_cp)     # sum_k W_cp[i,j,k] H_cp[m,l,k]
@@ -83,10 +89,27 @@ def em108(F, E, mu1, mu2, lamb, eps_2):
     H[:6, 6:] = -P_V
     H[6:, :6] = -P_V.T
     H[6:, 6:] = H_di
-    return D, sigma, H
+    return H
 
 
-MATERIALS = {"IsotropicElectroMechanics_108": em108}
+def em101(F, E, mu, lamb, eps_1):
+    """(D, sigma, H[9x9]) of IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94,
+    LLDispatch/CythonSource/_IsotropicElectroMechanics_101_.h): internal energy
+    W(C, D0) = W_neo(C) + |F D0|^2 / (2 eps_1), D = eps_1 / J E."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    D = (eps_1 / J) * E
+    sigma = (mu / J) * (b - d) + lamb * (J - 1.0) * d + (J / eps_1) * np.outer(D, D)
+    dd_ij_kl = d[:, :, None, None] * d[None, None, :, :]
+    sym = d[:, None, :, None] * d[None, :, None, :] + d[:, None, None, :] * d[None, :, :, None]
+    W_el = lamb * (2.0 * J - 1.0) * dd_ij_kl + (mu / J - lamb * (J - 1.0)) * sym
+    W_cp = (J / eps_1) * (d[:, None, :] * D[None, :, None] + D[:, None, None] * d[None, :, :])
+    W_di = (J / eps_1) * d
+    return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
+
+
+MATERIALS = {"IsotropicElectroMechanics_108": em108, "IsotropicElectroMechanics_101": em101}
 
 
 def b_matrix(SG):

@@ -5,11 +5,10 @@
 
 #include "../florence_gb300/csrc/fl_dpf.cuh"
 
-extern "C" double dpf_element(int npe, int nq, const double *Jm, const double *w, const double *X, const double *x,
-                              const double *phi, int update, double mu1, double mu2, double lamb, double eps2,
-                              double *K, double *t) {
+template <class MAT>
+static double element(const MAT &m, int npe, int nq, const double *Jm, const double *w, const double *X,
+                      const double *x, const double *phi, int update, double *K, double *t) {
     using namespace fl::dpf;
-    const Em108 m{mu1, mu2, lamb, eps2};
     const int ndof = NV * npe;
     std::vector<double> SG(3 * npe * nq), H(HV * HV * nq), sig(9 * nq), D(3 * nq), dv(nq);
     double minJ = 1e300;
@@ -31,4 +30,12 @@ extern "C" double dpf_element(int npe, int nq, const double *Jm, const double *w
         t[r] = s;
     }
     return minJ;
+}
+
+// material: 108 (params mu1, mu2, lamb, eps_2) or 101 (params mu, lamb, eps_1)
+extern "C" double dpf_element(int material, int npe, int nq, const double *Jm, const double *w, const double *X,
+                              const double *x, const double *phi, int update, const double *p, double *K, double *t) {
+    if (material == 108) return element(fl::dpf::Em108{p[0], p[1], p[2], p[3]}, npe, nq, Jm, w, X, x, phi, update, K, t);
+    if (material == 101) return element(fl::dpf::Em101{p[0], p[1], p[2]}, npe, nq, Jm, w, X, x, phi, update, K, t);
+    return -1.0;
 }

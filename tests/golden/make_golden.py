@@ -47,6 +47,9 @@ def make_material(F, name, params):
     elif name == "AnisotropicMooneyRivlin_1":
         # params (mu1, mu2, lamb, mu3); fibre directions set per element by make_case
         m = F.AnisotropicMooneyRivlin_1(3, mu1=params[0], mu2=params[1], lamb=params[2], mu3=params[3], rho=1.0)
+    elif name == "IsotropicElectroMechanics_101":
+        # params (mu, lamb, eps_1): neo-Hookean electromechanics in terms of internal energy
+        m = F.IsotropicElectroMechanics_101(3, mu=params[0], lamb=params[1], eps_1=params[2], rho=1.0)
     elif name == "IsotropicElectroMechanics_108":
         # params (mu1, mu2, lamb, eps_2): internal-energy electromechanics, displacement-potential form
         m = F.IsotropicElectroMechanics_108(3, mu1=params[0], mu2=params[1], lamb=params[2], eps_2=params[3], rho=1.0)
@@ -273,6 +276,8 @@ DPF_CASES = [
     dict(name="dpf_hex_p2_em108", mesh="box_hex", n=(2, 1, 1), L=(2.0, 1.0, 1.0), p=2,
          material="IsotropicElectroMechanics_108", params=(0.4, 0.2, 15.0, 1.5), seed=31, amp=0.03, phi_amp=0.2,
          emat=(0, 1)),
+    dict(name="dpf_tet_p2_em101", mesh="cube_tet", n=(1, 1, 1), p=2, material="IsotropicElectroMechanics_101",
+         params=(0.8, 12.0, 1.7), seed=32, amp=0.02, phi_amp=0.15, emat=(0, 3)),
 ]
 
 

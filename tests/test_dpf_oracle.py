@@ -55,7 +55,7 @@ def dpf_host(tmp_path_factory):
     subprocess.check_call(["g++", "-O2", "-shared", "-fPIC", "-o", so, os.path.join(here, "dpf_host_shim.cpp")])
     L = ctypes.CDLL(so)
     P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
-    L.dpf_element.argtypes = [I, I, P, P, P, P, P, I, D, D, D, D, P, P]
+    L.dpf_element.argtypes = [I, I, I, P, P, P, P, P, I, P, P, P]
     L.dpf_element.restype = D
     return L
 
@@ -75,9 +75,10 @@ def test_device_dpf_arithmetic_on_host(dpf_host, case):
         phi = np.ascontiguousarray(d["Eulerp"][nodes], np.float64)
         K = np.zeros((4 * npe, 4 * npe))
         t = np.zeros(4 * npe)
-        minJ = dpf_host.dpf_element(npe, nq, Jm.ctypes.data, w.ctypes.data, X.ctypes.data, x.ctypes.data,
-                                    phi.ctypes.data, int(d["update"]), *map(float, d["params"]), K.ctypes.data,
-                                    t.ctypes.data)
+        p = np.ascontiguousarray(d["params"], np.float64)
+        mat = int(str(d["material"]).rsplit("_", 1)[1])
+        minJ = dpf_host.dpf_element(mat, npe, nq, Jm.ctypes.data, w.ctypes.data, X.ctypes.data, x.ctypes.data,
+                                    phi.ctypes.data, int(d["update"]), p.ctypes.data, K.ctypes.data, t.ctypes.data)
         assert minJ > 0
         assert rel_fro(K, d["emat_K"][k]) < TOL
         assert rel_fro(t, d["emat_t"][k]) < TOL

@@ -27,8 +27,8 @@ def test_dpf_assembly(case, mode):
     import florence_gb300 as fl
     d = load_golden(case)
     n = 4 * d["points"].shape[0]
-    asm = fl.DPFAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], tuple(d["params"]), mode=mode,
-                          requires_geometry_update=int(d["update"]))
+    asm = fl.DPFAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], tuple(d["params"]),
+                          material=str(d["material"]), mode=mode, requires_geometry_update=int(d["update"]))
     out = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda(), torch.from_numpy(d["Eulerp"]).cuda())
     asm.check_flags()
     if mode == "triplet":
@@ -46,9 +46,10 @@ def test_dpf_assembly(case, mode):
 
 
 @pytest.mark.parametrize("recompute", [True, False])
-def test_dpf_drop_in(recompute):
+@pytest.mark.parametrize("case", ["dpf_tet_p2_em108", "dpf_tet_p2_em101"])
+def test_dpf_drop_in(case, recompute):
     import florence_gb300 as fl
-    d = load_golden("dpf_tet_p2_em108")
+    d = load_golden(case)
     n = 4 * d["points"].shape[0]
     solver = types.SimpleNamespace(recompute_sparsity_pattern=recompute, squeeze_sparsity_pattern=False,
                                    requires_geometry_update=int(d["update"]), indices=d["sp_indices"],
@@ -58,10 +59,11 @@ def test_dpf_drop_in(recompute):
     form = types.SimpleNamespace(ndim=3, nvar=4, fields="electro_mechanics")
     mesh = types.SimpleNamespace(points=d["points"], elements=d["elements"].astype(np.uint64),
                                  nelem=d["elements"].shape[0])
-    mu1, mu2, lamb, eps_2 = d["params"]
-    material = types.SimpleNamespace(mu1=mu1, mu2=mu2, lamb=lamb, eps_2=eps_2, H_VoigtSize=9)
-    out = fl._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_(solver, fs, form, mesh, material, d["Eulerx"],
-                                                                 d["Eulerp"])
+    name = str(d["material"])
+    names = ("mu1", "mu2", "lamb", "eps_2") if name.endswith("108") else ("mu", "lamb", "eps_1")
+    material = types.SimpleNamespace(H_VoigtSize=9, **dict(zip(names, map(float, d["params"]))))
+    fn = getattr(fl, "_LowLevelAssemblyDPF__" + name + "_")
+    out = fn(solver, fs, form, mesh, material, d["Eulerx"], d["Eulerp"])
     if recompute:
         I, J, V, T = out
         K = sp.csr_matrix((V, (I, J)), shape=(n, n))
