@@ -15,11 +15,13 @@ from .assembly import (AssembleBodyForces, AssembleExternalTractionForces, Compu
                        __TotalConstantMassIntegrand__, arithmetic, device_sparsity, fp32_peak_gflops, fp64_peak_gflops,
                        get_arithmetic, install, material_params, release_host_buffers, set_arithmetic,
                        set_tensor_core_tiling)
-from .electromechanics import (DPFAssembler, _LowLevelAssemblyDPF__IsotropicElectroMechanics_101_,
+from .electromechanics import (DPFAssembler, _LowLevelAssemblyDPF__IsotropicElectroMechanics_0_,
+                               _LowLevelAssemblyDPF__IsotropicElectroMechanics_101_,
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_)
 
 __all__ = ["AssembleBodyForces", "AssembleExternalTractionForces", "ComputeSparsityPattern", "DeviceAssembler", "DPFAssembler",
            "_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_", "_LowLevelAssemblyDPF__IsotropicElectroMechanics_101_",
+           "_LowLevelAssemblyDPF__IsotropicElectroMechanics_0_",
            "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",

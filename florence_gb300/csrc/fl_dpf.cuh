@@ -8,7 +8,7 @@
 //                            VariationalPrinciple/DisplacementPotentialFormulation.py:108-200
 //   B rows and traction      VariationalPrinciple/_ConstitutiveStiffness_/DisplacementPotentialApproachIndices.pyx:1-50, :203-230
 //                            (Voigt order xx, yy, zz, xy, xz, yz; the potential's row carries grad N)
-//   materials 101, 108       MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_101_.h,
+//   materials 0, 101, 108    MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h, _101_.h,
 //                            _IsotropicElectroMechanics_108_.h:32-112
 //   Legendre transform       MaterialLibrary/LLDispatch/CythonSource/_LegendreTransform_.h (InternalEnergyToEnthalpy)
 //   symmetric Voigt forms    Tensor/Numeric.pyx:166-270
@@ -157,6 +157,58 @@ FL_HD void material_point(const Em101 &m, const double *F, const double *E, doub
             sigma[i * 3 + j] = m.mu / J * (b[i * 3 + j] - kd(i, j)) + m.lamb * (J - 1.0) * kd(i, j) + c * D[i] * D[j];
     const Em101Point pt{D, J, c, m};
     enthalpy_hessian(pt, m.eps1 / J, H);
+}
+
+// IsotropicElectroMechanics_0 (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100,
+// LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h): electric enthalpy
+//   W(C, E0) = mu/2 (C:I - 3) - mu ln J + lamb/2 (ln J)^2 - eps_1/2 J C^-1:(E0 x E0),
+// its Hessian given in enthalpy form directly (no Legendre transform), D = eps_1 E
+struct Em0 {
+    double mu, lamb, eps1;
+};
+
+struct Em0Point {
+    const double *E;
+    double J, lnJ, EE;  // EE = E.E
+    Em0 m;
+    FL_HD double ee(int i, int j) const { return E[i] * E[j]; }
+    FL_HD double c(int i, int j, int k, int l) const {
+        const double sym = kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k);
+        const double dd = kd(i, j) * kd(k, l);
+        return m.lamb / J * dd - (m.lamb * lnJ - m.mu) / J * sym +
+               m.eps1 * (kd(i, j) * ee(k, l) + ee(i, j) * kd(k, l) - ee(i, k) * kd(j, l) - ee(i, l) * kd(j, k) -
+                         kd(i, k) * ee(j, l) - kd(i, l) * ee(j, k)) +
+               m.eps1 * EE * 0.5 * (sym - dd);
+    }
+    // eps_1 (delta_ik E_j + delta_jk E_i - delta_ij E_k)
+    FL_HD double p(int i, int j, int k) const { return m.eps1 * (kd(i, k) * E[j] + kd(j, k) * E[i] - kd(i, j) * E[k]); }
+};
+
+FL_HD void material_point(const Em0 &m, const double *F, const double *E, double *D, double *sigma, double *H) {
+    const double J = det3(F);
+    const double lnJ = std::log(J);
+    double b[9];
+    left_cauchy_green(F, b);
+    for (int k = 0; k < 3; ++k) D[k] = m.eps1 * E[k];
+    const double EE = E[0] * E[0] + E[1] * E[1] + E[2] * E[2];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            sigma[i * 3 + j] = m.mu / J * (b[i * 3 + j] - kd(i, j)) + m.lamb / J * lnJ * kd(i, j) +
+                               m.eps1 * (E[i] * E[j] - 0.5 * EE * kd(i, j));
+    const Em0Point pt{E, J, lnJ, EE, m};
+    for (int I = 0; I < 6; ++I) {
+        const int i = vp0(I), j = vp1(I);
+        for (int K = I; K < 6; ++K) {
+            const int k = vp0(K), l = vp1(K);
+            H[I * HV + K] = H[K * HV + I] = 0.5 * (pt.c(i, j, k, l) + pt.c(i, j, l, k));
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double P = 0.5 * (pt.p(i, j, k) + pt.p(j, i, k));
+            H[I * HV + 6 + k] = H[(6 + k) * HV + I] = -P;
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) H[(6 + k) * HV + 6 + l] = -m.eps1 * kd(k, l);
 }
 
 // Gauss point g of one element: spatial gradients SG[d * npe + a] (material gradients when the

@@ -13,6 +13,8 @@ What it restates (paths inside the Florence repository):
 * the DPF strain-displacement matrix and total traction (Voigt order xx, yy, zz, xy, xz, yz;
   electric rows carry grad N; VariationalPrinciple/_ConstitutiveStiffness_/
   DisplacementPotentialApproachIndices.pyx:1-50, :203-230);
+* IsotropicElectroMechanics_0, an electric-enthalpy model whose Hessian is given directly
+  (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100);
 * IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94) and
   IsotropicElectroMechanics_108, internal-energy models (MaterialLibrary/
   IsotropicElectroMechanics_108.py:36-113, LLDispatch/CythonSource/_IsotropicElectroMechanics_108_.h):
@@ -109,7 +111,39 @@ def em101(F, E, mu, lamb, eps_1):
     return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
 
 
-MATERIALS = {"IsotropicElectroMechanics_108": em108, "IsotropicElectroMechanics_101": em101}
+def em0(F, E, mu, lamb, eps_1):
+    """(D, sigma, H[9x9]) of IsotropicElectroMechanics_0 (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100):
+    electric enthalpy W(C, E0) = W_n(C) - eps_1/2 J C^-1:(E0 x E0); the Hessian is given in
+    enthalpy form directly, D = eps_1 E."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    EE = np.outer(E, E)
+    D = eps_1 * E
+    sigma = (mu / J) * (b - d) + (lamb / J) * np.log(J) * d + eps_1 * (EE - 0.5 * (E @ E) * d)
+    dd_ij_kl = d[:, :, None, None] * d[None, None, :, :]
+    sym = d[:, None, :, None] * d[None, :, None, :] + d[:, None, None, :] * d[None, :, :, None]
+    d_ij_EE_kl = d[:, :, None, None] * EE[None, None]
+    EE_ij_d_kl = EE[:, :, None, None] * d[None, None]
+    EE_ik_d_jl = EE[:, None, :, None] * d[None, :, None, :]
+    EE_il_d_jk = EE[:, None, None, :] * d[None, :, :, None]
+    d_ik_EE_jl = d[:, None, :, None] * EE[None, :, None, :]
+    d_il_EE_jk = d[:, None, None, :] * EE[None, :, :, None]
+    C = (lamb / J) * dd_ij_kl - (lamb * np.log(J) - mu) / J * sym \
+        + eps_1 * (d_ij_EE_kl + EE_ij_d_kl - EE_ik_d_jl - EE_il_d_jk - d_ik_EE_jl - d_il_EE_jk) \
+        + eps_1 * (E @ E) * 0.5 * (sym - dd_ij_kl)
+    # coupling P[i,j,k] = eps_1 (delta_ik E_j + delta_jk E_i - delta_ij E_k)
+    P = eps_1 * (d[:, None, :] * E[None, :, None] + E[:, None, None] * d[None, :, :] - d[:, :, None] * E[None, None, :])
+    H = np.zeros((9, 9))
+    H[:6, :6] = voigt4(C)
+    H[:6, 6:] = -voigt3(P)
+    H[6:, :6] = -voigt3(P).T
+    H[6:, 6:] = -eps_1 * d
+    return D, sigma, H
+
+
+MATERIALS = {"IsotropicElectroMechanics_108": em108, "IsotropicElectroMechanics_101": em101,
+             "IsotropicElectroMechanics_0": em0}
 
 
 def b_matrix(SG):

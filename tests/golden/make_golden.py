@@ -47,6 +47,9 @@ def make_material(F, name, params):
     elif name == "AnisotropicMooneyRivlin_1":
         # params (mu1, mu2, lamb, mu3); fibre directions set per element by make_case
         m = F.AnisotropicMooneyRivlin_1(3, mu1=params[0], mu2=params[1], lamb=params[2], mu3=params[3], rho=1.0)
+    elif name == "IsotropicElectroMechanics_0":
+        # params (mu, lamb, eps_1): electric enthalpy W_n(C) - eps_1/2 J C^-1:(E0 x E0)
+        m = F.IsotropicElectroMechanics_0(3, mu=params[0], lamb=params[1], eps_1=params[2], rho=1.0)
     elif name == "IsotropicElectroMechanics_101":
         # params (mu, lamb, eps_1): neo-Hookean electromechanics in terms of internal energy
         m = F.IsotropicElectroMechanics_101(3, mu=params[0], lamb=params[1], eps_1=params[2], rho=1.0)
@@ -275,6 +278,9 @@ DPF_CASES = [
          params=(0.5, 0.3, 10.0, 2.0), seed=30, amp=0.02, phi_amp=0.1, emat=(0, 4)),
     dict(name="dpf_hex_p2_em108", mesh="box_hex", n=(2, 1, 1), L=(2.0, 1.0, 1.0), p=2,
          material="IsotropicElectroMechanics_108", params=(0.4, 0.2, 15.0, 1.5), seed=31, amp=0.03, phi_amp=0.2,
+         emat=(0, 1)),
+    dict(name="dpf_hex_p2_em0", mesh="box_hex", n=(2, 1, 1), L=(2.0, 1.0, 1.0), p=2,
+         material="IsotropicElectroMechanics_0", params=(1.1, 9.0, 0.6), seed=33, amp=0.03, phi_amp=0.3,
          emat=(0, 1)),
     dict(name="dpf_tet_p2_em101", mesh="cube_tet", n=(1, 1, 1), p=2, material="IsotropicElectroMechanics_101",
          params=(0.8, 12.0, 1.7), seed=32, amp=0.02, phi_amp=0.15, emat=(0, 3)),

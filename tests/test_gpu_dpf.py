@@ -46,7 +46,7 @@ def test_dpf_assembly(case, mode):
 
 
 @pytest.mark.parametrize("recompute", [True, False])
-@pytest.mark.parametrize("case", ["dpf_tet_p2_em108", "dpf_tet_p2_em101"])
+@pytest.mark.parametrize("case", ["dpf_tet_p2_em108", "dpf_tet_p2_em101", "dpf_hex_p2_em0"])
 def test_dpf_drop_in(case, recompute):
     import florence_gb300 as fl
     d = load_golden(case)
