@@ -566,6 +566,7 @@ def install(florence):
     ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_
     ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_101_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_101_
     ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_0_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_0_
+    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_106_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_106_
     ll.has_low_level_dispatcher = True
     asm_mod = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly.Assembly")
     asm_mod.AssembleExternalTractionForces = AssembleExternalTractionForces

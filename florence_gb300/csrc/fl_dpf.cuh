@@ -8,7 +8,8 @@
 //                            VariationalPrinciple/DisplacementPotentialFormulation.py:108-200
 //   B rows and traction      VariationalPrinciple/_ConstitutiveStiffness_/DisplacementPotentialApproachIndices.pyx:1-50, :203-230
 //                            (Voigt order xx, yy, zz, xy, xz, yz; the potential's row carries grad N)
-//   materials 0, 101, 108    MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h, _101_.h,
+//   materials 0, 101, 106, 108
+//                            MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h, _101_.h, _106_.h,
 //                            _IsotropicElectroMechanics_108_.h:32-112
 //   Legendre transform       MaterialLibrary/LLDispatch/CythonSource/_LegendreTransform_.h (InternalEnergyToEnthalpy)
 //   symmetric Voigt forms    Tensor/Numeric.pyx:166-270
@@ -106,13 +107,8 @@ struct Em108Point {
     FL_HD double wcp(int i, int j, int k) const { return ie * (kd(i, k) * D[j] + D[i] * kd(j, k) - kd(i, j) * D[k]); }
 };
 
-// D = eps_2 E, Cauchy stress sigma[9] and the enthalpy Hessian; dielectric tensor I / eps_2
-FL_HD void material_point(const Em108 &m, const double *F, const double *E, double *D, double *sigma, double *H) {
-    const double J = det3(F);
-    double b[9];
-    left_cauchy_green(F, b);
-    for (int k = 0; k < 3; ++k) D[k] = m.eps2 * E[k];
-    const double DD = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+// Cauchy stress of IsotropicElectroMechanics_108 (and 106) at electric displacement D
+FL_HD void em108_stress(const Em108 &m, const double *b, double J, const double *D, double DD, double *sigma) {
     const double trb = b[0] + b[4] + b[8];
     const double ie = 1.0 / m.eps2;
     for (int i = 0; i < 3; ++i)
@@ -122,8 +118,73 @@ FL_HD void material_point(const Em108 &m, const double *F, const double *E, doub
                                2.0 * (m.mu1 + 2.0 * m.mu2) / J * kd(i, j) + m.lamb * (J - 1.0) * kd(i, j) +
                                ie * (D[i] * D[j] - 0.5 * DD * kd(i, j));
         }
-    const Em108Point pt{b, D, J, DD, ie, m};
+}
+
+// D = eps_2 E, Cauchy stress sigma[9] and the enthalpy Hessian; dielectric tensor I / eps_2
+FL_HD void material_point(const Em108 &m, const double *F, const double *E, double *D, double *sigma, double *H) {
+    const double J = det3(F);
+    double b[9];
+    left_cauchy_green(F, b);
+    for (int k = 0; k < 3; ++k) D[k] = m.eps2 * E[k];
+    const double DD = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    em108_stress(m, b, J, D, DD, sigma);
+    const Em108Point pt{b, D, J, DD, 1.0 / m.eps2, m};
     enthalpy_hessian(pt, m.eps2, H);
+}
+
+// Electric-enthalpy Hessian for a general (symmetric) dielectric tensor W_di, given its inverse
+// Winv: enthalpy coupling Q(i,j,k) = sum_n W_cp(i,j,n) Winv(n,k), enthalpy elasticity
+// W_el(i,j,k,l) - sum_n Q(i,j,n) W_cp(k,l,n), dielectric block -Winv; symmetric Voigt forms
+template <class Pt>
+FL_HD void enthalpy_hessian_general(const Pt &pt, const double *Winv, double *H) {
+    double Q[27];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) {
+                double q = 0.0;
+                for (int n = 0; n < 3; ++n) q += pt.wcp(i, j, n) * Winv[n * 3 + k];
+                Q[(i * 3 + j) * 3 + k] = q;
+            }
+    for (int I = 0; I < 6; ++I) {
+        const int i = vp0(I), j = vp1(I);
+        for (int K = I; K < 6; ++K) {
+            const int k = vp0(K), l = vp1(K);
+            double h1 = pt.wel(i, j, k, l), h2 = pt.wel(i, j, l, k);
+            for (int n = 0; n < 3; ++n) {
+                h1 -= Q[(i * 3 + j) * 3 + n] * pt.wcp(k, l, n);
+                h2 -= Q[(i * 3 + j) * 3 + n] * pt.wcp(l, k, n);
+            }
+            H[I * HV + K] = H[K * HV + I] = 0.5 * (h1 + h2);
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double P = 0.5 * (Q[(i * 3 + j) * 3 + k] + Q[(j * 3 + i) * 3 + k]);
+            H[I * HV + 6 + k] = H[(6 + k) * HV + I] = -P;
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l) H[(6 + k) * HV + 6 + l] = -Winv[k * 3 + l];
+}
+
+// IsotropicElectroMechanics_106 (MaterialLibrary/IsotropicElectroMechanics_106.py:41-125,
+// LLDispatch/CythonSource/_IsotropicElectroMechanics_106_.h): 108's stress, elasticity and
+// coupling with the dielectric tensor J/eps_1 b^-1 + I/eps_2; D = (that tensor)^-1 E
+struct Em106 {
+    double mu1, mu2, lamb, eps1, eps2;
+};
+
+FL_HD void material_point(const Em106 &m, const double *F, const double *E, double *D, double *sigma, double *H) {
+    const double J = det3(F);
+    double b[9], ib[9], W[9], Winv[9];
+    left_cauchy_green(F, b);
+    inv3(b, ib);
+    for (int k = 0; k < 9; ++k) W[k] = J / m.eps1 * ib[k] + (k % 4 == 0 ? 1.0 / m.eps2 : 0.0);
+    inv3(W, Winv);
+    for (int k = 0; k < 3; ++k) D[k] = Winv[k * 3] * E[0] + Winv[k * 3 + 1] * E[1] + Winv[k * 3 + 2] * E[2];
+    const double DD = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    const Em108 m8{m.mu1, m.mu2, m.lamb, m.eps2};
+    em108_stress(m8, b, J, D, DD, sigma);
+    const Em108Point pt{b, D, J, DD, 1.0 / m.eps2, m8};
+    enthalpy_hessian_general(pt, Winv, H);
 }
 
 // IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94,

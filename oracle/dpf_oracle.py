@@ -15,7 +15,8 @@ What it restates (paths inside the Florence repository):
   DisplacementPotentialApproachIndices.pyx:1-50, :203-230);
 * IsotropicElectroMechanics_0, an electric-enthalpy model whose Hessian is given directly
   (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100);
-* IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94) and
+* IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94),
+  IsotropicElectroMechanics_106 (IsotropicElectroMechanics_106.py:41-125) and
   IsotropicElectroMechanics_108, internal-energy models (MaterialLibrary/
   IsotropicElectroMechanics_108.py:36-113, LLDispatch/CythonSource/_IsotropicElectroMechanics_108_.h):
   D = eps_2 E, the internal-energy elasticity, coupling and dielectric tensors turned into the
@@ -49,17 +50,10 @@ def voigt3(e):
     return V
 
 
-def em108(F, E, mu1, mu2, lamb, eps_2):
-    """(D, sigma, H[9x9]) of IsotropicElectroMechanics_108 at deformation gradient F and spatial
-    electric field E."""
+def em108_tensors(b, J, D, mu1, mu2, lamb, eps_2):
+    """Internal-energy elasticity W_el[i,j,k,l] and coupling W_cp[i,j,k] of IsotropicElectroMechanics_108."""
     d = np.eye(3)
-    J = np.linalg.det(F)
-    b = F @ F.T
-    D = eps_2 * E
     DD = D @ D
-    sigma = (2.0 * mu1 / J) * b + (2.0 * mu2 / J) * (np.trace(b) * b - b @ b) \
-        - (2.0 * (mu1 + 2.0 * mu2) / J) * d + lamb * (J - 1.0) * d \
-        + (np.outer(D, D) - 0.5 * DD * d) / eps_2
     # 4th-order identities and b products, index order (i, j, k, l)
     dd_ij_kl = d[:, :, None, None] * d[None, None, :, :]
     dd_ik_jl = d[:, None, :, None] * d[None, :, None, :]
@@ -75,8 +69,27 @@ def em108(F, E, mu1, mu2, lamb, eps_2):
     # coupling W_cp[i,j,k] = (delta_ik D_j + D_i delta_jk - delta_ij D_k) / eps_2
     W_cp = (d[:, None, :] * D[None, :, None] + D[:, None, None] * d[None, :, :]
             - d[:, :, None] * D[None, None, :]) / eps_2
-    W_di = d / eps_2
-    return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
+    return W_el, W_cp
+
+
+def em108_from_D(F, D, mu1, mu2, lamb, eps_2):
+    """(J, sigma, b) of IsotropicElectroMechanics_108's stress at a given electric displacement."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    sigma = (2.0 * mu1 / J) * b + (2.0 * mu2 / J) * (np.trace(b) * b - b @ b) \
+        - (2.0 * (mu1 + 2.0 * mu2) / J) * d + lamb * (J - 1.0) * d \
+        + (np.outer(D, D) - 0.5 * (D @ D) * d) / eps_2
+    return J, sigma, b
+
+
+def em108(F, E, mu1, mu2, lamb, eps_2):
+    """(D, sigma, H[9x9]) of IsotropicElectroMechanics_108 at deformation gradient F and spatial
+    electric field E: D = eps_2 E, dielectric tensor I / eps_2."""
+    D = eps_2 * E
+    J, sigma, b = em108_from_D(F, D, mu1, mu2, lamb, eps_2)
+    W_el, W_cp = em108_tensors(b, J, D, mu1, mu2, lamb, eps_2)
+    return D, sigma, enthalpy_hessian(W_el, W_cp, np.eye(3) / eps_2)
 
 
 def enthalpy_hessian(W_el, W_cp, W_di):
@@ -92,6 +105,20 @@ def enthalpy_hessian(W_el, W_cp, W_di):
     H[6:, :6] = -P_V.T
     H[6:, 6:] = H_di
     return H
+
+
+def em106(F, E, mu1, mu2, lamb, eps_1, eps_2):
+    """(D, sigma, H[9x9]) of IsotropicElectroMechanics_106 (MaterialLibrary/IsotropicElectroMechanics_106.py:41-125,
+    LLDispatch/CythonSource/_IsotropicElectroMechanics_106_.h): 108's stress, elasticity and
+    coupling with the dielectric tensor J/eps_1 b^-1 + I/eps_2, D = (that tensor)^-1 E."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    W_di = (J / eps_1) * np.linalg.inv(b) + d / eps_2
+    D = np.linalg.solve(W_di, E)
+    _, sigma, _ = em108_from_D(F, D, mu1, mu2, lamb, eps_2)
+    W_el, W_cp = em108_tensors(b, J, D, mu1, mu2, lamb, eps_2)
+    return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
 
 
 def em101(F, E, mu, lamb, eps_1):
@@ -143,7 +170,7 @@ def em0(F, E, mu, lamb, eps_1):
 
 
 MATERIALS = {"IsotropicElectroMechanics_108": em108, "IsotropicElectroMechanics_101": em101,
-             "IsotropicElectroMechanics_0": em0}
+             "IsotropicElectroMechanics_0": em0, "IsotropicElectroMechanics_106": em106}
 
 
 def b_matrix(SG):
