@@ -17,12 +17,14 @@ from .assembly import (AssembleBodyForces, AssembleExternalTractionForces, Compu
                        set_tensor_core_tiling)
 from .electromechanics import (DPFAssembler, _LowLevelAssemblyDPF__IsotropicElectroMechanics_0_,
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_101_,
+                               _LowLevelAssemblyDPF__IsotropicElectroMechanics_105_,
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_106_,
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_)
 
 __all__ = ["AssembleBodyForces", "AssembleExternalTractionForces", "ComputeSparsityPattern", "DeviceAssembler", "DPFAssembler",
            "_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_", "_LowLevelAssemblyDPF__IsotropicElectroMechanics_101_",
            "_LowLevelAssemblyDPF__IsotropicElectroMechanics_0_", "_LowLevelAssemblyDPF__IsotropicElectroMechanics_106_",
+           "_LowLevelAssemblyDPF__IsotropicElectroMechanics_105_",
            "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",

@@ -563,10 +563,9 @@ def install(florence):
     ll._LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_ = _LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_
     ll._LowLevelAssemblyExplicit_DF_DPF_ = _LowLevelAssemblyExplicit_DF_DPF_
     from . import electromechanics as em
-    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_108_
-    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_101_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_101_
-    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_0_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_0_
-    ll._LowLevelAssemblyDPF__IsotropicElectroMechanics_106_ = em._LowLevelAssemblyDPF__IsotropicElectroMechanics_106_
+    for em_name in em.MATERIALS:  # the dispatcher's "_LowLevelAssemblyDPF__" + material name + "_"
+        name = "_LowLevelAssemblyDPF__" + em_name + "_"
+        setattr(ll, name, getattr(em, name))
     ll.has_low_level_dispatcher = True
     asm_mod = importlib.import_module(florence.__name__ + ".FiniteElements.Assembly.Assembly")
     asm_mod.AssembleExternalTractionForces = AssembleExternalTractionForces

@@ -8,8 +8,8 @@
 //                            VariationalPrinciple/DisplacementPotentialFormulation.py:108-200
 //   B rows and traction      VariationalPrinciple/_ConstitutiveStiffness_/DisplacementPotentialApproachIndices.pyx:1-50, :203-230
 //                            (Voigt order xx, yy, zz, xy, xz, yz; the potential's row carries grad N)
-//   materials 0, 101, 106, 108
-//                            MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h, _101_.h, _106_.h,
+//   materials 0, 101, 105, 106, 108
+//                            MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h, _101_.h, _105_.h, _106_.h,
 //                            _IsotropicElectroMechanics_108_.h:32-112
 //   Legendre transform       MaterialLibrary/LLDispatch/CythonSource/_LegendreTransform_.h (InternalEnergyToEnthalpy)
 //   symmetric Voigt forms    Tensor/Numeric.pyx:166-270
@@ -218,6 +218,47 @@ FL_HD void material_point(const Em101 &m, const double *F, const double *E, doub
             sigma[i * 3 + j] = m.mu / J * (b[i * 3 + j] - kd(i, j)) + m.lamb * (J - 1.0) * kd(i, j) + c * D[i] * D[j];
     const Em101Point pt{D, J, c, m};
     enthalpy_hessian(pt, m.eps1 / J, H);
+}
+
+// IsotropicElectroMechanics_105 (MaterialLibrary/IsotropicElectroMechanics_105.py:41-104,
+// LLDispatch/CythonSource/_IsotropicElectroMechanics_105_.h): internal energy
+//   W_mn(C) + |D0|^2 / (2 eps_1) + |F D0|^2 / (2 eps_2): 108's mechanical elasticity, coupling
+//   J/eps_2 (delta_ik D_j + D_i delta_jk), dielectric tensor J/eps_1 b^-1 + J/eps_2 I
+struct Em105 {
+    double mu1, mu2, lamb, eps1, eps2;
+};
+
+struct Em105Point {
+    const double *b, *D;
+    double J, c;  // c = J / eps_2
+    Em105 m;
+    FL_HD double wel(int i, int j, int k, int l) const {
+        const double sym = kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k);
+        return 2.0 * m.mu2 / J * (2.0 * b[i * 3 + j] * b[k * 3 + l] - b[i * 3 + k] * b[j * 3 + l] - b[i * 3 + l] * b[j * 3 + k]) +
+               (2.0 * (m.mu1 + 2.0 * m.mu2) / J - m.lamb * (J - 1.0)) * sym + m.lamb * (2.0 * J - 1.0) * kd(i, j) * kd(k, l);
+    }
+    FL_HD double wcp(int i, int j, int k) const { return c * (kd(i, k) * D[j] + D[i] * kd(j, k)); }
+};
+
+FL_HD void material_point(const Em105 &m, const double *F, const double *E, double *D, double *sigma, double *H) {
+    const double J = det3(F);
+    double b[9], ib[9], W[9], Winv[9];
+    left_cauchy_green(F, b);
+    inv3(b, ib);
+    for (int k = 0; k < 9; ++k) W[k] = J / m.eps1 * ib[k] + (k % 4 == 0 ? J / m.eps2 : 0.0);
+    inv3(W, Winv);
+    for (int k = 0; k < 3; ++k) D[k] = Winv[k * 3] * E[0] + Winv[k * 3 + 1] * E[1] + Winv[k * 3 + 2] * E[2];
+    const double trb = b[0] + b[4] + b[8];
+    const double c = J / m.eps2;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const double bb = b[i * 3] * b[j] + b[i * 3 + 1] * b[3 + j] + b[i * 3 + 2] * b[6 + j];
+            sigma[i * 3 + j] = 2.0 * m.mu1 / J * b[i * 3 + j] + 2.0 * m.mu2 / J * (trb * b[i * 3 + j] - bb) -
+                               2.0 * (m.mu1 + 2.0 * m.mu2) / J * kd(i, j) + m.lamb * (J - 1.0) * kd(i, j) +
+                               c * D[i] * D[j];
+        }
+    const Em105Point pt{b, D, J, c, m};
+    enthalpy_hessian_general(pt, Winv, H);
 }
 
 // IsotropicElectroMechanics_0 (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100,

@@ -1,11 +1,11 @@
 """Displacement-potential (electromechanics) assembly on the GPU: three displacements and the
-electric potential per node (nvar 4, global dof 4 n + v), IsotropicElectroMechanics_108, _106, _101
-and _0.
+electric potential per node (nvar 4, global dof 4 n + v), IsotropicElectroMechanics_108, _106, _105,
+_101 and _0.
 
 * ``DPFAssembler`` keeps the mesh, function-space tables and the nvar=4 CSR pattern on the device
   and assembles the tangent and residual from device coordinates and potentials
   (``fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_``).
-* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_`` / ``_106_`` / ``_101_`` / ``_0_`` are the drop-ins for the reference's
+* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_<108|106|105|101|0>_`` are the drop-ins for the reference's
   Cython wrapper (Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.pyx:53-160):
   the reference's dispatcher (_LowLevelAssembly_.py:45-83) finds it by name when
   ``formulation.fields == "electro_mechanics"``; ``florence_gb300.install`` registers them.
@@ -27,13 +27,15 @@ MATERIALS = {"IsotropicElectroMechanics_108": ("fl_GlobalAssemblyDPF__IsotropicE
              "IsotropicElectroMechanics_0": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_",
                                              ("mu", "lamb", "eps_1")),
              "IsotropicElectroMechanics_106": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_",
+                                               ("mu1", "mu2", "lamb", "eps_1", "eps_2")),
+             "IsotropicElectroMechanics_105": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_",
                                                ("mu1", "mu2", "lamb", "eps_1", "eps_2"))}
 _ABI_SCALARS = ("rho", "mu", "mu1", "mu2", "mu3", "mue", "lamb", "eps_1", "eps_2", "eps_3", "eps_e")
 
 
 class DPFAssembler:
     """points [N,3], elements [E,npe], Jm [3,npe,nq], AllGauss [nq]; params (mu1, mu2, lamb, eps_2)
-    for IsotropicElectroMechanics_108, (mu1, mu2, lamb, eps_1, eps_2) for _106, (mu, lamb, eps_1)
+    for IsotropicElectroMechanics_108, (mu1, mu2, lamb, eps_1, eps_2) for _106 and _105, (mu, lamb, eps_1)
     for _101 and _0; mode 'csr' (element-to-nonzero
     maps), 'squeeze' (row search) or 'triplet'."""
 
@@ -153,4 +155,12 @@ def _LowLevelAssemblyDPF__IsotropicElectroMechanics_106_(fem_solver, function_sp
     """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
     as AOT_Assembler.py builds it for _IsotropicElectroMechanics_106_ (mu1, mu2, lamb, eps_1, eps_2)."""
     return _low_level_dpf("IsotropicElectroMechanics_106", fem_solver, function_space, formulation, mesh, material,
+                          Eulerx, Eulerp)
+
+
+def _LowLevelAssemblyDPF__IsotropicElectroMechanics_105_(fem_solver, function_space, formulation, mesh, material,
+                                                         Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
+    as AOT_Assembler.py builds it for _IsotropicElectroMechanics_105_ (mu1, mu2, lamb, eps_1, eps_2)."""
+    return _low_level_dpf("IsotropicElectroMechanics_105", fem_solver, function_space, formulation, mesh, material,
                           Eulerx, Eulerp)

@@ -16,6 +16,7 @@ What it restates (paths inside the Florence repository):
 * IsotropicElectroMechanics_0, an electric-enthalpy model whose Hessian is given directly
   (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100);
 * IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94),
+  IsotropicElectroMechanics_105 (IsotropicElectroMechanics_105.py:41-104),
   IsotropicElectroMechanics_106 (IsotropicElectroMechanics_106.py:41-125) and
   IsotropicElectroMechanics_108, internal-energy models (MaterialLibrary/
   IsotropicElectroMechanics_108.py:36-113, LLDispatch/CythonSource/_IsotropicElectroMechanics_108_.h):
@@ -121,6 +122,23 @@ def em106(F, E, mu1, mu2, lamb, eps_1, eps_2):
     return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
 
 
+def em105(F, E, mu1, mu2, lamb, eps_1, eps_2):
+    """(D, sigma, H[9x9]) of IsotropicElectroMechanics_105 (MaterialLibrary/IsotropicElectroMechanics_105.py:41-104,
+    LLDispatch/CythonSource/_IsotropicElectroMechanics_105_.h): internal energy
+    W_mn(C) + |D0|^2 / (2 eps_1) + |F D0|^2 / (2 eps_2); dielectric tensor J/eps_1 b^-1 + J/eps_2 I,
+    D = (that tensor)^-1 E."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    W_di = (J / eps_1) * np.linalg.inv(b) + (J / eps_2) * d
+    D = np.linalg.solve(W_di, E)
+    sigma = (2.0 * mu1 / J) * b + (2.0 * mu2 / J) * (np.trace(b) * b - b @ b) \
+        - (2.0 * (mu1 + 2.0 * mu2) / J) * d + lamb * (J - 1.0) * d + (J / eps_2) * np.outer(D, D)
+    W_el, _ = em108_tensors(b, J, np.zeros(3), mu1, mu2, lamb, eps_2)   # the mechanical part alone
+    W_cp = (J / eps_2) * (d[:, None, :] * D[None, :, None] + D[:, None, None] * d[None, :, :])
+    return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
+
+
 def em101(F, E, mu, lamb, eps_1):
     """(D, sigma, H[9x9]) of IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94,
     LLDispatch/CythonSource/_IsotropicElectroMechanics_101_.h): internal energy
@@ -170,7 +188,8 @@ def em0(F, E, mu, lamb, eps_1):
 
 
 MATERIALS = {"IsotropicElectroMechanics_108": em108, "IsotropicElectroMechanics_101": em101,
-             "IsotropicElectroMechanics_0": em0, "IsotropicElectroMechanics_106": em106}
+             "IsotropicElectroMechanics_0": em0, "IsotropicElectroMechanics_106": em106,
+             "IsotropicElectroMechanics_105": em105}
 
 
 def b_matrix(SG):

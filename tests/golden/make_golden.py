@@ -53,6 +53,10 @@ def make_material(F, name, params):
     elif name == "IsotropicElectroMechanics_101":
         # params (mu, lamb, eps_1): neo-Hookean electromechanics in terms of internal energy
         m = F.IsotropicElectroMechanics_101(3, mu=params[0], lamb=params[1], eps_1=params[2], rho=1.0)
+    elif name == "IsotropicElectroMechanics_105":
+        # params (mu1, mu2, lamb, eps_1, eps_2): W_mn + |D0|^2 / (2 eps_1) + |F D0|^2 / (2 eps_2)
+        m = F.IsotropicElectroMechanics_105(3, mu1=params[0], mu2=params[1], lamb=params[2], eps_1=params[3],
+                                            eps_2=params[4], rho=1.0)
     elif name == "IsotropicElectroMechanics_106":
         # params (mu1, mu2, lamb, eps_1, eps_2): 108's energy plus |D0|^2 / (2 eps_1)
         m = F.IsotropicElectroMechanics_106(3, mu1=params[0], mu2=params[1], lamb=params[2], eps_1=params[3],
@@ -288,6 +292,9 @@ DPF_CASES = [
          emat=(0, 1)),
     dict(name="dpf_tet_p2_em106", mesh="cube_tet", n=(1, 1, 1), p=2, material="IsotropicElectroMechanics_106",
          params=(0.5, 0.3, 10.0, 1.5, 2.5), seed=34, amp=0.03, phi_amp=0.2, emat=(1, 5)),
+    dict(name="dpf_hex_p2_em105", mesh="box_hex", n=(2, 1, 1), L=(2.0, 1.0, 1.0), p=2,
+         material="IsotropicElectroMechanics_105", params=(0.6, 0.25, 12.0, 2.0, 1.2), seed=35, amp=0.03,
+         phi_amp=0.25, emat=(0, 1)),
     dict(name="dpf_tet_p2_em101", mesh="cube_tet", n=(1, 1, 1), p=2, material="IsotropicElectroMechanics_101",
          params=(0.8, 12.0, 1.7), seed=32, amp=0.02, phi_amp=0.15, emat=(0, 3)),
 ]
