@@ -77,6 +77,7 @@ def lib():
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_.argtypes = _DF_ARGS
+        L.fl_GlobalAssemblyDPF__SteinmannModel_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_Batched.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, P, P,
                                                   P]
         L.fl_SetAssemblyTuning.argtypes = [I64, I64, INT]
@@ -130,7 +131,7 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_", "fl_GlobalAssemblyDF_noalloc",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_",
-           "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_",
+           "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_", "fl_GlobalAssemblyDPF__SteinmannModel_",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_ConsistentMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak", "fl_TensorCoreSelfTest",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",

@@ -1,7 +1,7 @@
 // fl_dpf.cu -- global displacement-potential (electromechanics) assembly: the reference's
 // _GlobalAssemblyDPF_ (FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.h:8-198),
-// monomorphised for IsotropicElectroMechanics_0, _101, _105, _106 and _108 as AOT_Assembler.py:125-220 does it,
-// with its
+// monomorphised for IsotropicElectroMechanics_0, _101, _105, _106, _108 and SteinmannModel as
+// AOT_Assembler.py:125-220 does it, with its
 // tangent scattered like fill_global_data (triplets in element-local order, CSR through the
 // element-to-nonzero maps, or CSR by row search) and its residual accumulated into T[4 N].
 //
@@ -222,4 +222,11 @@ extern "C" int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_(FL_GLOBAL_AS
     (void)rho; (void)mu; (void)mu3; (void)mue; (void)eps_3; (void)eps_e; (void)anisotropic_orientations;
     if (!(eps_1 != 0.0) || !(eps_2 != 0.0)) return FL_ERR_ARG;
     return FL_DPF_FORWARD((fl::dpf::Em105{mu1, mu2, lamb, eps_1, eps_2}));
+}
+
+// mu, lamb, c1 (in the eps_3 slot), c2 (eps_2), eps_1 (AOT_Assembler.py:157-158, 202-203)
+extern "C" int fl_GlobalAssemblyDPF__SteinmannModel_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements; (void)sorter;
+    (void)rho; (void)mu1; (void)mu2; (void)mu3; (void)mue; (void)eps_e; (void)anisotropic_orientations;
+    return FL_DPF_FORWARD((fl::dpf::EmSteinmann{mu, lamb, eps_3, eps_2, eps_1}));
 }

@@ -8,7 +8,7 @@
 //                            VariationalPrinciple/DisplacementPotentialFormulation.py:108-200
 //   B rows and traction      VariationalPrinciple/_ConstitutiveStiffness_/DisplacementPotentialApproachIndices.pyx:1-50, :203-230
 //                            (Voigt order xx, yy, zz, xy, xz, yz; the potential's row carries grad N)
-//   materials 0, 101, 105, 106, 108
+//   materials 0, 101, 105, 106, 108, Steinmann
 //                            MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h, _101_.h, _105_.h, _106_.h,
 //                            _IsotropicElectroMechanics_108_.h:32-112
 //   Legendre transform       MaterialLibrary/LLDispatch/CythonSource/_LegendreTransform_.h (InternalEnergyToEnthalpy)
@@ -311,6 +311,47 @@ FL_HD void material_point(const Em0 &m, const double *F, const double *E, double
     }
     for (int k = 0; k < 3; ++k)
         for (int l = 0; l < 3; ++l) H[(6 + k) * HV + 6 + l] = -m.eps1 * kd(k, l);
+}
+
+// SteinmannModel (MaterialLibrary/SteinmannModel.py:40-120, LLDispatch/CythonSource/_SteinmannModel_.h):
+// electric enthalpy W_n(C) + c1 I:(E0 x E0) + c2 C:(E0 x E0) - eps_1/2 J C^-1:(E0 x E0); material
+// 0's Hessian with 2 c2/J (b_ik (bE)_j + (bE)_i b_jk) added to the coupling, dielectric block
+// -eps_1 I + 2 c1/J b + 2 c2/J b^2, D = eps_1 E - 2 c1/J bE - 2 c2/J b^2 E
+struct EmSteinmann {
+    double mu, lamb, c1, c2, eps1;
+};
+
+FL_HD void material_point(const EmSteinmann &m, const double *F, const double *E, double *D, double *sigma,
+                          double *H) {
+    const double J = det3(F);
+    double b[9], bb[9], be[3], bbe[3];
+    left_cauchy_green(F, b);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) bb[i * 3 + j] = b[i * 3] * b[j] + b[i * 3 + 1] * b[3 + j] + b[i * 3 + 2] * b[6 + j];
+    for (int i = 0; i < 3; ++i) {
+        be[i] = b[i * 3] * E[0] + b[i * 3 + 1] * E[1] + b[i * 3 + 2] * E[2];
+        bbe[i] = bb[i * 3] * E[0] + bb[i * 3 + 1] * E[1] + bb[i * 3 + 2] * E[2];
+    }
+    const Em0 m0{m.mu, m.lamb, m.eps1};
+    material_point(m0, F, E, D, sigma, H);
+    const double g = 2.0 * m.c2 / J;
+    for (int k = 0; k < 3; ++k) D[k] = m.eps1 * E[k] - 2.0 * m.c1 / J * be[k] - g * bbe[k];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) sigma[i * 3 + j] += g * be[i] * be[j];
+    for (int I = 0; I < 6; ++I) {
+        const int i = vp0(I), j = vp1(I);
+        for (int k = 0; k < 3; ++k) {
+            // coupling of material 0 plus g (b_ik be_j + be_i b_jk), symmetrised over i, j
+            const double pij = m.eps1 * (kd(i, k) * E[j] + kd(j, k) * E[i] - kd(i, j) * E[k]) +
+                               g * (b[i * 3 + k] * be[j] + be[i] * b[j * 3 + k]);
+            const double pji = m.eps1 * (kd(j, k) * E[i] + kd(i, k) * E[j] - kd(j, i) * E[k]) +
+                               g * (b[j * 3 + k] * be[i] + be[j] * b[i * 3 + k]);
+            H[I * HV + 6 + k] = H[(6 + k) * HV + I] = -0.5 * (pij + pji);
+        }
+    }
+    for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l)
+            H[(6 + k) * HV + 6 + l] = -m.eps1 * kd(k, l) + 2.0 * m.c1 / J * b[k * 3 + l] + g * bb[k * 3 + l];
 }
 
 // Gauss point g of one element: spatial gradients SG[d * npe + a] (material gradients when the

@@ -1,11 +1,12 @@
 """Displacement-potential (electromechanics) assembly on the GPU: three displacements and the
 electric potential per node (nvar 4, global dof 4 n + v), IsotropicElectroMechanics_108, _106, _105,
-_101 and _0.
+_101, _0 and SteinmannModel.
 
 * ``DPFAssembler`` keeps the mesh, function-space tables and the nvar=4 CSR pattern on the device
   and assembles the tangent and residual from device coordinates and potentials
   (``fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_``).
-* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_<108|106|105|101|0>_`` are the drop-ins for the reference's
+* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_<108|106|105|101|0>_`` and
+  ``_LowLevelAssemblyDPF__SteinmannModel_`` are the drop-ins for the reference's
   Cython wrapper (Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.pyx:53-160):
   the reference's dispatcher (_LowLevelAssembly_.py:45-83) finds it by name when
   ``formulation.fields == "electro_mechanics"``; ``florence_gb300.install`` registers them.
@@ -29,14 +30,18 @@ MATERIALS = {"IsotropicElectroMechanics_108": ("fl_GlobalAssemblyDPF__IsotropicE
              "IsotropicElectroMechanics_106": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_",
                                                ("mu1", "mu2", "lamb", "eps_1", "eps_2")),
              "IsotropicElectroMechanics_105": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_",
-                                               ("mu1", "mu2", "lamb", "eps_1", "eps_2"))}
+                                               ("mu1", "mu2", "lamb", "eps_1", "eps_2")),
+             "SteinmannModel": ("fl_GlobalAssemblyDPF__SteinmannModel_", ("mu", "lamb", "c1", "c2", "eps_1"))}
+# material attributes passed in other scalar slots of the reference's argument list
+# (_LowLevelAssemblyDPF_.pyx as AOT_Assembler.py:202-203 rewrites it for the Steinmann model)
+_ABI_SLOT = {"c1": "eps_3", "c2": "eps_2"}
 _ABI_SCALARS = ("rho", "mu", "mu1", "mu2", "mu3", "mue", "lamb", "eps_1", "eps_2", "eps_3", "eps_e")
 
 
 class DPFAssembler:
     """points [N,3], elements [E,npe], Jm [3,npe,nq], AllGauss [nq]; params (mu1, mu2, lamb, eps_2)
     for IsotropicElectroMechanics_108, (mu1, mu2, lamb, eps_1, eps_2) for _106 and _105, (mu, lamb, eps_1)
-    for _101 and _0; mode 'csr' (element-to-nonzero
+    for _101 and _0, (mu, lamb, c1, c2, eps_1) for SteinmannModel; mode 'csr' (element-to-nonzero
     maps), 'squeeze' (row search) or 'triplet'."""
 
     def __init__(self, points, elements, Jm, AllGauss, params, material="IsotropicElectroMechanics_108",
@@ -57,7 +62,7 @@ class DPFAssembler:
         self.params = tuple(float(p) for p in params)
         if len(self.params) != len(names):
             raise ValueError("%s takes (%s)" % (material, ", ".join(names)))
-        given = dict(zip(names, self.params))
+        given = {_ABI_SLOT.get(k, k): v for k, v in zip(names, self.params)}
         self.scalars = tuple(given.get(k, 1.0 if k == "rho" else 0.0) for k in _ABI_SCALARS)
         self.mode = mode
         self.update = int(requires_geometry_update)
@@ -164,3 +169,9 @@ def _LowLevelAssemblyDPF__IsotropicElectroMechanics_105_(fem_solver, function_sp
     as AOT_Assembler.py builds it for _IsotropicElectroMechanics_105_ (mu1, mu2, lamb, eps_1, eps_2)."""
     return _low_level_dpf("IsotropicElectroMechanics_105", fem_solver, function_space, formulation, mesh, material,
                           Eulerx, Eulerp)
+
+
+def _LowLevelAssemblyDPF__SteinmannModel_(fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
+    as AOT_Assembler.py builds it for _SteinmannModel_ (mu, lamb, c1, c2, eps_1)."""
+    return _low_level_dpf("SteinmannModel", fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp)

@@ -13,8 +13,8 @@ What it restates (paths inside the Florence repository):
 * the DPF strain-displacement matrix and total traction (Voigt order xx, yy, zz, xy, xz, yz;
   electric rows carry grad N; VariationalPrinciple/_ConstitutiveStiffness_/
   DisplacementPotentialApproachIndices.pyx:1-50, :203-230);
-* IsotropicElectroMechanics_0, an electric-enthalpy model whose Hessian is given directly
-  (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100);
+* IsotropicElectroMechanics_0 and SteinmannModel, electric-enthalpy models whose Hessians are
+  given directly (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100, SteinmannModel.py:40-120);
 * IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94),
   IsotropicElectroMechanics_105 (IsotropicElectroMechanics_105.py:41-104),
   IsotropicElectroMechanics_106 (IsotropicElectroMechanics_106.py:41-125) and
@@ -187,7 +187,27 @@ def em0(F, E, mu, lamb, eps_1):
     return D, sigma, H
 
 
-MATERIALS = {"IsotropicElectroMechanics_108": em108, "IsotropicElectroMechanics_101": em101,
+def steinmann(F, E, mu, lamb, c1, c2, eps_1):
+    """(D, sigma, H[9x9]) of SteinmannModel (MaterialLibrary/SteinmannModel.py:40-120,
+    LLDispatch/CythonSource/_SteinmannModel_.h): electric enthalpy
+    W_n(C) + c1 I:(E0 x E0) + c2 C:(E0 x E0) - eps_1/2 J C^-1:(E0 x E0), Hessian given directly:
+    material 0's plus c2 terms in the stress and coupling and c1, c2 terms in the dielectric block."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    be = b @ E
+    D0, sigma0, H = em0(F, E, mu, lamb, eps_1)
+    D = eps_1 * E - (2.0 * c1 / J) * be - (2.0 * c2 / J) * (b @ b) @ E
+    sigma = sigma0 + (2.0 * c2 / J) * np.outer(be, be)
+    P = eps_1 * (d[:, None, :] * E[None, :, None] + E[:, None, None] * d[None, :, :] - d[:, :, None] * E[None, None, :]) \
+        + (2.0 * c2 / J) * (b[:, None, :] * be[None, :, None] + be[:, None, None] * b[None, :, :])
+    H[:6, 6:] = -voigt3(P)
+    H[6:, :6] = -voigt3(P).T
+    H[6:, 6:] = -eps_1 * d + (2.0 * c1 / J) * b + (2.0 * c2 / J) * (b @ b)
+    return D, sigma, H
+
+
+MATERIALS = {"IsotropicElectroMechanics_108": em108, "SteinmannModel": steinmann, "IsotropicElectroMechanics_101": em101,
              "IsotropicElectroMechanics_0": em0, "IsotropicElectroMechanics_106": em106,
              "IsotropicElectroMechanics_105": em105}
 

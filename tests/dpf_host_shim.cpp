@@ -33,12 +33,14 @@ static double element(const MAT &m, int npe, int nq, const double *Jm, const dou
 }
 
 // material: 108 (params mu1, mu2, lamb, eps_2), 105 or 106 (mu1, mu2, lamb, eps_1, eps_2), 101 or 0
-// (mu, lamb, eps_1)
+// (mu, lamb, eps_1), 1 the Steinmann model (mu, lamb, c1, c2, eps_1)
 extern "C" double dpf_element(int material, int npe, int nq, const double *Jm, const double *w, const double *X,
                               const double *x, const double *phi, int update, const double *p, double *K, double *t) {
     if (material == 108) return element(fl::dpf::Em108{p[0], p[1], p[2], p[3]}, npe, nq, Jm, w, X, x, phi, update, K, t);
     if (material == 101) return element(fl::dpf::Em101{p[0], p[1], p[2]}, npe, nq, Jm, w, X, x, phi, update, K, t);
     if (material == 0) return element(fl::dpf::Em0{p[0], p[1], p[2]}, npe, nq, Jm, w, X, x, phi, update, K, t);
+    if (material == 1)
+        return element(fl::dpf::EmSteinmann{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, K, t);
     if (material == 105)
         return element(fl::dpf::Em105{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, K, t);
     if (material == 106)

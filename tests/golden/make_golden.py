@@ -47,6 +47,9 @@ def make_material(F, name, params):
     elif name == "AnisotropicMooneyRivlin_1":
         # params (mu1, mu2, lamb, mu3); fibre directions set per element by make_case
         m = F.AnisotropicMooneyRivlin_1(3, mu1=params[0], mu2=params[1], lamb=params[2], mu3=params[3], rho=1.0)
+    elif name == "SteinmannModel":
+        # params (mu, lamb, c1, c2, eps_1): W_n(C) + c1 I:(E0 x E0) + c2 C:(E0 x E0) - eps_1/2 J C^-1:(E0 x E0)
+        m = F.SteinmannModel(3, mu=params[0], lamb=params[1], c1=params[2], c2=params[3], eps_1=params[4], rho=1.0)
     elif name == "IsotropicElectroMechanics_0":
         # params (mu, lamb, eps_1): electric enthalpy W_n(C) - eps_1/2 J C^-1:(E0 x E0)
         m = F.IsotropicElectroMechanics_0(3, mu=params[0], lamb=params[1], eps_1=params[2], rho=1.0)
@@ -295,6 +298,8 @@ DPF_CASES = [
     dict(name="dpf_hex_p2_em105", mesh="box_hex", n=(2, 1, 1), L=(2.0, 1.0, 1.0), p=2,
          material="IsotropicElectroMechanics_105", params=(0.6, 0.25, 12.0, 2.0, 1.2), seed=35, amp=0.03,
          phi_amp=0.25, emat=(0, 1)),
+    dict(name="dpf_tet_p2_steinmann", mesh="cube_tet", n=(1, 1, 1), p=2, material="SteinmannModel",
+         params=(1.0, 8.0, 0.15, 0.1, 1.3), seed=36, amp=0.03, phi_amp=0.25, emat=(2, 3)),
     dict(name="dpf_tet_p2_em101", mesh="cube_tet", n=(1, 1, 1), p=2, material="IsotropicElectroMechanics_101",
          params=(0.8, 12.0, 1.7), seed=32, amp=0.02, phi_amp=0.15, emat=(0, 3)),
 ]

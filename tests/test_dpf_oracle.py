@@ -44,6 +44,11 @@ def test_dpf_sparsity_pattern_nvar4(oracle, case):
     assert np.array_equal(dl, d["sp_data_local"]) and np.array_equal(dg, d["sp_data_global"])
 
 
+SHIM_MATERIALS = {"IsotropicElectroMechanics_108": 108, "IsotropicElectroMechanics_106": 106,
+                  "IsotropicElectroMechanics_105": 105, "IsotropicElectroMechanics_101": 101,
+                  "IsotropicElectroMechanics_0": 0, "SteinmannModel": 1}
+
+
 @pytest.fixture(scope="module")
 def dpf_host(tmp_path_factory):
     """Host build of the device kernel's DPF arithmetic (florence_gb300/csrc/fl_dpf.cuh)."""
@@ -76,7 +81,7 @@ def test_device_dpf_arithmetic_on_host(dpf_host, case):
         K = np.zeros((4 * npe, 4 * npe))
         t = np.zeros(4 * npe)
         p = np.ascontiguousarray(d["params"], np.float64)
-        mat = int(str(d["material"]).rsplit("_", 1)[1])
+        mat = SHIM_MATERIALS[str(d["material"])]
         minJ = dpf_host.dpf_element(mat, npe, nq, Jm.ctypes.data, w.ctypes.data, X.ctypes.data, x.ctypes.data,
                                     phi.ctypes.data, int(d["update"]), p.ctypes.data, K.ctypes.data, t.ctypes.data)
         assert minJ > 0

@@ -47,7 +47,7 @@ def test_dpf_assembly(case, mode):
 
 @pytest.mark.parametrize("recompute", [True, False])
 @pytest.mark.parametrize("case", ["dpf_tet_p2_em108", "dpf_tet_p2_em101", "dpf_hex_p2_em0", "dpf_tet_p2_em106",
-                                  "dpf_hex_p2_em105"])
+                                  "dpf_hex_p2_em105", "dpf_tet_p2_steinmann"])
 def test_dpf_drop_in(case, recompute):
     import florence_gb300 as fl
     d = load_golden(case)
@@ -63,7 +63,8 @@ def test_dpf_drop_in(case, recompute):
     name = str(d["material"])
     names = {"IsotropicElectroMechanics_108": ("mu1", "mu2", "lamb", "eps_2"),
              "IsotropicElectroMechanics_106": ("mu1", "mu2", "lamb", "eps_1", "eps_2"),
-             "IsotropicElectroMechanics_105": ("mu1", "mu2", "lamb", "eps_1", "eps_2")}.get(name, ("mu", "lamb", "eps_1"))
+             "IsotropicElectroMechanics_105": ("mu1", "mu2", "lamb", "eps_1", "eps_2"),
+             "SteinmannModel": ("mu", "lamb", "c1", "c2", "eps_1")}.get(name, ("mu", "lamb", "eps_1"))
     material = types.SimpleNamespace(H_VoigtSize=9, **dict(zip(names, map(float, d["params"]))))
     fn = getattr(fl, "_LowLevelAssemblyDPF__" + name + "_")
     out = fn(solver, fs, form, mesh, material, d["Eulerx"], d["Eulerp"])
