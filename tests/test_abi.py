@@ -2,6 +2,7 @@
 import os
 import re
 
+import numpy as np
 import pytest
 
 from conftest import ROOT
@@ -74,3 +75,33 @@ def test_host_side_settings_validate_their_arguments():
     for bad in ((-1, 0), (17, 0), (0, -16), (0, 112)):
         with pytest.raises(FlorenceGB300Error):
             fl.set_tensor_core_tiling(*bad)
+
+
+def test_new_entry_points_reject_bad_arguments_before_any_device_work():
+    """The DPF, consistent-mass and mesher entry points validate their arguments on the host and
+    return an error status before any CUDA call (dummy, never dereferenced pointers)."""
+    import ctypes
+    from florence_gb300 import _native
+    L = _native.lib()
+    dummy = ctypes.c_void_p(16)
+    # DPF: nvar must be 4 and H_VoigtSize 9 (checked before anything is read)
+    args = [dummy] * 7 + [3, 3, 8, 6, 10, 27, 9, 1, None, None, dummy, dummy, dummy, dummy, 1, 0, None, None, None,
+                          None, 1.0, 1.0, 0.5, 0.3, 0.0, 0.0, 10.0, 1.0, 2.0, 0.0, 0.0, None, None, None]
+    for name in ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_", "fl_GlobalAssemblyDPF__SteinmannModel_"):
+        assert getattr(L, name)(*args) == _native.FL_ERR_ARG
+    # material 108 without eps_2
+    args108 = list(args)
+    args108[7], args108[8], args108[35] = 3, 4, 0.0  # ndim, nvar, eps_2
+    assert L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_(*args108) == _native.FL_ERR_ARG
+    # consistent mass: ndim 2 is refused
+    assert L.fl_ConsistentMass(dummy, dummy, dummy, dummy, dummy, 2, 3, 8, 6, 10, 27, 1.0, 1, 0, None, None, 0,
+                               None, None, dummy, dummy, dummy, None, None) == _native.FL_ERR_ARG
+    # mesher: an empty mesh is refused, an oversized layout is unsupported
+    nn = ctypes.c_int64(0)
+    lam = np.zeros((4, 4))
+    np.fill_diagonal(lam, 1.0)
+    assert L.fl_RaiseTetOrder(dummy, 10, dummy, 0, lam.ctypes.data, 4, None, 0, ctypes.byref(nn), dummy, dummy,
+                              1 << 20, None) == _native.FL_ERR_ARG
+    big = np.zeros((36, 4))
+    assert L.fl_RaiseTetOrder(dummy, 10, dummy, 1, big.ctypes.data, 36, None, 0, ctypes.byref(nn), dummy, dummy,
+                              1 << 20, None) == _native.FL_ERR_UNSUPPORTED
