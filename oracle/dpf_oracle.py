@@ -13,6 +13,8 @@ What it restates (paths inside the Florence repository):
 * the DPF strain-displacement matrix and total traction (Voigt order xx, yy, zz, xy, xz, yz;
   electric rows carry grad N; VariationalPrinciple/_ConstitutiveStiffness_/
   DisplacementPotentialApproachIndices.pyx:1-50, :203-230);
+* Piezoelectric_100 (MaterialLibrary/Piezoelectric_100.py:43-170), transversely isotropic with one
+  fibre direction per element;
 * IsotropicElectroMechanics_0 and SteinmannModel, electric-enthalpy models whose Hessians are
   given directly (MaterialLibrary/IsotropicElectroMechanics_0.py:43-100, SteinmannModel.py:40-120);
 * IsotropicElectroMechanics_101 (MaterialLibrary/IsotropicElectroMechanics_101.py:38-94),
@@ -207,7 +209,45 @@ def steinmann(F, E, mu, lamb, c1, c2, eps_1):
     return D, sigma, H
 
 
-MATERIALS = {"IsotropicElectroMechanics_108": em108, "SteinmannModel": steinmann, "IsotropicElectroMechanics_101": em101,
+def piezo100(F, E, N, mu1, mu2, mu3, lamb, eps_1, eps_2, eps_3):
+    """(D, sigma, H[9x9]) of Piezoelectric_100 (MaterialLibrary/Piezoelectric_100.py:43-170), a
+    transversely isotropic internal-energy model with fibre direction N (one per element):
+    D = W_di^-1 (E - 2 s F N + 2 s / J H N), s = sqrt(mu3 / eps_3), H = J F^-T."""
+    d = np.eye(3)
+    J = np.linalg.det(F)
+    b = F @ F.T
+    Hc = J * np.linalg.inv(F).T
+    FN, HN = F @ N, Hc @ N
+    s = np.sqrt(mu3 / eps_3)
+    W_di = (J / eps_1) * np.linalg.inv(b) + d / eps_2 + 2.0 * J * s * d
+    D = np.linalg.solve(W_di, E - 2.0 * s * FN + (2.0 / J) * s * HN)
+    hh = HN @ HN
+    sigma = (2.0 * mu1 / J) * b + (2.0 * mu2 / J) * (np.trace(b) * b - b @ b) \
+        - (2.0 * (mu1 + 2.0 * mu2 + mu3) / J) * d + lamb * (J - 1.0) * d \
+        + (2.0 * mu3 / J) * (np.outer(FN, FN) + hh * d - np.outer(HN, HN)) \
+        + (np.outer(D, D) - 0.5 * (D @ D) * d) / eps_2 + 2.0 * J * s * np.outer(D, D) \
+        + 2.0 * s * (np.outer(D, FN) + np.outer(FN, D))
+    dd_ij_kl = d[:, :, None, None] * d[None, None, :, :]
+    sym = d[:, None, :, None] * d[None, :, None, :] + d[:, None, None, :] * d[None, :, :, None]
+    hnhn = np.outer(HN, HN)
+    # 108's tensors: its mechanical elasticity (at D = 0), its electric elasticity and coupling at D
+    W_mech, _ = em108_tensors(b, J, np.zeros(3), mu1, mu2, lamb, eps_2)
+    W_elec, W_cp108 = em108_tensors(b, J, D, 0.0, 0.0, 0.0, eps_2)
+    # the fibre terms: delta_il HN_j HN_k + delta_jl HN_i HN_k + delta_ik HN_j HN_l + delta_jk HN_i HN_l
+    fibre = (d[:, None, None, :] * hnhn[None, :, :, None] + d[None, :, None, :] * hnhn[:, None, :, None]
+             + d[:, None, :, None] * hnhn[None, :, None, :] + d[None, :, :, None] * hnhn[:, None, None, :])
+    W_el = W_mech + W_elec + (2.0 * mu3 / J) * sym \
+        - (4.0 * mu3 / J) * (d[:, :, None, None] * hnhn[None, None] + hnhn[:, :, None, None] * d[None, None]) \
+        + (2.0 * mu3 / J) * hh * (2.0 * dd_ij_kl - sym) + (2.0 * mu3 / J) * fibre
+    W_cp = W_cp108 + 2.0 * J * s * (d[:, None, :] * D[None, :, None] + D[:, None, None] * d[None, :, :]) \
+        + 2.0 * s * (d[:, None, :] * FN[None, :, None] + FN[:, None, None] * d[None, :, :])
+    return D, sigma, enthalpy_hessian(W_el, W_cp, W_di)
+
+
+# materials whose kinetics take the element's fibre direction (after F and E)
+ORIENTED = {"Piezoelectric_100"}
+
+MATERIALS = {"IsotropicElectroMechanics_108": em108, "SteinmannModel": steinmann, "Piezoelectric_100": piezo100, "IsotropicElectroMechanics_101": em101,
              "IsotropicElectroMechanics_0": em0, "IsotropicElectroMechanics_106": em106,
              "IsotropicElectroMechanics_105": em105}
 
@@ -227,8 +267,9 @@ def b_matrix(SG):
     return B
 
 
-def element(material, params, X, x, phi, Jm, w, update=1):
-    """(K_e [4 npe, 4 npe], t_e [4 npe]) of one element."""
+def element(material, params, X, x, phi, Jm, w, update=1, orientation=None):
+    """(K_e [4 npe, 4 npe], t_e [4 npe]) of one element (orientation: its fibre direction, for the
+    transversely isotropic materials)."""
     kin = MATERIALS[material]
     npe = X.shape[0]
     K = np.zeros((NVAR * npe, NVAR * npe))
@@ -245,7 +286,8 @@ def element(material, params, X, x, phi, Jm, w, update=1):
             SG = MG
             dv = w[g] * abs(np.linalg.det(GX))
         E = -SG @ phi
-        D, sigma, H = kin(F, E, *params)
+        D, sigma, H = kin(F, E, np.asarray(orientation, np.float64), *params) if material in ORIENTED \
+            else kin(F, E, *params)
         B = b_matrix(SG)
         Kg = B @ H @ B.T
         geo = SG.T @ sigma @ SG               # grad N_a . sigma . grad N_b
@@ -258,7 +300,7 @@ def element(material, params, X, x, phi, Jm, w, update=1):
     return K, t
 
 
-def assemble(material, params, points, elements, Eulerx, Eulerp, Jm, AllGauss, update=1):
+def assemble(material, params, points, elements, Eulerx, Eulerp, Jm, AllGauss, update=1, orientations=None):
     """Dense global tangent [4N, 4N] and residual [4N]. For small meshes."""
     P = np.asarray(points, np.float64)
     x = np.asarray(Eulerx, np.float64)
@@ -271,7 +313,8 @@ def assemble(material, params, points, elements, Eulerx, Eulerp, Jm, AllGauss, u
     T = np.zeros(n)
     for e in range(el.shape[0]):
         nodes = el[e]
-        Ke, te = element(material, params, P[nodes], x[nodes], phi[nodes], Jm, w, update)
+        Ke, te = element(material, params, P[nodes], x[nodes], phi[nodes], Jm, w, update,
+                         None if orientations is None else orientations[e])
         dofs = (NVAR * nodes[:, None] + np.arange(NVAR)[None, :]).ravel()
         K[np.ix_(dofs, dofs)] += Ke
         T[dofs] += te

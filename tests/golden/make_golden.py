@@ -47,6 +47,10 @@ def make_material(F, name, params):
     elif name == "AnisotropicMooneyRivlin_1":
         # params (mu1, mu2, lamb, mu3); fibre directions set per element by make_case
         m = F.AnisotropicMooneyRivlin_1(3, mu1=params[0], mu2=params[1], lamb=params[2], mu3=params[3], rho=1.0)
+    elif name == "Piezoelectric_100":
+        # params (mu1, mu2, mu3, lamb, eps_1, eps_2, eps_3); fibre directions set per element by make_dpf_case
+        m = F.Piezoelectric_100(3, mu1=params[0], mu2=params[1], mu3=params[2], lamb=params[3], eps_1=params[4],
+                                eps_2=params[5], eps_3=params[6], rho=1.0)
     elif name == "SteinmannModel":
         # params (mu, lamb, c1, c2, eps_1): W_n(C) + c1 I:(E0 x E0) + c2 C:(E0 x E0) - eps_1/2 J C^-1:(E0 x E0)
         m = F.SteinmannModel(3, mu=params[0], lamb=params[1], c1=params[2], c2=params[3], eps_1=params[4], rho=1.0)
@@ -300,6 +304,8 @@ DPF_CASES = [
          phi_amp=0.25, emat=(0, 1)),
     dict(name="dpf_tet_p2_steinmann", mesh="cube_tet", n=(1, 1, 1), p=2, material="SteinmannModel",
          params=(1.0, 8.0, 0.15, 0.1, 1.3), seed=36, amp=0.03, phi_amp=0.25, emat=(2, 3)),
+    dict(name="dpf_tet_p2_piezo100", mesh="cube_tet", n=(1, 1, 1), p=2, material="Piezoelectric_100",
+         params=(0.5, 0.3, 0.4, 10.0, 1.5, 2.0, 3.0), fibre_seed=37, seed=38, amp=0.03, phi_amp=0.2, emat=(0, 2)),
     dict(name="dpf_tet_p2_em101", mesh="cube_tet", n=(1, 1, 1), p=2, material="IsotropicElectroMechanics_101",
          params=(0.8, 12.0, 1.7), seed=32, amp=0.02, phi_amp=0.15, emat=(0, 3)),
 ]
@@ -316,6 +322,8 @@ def make_dpf_case(F, spec):
     x = mesh.points + rng.uniform(-spec["amp"], spec["amp"], size=mesh.points.shape)
     phi = rng.uniform(-spec["phi_amp"], spec["phi_amp"], size=mesh.points.shape[0])
     mat = make_material(F, spec["material"], spec["params"])
+    if spec.get("fibre_seed") is not None:
+        mat.anisotropic_orientations = fibre_directions(mesh.nelem, spec["fibre_seed"])
     form = F.DisplacementPotentialFormulation(mesh)
     solver = F.FEMSolver(optimise=False, recompute_sparsity_pattern=False)
     K, T = F.AssembleForm(form, mesh, mat, solver, Eulerx=x, Eulerp=phi)
@@ -332,6 +340,8 @@ def make_dpf_case(F, spec):
         Jm=fs.Jm, AllGauss=fs.AllGauss.ravel(), Bases=fs.Bases, nvar=np.array(4),
         material=np.array(spec["material"]), params=np.array(spec["params"], np.float64),
         update=np.array(int(solver.requires_geometry_update)),
+        **({"orientations": np.asarray(mat.anisotropic_orientations, np.float64)}
+           if spec.get("fibre_seed") is not None else {}),
         K_indptr=K.indptr.astype(np.int32), K_indices=K.indices.astype(np.int32), K_data=K.data,
         T=np.asarray(T).ravel(),
         sp_indices=solver.indices.astype(np.int32), sp_indptr=solver.indptr.astype(np.int32),

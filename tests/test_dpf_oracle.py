@@ -18,7 +18,8 @@ def test_dpf_element_matrices(case):
     for k, e in enumerate(d["emat_ids"]):
         nodes = d["elements"][e]
         K, t = dpf_oracle.element(str(d["material"]), tuple(d["params"]), d["points"][nodes], d["Eulerx"][nodes],
-                                  d["Eulerp"][nodes], d["Jm"], np.ravel(d["AllGauss"]), int(d["update"]))
+                                  d["Eulerp"][nodes], d["Jm"], np.ravel(d["AllGauss"]), int(d["update"]),
+                                  d["orientations"][e] if "orientations" in d else None)
         assert rel_fro(K, d["emat_K"][k]) < TOL
         assert rel_fro(t, d["emat_t"][k]) < TOL
 
@@ -27,7 +28,7 @@ def test_dpf_element_matrices(case):
 def test_dpf_global_tangent_and_residual(case):
     d = load_golden(case)
     K, T = dpf_oracle.assemble(str(d["material"]), tuple(d["params"]), d["points"], d["elements"], d["Eulerx"],
-                               d["Eulerp"], d["Jm"], d["AllGauss"], int(d["update"]))
+                               d["Eulerp"], d["Jm"], d["AllGauss"], int(d["update"]), d.get("orientations"))
     n = K.shape[0]
     ref = sp.csr_matrix((d["K_data"], d["K_indices"], d["K_indptr"]), shape=(n, n)).toarray()
     assert rel_fro(K, ref) < TOL
@@ -80,6 +81,8 @@ def test_device_dpf_arithmetic_on_host(dpf_host, case):
         phi = np.ascontiguousarray(d["Eulerp"][nodes], np.float64)
         K = np.zeros((4 * npe, 4 * npe))
         t = np.zeros(4 * npe)
+        if str(d["material"]) not in SHIM_MATERIALS:
+            pytest.skip("no device arithmetic for this material yet (oracle pinned only)")
         p = np.ascontiguousarray(d["params"], np.float64)
         mat = SHIM_MATERIALS[str(d["material"])]
         minJ = dpf_host.dpf_element(mat, npe, nq, Jm.ctypes.data, w.ctypes.data, X.ctypes.data, x.ctypes.data,

@@ -20,8 +20,12 @@ def _golden_K(d):
     return sp.csr_matrix((d["K_data"], d["K_indices"], d["K_indptr"]), shape=(n, n))
 
 
+# materials with device arithmetic (the oracle also covers Piezoelectric_100)
+DEVICE_CASES = [c for c in dpf_cases() if "piezo" not in c]
+
+
 @pytest.mark.parametrize("mode", ["csr", "squeeze", "triplet"])
-@pytest.mark.parametrize("case", dpf_cases())
+@pytest.mark.parametrize("case", DEVICE_CASES)
 def test_dpf_assembly(case, mode):
     import torch
     import florence_gb300 as fl
