@@ -20,12 +20,13 @@ from .electromechanics import (DPFAssembler, _LowLevelAssemblyDPF__IsotropicElec
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_105_,
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_106_,
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_108_,
-                               _LowLevelAssemblyDPF__SteinmannModel_)
+                               _LowLevelAssemblyDPF__Piezoelectric_100_, _LowLevelAssemblyDPF__SteinmannModel_)
 
 __all__ = ["AssembleBodyForces", "AssembleExternalTractionForces", "ComputeSparsityPattern", "DeviceAssembler", "DPFAssembler",
            "_LowLevelAssemblyDPF__IsotropicElectroMechanics_108_", "_LowLevelAssemblyDPF__IsotropicElectroMechanics_101_",
            "_LowLevelAssemblyDPF__IsotropicElectroMechanics_0_", "_LowLevelAssemblyDPF__IsotropicElectroMechanics_106_",
            "_LowLevelAssemblyDPF__IsotropicElectroMechanics_105_", "_LowLevelAssemblyDPF__SteinmannModel_",
+           "_LowLevelAssemblyDPF__Piezoelectric_100_",
            "_LowLevelAssemblyDF__NeoHookean_",
            "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",

@@ -78,6 +78,7 @@ def lib():
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDPF__SteinmannModel_.argtypes = _DF_ARGS
+        L.fl_GlobalAssemblyDPF__Piezoelectric_100_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_Batched.argtypes = [INT, P, P, P, P, P, I64, I64, I64, I64, I64, P, P, P, P, P, P, P, P,
                                                   P]
         L.fl_SetAssemblyTuning.argtypes = [I64, I64, INT]
@@ -132,6 +133,7 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_", "fl_GlobalAssemblyDPF__SteinmannModel_",
+           "fl_GlobalAssemblyDPF__Piezoelectric_100_",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_ConsistentMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak", "fl_TensorCoreSelfTest",
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",

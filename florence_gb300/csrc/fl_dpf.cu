@@ -1,6 +1,6 @@
 // fl_dpf.cu -- global displacement-potential (electromechanics) assembly: the reference's
 // _GlobalAssemblyDPF_ (FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.h:8-198),
-// monomorphised for IsotropicElectroMechanics_0, _101, _105, _106, _108 and SteinmannModel as
+// monomorphised for IsotropicElectroMechanics_0, _101, _105, _106, _108, SteinmannModel and Piezoelectric_100 as
 // AOT_Assembler.py:125-220 does it, with its
 // tangent scattered like fill_global_data (triplets in element-local order, CSR through the
 // element-to-nonzero maps, or CSR by row search) and its residual accumulated into T[4 N].
@@ -22,6 +22,7 @@ constexpr int DP_NT = 128;
 
 struct DpfArgs {
     const double *points, *Eulerx, *Eulerp, *Jm, *w;
+    const double *orient;  // [nelem * 3] fibre directions (transversely isotropic materials), or null
     const uint64_t *elements;
     int64_t nelem, nnode;
     int npe, nq, update, mode;  // mode 0 CSR through maps, 1 triplets, 2 CSR by row search
@@ -69,7 +70,8 @@ __global__ void __launch_bounds__(DP_NT) dpf_kernel(const DpfArgs A, const MAT m
         __syncthreads();
         for (int g = threadIdx.x; g < nq; g += DP_NT) {
             const double J = dpf::gauss_point(npe, nq, g, A.Jm, A.w[g], X, x, phi, A.update, mat,
-                                              SG + (size_t)3 * npe * g, dv + g, D + 3 * g, sig + 9 * g, H + 81 * g);
+                                              A.orient ? A.orient + 3 * e : nullptr, SG + (size_t)3 * npe * g, dv + g,
+                                              D + 3 * g, sig + 9 * g, H + 81 * g);
             if (!(J > 0.0) && A.err) atomicOr(A.err, FL_FLAG_NONPOSITIVE_J);
         }
         __syncthreads();
@@ -140,7 +142,7 @@ static int dpf_assemble(const double *points, const uint64_t *elements, const do
                         int64_t requires_geometry_update, int32_t *I_stiff, int32_t *J_stiff, double *V_stiff,
                         double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
                         const int32_t *data_local_indices, const int32_t *data_global_indices, const MAT &mat,
-                        int *flags, cudaStream_t stream) {
+                        const double *orientations, int *flags, cudaStream_t stream) {
     if (ndim != 3 || nvar != 4 || H_VoigtSize != 9) return FL_ERR_ARG;
     if (nelem == 0 && nnode > 0 && ngauss > 0) return FL_OK;  // nothing is read or written
     if (!points || !elements || !Eulerx || !Eulerp || !Jm || !AllGauss || !V_stiff || !T || nelem < 0 ||
@@ -150,7 +152,7 @@ static int dpf_assemble(const double *points, const uint64_t *elements, const do
     A.points = points; A.Eulerx = Eulerx; A.Eulerp = Eulerp; A.Jm = Jm; A.w = AllGauss; A.elements = elements;
     A.nelem = nelem; A.nnode = nnode; A.npe = (int)nodeperelem; A.nq = (int)ngauss;
     A.update = requires_geometry_update ? 1 : 0;
-    A.V = V_stiff; A.T = T; A.err = flags;
+    A.V = V_stiff; A.T = T; A.err = flags; A.orient = orientations;
     const int64_t ndof = 4 * nodeperelem;
     if (recompute_sparsity_pattern) {
         if (!I_stiff || !J_stiff) return FL_ERR_ARG;
@@ -177,11 +179,13 @@ static int dpf_assemble(const double *points, const uint64_t *elements, const do
 
 }  // namespace fl
 
-#define FL_DPF_FORWARD(MAT_VALUE)                                                                              \
+#define FL_DPF_FORWARD_O(MAT_VALUE, ORIENT)                                                                    \
     fl::dpf_assemble(points, elements, Eulerx, Eulerp, Jm, AllGauss, ndim, nvar, ngauss, nelem, nodeperelem, nnode, \
                      H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T, recompute_sparsity_pattern, \
-                     squeeze_sparsity_pattern, data_local_indices, data_global_indices, MAT_VALUE, flags,           \
+                     squeeze_sparsity_pattern, data_local_indices, data_global_indices, MAT_VALUE, ORIENT, flags,   \
                      (cudaStream_t)stream)
+
+#define FL_DPF_FORWARD(MAT_VALUE) FL_DPF_FORWARD_O(MAT_VALUE, nullptr)
 
 // mu1, mu2, lamb, eps_2 (AOT_Assembler.py:167-168, 213-214)
 extern "C" int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
@@ -229,4 +233,14 @@ extern "C" int fl_GlobalAssemblyDPF__SteinmannModel_(FL_GLOBAL_ASSEMBLY_DF_ARGS)
     (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements; (void)sorter;
     (void)rho; (void)mu1; (void)mu2; (void)mu3; (void)mue; (void)eps_e; (void)anisotropic_orientations;
     return FL_DPF_FORWARD((fl::dpf::EmSteinmann{mu, lamb, eps_3, eps_2, eps_1}));
+}
+
+// mu1, mu2, mu3, lamb, eps_1, eps_2, eps_3 and one fibre direction per element in
+// anisotropic_orientations [nelem * 3] (AOT_Assembler.py:169-176, 215-220)
+extern "C" int fl_GlobalAssemblyDPF__Piezoelectric_100_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements; (void)sorter;
+    (void)rho; (void)mu; (void)mue; (void)eps_e;
+    if (!anisotropic_orientations || !(eps_1 != 0.0) || !(eps_2 != 0.0) || !(eps_3 > 0.0) || !(mu3 >= 0.0))
+        return FL_ERR_ARG;
+    return FL_DPF_FORWARD_O((fl::dpf::EmPiezo100{mu1, mu2, mu3, lamb, eps_1, eps_2, eps_3}), anisotropic_orientations);
 }

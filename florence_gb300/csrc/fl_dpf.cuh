@@ -8,7 +8,7 @@
 //                            VariationalPrinciple/DisplacementPotentialFormulation.py:108-200
 //   B rows and traction      VariationalPrinciple/_ConstitutiveStiffness_/DisplacementPotentialApproachIndices.pyx:1-50, :203-230
 //                            (Voigt order xx, yy, zz, xy, xz, yz; the potential's row carries grad N)
-//   materials 0, 101, 105, 106, 108, Steinmann
+//   materials 0, 101, 105, 106, 108, Steinmann, Piezoelectric_100
 //                            MaterialLibrary/LLDispatch/CythonSource/_IsotropicElectroMechanics_0_.h, _101_.h, _105_.h, _106_.h,
 //                            _IsotropicElectroMechanics_108_.h:32-112
 //   Legendre transform       MaterialLibrary/LLDispatch/CythonSource/_LegendreTransform_.h (InternalEnergyToEnthalpy)
@@ -354,14 +354,83 @@ FL_HD void material_point(const EmSteinmann &m, const double *F, const double *E
             H[(6 + k) * HV + 6 + l] = -m.eps1 * kd(k, l) + 2.0 * m.c1 / J * b[k * 3 + l] + g * bb[k * 3 + l];
 }
 
+// Piezoelectric_100 (MaterialLibrary/Piezoelectric_100.py:43-170, LLDispatch/CythonSource/
+// _Piezoelectric_100_.h): transversely isotropic internal energy with fibre direction N (one per
+// element); with s = sqrt(mu3 / eps_3), H = J F^-T: dielectric tensor
+// J/eps_1 b^-1 + (1/eps_2 + 2 J s) I, D = (that tensor)^-1 (E - 2 s F N + 2 s / J H N)
+struct EmPiezo100 {
+    double mu1, mu2, mu3, lamb, eps1, eps2, eps3;
+};
+
+struct EmPiezo100Point {
+    const double *b, *D, *FN, *HN;
+    double J, DD, hh, s;
+    EmPiezo100 m;
+    FL_HD double wel(int i, int j, int k, int l) const {
+        const double sym = kd(i, k) * kd(j, l) + kd(i, l) * kd(j, k);
+        const double dd = kd(i, j) * kd(k, l);
+        const double c = 2.0 * m.mu3 / J;
+        return 2.0 * m.mu2 / J * (2.0 * b[i * 3 + j] * b[k * 3 + l] - b[i * 3 + k] * b[j * 3 + l] - b[i * 3 + l] * b[j * 3 + k]) +
+               (2.0 * (m.mu1 + 2.0 * m.mu2) / J - m.lamb * (J - 1.0)) * sym + m.lamb * (2.0 * J - 1.0) * dd +
+               (0.5 * DD * (sym + dd) - kd(i, j) * D[k] * D[l] - D[i] * D[j] * kd(k, l)) / m.eps2 + c * sym -
+               2.0 * c * (kd(i, j) * HN[k] * HN[l] + HN[i] * HN[j] * kd(k, l)) + c * hh * (2.0 * dd - sym) +
+               c * (kd(i, l) * HN[j] * HN[k] + kd(j, l) * HN[i] * HN[k] + kd(i, k) * HN[j] * HN[l] + kd(j, k) * HN[i] * HN[l]);
+    }
+    FL_HD double wcp(int i, int j, int k) const {
+        return (kd(i, k) * D[j] + D[i] * kd(j, k) - kd(i, j) * D[k]) / m.eps2 +
+               2.0 * J * s * (kd(i, k) * D[j] + D[i] * kd(j, k)) + 2.0 * s * (kd(i, k) * FN[j] + FN[i] * kd(j, k));
+    }
+};
+
+FL_HD void material_point_n(const EmPiezo100 &m, const double *F, const double *E, const double *N, double *D,
+                            double *sigma, double *H) {
+    const double J = det3(F);
+    double b[9], ib[9], iF[9], W[9], Winv[9], FN[3], HN[3], r[3];
+    left_cauchy_green(F, b);
+    inv3(b, ib);
+    inv3(F, iF);
+    const double s = std::sqrt(m.mu3 / m.eps3);
+    for (int i = 0; i < 3; ++i) {
+        FN[i] = F[i * 3] * N[0] + F[i * 3 + 1] * N[1] + F[i * 3 + 2] * N[2];
+        HN[i] = J * (iF[i] * N[0] + iF[3 + i] * N[1] + iF[6 + i] * N[2]);  // (J F^-T N)_i
+    }
+    for (int k = 0; k < 9; ++k) W[k] = J / m.eps1 * ib[k] + (k % 4 == 0 ? 1.0 / m.eps2 + 2.0 * J * s : 0.0);
+    inv3(W, Winv);
+    for (int i = 0; i < 3; ++i) r[i] = E[i] - 2.0 * s * FN[i] + 2.0 / J * s * HN[i];
+    for (int k = 0; k < 3; ++k) D[k] = Winv[k * 3] * r[0] + Winv[k * 3 + 1] * r[1] + Winv[k * 3 + 2] * r[2];
+    const double DD = D[0] * D[0] + D[1] * D[1] + D[2] * D[2];
+    const double hh = HN[0] * HN[0] + HN[1] * HN[1] + HN[2] * HN[2];
+    const double trb = b[0] + b[4] + b[8];
+    const double c = 2.0 * m.mu3 / J;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const double bb = b[i * 3] * b[j] + b[i * 3 + 1] * b[3 + j] + b[i * 3 + 2] * b[6 + j];
+            sigma[i * 3 + j] = 2.0 * m.mu1 / J * b[i * 3 + j] + 2.0 * m.mu2 / J * (trb * b[i * 3 + j] - bb) -
+                               2.0 * (m.mu1 + 2.0 * m.mu2 + m.mu3) / J * kd(i, j) + m.lamb * (J - 1.0) * kd(i, j) +
+                               c * (FN[i] * FN[j] + hh * kd(i, j) - HN[i] * HN[j]) +
+                               (D[i] * D[j] - 0.5 * DD * kd(i, j)) / m.eps2 + 2.0 * J * s * D[i] * D[j] +
+                               2.0 * s * (D[i] * FN[j] + FN[i] * D[j]);
+        }
+    const EmPiezo100Point pt{b, D, FN, HN, J, DD, hh, s, m};
+    enthalpy_hessian_general(pt, Winv, H);
+}
+
+// materials without a fibre direction ignore N
+template <class MAT>
+FL_HD void material_point_n(const MAT &m, const double *F, const double *E, const double *, double *D, double *sigma,
+                            double *H) {
+    material_point(m, F, E, D, sigma, H);
+}
+
 // Gauss point g of one element: spatial gradients SG[d * npe + a] (material gradients when the
 // geometry is not updated), the weight dv = w |det dX/dxi| (|J| too with the update), the spatial
 // electric field E = -grad phi, and the material's D, sigma and H. X, x [npe * 3], phi [npe];
-// Jm [3 * npe * nq] (d-major, then node, then point). Returns det F.
+// Jm [3 * npe * nq] (d-major, then node, then point); N the element's fibre direction (transversely
+// isotropic materials; ignored by the others). Returns det F.
 template <class MAT>
 FL_HD double gauss_point(int npe, int nq, int g, const double *Jm, double w, const double *X, const double *x,
-                         const double *phi, int update, const MAT &m, double *SG, double *dv, double *D,
-                         double *sigma, double *H) {
+                         const double *phi, int update, const MAT &m, const double *N, double *SG, double *dv,
+                         double *D, double *sigma, double *H) {
     double GX[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, iGX[9];
     for (int a = 0; a < npe; ++a)
         for (int d = 0; d < 3; ++d) {
@@ -400,7 +469,7 @@ FL_HD double gauss_point(int npe, int nq, int g, const double *Jm, double w, con
     double E[3] = {0, 0, 0};
     for (int a = 0; a < npe; ++a)
         for (int k = 0; k < 3; ++k) E[k] -= SG[k * npe + a] * phi[a];
-    material_point(m, F, E, D, sigma, H);
+    material_point_n(m, F, E, N, D, sigma, H);
     return detF;
 }
 

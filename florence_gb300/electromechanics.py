@@ -1,12 +1,13 @@
 """Displacement-potential (electromechanics) assembly on the GPU: three displacements and the
 electric potential per node (nvar 4, global dof 4 n + v), IsotropicElectroMechanics_108, _106, _105,
-_101, _0 and SteinmannModel.
+_101, _0, SteinmannModel and Piezoelectric_100 (one fibre direction per element).
 
 * ``DPFAssembler`` keeps the mesh, function-space tables and the nvar=4 CSR pattern on the device
   and assembles the tangent and residual from device coordinates and potentials
   (``fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_``).
-* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_<108|106|105|101|0>_`` and
-  ``_LowLevelAssemblyDPF__SteinmannModel_`` are the drop-ins for the reference's
+* ``_LowLevelAssemblyDPF__IsotropicElectroMechanics_<108|106|105|101|0>_``,
+  ``_LowLevelAssemblyDPF__SteinmannModel_`` and ``_LowLevelAssemblyDPF__Piezoelectric_100_`` are the
+  drop-ins for the reference's
   Cython wrapper (Florence/FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.pyx:53-160):
   the reference's dispatcher (_LowLevelAssembly_.py:45-83) finds it by name when
   ``formulation.fields == "electro_mechanics"``; ``florence_gb300.install`` registers them.
@@ -31,7 +32,11 @@ MATERIALS = {"IsotropicElectroMechanics_108": ("fl_GlobalAssemblyDPF__IsotropicE
                                                ("mu1", "mu2", "lamb", "eps_1", "eps_2")),
              "IsotropicElectroMechanics_105": ("fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_",
                                                ("mu1", "mu2", "lamb", "eps_1", "eps_2")),
-             "SteinmannModel": ("fl_GlobalAssemblyDPF__SteinmannModel_", ("mu", "lamb", "c1", "c2", "eps_1"))}
+             "SteinmannModel": ("fl_GlobalAssemblyDPF__SteinmannModel_", ("mu", "lamb", "c1", "c2", "eps_1")),
+             "Piezoelectric_100": ("fl_GlobalAssemblyDPF__Piezoelectric_100_",
+                                   ("mu1", "mu2", "mu3", "lamb", "eps_1", "eps_2", "eps_3"))}
+# transversely isotropic: one fibre direction per element (material.anisotropic_orientations)
+ORIENTED = {"Piezoelectric_100"}
 # material attributes passed in other scalar slots of the reference's argument list
 # (_LowLevelAssemblyDPF_.pyx as AOT_Assembler.py:202-203 rewrites it for the Steinmann model)
 _ABI_SLOT = {"c1": "eps_3", "c2": "eps_2"}
@@ -41,11 +46,12 @@ _ABI_SCALARS = ("rho", "mu", "mu1", "mu2", "mu3", "mue", "lamb", "eps_1", "eps_2
 class DPFAssembler:
     """points [N,3], elements [E,npe], Jm [3,npe,nq], AllGauss [nq]; params (mu1, mu2, lamb, eps_2)
     for IsotropicElectroMechanics_108, (mu1, mu2, lamb, eps_1, eps_2) for _106 and _105, (mu, lamb, eps_1)
-    for _101 and _0, (mu, lamb, c1, c2, eps_1) for SteinmannModel; mode 'csr' (element-to-nonzero
+    for _101 and _0, (mu, lamb, c1, c2, eps_1) for SteinmannModel, (mu1, mu2, mu3, lamb, eps_1, eps_2,
+    eps_3) with `orientations` [E,3] for Piezoelectric_100; mode 'csr' (element-to-nonzero
     maps), 'squeeze' (row search) or 'triplet'."""
 
     def __init__(self, points, elements, Jm, AllGauss, params, material="IsotropicElectroMechanics_108",
-                 mode="csr", device="cuda", requires_geometry_update=1, sparsity=None):
+                 mode="csr", device="cuda", requires_geometry_update=1, sparsity=None, orientations=None):
         if material not in MATERIALS:
             raise NotImplementedError("the GB300 DPF assembly provides " + ", ".join(MATERIALS))
         self.device = torch.device(device)
@@ -64,6 +70,15 @@ class DPFAssembler:
             raise ValueError("%s takes (%s)" % (material, ", ".join(names)))
         given = {_ABI_SLOT.get(k, k): v for k, v in zip(names, self.params)}
         self.scalars = tuple(given.get(k, 1.0 if k == "rho" else 0.0) for k in _ABI_SCALARS)
+        self.orient = None
+        if material in ORIENTED:
+            if orientations is None:
+                raise ValueError(material + " needs one fibre direction per element (orientations)")
+            self.orient = _to_dev(np.asarray(orientations, np.float64).reshape(-1, 3)
+                                  if not isinstance(orientations, torch.Tensor) else orientations.reshape(-1, 3),
+                                  torch.float64, self.device)
+            if self.orient.shape[0] != self.nelem:
+                raise ValueError("orientations must hold one direction per element")
         self.mode = mode
         self.update = int(requires_geometry_update)
         self.flags = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -100,7 +115,7 @@ class DPFAssembler:
             _ptr(self.points), _ptr(self.elements), _ptr(x), _ptr(p), None, _ptr(self.Jm), _ptr(self.w), 3, NVAR,
             self.nq, self.nelem, self.npe, self.nnode, 9, self.update, None, None, _ptr(Ip), _ptr(Jp), _ptr(V),
             _ptr(T), 1 if self.mode == "triplet" else 0, 1 if self.mode == "squeeze" else 0, _ptr(dl), _ptr(dg),
-            None, None, *self.scalars, None, _ptr(self.flags), stream or _stream())
+            None, None, *self.scalars, _ptr(self.orient), _ptr(self.flags), stream or _stream())
         N.check(st, self.entry)
         if self.mode == "triplet":
             return I, J, V, T
@@ -120,9 +135,10 @@ def _low_level_dpf(name, fem_solver, function_space, formulation, mesh, material
     # search, which lands it where the maps would
     mode = "triplet" if recompute else "squeeze"
     sparsity = None if recompute else (fem_solver.indices, fem_solver.indptr, None, None)
+    orient = getattr(material, "anisotropic_orientations", None) if name in ORIENTED else None
     asm = DPFAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, params,
                        material=name, mode=mode, requires_geometry_update=fem_solver.requires_geometry_update,
-                       sparsity=sparsity)
+                       sparsity=sparsity, orientations=orient)
     x = _to_dev(Eulerx, torch.float64, asm.device)
     p = _to_dev(np.ravel(Eulerp), torch.float64, asm.device)
     out = asm.assemble(x, p)
@@ -175,3 +191,11 @@ def _LowLevelAssemblyDPF__SteinmannModel_(fem_solver, function_space, formulatio
     """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
     as AOT_Assembler.py builds it for _SteinmannModel_ (mu, lamb, c1, c2, eps_1)."""
     return _low_level_dpf("SteinmannModel", fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp)
+
+
+def _LowLevelAssemblyDPF__Piezoelectric_100_(fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
+    """(I, J, V, T) if fem_solver.recompute_sparsity_pattern else (V, T) -- _LowLevelAssemblyDPF_.pyx:53-160
+    as AOT_Assembler.py builds it for _Piezoelectric_100_ (mu1, mu2, mu3, lamb, eps_1, eps_2, eps_3 and the
+    material's anisotropic_orientations, one fibre direction per element)."""
+    return _low_level_dpf("Piezoelectric_100", fem_solver, function_space, formulation, mesh, material, Eulerx,
+                          Eulerp)

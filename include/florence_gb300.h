@@ -15,7 +15,8 @@
  *                                      called from _LowLevelAssemblyDF_.pyx:115-154
  *   fl_GlobalAssemblyExplicit_DF_DPF_  FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyExplicit_DF_DPF_.h:728-829
  *                                      (signature), called from _LowLevelAssemblyExplicit_DF_DPF_.pyx:123-152
- *   fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_, _106_, _105_, _101_, _0_, fl_GlobalAssemblyDPF__SteinmannModel_
+ *   fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_, _106_, _105_, _101_, _0_, fl_GlobalAssemblyDPF__SteinmannModel_,
+ *   fl_GlobalAssemblyDPF__Piezoelectric_100_
  *                                      FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.h:8-198 (signature),
  *                                      called from _LowLevelAssemblyDPF_.pyx:53-160
  *   fl_LumpedMass, fl_ConsistentMass   VariationalPrinciple/_Mass_/_MassIntegrand_.h:249-400 (mass_type 0 / 1),
@@ -279,7 +280,8 @@ int fl_GlobalAssemblyExplicit_DF_DPF_(const double *points, const uint64_t *elem
  * Displacement-potential (electromechanics) assembly, nvar 4 (three displacements and the electric
  * potential per node, global dof 4 n + v), H_VoigtSize 9: the reference's _GlobalAssemblyDPF_
  * (FiniteElements/Assembly/_Assembly_/_LowLevelAssemblyDPF_.h:8-198) as AOT_Assembler.py:125-175
- * monomorphises it for _IsotropicElectroMechanics_108_, _106_, _105_, _101_, _0_ and _SteinmannModel_, called from
+ * monomorphises it for _IsotropicElectroMechanics_108_, _106_, _105_, _101_, _0_, _SteinmannModel_ and
+ * _Piezoelectric_100_, called from
  * _LowLevelAssemblyDPF_.pyx:53-160. Same argument list and scatter modes as the DF entries:
  * recompute_sparsity_pattern -> triplets (I_stiff, J_stiff, V_stiff [nelem*(4 npe)^2]); else
  * I_stiff = indptr [4 nnode + 1], J_stiff = indices, V_stiff [nnz] += through the maps, or by row
@@ -294,6 +296,9 @@ int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_(FL_GLOBAL_ASSEMBLY_DF_ARG
 int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu1, mu2, lamb, eps_1, eps_2 */
 int fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu1, mu2, lamb, eps_1, eps_2 */
 int fl_GlobalAssemblyDPF__SteinmannModel_(FL_GLOBAL_ASSEMBLY_DF_ARGS); /* mu, lamb, c1 as eps_3, c2 as eps_2, eps_1 */
+/* mu1, mu2, mu3, lamb, eps_1, eps_2, eps_3; anisotropic_orientations [nelem*3] required (one fibre
+ * direction per element) */
+int fl_GlobalAssemblyDPF__Piezoelectric_100_(FL_GLOBAL_ASSEMBLY_DF_ARGS);
 
 /* ------------------------------------------------------------------------------------------
  * Lumped (row-sum) mass: M[nnode*nvar] += row sums of sum_g rho N N^T w_g |det dX/dxi|.

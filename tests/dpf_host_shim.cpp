@@ -7,14 +7,14 @@
 
 template <class MAT>
 static double element(const MAT &m, int npe, int nq, const double *Jm, const double *w, const double *X,
-                      const double *x, const double *phi, int update, double *K, double *t) {
+                      const double *x, const double *phi, int update, const double *N, double *K, double *t) {
     using namespace fl::dpf;
     const int ndof = NV * npe;
     std::vector<double> SG(3 * npe * nq), H(HV * HV * nq), sig(9 * nq), D(3 * nq), dv(nq);
     double minJ = 1e300;
     for (int g = 0; g < nq; ++g) {
-        const double J = gauss_point(npe, nq, g, Jm, w[g], X, x, phi, update, m, &SG[3 * npe * g], &dv[g], &D[3 * g],
-                                     &sig[9 * g], &H[HV * HV * g]);
+        const double J = gauss_point(npe, nq, g, Jm, w[g], X, x, phi, update, m, N, &SG[3 * npe * g], &dv[g],
+                                     &D[3 * g], &sig[9 * g], &H[HV * HV * g]);
         minJ = J < minJ ? J : minJ;
     }
     for (int r = 0; r < ndof; ++r) {
@@ -33,17 +33,21 @@ static double element(const MAT &m, int npe, int nq, const double *Jm, const dou
 }
 
 // material: 108 (params mu1, mu2, lamb, eps_2), 105 or 106 (mu1, mu2, lamb, eps_1, eps_2), 101 or 0
-// (mu, lamb, eps_1), 1 the Steinmann model (mu, lamb, c1, c2, eps_1)
+// (mu, lamb, eps_1), 1 the Steinmann model (mu, lamb, c1, c2, eps_1), 100 Piezoelectric_100
+// (mu1, mu2, mu3, lamb, eps_1, eps_2, eps_3, with the element's fibre direction N)
 extern "C" double dpf_element(int material, int npe, int nq, const double *Jm, const double *w, const double *X,
-                              const double *x, const double *phi, int update, const double *p, double *K, double *t) {
-    if (material == 108) return element(fl::dpf::Em108{p[0], p[1], p[2], p[3]}, npe, nq, Jm, w, X, x, phi, update, K, t);
-    if (material == 101) return element(fl::dpf::Em101{p[0], p[1], p[2]}, npe, nq, Jm, w, X, x, phi, update, K, t);
-    if (material == 0) return element(fl::dpf::Em0{p[0], p[1], p[2]}, npe, nq, Jm, w, X, x, phi, update, K, t);
+                              const double *x, const double *phi, int update, const double *p, const double *N,
+                              double *K, double *t) {
+    using namespace fl::dpf;
+    if (material == 108) return element(Em108{p[0], p[1], p[2], p[3]}, npe, nq, Jm, w, X, x, phi, update, N, K, t);
+    if (material == 101) return element(Em101{p[0], p[1], p[2]}, npe, nq, Jm, w, X, x, phi, update, N, K, t);
+    if (material == 0) return element(Em0{p[0], p[1], p[2]}, npe, nq, Jm, w, X, x, phi, update, N, K, t);
     if (material == 1)
-        return element(fl::dpf::EmSteinmann{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, K, t);
-    if (material == 105)
-        return element(fl::dpf::Em105{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, K, t);
-    if (material == 106)
-        return element(fl::dpf::Em106{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, K, t);
+        return element(EmSteinmann{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, N, K, t);
+    if (material == 105) return element(Em105{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, N, K, t);
+    if (material == 106) return element(Em106{p[0], p[1], p[2], p[3], p[4]}, npe, nq, Jm, w, X, x, phi, update, N, K, t);
+    if (material == 100)
+        return element(EmPiezo100{p[0], p[1], p[2], p[3], p[4], p[5], p[6]}, npe, nq, Jm, w, X, x, phi, update, N, K,
+                       t);
     return -1.0;
 }

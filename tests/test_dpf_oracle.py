@@ -47,7 +47,7 @@ def test_dpf_sparsity_pattern_nvar4(oracle, case):
 
 SHIM_MATERIALS = {"IsotropicElectroMechanics_108": 108, "IsotropicElectroMechanics_106": 106,
                   "IsotropicElectroMechanics_105": 105, "IsotropicElectroMechanics_101": 101,
-                  "IsotropicElectroMechanics_0": 0, "SteinmannModel": 1}
+                  "IsotropicElectroMechanics_0": 0, "SteinmannModel": 1, "Piezoelectric_100": 100}
 
 
 @pytest.fixture(scope="module")
@@ -61,7 +61,7 @@ def dpf_host(tmp_path_factory):
     subprocess.check_call(["g++", "-O2", "-shared", "-fPIC", "-o", so, os.path.join(here, "dpf_host_shim.cpp")])
     L = ctypes.CDLL(so)
     P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
-    L.dpf_element.argtypes = [I, I, I, P, P, P, P, P, I, P, P, P]
+    L.dpf_element.argtypes = [I, I, I, P, P, P, P, P, I, P, P, P, P]
     L.dpf_element.restype = D
     return L
 
@@ -81,12 +81,12 @@ def test_device_dpf_arithmetic_on_host(dpf_host, case):
         phi = np.ascontiguousarray(d["Eulerp"][nodes], np.float64)
         K = np.zeros((4 * npe, 4 * npe))
         t = np.zeros(4 * npe)
-        if str(d["material"]) not in SHIM_MATERIALS:
-            pytest.skip("no device arithmetic for this material yet (oracle pinned only)")
         p = np.ascontiguousarray(d["params"], np.float64)
+        N = np.ascontiguousarray(d["orientations"][e], np.float64) if "orientations" in d else None
         mat = SHIM_MATERIALS[str(d["material"])]
         minJ = dpf_host.dpf_element(mat, npe, nq, Jm.ctypes.data, w.ctypes.data, X.ctypes.data, x.ctypes.data,
-                                    phi.ctypes.data, int(d["update"]), p.ctypes.data, K.ctypes.data, t.ctypes.data)
+                                    phi.ctypes.data, int(d["update"]), p.ctypes.data,
+                                    N.ctypes.data if N is not None else None, K.ctypes.data, t.ctypes.data)
         assert minJ > 0
         assert rel_fro(K, d["emat_K"][k]) < TOL
         assert rel_fro(t, d["emat_t"][k]) < TOL

@@ -34,7 +34,7 @@ def test_install_registers_callables_in_reference_namespaces():
     em = F.IsotropicElectroMechanics_108(3, mu1=0.5, mu2=0.3, lamb=10.0, eps_2=2.0)
     assert ("_LowLevelAssemblyDPF__" + type(em).__name__ + "_") in vars(mod)
     for em_name in ("IsotropicElectroMechanics_101", "IsotropicElectroMechanics_0", "IsotropicElectroMechanics_106",
-                    "IsotropicElectroMechanics_105", "SteinmannModel"):
+                    "IsotropicElectroMechanics_105", "SteinmannModel", "Piezoelectric_100"):
         name = "_LowLevelAssemblyDPF__" + em_name + "_"
         assert getattr(mod, name) is getattr(florence_gb300, name)
     from Florence.FiniteElements.Assembly.ComputeSparsityPattern import ComputeSparsityPattern

@@ -20,8 +20,7 @@ def _golden_K(d):
     return sp.csr_matrix((d["K_data"], d["K_indices"], d["K_indptr"]), shape=(n, n))
 
 
-# materials with device arithmetic (the oracle also covers Piezoelectric_100)
-DEVICE_CASES = [c for c in dpf_cases() if "piezo" not in c]
+DEVICE_CASES = dpf_cases()
 
 
 @pytest.mark.parametrize("mode", ["csr", "squeeze", "triplet"])
@@ -32,7 +31,8 @@ def test_dpf_assembly(case, mode):
     d = load_golden(case)
     n = 4 * d["points"].shape[0]
     asm = fl.DPFAssembler(d["points"], d["elements"], d["Jm"], d["AllGauss"], tuple(d["params"]),
-                          material=str(d["material"]), mode=mode, requires_geometry_update=int(d["update"]))
+                          material=str(d["material"]), mode=mode, requires_geometry_update=int(d["update"]),
+                          orientations=d.get("orientations"))
     out = asm.assemble(torch.from_numpy(d["Eulerx"]).cuda(), torch.from_numpy(d["Eulerp"]).cuda())
     asm.check_flags()
     if mode == "triplet":
@@ -51,7 +51,7 @@ def test_dpf_assembly(case, mode):
 
 @pytest.mark.parametrize("recompute", [True, False])
 @pytest.mark.parametrize("case", ["dpf_tet_p2_em108", "dpf_tet_p2_em101", "dpf_hex_p2_em0", "dpf_tet_p2_em106",
-                                  "dpf_hex_p2_em105", "dpf_tet_p2_steinmann"])
+                                  "dpf_hex_p2_em105", "dpf_tet_p2_steinmann", "dpf_tet_p2_piezo100"])
 def test_dpf_drop_in(case, recompute):
     import florence_gb300 as fl
     d = load_golden(case)
@@ -68,8 +68,10 @@ def test_dpf_drop_in(case, recompute):
     names = {"IsotropicElectroMechanics_108": ("mu1", "mu2", "lamb", "eps_2"),
              "IsotropicElectroMechanics_106": ("mu1", "mu2", "lamb", "eps_1", "eps_2"),
              "IsotropicElectroMechanics_105": ("mu1", "mu2", "lamb", "eps_1", "eps_2"),
-             "SteinmannModel": ("mu", "lamb", "c1", "c2", "eps_1")}.get(name, ("mu", "lamb", "eps_1"))
-    material = types.SimpleNamespace(H_VoigtSize=9, **dict(zip(names, map(float, d["params"]))))
+             "SteinmannModel": ("mu", "lamb", "c1", "c2", "eps_1"),
+             "Piezoelectric_100": ("mu1", "mu2", "mu3", "lamb", "eps_1", "eps_2", "eps_3")}.get(name, ("mu", "lamb", "eps_1"))
+    material = types.SimpleNamespace(H_VoigtSize=9, anisotropic_orientations=d.get("orientations"),
+                                     **dict(zip(names, map(float, d["params"]))))
     fn = getattr(fl, "_LowLevelAssemblyDPF__" + name + "_")
     out = fn(solver, fs, form, mesh, material, d["Eulerx"], d["Eulerp"])
     if recompute:
