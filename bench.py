@@ -118,6 +118,14 @@ def tensor_launches(nelem, nq):
     return 1 + 2 * ((nelem + ce - 1) // ce)
 
 
+def rt_launches(nelem, nq):
+    """Kernels one reference-tensor assembly call launches (block offsets kept by the assembler):
+    the float-pair node and shape-function tables, the reference tensor's digit planes, then
+    (Gauss-point kernel + contraction) per chunk of at most 512 MB of Gauss-point data."""
+    ce = max(1, (512 << 20) // (8 * 54 * nq))
+    return 3 + 2 * ((nelem + ce - 1) // ce)
+
+
 def pair_macs(npe, nq):
     """Multiply-adds of the contraction per element (stiffness node blocks a <= b and the U
     build), each 12 FP32-pipe instructions in the float-pair arithmetic."""
@@ -190,26 +198,61 @@ def traffic_from_profile(kernel_tag):
     return float(m.group(1)) if m else None
 
 
+def bench_config(W, nnz, world=1):
+    """The `config` object of both arms' lines (identical keys and values for one workload)."""
+    nelem = int(W["elements"].shape[0])
+    nq = int(np.ravel(W["w"]).shape[0])
+    nnode = int(W["points"].shape[0])
+    return dict(W["desc"], nelem=nelem, nnode=nnode, nnz=int(nnz), gauss_points=nq,
+                parallelism="replicas" if world > 1 else "single GPU",
+                l2="inputs larger than L2: CSR values %.0f MB and element-to-nonzero map %.0f MB per step"
+                   % (nnz * 8 / 1e6, nelem * (3 * W["elements"].shape[1]) ** 2 * 4 / 1e6))
+
+
+def cpu_model():
+    """Model string of the host CPU (lscpu, else /proc/cpuinfo, else the platform module)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 # ------------------------------------------------------------------------------------------------
 # CPU reference (oracle restatement of _GlobalAssemblyDF_)
 # ------------------------------------------------------------------------------------------------
-def cpu_assembly_rate(W, spa, target_s=12.0, max_passes=5):
+def one_core_rate(W, sample_elems=6000, passes=3):
+    """Melem/s of the C restatement on one thread, on the first `sample_elems` elements of the
+    workload (renumbered to the nodes they use, their own CSR pattern), best of `passes`."""
     from oracle import oracle
-    nthreads = oracle.max_threads()
-    nelem = W["elements"].shape[0]
+    el = W["elements"][:sample_elems]
+    used, inv = np.unique(el, return_inverse=True)
+    el = inv.reshape(el.shape).astype(np.int64)
+    P, x = W["points"][used], W["x"][used]
+    spa = oracle.sparsity(el, P.shape[0])
     times = []
-    t_all = time.perf_counter()
-    while len(times) < max_passes and (time.perf_counter() - t_all) < target_s:
+    for _ in range(passes):
         t0 = time.perf_counter()
-        oracle.assemble_df(W["material"], W["params"], W["points"], W["elements"], W["x"], W["Jm"], W["w"],
-                           mode="csr", sparsity_arrays=spa, nthreads=nthreads, fast=True)
+        oracle.assemble_df(W["material"], W["params"], P, el, x, W["Jm"], W["w"], mode="csr", sparsity_arrays=spa,
+                           nthreads=1, fast=True)
         times.append(time.perf_counter() - t0)
-    best = min(times)
-    return nelem / best / 1e6, nthreads, "%d full assemblies of all %d elements (%d threads), best pass %.3f s" % (
-        len(times), nelem, nthreads, best)
+    return el.shape[0] / min(times) / 1e6
 
 
 def run_reference(args):
+    """The reference algorithm's CPU implementation (the C restatement of _GlobalAssemblyDF_,
+    liboracle_fast.so, compiled with the reference's optimisation flags) on all host threads:
+    each step one full assembly of the workload. Also the one-thread rate on a sample."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -227,15 +270,57 @@ def run_reference(args):
                            mode="csr", sparsity_arrays=spa, nthreads=nthreads, fast=True)
     dt = time.perf_counter() - t0
     value = nelem * args.steps / dt / 1e6
+    v1 = one_core_rate(W)
     line = dict(metric="FP64 assembly throughput (tangent CSR + residual)", value=value, unit="Melem/s",
                 n_gpus=args.gpus, steps=args.steps, warmup=args.warmup, ms_per_step=dt / args.steps * 1e3,
                 higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
-                config=dict(W["desc"], nelem=nelem, nnode=int(W["points"].shape[0]), nnz=int(spa[0].shape[0])),
+                config=bench_config(W, spa[0].shape[0], int(os.environ.get("WORLD_SIZE", "1"))),
                 impl="reference",
-                cpu_baseline=dict(value=value, unit="Melem/s", cores=nthreads, kind="port",
-                                  sample="%d steps, each a full assembly of all %d elements" % (args.steps, nelem)),
+                cpu_baseline=dict(value=value, unit="Melem/s", cores=nthreads, kind="port", cpu_model=cpu_model(),
+                                  host_threads=os.cpu_count(), value_1core=v1,
+                                  sample="%d steps, each a full assembly of all %d elements on %d threads; one-thread "
+                                         "rate on the first 6000 elements" % (args.steps, nelem, nthreads)),
                 e2e=dict(value=value, unit="Melem/s", h2d_bytes_per_step=0, d2h_bytes_per_step=0))
     print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_subprocess(args, steps=20):
+    """The reference arm run as its own process (`--impl reference`), so that the CPU figure this
+    arm reports comes from the same code, the same kind of process and the same threads as the
+    reference arm's line; returns its cpu_baseline object."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", str(steps), "--warmup", "3",
+           "--workload", args.workload]
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=900)
+    for line in r.stdout.splitlines()[::-1]:
+        if line.startswith("{"):
+            cb = json.loads(line)["cpu_baseline"]
+            cb["sample"] = "reference arm run as a subprocess: " + cb["sample"]
+            return cb
+    raise RuntimeError("CPU baseline subprocess failed: " + r.stderr[-2000:])
+
+
+def parity_check(W, asm, V, T):
+    """The bench's own last-step outputs against the oracle (IEEE build, all host threads), outside
+    the timed region: the device CSR pattern and element-to-nonzero maps bit-exact against the
+    oracle's, V and T in relative Frobenius norm."""
+    from oracle import oracle
+    ind, ptr, dl, dg = oracle.sparsity(W["elements"], W["points"].shape[0])
+    exact = (np.array_equal(ind, asm.indices.cpu().numpy()) and np.array_equal(ptr, asm.indptr.cpu().numpy())
+             and np.array_equal(dl, asm.data_local.cpu().numpy()) and np.array_equal(dg, asm.data_global.cpu().numpy()))
+    Vo, To = oracle.assemble_df(W["material"], W["params"], W["points"], W["elements"], W["x"], W["Jm"], W["w"],
+                                mode="csr", sparsity_arrays=(ind, ptr, dl, dg), nthreads=oracle.max_threads())
+    Vf, Tf = oracle.assemble_df(W["material"], W["params"], W["points"], W["elements"], W["x"], W["Jm"], W["w"],
+                                mode="csr", sparsity_arrays=(ind, ptr, dl, dg), nthreads=oracle.max_threads(),
+                                fast=True)
+    Vd, Td = V.double().cpu().numpy(), T.cpu().numpy()
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))  # noqa: E731
+    return dict(K=rel(Vd, Vo), T=rel(Td, To), pattern_bit_exact=bool(exact),
+                fp64_spread=dict(K=rel(Vf, Vo), T=rel(Tf, To),
+                                 note="the same reference algorithm in FP64 with reassociation and contraction "
+                                      "(-ffast-math build) against its IEEE build: the rounding sensitivity of this "
+                                      "mesh (sliver tetrahedra), the floor no FP64 evaluation order goes below"),
+                checker="oracle (C restatement of _GlobalAssemblyDF_, IEEE build), full workload")
 
 
 # ------------------------------------------------------------------------------------------------
@@ -339,6 +424,19 @@ def run_ours(args):
                         peak_source="MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
                         note="BF16 digit products; the operand build and the scatter bound the step",
                         fp64_equivalent_tflops=achieved, fp64_equivalent_frac=achieved / fp64_peak)
+    elif args.arith == "reference_tensor":  # tiles of 14 elements x 80 node pairs, 28 BF16 plane products
+        pairs = npe * (npe + 1) // 2
+        nch = (pairs + 79) // 80
+        nks = (9 * nq + 15) // 16
+        ntiles = (nelem + 13) // 14
+        tflop = 28 * 2.0 * 128 * 80 * 16 * nks * nch * ntiles / (kernel_ms * 1e-3) / 1e12
+        peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+        bf16_peak = peaks.get("bf16_tflops", 1900.0)
+        roofline = dict(bound="tensor", achieved=tflop, peak=bf16_peak, unit="TFLOP/s", frac=tflop / bf16_peak,
+                        peak_source="MEASURED_PEAKS.json bf16_tflops" if "bf16_tflops" in peaks else "fallback",
+                        note="BF16 digit-plane products of the whole assembly call (Gauss-point kernel included "
+                             "in the time)", fp64_equivalent_tflops=achieved,
+                        fp64_equivalent_frac=achieved / fp64_peak)
     else:  # the contraction runs as float pairs on the FP32 pipe
         instr = 12.0 * pair_macs(npe, nq) * nelem
         ach_i = instr / (kernel_ms * 1e-3) / 1e12
@@ -348,12 +446,45 @@ def run_ours(args):
                         fp64_equivalent_tflops=achieved, fp64_equivalent_frac=achieved / fp64_peak,
                         instr_per_launch=instr)
     tag = {"fp64": "assemble_df_%s_%s", "float_pair": "contract_float_pair_%s_%s", "tensor": "contract_oz_%s_%s",
-           "mixed": "contract_tc_%s_%s"}[args.arith] % (W["desc"]["element"], W["desc"]["material"])
+           "reference_tensor": "rt_contract_%s_%s", "mixed": "contract_tc_%s_%s"}[args.arith] % (
+        W["desc"]["element"], W["desc"]["material"])
     roofline.update(traffic=traffic_from_profile(tag), flop_alg_per_launch=f_alg, flop_executed_per_launch=f_exe,
                     kernel_ms=kernel_ms,
                     hbm=dict(bytes_min_per_launch=bmin, achieved_gbs=bmin / (kernel_ms * 1e-3) / 1e9,
                              peak_gbs=hbm_peak, frac=bmin / (kernel_ms * 1e-3) / 1e9 / hbm_peak,
                              peak_source="MEASURED_PEAKS.json" if os.path.exists(PEAKS) else "fallback 6.8 TB/s"))
+
+    # the same assembly scattering by row search (the drop-in's CSR path), device time
+    squeeze = None
+    if rank == 0 and not mixed and not args.no_e2e:
+        sq = fl.DeviceAssembler(W["points"], W["elements"], W["Jm"], W["w"], W["material"], W["params"],
+                                mode="squeeze", device=dev, sparsity=(asm.indices, asm.indptr, None, None))
+        Vs = torch.zeros_like(V)
+        for _ in range(3):
+            Vs.zero_()
+            sq.assemble(x, V=Vs, T=T.zero_())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        nsq = max(3, min(args.steps, 10))
+        for _ in range(nsq):
+            Vs.zero_()
+            T.zero_()
+            sq.assemble(x, V=Vs, T=T)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms_sq = e0.elapsed_time(e1) / nsq
+        squeeze = dict(ms_per_step=ms_sq, value=nelem / (ms_sq * 1e-3) / 1e6, unit="Melem/s",
+                       note="CSR positions found by row search in the pattern (no element-to-nonzero maps): "
+                            "the scatter of the drop-in callable")
+        del sq, Vs
+
+    # parity of the timed workload against the oracle (outside the timed region): rerun one step
+    parity = None
+    if rank == 0 and not args.no_parity:
+        step()
+        torch.cuda.synchronize()
+        parity = parity_check(W, asm, V, T)
 
     # end to end through the drop-in callable (host numpy in and out, copies inside)
     e2e = None
@@ -362,10 +493,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        spa = (asm.indices.cpu().numpy(), asm.indptr.cpu().numpy(), asm.data_local.cpu().numpy(),
-               asm.data_global.cpu().numpy())
-        v, cores, sample = cpu_assembly_rate(W, spa)
-        cpu = dict(value=v, unit="Melem/s", cores=cores, kind="port", sample=sample)
+        cpu = cpu_baseline_subprocess(args)
 
     if rank == 0:
         line = dict(metric="FP64 assembly throughput (tangent CSR + residual)" if not mixed else
@@ -374,15 +502,15 @@ def run_ours(args):
                     n_gpus=world, steps=args.steps, warmup=args.warmup, ms_per_step=ms / args.steps,
                     higher_is_better=True, scaling="weak", vs_baseline=None,
                     dtype={"fp64": "f64", "float_pair": "f64 (float-pair contraction)",
+                           "reference_tensor": "f64 (seven-digit BF16 plane products on tcgen05, exact levels, "
+                                               "integer recombination)",
                            "tensor": "f64 (six-digit BF16 products, exact f32 levels, float-pair recombination)",
                            "mixed": "bf16x3 products, f32 accumulate; f64 residual"}[args.arith], data="synthetic",
-                    config=dict(W["desc"], nelem=int(nelem), nnode=int(nnode), nnz=int(asm.nnz), gauss_points=nq,
-                                parallelism="replicas" if world > 1 else "single GPU",
-                                l2="inputs larger than L2: CSR values %.0f MB and element-to-nonzero map %.0f MB "
-                                   "per step" % (asm.nnz * 8 / 1e6, asm.data_global.numel() * 4 / 1e6)),
-                    roofline=roofline, cpu_baseline=cpu, e2e=e2e, clocks=clocks,
+                    config=bench_config(W, asm.nnz, world),
+                    roofline=roofline, cpu_baseline=cpu, e2e=e2e, clocks=clocks, parity=parity, squeeze=squeeze,
                     gpu_launches=args.steps * (mixed_launches(nelem, nq) if mixed else
                                                tensor_launches(nelem, nq) if args.arith == "tensor" else
+                                               rt_launches(nelem, nq) if args.arith == "reference_tensor" else
                                                assembly_launches(nelem, npe, nq)))
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -605,8 +733,10 @@ def run_batched(args):
 
 
 def e2e_dropin(W, asm, args):
-    """The reference-facing call (_LowLevelAssemblyDF__<Mat>_) with host arrays: uploads mesh,
-    tables, CSR pattern and coordinates, assembles, downloads V and T -- every step."""
+    """The reference-facing call (_LowLevelAssemblyDF__<Mat>_) with host arrays, as Florence's
+    Newton loop makes it: the first calls upload the mesh, its tables and the CSR pattern (kept on
+    the device between calls with the same arrays); every timed call uploads the coordinates
+    Eulerx, assembles, and downloads V and T into host arrays."""
     import torch
     import florence_gb300 as fl
     spa = (asm.indices.cpu().numpy(), asm.indptr.cpu().numpy(), asm.data_local.cpu().numpy(),
@@ -636,12 +766,13 @@ def e2e_dropin(W, asm, args):
     for _ in range(steps):
         V, T = fn(solver, fs, form, mesh, material, W["x"], Ep)
     dt = (time.perf_counter() - t0) / steps
-    # uploaded per call: mesh, tables, coordinates and the CSR pattern (the maps are not read)
-    h2d = sum(a.nbytes for a in (W["points"], mesh.elements, W["x"], W["Jm"], np.ravel(W["w"]), spa[0], spa[1]))
+    # uploaded per timed call: the coordinates (the mesh, tables and pattern stay on the device)
+    h2d = W["x"].nbytes
     d2h = V.nbytes + T.nbytes
     return dict(value=W["elements"].shape[0] / dt / 1e6, unit="Melem/s", h2d_bytes_per_step=int(h2d),
                 d2h_bytes_per_step=int(d2h), ms_per_step=dt * 1e3, steps=steps,
-                path="florence_gb300._LowLevelAssemblyDF__%s_ (host numpy, pageable)" % mat)
+                path="florence_gb300._LowLevelAssemblyDF__%s_ (host numpy in; outputs in pooled pinned host "
+                     "buffers; mesh kept on the device between calls)" % mat)
 
 
 def run_warmstart(args):
@@ -762,6 +893,118 @@ def run_meshing(args):
     print(json.dumps(line), flush=True)
 
 
+def _time_device(fn, steps, warmup=3):
+    """Mean device time (ms) of fn() over `steps` calls after `warmup`, CUDA events on the current
+    stream, with nvidia-smi clock samples over the timed calls."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(0) as clk:
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, clk.summary()
+
+
+def run_dpf(args):
+    """Electromechanics (displacement-potential, nvar 4) assembly of IsotropicElectroMechanics_108
+    (mu1 = 0.4, mu2 = 0.2, lambda = 15, eps_2 = 1.5, the golden case's parameters): the tet p=2 beam
+    (48x12x12 jittered lattice, Delaunay, 8 Gauss points) and a structured p=2 hex box (40x32x32,
+    27 Gauss points), CSR by row search plus the FP64 residual; deformation and potential seeded and
+    smooth. One step = zero the outputs and assemble."""
+    import torch
+    from florence_gb300 import meshes
+    from florence_gb300.electromechanics import DPFAssembler
+    res = {}
+    for kind in ("tet_p2", "hex_p2"):
+        g = np.load(os.path.join(GOLDEN, "dpf_%s_em108.npz" % kind))
+        if kind == "tet_p2":
+            pat = meshes.local_pattern(g["points"], g["elements"], 0, "tet")
+            cells = (48, 12, 12) if args.workload != "beam_s" else (24, 6, 6)
+            P, el = meshes.jittered_tet_beam(cells, (4.0, 1.0, 1.0), 1, pat)
+        else:
+            pat = meshes.local_pattern(g["points"], g["elements"], 0, "hex")
+            cells = (40, 32, 32) if args.workload != "beam_s" else (20, 16, 16)
+            P, el = meshes.structured_hex(cells, (4.0, 1.0, 1.0), pat)
+        x = P + smooth_displacement(P, seed=2)
+        phi = 0.1 * np.sin(np.pi * P[:, 0] / 4.0) * np.cos(np.pi * P[:, 1])
+        asm = DPFAssembler(P, el, g["Jm"], g["AllGauss"], tuple(g["params"]), material=str(g["material"]),
+                           mode="squeeze")
+        xd, pd = torch.from_numpy(x).cuda(), torch.from_numpy(phi).cuda()
+        V = torch.zeros(asm.nnz, dtype=torch.float64, device="cuda")
+        T = torch.zeros(asm.nnode * 4, dtype=torch.float64, device="cuda")
+
+        def step():
+            V.zero_()
+            T.zero_()
+            asm.assemble(xd, pd, V=V, T=T)
+        ms, clocks = _time_device(step, max(3, min(args.steps, 20)))
+        asm.check_flags("dpf bench")
+        nq = int(np.ravel(g["AllGauss"]).shape[0])
+        res[kind] = dict(nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz), gauss_points=nq,
+                         ms_per_step=ms, melem_s=el.shape[0] / (ms * 1e-3) / 1e6, clocks=clocks,
+                         bytes_min=int(8 * 4 * P.shape[0] * 2 + 8 * asm.nnz + 8 * 4 * P.shape[0]))
+        del asm, V, T
+        torch.cuda.empty_cache()
+    line = dict(metric="electromechanics (DPF, nvar 4) FP64 assembly throughput, tet p=2 beam", unit="Melem/s",
+                value=res["tet_p2"]["melem_s"], n_gpus=1, steps=max(3, min(args.steps, 20)), warmup=3,
+                higher_is_better=True, scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(workload="IsotropicElectroMechanics_108 (mu1 0.4, mu2 0.2, lambda 15, eps_2 1.5): tet p=2 "
+                                     "beam 48x12x12 jittered Delaunay and p=2 hex box 40x32x32, CSR by row search + "
+                                     "residual"), tet_p2=res["tet_p2"], hex_p2=res["hex_p2"],
+                clocks=res["tet_p2"]["clocks"])
+    print(json.dumps(line), flush=True)
+
+
+def run_mass(args):
+    """Consistent mass sum_g rho N_a N_b w |det dX/dxi| on the nvar diagonal (fl_ConsistentMass) of the
+    tet p=3 beam (47 535 elements, 14 Gauss points) into its CSR pattern, through the element-to-nonzero
+    maps and by row search; and the lumped mass."""
+    import torch
+    import florence_gb300 as fl
+    W = workload(args.workload)
+    g = np.load(os.path.join(GOLDEN, "tet_p3_mr_jitter.npz"))
+    res = {}
+    asm = fl.DeviceAssembler(W["points"], W["elements"], W["Jm"], W["w"], "NeoHookean", (1.0, 10.0), mode="csr",
+                             Bases=g["Bases"])
+    sq = fl.DeviceAssembler(W["points"], W["elements"], W["Jm"], W["w"], "NeoHookean", (1.0, 10.0), mode="squeeze",
+                            Bases=g["Bases"], sparsity=(asm.indices, asm.indptr, None, None))
+    V = torch.zeros(asm.nnz, dtype=torch.float64, device="cuda")
+    M = torch.zeros(asm.nnode * 3, dtype=torch.float64, device="cuda")
+    steps = max(3, min(args.steps, 20))
+    for name, a in (("maps", asm), ("row_search", sq)):
+        def step(a=a):
+            V.zero_()
+            a.consistent_mass(1.0, V=V)
+        ms, clocks = _time_device(step, steps)
+        a.check_flags("mass bench")
+        res[name] = dict(ms_per_step=ms, melem_s=W["elements"].shape[0] / (ms * 1e-3) / 1e6, clocks=clocks)
+
+    def lumped():
+        M.zero_()
+        asm.lumped_mass(1.0, M=M)
+    ms, clocks = _time_device(lumped, steps)
+    res["lumped"] = dict(ms_per_step=ms, melem_s=W["elements"].shape[0] / (ms * 1e-3) / 1e6)
+    nnz = asm.nnz
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    bmin = 8 * nnz + 4 * W["elements"].size + 8 * 3 * W["points"].shape[0]
+    line = dict(metric="consistent mass assembly throughput (CSR, element-to-nonzero maps)", unit="Melem/s",
+                value=res["maps"]["melem_s"], n_gpus=1, steps=steps, warmup=3, higher_is_better=True,
+                scaling="weak", vs_baseline=None, dtype="f64", data="synthetic",
+                config=dict(W["desc"], nelem=int(W["elements"].shape[0]), nnz=int(nnz)),
+                roofline=dict(bound="hbm", achieved=bmin / (res["maps"]["ms_per_step"] * 1e-3) / 1e9, peak=hbm,
+                              unit="GB/s", frac=bmin / (res["maps"]["ms_per_step"] * 1e-3) / 1e9 / hbm,
+                              bytes_min_per_launch=bmin,
+                              peak_source="MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"),
+                maps=res["maps"], row_search=res["row_search"], lumped=res["lumped"], clocks=res["maps"]["clocks"])
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -769,13 +1012,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
-    ap.add_argument("--arith", default="float_pair", choices=["fp64", "float_pair", "tensor", "mixed"],
+    ap.add_argument("--arith", default="float_pair",
+                    choices=["fp64", "float_pair", "tensor", "reference_tensor", "mixed"],
                     help="arithmetic of the stiffness contraction (FP64, float pairs on the FP32 pipe, or the "
                          "split-BF16 tensor-core tangent with FP32 values)")
     ap.add_argument("--tc-tiling", default="0,0",
                     help="tile group and reduction chunk of the split-BF16 kernel (0,0 = automatic)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the oracle check of the timed workload")
     ap.add_argument("--newton", action="store_true", help="Newton load stepping of the beam instead")
     ap.add_argument("--explicit", action="store_true", help="explicit dynamics of the hex beam instead")
     ap.add_argument("--explicit-steps", type=int, default=10000)
@@ -795,6 +1040,8 @@ def main():
     ap.add_argument("--batch-gb", type=float, default=40.0, help="CSR memory budget per sub-batch")
     ap.add_argument("--warmstart", action="store_true", help="learned warm start on the plate instead")
     ap.add_argument("--meshing", action="store_true", help="device high-order tet mesh generation instead")
+    ap.add_argument("--dpf", action="store_true", help="electromechanics (nvar 4) assembly instead")
+    ap.add_argument("--mass", action="store_true", help="consistent and lumped mass assembly instead")
     ap.add_argument("--ws-train", type=int, default=2000, help="training solves")
     ap.add_argument("--ws-test", type=int, default=200, help="held-out solves")
     ap.add_argument("--ws-increments", type=int, default=5)
@@ -816,6 +1063,10 @@ def main():
         run_warmstart(args)
     elif args.meshing:
         run_meshing(args)
+    elif args.dpf:
+        run_dpf(args)
+    elif args.mass:
+        run_mass(args)
     else:
         run_ours(args)
 

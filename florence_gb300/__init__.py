@@ -13,7 +13,7 @@ from .assembly import (AssembleBodyForces, AssembleExternalTractionForces, Compu
                        _LowLevelAssemblyDF__MooneyRivlin_, _LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_,
                        _LowLevelAssemblyDF__NeoHookean_, _LowLevelAssemblyExplicit_DF_DPF_,
                        __TotalConstantMassIntegrand__, arithmetic, device_sparsity, fp32_peak_gflops, fp64_peak_gflops,
-                       get_arithmetic, install, material_params, release_host_buffers, set_arithmetic,
+                       get_arithmetic, install, material_params, release_device_meshes, release_host_buffers, set_arithmetic,
                        set_tensor_core_tiling)
 from .electromechanics import (DPFAssembler, _LowLevelAssemblyDPF__IsotropicElectroMechanics_0_,
                                _LowLevelAssemblyDPF__IsotropicElectroMechanics_101_,
@@ -32,5 +32,5 @@ __all__ = ["AssembleBodyForces", "AssembleExternalTractionForces", "ComputeSpars
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyDF__NearlyIncompressibleMooneyRivlin_",
            "_LowLevelAssemblyDF__LinearElastic_", "_LowLevelAssemblyExplicit_DF_DPF_",
            "__TotalConstantMassIntegrand__", "arithmetic", "device_sparsity", "fp32_peak_gflops", "fp64_peak_gflops", "get_arithmetic",
-           "install", "material_params", "release_host_buffers", "set_arithmetic",
+           "install", "material_params", "release_device_meshes", "release_host_buffers", "set_arithmetic",
            "set_tensor_core_tiling"]

@@ -17,6 +17,7 @@ FL_ERR_MESH = 4
 FL_ERR_CAPACITY = 5
 FL_FLAG_NONPOSITIVE_J = 1
 FL_FLAG_BAD_INDEX = 2
+FL_FLAG_TIMEOUT = 4
 FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
 FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN = 3
@@ -25,6 +26,7 @@ FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1 = 11
 FL_ARITH_FP64 = 0
 FL_ARITH_FLOAT_PAIR = 1
 FL_ARITH_TENSOR = 2
+FL_ARITH_REFERENCE_TENSOR = 3
 FL_PCG_F64 = 64
 FL_PCG_F32 = 32
 FL_PCG_F64_SPLIT = 6432
@@ -72,6 +74,8 @@ def lib():
                      "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_"):
             getattr(L, name).argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_noalloc.argtypes = [INT] + _DF_ARGS
+        L.fl_GlobalAssemblyDF_Blocks.argtypes = [INT, P] + _DF_ARGS
+        L.fl_ElementBlockOffsets.argtypes = [P, I64, I64, I64, P, P, P, P, P]
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_.argtypes = _DF_ARGS
@@ -130,6 +134,7 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
            "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
            "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_", "fl_GlobalAssemblyDF_noalloc",
+           "fl_GlobalAssemblyDF_Blocks", "fl_ElementBlockOffsets",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_", "fl_GlobalAssemblyDPF__SteinmannModel_",

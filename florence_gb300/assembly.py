@@ -35,7 +35,7 @@ __all__ = ["DeviceAssembler", "ComputeSparsityPattern", "_LowLevelAssemblyDF__Ne
            "_LowLevelAssemblyDF__AnisotropicMooneyRivlin_1_",
            "_LowLevelAssemblyDF__MooneyRivlin_", "_LowLevelAssemblyExplicit_DF_DPF_",
            "__TotalConstantMassIntegrand__", "install", "material_params", "fp64_peak_gflops",
-           "release_host_buffers"]
+           "release_host_buffers", "release_device_meshes"]
 
 MATERIALS = {"NeoHookean": N.FL_MATERIAL_NEOHOOKEAN, "MooneyRivlin": N.FL_MATERIAL_MOONEYRIVLIN,
              "NearlyIncompressibleMooneyRivlin": N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
@@ -63,6 +63,12 @@ def _abi_params(mat_id, params):
     return 0.0, p0, p1, p2, p3
 
 
+def rt_supported(npe, nq):
+    """Element types the reference-tensor contraction takes (fl_reftensor.cu): 4-, 8-, 10- and
+    20-node elements with at most 15 Gauss points."""
+    return npe in (4, 8, 10, 20) and 1 <= nq <= 15
+
+
 class NonPositiveJacobianWarning(RuntimeWarning):
     """det F <= 0 at some Gauss point (the reference propagates such values silently)."""
 
@@ -76,23 +82,25 @@ class _HostPool:
     buffer was last returned as (tracked by a weak reference; a live view or a matrix built on the
     array keeps it alive). Fresh host memory costs a page fault per page on its first write, which
     made the device-to-host copy of a 761 MB tangent run at 27 GB/s; into memory written before,
-    the same copy runs at ~190 GB/s over the Grace-GPU link. At most `keep` idle buffers per size
-    are held; ``release_host_buffers()`` frees them."""
+    the same copy runs at ~190 GB/s over the Grace-GPU link. Buffers for device results are
+    page-locked (pinned), which lets the copy engine write them directly. At most `keep` idle
+    buffers per size are held; ``release_host_buffers()`` frees them."""
 
     def __init__(self, keep=2):
         self.keep = keep
         self.slots = []  # [tensor, weakref to the array last handed out]
         self.lock = threading.Lock()
 
-    def take(self, shape, dtype):
+    def take(self, shape, dtype, pinned=False):
         n = int(np.prod(shape))
         with self.lock:
-            same = [sl for sl in self.slots if sl[0].numel() == n and sl[0].dtype == dtype]
+            same = [sl for sl in self.slots if sl[0].numel() == n and sl[0].dtype == dtype
+                    and sl[0].is_pinned() == pinned]
             idle = [sl for sl in same if sl[1]() is None]
             if idle:
                 slot = idle.pop(0)
             else:
-                slot = [torch.empty(n, dtype=dtype), None]
+                slot = [torch.empty(n, dtype=dtype, pin_memory=pinned), None]
                 self.slots.append(slot)
             drop = {id(sl) for sl in idle[self.keep:]}
             self.slots = [sl for sl in self.slots if id(sl) not in drop]
@@ -104,7 +112,7 @@ class _HostPool:
 
     def to_host(self, dev):
         """Copy of a device tensor into a pooled host array (synchronous)."""
-        t, arr = self.take(tuple(dev.shape), dev.dtype)
+        t, arr = self.take(tuple(dev.shape), dev.dtype, pinned=dev.is_cuda)
         t.copy_(dev.reshape(-1))
         return arr
 
@@ -163,6 +171,8 @@ def _check_flags(flags, what):
     f = int(flags.item())
     if f & N.FL_FLAG_BAD_INDEX:
         raise N.FlorenceGB300Error(N.FL_ERR_ARG, what + " (element node id or index map out of range)")
+    if f & N.FL_FLAG_TIMEOUT:
+        raise N.FlorenceGB300Error(N.FL_ERR_CUDA, what + " (a bounded wait in a tensor-core kernel gave up)")
     if f & N.FL_FLAG_NONPOSITIVE_J:
         warnings.warn("det F <= 0 at some Gauss point in " + what, NonPositiveJacobianWarning, stacklevel=3)
 
@@ -263,18 +273,35 @@ class DeviceAssembler:
         else:
             V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
             Ip, Jp, dl, dg = self.indptr, self.indices, self.data_local, self.data_global
-        fn = getattr(L, _DF_ENTRY[self.mat_id])
         mu, mu1, mu2, lamb, mu3 = _abi_params(self.mat_id, self.params)
-        st = fn(_ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
+        args = (_ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
                 3, 3, self.nq, self.nelem, self.npe, self.nnode, 6, self.update, None, None,
                 _ptr(Ip), _ptr(Jp), _ptr(V), _ptr(T), 1 if self.mode == "triplet" else 0,
                 1 if self.mode == "squeeze" else 0, _ptr(dl), _ptr(dg), None, None,
                 1.0, mu, mu1, mu2, mu3, 0.0, lamb, 0.0, 0.0, 0.0, 0.0, _ptr(self.orient), _ptr(self.flags),
                 stream or _stream())
+        boff = self.block_offsets(stream) if self.mode != "triplet" and \
+            N.lib().fl_GetAssemblyArithmetic() == N.FL_ARITH_REFERENCE_TENSOR and rt_supported(self.npe, self.nq) \
+            else None
+        if boff is not None:
+            st = L.fl_GlobalAssemblyDF_Blocks(self.mat_id, _ptr(boff), *args)
+        else:
+            st = getattr(L, _DF_ENTRY[self.mat_id])(*args)
         N.check(st, "fl_GlobalAssemblyDF")
         if self.mode == "triplet":
             return I, J, V, T
         return V, T
+
+    def block_offsets(self, stream=None):
+        """The pattern's per-element node-block offsets (fl_ElementBlockOffsets), built on first
+        use and kept: [nelem, npe, npe] int32, -1 where an entry must be searched."""
+        if getattr(self, "_boff", None) is None:
+            boff = torch.empty((self.nelem, self.npe, self.npe), dtype=torch.int32, device=self.device)
+            st = N.lib().fl_ElementBlockOffsets(_ptr(self.elements), self.nelem, self.npe, self.nnode, _ptr(self.indptr),
+                                               _ptr(self.indices), _ptr(boff), _ptr(self.flags), stream or _stream())
+            N.check(st, "fl_ElementBlockOffsets")
+            self._boff = boff
+        return self._boff
 
     def assemble_mixed(self, Eulerx, V32=None, T=None, stream=None):
         """Inexact-Newton Jacobian: FP32 CSR values from the split-BF16 tensor-core contraction and
@@ -385,22 +412,95 @@ def _check_formulation(formulation, material):
         raise NotImplementedError("the GB300 assembly covers three-dimensional mechanics (ndim = nvar = 3)")
 
 
+def _fingerprint(a, samples=2048):
+    """(shape, dtype, hash of an evenly spaced sample of the entries) of a host array: cheap enough
+    for every call (microseconds), and it changes when an array is replaced or resized, or its
+    sampled entries are rewritten."""
+    a = np.asarray(a)
+    flat = a.reshape(-1)
+    n = flat.shape[0]
+    idx = np.linspace(0, n - 1, min(n, samples)).astype(np.int64) if n else np.zeros(0, np.int64)
+    return a.shape, a.dtype.str, hash(np.ascontiguousarray(flat[idx]).tobytes())
+
+
+class _DeviceMeshCache:
+    """Device-resident meshes of the drop-in callables. Florence calls the low-level assembly once
+    per Newton iteration with the same mesh, function space and sparsity pattern and a new Eulerx
+    (FEMSolver.py:973): the first call uploads the mesh, its tables and its CSR pattern, later
+    calls with the same arrays upload only Eulerx. An entry is reused when every input array is
+    the same object (held by a weak reference, so a freed and reallocated array never matches) with
+    the same shape, dtype and sampled entries, and the material and flags are equal. Arrays
+    rewritten in place between calls outside the sample go unnoticed: call
+    ``release_device_meshes()`` after modifying a mesh in place. At most `keep` meshes are held."""
+
+    def __init__(self, keep=2):
+        self.keep = keep
+        self.entries = []   # (refs, fingerprints, scalars, DeviceAssembler), most recent first
+        self.lock = threading.Lock()
+
+    @staticmethod
+    def _refs(arrays):
+        refs = []
+        for a in arrays:
+            if a is None:
+                refs.append(None)
+                continue
+            try:
+                refs.append(weakref.ref(a))
+            except TypeError:   # not weak-referenceable (a list, a scalar): never cached
+                return None
+        return refs
+
+    def get(self, arrays, scalars, build):
+        refs = self._refs(arrays)
+        if refs is None:
+            return build()
+        fps = [None if a is None else _fingerprint(a) for a in arrays]
+        with self.lock:
+            for k, (r, f, sc, asm) in enumerate(self.entries):
+                same = all((ri is None and a is None) or (ri is not None and ri() is a) for ri, a in zip(r, arrays))
+                if same and f == fps and sc == scalars:
+                    self.entries.insert(0, self.entries.pop(k))
+                    return asm
+        asm = build()
+        with self.lock:
+            self.entries.insert(0, (refs, fps, scalars, asm))
+            del self.entries[self.keep:]
+        return asm
+
+    def clear(self):
+        with self.lock:
+            self.entries = []
+
+
+_MESHES = _DeviceMeshCache()
+
+
+def release_device_meshes():
+    """Drops the device-resident meshes the drop-in callables keep between calls."""
+    _MESHES.clear()
+
+
 def _low_level_df(name, fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
     _check_formulation(formulation, material)
     mat_id, params = material_params(material, name)
     recompute = bool(fem_solver.recompute_sparsity_pattern)
     # CSR output with or without the reference's element-to-nonzero maps: the device scatter
     # finds every entry's position in the pattern itself (one row search per node pair), which
-    # lands each value where the maps would and spares uploading the two E*ndof^2 maps per call
+    # lands each value where the maps would and spares uploading the two E*ndof^2 maps
     mode = "triplet" if recompute else "squeeze"
     sparsity = None
     if not recompute:
         sparsity = (fem_solver.indices, fem_solver.indptr, None, None)
     orient = getattr(material, "anisotropic_orientations", None) if mat_id == N.FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1 \
         else None
-    asm = DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, name, params,
-                          mode=mode, requires_geometry_update=fem_solver.requires_geometry_update, sparsity=sparsity,
-                          orientations=orient)
+    update = int(fem_solver.requires_geometry_update)
+    arrays = [mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss, orient] + \
+        ([fem_solver.indices, fem_solver.indptr] if not recompute else [None, None])
+    asm = _MESHES.get(arrays, (name, tuple(params), mode, update, torch.cuda.current_device()),
+                      lambda: DeviceAssembler(mesh.points, mesh.elements, function_space.Jm, function_space.AllGauss,
+                                              name, params, mode=mode, requires_geometry_update=update,
+                                              sparsity=sparsity, orientations=orient))
     x = _to_dev(Eulerx, torch.float64, asm.device)
     out = asm.assemble(x)
     host = [_HOST.to_host(t) for t in out]
@@ -595,15 +695,18 @@ def fp32_peak_gflops():
     return g.value
 
 
-ARITHMETIC = {"fp64": N.FL_ARITH_FP64, "float_pair": N.FL_ARITH_FLOAT_PAIR, "tensor": N.FL_ARITH_TENSOR}
+ARITHMETIC = {"fp64": N.FL_ARITH_FP64, "float_pair": N.FL_ARITH_FLOAT_PAIR, "tensor": N.FL_ARITH_TENSOR,
+              "reference_tensor": N.FL_ARITH_REFERENCE_TENSOR}
 
 
 def set_arithmetic(name):
     """Arithmetic of the stiffness contraction for every later FP64 assembly in the process:
-    'float_pair' (the default: hi + lo float pairs on the FP32 pipe, ~1e-14 relative to FP64),
-    'fp64' (FP64 multiply-adds) or 'tensor' (tensor cores on operands split into six exact BF16
-    digits, ~1e-13; CSR outputs of supported element types, else float pairs). Kinematics,
-    material, residual and scatter are FP64 in all three."""
+    'float_pair' (hi + lo float pairs on the FP32 pipe, ~1e-14 relative to FP64), 'fp64' (FP64
+    multiply-adds), 'tensor' (tensor cores on the per-element operand U split into six exact BF16
+    digits, ~1e-13) or 'reference_tensor' (each tile of 14 elements as one tensor-core GEMM of the
+    pulled-back tangents against the element type's constant reference tensor, six BF16 digit
+    planes per operand, exact FP64 recombination, ~1e-14; CSR outputs of 4-, 8-, 10- and 20-node
+    elements with at most 15 Gauss points, else float pairs). The material law is FP64 in all."""
     N.check(N.lib().fl_SetAssemblyArithmetic(ARITHMETIC[name]), "fl_SetAssemblyArithmetic")
 
 

@@ -27,6 +27,7 @@
 #include <mutex>
 
 #include "fl_common.cuh"
+#include "fl_reftensor.cuh"
 #include "fl_tc.cuh"
 
 namespace fl {
@@ -70,6 +71,7 @@ struct AsmArgs {
     const float *npair;
     const float2 *jmp;
     int *flags;
+    const int32_t *boff;  // optional per-element block offsets [nelem][npe][npe] (fl_ElementBlockOffsets)
     double *Q;       // scratch [QSTRIDE][ldq]
     float *Qf;       // split-BF16 path: FP32 tangent part [45][ldq] (Q then holds S [9][ldq])
     int64_t e0, ne;  // element chunk [e0, e0+ne)
@@ -660,10 +662,103 @@ static int launch_oz(AsmArgs A, cudaStream_t stream);
 template <int NPE>
 static bool oz_supported(int nq);
 
+// FP64 tangent as tensor-core GEMMs against the reference tensor (fl_reftensor.cu): the Gauss-point
+// kernel writes the float-pair layout (float-pair kinematics) for a chunk of elements, the
+// contraction kernel reads it tile by tile. Scratch from the stream-ordered allocator: the chunk's
+// Gauss-point data (432 bytes per point, chunks of at most 512 MB), the float-pair kinematics
+// inputs, the reference tensor's digit planes and, unless the caller supplies them, the block
+// offsets of the pattern.
+constexpr size_t RT_CHUNK_BYTES = (size_t)512 << 20;
+
+// Freed stream-ordered memory is returned to the device at synchronisation points only above the
+// pool's release threshold (0 by default): a Newton or time loop that synchronises between
+// assembly calls would otherwise unmap and map its scratch again every call. Raised once per
+// device to `bytes` on the device's current pool (a setting of this process only).
+static void keep_pool_reserve(uint64_t bytes) {
+    static std::mutex m;
+    static bool done[256];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return;
+    std::lock_guard<std::mutex> g(m);
+    if (done[dev]) return;
+    done[dev] = true;
+    cudaMemPool_t pool;
+    if (cudaDeviceGetMemPool(&pool, dev) != cudaSuccess) return;
+    uint64_t cur = 0;
+    if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &cur) == cudaSuccess && cur < bytes)
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &bytes);
+}
+
+template <int NPE, int MAT>
+static int launch_rt(AsmArgs A, cudaStream_t stream) {
+    if (A.nelem == 0) return FL_OK;
+    int64_t chunk = std::max<int64_t>(1, (int64_t)(RT_CHUNK_BYTES / ((size_t)QSTRIDE * sizeof(double) * A.nq)));
+    if (chunk > A.nelem) chunk = A.nelem;
+    const size_t qbytes = ((size_t)QSTRIDE * sizeof(double) * A.nq * chunk + 255) & ~(size_t)255;
+    const size_t pbytes = (pair_prep_bytes(A.nnode, NPE, A.nq) + 255) & ~(size_t)255;
+    const size_t phibytes = rt_phi_bytes(NPE, A.nq);
+    const size_t obytes = A.boff ? 0 : ((sizeof(int32_t) * (size_t)NPE * NPE * A.nelem + 255) & ~(size_t)255);
+    keep_pool_reserve((uint64_t)2 << 30);
+    char *base = nullptr;
+    FL_CUDA_TRY(cudaMallocAsync((void **)&base, qbytes + pbytes + phibytes + obytes, stream));
+    int st = FL_OK;
+    do {
+        A.Q = reinterpret_cast<double *>(base);
+        A.ldq = chunk * A.nq;
+        A.Qf = reinterpret_cast<float *>(A.Q + (size_t)9 * A.ldq);
+        pair_prep(A, NPE, base + qbytes, stream);
+        void *phi = base + qbytes + pbytes;
+        if ((st = rt_build_phi(A.Jm, NPE, A.nq, phi, stream)) != FL_OK) break;
+        const int32_t *boff = A.boff;
+        if (!boff) {
+            int32_t *ob = reinterpret_cast<int32_t *>(base + qbytes + pbytes + phibytes);
+            if ((st = rt_block_offsets(A.elements, A.nelem, NPE, A.nnode, A.indptr, A.indices, ob, A.flags, stream)) !=
+                FL_OK)
+                break;
+            boff = ob;
+        }
+        RtArgs R;
+        R.Qh = A.Qf;
+        R.Ql = A.Qf + (size_t)45 * A.ldq;
+        R.S = A.Q;
+        R.ldq = A.ldq;
+        R.nq = A.nq;
+        R.update = A.update;
+        R.elements = A.elements;
+        R.nnode = A.nnode;
+        R.indptr = A.indptr;
+        R.indices = A.indices;
+        R.boff = boff;
+        R.jmp = A.jmp;
+        R.phi = phi;
+        R.phiexp = rt_phi_exponents(phi, NPE, A.nq);
+        R.V = A.V;
+        R.T = A.T;
+        R.flags = A.flags;
+        for (int64_t e0 = 0; e0 < A.nelem && st == FL_OK; e0 += chunk) {
+            A.e0 = e0;
+            A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
+            const int64_t nqp = A.ne * A.nq;
+            qp_kernel<NPE, MAT, QOUT_DF><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+            R.e0 = e0;
+            R.ne = A.ne;
+            st = rt_contract(R, NPE, stream);
+        }
+    } while (false);
+    if (st == FL_OK) st = launch_status();
+    const cudaError_t fe = cudaFreeAsync(base, stream);
+    if (st != FL_OK) return st;
+    return fe == cudaSuccess ? FL_OK : FL_ERR_CUDA;
+}
+
 template <int NPE, int MAT>
 static int launch_asm(AsmArgs A, double *scratch, size_t scratch_bytes, cudaStream_t stream) {
     constexpr int EPC = AsmCfg<NPE>::EPC;
     if (A.nelem == 0) return FL_OK;
+    // FP64 tangent as tensor-core GEMMs against the reference tensor: CSR output, its own
+    // scratch, element types it supports
+    if (g_arith.load() == FL_ARITH_REFERENCE_TENSOR && !scratch && A.mode != 0 && rt_supported(NPE, A.nq))
+        return launch_rt<NPE, MAT>(A, stream);
     // FP64 tangent on the tensor cores: CSR output, its own scratch, elements it supports
     if (g_arith.load() == FL_ARITH_TENSOR && !scratch && A.mode != 0 && oz_supported<NPE>(A.nq))
         return launch_oz<NPE, MAT>(A, stream);
@@ -706,7 +801,8 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
                        double *T, int recompute_sparsity_pattern, int squeeze_sparsity_pattern,
                        const int32_t *data_local_indices, const int32_t *data_global_indices, MatParams mp,
                        int *flags, double *scratch, size_t scratch_bytes, cudaStream_t stream,
-                       const double *eparams = nullptr, const double *orient = nullptr) {
+                       const double *eparams = nullptr, const double *orient = nullptr,
+                       const int32_t *boff = nullptr) {
     if (ndim != 3 || nvar != 3 || H_VoigtSize != 6) return FL_ERR_ARG;
     if (nelem < 0 || nnode <= 0) return FL_ERR_ARG;
     if (ngauss <= 0 || ngauss > 343) return FL_ERR_UNSUPPORTED;
@@ -741,6 +837,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.orient = mat == ANISOTROPICMR1 ? orient : nullptr;
     A.npair = nullptr;
     A.jmp = nullptr;
+    A.boff = boff;
     A.e0 = A.ne = A.ldq = 0;
     A.qc = 1;
     if (recompute_sparsity_pattern) {
@@ -1969,9 +2066,14 @@ int fl_GlobalAssemblyDF_noalloc(int material_number, FL_GLOBAL_ASSEMBLY_DF_ARGS)
     (void)sorter; (void)rho; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
     fl::MatParams mp;
     int mat = 0;
+    // the two materials of its contract (the others read further arrays a range-by-range caller
+    // would have to offset)
+    if (material_number != FL_MATERIAL_NEOHOOKEAN && material_number != FL_MATERIAL_MOONEYRIVLIN)
+        return FL_ERR_UNSUPPORTED;
     if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &mp, mu3) != FL_OK) return FL_ERR_UNSUPPORTED;
     if (ngauss <= 0 || ngauss > 343 || nelem < 0) return FL_ERR_ARG;
-    // the whole mesh must fit the array in one pass: nelem * ngauss Gauss points of 54 doubles
+    // the whole mesh must fit the array: nelem * ngauss Gauss points of 54 doubles (the kernels
+    // may still process it in more than one chunk of whole contraction tiles)
     if ((double)nelem * (double)ngauss * fl::QSTRIDE * sizeof(double) > (double)FL_NOALLOC_SCRATCH_BYTES)
         return FL_ERR_CAPACITY;
     if (nelem == 0) return FL_OK;
@@ -2008,6 +2110,7 @@ int fl_GlobalAssemblyDF_Mixed(int material_number, const double *points, const u
     A.nnode = nnode;
     A.nq = (int)ngauss;
     A.update = requires_geometry_update ? 1 : 0;
+    A.boff = nullptr;
     A.mode = 1;
     A.qc = 1;
     A.I = A.J = nullptr;
@@ -2062,7 +2165,8 @@ int fl_GlobalAssemblyDF_Batched(int material_number, const double *points, const
 }
 
 int fl_SetAssemblyArithmetic(int arithmetic) {
-    if (arithmetic != FL_ARITH_FP64 && arithmetic != FL_ARITH_FLOAT_PAIR && arithmetic != FL_ARITH_TENSOR)
+    if (arithmetic != FL_ARITH_FP64 && arithmetic != FL_ARITH_FLOAT_PAIR && arithmetic != FL_ARITH_TENSOR &&
+        arithmetic != FL_ARITH_REFERENCE_TENSOR)
         return FL_ERR_ARG;
     fl::g_arith.store(arithmetic);
     return FL_OK;
@@ -2146,6 +2250,19 @@ int fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_(FL_GLOBAL_ASSEMBLY_DF_ARGS) 
                                   V_stiff, T, recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
                                   data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream, nullptr,
                                   anisotropic_orientations);
+}
+
+int fl_GlobalAssemblyDF_Blocks(int material_number, const int32_t *block_offsets, FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+    (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
+    (void)sorter; (void)rho; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
+    fl::MatParams mp;
+    int mat = 0;
+    if (fl::material_of(material_number, mu, mu1, mu2, lamb, &mat, &mp, mu3) != FL_OK) return FL_ERR_UNSUPPORTED;
+    return fl::global_assembly_df(mat, points, elements, Eulerx, Jm, AllGauss, ndim, nvar, ngauss, nelem, nodeperelem,
+                                  nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
+                                  recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
+                                  data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream, nullptr,
+                                  anisotropic_orientations, block_offsets);
 }
 
 int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {

@@ -6,7 +6,6 @@
 
 #include "../../include/florence_gb300.h"
 
-#define FL_FLAG_BAD_INDEX 2 /* an element node id or a map entry is out of range; the entry was skipped */
 
 namespace fl {
 

@@ -56,8 +56,11 @@ __global__ void __launch_bounds__(128) tc_selftest_kernel(const __nv_bfloat16 *A
         tc::tmem_ld32(taddr + ((uint32_t)(32 * warp) << 16), v);
 #pragma unroll
         for (int j = 0; j < 32; ++j) D[(size_t)(32 * warp + lane) * TC_N + j] = v[j];
-    } else if (lane == 0) {
-        atomicOr(status, 1);
+    } else {
+        if (lane == 0) atomicOr(status, 1);
+        // the MMAs may still be writing the accumulator: wait once more (bounded) before the
+        // tensor memory is released
+        tc::mbar_wait(&mbar, 0, TC_WAIT_LIMIT);
     }
     tc::fence_before_sync();
     __syncthreads();

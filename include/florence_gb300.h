@@ -47,6 +47,8 @@ typedef struct CUstream_st *fl_stream_t;
 
 /* bits OR-ed into the optional device word `flags` by the assembly kernels */
 #define FL_FLAG_NONPOSITIVE_J 1 /* det F <= 0 at some Gauss point; results are still written */
+#define FL_FLAG_BAD_INDEX 2     /* an element node id or a map entry is out of range; the entry was skipped */
+#define FL_FLAG_TIMEOUT 4       /* a bounded wait inside a tensor-core kernel gave up; outputs incomplete */
 
 /* material numbers of the explicit entry point (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-109) */
 #define FL_MATERIAL_NEOHOOKEAN 1
@@ -170,7 +172,8 @@ int fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_(FL_GLOBAL_ASSEMBLY_DF_ARGS);
  * cudaFree or other allocating routine. The caller still passes every input and output.
  *
  * Same arguments and results as fl_GlobalAssemblyDF__NeoHookean_ / __MooneyRivlin_, preceded by
- * material_number (FL_MATERIAL_NEOHOOKEAN: mu, lamb; FL_MATERIAL_MOONEYRIVLIN: mu1, mu2, lamb).
+ * material_number (FL_MATERIAL_NEOHOOKEAN: mu, lamb; FL_MATERIAL_MOONEYRIVLIN: mu1, mu2, lamb; any
+ * other material number returns FL_ERR_UNSUPPORTED).
  * Limit: nelem * ngauss * 432 bytes (54 doubles per Gauss point) must fit in
  * FL_NOALLOC_SCRATCH_BYTES, e.g. up to 621 hex p=2 elements with 125 Gauss points or 5 548 tet
  * p=3 elements with 14; larger meshes return FL_ERR_CAPACITY without launching anything. Such a
@@ -249,8 +252,37 @@ int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
  * caller-provided scratch, for element types whose reduction fits (3 * 3 * ngauss * 2^14 < 2^24);
  * other calls use the float-pair contraction. */
 #define FL_ARITH_TENSOR 2
+/* FL_ARITH_REFERENCE_TENSOR: every element matrix of a tile of 14 elements as one tensor-core GEMM
+ * of the pulled-back tangents [(element, i, k) x (Gauss point, d, e)] against the element-type
+ * constant reference tensor Phi[(a, b) x (Gauss point, d, e)] = Jm[d][a][g] Jm[e][b][g] (node
+ * pairs a <= b), both operands split into six BF16 digit planes (21 plane products, five FP32
+ * tensor-memory accumulators, the leading four levels exact), recombined exactly into FP64 with
+ * integer instructions: element matrices within ~1e-14 of FP64. The kinematics and the tangent's
+ * pull-back run as float pairs, the material law in FP64, the residual as float pairs. Applies to
+ * CSR outputs (maps or squeeze) without a caller-provided scratch, for 4-, 8-, 10- and 20-node
+ * elements with at most 15 Gauss points; other calls use the float-pair contraction. */
+#define FL_ARITH_REFERENCE_TENSOR 3
 int fl_SetAssemblyArithmetic(int arithmetic);
 int fl_GetAssemblyArithmetic(void);
+
+/* Per-element block offsets of a node-blocked CSR pattern (no reference counterpart: the
+ * reference's element-to-nonzero maps, ComputeSparsityPattern.h:67-125, hold one position per
+ * element matrix entry; this holds one per node pair, 9x fewer): block_offsets[e][a][b]
+ * (nelem * nodeperelem^2 int32, device) = the offset of column 3 * elements[e][b] within row
+ * 3 * elements[e][a] when the 3x3 node block sits where a node-blocked CSR puts it (the node's three
+ * rows of equal length and consecutive, the block's entries at indptr[3 n] + i * rowlength +
+ * offset + k), else -1. Built once per mesh for fl_GlobalAssemblyDF_Blocks. flags: optional
+ * device int, FL_FLAG_BAD_INDEX for an out-of-range node id. No synchronisation. */
+int fl_ElementBlockOffsets(const uint64_t *elements, int64_t nelem, int64_t nodeperelem, int64_t nnode,
+                           const int32_t *indptr, const int32_t *indices, int32_t *block_offsets, int *flags,
+                           fl_stream_t stream);
+
+/* fl_GlobalAssemblyDF__<Mat>_ with the mesh's block offsets (fl_ElementBlockOffsets) supplied by a
+ * caller that keeps the mesh on the device between calls (no reference counterpart): in CSR mode
+ * with FL_ARITH_REFERENCE_TENSOR the contraction scatters through them instead of building them in
+ * the call. Same arguments and results otherwise, preceded by material_number (FL_MATERIAL_*) and
+ * block_offsets (may be NULL: then as fl_GlobalAssemblyDF__<Mat>_). */
+int fl_GlobalAssemblyDF_Blocks(int material_number, const int32_t *block_offsets, FL_GLOBAL_ASSEMBLY_DF_ARGS);
 
 /* Tiling of the split-BF16 tensor-core tangent (fl_GlobalAssemblyDF_Mixed; no reference
  * counterpart) for every later call of the process: tile_group = 128-row tiles of the element's

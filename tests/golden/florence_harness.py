@@ -1,14 +1,14 @@
 """Builds and imports the reference Florence package (pure-Python assembly path).
 
 Test infrastructure only: used to generate the golden fixtures in this folder.
-It runs in a container that has the reference checkout mounted read-only at
-``/root/reference``; it never runs on the GPU machine and nothing in the
-product imports it.
+It runs where a checkout of the reference is available (its root directory
+named by the environment variable ``FLORENCE_REFERENCE``); it never runs on the
+GPU machine and nothing in the product imports it.
 
 What it does (the reference cannot be built as shipped: its native element
 kernels need the third-party Fastor headers, CBLAS and x86 intrinsics):
 
-1. copies ``/root/reference/Florence`` to ``baseline/_ref/Florence`` (git-ignored);
+1. copies ``$FLORENCE_REFERENCE/Florence`` to ``baseline/_ref/Florence`` (git-ignored);
 2. compiles the ten Fastor-free Cython modules of the reference from their own
    sources (tensor helpers, Jacobi/Bernstein bases, geometric stiffness, Voigt
    B-matrix filler, sparse/RHS assembly helpers and ``ComputeSparsityPattern``);
@@ -25,7 +25,8 @@ import subprocess
 import sys
 import sysconfig
 
-REF_SRC = "/root/reference/Florence"
+REF_ROOT = os.environ.get("FLORENCE_REFERENCE", "")  # root of the read-only reference checkout
+REF_SRC = os.path.join(REF_ROOT, "Florence")
 REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 HARNESS_ROOT = os.path.join(REPO, "baseline", "_ref")
 PKG = os.path.join(HARNESS_ROOT, "Florence")
@@ -83,7 +84,7 @@ def _compile(pyx, incs, outdir, extra_cpp):
 def build():
     """Create the patched copy and compile what can be compiled (idempotent)."""
     if not os.path.isdir(REF_SRC) and not os.path.isdir(PKG):
-        raise RuntimeError("reference checkout not found at " + REF_SRC)
+        raise RuntimeError("reference checkout not found at %r (set FLORENCE_REFERENCE to its root)" % REF_SRC)
     if not os.path.isdir(PKG):
         os.makedirs(HARNESS_ROOT, exist_ok=True)
         shutil.copytree(REF_SRC, PKG)

@@ -1,10 +1,10 @@
 """Generates the golden fixtures in this folder from the reference Florence package.
 
-Test infrastructure only. Run in a container with the reference checkout at
-``/root/reference`` (it is not present on the GPU machine, which only reads the
+Test infrastructure only. Run where a checkout of the reference is available, its root
+named by ``FLORENCE_REFERENCE`` (it is not present on the GPU machine, which only reads the
 committed ``.npz`` files):
 
-    python tests/golden/make_golden.py
+    FLORENCE_REFERENCE=<reference checkout> python tests/golden/make_golden.py
 
 Every output is produced by the reference's own pure-numpy assembly path
 (``AssembleForm`` -> ``AssemblySmall`` -> ``DisplacementFormulation.GetLocalStiffness``,

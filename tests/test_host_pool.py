@@ -42,3 +42,32 @@ def test_idle_buffers_are_bounded_and_released():
     assert len(pool.slots) <= 2
     pool.release()
     assert len(pool.slots) == 0 or all(sl[1]() is not None for sl in pool.slots)
+
+
+def test_device_mesh_cache_reuses_only_identical_inputs():
+    """The drop-ins' device-mesh cache (host logic, a stand-in builder): the same array objects with
+    the same sampled content reuse the entry; a rewritten array, another object or other scalars
+    build anew; at most `keep` entries are held."""
+    from florence_gb300.assembly import _DeviceMeshCache
+    cache = _DeviceMeshCache(keep=2)
+    built = []
+
+    def build():
+        built.append(object())
+        return built[-1]
+
+    P = np.random.default_rng(0).random((1000, 3))
+    E = np.arange(4000, dtype=np.uint64).reshape(1000, 4)
+    a = cache.get([P, E, None], ("NeoHookean", 1), build)
+    assert cache.get([P, E, None], ("NeoHookean", 1), build) is a and len(built) == 1
+    assert cache.get([P, E, None], ("NeoHookean", 2), build) is not a          # other scalars
+    P2 = P.copy()
+    assert cache.get([P2, E, None], ("NeoHookean", 1), build) is not a         # another object
+    assert len(cache.entries) == 2
+    P[:] += 1.0                                                                # rewritten in place
+    n = len(built)
+    cache.get([P, E, None], ("NeoHookean", 1), build)
+    assert len(built) == n + 1
+    assert cache.get([[1.0], E, None], ("NeoHookean", 1), build) is built[-1] and len(built) == n + 2  # not cacheable
+    cache.clear()
+    assert cache.entries == []

@@ -4,10 +4,12 @@ Some callers cannot allocate device memory while they run (an application that r
 device memory at start-up, or a solver loop that must not stall on cudaMalloc/cudaFree, which can
 synchronise the device, or fail under memory pressure). For them the library keeps a fixed 32 MiB
 device array as the Gauss-point scratch of this one entry point. This test calls it through the C
-ABI, twice in a row (the array is reused and keeps the previous call's contents), and compares
-each result with the regular entry point's, within the parity tolerance of the other tests. It
-also checks that a mesh too large for the array is rejected. The file name makes pytest collect
-it last.
+ABI, twice in a row (the array is reused and keeps the previous call's contents), in each
+contraction arithmetic, and compares each result with the regular entry point's, within the parity
+tolerance of the other tests. It checks the entry point's defining property through the driver's
+high-water mark of the device's stream-ordered memory pool (the regular entry point raises it, this
+one must not), and that a mesh too large for the array is rejected. The file name makes pytest
+collect it last.
 """
 import ctypes
 
@@ -20,6 +22,28 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 TOL = 1e-12
+CU_MEMPOOL_ATTR_USED_MEM_HIGH = 8  # CUmemPool_attribute (cuda.h)
+
+
+class _PoolHighWater:
+    """High-water mark of the current memory pool of device 0 (the pool cudaMallocAsync draws
+    from), through the driver API: reset() zeroes it, value() reads it."""
+
+    def __init__(self):
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        dev = ctypes.c_int(0)
+        assert self.cu.cuDeviceGet(ctypes.byref(dev), torch.cuda.current_device()) == 0
+        self.pool = ctypes.c_void_p()
+        assert self.cu.cuDeviceGetMemPool(ctypes.byref(self.pool), dev) == 0
+
+    def reset(self):
+        zero = ctypes.c_uint64(0)
+        assert self.cu.cuMemPoolSetAttribute(self.pool, CU_MEMPOOL_ATTR_USED_MEM_HIGH, ctypes.byref(zero)) == 0
+
+    def value(self):
+        v = ctypes.c_uint64(0)
+        assert self.cu.cuMemPoolGetAttribute(self.pool, CU_MEMPOOL_ATTR_USED_MEM_HIGH, ctypes.byref(v)) == 0
+        return v.value
 
 
 def _p(t):
@@ -76,16 +100,31 @@ def _zero(b):
         b[k].zero_()
 
 
+@pytest.fixture
+def arithmetic():
+    """Yields a setter of the contraction arithmetic and restores the library's default after."""
+    import florence_gb300 as fl
+    old = fl.get_arithmetic()
+    yield fl.set_arithmetic
+    fl.set_arithmetic(old)
+
+
+@pytest.mark.parametrize("arith", ["float_pair", "fp64", "tensor"])
 @pytest.mark.parametrize("case,mode", [("hex_p2_nh_q5", "csr"), ("tet_p3_mr_jitter", "triplet")])
-def test_noalloc_matches_regular_entry_point_twice(case, mode):
+def test_noalloc_matches_regular_entry_point_twice(case, mode, arith, arithmetic):
     from florence_gb300 import _native as N
     L = N.lib()
+    arithmetic(arith)
     d = load_golden(case)
     mat = str(d["material"])
     mat_no = N.FL_MATERIAL_NEOHOOKEAN if mat == "NeoHookean" else N.FL_MATERIAL_MOONEYRIVLIN
     b = _buffers(d, mode)
+    pool = _PoolHighWater()
+    torch.cuda.synchronize()
+    pool.reset()
     assert _call(L, "fl_GlobalAssemblyDF__" + mat + "_", None, d, b, mode) == N.FL_OK
     torch.cuda.synchronize()
+    assert pool.value() > 0  # the regular entry point draws its scratch from the pool
     V_ref, T_ref = b["V"].cpu().numpy().copy(), b["T"].cpu().numpy().copy()
     I_ref, J_ref = b["I"].cpu().numpy().copy(), b["J"].cpu().numpy().copy()
     assert int(b["flags"].item()) == 0
@@ -94,8 +133,11 @@ def test_noalloc_matches_regular_entry_point_twice(case, mode):
         if mode == "triplet":
             b["I"].zero_()
             b["J"].zero_()
+        torch.cuda.synchronize()
+        pool.reset()
         assert _call(L, "fl_GlobalAssemblyDF_noalloc", mat_no, d, b, mode) == N.FL_OK, call
         torch.cuda.synchronize()
+        assert pool.value() == 0, call  # nothing drawn from the stream-ordered allocator
         assert int(b["flags"].item()) == 0
         assert rel_fro(b["V"].cpu().numpy(), V_ref) < TOL, call
         assert rel_fro(b["T"].cpu().numpy(), T_ref) < TOL, call
@@ -119,3 +161,14 @@ def test_noalloc_rejects_mesh_larger_than_its_array():
     assert st == N.FL_ERR_CAPACITY
     torch.cuda.synchronize()
     assert float(b["V"].abs().sum()) == 0.0 and float(b["T"].abs().sum()) == 0.0
+
+
+def test_noalloc_rejects_materials_outside_its_contract():
+    """Only neo-Hookean and Mooney-Rivlin: any other material number is FL_ERR_UNSUPPORTED."""
+    from florence_gb300 import _native as N
+    L = N.lib()
+    d = load_golden("hex_p2_nh_q5")
+    b = _buffers(d, "csr")
+    for mat_no in (N.FL_MATERIAL_LINEARELASTIC, N.FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN,
+                   N.FL_MATERIAL_ANISOTROPICMOONEYRIVLIN_1, 12345):
+        assert _call(L, "fl_GlobalAssemblyDF_noalloc", mat_no, d, b, "csr") == N.FL_ERR_UNSUPPORTED
