@@ -526,13 +526,18 @@ def run_newton(args):
     cells = (48, 12, 12) if args.workload != "beam_s" else (24, 6, 6)
     P, el, Jm, w, fixed, f = build_beam_problem(*cells, traction=0.01)
     asm = fl.DeviceAssembler(P, el, Jm, w, "MooneyRivlin", (0.5, 0.5, 20.0), mode="csr")
+    from florence_gb300 import meshes
+    g = np.load(os.path.join(GOLDEN, "tet_p3_mr_jitter.npz"))
+    pat = meshes.local_pattern(g["points"], g["elements"], 0, "tet")
     tangents = {"both": ["fp64", "mixed"], "all": ["fp64", "mixed", "hybrid"]}.get(args.tangent, [args.tangent])
     runs = {}
+    lin = dict(linear=args.linear, pattern=pat if args.linear == "pmg" else None)
     for tg in tangents:
         # warm-up: module loading, one assembly and one short linear solve
-        NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32, tangent=tg, spmv=args.spmv).solve()
+        NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32, tangent=tg, spmv=args.spmv,
+                     **lin).solve()
         runs[tg] = NewtonSolver(asm, fixed, f, n_increments=10, tol=1e-10, tangent=tg, spmv=args.spmv,
-                                max_iter=args.newton_max_iter, forcing=args.forcing).solve()
+                                max_iter=args.newton_max_iter, forcing=args.forcing, **lin).solve()
     out = runs[tangents[-1]]
     extra = {}
     if len(runs) > 1:
@@ -556,7 +561,7 @@ def run_newton(args):
                 value=out["wall_s"], unit="s", n_gpus=1, steps=1, warmup=1, higher_is_better=False,
                 scaling="weak", vs_baseline=None, dtype="f64", data="synthetic", tangent=args.tangent,
                 spmv=args.spmv if args.tangent != "mixed" else "fp32 values, float-pair product",
-                forcing=args.forcing,
+                forcing=args.forcing, linear=args.linear,
                 config=dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice), Mooney-Rivlin mu1=mu2=0.5 "
                                      "lambda=20, x=0 clamped, traction (0,0,-0.01) on x=4" % cells,
                             nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
@@ -1033,6 +1038,9 @@ def main():
                     help="PCG tolerance per Newton step: Eisenstat-Walker, or 0.1 x relative residual")
     ap.add_argument("--spmv", default="split", choices=["split", "fp64"],
                     help="PCG product for FP64 tangents: float-pair split on the FP32 pipe, or FP64")
+    ap.add_argument("--linear", default="pcg", choices=["pcg", "pmg"],
+                    help="Newton's linear step: block-Jacobi PCG, or flexible CG with the two-level p-multigrid "
+                         "cycle (FP64 tangent)")
     ap.add_argument("--pcg", action="store_true", help="PCG iterations on the beam's tangent instead")
     ap.add_argument("--pcg-iters", type=int, default=400)
     ap.add_argument("--batched", action="store_true", help="batched uneven instances instead")

@@ -115,6 +115,10 @@ def lib():
         L.fl_MLPGradients.argtypes = [P, P, P, I64, P, P, P, ctypes.c_size_t, P]
         L.fl_MLPAdamStep.argtypes = [P, P, P, P, I64, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                      P]
+        L.fl_NodalTransfer.argtypes = [I64, P, P, P, P, P, INT, P]
+        L.fl_MaskedMatVec.argtypes = [P, P, P, I64, P, P, P, P, P]
+        L.fl_BlockJacobiInverse.argtypes = [P, P, P, I64, P, P, P, P]
+        L.fl_BlockJacobiApply.argtypes = [I64, P, P, D, P, P, INT, P]
         L.fl_BlockJacobiPCG_workspace_size.argtypes = [I64, I64, INT]
         L.fl_BlockJacobiPCG_workspace_size.restype = ctypes.c_size_t
         L.fl_BlockJacobiPCG.argtypes = [P, P, P, INT, I64, P, P, P, D, I64, P, ctypes.c_size_t,
@@ -143,4 +147,5 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
            "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_AssembleExternalTractionForces", "fl_AssembleBodyForces", "fl_MLP_num_params", "fl_MLP_workspace_size",
-           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep"]
+           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec",
+           "fl_BlockJacobiInverse", "fl_BlockJacobiApply"]

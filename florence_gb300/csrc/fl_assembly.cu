@@ -205,8 +205,9 @@ struct QOutDF {
 
 // Gauss-point output layout: FP64 [54][ldq] in Q; FP32 tangent [45][ldq] in Qf with S [9][ldq]
 // in Q; the tangent formed in float-pair arithmetic (hi [45][ldq] then lo [45][ldq]) in Qf with
-// S [9][ldq] in Q
-enum { QOUT_F64 = 0, QOUT_F32 = 1, QOUT_DF = 2 };
+// S [9][ldq] in Q; the float-pair tangent with S as float pairs too (Sh [9][ldq], Sl [9][ldq] floats
+// in S's 72 bytes per point) for the reference-tensor contraction
+enum { QOUT_F64 = 0, QOUT_F32 = 1, QOUT_DF = 2, QOUT_RT = 3 };
 
 // QOUT: layout of the Gauss-point data (QOUT_F64 for the FP64 contraction, QOUT_F32 for the
 // split-BF16 Jacobian, QOUT_DF for the float-pair and tensor-core contractions); the kinematics,
@@ -265,12 +266,21 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-                qs[(i * 3 + d) * ld] =
+            for (int d = 0; d < 3; ++d) {
+                const double sv =
                     detJ * fma(sig[s6(i, 0)], G[0 * 3 + d], fma(sig[s6(i, 1)], G[1 * 3 + d], sig[s6(i, 2)] * G[2 * 3 + d]));
+                if constexpr (QOUT == QOUT_RT) {
+                    const FloatPair sp(sv);
+                    float *sf = reinterpret_cast<float *>(A.Q) + t;
+                    sf[(i * 3 + d) * ld] = sp.h;
+                    sf[(9 + i * 3 + d) * ld] = sp.l;
+                } else {
+                    qs[(i * 3 + d) * ld] = sv;
+                }
+            }
         if constexpr (QOUT == QOUT_F32)
             pulled_back_tangent<float, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF32{A.Qf + t, ld});
-        else if constexpr (QOUT == QOUT_DF)
+        else if constexpr (QOUT == QOUT_DF || QOUT == QOUT_RT)
             pulled_back_tangent<FloatPair, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutDF{A.Qf + t, A.Qf + 45 * ld + t, ld});
         else
             pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF64{q, ld});
@@ -694,7 +704,9 @@ static int launch_rt(AsmArgs A, cudaStream_t stream) {
     if (A.nelem == 0) return FL_OK;
     int64_t chunk = std::max<int64_t>(1, (int64_t)(RT_CHUNK_BYTES / ((size_t)QSTRIDE * sizeof(double) * A.nq)));
     if (chunk > A.nelem) chunk = A.nelem;
-    const size_t qbytes = ((size_t)QSTRIDE * sizeof(double) * A.nq * chunk + 255) & ~(size_t)255;
+    // the contraction stages the Gauss-point data with 16-byte loads: rows of a multiple of 4 floats
+    const int64_t ldq = (chunk * A.nq + 3) / 4 * 4;
+    const size_t qbytes = ((size_t)QSTRIDE * sizeof(double) * ldq + 255) & ~(size_t)255;
     const size_t pbytes = (pair_prep_bytes(A.nnode, NPE, A.nq) + 255) & ~(size_t)255;
     const size_t phibytes = rt_phi_bytes(NPE, A.nq);
     const size_t obytes = A.boff ? 0 : ((sizeof(int32_t) * (size_t)NPE * NPE * A.nelem + 255) & ~(size_t)255);
@@ -704,9 +716,14 @@ static int launch_rt(AsmArgs A, cudaStream_t stream) {
     int st = FL_OK;
     do {
         A.Q = reinterpret_cast<double *>(base);
-        A.ldq = chunk * A.nq;
+        A.ldq = ldq;
         A.Qf = reinterpret_cast<float *>(A.Q + (size_t)9 * A.ldq);
         pair_prep(A, NPE, base + qbytes, stream);
+        // FP64 kinematics: float-pair coordinate sums lose ~2^-46 of sum |Jm X| to cancellation,
+        // which the inverse Jacobian of a sliver element amplifies past the FP64 bar (measured
+        // 1.8e-11 against 6.4e-13 on the Delaunay beam); the float-pair shape-function gradients
+        // still serve the residual
+        A.npair = nullptr;
         void *phi = base + qbytes + pbytes;
         if ((st = rt_build_phi(A.Jm, NPE, A.nq, phi, stream)) != FL_OK) break;
         const int32_t *boff = A.boff;
@@ -720,7 +737,7 @@ static int launch_rt(AsmArgs A, cudaStream_t stream) {
         RtArgs R;
         R.Qh = A.Qf;
         R.Ql = A.Qf + (size_t)45 * A.ldq;
-        R.S = A.Q;
+        R.Sp = reinterpret_cast<const float *>(A.Q);
         R.ldq = A.ldq;
         R.nq = A.nq;
         R.update = A.update;
@@ -739,7 +756,7 @@ static int launch_rt(AsmArgs A, cudaStream_t stream) {
             A.e0 = e0;
             A.ne = A.nelem - e0 < chunk ? A.nelem - e0 : chunk;
             const int64_t nqp = A.ne * A.nq;
-            qp_kernel<NPE, MAT, QOUT_DF><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
+            qp_kernel<NPE, MAT, QOUT_RT><<<(unsigned)((nqp + QP_THREADS - 1) / QP_THREADS), QP_THREADS, 0, stream>>>(A);
             R.e0 = e0;
             R.ne = A.ne;
             st = rt_contract(R, NPE, stream);

@@ -61,6 +61,8 @@ constexpr int RT_NPROD = 256;             // producer threads
 constexpr int RT_THREADS = 128 + RT_NPROD + 32;
 constexpr int RT_MAX_NQ = 15;             // the tile's Gauss-point data must fit in shared memory
 constexpr long long RT_WAIT_LIMIT = 1ll << 23;
+constexpr int RT_MAXCOLS = 256;           // pair columns of the largest element type taken (20 nodes: 240)
+constexpr int RT_MAXK = 16 * 9;           // K columns for up to 15 Gauss points (135, padded to 144)
 
 // ------------------------------------------------------------------------------------------------
 // device pieces: barriers, bulk copies, tensor-memory loads
@@ -89,13 +91,30 @@ __device__ __forceinline__ bool mbar_test(uint64_t *mbar, uint32_t parity) {
     return done != 0;
 }
 
-// bounded wait; gives up (and raises the CTA's abort flag) after RT_WAIT_LIMIT polls, or at once
-// when another role has aborted
+// phase `parity` of the mbarrier complete, waiting in hardware (the thread is suspended until the
+// phase completes or about `ns` nanoseconds pass, so waiting warps take no issue slots)
+__device__ __forceinline__ bool mbar_try(uint64_t *mbar, uint32_t parity, uint32_t ns) {
+    uint32_t done;
+    asm volatile(
+        "{\n"
+        ".reg .pred p;\n"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        "selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(done)
+        : "r"(saddr(mbar)), "r"(parity), "r"(ns)
+        : "memory");
+    return done != 0;
+}
+
+// bounded wait; gives up (and raises the CTA's abort flag) after RT_WAIT_TRIES suspensions of up
+// to 100 microseconds (well under a second in all), or at once when another role has aborted
+constexpr int RT_WAIT_TRIES = 4000;
 __device__ __forceinline__ bool rt_wait(uint64_t *mbar, uint32_t parity, volatile int *abort_flag) {
-    for (long long i = 0; i < RT_WAIT_LIMIT; ++i) {
-        if (mbar_test(mbar, parity)) return true;
+    if (mbar_test(mbar, parity)) return true;
+    for (int i = 0; i < RT_WAIT_TRIES; ++i) {
+        if (mbar_try(mbar, parity, 100000u)) return true;
         if (*abort_flag) return false;
-        if (i > 64) __nanosleep(32);
     }
     *abort_flag = 1;
     return false;
@@ -138,11 +157,16 @@ struct RtTables {
 template <int NPE>
 __host__ __device__ constexpr size_t rt_tables_bytes() { return (sizeof(RtTables<NPE>) + 127) / 128 * 128; }
 
+// shared memory: stages | the tile's Gauss-point data (tangent hi [45][TQ], lo [45][TQ], residual
+// factor hi [9][TQ], lo [9][TQ]; TQ = 14 nq) | tables x 2 | column exponents | row scales | Jm pairs
+__host__ __device__ inline size_t rt_tile_bytes(int nq) {
+    return ((size_t)(2 * 45 + 2 * 9) * RT_EPT * nq * sizeof(float) + 127) / 128 * 128;
+}
 template <int NPE>
 __host__ __device__ inline size_t rt_smem_bytes(int nq) {
-    const size_t tile = (size_t)2 * 45 * RT_EPT * nq * sizeof(float);
-    return (size_t)RT_NST * RT_STAGE + (tile + 127) / 128 * 128 + 2 * rt_tables_bytes<NPE>() +
-           (size_t)rt_chunks(NPE) * RT_NB * sizeof(int) + RT_M * sizeof(float) + 256;
+    return (size_t)RT_NST * RT_STAGE + rt_tile_bytes(nq) + 2 * rt_tables_bytes<NPE>() +
+           (size_t)rt_chunks(NPE) * RT_NB * sizeof(int) + RT_M * sizeof(float) +
+           ((size_t)3 * NPE * nq * sizeof(float2) + 127) / 128 * 128 + 256;
 }
 
 // CSR position of entry (3 nr + ri, 3 nc + ci) by binary search in the row, -1 if absent
@@ -166,21 +190,28 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
     unsigned char *stages = smem;
     float *AH = reinterpret_cast<float *>(smem + (size_t)RT_NST * RT_STAGE);
     float *AL = AH + 45 * TQ;
-    const size_t tile_bytes = ((size_t)2 * 45 * TQ * sizeof(float) + 127) / 128 * 128;
-    RtTables<NPE> *tables = reinterpret_cast<RtTables<NPE> *>(smem + (size_t)RT_NST * RT_STAGE + tile_bytes);
+    float *SH = AL + 45 * TQ;  // residual factor S_g[i][d] of the tile, hi [9][TQ] then lo [9][TQ]
+    float *SL = SH + 9 * TQ;
+    RtTables<NPE> *tables = reinterpret_cast<RtTables<NPE> *>(smem + (size_t)RT_NST * RT_STAGE + rt_tile_bytes(nq));
     int *colexp = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(tables) + 2 * rt_tables_bytes<NPE>());
     float *rsc = reinterpret_cast<float *>(colexp + NCH * RT_NB);
+    float2 *jms = reinterpret_cast<float2 *>(rsc + RT_M);  // Jm as float pairs [3][NPE][nq]
 
     // fullA: the 8 producer warps wrote a stage's A planes; fullB: its Phi planes arrived (bulk
     // copy bytes); empty: the MMAs reading the stage completed; accf / acce: a chunk's
     // accumulators are complete / were read out; tblf / tble: a tile's tables are written / no
     // longer needed; fin: every MMA issued has completed
     __shared__ __align__(8) uint64_t fullA[RT_NST], fullB[RT_NST], empty_bar[RT_NST], accf_bar, acce_bar,
-        tblf_bar[2], tble_bar[2], fin_bar;
+        tblf_bar[2], tble_bar[2], rdone_bar, fin_bar;
     __shared__ uint32_t taddr_s;
     __shared__ volatile int s_abort;
     __shared__ int s_flag;
     __shared__ int64_t s_nnz;
+    // index tables: node pair (a, b) of each pair column; Gauss point and (d, e) of each K column;
+    // per row (el, i, k) the offset of its tangent entries (3i + d, 3k + e) in the tile data
+    __shared__ int8_t pair_a[RT_MAXCOLS], pair_b[RT_MAXCOLS];
+    __shared__ uint8_t k_g[RT_MAXK], k_de[RT_MAXK];
+    __shared__ int16_t row_off[RT_M][9];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int64_t ntiles = (R.ne + RT_EPT - 1) / RT_EPT;
@@ -199,12 +230,29 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
             tc::mbar_init(&tblf_bar[b], 8);
             tc::mbar_init(&tble_bar[b], 4);
         }
+        tc::mbar_init(&rdone_bar, 4);  // the epilogue warps read the tile's residual factors
         tc::mbar_init(&fin_bar, 1);
         s_abort = 0;
         s_flag = 0;
         s_nnz = (int64_t)R.indptr[3 * R.nnode];
     }
-    for (int n = tid; n < NCH * RT_NB; n += RT_THREADS) colexp[n] = R.phiexp[n];
+    for (int n = tid; n < NCH * RT_NB; n += RT_THREADS) {
+        colexp[n] = R.phiexp[n];
+        int a = 0, b = 0;
+        if (n < P) rt_pair(n, a, b);
+        pair_a[n] = (int8_t)a;
+        pair_b[n] = (int8_t)b;
+    }
+    for (int kk = tid; kk < NKS * 16; kk += RT_THREADS) {
+        k_g[kk] = (uint8_t)(kk < K ? kk / 9 : 0);
+        k_de[kk] = (uint8_t)(kk < K ? kk % 9 : 0);
+    }
+    if (tid < RT_M) {
+        const int el = tid / 9, i = (tid % 9) / 3, k = tid % 3;
+        for (int de = 0; de < 9; ++de)
+            row_off[tid][de] = (int16_t)(tid < 9 * RT_EPT ? rt_sym9(3 * i + de / 3, 3 * k + de % 3) * TQ + el * nq : 0);
+    }
+    for (int n = tid; n < 3 * NPE * nq; n += RT_THREADS) jms[n] = R.jmp[n];
     if (warp == 12) tc::tmem_alloc(&taddr_s, RT_TMEM_COLS);
     tc::fence_before_sync();
     __syncthreads();
@@ -245,56 +293,64 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                 if (e < R.ne) v = R.boff[(R.e0 + e) * (NPE * NPE) + idx % (NPE * NPE)];
                 tb.boff[idx] = (int16_t)(v >= 0 && v < 32768 ? v : -1);
             }
+            // the tile data are overwritten once the epilogue has formed the previous tile's residual
+            if (it >= 1 && !rt_wait(&rdone_bar, (uint32_t)((it - 1) & 1), &s_abort)) break;
             producers_sync();  // every producer is past the previous tile's K steps
-            for (int idx = p; idx < 45 * TQ; idx += RT_NPROD) {
-                const int k = idx / TQ, c = idx % TQ;
-                const int64_t col = el0 * nq + c;
-                float h = 0.f, l = 0.f;
-                if (col < R.ne * nq) {
-                    h = R.Qh[(size_t)k * R.ldq + col];
-                    l = R.Ql[(size_t)k * R.ldq + col];
+            {
+                // the tile's Gauss-point data: 108 rows (tangent hi, lo; residual factor hi, lo) of
+                // TQ floats, with 16-byte loads where the rows allow them
+                const int64_t c0 = el0 * nq, cend = R.ne * nq;
+                auto row_src = [&](int row) -> const float * {
+                    return row < 45 ? R.Qh + (size_t)row * R.ldq
+                           : row < 90 ? R.Ql + (size_t)(row - 45) * R.ldq
+                                      : R.Sp + (size_t)(row - 90) * R.ldq;
+                };
+                if ((TQ & 3) == 0) {
+                    const int q4 = TQ / 4;
+                    for (int idx = p; idx < 108 * q4; idx += RT_NPROD) {
+                        const int row = idx / q4, c = 4 * (idx % q4);
+                        const float *src = row_src(row);
+                        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (c0 + c + 3 < cend) {
+                            v = __ldg(reinterpret_cast<const float4 *>(src + c0 + c));
+                        } else {
+                            if (c0 + c < cend) v.x = src[c0 + c];
+                            if (c0 + c + 1 < cend) v.y = src[c0 + c + 1];
+                            if (c0 + c + 2 < cend) v.z = src[c0 + c + 2];
+                        }
+                        *reinterpret_cast<float4 *>(AH + (size_t)row * TQ + c) = v;
+                    }
+                } else {
+                    for (int idx = p; idx < 108 * TQ; idx += RT_NPROD) {
+                        const int row = idx / TQ, c = idx % TQ;
+                        AH[idx] = c0 + c < cend ? row_src(row)[c0 + c] : 0.f;
+                    }
                 }
-                AH[idx] = h;
-                AL[idx] = l;
             }
             producers_sync();
-            if (p < RT_M) {  // row scale from the largest |hi| of the row over (g, d, e)
-                const int r = p, el = r / 9, i = (r % 9) / 3, k = r % 3;
+            {   // row scales: the largest |hi| of each row over (g, d, e), two threads per row
+                const int r = p >> 1, half = p & 1;
                 float mx = 0.f;
                 if (r < 9 * RT_EPT)
-                    for (int d = 0; d < 3; ++d)
-                        for (int e2 = 0; e2 < 3; ++e2) {
-                            const float *src = AH + rt_sym9(3 * i + d, 3 * k + e2) * TQ + el * nq;
-                            for (int g = 0; g < nq; ++g) mx = fmaxf(mx, fabsf(src[g]));
-                        }
-                int E;
-                float sc;
-                rt_row_scale(mx, E, sc);
-                tb.rexp[r] = E;
-                rsc[r] = sc;
-            }
-            if (R.update) {  // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d], float pairs
-                for (int idx = p; idx < RT_EPT * NPE * 3; idx += RT_NPROD) {
-                    const int el = idx / (NPE * 3), a = (idx % (NPE * 3)) / 3, i = idx % 3;
-                    const int node = tb.nodes[el * NPE + a];
-                    if (el0 + el >= R.ne || node < 0) continue;
-                    FloatPair t(0.f, 0.f);
-                    const size_t col = (size_t)(el0 + el) * nq;
-                    for (int g = 0; g < nq; ++g)
-#pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            const float2 j = __ldg(R.jmp + ((size_t)d * NPE + a) * nq + g);
-                            const FloatPair sv(__ldg(R.S + (size_t)(i * 3 + d) * R.ldq + col + g));
-                            t = fma(FloatPair(j.x, j.y), sv, t);
-                        }
-                    atomicAdd(R.T + 3 * (int64_t)node + i, to_double(t));
+                    for (int de = half ? 5 : 0; de < (half ? 9 : 5); ++de) {
+                        const float *src = AH + row_off[r][de];
+#pragma unroll 2
+                        for (int g = 0; g < nq; ++g) mx = fmaxf(mx, fabsf(src[g]));
+                    }
+                mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+                if (half == 0) {
+                    int E;
+                    float sc;
+                    rt_row_scale(mx, E, sc);
+                    tb.rexp[r] = E;
+                    rsc[r] = sc;
                 }
             }
             producers_sync();  // row scales visible to every producer
             if (lane == 0) mbar_arrive(&tblf_bar[buf]);
             // A planes, chunk by chunk (the same planes for every chunk of the tile)
             const int r = p & (RT_M - 1), kg = p >> 7;
-            const int el = r / 9, i = (r % 9) / 3, k = r % 3;
+            const int el = r / 9;
             const bool rowok = r < 9 * RT_EPT && el0 + el < R.ne;
             const float sc = rowok ? rsc[r] : 0.f;
             for (int c = 0; c < NCH && !s_abort; ++c)
@@ -308,8 +364,7 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                         const int kk = 16 * j + 8 * kg + q;
                         float h = 0.f, l = 0.f;
                         if (rowok && kk < K) {
-                            const int g = kk / 9, de = kk % 9;
-                            const int src = rt_sym9(3 * i + de / 3, 3 * k + de % 3) * TQ + el * nq + g;
+                            const int src = row_off[r][k_de[kk]] + k_g[kk];
                             h = AH[src];
                             l = AL[src];
                         }
@@ -395,6 +450,24 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
             const int buf = (int)(it & 1);
             const RtTables<NPE> &tb = tables[buf];
             if (!rt_wait(&tblf_bar[buf], (uint32_t)((it >> 1) & 1), &s_abort)) break;
+            if (R.update) {  // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d] in float pairs
+                for (int idx = tid; idx < RT_EPT * NPE * 3; idx += 128) {
+                    const int re = idx / (NPE * 3), a = (idx % (NPE * 3)) / 3, ri = idx % 3;
+                    const int node = tb.nodes[re * NPE + a];
+                    if (tile * RT_EPT + re >= R.ne || node < 0) continue;
+                    FloatPair t(0.f, 0.f);
+                    for (int g = 0; g < nq; ++g)
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            const float2 j = jms[(d * NPE + a) * nq + g];
+                            const int o = (ri * 3 + d) * TQ + re * nq + g;
+                            t = fma(FloatPair(j.x, j.y), FloatPair(SH[o], SL[o]), t);
+                        }
+                    atomicAdd(R.T + 3 * (int64_t)node + ri, to_double(t));
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&rdone_bar);
             const bool rv = r < 9 * RT_EPT && tile * RT_EPT + el < R.ne;
             const int Er = tb.rexp[r];
             bool ok = true;
@@ -422,8 +495,7 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                     for (int jj = 0; jj < 16; ++jj) {
                         const int n = c * RT_NB + cg * 16 + jj;
                         if (n >= P) continue;
-                        int a, b;
-                        rt_pair(n, a, b);
+                        const int a = pair_a[n], b = pair_b[n];
                         const int na = tb.nodes[el * NPE + a], nb = tb.nodes[el * NPE + b];
                         if (na < 0 || nb < 0) continue;
                         const double val = rt_combine(__uint_as_float(v[0][jj]), __uint_as_float(v[1][jj]),

@@ -9,12 +9,13 @@
 
 namespace fl {
 
-// One chunk of elements whose Gauss-point data the Gauss-point kernel wrote in the float-pair
-// layout: residual factor S [9][ldq] (FP64) and the pulled-back tangent hi [45][ldq], lo [45][ldq]
-// (floats), column (e - e0) * nq + g for element e of the chunk and Gauss point g.
+// One chunk of elements whose Gauss-point data the Gauss-point kernel wrote as float pairs: the
+// residual factor S (hi [9][ldq] then lo [9][ldq]) and the pulled-back tangent hi [45][ldq], lo
+// [45][ldq], column (e - e0) * nq + g for element e of the chunk and Gauss point g; ldq a multiple of
+// 4 and every array 16-byte aligned (the contraction stages them with 16-byte loads).
 struct RtArgs {
     const float *Qh, *Ql;
-    const double *S;
+    const float *Sp;
     int64_t ldq;
     int64_t e0, ne;            // the chunk: mesh elements [e0, e0 + ne)
     int nq, update;            // update: form the residual (requires_geometry_update)

@@ -66,7 +66,7 @@ class NewtonSolver:
 
     def __init__(self, asm, fixed, f_ext, n_increments=10, tol=1e-10, max_iter=25, pcg_maxiter=50000,
                  eta_max=1e-2, eta_min=1e-12, tangent="fp64", criterion="reference", spmv="split",
-                 forcing="ew", eta0=1e-3, hybrid_switch=1e-2):
+                 forcing="ew", eta0=1e-3, hybrid_switch=1e-2, linear="pcg", pattern=None):
         if asm.mode != "csr":
             raise ValueError("Newton needs the CSR tangent (mode='csr')")
         self.asm = asm
@@ -113,6 +113,17 @@ class NewtonSolver:
         self.eta0 = eta0
         self.ws = pcg_workspace(asm, self.V, spmv)   # the FP64 workspace is the larger one
         self.history = []
+        # linear step: "pcg" (block-Jacobi PCG, fl_BlockJacobiPCG) or "pmg" (flexible CG with the
+        # two-level p-multigrid cycle of multigrid.PMultigrid; FP64 tangent, high-order tets,
+        # `pattern` = the element's barycentric node layout)
+        if linear not in ("pcg", "pmg"):
+            raise ValueError("linear must be 'pcg' or 'pmg'")
+        self.mg = None
+        if linear == "pmg":
+            if tangent != "fp64" or pattern is None:
+                raise ValueError("the p-multigrid linear step takes the FP64 tangent and the element's node pattern")
+            from .multigrid import PMultigrid
+            self.mg = PMultigrid(asm, pattern, np.asarray(fixed, dtype=np.int8))
 
     def _assemble(self, u, mixed=None):
         """Tangent and residual at u; mixed selects the FP32 tensor-core Jacobian (default: as
@@ -153,8 +164,13 @@ class NewtonSolver:
         failed = False
         while True:
             self._set_jacobian(u, r_before, norm_load)
-            du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
-                                 workspace=self.ws, spmv=self.spmv)
+            if self.mg is not None:
+                from .multigrid import fcg
+                self.mg.update(self.V, u)
+                du, pits, prel = fcg(self.mg, -R, rtol=eta, maxiter=self.pcg_maxiter)
+            else:
+                du, pits, prel = pcg(self.asm, self.V, -R, self.fixed, rtol=eta, maxiter=self.pcg_maxiter,
+                                     workspace=self.ws, spmv=self.spmv)
             pcg_total += pits
             u += du
             self._assemble(u)

@@ -427,6 +427,30 @@ int fl_StrainEnergy(const double *points, const uint64_t *elements, const double
 #define FL_PCG_F64 64
 #define FL_PCG_F32 32
 #define FL_PCG_F64_SPLIT 6432
+/* ------------------------------------------------------------------------------------------
+ * Pieces of the two-level p-multigrid preconditioner of Newton's linear step on high-order
+ * tetrahedra (florence_gb300/multigrid.py). No reference counterpart: the reference solves the
+ * reduced system with a direct or a scipy iterative solver (Solver/LinearSolver.py:153-330).
+ * All pointers are device pointers; nothing synchronises.
+ *
+ * fl_NodalTransfer: y[3r + i] (=, or += with accumulate) sum_{k = ptr[r]}^{ptr[r+1]-1} w[k]
+ *   x[3 cols[k] + i] for the nrows node rows (a prolongation from vertex values to the nodes of
+ *   the high-order elements, or its transpose, the restriction).
+ * fl_MaskedMatVec: y = K_ff x on the rows of an FP64 CSR matrix, rows and columns of fixed dofs
+ *   (fixed[dof] != 0) masked; with b non-NULL y = b - K_ff x instead (y = 0 on fixed rows).
+ * fl_BlockJacobiInverse: Binv[n][9] = inverse of each node's 3x3 diagonal block, fixed rows and
+ *   columns replaced by the identity (FL_FLAG_BAD_INDEX in flags for a missing or singular block).
+ * fl_BlockJacobiApply: z (=, or +=) omega Binv r per node, 0 on fixed dofs.
+ * ------------------------------------------------------------------------------------------ */
+int fl_NodalTransfer(int64_t nrows, const int32_t *ptr, const int32_t *cols, const double *weights, const double *x,
+                     double *y, int accumulate, fl_stream_t stream);
+int fl_MaskedMatVec(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
+                    const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
+int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nnode,
+                          const int8_t *fixed, double *Binv, int *flags, fl_stream_t stream);
+int fl_BlockJacobiApply(int64_t nnode, const double *Binv, const int8_t *fixed, double omega, const double *r,
+                        double *z, int accumulate, fl_stream_t stream);
+
 size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows, int64_t nnz, int value_bits);
 int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const void *values, int value_bits,
                       int64_t nrows, const int8_t *fixed, const double *b, double *x, double rtol, int64_t maxiter,
