@@ -26,9 +26,10 @@
 // value exactly rounded, with integer instructions only (GB300's FP64 pipe is 1/64 of FP32).
 //
 // Work split (one persistent CTA per SM, 416 threads):
-//   warps 0-3   epilogue: tensor memory -> FP64 entries -> atomic adds into the CSR values
+//   warps 0-3   epilogue: per tile the residual (float pairs, atomic adds); per chunk tensor
+//               memory -> FP64 entries -> atomic adds into the CSR values
 //   warps 4-11  producers: per tile the node tables, block offsets, the tile's Gauss-point data and
-//               row scales, the residual (float pairs); per 16-wide K step the six A planes
+//               row scales; per 16-wide K step the seven A planes
 //   warp 12     one thread: bulk copies of the Phi planes (cp.async.bulk) and the 28 MMAs per step
 // A tile is 14 elements (126 of the 128 MMA rows); the 210 node pairs of a 20-node tet run as
 // three 80-column chunks (five accumulators of 80 columns fit the 512 tensor-memory columns),
