@@ -566,7 +566,8 @@ def run_newton(args):
                                      "lambda=20, x=0 clamped, traction (0,0,-0.01) on x=4" % cells,
                             nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
                 newton_iters=out["newton_iters"], pcg_iters=out["pcg_iters"], failed=out["failed"],
-                tip_uz=float(u[tip, 2].mean()), increments=incs, **extra)
+                tip_uz=float(u[tip, 2].mean()), increments=incs,
+                **{k: out[k] for k in ("mg_cycles", "mg_coarse_iters") if k in out}, **extra)
     print(json.dumps(line), flush=True)
 
 
@@ -1017,10 +1018,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="beam", choices=["beam", "beam_s", "cube"])
-    ap.add_argument("--arith", default="float_pair",
+    ap.add_argument("--arith", default="reference_tensor",
                     choices=["fp64", "float_pair", "tensor", "reference_tensor", "mixed"],
-                    help="arithmetic of the stiffness contraction (FP64, float pairs on the FP32 pipe, or the "
-                         "split-BF16 tensor-core tangent with FP32 values)")
+                    help="arithmetic of the stiffness contraction (the default: FP64 tangent as tensor-core GEMMs "
+                         "against the reference tensor; FP64, float pairs on the FP32 pipe, the per-element digit "
+                         "split, or the split-BF16 tensor-core tangent with FP32 values)")
     ap.add_argument("--tc-tiling", default="0,0",
                     help="tile group and reduction chunk of the split-BF16 kernel (0,0 = automatic)")
     ap.add_argument("--no-cpu", action="store_true")

@@ -18,6 +18,7 @@ FL_ERR_CAPACITY = 5
 FL_FLAG_NONPOSITIVE_J = 1
 FL_FLAG_BAD_INDEX = 2
 FL_FLAG_TIMEOUT = 4
+FL_FLAG_PAIR_RANGE = 8
 FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
 FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN = 3
@@ -119,6 +120,9 @@ def lib():
         L.fl_MaskedMatVec.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_BlockJacobiInverse.argtypes = [P, P, P, I64, P, P, P, P]
         L.fl_BlockJacobiApply.argtypes = [I64, P, P, D, P, P, INT, P]
+        L.fl_CoarsePCG_workspace_size.argtypes = [I64]
+        L.fl_CoarsePCG_workspace_size.restype = ctypes.c_size_t
+        L.fl_CoarsePCG.argtypes = [P, P, P, I64, P, P, P, P, D, I64, P, ctypes.c_size_t, P, P, P, P]
         L.fl_BlockJacobiPCG_workspace_size.argtypes = [I64, I64, INT]
         L.fl_BlockJacobiPCG_workspace_size.restype = ctypes.c_size_t
         L.fl_BlockJacobiPCG.argtypes = [P, P, P, INT, I64, P, P, P, D, I64, P, ctypes.c_size_t,
@@ -148,4 +152,4 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
            "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_AssembleExternalTractionForces", "fl_AssembleBodyForces", "fl_MLP_num_params", "fl_MLP_workspace_size",
            "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec",
-           "fl_BlockJacobiInverse", "fl_BlockJacobiApply"]
+           "fl_BlockJacobiInverse", "fl_BlockJacobiApply", "fl_CoarsePCG_workspace_size", "fl_CoarsePCG"]

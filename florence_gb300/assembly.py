@@ -173,6 +173,9 @@ def _check_flags(flags, what):
         raise N.FlorenceGB300Error(N.FL_ERR_ARG, what + " (element node id or index map out of range)")
     if f & N.FL_FLAG_TIMEOUT:
         raise N.FlorenceGB300Error(N.FL_ERR_CUDA, what + " (a bounded wait in a tensor-core kernel gave up)")
+    if f & N.FL_FLAG_PAIR_RANGE:
+        raise N.FlorenceGB300Error(N.FL_ERR_UNSUPPORTED, what + " (the pulled-back tangent left the float-pair "
+                                   "exponent range [2^-78, 2^120]: assemble with set_arithmetic('fp64'))")
     if f & N.FL_FLAG_NONPOSITIVE_J:
         warnings.warn("det F <= 0 at some Gauss point in " + what, NonPositiveJacobianWarning, stacklevel=3)
 
@@ -503,6 +506,12 @@ def _low_level_df(name, fem_solver, function_space, formulation, mesh, material,
                                               sparsity=sparsity, orientations=orient))
     x = _to_dev(Eulerx, torch.float64, asm.device)
     out = asm.assemble(x)
+    if int(asm.flags.item()) & N.FL_FLAG_PAIR_RANGE:
+        # values too small or too large for the float pairs of the default arithmetics (units far
+        # from O(1)): the same call in FP64
+        asm.flags.zero_()
+        with arithmetic("fp64"):
+            out = asm.assemble(x)
     host = [_HOST.to_host(t) for t in out]
     asm.check_flags("_LowLevelAssemblyDF_" + name)
     return tuple(host)
@@ -701,12 +710,13 @@ ARITHMETIC = {"fp64": N.FL_ARITH_FP64, "float_pair": N.FL_ARITH_FLOAT_PAIR, "ten
 
 def set_arithmetic(name):
     """Arithmetic of the stiffness contraction for every later FP64 assembly in the process:
-    'float_pair' (hi + lo float pairs on the FP32 pipe, ~1e-14 relative to FP64), 'fp64' (FP64
-    multiply-adds), 'tensor' (tensor cores on the per-element operand U split into six exact BF16
-    digits, ~1e-13) or 'reference_tensor' (each tile of 14 elements as one tensor-core GEMM of the
-    pulled-back tangents against the element type's constant reference tensor, six BF16 digit
+    'reference_tensor' (the default: each tile of 14 elements as one tensor-core GEMM of the
+    pulled-back tangents against the element type's constant reference tensor, seven BF16 digit
     planes per operand, exact FP64 recombination, ~1e-14; CSR outputs of 4-, 8-, 10- and 20-node
-    elements with at most 15 Gauss points, else float pairs). The material law is FP64 in all."""
+    elements with at most 15 Gauss points, else float pairs), 'float_pair' (hi + lo float pairs on
+    the FP32 pipe, ~1e-14 relative to FP64), 'fp64' (FP64 multiply-adds) or 'tensor' (tensor cores
+    on the per-element operand U split into six exact BF16 digits, ~1e-13). The material law is
+    FP64 in all."""
     N.check(N.lib().fl_SetAssemblyArithmetic(ARITHMETIC[name]), "fl_SetAssemblyArithmetic")
 
 

@@ -197,11 +197,20 @@ struct QOutF32 {
 struct QOutDF {
     float *h, *l;
     int64_t ld;
+    float *amax;  // the largest |hi| written (a register of the caller once inlined)
     __device__ void put(int p, FloatPair v) const {
         h[p * ld] = v.h;
         l[p * ld] = v.l;
+        *amax = v.h == v.h ? fmaxf(*amax, fabsf(v.h)) : INFINITY;  // NaN: an overflow met inf - inf
     }
 };
+
+// Float pairs keep ~2^-46 of their value while the low word stays a normal FP32 number and the
+// high word far from overflow: a Gauss point whose largest tangent entry (or stress factor) lies
+// outside [2^-78, 2^120] is reported (FL_FLAG_PAIR_RANGE) so that the caller can assemble in FP64.
+__device__ __forceinline__ bool pair_out_of_range(float amax) {
+    return amax > 0x1p120f || (amax > 0.f && amax < 0x1p-78f);
+}
 
 // Gauss-point output layout: FP64 [54][ldq] in Q; FP32 tangent [45][ldq] in Qf with S [9][ldq]
 // in Q; the tangent formed in float-pair arithmetic (hi [45][ldq] then lo [45][ldq]) in Qf with
@@ -263,6 +272,7 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         double *q = A.Q + t;
         // S[i][d] = detJ sum_j sigma_ij G[j][d], the residual's Gauss-point factor, in FP64
         double *qs = QOUT != QOUT_F64 ? q : q + 45 * ld;
+        float amax = 0.f;  // largest magnitude held as float pairs
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -274,6 +284,7 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
                     float *sf = reinterpret_cast<float *>(A.Q) + t;
                     sf[(i * 3 + d) * ld] = sp.h;
                     sf[(9 + i * 3 + d) * ld] = sp.l;
+                    amax = sp.h == sp.h ? fmaxf(amax, fabsf(sp.h)) : INFINITY;
                 } else {
                     qs[(i * 3 + d) * ld] = sv;
                 }
@@ -281,9 +292,11 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         if constexpr (QOUT == QOUT_F32)
             pulled_back_tangent<float, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF32{A.Qf + t, ld});
         else if constexpr (QOUT == QOUT_DF || QOUT == QOUT_RT)
-            pulled_back_tangent<FloatPair, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutDF{A.Qf + t, A.Qf + 45 * ld + t, ld});
+            pulled_back_tangent<FloatPair, MAT>(G, sig, b, ex, c1, c2, cbb, detJ,
+                                                QOutDF{A.Qf + t, A.Qf + 45 * ld + t, ld, &amax});
         else
             pulled_back_tangent<double, MAT>(G, sig, b, ex, c1, c2, cbb, detJ, QOutF64{q, ld});
+        if ((QOUT == QOUT_DF || QOUT == QOUT_RT) && pair_out_of_range(amax)) flag |= FL_FLAG_PAIR_RANGE;
     }
     if (flag && A.flags) atomicOr(A.flags, flag);
 }
@@ -588,9 +601,10 @@ static int64_t chunk_elements(size_t bytes, int nq, int epc) {
     return ce - ce % epc;
 }
 
-// Arithmetic of the contraction kernel (fl_SetAssemblyArithmetic): float pairs by default, the
-// faster of the two on GB300, within the FP64 path's accuracy bar
-static std::atomic<int> g_arith{FL_ARITH_FLOAT_PAIR};
+// Arithmetic of the contraction (fl_SetAssemblyArithmetic): by default the reference-tensor GEMMs
+// on the tensor cores where they apply, float pairs on the FP32 pipe elsewhere; FP64 multiply-adds
+// only when asked for
+static std::atomic<int> g_arith{FL_ARITH_REFERENCE_TENSOR};
 
 // Float-pair kinematics inputs, once per assembly call: per node the reference coordinates X and
 // the displacement u = x - X (formed in FP64) as float pairs, 12 floats in three float4 words
@@ -663,8 +677,8 @@ static int run_chunks_t(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream
 
 template <int NPE, int MAT>
 static int run_chunks(AsmArgs A, double *Q, int64_t chunk, cudaStream_t stream) {
-    if (g_arith.load() == FL_ARITH_FLOAT_PAIR) return run_chunks_t<NPE, MAT, true>(A, Q, chunk, stream);
-    return run_chunks_t<NPE, MAT, false>(A, Q, chunk, stream);
+    if (g_arith.load() == FL_ARITH_FP64) return run_chunks_t<NPE, MAT, false>(A, Q, chunk, stream);
+    return run_chunks_t<NPE, MAT, true>(A, Q, chunk, stream);
 }
 
 template <int NPE, int MAT>
@@ -2007,6 +2021,7 @@ static int launch_oz(AsmArgs A, cudaStream_t stream) {
     double *Q = nullptr;
     FL_CUDA_TRY(cudaMallocAsync((void **)&Q, sbytes + fbytes + 2 * jbytes + pair_prep_bytes(A.nnode, NPE, A.nq), stream));
     pair_prep(A, NPE, reinterpret_cast<char *>(Q) + sbytes + fbytes + 2 * jbytes, stream);
+    A.npair = nullptr;  // FP64 kinematics: see launch_rt (sliver elements)
     A.Q = Q;
     A.Qf = reinterpret_cast<float *>(reinterpret_cast<char *>(Q) + sbytes);
     A.ldq = chunk * A.nq;

@@ -119,6 +119,207 @@ static unsigned grid_of(int64_t n, int per_block) {
     return (unsigned)std::max<int64_t>(1, (n + per_block - 1) / per_block);
 }
 
+// ------------------------------------------------------------------------------------------------
+// The coarse problem's block-Jacobi PCG in one cooperative launch. The coarse system is small
+// (three dofs per mesh vertex) and needs hundreds of iterations per cycle; as separate launches
+// each iteration would cost three kernel boundaries and a host poll, far more than its work.
+// Here every CTA stays resident (cooperative launch), the iteration's three phases are separated
+// by grid barriers, and the dot products go through rotating device slots:
+//   phase 1  q = K_ff p, p.q                         (a warp per row)
+//   phase 2  alpha = r.z / p.q; x += alpha p; r -= alpha q; z = B^-1 r; r.z, r.r   (a thread per node)
+//   phase 3  stop when r.r <= rtol^2 b.b; beta = r.z(new) / r.z(old); p = z + beta p
+// Data written by other CTAs inside the launch are read past L1 (ld.global.cg). Every barrier
+// wait is bounded: on a timeout the kernel records FL_FLAG_TIMEOUT and every CTA leaves.
+constexpr int CG_NT = 512;
+constexpr long long CG_SPIN_LIMIT = 1ll << 24;
+
+struct CgArgs {
+    const int32_t *indptr, *indices;
+    const double *vals, *Binv, *b;
+    const int8_t *fixed;
+    double *x, *r, *z, *p, *q;
+    double *sc;          // [0..2] p.q, [3..5] r.z, [6..8] r.r (rotating by iteration), [9] b.b
+    unsigned *bar;       // [0] arrivals, [1] generation
+    int *abort_flag;     // set by a CTA whose barrier wait timed out
+    int64_t n, maxiter;
+    double rtol2;
+    int64_t *iters;      // optional: the iteration count is added here
+    double *relres;      // optional: |r| / |b| at the end
+    int *flags;          // optional: FL_FLAG_TIMEOUT, FL_FLAG_BAD_INDEX (non-positive p.q)
+};
+
+__device__ __forceinline__ double cg_block_sum(double v, double *red) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (threadIdx.x < 32) {
+        t = threadIdx.x < CG_NT / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    }
+    __syncthreads();
+    return t;  // in thread 0
+}
+
+// grid barrier (arrival counter + generation); false when a wait timed out here or elsewhere
+__device__ bool cg_barrier(const CgArgs &a, unsigned &gen, volatile int *s_abort) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&a.bar[0], 1u) == gridDim.x - 1) {
+            atomicExch(&a.bar[0], 0u);
+            __threadfence();
+            atomicExch(&a.bar[1], gen + 1);
+        } else {
+            long long t = 0;
+            while (*(volatile unsigned *)&a.bar[1] == gen) {
+                if (*(volatile int *)a.abort_flag) break;
+                if (++t > CG_SPIN_LIMIT) {
+                    atomicExch(a.abort_flag, 1);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+        ++gen;
+        *s_abort = *(volatile int *)a.abort_flag;
+    }
+    __syncthreads();
+    return *s_abort == 0;
+}
+
+__global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
+    __shared__ double red[CG_NT / 32];
+    __shared__ volatile int s_abort;
+    const int lane = threadIdx.x & 31;
+    const int64_t gt = blockIdx.x * (int64_t)CG_NT + threadIdx.x, nthr = (int64_t)gridDim.x * CG_NT;
+    const int64_t gwarp = gt >> 5, nwarps = nthr >> 5;
+    const int64_t nnode = a.n / 3;
+    unsigned gen = 0;
+    if (threadIdx.x == 0) s_abort = 0;
+    __syncthreads();
+    double *sc = a.sc;
+    // r = b, z = B^-1 r, p = z, x = 0 (fixed dofs 0 throughout)
+    double rz = 0.0, bb = 0.0;
+    for (int64_t m = gt; m < nnode; m += nthr) {
+        double rv[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int64_t d = 3 * m + i;
+            rv[i] = a.fixed[d] ? 0.0 : a.b[d];
+            __stcg(a.r + d, rv[i]);
+            __stcg(a.x + d, 0.0);
+            bb = fma(rv[i], rv[i], bb);
+        }
+        const double *B = a.Binv + m * 9;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int64_t d = 3 * m + i;
+            const double zv = a.fixed[d] ? 0.0 : fma(B[3 * i], rv[0], fma(B[3 * i + 1], rv[1], B[3 * i + 2] * rv[2]));
+            __stcg(a.z + d, zv);
+            __stcg(a.p + d, zv);
+            rz = fma(rv[i], zv, rz);
+        }
+    }
+    rz = cg_block_sum(rz, red);
+    bb = cg_block_sum(bb, red);
+    if (threadIdx.x == 0) {
+        atomicAdd(sc + 3, rz);
+        atomicAdd(sc + 9, bb);
+    }
+    bool ok = cg_barrier(a, gen, &s_abort);
+    const double b2 = __ldcg(sc + 9);
+    int64_t k = 0;
+    double rr = b2;
+    bool bad = false;
+    if (b2 > 0.0)
+        for (; ok && k < a.maxiter; ++k) {
+            const int s0 = (int)(k % 3), s1 = (int)((k + 1) % 3);
+            // phase 1: q = K_ff p, p.q; the slots of the next iteration are cleared
+            if (gt == 0) {
+                __stcg(sc + s1, 0.0);
+                __stcg(sc + 3 + s1, 0.0);
+                __stcg(sc + 6 + s1, 0.0);
+            }
+            double pq = 0.0;
+            for (int64_t row = gwarp; row < a.n; row += nwarps) {
+                double acc = 0.0;
+                const bool fr = a.fixed[row] != 0;
+                if (!fr)
+                    for (int j = a.indptr[row] + lane; j < a.indptr[row + 1]; j += 32) {
+                        const int c = a.indices[j];
+                        if (!a.fixed[c]) acc = fma(a.vals[j], __ldcg(a.p + c), acc);
+                    }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+                if (lane == 0) {
+                    acc = fr ? 0.0 : acc;
+                    __stcg(a.q + row, acc);
+                    pq = fma(__ldcg(a.p + row), acc, pq);
+                }
+            }
+            pq = cg_block_sum(pq, red);
+            if (threadIdx.x == 0) atomicAdd(sc + s0, pq);
+            if (!(ok = cg_barrier(a, gen, &s_abort))) break;
+            // phase 2
+            const double pqk = __ldcg(sc + s0), rzk = __ldcg(sc + 3 + s0);
+            if (!(pqk > 0.0) || !isfinite(pqk)) {  // K_ff not positive definite on p (or no progress)
+                bad = true;
+                break;
+            }
+            const double alpha = rzk / pqk;
+            double rz1 = 0.0, rr1 = 0.0;
+            for (int64_t m = gt; m < nnode; m += nthr) {
+                double rv[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int64_t d = 3 * m + i;
+                    const double pv = __ldcg(a.p + d);
+                    __stcg(a.x + d, fma(alpha, pv, __ldcg(a.x + d)));
+                    rv[i] = fma(-alpha, __ldcg(a.q + d), __ldcg(a.r + d));
+                    __stcg(a.r + d, rv[i]);
+                    rr1 = fma(rv[i], rv[i], rr1);
+                }
+                const double *B = a.Binv + m * 9;
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const int64_t d = 3 * m + i;
+                    const double zv =
+                        a.fixed[d] ? 0.0 : fma(B[3 * i], rv[0], fma(B[3 * i + 1], rv[1], B[3 * i + 2] * rv[2]));
+                    __stcg(a.z + d, zv);
+                    rz1 = fma(rv[i], zv, rz1);
+                }
+            }
+            rz1 = cg_block_sum(rz1, red);
+            rr1 = cg_block_sum(rr1, red);
+            if (threadIdx.x == 0) {
+                atomicAdd(sc + 3 + s1, rz1);
+                atomicAdd(sc + 6 + s1, rr1);
+            }
+            if (!(ok = cg_barrier(a, gen, &s_abort))) break;
+            // phase 3
+            rr = __ldcg(sc + 6 + s1);
+            if (rr <= a.rtol2 * b2) {
+                ++k;
+                break;
+            }
+            const double beta = __ldcg(sc + 3 + s1) / rzk;
+            for (int64_t d = gt; d < a.n; d += nthr) __stcg(a.p + d, fma(beta, __ldcg(a.p + d), __ldcg(a.z + d)));
+            if (!(ok = cg_barrier(a, gen, &s_abort))) {
+                ++k;
+                break;
+            }
+        }
+    if (gt == 0) {
+        if (a.iters) atomicAdd((unsigned long long *)a.iters, (unsigned long long)k);
+        if (a.relres) *a.relres = b2 > 0.0 ? sqrt(rr / b2) : 0.0;
+        if (a.flags && (!ok || bad)) atomicOr(a.flags, !ok ? FL_FLAG_TIMEOUT : FL_FLAG_BAD_INDEX);
+    }
+}
+
 }  // namespace fl
 
 extern "C" {
@@ -152,6 +353,64 @@ int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const d
     fl::block_inverse_kernel<<<fl::grid_of(nnode, fl::MG_NT), fl::MG_NT, 0, (cudaStream_t)stream>>>(
         indptr, indices, values, fixed, nnode, Binv, flags);
     return fl::launch_status();
+}
+
+size_t fl_CoarsePCG_workspace_size(int64_t nrows) {
+    if (nrows < 0) return 0;
+    return sizeof(double) * (size_t)(4 * nrows + 16) + 64;
+}
+
+int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
+                 const int8_t *fixed, const double *Binv, const double *b, double *x, double rtol, int64_t maxiter,
+                 void *workspace, size_t workspace_bytes, int64_t *iterations, double *relres, int *flags,
+                 fl_stream_t stream) {
+    if (nrows < 0 || nrows % 3 || maxiter < 0 || !(rtol >= 0.0)) return FL_ERR_ARG;
+    if (nrows == 0) return FL_OK;
+    if (!indptr || !indices || !values || !fixed || !Binv || !b || !x || !workspace) return FL_ERR_ARG;
+    if (workspace_bytes < fl_CoarsePCG_workspace_size(nrows)) return FL_ERR_CAPACITY;
+    cudaStream_t st = (cudaStream_t)stream;
+    static int per_sm[64] = {}, sms[64] = {};
+    int dev = 0;
+    FL_CUDA_TRY(cudaGetDevice(&dev));
+    if (per_sm[dev & 63] == 0) {
+        int coop = 0;
+        FL_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
+        if (!coop) return FL_ERR_UNSUPPORTED;
+        FL_CUDA_TRY(cudaDeviceGetAttribute(&sms[dev & 63], cudaDevAttrMultiProcessorCount, dev));
+        int b = 0;
+        FL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fl::coarse_pcg_kernel, fl::CG_NT, 0));
+        per_sm[dev & 63] = std::max(1, b);
+    }
+    // enough CTAs for a warp per row, at most every resident one (a cooperative launch needs them all resident)
+    const int64_t want = (nrows + fl::CG_NT / 32 - 1) / (fl::CG_NT / 32);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms[dev & 63] * per_sm[dev & 63]));
+    fl::CgArgs a{};
+    char *w = (char *)workspace;
+    a.sc = (double *)w;
+    a.bar = (unsigned *)(w + 16 * sizeof(double));
+    a.abort_flag = (int *)(w + 16 * sizeof(double) + 2 * sizeof(unsigned));
+    double *v = (double *)(w + 16 * sizeof(double) + 64);
+    a.r = v;
+    a.z = v + nrows;
+    a.p = v + 2 * nrows;
+    a.q = v + 3 * nrows;
+    a.indptr = indptr;
+    a.indices = indices;
+    a.vals = values;
+    a.Binv = Binv;
+    a.b = b;
+    a.fixed = fixed;
+    a.x = x;
+    a.n = nrows;
+    a.maxiter = maxiter;
+    a.rtol2 = rtol * rtol;
+    a.iters = iterations;
+    a.relres = relres;
+    a.flags = flags;
+    FL_CUDA_TRY(cudaMemsetAsync(w, 0, 16 * sizeof(double) + 64, st));
+    void *args[] = {(void *)&a};
+    FL_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)fl::coarse_pcg_kernel, dim3(grid), dim3(fl::CG_NT), args, 0, st));
+    return FL_OK;
 }
 
 int fl_BlockJacobiApply(int64_t nnode, const double *Binv, const int8_t *fixed, double omega, const double *r,

@@ -21,8 +21,9 @@ Adams, Brezina, Hu and Tuminaro (J. Comput. Phys. 188, 2003); lmax comes from a 
 iterations per tangent.
 
 Everything runs on the GPU through the library's kernels (fl_MaskedMatVec, fl_BlockJacobiApply,
-fl_NodalTransfer, the assembly and the block-Jacobi PCG); vector updates and dot products are
-torch operations on the same stream.
+fl_NodalTransfer, the assembly, and the coarse block-Jacobi PCG in one cooperative launch,
+fl_CoarsePCG); vector updates and dot products are torch operations on the same stream, and the
+outer iteration reads one scalar (|r|) per iteration on the host.
 """
 import numpy as np
 import torch
@@ -99,14 +100,22 @@ class PMultigrid:
         self.Vc = torch.zeros(self.coarse.nnz, dtype=torch.float64, device=dev)
         self.Tc = torch.zeros(self.nc, dtype=torch.float64, device=dev)
         self.Binv = torch.empty((asm.nnode, 9), dtype=torch.float64, device=dev)
+        self.Binv_c = torch.empty((self.coarse.nnode, 9), dtype=torch.float64, device=dev)
         self.nu, self.ratio, self.power_iters = nu, ratio, power_iters
         self.coarse_rtol, self.coarse_maxiter = coarse_rtol, coarse_maxiter
         self.flags = torch.zeros(1, dtype=torch.int32, device=dev)
         self.V = None
         self.lmax = None
-        self.coarse_iters = 0
         self.cycles = 0
-        self._ws = None
+        # the coarse solve (fl_CoarsePCG): its workspace, solution and iteration counter on the device
+        self._cws = torch.empty(int(N.lib().fl_CoarsePCG_workspace_size(self.nc)), dtype=torch.uint8, device=dev)
+        self._xc = torch.zeros(self.nc, dtype=torch.float64, device=dev)
+        self._citers = torch.zeros(1, dtype=torch.int64, device=dev)
+
+    @property
+    def coarse_iters(self):
+        """Coarse PCG iterations of every cycle so far (reads a device counter)."""
+        return int(self._citers.item())
 
     # -- kernels ------------------------------------------------------------------------------
     def matvec(self, x, y, b=None):
@@ -154,6 +163,10 @@ class PMultigrid:
         self.Vc.zero_()
         self.Tc.zero_()
         self.coarse.assemble((self.coarse.points + uc).contiguous(), V=self.Vc, T=self.Tc)
+        c = self.coarse
+        N.check(N.lib().fl_BlockJacobiInverse(_ptr(c.indptr), _ptr(c.indices), _ptr(self.Vc), c.nnode,
+                                              _ptr(self.fixed_c), _ptr(self.Binv_c), _ptr(self.flags), _stream()),
+                "fl_BlockJacobiInverse")
 
     # -- the cycle --------------------------------------------------------------------------------
     def _chebyshev(self, r, z, first):
@@ -182,20 +195,33 @@ class PMultigrid:
             rho = rho_new
         return z
 
+    def coarse_solve(self, rc):
+        """The coarse correction: block-Jacobi PCG on the vertex tangent to coarse_rtol (at most
+        coarse_maxiter iterations) in one cooperative launch; returns the device solution."""
+        c = self.coarse
+        N.check(N.lib().fl_CoarsePCG(_ptr(c.indptr), _ptr(c.indices), _ptr(self.Vc), self.nc, _ptr(self.fixed_c),
+                                     _ptr(self.Binv_c), _ptr(rc), _ptr(self._xc), float(self.coarse_rtol),
+                                     int(self.coarse_maxiter), _ptr(self._cws), self._cws.numel(), _ptr(self._citers),
+                                     None, _ptr(self.flags), _stream()), "fl_CoarsePCG")
+        return self._xc
+
+    def check_flags(self):
+        f = int(self.flags.item())
+        if f & N.FL_FLAG_TIMEOUT:
+            raise N.FlorenceGB300Error(N.FL_ERR_CUDA, "p-multigrid coarse solve (a grid barrier wait gave up)")
+        if f & N.FL_FLAG_BAD_INDEX:
+            raise N.FlorenceGB300Error(N.FL_ERR_ARG, "p-multigrid (missing or singular diagonal block, or a "
+                                                     "coarse tangent that is not positive definite)")
+
     def apply(self, r, z):
         """z = M^-1 r (one cycle)."""
-        from .newton import pcg, pcg_workspace
         self._chebyshev(r, z, first=True)
         res = torch.empty_like(r)
         self.matvec(z, res, b=r)
         rc = torch.empty(self.nc, dtype=torch.float64, device=self.dev)
         self.restrict(res, rc)
         rc *= (self.fixed_c == 0)
-        if self._ws is None:
-            self._ws = pcg_workspace(self.coarse, self.Vc, "fp64")
-        ec, it, _ = pcg(self.coarse, self.Vc, rc, self.fixed_c, rtol=self.coarse_rtol, maxiter=self.coarse_maxiter,
-                        workspace=self._ws, spmv="fp64")
-        self.coarse_iters += it
+        ec = self.coarse_solve(rc)
         self.cycles += 1
         self.prolong_add(ec, z)
         z *= (self.fixed == 0)
@@ -220,25 +246,25 @@ def fcg(mg, b, x=None, rtol=1e-8, maxiter=500):
     z = torch.empty_like(b)
     q = torch.empty_like(b)
     p = None
-    r_prev = None
-    rz = 0.0
+    r_prev = torch.empty_like(b)
     it = 0
     rel = float(torch.linalg.vector_norm(r)) / nb
+    # the scalars stay on the device (0-d tensors); the host reads |r| once per iteration
     while it < maxiter and rel > rtol:
         mg.apply(r, z)
+        rz_new = torch.dot(r, z)
         if p is None:
             p = z.clone()
-            rz = float(torch.dot(r, z))
         else:
-            rz_new = float(torch.dot(r, z))
-            beta = float(torch.dot(z, r - r_prev)) / rz   # flexible (Polak-Ribiere) beta
-            rz = rz_new
+            beta = torch.dot(z, r - r_prev) / rz   # flexible (Polak-Ribiere) beta
             p.mul_(beta).add_(z)
+        rz = rz_new
         mg.matvec(p, q)
-        alpha = rz / float(torch.dot(p, q))
-        x.add_(p, alpha=alpha)
-        r_prev = r.clone()
-        r.add_(q, alpha=-alpha)
+        alpha = rz / torch.dot(p, q)
+        x.add_(alpha * p)
+        r_prev.copy_(r)
+        r.sub_(alpha * q)
         it += 1
         rel = float(torch.linalg.vector_norm(r)) / nb
+    mg.check_flags()
     return x, it, rel

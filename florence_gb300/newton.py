@@ -268,8 +268,11 @@ class NewtonSolver:
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         self.history = incs
-        return dict(u=u, wall_s=wall, newton_iters=total_newton, pcg_iters=total_pcg, failed=failed,
-                    increments=incs)
+        out = dict(u=u, wall_s=wall, newton_iters=total_newton, pcg_iters=total_pcg, failed=failed,
+                   increments=incs)
+        if self.mg is not None:
+            out.update(mg_cycles=self.mg.cycles, mg_coarse_iters=self.mg.coarse_iters)
+        return out
 
 
 # ------------------------------------------------------------------------------------------------

@@ -49,6 +49,11 @@ typedef struct CUstream_st *fl_stream_t;
 #define FL_FLAG_NONPOSITIVE_J 1 /* det F <= 0 at some Gauss point; results are still written */
 #define FL_FLAG_BAD_INDEX 2     /* an element node id or a map entry is out of range; the entry was skipped */
 #define FL_FLAG_TIMEOUT 4       /* a bounded wait inside a tensor-core kernel gave up; outputs incomplete */
+#define FL_FLAG_PAIR_RANGE 8    /* a Gauss point's pulled-back tangent (or, with FL_ARITH_REFERENCE_TENSOR,
+                                 * its stress factor) has its largest magnitude outside [2^-78, 2^120]:
+                                 * the float pairs these arithmetics hold it in (FP32 exponent range) may
+                                 * have lost digits. The values are written; assemble again with
+                                 * FL_ARITH_FP64 (the Python drop-ins do this by themselves) */
 
 /* material numbers of the explicit entry point (_LowLevelAssemblyExplicit_DF_DPF_.pyx:72-109) */
 #define FL_MATERIAL_NEOHOOKEAN 1
@@ -238,7 +243,7 @@ int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
 
 /* Arithmetic of the stiffness contraction in every later FP64-valued assembly call of the process
  * (no reference counterpart; the reference contracts in FP64). FL_ARITH_FP64: FP64 fused
- * multiply-adds. FL_ARITH_FLOAT_PAIR (the default): each operand held as an unevaluated pair of
+ * multiply-adds. FL_ARITH_FLOAT_PAIR: each operand held as an unevaluated pair of
  * floats (hi + lo), products formed error-free in their leading part and summed with a
  * compensated two-sum on the FP32 pipe, ~2^-46 relative per multiply-add (element matrices
  * within ~1e-14 of FP64), about 1.6x faster on GB300, whose FP64 rate is 1/64 of its FP32 rate. The kinematics, the material law, the residual and the scatter stay FP64
@@ -255,12 +260,13 @@ int fl_SetAssemblyTuning(int64_t nodeperelem, int64_t ngauss, int gauss_chunk);
 /* FL_ARITH_REFERENCE_TENSOR: every element matrix of a tile of 14 elements as one tensor-core GEMM
  * of the pulled-back tangents [(element, i, k) x (Gauss point, d, e)] against the element-type
  * constant reference tensor Phi[(a, b) x (Gauss point, d, e)] = Jm[d][a][g] Jm[e][b][g] (node
- * pairs a <= b), both operands split into six BF16 digit planes (21 plane products, five FP32
+ * pairs a <= b), both operands split into seven BF16 digit planes (28 plane products, five FP32
  * tensor-memory accumulators, the leading four levels exact), recombined exactly into FP64 with
- * integer instructions: element matrices within ~1e-14 of FP64. The kinematics and the tangent's
- * pull-back run as float pairs, the material law in FP64, the residual as float pairs. Applies to
- * CSR outputs (maps or squeeze) without a caller-provided scratch, for 4-, 8-, 10- and 20-node
- * elements with at most 15 Gauss points; other calls use the float-pair contraction. */
+ * integer instructions: element matrices within ~1e-14 of FP64. The kinematics and the material
+ * law run in FP64, the tangent's pull-back and the residual as float pairs. Applies to CSR
+ * outputs (maps or squeeze) without a caller-provided scratch, for 4-, 8-, 10- and 20-node
+ * elements with at most 15 Gauss points; other calls use the float-pair contraction. The
+ * default. */
 #define FL_ARITH_REFERENCE_TENSOR 3
 int fl_SetAssemblyArithmetic(int arithmetic);
 int fl_GetAssemblyArithmetic(void);
@@ -441,6 +447,15 @@ int fl_StrainEnergy(const double *points, const uint64_t *elements, const double
  * fl_BlockJacobiInverse: Binv[n][9] = inverse of each node's 3x3 diagonal block, fixed rows and
  *   columns replaced by the identity (FL_FLAG_BAD_INDEX in flags for a missing or singular block).
  * fl_BlockJacobiApply: z (=, or +=) omega Binv r per node, 0 on fixed dofs.
+ * fl_CoarsePCG: x = the block-Jacobi PCG solution of K_ff x = b_f from x = 0 (Binv from
+ *   fl_BlockJacobiInverse of the same matrix), stopped at |r| <= rtol |b_f| or after maxiter
+ *   iterations, in ONE cooperative launch (every CTA resident, grid barriers between the three
+ *   phases of an iteration, bounded waits): for small systems, whose iterations would otherwise
+ *   be bound by kernel boundaries. workspace: fl_CoarsePCG_workspace_size(nrows) bytes.
+ *   iterations (optional, device int64): the iteration count is ADDED to it; relres (optional,
+ *   device double): |r| / |b_f| at the end; flags (optional, device int): FL_FLAG_TIMEOUT when a
+ *   barrier wait gave up, FL_FLAG_BAD_INDEX when p.K_ff p <= 0. FL_ERR_UNSUPPORTED without
+ *   cooperative launch. Nothing synchronises.
  * ------------------------------------------------------------------------------------------ */
 int fl_NodalTransfer(int64_t nrows, const int32_t *ptr, const int32_t *cols, const double *weights, const double *x,
                      double *y, int accumulate, fl_stream_t stream);
@@ -450,6 +465,11 @@ int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const d
                           const int8_t *fixed, double *Binv, int *flags, fl_stream_t stream);
 int fl_BlockJacobiApply(int64_t nnode, const double *Binv, const int8_t *fixed, double omega, const double *r,
                         double *z, int accumulate, fl_stream_t stream);
+size_t fl_CoarsePCG_workspace_size(int64_t nrows);
+int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
+                 const int8_t *fixed, const double *Binv, const double *b, double *x, double rtol, int64_t maxiter,
+                 void *workspace, size_t workspace_bytes, int64_t *iterations, double *relres, int *flags,
+                 fl_stream_t stream);
 
 size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows, int64_t nnz, int value_bits);
 int fl_BlockJacobiPCG(const int32_t *indptr, const int32_t *indices, const void *values, int value_bits,

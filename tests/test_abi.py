@@ -59,17 +59,17 @@ def test_pcg_workspace_sizes():
 
 
 def test_host_side_settings_validate_their_arguments():
-    """Process-wide settings are host-only calls: the contraction arithmetic (three names) and the
-    split-BF16 tiling (ranges checked, 0 = automatic)."""
+    """Process-wide settings are host-only calls: the contraction arithmetic (four names, the
+    reference-tensor GEMMs by default) and the split-BF16 tiling (ranges checked, 0 = automatic)."""
     import florence_gb300 as fl
     from florence_gb300._native import FlorenceGB300Error
-    assert fl.get_arithmetic() == "float_pair"
-    for name in ("fp64", "tensor", "float_pair"):
+    assert fl.get_arithmetic() == "reference_tensor"
+    for name in ("fp64", "tensor", "float_pair", "reference_tensor"):
         fl.set_arithmetic(name)
         assert fl.get_arithmetic() == name
     with fl.arithmetic("tensor"):
         assert fl.get_arithmetic() == "tensor"
-    assert fl.get_arithmetic() == "float_pair"
+    assert fl.get_arithmetic() == "reference_tensor"
     fl.set_tensor_core_tiling(2, 48)
     fl.set_tensor_core_tiling(0, 0)
     for bad in ((-1, 0), (17, 0), (0, -16), (0, 112)):

@@ -68,19 +68,21 @@ def test_csr_assembly_matches_reference(fl, case, mode):
 @pytest.mark.parametrize("case", golden_cases())
 @pytest.mark.parametrize("mode", ["csr", "squeeze", "triplet"])
 def test_both_contraction_arithmetics_match_reference(fl, case, mode):
-    """The contraction in FP64 multiply-adds and in float-pair arithmetic on the FP32 pipe (the
-    default; every other test runs it) both meet the FP64 path's bar (1e-12 relative Frobenius
-    against the reference) in every scatter mode; the residual is formed in FP64 either way from
-    kinematics summed in FP64 or in float pairs (the two agree to ~1e-14)."""
+    """The contraction in FP64 multiply-adds and in float-pair arithmetic on the FP32 pipe (what
+    the default reference-tensor arithmetic falls back to in triplet mode and for element types
+    its GEMM does not take) both meet the FP64 path's bar (1e-12 relative Frobenius against the
+    reference) in every scatter mode; the residual is formed in FP64 either way from kinematics
+    summed in FP64 or in float pairs (the two agree to ~1e-14)."""
     d = load_golden(case)
     asm = _asm(fl, d, mode)
     x = torch.from_numpy(d["Eulerx"]).cuda()
-    assert fl.get_arithmetic() == "float_pair"
+    assert fl.get_arithmetic() == "reference_tensor"
     with fl.arithmetic("fp64"):
         assert fl.get_arithmetic() == "fp64"
         out64 = asm.assemble(x)
-    assert fl.get_arithmetic() == "float_pair"
-    out = asm.assemble(x)
+    assert fl.get_arithmetic() == "reference_tensor"
+    with fl.arithmetic("float_pair"):
+        out = asm.assemble(x)
     if mode == "triplet":
         n = d["points"].shape[0] * 3
         K64 = sp.csr_matrix((out64[2].cpu().numpy(), (out64[0].cpu().numpy(), out64[1].cpu().numpy())), shape=(n, n))
@@ -118,7 +120,7 @@ def test_tensor_core_fp64_tangent_matches_reference(fl, case, mode):
         assert fl.get_arithmetic() == "tensor"
         V, T = asm.assemble(x)
         asm.check_flags()
-    assert fl.get_arithmetic() == "float_pair"
+    assert fl.get_arithmetic() == "reference_tensor"
     assert rel_fro(V.cpu().numpy(), d["K_data"]) < TOL
     assert rel_fro(T.cpu().numpy(), d["T"]) < TOL
 

@@ -109,7 +109,7 @@ def arithmetic():
     fl.set_arithmetic(old)
 
 
-@pytest.mark.parametrize("arith", ["float_pair", "fp64", "tensor"])
+@pytest.mark.parametrize("arith", ["float_pair", "fp64", "tensor", "reference_tensor"])
 @pytest.mark.parametrize("case,mode", [("hex_p2_nh_q5", "csr"), ("tet_p3_mr_jitter", "triplet")])
 def test_noalloc_matches_regular_entry_point_twice(case, mode, arith, arithmetic):
     from florence_gb300 import _native as N
