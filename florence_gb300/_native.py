@@ -118,11 +118,14 @@ def lib():
                                      P]
         L.fl_NodalTransfer.argtypes = [I64, P, P, P, P, P, INT, P]
         L.fl_MaskedMatVec.argtypes = [P, P, P, I64, P, P, P, P, P]
+        L.fl_MaskedMatVecBlocks.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_BlockJacobiInverse.argtypes = [P, P, P, I64, P, P, P, P]
         L.fl_BlockJacobiApply.argtypes = [I64, P, P, D, P, P, INT, P]
         L.fl_CoarsePCG_workspace_size.argtypes = [I64]
         L.fl_CoarsePCG_workspace_size.restype = ctypes.c_size_t
         L.fl_CoarsePCG.argtypes = [P, P, P, I64, P, P, P, P, D, I64, P, ctypes.c_size_t, P, P, P, P]
+        L.fl_SetPCGDeviceLoop.argtypes = [INT]
+        L.fl_GetPCGDeviceLoop.argtypes = []
         L.fl_BlockJacobiPCG_workspace_size.argtypes = [I64, I64, INT]
         L.fl_BlockJacobiPCG_workspace_size.restype = ctypes.c_size_t
         L.fl_BlockJacobiPCG.argtypes = [P, P, P, INT, I64, P, P, P, D, I64, P, ctypes.c_size_t,
@@ -148,8 +151,8 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_", "fl_GlobalAssemblyDPF__SteinmannModel_",
            "fl_GlobalAssemblyDPF__Piezoelectric_100_",
            "fl_GlobalAssemblyExplicit_DF_DPF_", "fl_LumpedMass", "fl_ConsistentMass", "fl_measure_fp64_peak", "fl_measure_fp32_peak", "fl_TensorCoreSelfTest",
-           "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
+           "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_SetPCGDeviceLoop", "fl_GetPCGDeviceLoop", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
            "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_AssembleExternalTractionForces", "fl_AssembleBodyForces", "fl_MLP_num_params", "fl_MLP_workspace_size",
-           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec",
+           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec", "fl_MaskedMatVecBlocks",
            "fl_BlockJacobiInverse", "fl_BlockJacobiApply", "fl_CoarsePCG_workspace_size", "fl_CoarsePCG"]

@@ -64,6 +64,48 @@ __global__ void __launch_bounds__(MG_NT) masked_spmv_kernel(const int32_t *indpt
     }
 }
 
+// The same product on a node-blocked pattern (the three rows of a node list the same nodes, three
+// columns each, as every assembled tangent's pattern does): one warp per node, lanes over its
+// column blocks, nine values and one column index per block. x must be zero on fixed dofs (the
+// columns are then masked by x itself); fixed rows give 0 (or nothing subtracted from b).
+__global__ void __launch_bounds__(MG_NT) masked_spmv_blocks_kernel(const int32_t *indptr, const int32_t *indices,
+                                                                   const double *vals, int64_t nnode,
+                                                                   const int8_t *fixed, const double *x,
+                                                                   const double *b, double *y, int64_t ncols) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)MG_NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * MG_NT) >> 5;
+    for (int64_t m = warp; m < nnode; m += nwarps) {
+        const int64_t r0 = 3 * m;
+        const int p0 = indptr[r0], p1 = indptr[r0 + 1], p2 = indptr[r0 + 2];
+        const int nb = (p1 - p0) / 3;
+        double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        for (int blk = lane; blk < nb; blk += 32) {
+            const int c = indices[p0 + 3 * blk];
+            if (c < 0 || c + 2 >= ncols) continue;
+            const double x0 = x[c], x1 = x[c + 1], x2 = x[c + 2];
+            const double *v0 = vals + p0 + 3 * blk, *v1 = vals + p1 + 3 * blk, *v2 = vals + p2 + 3 * blk;
+            a0 = fma(v0[0], x0, fma(v0[1], x1, fma(v0[2], x2, a0)));
+            a1 = fma(v1[0], x0, fma(v1[1], x1, fma(v1[2], x2, a1)));
+            a2 = fma(v2[0], x0, fma(v2[1], x1, fma(v2[2], x2, a2)));
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a0 += __shfl_down_sync(0xffffffffu, a0, o);
+            a1 += __shfl_down_sync(0xffffffffu, a1, o);
+            a2 += __shfl_down_sync(0xffffffffu, a2, o);
+        }
+        if (lane == 0) {
+            const double a[3] = {a0, a1, a2};
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                const int64_t row = r0 + i;
+                y[row] = fixed[row] ? 0.0 : (b ? b[row] - a[i] : a[i]);
+            }
+        }
+    }
+}
+
 // z (+)= omega B^-1 r per node; fixed dofs of z set to 0
 __global__ void __launch_bounds__(MG_NT) block_apply_kernel(int64_t nnode, const double *Binv, const int8_t *fixed,
                                                             double omega, const double *r, double *z, int accumulate) {
@@ -345,6 +387,18 @@ int fl_MaskedMatVec(const int32_t *indptr, const int32_t *indices, const double 
     return fl::launch_status();
 }
 
+int fl_MaskedMatVecBlocks(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
+                          const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream) {
+    if (nrows < 0 || nrows % 3) return FL_ERR_ARG;
+    if (nrows == 0) return FL_OK;
+    if (!indptr || !indices || !values || !fixed || !x || !y) return FL_ERR_ARG;
+    const int64_t nnode = nrows / 3;
+    const int64_t warps = std::min<int64_t>(nnode, (int64_t)152 * 64);
+    fl::masked_spmv_blocks_kernel<<<fl::grid_of(warps * 32, fl::MG_NT), fl::MG_NT, 0, (cudaStream_t)stream>>>(
+        indptr, indices, values, nnode, fixed, x, b, y, nrows);
+    return fl::launch_status();
+}
+
 int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nnode,
                           const int8_t *fixed, double *Binv, int *flags, fl_stream_t stream) {
     if (nnode < 0) return FL_ERR_ARG;
@@ -381,9 +435,11 @@ int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *va
         FL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fl::coarse_pcg_kernel, fl::CG_NT, 0));
         per_sm[dev & 63] = std::max(1, b);
     }
-    // enough CTAs for a warp per row, at most every resident one (a cooperative launch needs them all resident)
+    // enough CTAs for a warp per row, at most one per SM: every grid barrier serialises one atomic
+    // arrival per CTA, so fewer, larger CTAs make the barriers cheaper (a cooperative launch also
+    // needs them all resident, which per_sm >= 1 guarantees)
     const int64_t want = (nrows + fl::CG_NT / 32 - 1) / (fl::CG_NT / 32);
-    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms[dev & 63] * per_sm[dev & 63]));
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms[dev & 63]));
     fl::CgArgs a{};
     char *w = (char *)workspace;
     a.sc = (double *)w;

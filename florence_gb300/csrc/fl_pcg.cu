@@ -29,6 +29,7 @@
 // block; the scalars never travel to the host inside the iteration (kernels read them from the
 // slots), and the host checks the done flag every PCG_CHECK iterations.
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 #include <utility>
@@ -46,7 +47,8 @@ struct PcgState {
     float *ph, *pl;                // p as a float pair (p ~ ph + pl), for the float-pair products
     float *qh, *ql;                // q = K p as a float pair, written by the float-pair products
     double *acc;                   // [0] p.q, [1],[2] r.z of even/odd iterates, [3] r.r, [4] |b|^2
-    int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits
+    int *done;                     // [0] done flag, [1] iterations at convergence, [2] error bits,
+                                   // [3] the iteration index k (advanced by pcg_tail)
     // float-pair iteration vectors (with the float-pair products): x, r, z as hi/lo floats [n],
     // the block inverses as hi/lo floats [n/3][9]
     float *xh, *xl, *rh, *rl, *zh, *zl, *Bh, *Bl;
@@ -331,8 +333,9 @@ __global__ void pcg_check_blocks(const int32_t *indptr, const int32_t *indices, 
 // K1: q = mask(K p), p.q; zeroes r.z of iterate k+1 and r.r for K2
 template <class VT, bool NODEBLK, int NB = 8>
 __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const int32_t *indices, const VT *vals,
-                                                 const int8_t *fixed, int64_t n, int k, PcgState s) {
+                                                 const int8_t *fixed, int64_t n, PcgState s) {
     if (s.done[0]) return;
+    const int k = s.done[3];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         s.acc[1 + ((k + 1) & 1)] = 0.0;
         s.acc[3] = 0.0;
@@ -401,11 +404,12 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k1(const int32_t *indptr, const in
 
 // K2: alpha = rz_k / p.q, x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r. One thread per
 // dof, 30 lanes of a warp = 10 nodes; a node's three residual entries meet through shuffles.
-__global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x, PcgState s, int qpair) {
+__global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, double *x, PcgState s, int qpair) {
     // one read of the done flag and one division per CTA (FP64 division is a long FP64-pipe
     // sequence); the flag read by one thread keeps the early return uniform across the CTA
     __shared__ double s_alpha;
     __shared__ int s_done;
+    const int k = s.done[3];
     if (threadIdx.x == 0) {
         s_done = s.done[0];
         s_alpha = s_done ? 0.0 : s.acc[1 + (k & 1)] / s.acc[0];
@@ -443,12 +447,12 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k2(int64_t nnode, int k, double *x
     block_atomic_add(rr, s.acc + 3);
 }
 
-// K3: beta = rz_{k+1} / rz_k, p = z + beta p, convergence test; zeroes p.q for the next K1
-__global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, int split, PcgState s) {
-    // block 0 sets the done flag at its end while other CTAs of this launch may still start:
-    // one thread reads it for the whole CTA, so every thread takes the same branch
+// K3: beta = rz_{k+1} / rz_k, p = z + beta p; zeroes p.q for the next K1
+__global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int split, PcgState s) {
+    // one thread reads the done flag for the whole CTA, so every thread takes the same branch
     __shared__ double s_beta;
     __shared__ int s_done;
+    const int k = s.done[3];
     if (threadIdx.x == 0) {
         s_done = s.done[0];
         s_beta = s_done ? 0.0 : s.acc[1 + ((k + 1) & 1)] / s.acc[1 + (k & 1)];
@@ -456,23 +460,34 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3(int64_t n, int k, double tol2, 
     __syncthreads();
     if (s_done) return;
     const double beta = s_beta;
-    const double rr = s.acc[3];
     for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT) {
         const double pv = fma(beta, s.p[d], s.z[d]);
         s.p[d] = pv;
         if (split) split_store(s, d, pv);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        s.acc[0] = 0.0;  // p.q of the next iterate (K2, the only reader, has finished)
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.acc[0] = 0.0;  // p.q of the next iterate (K2 has read it)
+}
+
+// The end of an iteration (one thread): the convergence test on r.r, the iteration index, and,
+// when the iteration runs as the body of a conditional WHILE node of a CUDA graph, the loop
+// condition -- continue while not converged and fewer than maxiter iterations have run.
+__global__ void pcg_tail(double tol2, int64_t maxiter, PcgState s, cudaGraphConditionalHandle h, int cond) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int *d = s.done;
+    if (!d[0]) {
+        const int k = d[3];
+        const double rr = s.acc[3];
         if (rr <= tol2) {
-            s.done[0] = 1;
-            s.done[1] = k + 1;
+            d[0] = 1;
+            d[1] = k + 1;
         } else if (!isfinite(rr)) {
-            s.done[0] = 1;
-            s.done[1] = k + 1;
-            s.done[2] |= 4;
+            d[0] = 1;
+            d[1] = k + 1;
+            d[2] |= 4;
         }
+        d[3] = k + 1;
     }
+    if (cond) cudaGraphSetConditional(h, (!d[0] && (int64_t)d[3] < maxiter) ? 1u : 0u);
 }
 
 // Float-pair iteration (with the float-pair products): x, r, z, p and the block inverses as
@@ -501,9 +516,10 @@ __global__ void __launch_bounds__(PCG_NT) pcg_from_pairs(int64_t n, double *x, P
 }
 
 // K2 in float pairs: x += alpha p, r -= alpha q, z = B^-1 r, r.z and r.r (layout as pcg_k2)
-__global__ void __launch_bounds__(PCG_NT) pcg_k2_pair(int64_t nnode, int k, PcgState s) {
+__global__ void __launch_bounds__(PCG_NT) pcg_k2_pair(int64_t nnode, PcgState s) {
     __shared__ double s_alpha;
     __shared__ int s_done;
+    const int k = s.done[3];
     if (threadIdx.x == 0) {
         s_done = s.done[0];
         s_alpha = s_done ? 0.0 : s.acc[1 + (k & 1)] / s.acc[0];
@@ -549,9 +565,10 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k2_pair(int64_t nnode, int k, PcgS
 }
 
 // K3 in float pairs: p = z + beta p (written straight as the product's float pair), convergence
-__global__ void __launch_bounds__(PCG_NT) pcg_k3_pair(int64_t n, int k, double tol2, PcgState s) {
+__global__ void __launch_bounds__(PCG_NT) pcg_k3_pair(int64_t n, PcgState s) {
     __shared__ double s_beta;
     __shared__ int s_done;
+    const int k = s.done[3];
     if (threadIdx.x == 0) {
         s_done = s.done[0];
         s_beta = s_done ? 0.0 : s.acc[1 + ((k + 1) & 1)] / s.acc[1 + (k & 1)];
@@ -559,23 +576,12 @@ __global__ void __launch_bounds__(PCG_NT) pcg_k3_pair(int64_t n, int k, double t
     __syncthreads();
     if (s_done) return;
     const FloatPair beta(s_beta);
-    const double rr = s.acc[3];
     for (int64_t d = blockIdx.x * (int64_t)PCG_NT + threadIdx.x; d < n; d += (int64_t)gridDim.x * PCG_NT) {
         const FloatPair pv = fma(beta, FloatPair(s.ph[d], s.pl[d]), FloatPair(s.zh[d], s.zl[d]));
         s.ph[d] = pv.h;
         s.pl[d] = pv.l;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        s.acc[0] = 0.0;  // p.q of the next iterate (K2, the only reader, has finished)
-        if (rr <= tol2) {
-            s.done[0] = 1;
-            s.done[1] = k + 1;
-        } else if (!isfinite(rr)) {
-            s.done[0] = 1;
-            s.done[1] = k + 1;
-            s.done[2] |= 4;
-        }
-    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.acc[0] = 0.0;  // p.q of the next iterate (K2 has read it)
 }
 
 // Resident blocks of a kernel over the whole GPU (one wave), for grid sizes of the grid-stride
@@ -593,7 +599,7 @@ static int64_t resident_blocks() {
 // run out first
 template <class MT, int NB>
 static void launch_k1(const int32_t *indptr, const int32_t *indices, const MT *vals, const int8_t *fixed, int64_t n,
-                      int k, const PcgState &s, cudaStream_t st) {
+                      const PcgState &s, cudaStream_t st) {
     static thread_local int64_t wave[64] = {};
     int dev = 0;
     cudaGetDevice(&dev);
@@ -602,17 +608,17 @@ static void launch_k1(const int32_t *indptr, const int32_t *indices, const MT *v
     const int64_t nodes_per_block = (PCG_NT / 32) * (32 / NB);
     const int64_t need = (n / 3 + nodes_per_block - 1) / nodes_per_block;
     pcg_k1<MT, true, NB><<<(unsigned)std::max<int64_t>(1, std::min(need, w)), PCG_NT, 0, st>>>(indptr, indices, vals,
-                                                                                              fixed, n, k, s);
+                                                                                              fixed, n, s);
 }
 
 template <class MT>
 static void launch_k1_nb(int nb, const int32_t *indptr, const int32_t *indices, const MT *vals, const int8_t *fixed,
-                         int64_t n, int k, const PcgState &s, cudaStream_t st) {
+                         int64_t n, const PcgState &s, cudaStream_t st) {
     switch (nb) {
-        case 4: launch_k1<MT, 4>(indptr, indices, vals, fixed, n, k, s, st); break;
-        case 16: launch_k1<MT, 16>(indptr, indices, vals, fixed, n, k, s, st); break;
-        case 32: launch_k1<MT, 32>(indptr, indices, vals, fixed, n, k, s, st); break;
-        default: launch_k1<MT, 8>(indptr, indices, vals, fixed, n, k, s, st); break;
+        case 4: launch_k1<MT, 4>(indptr, indices, vals, fixed, n, s, st); break;
+        case 16: launch_k1<MT, 16>(indptr, indices, vals, fixed, n, s, st); break;
+        case 32: launch_k1<MT, 32>(indptr, indices, vals, fixed, n, s, st); break;
+        default: launch_k1<MT, 8>(indptr, indices, vals, fixed, n, s, st); break;
     }
 }
 
@@ -645,9 +651,9 @@ static int pick_lanes(const int32_t *indptr, const int32_t *indices, const MT *v
         return best;
     }
     for (int nb : {4, 8, 16, 32}) {
-        launch_k1_nb<MT>(nb, indptr, indices, vals, fixed, n, 0, s, st);  // first touch
+        launch_k1_nb<MT>(nb, indptr, indices, vals, fixed, n, s, st);  // first touch
         cudaEventRecord(e0, st);
-        for (int r = 0; r < 2; ++r) launch_k1_nb<MT>(nb, indptr, indices, vals, fixed, n, 0, s, st);
+        for (int r = 0; r < 2; ++r) launch_k1_nb<MT>(nb, indptr, indices, vals, fixed, n, s, st);
         cudaEventRecord(e1, st);
         float ms = 0.f;
         if (cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess &&
@@ -661,6 +667,65 @@ static int pick_lanes(const int32_t *indptr, const int32_t *indices, const MT *v
     std::lock_guard<std::mutex> lock(g_lane_mutex);
     g_lane_cache.push_back({LaneKey{dev, kind, n, nnz}, best});
     return best;
+}
+
+// The PCG iterations as one CUDA graph: a conditional WHILE node whose body -- captured from
+// `iteration` on a private stream -- is one iteration, its last kernel setting the condition.
+// Launched on `st`; the host waits only for the final result. Returns the executable graph (to be
+// destroyed after the stream has synchronised), or nullptr when the graph cannot be built, in
+// which case nothing was enqueued and the caller iterates from the host.
+static std::atomic<int> g_device_loop{1};
+
+template <class Iter>
+static cudaGraphExec_t device_loop(cudaStream_t st, Iter &&iteration) {
+    static std::mutex m;
+    static cudaStream_t cs[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+    {
+        std::lock_guard<std::mutex> g(m);
+        if (!cs[dev & 63] && cudaStreamCreateWithFlags(&cs[dev & 63], cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+    }
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    if (cudaGraphCreate(&graph, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    bool ok = false;
+    do {
+        cudaGraphConditionalHandle h;
+        if (cudaGraphConditionalHandleCreate(&h, graph, 1, cudaGraphCondAssignDefault) != cudaSuccess) break;
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np) != cudaSuccess) break;
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        if (cudaStreamBeginCaptureToGraph(cs[dev & 63], body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+            cudaSuccess)
+            break;
+        iteration(cs[dev & 63], h, 1);
+        cudaGraph_t captured = nullptr;
+        if (cudaStreamEndCapture(cs[dev & 63], &captured) != cudaSuccess) break;
+        if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) {
+            exec = nullptr;
+            break;
+        }
+        ok = cudaGraphLaunch(exec, st) == cudaSuccess;
+    } while (false);
+    cudaGraphDestroy(graph);
+    if (!ok) {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        cudaGetLastError();
+    }
+    return exec;
 }
 
 template <class VT>
@@ -719,29 +784,41 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
     const bool pairs = nodeblk && (split || sizeof(VT) == 4);
     if (pairs) pcg_to_pairs<<<g_dofs, PCG_NT, 0, st>>>(n, x, s);
     int hd[4] = {0, 0, 0, 0};
-    int64_t k = 0;
-    while (k < maxiter) {
-        const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
-        for (; k < kend; ++k) {
-            if (split) launch_k1_nb<float2>(nb, indptr, indices, vsplit, fixed, n, (int)k, s, st);
-            else if (nodeblk) launch_k1_nb<VT>(nb, indptr, indices, vals, fixed, n, (int)k, s, st);
-            else pcg_k1<VT, false><<<g_rows, PCG_NT, 0, st>>>(indptr, indices, vals, fixed, n, (int)k, s);
-            if (pairs) {
-                pcg_k2_pair<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, s);
-                pcg_k3_pair<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, s);
-            } else {
-                pcg_k2<<<g_k2, PCG_NT, 0, st>>>(nnode, (int)k, x, s, 0);
-                pcg_k3<<<g_dofs, PCG_NT, 0, st>>>(n, (int)k, tol2, 0, s);
-            }
+    // one iteration: K1, K2, K3 and the tail (convergence test, iteration index, loop condition)
+    auto iteration = [&](cudaStream_t q, cudaGraphConditionalHandle h, int cond) {
+        if (split) launch_k1_nb<float2>(nb, indptr, indices, vsplit, fixed, n, s, q);
+        else if (nodeblk) launch_k1_nb<VT>(nb, indptr, indices, vals, fixed, n, s, q);
+        else pcg_k1<VT, false><<<g_rows, PCG_NT, 0, q>>>(indptr, indices, vals, fixed, n, s);
+        if (pairs) {
+            pcg_k2_pair<<<g_k2, PCG_NT, 0, q>>>(nnode, s);
+            pcg_k3_pair<<<g_dofs, PCG_NT, 0, q>>>(n, s);
+        } else {
+            pcg_k2<<<g_k2, PCG_NT, 0, q>>>(nnode, x, s, 0);
+            pcg_k3<<<g_dofs, PCG_NT, 0, q>>>(n, 0, s);
         }
-        FL_CUDA_TRY(cudaGetLastError());
-        FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
-        FL_CUDA_TRY(cudaStreamSynchronize(st));
-        if (hd[0]) break;
+        pcg_tail<<<1, 32, 0, q>>>(tol2, maxiter, s, h, cond);
+    };
+    // the whole loop on the device (a conditional WHILE node), or host-driven with a poll of the
+    // done flag every PCG_CHECK iterations
+    cudaGraphExec_t loop = nullptr;
+    if (maxiter > 0 && g_device_loop.load()) loop = device_loop(st, iteration);
+    if (!loop) {
+        int64_t k = 0;
+        while (k < maxiter) {
+            const int64_t kend = std::min<int64_t>(maxiter, k + PCG_CHECK);
+            for (; k < kend; ++k) iteration(st, cudaGraphConditionalHandle{}, 0);
+            FL_CUDA_TRY(cudaGetLastError());
+            FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+            FL_CUDA_TRY(cudaStreamSynchronize(st));
+            if (hd[0]) break;
+        }
     }
     if (pairs) pcg_from_pairs<<<g_dofs, PCG_NT, 0, st>>>(n, x, s);
     FL_CUDA_TRY(cudaMemcpyAsync(hacc, s.acc, sizeof(hacc), cudaMemcpyDeviceToHost, st));
-    FL_CUDA_TRY(cudaStreamSynchronize(st));
+    FL_CUDA_TRY(cudaMemcpyAsync(hd, s.done, sizeof(int) * 4, cudaMemcpyDeviceToHost, st));
+    const cudaError_t se = cudaStreamSynchronize(st);
+    if (loop) cudaGraphExecDestroy(loop);
+    if (se != cudaSuccess) return FL_ERR_CUDA;
     *iters = hd[0] ? hd[1] : maxiter;
     *relres = sqrt(hacc[3] / b2);
     if (hd[2] & 4) return FL_ERR_ARG;  // breakdown: non-finite residual
@@ -751,6 +828,14 @@ static int bj_pcg(const int32_t *indptr, const int32_t *indices, const VT *vals,
 }  // namespace fl
 
 extern "C" {
+
+int fl_SetPCGDeviceLoop(int enable) {
+    if (enable != 0 && enable != 1) return FL_ERR_ARG;
+    fl::g_device_loop.store(enable);
+    return FL_OK;
+}
+
+int fl_GetPCGDeviceLoop(void) { return fl::g_device_loop.load(); }
 
 size_t fl_BlockJacobiPCG_workspace_size(int64_t nrows, int64_t nnz, int value_bits) {
     return fl::pcg_layout(nrows, value_bits == FL_PCG_F64_SPLIT ? nnz : 0, nullptr, nullptr);

@@ -25,12 +25,14 @@
 // The epilogue turns the five sums into one 64-bit fixed-point integer and that into the FP64
 // value exactly rounded, with integer instructions only (GB300's FP64 pipe is 1/64 of FP32).
 //
-// Work split (one persistent CTA per SM, 416 threads):
-//   warps 0-3   epilogue: per tile the residual (float pairs, atomic adds); per chunk tensor
-//               memory -> FP64 entries -> atomic adds into the CSR values
-//   warps 4-11  producers: per tile the node tables, block offsets, the tile's Gauss-point data and
-//               row scales; per 16-wide K step the seven A planes
-//   warp 12     one thread: bulk copies of the Phi planes (cp.async.bulk) and the 28 MMAs per step
+// Work split (one persistent CTA per SM, 544 threads):
+//   warps 0-7   epilogue: per tile the residual (float pairs, atomic adds); per chunk, two warps
+//               per tensor-memory lane quarter (alternate groups of 8 columns), tensor memory ->
+//               FP64 entries -> atomic adds into the CSR values
+//   warps 8-15  producers: per tile the node tables, block offsets, one bulk copy per row of the
+//               tile's Gauss-point data, the row scales; per 16-wide K step the seven A planes
+//               (two threads per row, one 8-column half each)
+//   warp 16     one thread: bulk copies of the Phi planes (cp.async.bulk) and the 28 MMAs per step
 // A tile is 14 elements (126 of the 128 MMA rows); the 210 node pairs of a 20-node tet run as
 // three 80-column chunks (five accumulators of 80 columns fit the 512 tensor-memory columns),
 // each chunk re-deriving the A planes. Every wait is bounded: a timeout sets FL_FLAG_TIMEOUT,
@@ -58,8 +60,10 @@ constexpr int RT_B_PLANE = RT_NB * 16 * 2;
 constexpr int RT_A_BYTES = RT_DIG * RT_A_PLANE;           // 28 672
 constexpr int RT_B_BYTES = RT_DIG * RT_B_PLANE;           // 17 920
 constexpr int RT_STAGE = RT_A_BYTES + RT_B_BYTES;
-constexpr int RT_NPROD = 256;             // producer threads
-constexpr int RT_THREADS = 128 + RT_NPROD + 32;
+constexpr int RT_NEPI = 256;              // epilogue threads: two warps per tensor-memory lane quarter
+constexpr int RT_NPROD = 256;             // producer threads: two per A row
+constexpr int RT_THREADS = RT_NEPI + RT_NPROD + 32;
+constexpr int RT_MMA_WARP = (RT_NEPI + RT_NPROD) / 32;
 constexpr int RT_MAX_NQ = 15;             // the tile's Gauss-point data must fit in shared memory
 constexpr long long RT_WAIT_LIMIT = 1ll << 23;
 constexpr int RT_MAXCOLS = 256;           // pair columns of the largest element type taken (20 nodes: 240)
@@ -129,6 +133,13 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 }
 
 __device__ __forceinline__ void producers_sync() { asm volatile("bar.sync 1, 256;\n" ::: "memory"); }
+
+// 8 consecutive FP32 columns of this warp's 32 lanes, no wait
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+                 : "r"(taddr));
+}
 
 // 16 consecutive FP32 columns of this warp's 32 lanes, no wait
 __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
@@ -203,7 +214,7 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
     // accumulators are complete / were read out; tblf / tble: a tile's tables are written / no
     // longer needed; fin: every MMA issued has completed
     __shared__ __align__(8) uint64_t fullA[RT_NST], fullB[RT_NST], empty_bar[RT_NST], accf_bar, acce_bar,
-        tblf_bar[2], tble_bar[2], rdone_bar, fin_bar;
+        tblf_bar[2], tble_bar[2], rdone_bar, stage_bar, fin_bar;
     __shared__ uint32_t taddr_s;
     __shared__ volatile int s_abort;
     __shared__ int s_flag;
@@ -221,17 +232,18 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
 
     if (tid == 0) {
         for (int s = 0; s < RT_NST; ++s) {
-            tc::mbar_init(&fullA[s], 8);
+            tc::mbar_init(&fullA[s], RT_NPROD / 32);
             tc::mbar_init(&fullB[s], 1);
             tc::mbar_init(&empty_bar[s], 1);
         }
         tc::mbar_init(&accf_bar, 1);
-        tc::mbar_init(&acce_bar, 4);
+        tc::mbar_init(&acce_bar, RT_NEPI / 32);
         for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(&tblf_bar[b], 8);
-            tc::mbar_init(&tble_bar[b], 4);
+            tc::mbar_init(&tblf_bar[b], RT_NPROD / 32);
+            tc::mbar_init(&tble_bar[b], RT_NEPI / 32);
         }
-        tc::mbar_init(&rdone_bar, 4);  // the epilogue warps read the tile's residual factors
+        tc::mbar_init(&rdone_bar, RT_NEPI / 32);  // the epilogue warps read the tile's residual factors
+        tc::mbar_init(&stage_bar, 1);  // the tile's Gauss-point data landed (bulk copy bytes)
         tc::mbar_init(&fin_bar, 1);
         s_abort = 0;
         s_flag = 0;
@@ -254,22 +266,47 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
             row_off[tid][de] = (int16_t)(tid < 9 * RT_EPT ? rt_sym9(3 * i + de / 3, 3 * k + de % 3) * TQ + el * nq : 0);
     }
     for (int n = tid; n < 3 * NPE * nq; n += RT_THREADS) jms[n] = R.jmp[n];
-    if (warp == 12) tc::tmem_alloc(&taddr_s, RT_TMEM_COLS);
+    if (warp == RT_MMA_WARP) tc::tmem_alloc(&taddr_s, RT_TMEM_COLS);
     tc::fence_before_sync();
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t taddr = taddr_s;
     int flag = 0;
 
-    if (warp >= 4 && warp < 12) {
+    if (warp >= RT_NEPI / 32 && warp < RT_MMA_WARP) {
         // ---------------------------------------------------------------------------- producers
-        const int p = tid - 128;
+        const int p = tid - RT_NEPI;
+        bool stage_pending = false;  // (thread p == 0) a bulk copy of tile data not yet waited for
+        uint32_t stage_parity = 0;
         int64_t gs = 0;
         for (int64_t it = 0; it < mine && !s_abort; ++it) {
             const int64_t tile = blockIdx.x + it * (int64_t)gridDim.x;
             const int buf = (int)(it & 1);
             const int64_t el0 = tile * RT_EPT;  // chunk-local index of the tile's first element
             RtTables<NPE> &tb = tables[buf];
+            // the tile data are overwritten once the epilogue has formed the previous tile's residual
+            if (it >= 1 && !rt_wait(&rdone_bar, (uint32_t)((it - 1) & 1), &s_abort)) break;
+            producers_sync();  // every producer is past the previous tile's K steps
+            // the tile's Gauss-point data: 108 rows (tangent hi, lo; residual factor hi, lo) of TQ
+            // floats; as one bulk copy per row when the rows are 16-byte aligned (an even number of
+            // Gauss points), overlapping the table loads, else with plain loads
+            const int64_t c0 = el0 * nq, cend = R.ne * nq;
+            auto row_src = [&](int row) -> const float * {
+                return row < 45 ? R.Qh + (size_t)row * R.ldq
+                       : row < 90 ? R.Ql + (size_t)(row - 45) * R.ldq
+                                  : R.Sp + (size_t)(row - 90) * R.ldq;
+            };
+            const bool bulk = (TQ & 3) == 0;
+            if (bulk && p == 0) {
+                const int64_t avail = R.ldq - c0;  // the rows' floats from c0 to the end of the row
+                const uint32_t nb = (uint32_t)((avail < TQ ? avail : TQ) * 4) & ~15u;
+                tc::fence_async_smem();  // the previous tile's generic reads of the buffer come first
+                mbar_arrive_tx(&stage_bar, 108u * nb);
+                if (nb)
+                    for (int row = 0; row < 108; ++row) bulk_g2s(AH + (size_t)row * TQ, row_src(row) + c0, nb, &stage_bar);
+                stage_pending = true;
+                stage_parity = (uint32_t)(it & 1);
+            }
             if (it >= 2 && !rt_wait(&tble_bar[buf], (uint32_t)(((it - 2) >> 1) & 1), &s_abort)) break;
             for (int idx = p; idx < RT_EPT * NPE; idx += RT_NPROD) {
                 const int64_t e = el0 + idx / NPE;
@@ -294,52 +331,28 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                 if (e < R.ne) v = R.boff[(R.e0 + e) * (NPE * NPE) + idx % (NPE * NPE)];
                 tb.boff[idx] = (int16_t)(v >= 0 && v < 32768 ? v : -1);
             }
-            // the tile data are overwritten once the epilogue has formed the previous tile's residual
-            if (it >= 1 && !rt_wait(&rdone_bar, (uint32_t)((it - 1) & 1), &s_abort)) break;
-            producers_sync();  // every producer is past the previous tile's K steps
-            {
-                // the tile's Gauss-point data: 108 rows (tangent hi, lo; residual factor hi, lo) of
-                // TQ floats, with 16-byte loads where the rows allow them
-                const int64_t c0 = el0 * nq, cend = R.ne * nq;
-                auto row_src = [&](int row) -> const float * {
-                    return row < 45 ? R.Qh + (size_t)row * R.ldq
-                           : row < 90 ? R.Ql + (size_t)(row - 45) * R.ldq
-                                      : R.Sp + (size_t)(row - 90) * R.ldq;
-                };
-                if ((TQ & 3) == 0) {
-                    const int q4 = TQ / 4;
-                    for (int idx = p; idx < 108 * q4; idx += RT_NPROD) {
-                        const int row = idx / q4, c = 4 * (idx % q4);
-                        const float *src = row_src(row);
-                        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-                        if (c0 + c + 3 < cend) {
-                            v = __ldg(reinterpret_cast<const float4 *>(src + c0 + c));
-                        } else {
-                            if (c0 + c < cend) v.x = src[c0 + c];
-                            if (c0 + c + 1 < cend) v.y = src[c0 + c + 1];
-                            if (c0 + c + 2 < cend) v.z = src[c0 + c + 2];
-                        }
-                        *reinterpret_cast<float4 *>(AH + (size_t)row * TQ + c) = v;
-                    }
-                } else {
-                    for (int idx = p; idx < 108 * TQ; idx += RT_NPROD) {
-                        const int row = idx / TQ, c = idx % TQ;
-                        AH[idx] = c0 + c < cend ? row_src(row)[c0 + c] : 0.f;
-                    }
+            if (bulk) {
+                if (!rt_wait(&stage_bar, (uint32_t)(it & 1), &s_abort)) break;
+                if (p == 0) stage_pending = false;
+            } else {
+                for (int idx = p; idx < 108 * TQ; idx += RT_NPROD) {
+                    const int row = idx / TQ, c = idx % TQ;
+                    AH[idx] = c0 + c < cend ? row_src(row)[c0 + c] : 0.f;
                 }
             }
             producers_sync();
-            {   // row scales: the largest |hi| of each row over (g, d, e), two threads per row
-                const int r = p >> 1, half = p & 1;
+            {   // row scales: the largest |hi| of each row over (g, d, e), RT_NPROD / 128 threads per row
+                constexpr int TPR = RT_NPROD / RT_M;
+                const int r = p / TPR, hf = p % TPR;
                 float mx = 0.f;
                 if (r < 9 * RT_EPT)
-                    for (int de = half ? 5 : 0; de < (half ? 9 : 5); ++de) {
+                    for (int de = hf; de < 9; de += TPR) {
                         const float *src = AH + row_off[r][de];
 #pragma unroll 2
                         for (int g = 0; g < nq; ++g) mx = fmaxf(mx, fabsf(src[g]));
                     }
-                mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
-                if (half == 0) {
+                if (TPR == 2) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, 1));
+                if (hf == 0) {
                     int E;
                     float sc;
                     rt_row_scale(mx, E, sc);
@@ -350,7 +363,8 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
             producers_sync();  // row scales visible to every producer
             if (lane == 0) mbar_arrive(&tblf_bar[buf]);
             // A planes, chunk by chunk (the same planes for every chunk of the tile)
-            const int r = p & (RT_M - 1), kg = p >> 7;
+            const int r = p & (RT_M - 1);  // the row; its 8-column halves of each K step from kg0 by KGS
+            const int kg0 = p / RT_M, KGS = RT_NPROD / RT_M;
             const int el = r / 9;
             const bool rowok = r < 9 * RT_EPT && el0 + el < R.ne;
             const float sc = rowok ? rsc[r] : 0.f;
@@ -359,6 +373,8 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                     const int s = (int)(gs % RT_NST);
                     const int64_t u = gs / RT_NST;
                     if (u > 0 && !rt_wait(&empty_bar[s], (uint32_t)((u - 1) & 1), &s_abort)) break;
+#pragma unroll 1
+                    for (int kg = kg0; kg < 2; kg += KGS) {
                     float dg[8][RT_DIG];
 #pragma unroll
                     for (int q = 0; q < 8; ++q) {
@@ -378,12 +394,16 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                                                    pack_bf16(dg[4][t], dg[5][t]), pack_bf16(dg[6][t], dg[7][t]));
                         *reinterpret_cast<uint4 *>(ab + (size_t)t * RT_A_PLANE) = w;
                     }
+                    }
                     tc::fence_async_smem();
                     __syncwarp();
                     if (lane == 0) mbar_arrive(&fullA[s]);
                 }
         }
-    } else if (warp == 12) {
+        // an aborted run can leave a bulk copy of tile data in flight: wait for it (bounded) before
+        // the CTA's shared memory is released
+        if (stage_pending) tc::mbar_wait(&stage_bar, stage_parity, RT_WAIT_LIMIT);
+    } else if (warp == RT_MMA_WARP) {
         // ---------------------------------------------------------------------------- MMA issue
         if (lane == 0 && total_steps > 0) {
             const uint32_t idesc = tc::idesc_bf16_f32(RT_M, RT_NB);
@@ -442,9 +462,12 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
         }
     } else {
         // ---------------------------------------------------------------------------- epilogue
-        const int r = tid;  // warp w reads tensor-memory lanes 32 w .. 32 w + 31
+        // warp w reads tensor-memory lanes 32 (w % 4) .. + 31 (its rows) and the column groups of 8
+        // whose index has the parity w / 4
+        const int quarter = warp & 3, half = warp >> 2;
+        const int r = 32 * quarter + lane;
         const int el = r / 9, i = (r % 9) / 3, k = r % 3;
-        const uint32_t trow = taddr + ((uint32_t)(32 * warp) << 16);
+        const uint32_t trow = taddr + ((uint32_t)(32 * quarter) << 16);
         int64_t cc = 0;
         for (int64_t it = 0; it < mine && !s_abort; ++it) {
             const int64_t tile = blockIdx.x + it * (int64_t)gridDim.x;
@@ -452,7 +475,7 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
             const RtTables<NPE> &tb = tables[buf];
             if (!rt_wait(&tblf_bar[buf], (uint32_t)((it >> 1) & 1), &s_abort)) break;
             if (R.update) {  // residual t[(a,i)] = sum_g sum_d Jm[d][a][g] S_g[i][d] in float pairs
-                for (int idx = tid; idx < RT_EPT * NPE * 3; idx += 128) {
+                for (int idx = tid; idx < RT_EPT * NPE * 3; idx += RT_NEPI) {
                     const int re = idx / (NPE * 3), a = (idx % (NPE * 3)) / 3, ri = idx % 3;
                     const int node = tb.nodes[re * NPE + a];
                     if (tile * RT_EPT + re >= R.ne || node < 0) continue;
@@ -479,13 +502,13 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                 }
                 tc::fence_after_sync();
 #pragma unroll 1
-                for (int cg = 0; cg < RT_NB / 16; ++cg) {
-                    uint32_t v[RT_NACC][16];
+                for (int cg = half; cg < RT_NB / 8; cg += 2) {
+                    uint32_t v[RT_NACC][8];
 #pragma unroll
                     for (int L = 0; L < RT_NACC; ++L)
-                        tmem_ld16_nowait(trow + (uint32_t)(L * RT_ACCSTRIDE + 16 * cg), v[L]);
+                        tmem_ld8_nowait(trow + (uint32_t)(L * RT_ACCSTRIDE + 8 * cg), v[L]);
                     tmem_wait_ld();
-                    if (cg == RT_NB / 16 - 1) {  // the chunk's accumulators are read: release them
+                    if (cg + 2 >= RT_NB / 8) {  // this warp's last columns of the chunk are read
                         tc::fence_before_sync();
                         __syncwarp();
                         if (lane == 0) mbar_arrive(&acce_bar);
@@ -493,8 +516,8 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
                     if (!rv) continue;
                     const int64_t nnz = s_nnz;
 #pragma unroll
-                    for (int jj = 0; jj < 16; ++jj) {
-                        const int n = c * RT_NB + cg * 16 + jj;
+                    for (int jj = 0; jj < 8; ++jj) {
+                        const int n = c * RT_NB + cg * 8 + jj;
                         if (n >= P) continue;
                         const int a = pair_a[n], b = pair_b[n];
                         const int na = tb.nodes[el * NPE + a], nb = tb.nodes[el * NPE + b];
@@ -528,7 +551,7 @@ __global__ void __launch_bounds__(RT_THREADS, 1) rt_contract_kernel(const RtArgs
     __syncthreads();
     tc::fence_after_sync();
     if (tid == 0 && (s_flag || s_abort) && R.flags) atomicOr(R.flags, s_flag | (s_abort ? FL_FLAG_TIMEOUT : 0));
-    if (warp == 12) tc::tmem_dealloc(taddr, RT_TMEM_COLS);
+    if (warp == RT_MMA_WARP) tc::tmem_dealloc(taddr, RT_TMEM_COLS);
 }
 
 // Phi digit planes: one block per pair column n (all NCH * 80, padding columns zero), FP64

@@ -34,6 +34,16 @@ def pcg_value_mode(V, spmv="split"):
     return N.FL_PCG_F64_SPLIT if spmv == "split" else N.FL_PCG_F64
 
 
+def set_pcg_device_loop(enable=True):
+    """PCG iterations as one CUDA graph with a device-side loop (the default), or launched from the
+    host with a convergence poll every 16 iterations."""
+    N.check(N.lib().fl_SetPCGDeviceLoop(1 if enable else 0), "fl_SetPCGDeviceLoop")
+
+
+def get_pcg_device_loop():
+    return bool(N.lib().fl_GetPCGDeviceLoop())
+
+
 def pcg_workspace(asm, V, spmv="split"):
     L = N.lib()
     size = L.fl_BlockJacobiPCG_workspace_size(asm.nnode * 3, asm.nnz, pcg_value_mode(V, spmv))

@@ -427,9 +427,14 @@ int fl_StrainEnergy(const double *points, const uint64_t *elements, const double
  *   stop when |r| <= rtol |b| (free dofs) or after maxiter iterations; iterations and relres
  *   (host out) report where it stopped. workspace: fl_BlockJacobiPCG_workspace_size(nrows, nnz,
  *   value_bits) bytes.
- * Synchronises the stream every 16 iterations to test convergence. FL_ERR_ARG on a missing or
- * singular diagonal block or a non-finite residual.
+ * The iterations run on the device as one CUDA graph: a conditional WHILE node whose body is one
+ * iteration (three kernels and a one-thread tail that tests convergence and sets the loop
+ * condition), so the host waits once per solve. With fl_SetPCGDeviceLoop(0), or where the graph
+ * cannot be built, the host launches the iterations and synchronises every 16 of them to test
+ * convergence. FL_ERR_ARG on a missing or singular diagonal block or a non-finite residual.
  * ------------------------------------------------------------------------------------------ */
+int fl_SetPCGDeviceLoop(int enable);
+int fl_GetPCGDeviceLoop(void);
 #define FL_PCG_F64 64
 #define FL_PCG_F32 32
 #define FL_PCG_F64_SPLIT 6432
@@ -444,6 +449,9 @@ int fl_StrainEnergy(const double *points, const uint64_t *elements, const double
  *   the high-order elements, or its transpose, the restriction).
  * fl_MaskedMatVec: y = K_ff x on the rows of an FP64 CSR matrix, rows and columns of fixed dofs
  *   (fixed[dof] != 0) masked; with b non-NULL y = b - K_ff x instead (y = 0 on fixed rows).
+ * fl_MaskedMatVecBlocks: the same product for a node-blocked pattern (the three rows of a node list
+ *   the same nodes, three columns each: every assembled tangent's pattern), one warp per node and
+ *   one column index per 3x3 block; x must be zero on fixed dofs.
  * fl_BlockJacobiInverse: Binv[n][9] = inverse of each node's 3x3 diagonal block, fixed rows and
  *   columns replaced by the identity (FL_FLAG_BAD_INDEX in flags for a missing or singular block).
  * fl_BlockJacobiApply: z (=, or +=) omega Binv r per node, 0 on fixed dofs.
@@ -461,6 +469,8 @@ int fl_NodalTransfer(int64_t nrows, const int32_t *ptr, const int32_t *cols, con
                      double *y, int accumulate, fl_stream_t stream);
 int fl_MaskedMatVec(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
                     const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
+int fl_MaskedMatVecBlocks(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
+                          const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
 int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nnode,
                           const int8_t *fixed, double *Binv, int *flags, fl_stream_t stream);
 int fl_BlockJacobiApply(int64_t nnode, const double *Binv, const int8_t *fixed, double omega, const double *r,

@@ -50,6 +50,33 @@ def test_pcg_matches_direct_solve(small_beam, spmv):
     assert rel_fro(xg[free], xr) < 1e-8
 
 
+@pytest.mark.parametrize("spmv", ["fp64", "split"])
+def test_pcg_device_loop_matches_host_loop(small_beam, spmv):
+    """The iterations as one CUDA graph (conditional WHILE node, the default) and launched from the
+    host with a poll every 16 iterations: the same kernels in the same order, so the same
+    iteration count (up to the order of the FP64 atomic adds of the dot products' block sums) and
+    the same solution; and the maximum-iteration stop holds in the device loop (a count that is
+    not a multiple of the host's poll interval)."""
+    from florence_gb300.newton import get_pcg_device_loop, pcg, set_pcg_device_loop
+    P, el, Jm, w, fixed, f = small_beam
+    asm = _asm(P, el, Jm, w)
+    V, _ = asm.assemble(torch.from_numpy(P).cuda())
+    n = P.shape[0] * 3
+    b = torch.from_numpy(np.where(fixed, 0.0, np.random.default_rng(7).standard_normal(n))).cuda()
+    fx = torch.from_numpy(fixed.astype(np.int8)).cuda()
+    assert get_pcg_device_loop()
+    xd, itd, reld = pcg(asm, V, b, fx, rtol=1e-10, maxiter=20000, spmv=spmv)
+    try:
+        set_pcg_device_loop(False)
+        xh, ith, relh = pcg(asm, V, b, fx, rtol=1e-10, maxiter=20000, spmv=spmv)
+    finally:
+        set_pcg_device_loop(True)
+    assert abs(itd - ith) <= 2 and itd > 16 and reld <= 1e-10 and relh <= 1e-10
+    assert rel_fro(xd.cpu().numpy(), xh.cpu().numpy()) < 1e-8
+    x7, it7, rel7 = pcg(asm, V, b, fx, rtol=1e-30, maxiter=37, spmv=spmv)
+    assert it7 == 37 and rel7 > 1e-10
+
+
 def test_pcg_zero_rhs_returns_immediately(small_beam):
     from florence_gb300.newton import pcg
     P, el, Jm, w, fixed, f = small_beam
