@@ -531,7 +531,8 @@ def run_newton(args):
     pat = meshes.local_pattern(g["points"], g["elements"], 0, "tet")
     tangents = {"both": ["fp64", "mixed"], "all": ["fp64", "mixed", "hybrid"]}.get(args.tangent, [args.tangent])
     runs = {}
-    lin = dict(linear=args.linear, pattern=pat if args.linear == "pmg" else None)
+    linear = args.linear if args.tangent == "fp64" else "pcg"  # the p-multigrid cycle takes the FP64 tangent
+    lin = dict(linear=linear, pattern=pat if linear == "pmg" else None)
     for tg in tangents:
         # warm-up: module loading, one assembly and one short linear solve
         NewtonSolver(asm, fixed, f, n_increments=1, max_iter=1, pcg_maxiter=32, tangent=tg, spmv=args.spmv,
@@ -553,7 +554,8 @@ def run_newton(args):
     incs = [dict(increment=i["increment"], newton=i["newton_iters"],
                  pcg=[h["pcg_iters"] for h in i["history"]], rel=[h["rel"] for h in i["history"]])
             for i in out["increments"]]
-    line = dict(metric="Newton wall time to rel-res 1e-10 (10 load increments, %s tangent, device PCG)"
+    line = dict(metric=("Newton wall time to rel-res 1e-10 (10 load increments, %s tangent, "
+                        + ("flexible CG with the p-multigrid cycle)" if linear == "pmg" else "block-Jacobi PCG)"))
                        % {"fp64": "FP64", "mixed": "split-BF16 tensor-core FP32",
                           "hybrid": "split-BF16 FP32 far from the solution, FP64 near it",
                           "both": "split-BF16 tensor-core FP32 (FP64 run alongside)",
@@ -561,7 +563,7 @@ def run_newton(args):
                 value=out["wall_s"], unit="s", n_gpus=1, steps=1, warmup=1, higher_is_better=False,
                 scaling="weak", vs_baseline=None, dtype="f64", data="synthetic", tangent=args.tangent,
                 spmv=args.spmv if args.tangent != "mixed" else "fp32 values, float-pair product",
-                forcing=args.forcing, linear=args.linear,
+                forcing=args.forcing, linear=linear, pcg_loop=args.pcg_loop,
                 config=dict(workload="tet p=3 beam 4x1x1 (%dx%dx%d jittered lattice), Mooney-Rivlin mu1=mu2=0.5 "
                                      "lambda=20, x=0 clamped, traction (0,0,-0.01) on x=4" % cells,
                             nelem=int(el.shape[0]), nnode=int(P.shape[0]), nnz=int(asm.nnz)),
@@ -618,7 +620,7 @@ def run_pcg(args):
                 roofline=dict(bound="hbm", achieved=res["split"]["achieved_gbs"], peak=hbm, unit="GB/s",
                               frac=res["split"]["frac"], bytes_per_iter=nbytes,
                               peak_source="MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"),
-                split=res["split"], fp64=res["fp64"], clocks=res["split"]["clocks"])
+                split=res["split"], fp64=res["fp64"], clocks=res["split"]["clocks"], pcg_loop=args.pcg_loop)
     print(json.dumps(line), flush=True)
 
 
@@ -1040,9 +1042,11 @@ def main():
                     help="PCG tolerance per Newton step: Eisenstat-Walker, or 0.1 x relative residual")
     ap.add_argument("--spmv", default="split", choices=["split", "fp64"],
                     help="PCG product for FP64 tangents: float-pair split on the FP32 pipe, or FP64")
-    ap.add_argument("--linear", default="pcg", choices=["pcg", "pmg"],
-                    help="Newton's linear step: block-Jacobi PCG, or flexible CG with the two-level p-multigrid "
-                         "cycle (FP64 tangent)")
+    ap.add_argument("--linear", default="pmg", choices=["pcg", "pmg"],
+                    help="Newton's linear step: flexible CG with the two-level p-multigrid cycle (the default; FP64 "
+                         "tangent), or block-Jacobi PCG (any tangent)")
+    ap.add_argument("--pcg-loop", default="device", choices=["device", "host"],
+                    help="PCG iterations as one CUDA graph with a device-side loop, or launched from the host")
     ap.add_argument("--pcg", action="store_true", help="PCG iterations on the beam's tangent instead")
     ap.add_argument("--pcg-iters", type=int, default=400)
     ap.add_argument("--batched", action="store_true", help="batched uneven instances instead")
@@ -1059,6 +1063,9 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.pcg_loop == "host" and args.impl != "reference":
+        from florence_gb300.newton import set_pcg_device_loop
+        set_pcg_device_loop(False)
     if args.impl == "reference":
         run_reference(args)
     elif args.newton:

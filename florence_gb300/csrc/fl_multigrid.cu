@@ -12,6 +12,7 @@
 // Dirichlet dofs masked (the system K_ff that Newton solves) and the 3x3 nodal block-Jacobi
 // inverse, the same blocks the device PCG uses.
 #include <algorithm>
+#include <type_traits>
 
 #include "fl_common.cuh"
 
@@ -67,9 +68,11 @@ __global__ void __launch_bounds__(MG_NT) masked_spmv_kernel(const int32_t *indpt
 // The same product on a node-blocked pattern (the three rows of a node list the same nodes, three
 // columns each, as every assembled tangent's pattern does): one warp per node, lanes over its
 // column blocks, nine values and one column index per block. x must be zero on fixed dofs (the
-// columns are then masked by x itself); fixed rows give 0 (or nothing subtracted from b).
+// columns are then masked by x itself); fixed rows give 0 (or nothing subtracted from b). With
+// FP32 values (a smoother's copy of the tangent) the products and sums run on the FP32 pipe.
+template <class VT>
 __global__ void __launch_bounds__(MG_NT) masked_spmv_blocks_kernel(const int32_t *indptr, const int32_t *indices,
-                                                                   const double *vals, int64_t nnode,
+                                                                   const VT *vals, int64_t nnode,
                                                                    const int8_t *fixed, const double *x,
                                                                    const double *b, double *y, int64_t ncols) {
     const int lane = threadIdx.x & 31;
@@ -80,20 +83,40 @@ __global__ void __launch_bounds__(MG_NT) masked_spmv_blocks_kernel(const int32_t
         const int p0 = indptr[r0], p1 = indptr[r0 + 1], p2 = indptr[r0 + 2];
         const int nb = (p1 - p0) / 3;
         double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+        float f0 = 0.f, f1 = 0.f, f2 = 0.f;
         for (int blk = lane; blk < nb; blk += 32) {
             const int c = indices[p0 + 3 * blk];
             if (c < 0 || c + 2 >= ncols) continue;
             const double x0 = x[c], x1 = x[c + 1], x2 = x[c + 2];
-            const double *v0 = vals + p0 + 3 * blk, *v1 = vals + p1 + 3 * blk, *v2 = vals + p2 + 3 * blk;
-            a0 = fma(v0[0], x0, fma(v0[1], x1, fma(v0[2], x2, a0)));
-            a1 = fma(v1[0], x0, fma(v1[1], x1, fma(v1[2], x2, a1)));
-            a2 = fma(v2[0], x0, fma(v2[1], x1, fma(v2[2], x2, a2)));
+            const VT *v0 = vals + p0 + 3 * blk, *v1 = vals + p1 + 3 * blk, *v2 = vals + p2 + 3 * blk;
+            if constexpr (std::is_same<VT, float>::value) {  // FP32 values: the sums in FP32 too
+                const float y0 = (float)x0, y1 = (float)x1, y2 = (float)x2;
+                f0 = fmaf(v0[0], y0, fmaf(v0[1], y1, fmaf(v0[2], y2, f0)));
+                f1 = fmaf(v1[0], y0, fmaf(v1[1], y1, fmaf(v1[2], y2, f1)));
+                f2 = fmaf(v2[0], y0, fmaf(v2[1], y1, fmaf(v2[2], y2, f2)));
+            } else {
+                a0 = fma(v0[0], x0, fma(v0[1], x1, fma(v0[2], x2, a0)));
+                a1 = fma(v1[0], x0, fma(v1[1], x1, fma(v1[2], x2, a1)));
+                a2 = fma(v2[0], x0, fma(v2[1], x1, fma(v2[2], x2, a2)));
+            }
         }
+        if constexpr (std::is_same<VT, float>::value) {
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            a0 += __shfl_down_sync(0xffffffffu, a0, o);
-            a1 += __shfl_down_sync(0xffffffffu, a1, o);
-            a2 += __shfl_down_sync(0xffffffffu, a2, o);
+            for (int o = 16; o > 0; o >>= 1) {
+                f0 += __shfl_down_sync(0xffffffffu, f0, o);
+                f1 += __shfl_down_sync(0xffffffffu, f1, o);
+                f2 += __shfl_down_sync(0xffffffffu, f2, o);
+            }
+            a0 = f0;
+            a1 = f1;
+            a2 = f2;
+        } else {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a0 += __shfl_down_sync(0xffffffffu, a0, o);
+                a1 += __shfl_down_sync(0xffffffffu, a1, o);
+                a2 += __shfl_down_sync(0xffffffffu, a2, o);
+            }
         }
         if (lane == 0) {
             const double a[3] = {a0, a1, a2};
@@ -163,23 +186,29 @@ static unsigned grid_of(int64_t n, int per_block) {
 
 // ------------------------------------------------------------------------------------------------
 // The coarse problem's block-Jacobi PCG in one cooperative launch. The coarse system is small
-// (three dofs per mesh vertex) and needs hundreds of iterations per cycle; as separate launches
-// each iteration would cost three kernel boundaries and a host poll, far more than its work.
-// Here every CTA stays resident (cooperative launch), the iteration's three phases are separated
-// by grid barriers, and the dot products go through rotating device slots:
-//   phase 1  q = K_ff p, p.q                         (a warp per row)
-//   phase 2  alpha = r.z / p.q; x += alpha p; r -= alpha q; z = B^-1 r; r.z, r.r   (a thread per node)
-//   phase 3  stop when r.r <= rtol^2 b.b; beta = r.z(new) / r.z(old); p = z + beta p
-// Data written by other CTAs inside the launch are read past L1 (ld.global.cg). Every barrier
-// wait is bounded: on a timeout the kernel records FL_FLAG_TIMEOUT and every CTA leaves.
+// (three dofs per mesh vertex) and needs up to a hundred iterations per cycle; as separate
+// launches each iteration would cost three kernel boundaries and a host poll, far more than its
+// work. Here every CTA stays resident (cooperative launch, one CTA per SM), an iteration is two
+// phases separated by grid barriers, and the dot products go through rotating device slots:
+//   phase 1  beta = r.z(k) / r.z(k-1); p_k = z_k + beta p_(k-1) formed on the fly where the
+//            product gathers it (and stored by the owner of each node); q = K_ff p_k; p_k.q
+//            (8 lanes per node of a node-blocked pattern)
+//   phase 2  alpha = r.z / p.q; x += alpha p; r -= alpha q; z = B^-1 r; r.z, r.r  (a thread per node)
+//   then     stop when r.r <= rtol^2 b.b
+// p alternates between two buffers (iteration k writes p_k while others still gather p_(k-1)).
+// Data written by other CTAs inside the launch are read past L1 (ld.global.cg); the barrier is
+// an arrival counter (release) and a generation word (acquire). Every barrier wait is bounded: on
+// a timeout the kernel records FL_FLAG_TIMEOUT and every CTA leaves.
 constexpr int CG_NT = 512;
+constexpr int CG_LPN = 8;  // lanes per node in the product
 constexpr long long CG_SPIN_LIMIT = 1ll << 24;
 
 struct CgArgs {
     const int32_t *indptr, *indices;
     const double *vals, *Binv, *b;
     const int8_t *fixed;
-    double *x, *r, *z, *p, *q;
+    double *x, *r, *z, *q;
+    double *pb[2];       // p_k in pb[k & 1]
     double *sc;          // [0..2] p.q, [3..5] r.z, [6..8] r.r (rotating by iteration), [9] b.b
     unsigned *bar;       // [0] arrivals, [1] generation
     int *abort_flag;     // set by a CTA whose barrier wait timed out
@@ -205,27 +234,38 @@ __device__ __forceinline__ double cg_block_sum(double v, double *red) {
     return t;  // in thread 0
 }
 
-// grid barrier (arrival counter + generation); false when a wait timed out here or elsewhere
+__device__ __forceinline__ unsigned cg_arrive(unsigned *count) {
+    unsigned old;
+    asm volatile("atom.add.release.gpu.u32 %0, [%1], 1;\n" : "=r"(old) : "l"(count) : "memory");
+    return old;
+}
+__device__ __forceinline__ unsigned cg_load_acquire(const unsigned *p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void cg_store_release(unsigned *p, unsigned v) {
+    asm volatile("st.release.gpu.u32 [%0], %1;\n" ::"l"(p), "r"(v) : "memory");
+}
+
+// grid barrier; false when a wait timed out here or elsewhere. The CTA's writes before it (ordered
+// by bar.sync, then released by thread 0's arrival) are visible to every CTA after it.
 __device__ bool cg_barrier(const CgArgs &a, unsigned &gen, volatile int *s_abort) {
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        if (atomicAdd(&a.bar[0], 1u) == gridDim.x - 1) {
-            atomicExch(&a.bar[0], 0u);
-            __threadfence();
-            atomicExch(&a.bar[1], gen + 1);
+        if (cg_arrive(&a.bar[0]) == gridDim.x - 1) {
+            a.bar[0] = 0;                       // ordered before the release below
+            cg_store_release(&a.bar[1], gen + 1);
         } else {
             long long t = 0;
-            while (*(volatile unsigned *)&a.bar[1] == gen) {
-                if (*(volatile int *)a.abort_flag) break;
-                if (++t > CG_SPIN_LIMIT) {
+            while (cg_load_acquire(&a.bar[1]) == gen) {
+                if (++t > CG_SPIN_LIMIT || ((t & 255) == 0 && *(volatile int *)a.abort_flag)) {
                     atomicExch(a.abort_flag, 1);
                     break;
                 }
-                __nanosleep(32);
+                __nanosleep(20);
             }
         }
-        __threadfence();
         ++gen;
         *s_abort = *(volatile int *)a.abort_flag;
     }
@@ -244,7 +284,7 @@ __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
     if (threadIdx.x == 0) s_abort = 0;
     __syncthreads();
     double *sc = a.sc;
-    // r = b, z = B^-1 r, p = z, x = 0 (fixed dofs 0 throughout)
+    // r = b, z = B^-1 r, x = 0, p_(-1) = 0 (fixed dofs 0 throughout)
     double rz = 0.0, bb = 0.0;
     for (int64_t m = gt; m < nnode; m += nthr) {
         double rv[3];
@@ -254,6 +294,7 @@ __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
             rv[i] = a.fixed[d] ? 0.0 : a.b[d];
             __stcg(a.r + d, rv[i]);
             __stcg(a.x + d, 0.0);
+            __stcg(a.pb[1] + d, 0.0);
             bb = fma(rv[i], rv[i], bb);
         }
         const double *B = a.Binv + m * 9;
@@ -262,7 +303,6 @@ __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
             const int64_t d = 3 * m + i;
             const double zv = a.fixed[d] ? 0.0 : fma(B[3 * i], rv[0], fma(B[3 * i + 1], rv[1], B[3 * i + 2] * rv[2]));
             __stcg(a.z + d, zv);
-            __stcg(a.p + d, zv);
             rz = fma(rv[i], zv, rz);
         }
     }
@@ -279,35 +319,66 @@ __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
     bool bad = false;
     if (b2 > 0.0)
         for (; ok && k < a.maxiter; ++k) {
-            const int s0 = (int)(k % 3), s1 = (int)((k + 1) % 3);
-            // phase 1: q = K_ff p, p.q; the slots of the next iteration are cleared
+            const int s0 = (int)(k % 3), s1 = (int)((k + 1) % 3), sm = (int)((k + 2) % 3);  // sm: k - 1
+            const double rzk = __ldcg(sc + 3 + s0);
+            const double beta = k == 0 ? 0.0 : rzk / __ldcg(sc + 3 + sm);
+            const double *pold = a.pb[(k + 1) & 1];
+            double *pnew = a.pb[k & 1];
+            // phase 1; the slots of the next iteration are cleared
             if (gt == 0) {
                 __stcg(sc + s1, 0.0);
                 __stcg(sc + 3 + s1, 0.0);
                 __stcg(sc + 6 + s1, 0.0);
             }
+            // CG_LPN lanes per node, 32 / CG_LPN nodes per warp at once (a coarse node has ~15
+            // column blocks: one pass of dependent loads covers the whole product); warp-uniform
+            // trip count, so that every lane takes part in the shuffles
             double pq = 0.0;
-            for (int64_t row = gwarp; row < a.n; row += nwarps) {
-                double acc = 0.0;
-                const bool fr = a.fixed[row] != 0;
-                if (!fr)
-                    for (int j = a.indptr[row] + lane; j < a.indptr[row + 1]; j += 32) {
-                        const int c = a.indices[j];
-                        if (!a.fixed[c]) acc = fma(a.vals[j], __ldcg(a.p + c), acc);
-                    }
+            for (int64_t base = gwarp * (32 / CG_LPN); base < nnode; base += nwarps * (32 / CG_LPN)) {
+                const int64_t m = base + lane / CG_LPN;
+                const int sub = lane & (CG_LPN - 1);
+                const bool valid = m < nnode;
+                const int64_t r0 = 3 * m;
+                int j0 = 0, j1 = 0, j2 = 0, nb = 0;
+                if (valid) {
+                    j0 = a.indptr[r0];
+                    j1 = a.indptr[r0 + 1];
+                    j2 = a.indptr[r0 + 2];
+                    nb = (j1 - j0) / 3;
+                }
+                double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+                for (int blk = sub; blk < nb; blk += CG_LPN) {
+                    const int c = a.indices[j0 + 3 * blk];
+                    if (c < 0 || c + 2 >= a.n) continue;
+                    const double x0 = fma(beta, __ldcg(pold + c), __ldcg(a.z + c));
+                    const double x1 = fma(beta, __ldcg(pold + c + 1), __ldcg(a.z + c + 1));
+                    const double x2 = fma(beta, __ldcg(pold + c + 2), __ldcg(a.z + c + 2));
+                    const double *v0 = a.vals + j0 + 3 * blk, *v1 = a.vals + j1 + 3 * blk, *v2 = a.vals + j2 + 3 * blk;
+                    a0 = fma(__ldg(v0), x0, fma(__ldg(v0 + 1), x1, fma(__ldg(v0 + 2), x2, a0)));
+                    a1 = fma(__ldg(v1), x0, fma(__ldg(v1 + 1), x1, fma(__ldg(v1 + 2), x2, a1)));
+                    a2 = fma(__ldg(v2), x0, fma(__ldg(v2 + 1), x1, fma(__ldg(v2 + 2), x2, a2)));
+                }
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-                if (lane == 0) {
-                    acc = fr ? 0.0 : acc;
-                    __stcg(a.q + row, acc);
-                    pq = fma(__ldcg(a.p + row), acc, pq);
+                for (int o = CG_LPN / 2; o > 0; o >>= 1) {
+                    a0 += __shfl_xor_sync(0xffffffffu, a0, o);
+                    a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+                    a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+                }
+                if (valid && sub < 3) {  // lane sub of the group finishes row 3m + sub
+                    const int64_t d = r0 + sub;
+                    const double av = sub == 0 ? a0 : sub == 1 ? a1 : a2;
+                    const double pv = fma(beta, __ldcg(pold + d), __ldcg(a.z + d));  // 0 on fixed dofs
+                    const double qv = a.fixed[d] ? 0.0 : av;
+                    __stcg(pnew + d, pv);
+                    __stcg(a.q + d, qv);
+                    pq = fma(pv, qv, pq);
                 }
             }
             pq = cg_block_sum(pq, red);
             if (threadIdx.x == 0) atomicAdd(sc + s0, pq);
             if (!(ok = cg_barrier(a, gen, &s_abort))) break;
             // phase 2
-            const double pqk = __ldcg(sc + s0), rzk = __ldcg(sc + 3 + s0);
+            const double pqk = __ldcg(sc + s0);
             if (!(pqk > 0.0) || !isfinite(pqk)) {  // K_ff not positive definite on p (or no progress)
                 bad = true;
                 break;
@@ -319,8 +390,7 @@ __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
                     const int64_t d = 3 * m + i;
-                    const double pv = __ldcg(a.p + d);
-                    __stcg(a.x + d, fma(alpha, pv, __ldcg(a.x + d)));
+                    __stcg(a.x + d, fma(alpha, __ldcg(pnew + d), __ldcg(a.x + d)));
                     rv[i] = fma(-alpha, __ldcg(a.q + d), __ldcg(a.r + d));
                     __stcg(a.r + d, rv[i]);
                     rr1 = fma(rv[i], rv[i], rr1);
@@ -341,16 +411,12 @@ __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
                 atomicAdd(sc + 3 + s1, rz1);
                 atomicAdd(sc + 6 + s1, rr1);
             }
-            if (!(ok = cg_barrier(a, gen, &s_abort))) break;
-            // phase 3
-            rr = __ldcg(sc + 6 + s1);
-            if (rr <= a.rtol2 * b2) {
+            if (!(ok = cg_barrier(a, gen, &s_abort))) {
                 ++k;
                 break;
             }
-            const double beta = __ldcg(sc + 3 + s1) / rzk;
-            for (int64_t d = gt; d < a.n; d += nthr) __stcg(a.p + d, fma(beta, __ldcg(a.p + d), __ldcg(a.z + d)));
-            if (!(ok = cg_barrier(a, gen, &s_abort))) {
+            rr = __ldcg(sc + 6 + s1);
+            if (rr <= a.rtol2 * b2) {
                 ++k;
                 break;
             }
@@ -394,7 +460,19 @@ int fl_MaskedMatVecBlocks(const int32_t *indptr, const int32_t *indices, const d
     if (!indptr || !indices || !values || !fixed || !x || !y) return FL_ERR_ARG;
     const int64_t nnode = nrows / 3;
     const int64_t warps = std::min<int64_t>(nnode, (int64_t)152 * 64);
-    fl::masked_spmv_blocks_kernel<<<fl::grid_of(warps * 32, fl::MG_NT), fl::MG_NT, 0, (cudaStream_t)stream>>>(
+    fl::masked_spmv_blocks_kernel<double><<<fl::grid_of(warps * 32, fl::MG_NT), fl::MG_NT, 0, (cudaStream_t)stream>>>(
+        indptr, indices, values, nnode, fixed, x, b, y, nrows);
+    return fl::launch_status();
+}
+
+int fl_MaskedMatVecBlocksF32(const int32_t *indptr, const int32_t *indices, const float *values, int64_t nrows,
+                             const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream) {
+    if (nrows < 0 || nrows % 3) return FL_ERR_ARG;
+    if (nrows == 0) return FL_OK;
+    if (!indptr || !indices || !values || !fixed || !x || !y) return FL_ERR_ARG;
+    const int64_t nnode = nrows / 3;
+    const int64_t warps = std::min<int64_t>(nnode, (int64_t)152 * 64);
+    fl::masked_spmv_blocks_kernel<float><<<fl::grid_of(warps * 32, fl::MG_NT), fl::MG_NT, 0, (cudaStream_t)stream>>>(
         indptr, indices, values, nnode, fixed, x, b, y, nrows);
     return fl::launch_status();
 }
@@ -411,7 +489,7 @@ int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const d
 
 size_t fl_CoarsePCG_workspace_size(int64_t nrows) {
     if (nrows < 0) return 0;
-    return sizeof(double) * (size_t)(4 * nrows + 16) + 64;
+    return sizeof(double) * (size_t)(5 * nrows + 16) + 64;
 }
 
 int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
@@ -435,10 +513,10 @@ int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *va
         FL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fl::coarse_pcg_kernel, fl::CG_NT, 0));
         per_sm[dev & 63] = std::max(1, b);
     }
-    // enough CTAs for a warp per row, at most one per SM: every grid barrier serialises one atomic
+    // enough CTAs for a warp per node, at most one per SM: every grid barrier serialises one atomic
     // arrival per CTA, so fewer, larger CTAs make the barriers cheaper (a cooperative launch also
     // needs them all resident, which per_sm >= 1 guarantees)
-    const int64_t want = (nrows + fl::CG_NT / 32 - 1) / (fl::CG_NT / 32);
+    const int64_t want = (nrows / 3 + fl::CG_NT / 32 - 1) / (fl::CG_NT / 32);
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms[dev & 63]));
     fl::CgArgs a{};
     char *w = (char *)workspace;
@@ -448,8 +526,9 @@ int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *va
     double *v = (double *)(w + 16 * sizeof(double) + 64);
     a.r = v;
     a.z = v + nrows;
-    a.p = v + 2 * nrows;
-    a.q = v + 3 * nrows;
+    a.pb[0] = v + 2 * nrows;
+    a.pb[1] = v + 3 * nrows;
+    a.q = v + 4 * nrows;
     a.indptr = indptr;
     a.indices = indices;
     a.vals = values;

@@ -78,7 +78,7 @@ class PMultigrid:
     pattern: barycentric layout of the element's nodes [npe, 4]; fixed: Dirichlet mask [3N];
     nu: Chebyshev degree of each smoothing; coarse_rtol / coarse_maxiter: the coarse PCG."""
 
-    def __init__(self, asm, pattern, fixed, nu=2, ratio=30.0, coarse_rtol=1e-2, coarse_maxiter=500,
+    def __init__(self, asm, pattern, fixed, nu=3, ratio=30.0, coarse_rtol=0.1, coarse_maxiter=100,
                  power_iters=20):
         self.asm = asm
         dev = asm.device
@@ -100,6 +100,7 @@ class PMultigrid:
         self.Vc = torch.zeros(self.coarse.nnz, dtype=torch.float64, device=dev)
         self.Tc = torch.zeros(self.nc, dtype=torch.float64, device=dev)
         self.Binv = torch.empty((asm.nnode, 9), dtype=torch.float64, device=dev)
+        self.V32 = torch.empty(asm.nnz, dtype=torch.float32, device=dev)
         self.Binv_c = torch.empty((self.coarse.nnode, 9), dtype=torch.float64, device=dev)
         self.nu, self.ratio, self.power_iters = nu, ratio, power_iters
         self.coarse_rtol, self.coarse_maxiter = coarse_rtol, coarse_maxiter
@@ -126,6 +127,15 @@ class PMultigrid:
                 "fl_MaskedMatVecBlocks")
         return y
 
+    def smooth_matvec(self, x, y, b=None):
+        """The same product with the tangent's FP32 copy, for the smoother, the residual restricted to
+        the coarse level and the Chebyshev interval (the cycle is a preconditioner: the outer
+        iteration's products stay FP64)."""
+        N.check(N.lib().fl_MaskedMatVecBlocksF32(_ptr(self.asm.indptr), _ptr(self.asm.indices), _ptr(self.V32),
+                                                 self.n, _ptr(self.fixed), _ptr(x), _ptr(b), _ptr(y), _stream()),
+                "fl_MaskedMatVecBlocksF32")
+        return y
+
     def jacobi(self, r, z, omega=1.0, accumulate=False):
         N.check(N.lib().fl_BlockJacobiApply(self.asm.nnode, _ptr(self.Binv), _ptr(self.fixed), float(omega), _ptr(r),
                                             _ptr(z), 1 if accumulate else 0, _stream()), "fl_BlockJacobiApply")
@@ -146,6 +156,7 @@ class PMultigrid:
         """New fine tangent values V (FP64, the fine pattern) at displacement u [3N]: block
         inverses, the largest eigenvalue estimate, the coarse tangent at the vertices."""
         self.V = V
+        self.V32.copy_(V)
         N.check(N.lib().fl_BlockJacobiInverse(_ptr(self.asm.indptr), _ptr(self.asm.indices), _ptr(V), self.asm.nnode,
                                               _ptr(self.fixed), _ptr(self.Binv), _ptr(self.flags), _stream()),
                 "fl_BlockJacobiInverse")
@@ -175,7 +186,7 @@ class PMultigrid:
         rz = torch.dot(r, z)
         alphas, betas = [], []
         for _ in range(steps):
-            self.matvec(p, q)
+            self.smooth_matvec(p, q)
             alpha = rz / torch.dot(p, q)
             r.sub_(alpha * q)
             self.jacobi(r, z)
@@ -211,12 +222,12 @@ class PMultigrid:
             self.jacobi(r, d, 1.0 / theta)
             z.zero_()
         else:
-            self.matvec(z, res, b=r)
+            self.smooth_matvec(z, res, b=r)
             self.jacobi(res, d, 1.0 / theta)
         z += d
         for _ in range(1, self.nu):
             rho_new = 1.0 / (2.0 * sigma - rho)
-            self.matvec(z, res, b=r)
+            self.smooth_matvec(z, res, b=r)
             d *= rho_new * rho
             self.jacobi(res, d, 2.0 * rho_new / delta, accumulate=True)
             z += d
@@ -245,7 +256,7 @@ class PMultigrid:
         """z = M^-1 r (one cycle)."""
         self._chebyshev(r, z, first=True)
         res = torch.empty_like(r)
-        self.matvec(z, res, b=r)
+        self.smooth_matvec(z, res, b=r)
         rc = torch.empty(self.nc, dtype=torch.float64, device=self.dev)
         self.restrict(res, rc)
         rc *= (self.fixed_c == 0)

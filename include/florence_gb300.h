@@ -451,12 +451,14 @@ int fl_GetPCGDeviceLoop(void);
  *   (fixed[dof] != 0) masked; with b non-NULL y = b - K_ff x instead (y = 0 on fixed rows).
  * fl_MaskedMatVecBlocks: the same product for a node-blocked pattern (the three rows of a node list
  *   the same nodes, three columns each: every assembled tangent's pattern), one warp per node and
- *   one column index per 3x3 block; x must be zero on fixed dofs.
+ *   one column index per 3x3 block; x must be zero on fixed dofs. fl_MaskedMatVecBlocksF32: with
+ *   FP32 values (FP32 products, FP64 sums), for smoothers.
  * fl_BlockJacobiInverse: Binv[n][9] = inverse of each node's 3x3 diagonal block, fixed rows and
  *   columns replaced by the identity (FL_FLAG_BAD_INDEX in flags for a missing or singular block).
  * fl_BlockJacobiApply: z (=, or +=) omega Binv r per node, 0 on fixed dofs.
  * fl_CoarsePCG: x = the block-Jacobi PCG solution of K_ff x = b_f from x = 0 (Binv from
- *   fl_BlockJacobiInverse of the same matrix), stopped at |r| <= rtol |b_f| or after maxiter
+ *   fl_BlockJacobiInverse of the same matrix; a node-blocked pattern as fl_MaskedMatVecBlocks
+ *   takes), stopped at |r| <= rtol |b_f| or after maxiter
  *   iterations, in ONE cooperative launch (every CTA resident, grid barriers between the three
  *   phases of an iteration, bounded waits): for small systems, whose iterations would otherwise
  *   be bound by kernel boundaries. workspace: fl_CoarsePCG_workspace_size(nrows) bytes.
@@ -471,6 +473,8 @@ int fl_MaskedMatVec(const int32_t *indptr, const int32_t *indices, const double 
                     const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
 int fl_MaskedMatVecBlocks(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
                           const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
+int fl_MaskedMatVecBlocksF32(const int32_t *indptr, const int32_t *indices, const float *values, int64_t nrows,
+                             const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
 int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nnode,
                           const int8_t *fixed, double *Binv, int *flags, fl_stream_t stream);
 int fl_BlockJacobiApply(int64_t nnode, const double *Binv, const int8_t *fixed, double omega, const double *r,

@@ -1,7 +1,9 @@
 """GPU tests of the p-multigrid linear step (florence_gb300/multigrid.py): on the tet p=3 beam
 (24x6x6 lattice) the flexible CG with the two-level cycle solves the Newton system to the same
 solution as a tight block-Jacobi PCG in far fewer iterations, and Newton with it converges to
-the same displacement as Newton with the block-Jacobi PCG."""
+the same displacement as Newton with the block-Jacobi PCG; its pieces -- the node-block masked
+products (FP64 and FP32 values) against the row-wise one and scipy, and the coarse PCG in one
+cooperative launch against scipy's direct solve of the coarse system."""
 import os
 
 import numpy as np
@@ -49,3 +51,37 @@ def test_newton_with_pmg_matches_newton_with_block_jacobi(beam):
     assert not a["failed"] and not b["failed"]
     d = float(torch.linalg.vector_norm(b["u"] - a["u"]) / torch.linalg.vector_norm(a["u"]))
     assert d < 1e-7, d
+
+
+def test_node_block_products_and_coarse_solve(beam):
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    from florence_gb300.multigrid import PMultigrid
+    asm, P, fixed, f, pat = beam
+    V, _ = asm.assemble(torch.from_numpy(P).cuda())
+    mg = PMultigrid(asm, pat, fixed)
+    mg.update(V, torch.zeros(P.size, dtype=torch.float64, device="cuda"))
+    n = P.size
+    free = ~fixed.astype(bool)
+    x = torch.from_numpy(np.where(free, np.random.default_rng(3).standard_normal(n), 0.0)).cuda()
+    K = sp.csr_matrix((V.cpu().numpy(), asm.indices.cpu().numpy(), asm.indptr.cpu().numpy()), shape=(n, n))
+    ref = np.where(free, K @ x.cpu().numpy(), 0.0)
+    y = torch.empty_like(x)
+    mg.matvec(x, y)
+    assert np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref) < 1e-14
+    mg.smooth_matvec(x, y)
+    assert np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref) < 1e-5
+    # the coarse PCG (one cooperative launch) to 1e-10 against a direct solve of the coarse system
+    c = mg.coarse
+    nc = mg.nc
+    fc = mg.fixed_c.cpu().numpy().astype(bool)
+    Kc = sp.csr_matrix((mg.Vc.cpu().numpy(), c.indices.cpu().numpy(), c.indptr.cpu().numpy()), shape=(nc, nc))
+    bc = np.where(fc, 0.0, np.random.default_rng(4).standard_normal(nc))
+    mg.coarse_rtol, mg.coarse_maxiter = 1e-10, 20000
+    it0 = mg.coarse_iters
+    xc = mg.coarse_solve(torch.from_numpy(bc).cuda()).cpu().numpy()
+    mg.check_flags()
+    its = mg.coarse_iters - it0
+    xr = spla.spsolve(Kc[~fc][:, ~fc].tocsc(), bc[~fc])
+    assert 0 < its < 20000 and np.all(xc[fc] == 0.0)
+    assert np.linalg.norm(xc[~fc] - xr) / np.linalg.norm(xr) < 1e-7
