@@ -19,6 +19,7 @@ FL_FLAG_NONPOSITIVE_J = 1
 FL_FLAG_BAD_INDEX = 2
 FL_FLAG_TIMEOUT = 4
 FL_FLAG_PAIR_RANGE = 8
+FL_FLAG_CAPACITY = 16
 FL_MATERIAL_NEOHOOKEAN = 1
 FL_MATERIAL_MOONEYRIVLIN = 2
 FL_MATERIAL_NEARLYINCOMPRESSIBLEMOONEYRIVLIN = 3
@@ -120,6 +121,8 @@ def lib():
         L.fl_MaskedMatVec.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_MaskedMatVecBlocks.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_MaskedMatVecBlocksF32.argtypes = [P, P, P, I64, P, P, P, P, P]
+        L.fl_SplitPairs.argtypes = [I64, P, P, P]
+        L.fl_MaskedMatVecBlocksPair.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_BlockJacobiInverse.argtypes = [P, P, P, I64, P, P, P, P]
         L.fl_BlockJacobiApply.argtypes = [I64, P, P, D, P, P, INT, P]
         L.fl_CoarsePCG_workspace_size.argtypes = [I64]
@@ -155,5 +158,5 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_SetPCGDeviceLoop", "fl_GetPCGDeviceLoop", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
            "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_AssembleExternalTractionForces", "fl_AssembleBodyForces", "fl_MLP_num_params", "fl_MLP_workspace_size",
-           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec", "fl_MaskedMatVecBlocks", "fl_MaskedMatVecBlocksF32",
+           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec", "fl_MaskedMatVecBlocks", "fl_MaskedMatVecBlocksF32", "fl_SplitPairs", "fl_MaskedMatVecBlocksPair",
            "fl_BlockJacobiInverse", "fl_BlockJacobiApply", "fl_CoarsePCG_workspace_size", "fl_CoarsePCG"]

@@ -129,6 +129,82 @@ __global__ void __launch_bounds__(MG_NT) masked_spmv_blocks_kernel(const int32_t
     }
 }
 
+// FP64 values or vectors -> float pairs hi + lo (hi = RN(v), lo = RN(v - hi))
+__global__ void __launch_bounds__(MG_NT) split_pairs_kernel(int64_t n, const double *v, float2 *out) {
+    for (int64_t i = blockIdx.x * (int64_t)MG_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * MG_NT) {
+        const double x = v[i];
+        const float h = (float)x;
+        out[i] = make_float2(h, (float)(x - (double)h));
+    }
+}
+
+__device__ __forceinline__ void mg_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+
+// (s, c) += (vh + vl)(xh + xl): the leading product error-free by FMA, the sum compensated
+__device__ __forceinline__ void mg_pair_mac(float2 v, float2 x, float &s, float &c) {
+    const float prod = v.x * x.x;
+    const float perr = fmaf(v.x, x.x, -prod);
+    float t, e;
+    mg_two_sum(s, prod, t, e);
+    s = t;
+    c += e + perr + fmaf(v.x, x.y, v.y * x.x);
+}
+
+// The node-block product with the values and x as float pairs (~2^-44 relative), every operation
+// on the FP32 pipe: the outer iteration's product, which GB300's FP64 rate (1/64 of FP32) would
+// otherwise bound. LPN lanes per node; x zero on fixed dofs, fixed rows give 0.
+template <int LPN>
+__global__ void __launch_bounds__(MG_NT) masked_spmv_pair_kernel(const int32_t *indptr, const int32_t *indices,
+                                                                 const float2 *vals, int64_t nnode,
+                                                                 const int8_t *fixed, const float2 *x,
+                                                                 const double *b, double *y, int64_t ncols) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)MG_NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * MG_NT) >> 5;
+    for (int64_t base = warp * (32 / LPN); base < nnode; base += nwarps * (32 / LPN)) {  // warp-uniform
+        const int64_t m = base + lane / LPN;
+        const int sub = lane & (LPN - 1);
+        const bool valid = m < nnode;
+        float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f, s2 = 0.f, c2 = 0.f;
+        if (valid) {
+            const int p0 = indptr[3 * m], p1 = indptr[3 * m + 1], p2 = indptr[3 * m + 2];
+            const int nb = (p1 - p0) / 3;
+            for (int blk = sub; blk < nb; blk += LPN) {
+                const int c = indices[p0 + 3 * blk];
+                if (c < 0 || c + 2 >= ncols) continue;
+                const float2 x0 = x[c], x1 = x[c + 1], x2 = x[c + 2];
+                const float2 *v0 = vals + p0 + 3 * blk, *v1 = vals + p1 + 3 * blk, *v2 = vals + p2 + 3 * blk;
+                mg_pair_mac(v0[0], x0, s0, c0); mg_pair_mac(v0[1], x1, s0, c0); mg_pair_mac(v0[2], x2, s0, c0);
+                mg_pair_mac(v1[0], x0, s1, c1); mg_pair_mac(v1[1], x1, s1, c1); mg_pair_mac(v1[2], x2, s1, c1);
+                mg_pair_mac(v2[0], x0, s2, c2); mg_pair_mac(v2[1], x1, s2, c2); mg_pair_mac(v2[2], x2, s2, c2);
+            }
+        }
+#pragma unroll
+        for (int o = LPN / 2; o > 0; o >>= 1) {
+            float t, e;
+            mg_two_sum(s0, __shfl_xor_sync(0xffffffffu, s0, o), t, e);
+            c0 += e + __shfl_xor_sync(0xffffffffu, c0, o);
+            s0 = t;
+            mg_two_sum(s1, __shfl_xor_sync(0xffffffffu, s1, o), t, e);
+            c1 += e + __shfl_xor_sync(0xffffffffu, c1, o);
+            s1 = t;
+            mg_two_sum(s2, __shfl_xor_sync(0xffffffffu, s2, o), t, e);
+            c2 += e + __shfl_xor_sync(0xffffffffu, c2, o);
+            s2 = t;
+        }
+        if (valid && sub < 3) {
+            const int64_t row = 3 * m + sub;
+            const double a = sub == 0 ? (double)s0 + (double)c0 : sub == 1 ? (double)s1 + (double)c1
+                                                                            : (double)s2 + (double)c2;
+            y[row] = fixed[row] ? 0.0 : (b ? b[row] - a : a);
+        }
+    }
+}
+
 // z (+)= omega B^-1 r per node; fixed dofs of z set to 0
 __global__ void __launch_bounds__(MG_NT) block_apply_kernel(int64_t nnode, const double *Binv, const int8_t *fixed,
                                                             double omega, const double *r, double *z, int accumulate) {
@@ -188,35 +264,42 @@ static unsigned grid_of(int64_t n, int per_block) {
 // The coarse problem's block-Jacobi PCG in one cooperative launch. The coarse system is small
 // (three dofs per mesh vertex) and needs up to a hundred iterations per cycle; as separate
 // launches each iteration would cost three kernel boundaries and a host poll, far more than its
-// work. Here every CTA stays resident (cooperative launch, one CTA per SM), an iteration is two
-// phases separated by grid barriers, and the dot products go through rotating device slots:
-//   phase 1  beta = r.z(k) / r.z(k-1); p_k = z_k + beta p_(k-1) formed on the fly where the
-//            product gathers it (and stored by the owner of each node); q = K_ff p_k; p_k.q
+// work. Here one CTA per SM stays resident (cooperative launch) and owns a contiguous range of
+// nodes: their CSR rows, block inverses and iteration vectors live in its shared memory for the
+// whole solve, so that an iteration reads global memory only to gather the neighbours' search
+// directions. An iteration is two phases separated by grid barriers, and the dot products go
+// through rotating device slots:
+//   phase 1  beta = r.z(k) / r.z(k-1); p_k = z_k + beta p_(k-1), formed on the fly where the
+//            product gathers it (and stored by each node's owner); q = K_ff p_k; p_k.q
 //            (8 lanes per node of a node-blocked pattern)
 //   phase 2  alpha = r.z / p.q; x += alpha p; r -= alpha q; z = B^-1 r; r.z, r.r  (a thread per node)
 //   then     stop when r.r <= rtol^2 b.b
-// p alternates between two buffers (iteration k writes p_k while others still gather p_(k-1)).
-// Data written by other CTAs inside the launch are read past L1 (ld.global.cg); the barrier is
-// an arrival counter (release) and a generation word (acquire). Every barrier wait is bounded: on
-// a timeout the kernel records FL_FLAG_TIMEOUT and every CTA leaves.
+// p and z are published in global memory for the gathers, p alternating between two buffers
+// (iteration k writes p_k while others still gather p_(k-1)); they are read past L1
+// (ld.global.cg). The barrier is an arrival counter (release) and a generation word (acquire).
+// Every barrier wait is bounded: on a timeout the kernel records FL_FLAG_TIMEOUT and every CTA
+// leaves. A CTA whose rows exceed its shared memory makes every CTA leave at once with
+// FL_FLAG_CAPACITY (the caller then solves the coarse system another way).
 constexpr int CG_NT = 512;
-constexpr int CG_LPN = 8;  // lanes per node in the product
+constexpr int CG_LPN = 8;                    // lanes per node in the product
+constexpr int CG_SMEM = 200 * 1024;          // dynamic shared memory per CTA
 constexpr long long CG_SPIN_LIMIT = 1ll << 24;
 
 struct CgArgs {
     const int32_t *indptr, *indices;
     const double *vals, *Binv, *b;
     const int8_t *fixed;
-    double *x, *r, *z, *q;
-    double *pb[2];       // p_k in pb[k & 1]
-    double *sc;          // [0..2] p.q, [3..5] r.z, [6..8] r.r (rotating by iteration), [9] b.b
+    double *x, *z;       // z published for the gathers
+    double *pb[2];       // p_k published in pb[k & 1]
+    double *sc;          // slot s (iteration mod 3) at sc[4 s]: [0] p.q, [2] r.z, [3] r.r; [12] b.b
     unsigned *bar;       // [0] arrivals, [1] generation
     int *abort_flag;     // set by a CTA whose barrier wait timed out
+    int *nofit;          // set by a CTA whose rows do not fit its shared memory
     int64_t n, maxiter;
     double rtol2;
     int64_t *iters;      // optional: the iteration count is added here
     double *relres;      // optional: |r| / |b| at the end
-    int *flags;          // optional: FL_FLAG_TIMEOUT, FL_FLAG_BAD_INDEX (non-positive p.q)
+    int *flags;          // optional: FL_FLAG_TIMEOUT, FL_FLAG_BAD_INDEX (non-positive p.q), FL_FLAG_CAPACITY
 };
 
 __device__ __forceinline__ double cg_block_sum(double v, double *red) {
@@ -232,6 +315,28 @@ __device__ __forceinline__ double cg_block_sum(double v, double *red) {
     }
     __syncthreads();
     return t;  // in thread 0
+}
+
+// two block sums in one pass (valid in thread 0)
+__device__ __forceinline__ void cg_block_sum2(double &u, double &v, double2 *red2) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        u += __shfl_down_sync(0xffffffffu, u, o);
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    if ((threadIdx.x & 31) == 0) red2[threadIdx.x >> 5] = make_double2(u, v);
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double2 t = threadIdx.x < CG_NT / 32 ? red2[threadIdx.x] : make_double2(0.0, 0.0);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            t.x += __shfl_down_sync(0xffffffffu, t.x, o);
+            t.y += __shfl_down_sync(0xffffffffu, t.y, o);
+        }
+        u = t.x;
+        v = t.y;
+    }
+    __syncthreads();
 }
 
 __device__ __forceinline__ unsigned cg_arrive(unsigned *count) {
@@ -274,89 +379,116 @@ __device__ bool cg_barrier(const CgArgs &a, unsigned &gen, volatile int *s_abort
 }
 
 __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
+    extern __shared__ __align__(16) unsigned char cg_smem[];
     __shared__ double red[CG_NT / 32];
+    __shared__ double2 red2[CG_NT / 32];
     __shared__ volatile int s_abort;
-    const int lane = threadIdx.x & 31;
-    const int64_t gt = blockIdx.x * (int64_t)CG_NT + threadIdx.x, nthr = (int64_t)gridDim.x * CG_NT;
-    const int64_t gwarp = gt >> 5, nwarps = nthr >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int64_t nnode = a.n / 3;
+    // this CTA's nodes [n0, n1) and their rows [jlo, jhi) of the CSR arrays
+    const int64_t M = (nnode + gridDim.x - 1) / gridDim.x;
+    const int64_t n0 = min(nnode, (int64_t)blockIdx.x * M), n1 = min(nnode, n0 + M);
+    const int cnt = (int)(n1 - n0);
+    const int64_t jlo = a.indptr[3 * n0], jhi = a.indptr[3 * n1];
+    const int64_t snnz = jhi - jlo;
+    // shared memory: own x, r, z, p, q [3M] each, block inverses [9M], row starts [3M] + block
+    // counts [M] (ints), the rows' values and column indices [snnz] each
+    double *sx = reinterpret_cast<double *>(cg_smem);
+    double *sr = sx + 3 * M, *sz = sr + 3 * M, *sp = sz + 3 * M, *sq = sp + 3 * M, *sB = sq + 3 * M;
+    double *sv = sB + 9 * M;
+    int *si = reinterpret_cast<int *>(sv + snnz);
+    int *srow = si + snnz;  // [3M] local row starts, then [M] block counts
+    const size_t need = sizeof(double) * (24 * (size_t)M + (size_t)snnz) + sizeof(int) * ((size_t)snnz + 4 * M);
     unsigned gen = 0;
-    if (threadIdx.x == 0) s_abort = 0;
-    __syncthreads();
-    double *sc = a.sc;
+    if (tid == 0) {
+        s_abort = 0;
+        if (need > (size_t)CG_SMEM || snnz < 0) atomicOr(a.nofit, 1);
+    }
+    bool ok = cg_barrier(a, gen, &s_abort);
+    if (!ok || *(volatile int *)a.nofit) {
+        if (blockIdx.x == 0 && tid == 0 && a.flags) atomicOr(a.flags, ok ? FL_FLAG_CAPACITY : FL_FLAG_TIMEOUT);
+        return;
+    }
+    // the CTA's rows, block inverses and row starts into shared memory
+    for (int64_t t = tid; t < snnz; t += CG_NT) {
+        sv[t] = a.vals[jlo + t];
+        si[t] = a.indices[jlo + t];
+    }
+    for (int t = tid; t < 9 * cnt; t += CG_NT) sB[t] = a.Binv[9 * n0 + t];
+    for (int t = tid; t < cnt; t += CG_NT) {
+        const int64_t r0 = 3 * (n0 + t);
+        const int j0 = (int)(a.indptr[r0] - jlo), j1 = (int)(a.indptr[r0 + 1] - jlo), j2 = (int)(a.indptr[r0 + 2] - jlo);
+        srow[3 * t] = j0;
+        srow[3 * t + 1] = j1;
+        srow[3 * t + 2] = j2;
+        srow[3 * M + t] = (j1 - j0) / 3;
+    }
     // r = b, z = B^-1 r, x = 0, p_(-1) = 0 (fixed dofs 0 throughout)
+    double *sc = a.sc;
     double rz = 0.0, bb = 0.0;
-    for (int64_t m = gt; m < nnode; m += nthr) {
+    for (int t = tid; t < cnt; t += CG_NT) {
+        const int64_t g0 = 3 * (n0 + t);
         double rv[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            const int64_t d = 3 * m + i;
-            rv[i] = a.fixed[d] ? 0.0 : a.b[d];
-            __stcg(a.r + d, rv[i]);
-            __stcg(a.x + d, 0.0);
-            __stcg(a.pb[1] + d, 0.0);
+            rv[i] = a.fixed[g0 + i] ? 0.0 : a.b[g0 + i];
+            sr[3 * t + i] = rv[i];
+            sx[3 * t + i] = 0.0;
+            sp[3 * t + i] = 0.0;
+            __stcg(a.pb[1] + g0 + i, 0.0);
             bb = fma(rv[i], rv[i], bb);
         }
-        const double *B = a.Binv + m * 9;
+        const double *B = a.Binv + (n0 + t) * 9;
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            const int64_t d = 3 * m + i;
-            const double zv = a.fixed[d] ? 0.0 : fma(B[3 * i], rv[0], fma(B[3 * i + 1], rv[1], B[3 * i + 2] * rv[2]));
-            __stcg(a.z + d, zv);
+            const double zv =
+                a.fixed[g0 + i] ? 0.0 : fma(B[3 * i], rv[0], fma(B[3 * i + 1], rv[1], B[3 * i + 2] * rv[2]));
+            sz[3 * t + i] = zv;
+            __stcg(a.z + g0 + i, zv);
             rz = fma(rv[i], zv, rz);
         }
     }
-    rz = cg_block_sum(rz, red);
-    bb = cg_block_sum(bb, red);
-    if (threadIdx.x == 0) {
-        atomicAdd(sc + 3, rz);
-        atomicAdd(sc + 9, bb);
+    cg_block_sum2(rz, bb, red2);
+    if (tid == 0) {
+        atomicAdd(sc + 2, rz);
+        atomicAdd(sc + 12, bb);
     }
-    bool ok = cg_barrier(a, gen, &s_abort);
-    const double b2 = __ldcg(sc + 9);
+    ok = cg_barrier(a, gen, &s_abort);
+    const double b2 = __ldcg(sc + 12);
     int64_t k = 0;
     double rr = b2;
+    double rzk = __ldcg(sc + 2), rz_prev = 1.0;  // r.z of this and the previous iterate, carried along
     bool bad = false;
     if (b2 > 0.0)
         for (; ok && k < a.maxiter; ++k) {
-            const int s0 = (int)(k % 3), s1 = (int)((k + 1) % 3), sm = (int)((k + 2) % 3);  // sm: k - 1
-            const double rzk = __ldcg(sc + 3 + s0);
-            const double beta = k == 0 ? 0.0 : rzk / __ldcg(sc + 3 + sm);
+            const int s0 = (int)(k % 3), s1 = (int)((k + 1) % 3);
+            const double beta = k == 0 ? 0.0 : rzk / rz_prev;
             const double *pold = a.pb[(k + 1) & 1];
             double *pnew = a.pb[k & 1];
             // phase 1; the slots of the next iteration are cleared
-            if (gt == 0) {
-                __stcg(sc + s1, 0.0);
-                __stcg(sc + 3 + s1, 0.0);
-                __stcg(sc + 6 + s1, 0.0);
+            if (blockIdx.x == 0 && tid == 0) {
+                __stcg(sc + 4 * s1, 0.0);
+                __stcg(sc + 4 * s1 + 2, 0.0);
+                __stcg(sc + 4 * s1 + 3, 0.0);
             }
-            // CG_LPN lanes per node, 32 / CG_LPN nodes per warp at once (a coarse node has ~15
-            // column blocks: one pass of dependent loads covers the whole product); warp-uniform
-            // trip count, so that every lane takes part in the shuffles
             double pq = 0.0;
-            for (int64_t base = gwarp * (32 / CG_LPN); base < nnode; base += nwarps * (32 / CG_LPN)) {
-                const int64_t m = base + lane / CG_LPN;
+            for (int base = warp * (32 / CG_LPN); base < cnt; base += (CG_NT / 32) * (32 / CG_LPN)) {
+                const int ml = base + lane / CG_LPN;  // warp-uniform trip count: every lane shuffles
                 const int sub = lane & (CG_LPN - 1);
-                const bool valid = m < nnode;
-                const int64_t r0 = 3 * m;
-                int j0 = 0, j1 = 0, j2 = 0, nb = 0;
-                if (valid) {
-                    j0 = a.indptr[r0];
-                    j1 = a.indptr[r0 + 1];
-                    j2 = a.indptr[r0 + 2];
-                    nb = (j1 - j0) / 3;
-                }
+                const bool valid = ml < cnt;
+                const int j0 = valid ? srow[3 * ml] : 0, j1 = valid ? srow[3 * ml + 1] : 0;
+                const int j2 = valid ? srow[3 * ml + 2] : 0, nb = valid ? srow[3 * M + ml] : 0;
                 double a0 = 0.0, a1 = 0.0, a2 = 0.0;
                 for (int blk = sub; blk < nb; blk += CG_LPN) {
-                    const int c = a.indices[j0 + 3 * blk];
+                    const int c = si[j0 + 3 * blk];
                     if (c < 0 || c + 2 >= a.n) continue;
                     const double x0 = fma(beta, __ldcg(pold + c), __ldcg(a.z + c));
                     const double x1 = fma(beta, __ldcg(pold + c + 1), __ldcg(a.z + c + 1));
                     const double x2 = fma(beta, __ldcg(pold + c + 2), __ldcg(a.z + c + 2));
-                    const double *v0 = a.vals + j0 + 3 * blk, *v1 = a.vals + j1 + 3 * blk, *v2 = a.vals + j2 + 3 * blk;
-                    a0 = fma(__ldg(v0), x0, fma(__ldg(v0 + 1), x1, fma(__ldg(v0 + 2), x2, a0)));
-                    a1 = fma(__ldg(v1), x0, fma(__ldg(v1 + 1), x1, fma(__ldg(v1 + 2), x2, a1)));
-                    a2 = fma(__ldg(v2), x0, fma(__ldg(v2 + 1), x1, fma(__ldg(v2 + 2), x2, a2)));
+                    const double *v0 = sv + j0 + 3 * blk, *v1 = sv + j1 + 3 * blk, *v2 = sv + j2 + 3 * blk;
+                    a0 = fma(v0[0], x0, fma(v0[1], x1, fma(v0[2], x2, a0)));
+                    a1 = fma(v1[0], x0, fma(v1[1], x1, fma(v1[2], x2, a1)));
+                    a2 = fma(v2[0], x0, fma(v2[1], x1, fma(v2[2], x2, a2)));
                 }
 #pragma unroll
                 for (int o = CG_LPN / 2; o > 0; o >>= 1) {
@@ -364,64 +496,71 @@ __global__ void __launch_bounds__(CG_NT) coarse_pcg_kernel(const CgArgs a) {
                     a1 += __shfl_xor_sync(0xffffffffu, a1, o);
                     a2 += __shfl_xor_sync(0xffffffffu, a2, o);
                 }
-                if (valid && sub < 3) {  // lane sub of the group finishes row 3m + sub
-                    const int64_t d = r0 + sub;
+                if (valid && sub < 3) {  // lane sub of the group finishes row 3 ml + sub
+                    const int dl = 3 * ml + sub;
+                    const int64_t d = 3 * n0 + dl;
                     const double av = sub == 0 ? a0 : sub == 1 ? a1 : a2;
-                    const double pv = fma(beta, __ldcg(pold + d), __ldcg(a.z + d));  // 0 on fixed dofs
+                    const double pv = fma(beta, sp[dl], sz[dl]);  // 0 on fixed dofs
                     const double qv = a.fixed[d] ? 0.0 : av;
+                    sp[dl] = pv;
+                    sq[dl] = qv;
                     __stcg(pnew + d, pv);
-                    __stcg(a.q + d, qv);
                     pq = fma(pv, qv, pq);
                 }
             }
             pq = cg_block_sum(pq, red);
-            if (threadIdx.x == 0) atomicAdd(sc + s0, pq);
+            if (tid == 0) atomicAdd(sc + 4 * s0, pq);
             if (!(ok = cg_barrier(a, gen, &s_abort))) break;
-            // phase 2
-            const double pqk = __ldcg(sc + s0);
+            // phase 2 (own nodes, shared memory; z published)
+            const double pqk = __ldcg(sc + 4 * s0);
             if (!(pqk > 0.0) || !isfinite(pqk)) {  // K_ff not positive definite on p (or no progress)
                 bad = true;
                 break;
             }
             const double alpha = rzk / pqk;
             double rz1 = 0.0, rr1 = 0.0;
-            for (int64_t m = gt; m < nnode; m += nthr) {
+            for (int t = tid; t < cnt; t += CG_NT) {
                 double rv[3];
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
-                    const int64_t d = 3 * m + i;
-                    __stcg(a.x + d, fma(alpha, __ldcg(pnew + d), __ldcg(a.x + d)));
-                    rv[i] = fma(-alpha, __ldcg(a.q + d), __ldcg(a.r + d));
-                    __stcg(a.r + d, rv[i]);
+                    const int dl = 3 * t + i;
+                    sx[dl] = fma(alpha, sp[dl], sx[dl]);
+                    rv[i] = fma(-alpha, sq[dl], sr[dl]);
+                    sr[dl] = rv[i];
                     rr1 = fma(rv[i], rv[i], rr1);
                 }
-                const double *B = a.Binv + m * 9;
+                const double *B = sB + 9 * t;
 #pragma unroll
                 for (int i = 0; i < 3; ++i) {
-                    const int64_t d = 3 * m + i;
-                    const double zv =
-                        a.fixed[d] ? 0.0 : fma(B[3 * i], rv[0], fma(B[3 * i + 1], rv[1], B[3 * i + 2] * rv[2]));
-                    __stcg(a.z + d, zv);
+                    const int dl = 3 * t + i;
+                    const double zv = a.fixed[3 * n0 + dl]
+                                          ? 0.0
+                                          : fma(B[3 * i], rv[0], fma(B[3 * i + 1], rv[1], B[3 * i + 2] * rv[2]));
+                    sz[dl] = zv;
+                    __stcg(a.z + 3 * n0 + dl, zv);
                     rz1 = fma(rv[i], zv, rz1);
                 }
             }
-            rz1 = cg_block_sum(rz1, red);
-            rr1 = cg_block_sum(rr1, red);
-            if (threadIdx.x == 0) {
-                atomicAdd(sc + 3 + s1, rz1);
-                atomicAdd(sc + 6 + s1, rr1);
+            cg_block_sum2(rz1, rr1, red2);
+            if (tid == 0) {
+                atomicAdd(sc + 4 * s1 + 2, rz1);
+                atomicAdd(sc + 4 * s1 + 3, rr1);
             }
             if (!(ok = cg_barrier(a, gen, &s_abort))) {
                 ++k;
                 break;
             }
-            rr = __ldcg(sc + 6 + s1);
+            const double2 zr = __ldcg(reinterpret_cast<const double2 *>(sc + 4 * s1 + 2));  // r.z, r.r: one load
+            rz_prev = rzk;
+            rzk = zr.x;
+            rr = zr.y;
             if (rr <= a.rtol2 * b2) {
                 ++k;
                 break;
             }
         }
-    if (gt == 0) {
+    for (int t = tid; t < 3 * cnt; t += CG_NT) a.x[3 * n0 + t] = sx[t];
+    if (blockIdx.x == 0 && tid == 0) {
         if (a.iters) atomicAdd((unsigned long long *)a.iters, (unsigned long long)k);
         if (a.relres) *a.relres = b2 > 0.0 ? sqrt(rr / b2) : 0.0;
         if (a.flags && (!ok || bad)) atomicOr(a.flags, !ok ? FL_FLAG_TIMEOUT : FL_FLAG_BAD_INDEX);
@@ -477,6 +616,30 @@ int fl_MaskedMatVecBlocksF32(const int32_t *indptr, const int32_t *indices, cons
     return fl::launch_status();
 }
 
+int fl_SplitPairs(int64_t n, const double *v, float *pairs, fl_stream_t stream) {
+    if (n < 0) return FL_ERR_ARG;
+    if (n == 0) return FL_OK;
+    if (!v || !pairs) return FL_ERR_ARG;
+    const unsigned grid = (unsigned)std::min<int64_t>((n + fl::MG_NT - 1) / fl::MG_NT, 152 * 16);
+    fl::split_pairs_kernel<<<grid, fl::MG_NT, 0, (cudaStream_t)stream>>>(n, v, reinterpret_cast<float2 *>(pairs));
+    return fl::launch_status();
+}
+
+int fl_MaskedMatVecBlocksPair(const int32_t *indptr, const int32_t *indices, const float *value_pairs, int64_t nrows,
+                              const int8_t *fixed, const float *x_pairs, const double *b, double *y,
+                              fl_stream_t stream) {
+    if (nrows < 0 || nrows % 3) return FL_ERR_ARG;
+    if (nrows == 0) return FL_OK;
+    if (!indptr || !indices || !value_pairs || !fixed || !x_pairs || !y) return FL_ERR_ARG;
+    const int64_t nnode = nrows / 3;
+    constexpr int LPN = 16;
+    const int64_t warps = std::min<int64_t>((nnode + 32 / LPN - 1) / (32 / LPN), (int64_t)152 * 64);
+    fl::masked_spmv_pair_kernel<LPN><<<fl::grid_of(warps * 32, fl::MG_NT), fl::MG_NT, 0, (cudaStream_t)stream>>>(
+        indptr, indices, reinterpret_cast<const float2 *>(value_pairs), nnode, fixed,
+        reinterpret_cast<const float2 *>(x_pairs), b, y, nrows);
+    return fl::launch_status();
+}
+
 int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nnode,
                           const int8_t *fixed, double *Binv, int *flags, fl_stream_t stream) {
     if (nnode < 0) return FL_ERR_ARG;
@@ -489,7 +652,7 @@ int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const d
 
 size_t fl_CoarsePCG_workspace_size(int64_t nrows) {
     if (nrows < 0) return 0;
-    return sizeof(double) * (size_t)(5 * nrows + 16) + 64;
+    return sizeof(double) * (size_t)(3 * nrows + 16) + 64;
 }
 
 int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nrows,
@@ -501,34 +664,34 @@ int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *va
     if (!indptr || !indices || !values || !fixed || !Binv || !b || !x || !workspace) return FL_ERR_ARG;
     if (workspace_bytes < fl_CoarsePCG_workspace_size(nrows)) return FL_ERR_CAPACITY;
     cudaStream_t st = (cudaStream_t)stream;
-    static int per_sm[64] = {}, sms[64] = {};
+    static int sms[64] = {};
     int dev = 0;
     FL_CUDA_TRY(cudaGetDevice(&dev));
-    if (per_sm[dev & 63] == 0) {
+    if (sms[dev & 63] == 0) {
         int coop = 0;
         FL_CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev));
         if (!coop) return FL_ERR_UNSUPPORTED;
+        FL_CUDA_TRY(cudaFuncSetAttribute(fl::coarse_pcg_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, fl::CG_SMEM));
+        int resident = 0;
+        FL_CUDA_TRY(
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, fl::coarse_pcg_kernel, fl::CG_NT, fl::CG_SMEM));
+        if (resident < 1) return FL_ERR_UNSUPPORTED;
         FL_CUDA_TRY(cudaDeviceGetAttribute(&sms[dev & 63], cudaDevAttrMultiProcessorCount, dev));
-        int b = 0;
-        FL_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, fl::coarse_pcg_kernel, fl::CG_NT, 0));
-        per_sm[dev & 63] = std::max(1, b);
     }
-    // enough CTAs for a warp per node, at most one per SM: every grid barrier serialises one atomic
-    // arrival per CTA, so fewer, larger CTAs make the barriers cheaper (a cooperative launch also
-    // needs them all resident, which per_sm >= 1 guarantees)
-    const int64_t want = (nrows / 3 + fl::CG_NT / 32 - 1) / (fl::CG_NT / 32);
+    // one CTA per SM (all resident, as a cooperative launch needs; every grid barrier serialises
+    // one arrival per CTA), at most one per 16 nodes
+    const int64_t want = (nrows / 3 + 15) / 16;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms[dev & 63]));
     fl::CgArgs a{};
     char *w = (char *)workspace;
     a.sc = (double *)w;
     a.bar = (unsigned *)(w + 16 * sizeof(double));
     a.abort_flag = (int *)(w + 16 * sizeof(double) + 2 * sizeof(unsigned));
+    a.nofit = (int *)(w + 16 * sizeof(double) + 3 * sizeof(unsigned));
     double *v = (double *)(w + 16 * sizeof(double) + 64);
-    a.r = v;
-    a.z = v + nrows;
-    a.pb[0] = v + 2 * nrows;
-    a.pb[1] = v + 3 * nrows;
-    a.q = v + 4 * nrows;
+    a.z = v;
+    a.pb[0] = v + nrows;
+    a.pb[1] = v + 2 * nrows;
     a.indptr = indptr;
     a.indices = indices;
     a.vals = values;
@@ -544,7 +707,8 @@ int fl_CoarsePCG(const int32_t *indptr, const int32_t *indices, const double *va
     a.flags = flags;
     FL_CUDA_TRY(cudaMemsetAsync(w, 0, 16 * sizeof(double) + 64, st));
     void *args[] = {(void *)&a};
-    FL_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)fl::coarse_pcg_kernel, dim3(grid), dim3(fl::CG_NT), args, 0, st));
+    FL_CUDA_TRY(cudaLaunchCooperativeKernel((const void *)fl::coarse_pcg_kernel, dim3(grid), dim3(fl::CG_NT), args,
+                                            fl::CG_SMEM, st));
     return FL_OK;
 }
 

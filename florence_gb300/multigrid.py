@@ -101,6 +101,8 @@ class PMultigrid:
         self.Tc = torch.zeros(self.nc, dtype=torch.float64, device=dev)
         self.Binv = torch.empty((asm.nnode, 9), dtype=torch.float64, device=dev)
         self.V32 = torch.empty(asm.nnz, dtype=torch.float32, device=dev)
+        self.Vp = torch.empty(2 * asm.nnz, dtype=torch.float32, device=dev)   # the tangent as float pairs
+        self._xp = torch.empty(2 * self.n, dtype=torch.float32, device=dev)
         self.Binv_c = torch.empty((self.coarse.nnode, 9), dtype=torch.float64, device=dev)
         self.nu, self.ratio, self.power_iters = nu, ratio, power_iters
         self.coarse_rtol, self.coarse_maxiter = coarse_rtol, coarse_maxiter
@@ -112,6 +114,18 @@ class PMultigrid:
         self._cws = torch.empty(int(N.lib().fl_CoarsePCG_workspace_size(self.nc)), dtype=torch.uint8, device=dev)
         self._xc = torch.zeros(self.nc, dtype=torch.float64, device=dev)
         self._citers = torch.zeros(1, dtype=torch.int64, device=dev)
+        # the one-launch coarse solve keeps each SM's share of the coarse rows in shared memory:
+        # checked once here; a coarse system too large for it is solved by the block-Jacobi PCG
+        # launched iteration by iteration (fl_BlockJacobiPCG) instead
+        self._coarse_fast = True
+        self._pcg_ws = None
+        saved = self.coarse_maxiter
+        self.coarse_maxiter = 0
+        self.coarse_solve(torch.zeros(self.nc, dtype=torch.float64, device=dev))
+        self.coarse_maxiter = saved
+        if int(self.flags.item()) & N.FL_FLAG_CAPACITY:
+            self._coarse_fast = False
+        self.flags.zero_()
 
     @property
     def coarse_iters(self):
@@ -121,10 +135,13 @@ class PMultigrid:
     # -- kernels ------------------------------------------------------------------------------
     def matvec(self, x, y, b=None):
         """y = K_ff x (or b - K_ff x) with the fine tangent; x is zero on the fixed dofs (every
-        vector of the cycle and of the outer iteration is)."""
-        N.check(N.lib().fl_MaskedMatVecBlocks(_ptr(self.asm.indptr), _ptr(self.asm.indices), _ptr(self.V), self.n,
-                                              _ptr(self.fixed), _ptr(x), _ptr(b), _ptr(y), _stream()),
-                "fl_MaskedMatVecBlocks")
+        vector of the cycle and of the outer iteration is). The tangent and x as float pairs
+        (~2^-44 relative, FP32 pipe)."""
+        L = N.lib()
+        N.check(L.fl_SplitPairs(self.n, _ptr(x), _ptr(self._xp), _stream()), "fl_SplitPairs")
+        N.check(L.fl_MaskedMatVecBlocksPair(_ptr(self.asm.indptr), _ptr(self.asm.indices), _ptr(self.Vp), self.n,
+                                            _ptr(self.fixed), _ptr(self._xp), _ptr(b), _ptr(y), _stream()),
+                "fl_MaskedMatVecBlocksPair")
         return y
 
     def smooth_matvec(self, x, y, b=None):
@@ -157,6 +174,7 @@ class PMultigrid:
         inverses, the largest eigenvalue estimate, the coarse tangent at the vertices."""
         self.V = V
         self.V32.copy_(V)
+        N.check(N.lib().fl_SplitPairs(self.asm.nnz, _ptr(V), _ptr(self.Vp), _stream()), "fl_SplitPairs")
         N.check(N.lib().fl_BlockJacobiInverse(_ptr(self.asm.indptr), _ptr(self.asm.indices), _ptr(V), self.asm.nnode,
                                               _ptr(self.fixed), _ptr(self.Binv), _ptr(self.flags), _stream()),
                 "fl_BlockJacobiInverse")
@@ -238,6 +256,14 @@ class PMultigrid:
         """The coarse correction: block-Jacobi PCG on the vertex tangent to coarse_rtol (at most
         coarse_maxiter iterations) in one cooperative launch; returns the device solution."""
         c = self.coarse
+        if not self._coarse_fast:
+            from .newton import pcg, pcg_workspace
+            if self._pcg_ws is None:
+                self._pcg_ws = pcg_workspace(c, self.Vc, "fp64")
+            xc, it, _ = pcg(c, self.Vc, rc, self.fixed_c, rtol=self.coarse_rtol, maxiter=self.coarse_maxiter,
+                            workspace=self._pcg_ws, spmv="fp64")
+            self._citers += it
+            return xc
         N.check(N.lib().fl_CoarsePCG(_ptr(c.indptr), _ptr(c.indices), _ptr(self.Vc), self.nc, _ptr(self.fixed_c),
                                      _ptr(self.Binv_c), _ptr(rc), _ptr(self._xc), float(self.coarse_rtol),
                                      int(self.coarse_maxiter), _ptr(self._cws), self._cws.numel(), _ptr(self._citers),

@@ -49,6 +49,8 @@ typedef struct CUstream_st *fl_stream_t;
 #define FL_FLAG_NONPOSITIVE_J 1 /* det F <= 0 at some Gauss point; results are still written */
 #define FL_FLAG_BAD_INDEX 2     /* an element node id or a map entry is out of range; the entry was skipped */
 #define FL_FLAG_TIMEOUT 4       /* a bounded wait inside a tensor-core kernel gave up; outputs incomplete */
+#define FL_FLAG_CAPACITY 16     /* fl_CoarsePCG: a CTA's share of the rows does not fit its shared memory;
+                                 * nothing was solved */
 #define FL_FLAG_PAIR_RANGE 8    /* a Gauss point's pulled-back tangent (or, with FL_ARITH_REFERENCE_TENSOR,
                                  * its stress factor) has its largest magnitude outside [2^-78, 2^120]:
                                  * the float pairs these arithmetics hold it in (FP32 exponent range) may
@@ -452,7 +454,9 @@ int fl_GetPCGDeviceLoop(void);
  * fl_MaskedMatVecBlocks: the same product for a node-blocked pattern (the three rows of a node list
  *   the same nodes, three columns each: every assembled tangent's pattern), one warp per node and
  *   one column index per 3x3 block; x must be zero on fixed dofs. fl_MaskedMatVecBlocksF32: with
- *   FP32 values (FP32 products, FP64 sums), for smoothers.
+ *   FP32 values (FP32 products and sums), for smoothers. fl_MaskedMatVecBlocksPair: with the
+ *   values and x as float pairs (hi, lo interleaved, from fl_SplitPairs), ~2^-44 relative, on the
+ *   FP32 pipe. fl_SplitPairs: pairs[2i], pairs[2i + 1] = hi, lo of v[i].
  * fl_BlockJacobiInverse: Binv[n][9] = inverse of each node's 3x3 diagonal block, fixed rows and
  *   columns replaced by the identity (FL_FLAG_BAD_INDEX in flags for a missing or singular block).
  * fl_BlockJacobiApply: z (=, or +=) omega Binv r per node, 0 on fixed dofs.
@@ -464,7 +468,9 @@ int fl_GetPCGDeviceLoop(void);
  *   be bound by kernel boundaries. workspace: fl_CoarsePCG_workspace_size(nrows) bytes.
  *   iterations (optional, device int64): the iteration count is ADDED to it; relres (optional,
  *   device double): |r| / |b_f| at the end; flags (optional, device int): FL_FLAG_TIMEOUT when a
- *   barrier wait gave up, FL_FLAG_BAD_INDEX when p.K_ff p <= 0. FL_ERR_UNSUPPORTED without
+ *   barrier wait gave up, FL_FLAG_BAD_INDEX when p.K_ff p <= 0, FL_FLAG_CAPACITY (nothing solved)
+ *   when the rows of one SM's share of the nodes exceed its 200 KB of shared memory, where they
+ *   stay for the whole solve (about 16 k nodes on 152 SMs). FL_ERR_UNSUPPORTED without
  *   cooperative launch. Nothing synchronises.
  * ------------------------------------------------------------------------------------------ */
 int fl_NodalTransfer(int64_t nrows, const int32_t *ptr, const int32_t *cols, const double *weights, const double *x,
@@ -475,6 +481,10 @@ int fl_MaskedMatVecBlocks(const int32_t *indptr, const int32_t *indices, const d
                           const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
 int fl_MaskedMatVecBlocksF32(const int32_t *indptr, const int32_t *indices, const float *values, int64_t nrows,
                              const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
+int fl_SplitPairs(int64_t n, const double *v, float *pairs, fl_stream_t stream);
+int fl_MaskedMatVecBlocksPair(const int32_t *indptr, const int32_t *indices, const float *value_pairs, int64_t nrows,
+                              const int8_t *fixed, const float *x_pairs, const double *b, double *y,
+                              fl_stream_t stream);
 int fl_BlockJacobiInverse(const int32_t *indptr, const int32_t *indices, const double *values, int64_t nnode,
                           const int8_t *fixed, double *Binv, int *flags, fl_stream_t stream);
 int fl_BlockJacobiApply(int64_t nnode, const double *Binv, const int8_t *fixed, double omega, const double *r,
