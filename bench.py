@@ -888,6 +888,29 @@ def run_meshing(args):
         cpu = dict(value=els.shape[0] / dt / 1e6, unit="Melem/s", cores=1, kind="port",
                    sample="host builder (numpy np.unique of entity keys) on a 24x24x24 Kuhn box, %d tets" % els.shape[0])
     launches = 18  # count, degree, fill, entities (count and write), nodes, four 3-kernel scans
+    # hexes (fl_RaiseHexOrder): a structured box of linear hexes raised to p=3 with the reference's
+    # 64-node Gauss-Lobatto layout (taken from a golden fixture)
+    g = np.load(os.path.join(GOLDEN, "hex_p3_nh.npz"))
+    xi = meshes.local_pattern(g["points"], g["elements"], 0, "hex")
+    hcells = (128, 64, 64) if args.workload != "beam_s" else (32, 16, 16)
+    lin = np.load(os.path.join(GOLDEN, "hex_p1_nh.npz"))
+    xi1 = meshes.local_pattern(lin["points"], lin["elements"], 0, "hex")
+    Ph, elh = meshes.structured_hex(hcells, (2.0, 1.0, 1.0), xi1)   # linear hexes
+    Phd, elhd = torch.from_numpy(Ph).cuda(), torch.from_numpy(elh).cuda()
+    for _ in range(args.warmup):
+        Xh3, Eh3 = meshes.raise_hex_order_device(Phd, elhd, xi)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        Xh3, Eh3 = meshes.raise_hex_order_device(Phd, elhd, xi)
+    e1.record()
+    torch.cuda.synchronize()
+    ms_h = e0.elapsed_time(e1) / steps
+    hexes = dict(workload="structured box %dx%dx%d linear hexes on 2x1x1 -> p=3 (64-node Gauss-Lobatto layout)"
+                          % hcells, nelem=int(elh.shape[0]), nnode=int(Xh3.shape[0]), ms_per_step=ms_h,
+                 melem_s=elh.shape[0] / (ms_h * 1e-3) / 1e6,
+                 note="each call counts the nodes first and allocates the outputs (two calls of the C entry point)")
+    del Xh3, Eh3
     line = dict(metric="high-order tet mesh generation rate (linear tets raised to p=3 per second)", value=value,
                 unit="Melem/s", n_gpus=1, steps=steps, warmup=args.warmup, ms_per_step=ms, higher_is_better=True,
                 scaling="weak", vs_baseline=None, dtype="int64+f64", data="synthetic",
@@ -897,7 +920,7 @@ def run_meshing(args):
                 roofline=dict(bound="hbm", achieved=nbytes / (ms * 1e-3) / 1e9, peak=hbm, unit="GB/s",
                               frac=nbytes / (ms * 1e-3) / 1e9 / hbm, traffic=None, bytes_min_per_step=nbytes,
                               peak_source="MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback"),
-                e2e=e2e, cpu_baseline=cpu, gpu_launches=launches * steps, clocks=clk.summary())
+                e2e=e2e, cpu_baseline=cpu, gpu_launches=launches * steps, clocks=clk.summary(), hex=hexes)
     print(json.dumps(line), flush=True)
 
 

@@ -71,6 +71,10 @@ def lib():
         L.fl_RaiseTetOrder_workspace_size.argtypes = [I64, I64]
         L.fl_RaiseTetOrder_workspace_size.restype = ctypes.c_size_t
         L.fl_RaiseTetOrder.argtypes = [P, I64, P, I64, P, I64, P, I64, ctypes.POINTER(I64), P, P, ctypes.c_size_t, P]
+        L.fl_HexNodeLayout.argtypes = [P, I64, P]
+        L.fl_RaiseHexOrder_workspace_size.argtypes = [I64, I64]
+        L.fl_RaiseHexOrder_workspace_size.restype = ctypes.c_size_t
+        L.fl_RaiseHexOrder.argtypes = [P, I64, P, I64, P, I64, P, I64, ctypes.POINTER(I64), P, P, ctypes.c_size_t, P]
         for name in ("fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
                      "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
                      "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_"):
@@ -145,7 +149,8 @@ def check(status, what=""):
 
 # every symbol include/florence_gb300.h declares
 EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_ComputeSparsityPattern",
-           "fl_TetNodeLayout", "fl_RaiseTetOrder_workspace_size", "fl_RaiseTetOrder",
+           "fl_TetNodeLayout", "fl_RaiseTetOrder_workspace_size", "fl_RaiseTetOrder", "fl_HexNodeLayout",
+           "fl_RaiseHexOrder_workspace_size", "fl_RaiseHexOrder",
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
            "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
            "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_", "fl_GlobalAssemblyDF_noalloc",

@@ -11,9 +11,10 @@ replicate it over larger meshes:
   positive volume, raised to order p with the pattern's barycentric node positions.
 
 Global node numbering differs from Florence's; the assembled operator is the same up to that
-permutation. ``raise_tet_order_device`` is the GPU form of ``raise_tet_order`` (``fl_RaiseTetOrder``):
-the same node numbering and the same weighted sums for the positions, for meshes too large to
-raise on the host.
+permutation. ``raise_tet_order_device`` / ``raise_hex_order_device`` are the GPU forms of
+``raise_tet_order`` / ``raise_hex_order`` (``fl_RaiseTetOrder`` / ``fl_RaiseHexOrder``): the same
+node numbering and the same weighted sums for the positions, for meshes too large to raise on the
+host.
 """
 import numpy as np
 
@@ -163,6 +164,104 @@ def raise_tet_order_device(points, elements, pattern, device="cuda", out_points=
     if st == N.FL_ERR_MESH:
         raise ValueError("an element repeats a vertex")
     N.check(st, "fl_RaiseTetOrder")
+    return out_pts[:nnode.value], out_el
+
+
+def hex_weights(pattern):
+    """Trilinear weights [npe, 8] of the local nodes (reference coordinates `pattern` [npe, 3],
+    the first 8 nodes the vertices) at the 8 vertices, zeroed below 1e-10, as the device mesher
+    forms them."""
+    xi = np.asarray(pattern, np.float64)
+    sg = np.where(xi[:8] > 0, 1.0, -1.0)
+    w = np.ones((xi.shape[0], 8))
+    for d in range(3):
+        w = w * (0.5 * (1.0 + sg[None, :, d] * xi[:, None, d]))
+    w[np.abs(w) <= 1e-10] = 0.0
+    return w
+
+
+def raise_hex_order(P, el, pattern):
+    """High-order hex mesh from linear hexes P/el [E,8] and the reference-coordinate node layout
+    `pattern` [npe,3] (first 8 nodes the vertices). Numbering: the lexicographic order of (entity
+    size, global vertices ascending, weights in that order), as fl_RaiseHexOrder numbers them;
+    positions the weighted vertex sums in vertex order."""
+    el = np.asarray(el, np.int64)
+    w = hex_weights(pattern)
+    E, npe = el.shape[0], w.shape[0]
+    q = np.rint(w * 1e6).astype(np.int64)
+    nz = w != 0.0
+    keys = np.zeros((E, npe, 9), np.int64)
+    for a in range(npe):
+        idx = np.nonzero(nz[a])[0]
+        k = len(idx)
+        keys[:, a, 0] = k
+        if k == 8:                            # element interior: unique per element
+            keys[:, a, 1] = np.arange(E)
+            keys[:, a, 2] = a
+            continue
+        g = el[:, idx]
+        order = np.argsort(g, axis=1)
+        keys[:, a, 1:1 + k] = np.take_along_axis(g, order, 1)
+        if k > 1:
+            keys[:, a, 5:5 + k] = q[a, idx][order]
+    uniq, first, inv = np.unique(keys.reshape(-1, 9), axis=0, return_index=True, return_inverse=True)
+    elements = inv.reshape(E, npe).astype(np.int64)
+    X = np.asarray(P, np.float64)[el]       # [E, 8, 3]
+    pos = w[None, :, 0, None] * X[:, None, 0, :]
+    for k in range(1, 8):
+        pos = pos + w[None, :, k, None] * X[:, None, k, :]
+    points = pos.reshape(-1, 3)[first]
+    return points, elements
+
+
+def hex_node_layout(pattern):
+    """(nodes inside one edge, inside one face, inside the element) of the hex layout `pattern`
+    [npe,3], as the device mesher classifies it; ValueError for a layout it rejects."""
+    import ctypes
+    from . import _native as N
+    xi = np.ascontiguousarray(pattern, dtype=np.float64)
+    counts = (ctypes.c_int64 * 3)()
+    st = N.lib().fl_HexNodeLayout(xi.ctypes.data, xi.shape[0], ctypes.cast(counts, ctypes.c_void_p))
+    if st != N.FL_OK:
+        raise ValueError("node layout rejected: " + N.lib().fl_status_string(st).decode())
+    return tuple(int(c) for c in counts)
+
+
+def raise_hex_order_device(points, elements, pattern, device="cuda"):
+    """High-order hex mesh built on the GPU from linear hexes (``fl_RaiseHexOrder``): node numbers
+    identical to ``raise_hex_order``, positions the same weighted vertex sums. Returns (points
+    [nnode,3] float64, elements [E,npe] int64) as device tensors on the current stream."""
+    import ctypes
+    import torch
+    from . import _native as N
+    L = N.lib()
+    dev = torch.device(device)
+    xi = np.ascontiguousarray(pattern, dtype=np.float64)
+    X = torch.as_tensor(points, dtype=torch.float64).to(dev).contiguous()
+    el = torch.as_tensor(np.asarray(elements).astype(np.int64) if not isinstance(elements, torch.Tensor)
+                         else elements, dtype=torch.int64).to(dev).contiguous()
+    nvert, nelem, npe = X.shape[0], el.shape[0], xi.shape[0]
+    ws_bytes = L.fl_RaiseHexOrder_workspace_size(nelem, nvert)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    out_el = torch.empty((nelem, npe), dtype=torch.int64, device=dev)
+    nnode = ctypes.c_int64(0)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+
+    def call(out_pts):
+        return L.fl_RaiseHexOrder(ctypes.c_void_p(X.data_ptr()), nvert, ctypes.c_void_p(el.data_ptr()), nelem,
+                                  xi.ctypes.data, npe,
+                                  ctypes.c_void_p(out_pts.data_ptr()) if out_pts is not None else None,
+                                  out_pts.shape[0] if out_pts is not None else 0, ctypes.byref(nnode),
+                                  ctypes.c_void_p(out_el.data_ptr()), ctypes.c_void_p(ws.data_ptr()), ws_bytes, stream)
+
+    st = call(None)  # counts the nodes
+    out_pts = None
+    if st == N.FL_ERR_CAPACITY:
+        out_pts = torch.empty((max(nnode.value, 1), 3), dtype=torch.float64, device=dev)
+        st = call(out_pts)
+    if st == N.FL_ERR_MESH:
+        raise ValueError("an element repeats a vertex")
+    N.check(st, "fl_RaiseHexOrder")
     return out_pts[:nnode.value], out_el
 
 

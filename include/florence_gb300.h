@@ -118,6 +118,25 @@ int fl_RaiseTetOrder(const double *points, int64_t nvert, const int64_t *element
                      const double *pattern, int64_t nodeperelem, double *out_points, int64_t points_capacity,
                      int64_t *nnode, int64_t *out_elements, void *workspace, size_t workspace_bytes,
                      fl_stream_t stream);
+/* fl_RaiseHexOrder: the hex branch of Mesh.GetHighOrderMesh (MeshGeneration/Mesh.py:1388-1389 ->
+ * HigherOrderMeshing/HigherOrderMeshingHex.py:19-135, HighOrderMeshHex) on the device, with the
+ * same arguments and behaviour as fl_RaiseTetOrder except:
+ *   elements        [nelem * 8] linear hexes (int64 vertex ids, the reference's hex vertex order)
+ *   pattern         [nodeperelem * 3] reference coordinates in [-1, 1]^3 of the high-order
+ *                   element's local nodes, its first 8 nodes the vertices in the order of the
+ *                   linear element's columns (the reference's node arrangement); a node's weights
+ *                   are the trilinear shape functions of the 8 vertices at it
+ *   workspace       fl_RaiseHexOrder_workspace_size() bytes (about 180 B per element + 40 B per
+ *                   vertex)
+ * FL_ERR_UNSUPPORTED for a layout that is not vertex / edge / face / interior nodes symmetric
+ * under the edge swaps and the square's symmetries, or nodeperelem > 125 (p = 4).
+ * fl_HexNodeLayout (host only) classifies a pattern the same way (counts as fl_TetNodeLayout). */
+int fl_HexNodeLayout(const double *pattern, int64_t nodeperelem, int64_t *counts);
+size_t fl_RaiseHexOrder_workspace_size(int64_t nelem, int64_t nvert);
+int fl_RaiseHexOrder(const double *points, int64_t nvert, const int64_t *elements, int64_t nelem,
+                     const double *pattern, int64_t nodeperelem, double *out_points, int64_t points_capacity,
+                     int64_t *nnode, int64_t *out_elements, void *workspace, size_t workspace_bytes,
+                     fl_stream_t stream);
 
 /* ------------------------------------------------------------------------------------------
  * Implicit assembly of the tangent stiffness and the internal-force residual (FP64), one

@@ -90,3 +90,63 @@ def test_device_rejects_bad_meshes():
     bad[5, 0] = len(P)  # vertex id out of range
     with pytest.raises(RuntimeError):
         meshes.raise_tet_order_device(P, bad, lam)
+
+
+# ------------------------------------------------------------------------------------------------
+# hexes (fl_RaiseHexOrder)
+# ------------------------------------------------------------------------------------------------
+from test_meshing import REFERENCE_HEX_MESHES, linear_hex_part  # noqa: E402
+
+
+def assert_hex_same_as_host(P, el, xi):
+    Ph, Eh = meshes.raise_hex_order(P, el, xi)
+    Pd, Ed = meshes.raise_hex_order_device(P, el, xi)
+    Pd, Ed = Pd.cpu().numpy(), Ed.cpu().numpy()
+    assert Pd.shape == Ph.shape
+    assert np.array_equal(Ed, Eh)
+    assert np.array_equal(Pd, Ph)  # the same products and sums in the same order
+    return Pd, Ed
+
+
+@pytest.mark.parametrize("name", REFERENCE_HEX_MESHES)
+def test_device_reproduces_reference_high_order_hex_mesh(name):
+    d = load_golden(name)
+    P_ref, E_ref = d["points"], d["elements"].astype(np.int64)
+    xi = meshes.local_pattern(P_ref, E_ref, 0, "hex")
+    P_lin, E_lin = linear_hex_part(P_ref, E_ref)
+    Pd, Ed = assert_hex_same_as_host(P_lin, E_lin, xi)
+    m = permutation_between(Ed, E_ref)
+    assert m is not None
+    assert np.abs(Pd - P_ref[m]).max() <= 1e-12 * np.abs(P_ref).max()
+
+
+@pytest.mark.parametrize("p", [2, 3, 4])
+def test_device_hex_matches_host_on_distorted_shuffled_box(p):
+    """A 7 x 5 x 4 box with jittered vertices, shuffled elements, every element's vertices
+    relabelled by one of the cube's symmetries (so shared edges and faces are seen in every
+    orientation) and two unused vertices."""
+    d = load_golden({2: "hex_p2_nh_q5", 3: "hex_p3_nh", 4: "hex_p4_nh"}[p])
+    xi = meshes.local_pattern(d["points"], d["elements"], 0, "hex")
+    P_s, E_s = meshes.structured_hex((7, 5, 4), (2.0, 1.5, 1.0), xi)
+    P, el = linear_hex_part(P_s, E_s)
+    rng = np.random.default_rng(p)
+    P = P + rng.uniform(-0.02, 0.02, P.shape)
+    el = el[rng.permutation(len(el))]
+    # the cube's rotations as permutations of the reference vertices (sign patterns of xi[:8])
+    sg = np.where(xi[:8] > 0, 1, -1)
+    perms = []
+    for axes in ([0, 1, 2], [1, 2, 0], [2, 0, 1]):
+        for flip in ([1, 1, 1], [-1, -1, 1], [-1, 1, -1], [1, -1, -1]):
+            t = sg[:, axes] * np.array(flip)
+            perms.append([int(np.nonzero((sg == t[k]).all(1))[0][0]) for k in range(8)])
+    pick = rng.integers(0, len(perms), len(el))
+    el = np.stack([el[i, perms[pick[i]]] for i in range(len(el))])
+    P = np.vstack([[[9.0, 9.0, 9.0]], P, [[8.0, 8.0, 8.0]]])
+    el = el + 1
+    Pd, Ed = assert_hex_same_as_host(P, el, xi)
+    assert not np.any(np.abs(Pd - 8.0).max(1) < 1.5)  # the unused vertices are gone
+    nv = P.shape[0] - 2
+    ne, nf, ni = meshes.hex_node_layout(xi)
+    edges = 3 * 7 * 5 * 4 + 2 * (7 * 5 + 5 * 4 + 7 * 4) + 7 + 5 + 4  # edges of a 7 x 5 x 4 box
+    faces = 3 * 7 * 5 * 4 + 7 * 5 + 5 * 4 + 7 * 4
+    assert Pd.shape[0] == nv + edges * ne + faces * nf + len(el) * ni

@@ -94,3 +94,58 @@ def test_host_builder_equispaced_p4_counts():
     # 5 vertices, 9 edges x 3, 7 faces x 3, 2 interiors x 1
     assert P.shape[0] == 5 + 27 + 21 + 2
     assert np.array_equal(E[:, :4], E_lin)
+
+
+# ------------------------------------------------------------------------------------------------
+# hexes (HighOrderMeshHex, Florence/MeshGeneration/HigherOrderMeshing/HigherOrderMeshingHex.py)
+# ------------------------------------------------------------------------------------------------
+REFERENCE_HEX_MESHES = ["hex_p2_nh_q5", "hex_p2_mr", "hex_p3_nh", "hex_p4_nh"]
+
+
+def linear_hex_part(points, elements):
+    """The linear hexes under a high-order hex mesh: vertex nodes (local nodes 0-7) renumbered
+    compactly in increasing id order."""
+    verts = np.unique(elements[:, :8])
+    remap = np.full(int(elements.max()) + 1, -1, np.int64)
+    remap[verts] = np.arange(len(verts))
+    return points[verts], remap[elements[:, :8]]
+
+
+@pytest.mark.parametrize("name", REFERENCE_HEX_MESHES)
+def test_host_hex_builder_reproduces_reference_mesh(name):
+    """The reference's own p = 2, 3, 4 hex meshes (GetHighOrderMesh on a Florence box, Gauss-Lobatto
+    nodes) rebuilt from their linear hexes and one element's node layout: the same mesh up to a
+    node permutation, positions within 1e-12."""
+    d = load_golden(name)
+    P_ref, E_ref = d["points"], d["elements"].astype(np.int64)
+    xi = meshes.local_pattern(P_ref, E_ref, 0, "hex")
+    P_lin, E_lin = linear_hex_part(P_ref, E_ref)
+    Ph, Eh = meshes.raise_hex_order(P_lin, E_lin, xi)
+    m = permutation_between(Eh, E_ref)
+    assert m is not None
+    assert np.abs(Ph - P_ref[m]).max() <= 1e-12 * np.abs(P_ref).max()
+
+
+@pytest.mark.parametrize("p", [2, 3, 4])
+def test_host_hex_builder_matches_structured_builder(p):
+    """A 5 x 4 x 3 box raised from its linear hexes against the structured builder of the same
+    order: the same mesh up to a node permutation (shared edges and faces in every orientation a
+    structured box has), and the classification the device mesher makes of the layout."""
+    d = load_golden({2: "hex_p2_nh_q5", 3: "hex_p3_nh", 4: "hex_p4_nh"}[p])
+    xi = meshes.local_pattern(d["points"], d["elements"], 0, "hex")
+    P_s, E_s = meshes.structured_hex((5, 4, 3), (2.0, 1.5, 1.0), xi)
+    P_lin, E_lin = linear_hex_part(P_s, E_s)
+    Ph, Eh = meshes.raise_hex_order(P_lin, E_lin, xi)
+    m = permutation_between(Eh, E_s)
+    assert m is not None
+    assert np.abs(Ph - P_s[m]).max() <= 1e-12 * np.abs(P_s).max()
+    assert meshes.hex_node_layout(xi) == (p - 1, (p - 1) ** 2, (p - 1) ** 3)
+
+
+def test_hex_layout_without_symmetry_is_rejected():
+    d = load_golden("hex_p2_nh_q5")
+    xi = meshes.local_pattern(d["points"], d["elements"], 0, "hex").copy()
+    edge_nodes = [a for a in range(8, xi.shape[0]) if (np.abs(np.abs(xi[a]) - 1.0) < 1e-9).sum() == 2]
+    xi[edge_nodes[0]] += 0.1 * (np.abs(np.abs(xi[edge_nodes[0]]) - 1.0) > 1e-9)  # off the edge's midpoint
+    with pytest.raises(ValueError):
+        meshes.hex_node_layout(xi)
