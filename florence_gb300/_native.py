@@ -80,7 +80,8 @@ def lib():
                      "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_"):
             getattr(L, name).argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDF_noalloc.argtypes = [INT] + _DF_ARGS
-        L.fl_GlobalAssemblyDF_Blocks.argtypes = [INT, P] + _DF_ARGS
+        L.fl_GlobalAssemblyDF_Blocks.argtypes = [INT, P, P] + _DF_ARGS
+        L.fl_ReferenceGeometry.argtypes = [P, P, P, I64, I64, I64, I64, P, P, P]
         L.fl_ElementBlockOffsets.argtypes = [P, I64, I64, I64, P, P, P, P, P]
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_.argtypes = _DF_ARGS
         L.fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_.argtypes = _DF_ARGS
@@ -154,7 +155,7 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_GlobalAssemblyDF__NeoHookean_", "fl_GlobalAssemblyDF__MooneyRivlin_",
            "fl_GlobalAssemblyDF__NearlyIncompressibleMooneyRivlin_", "fl_GlobalAssemblyDF__LinearElastic_",
            "fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_", "fl_GlobalAssemblyDF_noalloc",
-           "fl_GlobalAssemblyDF_Blocks", "fl_ElementBlockOffsets",
+           "fl_GlobalAssemblyDF_Blocks", "fl_ElementBlockOffsets", "fl_ReferenceGeometry",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_108_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_101_",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_0_", "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_106_",
            "fl_GlobalAssemblyDPF__IsotropicElectroMechanics_105_", "fl_GlobalAssemblyDPF__SteinmannModel_",

@@ -286,14 +286,23 @@ class DeviceAssembler:
         boff = self.block_offsets(stream) if self.mode != "triplet" and \
             N.lib().fl_GetAssemblyArithmetic() == N.FL_ARITH_REFERENCE_TENSOR and rt_supported(self.npe, self.nq) \
             else None
-        if boff is not None:
-            st = L.fl_GlobalAssemblyDF_Blocks(self.mat_id, _ptr(boff), *args)
-        else:
-            st = getattr(L, _DF_ENTRY[self.mat_id])(*args)
+        st = L.fl_GlobalAssemblyDF_Blocks(self.mat_id, _ptr(boff), _ptr(self.reference_geometry(stream)), *args)
         N.check(st, "fl_GlobalAssemblyDF")
         if self.mode == "triplet":
             return I, J, V, T
         return V, T
+
+    def reference_geometry(self, stream=None):
+        """(dX/dxi)^-1 and det(dX/dxi) per element and Gauss point (fl_ReferenceGeometry), computed
+        on first use and kept: [10, nelem * nq] float64. The assembly then forms only the current
+        configuration's part of the kinematics."""
+        if getattr(self, "_geo", None) is None:
+            geo = torch.empty((10, max(1, self.nelem * self.nq)), dtype=torch.float64, device=self.device)
+            N.check(N.lib().fl_ReferenceGeometry(_ptr(self.points), _ptr(self.elements), _ptr(self.Jm), self.nelem,
+                                                 self.npe, self.nq, self.nnode, _ptr(geo), _ptr(self.flags),
+                                                 stream or _stream()), "fl_ReferenceGeometry")
+            self._geo = geo
+        return self._geo
 
     def block_offsets(self, stream=None):
         """The pattern's per-element node-block offsets (fl_ElementBlockOffsets), built on first

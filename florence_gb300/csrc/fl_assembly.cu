@@ -72,6 +72,7 @@ struct AsmArgs {
     const float2 *jmp;
     int *flags;
     const int32_t *boff;  // optional per-element block offsets [nelem][npe][npe] (fl_ElementBlockOffsets)
+    const double *geo = nullptr;  // optional reference geometry [10][nelem * nq] (fl_ReferenceGeometry)
     double *Q;       // scratch [QSTRIDE][ldq]
     float *Qf;       // split-BF16 path: FP32 tangent part [45][ldq] (Q then holds S [9][ldq])
     int64_t e0, ne;  // element chunk [e0, e0+ne)
@@ -242,7 +243,22 @@ __global__ void __launch_bounds__(QP_THREADS) qp_kernel(const AsmArgs A) {
         };
         double G[9], F[9];
         double detJ;
-        if (A.npair) {  // coordinate sums as float pairs (FP32 pipe)
+        if (A.geo && !A.npair) {  // the reference configuration's part from the per-mesh table
+            const int64_t gi = e * nq + g, gs = A.nelem * (int64_t)nq;
+            double iPX[9];
+#pragma unroll
+            for (int k = 0; k < 9; ++k) iPX[k] = __ldg(A.geo + k * gs + gi);
+            const double detX = __ldg(A.geo + 9 * gs + gi);
+            auto xcoords = [&](int a, double &x0, double &x1, double &x2) {
+                uint64_t nd = __ldg(el + a);
+                if (nd >= (uint64_t)A.nnode) {
+                    flag |= FL_FLAG_BAD_INDEX;
+                    nd = 0;
+                }
+                x0 = __ldg(A.Eulerx + nd * 3); x1 = __ldg(A.Eulerx + nd * 3 + 1); x2 = __ldg(A.Eulerx + nd * 3 + 2);
+            };
+            detJ = kinematics_ref<NPE>(jm, xcoords, iPX, detX, __ldg(A.w + g), A.update, G, F);
+        } else if (A.npair) {  // coordinate sums as float pairs (FP32 pipe)
             auto jp = [&](int d, int a) {
                 const float2 v = __ldg(A.jmp + ((size_t)d * NPE + a) * nq + g);
                 return FloatPair(v.x, v.y);
@@ -633,6 +649,45 @@ __global__ void jm_pairs_kernel(const double *Jm, float2 *out, int64_t n) {
     out[i] = make_float2(v.h, v.l);
 }
 
+// The reference configuration's part of the kinematics per (element, Gauss point): (dX/dxi)^-1 and
+// det(dX/dxi), as kinematics_fn forms them (the same sums in the same order), into
+// geo[10][nelem * nq]; constant for a mesh.
+template <int NPE>
+__global__ void __launch_bounds__(QP_THREADS) reference_geometry_kernel(const double *points, const uint64_t *elements,
+                                                                         const double *Jm, int64_t nelem, int nq,
+                                                                         int64_t nnode, double *geo, int *flags) {
+    const int64_t t = (int64_t)blockIdx.x * QP_THREADS + threadIdx.x;
+    if (t >= nelem * nq) return;
+    const int64_t e = t / nq;
+    const int g = (int)(t % nq);
+    const uint64_t *el = elements + e * NPE;
+    double PX[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) PX[k] = 0.0;
+    int flag = 0;
+#pragma unroll 4
+    for (int a = 0; a < NPE; ++a) {
+        const double j0 = __ldg(Jm + ((size_t)0 * NPE + a) * nq + g), j1 = __ldg(Jm + ((size_t)1 * NPE + a) * nq + g),
+                     j2 = __ldg(Jm + ((size_t)2 * NPE + a) * nq + g);
+        uint64_t nd = __ldg(el + a);
+        if (nd >= (uint64_t)nnode) {
+            flag |= FL_FLAG_BAD_INDEX;
+            nd = 0;
+        }
+        const double X0 = __ldg(points + nd * 3), X1 = __ldg(points + nd * 3 + 1), X2 = __ldg(points + nd * 3 + 2);
+        PX[0] += j0 * X0; PX[1] += j0 * X1; PX[2] += j0 * X2;
+        PX[3] += j1 * X0; PX[4] += j1 * X1; PX[5] += j1 * X2;
+        PX[6] += j2 * X0; PX[7] += j2 * X1; PX[8] += j2 * X2;
+    }
+    double iPX[9];
+    const double detX = inv3(PX, iPX);
+    const int64_t gs = nelem * (int64_t)nq;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) geo[k * gs + t] = iPX[k];
+    geo[9 * gs + t] = detX;
+    if (flag && flags) atomicOr(flags, flag);
+}
+
 static size_t pair_prep_bytes(int64_t nnode, int npe, int nq) {
     return ((sizeof(float) * 12 * (size_t)nnode + 255) & ~(size_t)255) +
            ((sizeof(float2) * 3 * (size_t)npe * nq + 255) & ~(size_t)255);
@@ -833,7 +888,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
                        const int32_t *data_local_indices, const int32_t *data_global_indices, MatParams mp,
                        int *flags, double *scratch, size_t scratch_bytes, cudaStream_t stream,
                        const double *eparams = nullptr, const double *orient = nullptr,
-                       const int32_t *boff = nullptr) {
+                       const int32_t *boff = nullptr, const double *geo = nullptr) {
     if (ndim != 3 || nvar != 3 || H_VoigtSize != 6) return FL_ERR_ARG;
     if (nelem < 0 || nnode <= 0) return FL_ERR_ARG;
     if (ngauss <= 0 || ngauss > 343) return FL_ERR_UNSUPPORTED;
@@ -869,6 +924,7 @@ int global_assembly_df(int mat, const double *points, const uint64_t *elements, 
     A.npair = nullptr;
     A.jmp = nullptr;
     A.boff = boff;
+    A.geo = geo;
     A.e0 = A.ne = A.ldq = 0;
     A.qc = 1;
     if (recompute_sparsity_pattern) {
@@ -2284,7 +2340,28 @@ int fl_GlobalAssemblyDF__AnisotropicMooneyRivlin_1_(FL_GLOBAL_ASSEMBLY_DF_ARGS) 
                                   anisotropic_orientations);
 }
 
-int fl_GlobalAssemblyDF_Blocks(int material_number, const int32_t *block_offsets, FL_GLOBAL_ASSEMBLY_DF_ARGS) {
+int fl_ReferenceGeometry(const double *points, const uint64_t *elements, const double *Jm, int64_t nelem,
+                         int64_t nodeperelem, int64_t ngauss, int64_t nnode, double *geometry, int *flags,
+                         fl_stream_t stream) {
+    if (nelem < 0 || ngauss <= 0 || nnode <= 0) return FL_ERR_ARG;
+    if (nelem == 0) return FL_OK;
+    if (!points || !elements || !Jm || !geometry) return FL_ERR_ARG;
+    const int64_t n = nelem * ngauss;
+    const unsigned grid = (unsigned)((n + fl::QP_THREADS - 1) / fl::QP_THREADS);
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (nodeperelem) {
+#define FL_GEO_CASE(NPE) \
+        case NPE: fl::reference_geometry_kernel<NPE><<<grid, fl::QP_THREADS, 0, st>>>(points, elements, Jm, nelem, (int)ngauss, nnode, geometry, flags); break;
+        FL_GEO_CASE(4) FL_GEO_CASE(8) FL_GEO_CASE(10) FL_GEO_CASE(20) FL_GEO_CASE(27) FL_GEO_CASE(35) FL_GEO_CASE(64)
+        FL_GEO_CASE(125)
+#undef FL_GEO_CASE
+        default: return FL_ERR_UNSUPPORTED;
+    }
+    return fl::launch_status();
+}
+
+int fl_GlobalAssemblyDF_Blocks(int material_number, const int32_t *block_offsets, const double *reference_geometry,
+                               FL_GLOBAL_ASSEMBLY_DF_ARGS) {
     (void)Eulerp; (void)bases; (void)local_rows_stiffness; (void)local_cols_stiffness; (void)sorted_elements;
     (void)sorter; (void)rho; (void)mue; (void)eps_1; (void)eps_2; (void)eps_3; (void)eps_e;
     fl::MatParams mp;
@@ -2294,7 +2371,7 @@ int fl_GlobalAssemblyDF_Blocks(int material_number, const int32_t *block_offsets
                                   nnode, H_VoigtSize, requires_geometry_update, I_stiff, J_stiff, V_stiff, T,
                                   recompute_sparsity_pattern, squeeze_sparsity_pattern, data_local_indices,
                                   data_global_indices, mp, flags, nullptr, 0, (cudaStream_t)stream, nullptr,
-                                  anisotropic_orientations, block_offsets);
+                                  anisotropic_orientations, block_offsets, reference_geometry);
 }
 
 int fl_GlobalAssemblyDF__MooneyRivlin_(FL_GLOBAL_ASSEMBLY_DF_ARGS) {

@@ -251,6 +251,34 @@ __device__ __forceinline__ double kinematics_fn(JmFn jm, CoordFn coords, double 
     return update ? w * fabs(detx) : w * fabs(detX);
 }
 
+// kinematics_fn with the reference-configuration part read from a per-mesh table: iPX = (dX/dxi)^-1
+// and detX = det(dX/dxi) at the Gauss point (reference_geometry_kernel) -- the same values the sums
+// over the reference coordinates give, so the results are identical; only the current
+// configuration's sums are formed. coords(a, x0, x1, x2): current coordinates of node a.
+template <int NPE, class JmFn, class CoordFn>
+__device__ __forceinline__ double kinematics_ref(JmFn jm, CoordFn coords, const double *iPX, double detX, double w,
+                                                 int update, double *G, double *F) {
+    double Px[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) Px[k] = 0.0;
+#pragma unroll 4
+    for (int a = 0; a < NPE; ++a) {
+        const double j0 = jm(0, a), j1 = jm(1, a), j2 = jm(2, a);
+        double x0, x1, x2;
+        coords(a, x0, x1, x2);
+        Px[0] += j0 * x0; Px[1] += j0 * x1; Px[2] += j0 * x2;
+        Px[3] += j1 * x0; Px[4] += j1 * x1; Px[5] += j1 * x2;
+        Px[6] += j2 * x0; Px[7] += j2 * x1; Px[8] += j2 * x2;
+    }
+    const double detx = inv3(Px, G);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            F[i * 3 + j] = Px[0 * 3 + i] * iPX[j * 3 + 0] + Px[1 * 3 + i] * iPX[j * 3 + 1] + Px[2 * 3 + i] * iPX[j * 3 + 2];
+    return update ? w * fabs(detx) : w * fabs(detX);
+}
+
 // kinematics_fn with the element coordinates in arrays X, x [npe*3]
 template <int NPE, class JmFn>
 __device__ __forceinline__ double kinematics(JmFn jm, const double *X, const double *x, double w, int update, double *G,

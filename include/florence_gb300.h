@@ -304,12 +304,25 @@ int fl_ElementBlockOffsets(const uint64_t *elements, int64_t nelem, int64_t node
                            const int32_t *indptr, const int32_t *indices, int32_t *block_offsets, int *flags,
                            fl_stream_t stream);
 
-/* fl_GlobalAssemblyDF__<Mat>_ with the mesh's block offsets (fl_ElementBlockOffsets) supplied by a
- * caller that keeps the mesh on the device between calls (no reference counterpart): in CSR mode
- * with FL_ARITH_REFERENCE_TENSOR the contraction scatters through them instead of building them in
- * the call. Same arguments and results otherwise, preceded by material_number (FL_MATERIAL_*) and
- * block_offsets (may be NULL: then as fl_GlobalAssemblyDF__<Mat>_). */
-int fl_GlobalAssemblyDF_Blocks(int material_number, const int32_t *block_offsets, FL_GLOBAL_ASSEMBLY_DF_ARGS);
+/* The reference configuration's part of the kinematics (no reference counterpart; the reference
+ * recomputes it in every call, _KinematicMeasures_.h:64-99): per element and Gauss point the
+ * inverse of dX/dxi = sum_a Jm[.][a][g] X_a (9 values, row-major) and its determinant, into
+ * geometry[10][nelem * ngauss] (device FP64, element-major within each row: index e * ngauss + g).
+ * Constant for a mesh; the assembly given it (fl_GlobalAssemblyDF_Blocks) forms only the current
+ * configuration's sums, with results identical to recomputing it. flags: optional device int,
+ * FL_FLAG_BAD_INDEX for an out-of-range node id. No synchronisation. */
+int fl_ReferenceGeometry(const double *points, const uint64_t *elements, const double *Jm, int64_t nelem,
+                         int64_t nodeperelem, int64_t ngauss, int64_t nnode, double *geometry, int *flags,
+                         fl_stream_t stream);
+
+/* fl_GlobalAssemblyDF__<Mat>_ with per-mesh data supplied by a caller that keeps the mesh on the
+ * device between calls (no reference counterpart): the block offsets (fl_ElementBlockOffsets; in
+ * CSR mode with FL_ARITH_REFERENCE_TENSOR the contraction scatters through them instead of building
+ * them in the call) and the reference geometry (fl_ReferenceGeometry, computed for the same points,
+ * elements and Jm). Same arguments and results otherwise, preceded by material_number
+ * (FL_MATERIAL_*), block_offsets and reference_geometry (each may be NULL). */
+int fl_GlobalAssemblyDF_Blocks(int material_number, const int32_t *block_offsets, const double *reference_geometry,
+                               FL_GLOBAL_ASSEMBLY_DF_ARGS);
 
 /* Tiling of the split-BF16 tensor-core tangent (fl_GlobalAssemblyDF_Mixed; no reference
  * counterpart) for every later call of the process: tile_group = 128-row tiles of the element's
