@@ -127,6 +127,7 @@ def lib():
         L.fl_MaskedMatVecBlocks.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_MaskedMatVecBlocksF32.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_SplitPairs.argtypes = [I64, P, P, P]
+        L.fl_MaskedMatMatBlocksF32.argtypes = [P, P, P, I64, P, P, P, I64, P]
         L.fl_MaskedMatVecBlocksPair.argtypes = [P, P, P, I64, P, P, P, P, P]
         L.fl_BlockJacobiInverse.argtypes = [P, P, P, I64, P, P, P, P]
         L.fl_BlockJacobiApply.argtypes = [I64, P, P, D, P, P, INT, P]
@@ -164,5 +165,5 @@ EXPORTS = ["fl_status_string", "fl_ComputeSparsityPattern_workspace_size", "fl_C
            "fl_BlockJacobiPCG_workspace_size", "fl_BlockJacobiPCG", "fl_SetPCGDeviceLoop", "fl_GetPCGDeviceLoop", "fl_ReferenceGradients", "fl_ReferenceGradientsPair", "fl_InternalForcePair",
            "fl_InternalForceF32", "fl_CentralDifferenceUpdate", "fl_StrainEnergy", "fl_GlobalAssemblyDF_Mixed",
            "fl_GlobalAssemblyDF_Batched", "fl_SetAssemblyTuning", "fl_SetAssemblyArithmetic", "fl_GetAssemblyArithmetic", "fl_SetTensorCoreTiling", "fl_AssembleExternalTractionForces", "fl_AssembleBodyForces", "fl_MLP_num_params", "fl_MLP_workspace_size",
-           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec", "fl_MaskedMatVecBlocks", "fl_MaskedMatVecBlocksF32", "fl_SplitPairs", "fl_MaskedMatVecBlocksPair",
+           "fl_MLPForward", "fl_MLPGradients", "fl_MLPAdamStep", "fl_NodalTransfer", "fl_MaskedMatVec", "fl_MaskedMatVecBlocks", "fl_MaskedMatVecBlocksF32", "fl_SplitPairs", "fl_MaskedMatVecBlocksPair", "fl_MaskedMatMatBlocksF32",
            "fl_BlockJacobiInverse", "fl_BlockJacobiApply", "fl_CoarsePCG_workspace_size", "fl_CoarsePCG"]

@@ -129,6 +129,56 @@ __global__ void __launch_bounds__(MG_NT) masked_spmv_blocks_kernel(const int32_t
     }
 }
 
+// Y = K_ff X for M columns at once (X, Y row-major [nrows][M], FP32; values FP32), node-blocked
+// pattern: a warp per node, lanes over columns (M / 32 each), the node's column blocks in turn
+// (their nine values broadcast to the warp); X zero on fixed dofs, fixed rows give 0. For
+// projections onto a reduced basis, where FP32 products suffice.
+template <int M>
+__global__ void __launch_bounds__(MG_NT) masked_spmm_blocks_kernel(const int32_t *indptr, const int32_t *indices,
+                                                                   const float *vals, int64_t nnode,
+                                                                   const int8_t *fixed, const float *X, float *Y,
+                                                                   int64_t ncols) {
+    constexpr int CPL = M / 32;  // columns per lane
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = (blockIdx.x * (int64_t)MG_NT + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * MG_NT) >> 5;
+    for (int64_t m = warp; m < nnode; m += nwarps) {
+        const int p0 = indptr[3 * m], p1 = indptr[3 * m + 1], p2 = indptr[3 * m + 2];
+        const int nb = (p1 - p0) / 3;
+        float acc[3][CPL];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) acc[i][j] = 0.f;
+        for (int blk = 0; blk < nb; ++blk) {
+            const int c = indices[p0 + 3 * blk];
+            if (c < 0 || c + 2 >= ncols) continue;
+            float v[3][3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                v[0][k] = vals[p0 + 3 * blk + k];
+                v[1][k] = vals[p1 + 3 * blk + k];
+                v[2][k] = vals[p2 + 3 * blk + k];
+            }
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) {
+                const int col = lane + 32 * j;
+                const float x0 = X[(c + 0) * (int64_t)M + col], x1 = X[(c + 1) * (int64_t)M + col],
+                            x2 = X[(c + 2) * (int64_t)M + col];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) acc[i][j] = fmaf(v[i][0], x0, fmaf(v[i][1], x1, fmaf(v[i][2], x2, acc[i][j])));
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int64_t row = 3 * m + i;
+            const bool fr = fixed[row] != 0;
+#pragma unroll
+            for (int j = 0; j < CPL; ++j) Y[row * M + lane + 32 * j] = fr ? 0.f : acc[i][j];
+        }
+    }
+}
+
 // FP64 values or vectors -> float pairs hi + lo (hi = RN(v), lo = RN(v - hi))
 __global__ void __launch_bounds__(MG_NT) split_pairs_kernel(int64_t n, const double *v, float2 *out) {
     for (int64_t i = blockIdx.x * (int64_t)MG_NT + threadIdx.x; i < n; i += (int64_t)gridDim.x * MG_NT) {
@@ -637,6 +687,24 @@ int fl_MaskedMatVecBlocksPair(const int32_t *indptr, const int32_t *indices, con
     fl::masked_spmv_pair_kernel<LPN><<<fl::grid_of(warps * 32, fl::MG_NT), fl::MG_NT, 0, (cudaStream_t)stream>>>(
         indptr, indices, reinterpret_cast<const float2 *>(value_pairs), nnode, fixed,
         reinterpret_cast<const float2 *>(x_pairs), b, y, nrows);
+    return fl::launch_status();
+}
+
+int fl_MaskedMatMatBlocksF32(const int32_t *indptr, const int32_t *indices, const float *values, int64_t nrows,
+                             const int8_t *fixed, const float *X, float *Y, int64_t ncolumns, fl_stream_t stream) {
+    if (nrows < 0 || nrows % 3) return FL_ERR_ARG;
+    if (nrows == 0) return FL_OK;
+    if (!indptr || !indices || !values || !fixed || !X || !Y) return FL_ERR_ARG;
+    const int64_t nnode = nrows / 3;
+    const int64_t warps = std::min<int64_t>(nnode, (int64_t)152 * 64);
+    const unsigned grid = fl::grid_of(warps * 32, fl::MG_NT);
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (ncolumns) {
+        case 32: fl::masked_spmm_blocks_kernel<32><<<grid, fl::MG_NT, 0, st>>>(indptr, indices, values, nnode, fixed, X, Y, nrows); break;
+        case 64: fl::masked_spmm_blocks_kernel<64><<<grid, fl::MG_NT, 0, st>>>(indptr, indices, values, nnode, fixed, X, Y, nrows); break;
+        case 128: fl::masked_spmm_blocks_kernel<128><<<grid, fl::MG_NT, 0, st>>>(indptr, indices, values, nnode, fixed, X, Y, nrows); break;
+        default: return FL_ERR_UNSUPPORTED;
+    }
     return fl::launch_status();
 }
 

@@ -162,14 +162,29 @@ class WarmStart:
         n = asm.nnode * 3
         free = newton.free
         P = self.Phi * free[:, None]
+        m = P.shape[1]
+        mp = next(k for k in (32, 64, 128, m) if k >= m)
+        if mp > 128:
+            raise ValueError("the Galerkin correction takes at most 128 modes")
+        # K P with the library's node-block product on FP32 values (the projection is a start for
+        # the FP64 Newton iteration, which removes the FP32 rounding); the small reduced system is
+        # solved on the host
+        P32 = torch.zeros((n, mp), dtype=torch.float32, device=P.device)
+        P32[:, :m] = P
+        KP = torch.empty_like(P32)
+        V32 = torch.empty(asm.nnz, dtype=torch.float32, device=P.device)
         c = P.T @ u
         u = P @ c
         for _ in range(iters):
             newton._assemble(u, mixed=False)
-            K = torch.sparse_csr_tensor(asm.indptr, asm.indices, newton.V, size=(n, n))
-            Kr = P.T @ ((K @ P) * free[:, None])
+            V32.copy_(newton.V)
+            N.check(N.lib().fl_MaskedMatMatBlocksF32(_ptr(asm.indptr), _ptr(asm.indices), _ptr(V32), n,
+                                                     _ptr(newton.fixed), _ptr(P32), _ptr(KP), mp, _stream()),
+                    "fl_MaskedMatMatBlocksF32")
+            Kr = P.T @ KP[:, :m].double()
             Rr = P.T @ ((newton.T - F) * free)
-            c = c - torch.linalg.solve(Kr, Rr)
+            dc = np.linalg.solve(Kr.cpu().numpy(), Rr.cpu().numpy())
+            c = c - torch.from_numpy(dc).to(P.device)
             u = P @ c
         return u
 

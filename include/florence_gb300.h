@@ -514,6 +514,11 @@ int fl_MaskedMatVecBlocks(const int32_t *indptr, const int32_t *indices, const d
 int fl_MaskedMatVecBlocksF32(const int32_t *indptr, const int32_t *indices, const float *values, int64_t nrows,
                              const int8_t *fixed, const double *x, const double *b, double *y, fl_stream_t stream);
 int fl_SplitPairs(int64_t n, const double *v, float *pairs, fl_stream_t stream);
+/* fl_MaskedMatMatBlocksF32: Y = K_ff X for ncolumns (32, 64 or 128) columns at once, X and Y
+ * row-major [nrows][ncolumns] FP32, FP32 values of a node-blocked pattern; X zero on fixed dofs.
+ * For projections onto a reduced basis (the warm start's Galerkin correction). */
+int fl_MaskedMatMatBlocksF32(const int32_t *indptr, const int32_t *indices, const float *values, int64_t nrows,
+                             const int8_t *fixed, const float *X, float *Y, int64_t ncolumns, fl_stream_t stream);
 int fl_MaskedMatVecBlocksPair(const int32_t *indptr, const int32_t *indices, const float *value_pairs, int64_t nrows,
                               const int8_t *fixed, const float *x_pairs, const double *b, double *y,
                               fl_stream_t stream);

@@ -105,3 +105,28 @@ def test_coarse_fallback_path_matches(beam):
         assert rel <= 1e-10
         sols.append(x)
     assert float(torch.linalg.vector_norm(sols[0] - sols[1]) / torch.linalg.vector_norm(sols[1])) < 1e-8
+
+
+@pytest.mark.parametrize("m", [32, 64, 128])
+def test_multi_column_product(beam, m):
+    """fl_MaskedMatMatBlocksF32 (the warm start's K Phi): FP32 values and columns against scipy's
+    FP64 product, fixed rows zero."""
+    import scipy.sparse as sp
+    from florence_gb300 import _native as N
+    from florence_gb300.assembly import _ptr, _stream
+    asm, P, fixed, f, pat = beam
+    V, _ = asm.assemble(torch.from_numpy(P).cuda())
+    n = P.size
+    free = ~fixed.astype(bool)
+    X = np.random.default_rng(m).standard_normal((n, m)) * free[:, None]
+    X32 = torch.from_numpy(X).float().cuda().contiguous()
+    Y = torch.empty_like(X32)
+    fx = torch.from_numpy(fixed.astype(np.int8)).cuda()
+    V32 = V.float().contiguous()
+    N.check(N.lib().fl_MaskedMatMatBlocksF32(_ptr(asm.indptr), _ptr(asm.indices), _ptr(V32), n, _ptr(fx), _ptr(X32),
+                                             _ptr(Y), m, _stream()), "fl_MaskedMatMatBlocksF32")
+    K = sp.csr_matrix((V.cpu().numpy(), asm.indices.cpu().numpy(), asm.indptr.cpu().numpy()), shape=(n, n))
+    ref = (K @ X32.double().cpu().numpy()) * free[:, None]
+    got = Y.double().cpu().numpy()
+    assert np.all(got[~free] == 0.0)
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-5
