@@ -217,10 +217,14 @@ class DeviceAssembler:
     (mu1, mu2, lamb, mu3, with `orientations` [E,3], one fibre direction per element).
     mode: 'csr' (the reference's element-to-nonzero maps), 'squeeze' (binary search in each row)
     or 'triplet' (I, J, V per element entry).
+    deterministic: CSR outputs bit-identical from run to run (the atomic adds of the scatter
+    otherwise land in an order that varies): the elements are coloured so that no two elements of
+    a colour share a node, and the colours are assembled one after another, so that every CSR entry
+    and residual entry receives its contributions in colour order, one per colour.
     """
 
     def __init__(self, points, elements, Jm, AllGauss, material, params, mode="csr", device="cuda",
-                 requires_geometry_update=1, Bases=None, sparsity=None, orientations=None):
+                 requires_geometry_update=1, Bases=None, sparsity=None, orientations=None, deterministic=False):
         self.device = torch.device(device)
         self.points = _to_dev(points, torch.float64, self.device)
         self.elements = _to_dev(elements, torch.int64, self.device)
@@ -258,6 +262,50 @@ class DeviceAssembler:
             self.nnz = self.indices.shape[0]
         elif mode != "triplet":
             raise ValueError("mode must be 'csr', 'squeeze' or 'triplet'")
+        self.deterministic = bool(deterministic)
+        self._colour = None
+        if self.deterministic:
+            if mode == "triplet":
+                raise ValueError("deterministic assembly takes the CSR modes (triplets have no additions)")
+            self._colour = self._colour_elements()
+
+    def _colour_elements(self):
+        """Greedy node-disjoint colouring (host, once per mesh): each element takes the smallest
+        colour none of its nodes' elements has so far. Returns the colour-sorted element order's
+        pieces per colour: (elements, orientations, block offsets, reference geometry)."""
+        el = self.elements.cpu().numpy()
+        used = np.zeros(self.nnode, np.uint64)          # per node: bitmask of the colours around it
+        colour = np.empty(self.nelem, np.int64)
+        extra = {}                                      # beyond 64 colours: node -> set of colours
+        for e in range(self.nelem):
+            nodes = el[e]
+            m = np.bitwise_or.reduce(used[nodes])
+            if m != np.uint64(0xFFFFFFFFFFFFFFFF):
+                c = int((~int(m) & (int(m) + 1)).bit_length() - 1)
+            else:
+                taken = set().union(*(extra.get(int(n), set()) for n in nodes))
+                c = 64
+                while c in taken:
+                    c += 1
+            colour[e] = c
+            if c < 64:
+                used[nodes] |= np.uint64(1) << np.uint64(c)
+            else:
+                for n in nodes:
+                    extra.setdefault(int(n), set()).add(c)
+        order = np.argsort(colour, kind="stable")
+        counts = np.bincount(colour)
+        pieces = []
+        start = 0
+        for c, k in enumerate(counts):
+            if k == 0:
+                continue
+            idx = torch.from_numpy(order[start:start + k]).to(self.device)
+            sub = self.elements[idx].contiguous()
+            orient = self.orient[idx].contiguous() if self.orient is not None else None
+            pieces.append(dict(elements=sub, orient=orient, count=int(k)))
+            start += k
+        return pieces
 
     # -- implicit tangent + residual ------------------------------------------------------------
     def assemble(self, Eulerx, V=None, T=None, I=None, J=None, stream=None):
@@ -277,6 +325,9 @@ class DeviceAssembler:
             V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device) if V is None else V
             Ip, Jp, dl, dg = self.indptr, self.indices, self.data_local, self.data_global
         mu, mu1, mu2, lamb, mu3 = _abi_params(self.mat_id, self.params)
+        if self.deterministic:
+            self._assemble_by_colour(x, V, T, mu, mu1, mu2, lamb, mu3, stream)
+            return V, T
         args = (_ptr(self.points), _ptr(self.elements), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
                 3, 3, self.nq, self.nelem, self.npe, self.nnode, 6, self.update, None, None,
                 _ptr(Ip), _ptr(Jp), _ptr(V), _ptr(T), 1 if self.mode == "triplet" else 0,
@@ -291,6 +342,37 @@ class DeviceAssembler:
         if self.mode == "triplet":
             return I, J, V, T
         return V, T
+
+    def _assemble_by_colour(self, x, V, T, mu, mu1, mu2, lamb, mu3, stream):
+        """One call per colour on that colour's elements (their block offsets and reference
+        geometry built on first use); the CSR positions by block offsets (reference tensor) or row
+        search, never the element-to-nonzero maps (which follow the original element order)."""
+        L = N.lib()
+        rt = N.lib().fl_GetAssemblyArithmetic() == N.FL_ARITH_REFERENCE_TENSOR and rt_supported(self.npe, self.nq)
+        st_ = stream or _stream()
+        for pc in self._colour:
+            el = pc["elements"]
+            if "geo" not in pc:
+                geo = torch.empty((10, max(1, pc["count"] * self.nq)), dtype=torch.float64, device=self.device)
+                N.check(L.fl_ReferenceGeometry(_ptr(self.points), _ptr(el), _ptr(self.Jm), pc["count"], self.npe,
+                                               self.nq, self.nnode, _ptr(geo), _ptr(self.flags), st_),
+                        "fl_ReferenceGeometry")
+                pc["geo"] = geo
+            boff = None
+            if rt:
+                if "boff" not in pc:
+                    b = torch.empty((pc["count"], self.npe, self.npe), dtype=torch.int32, device=self.device)
+                    N.check(L.fl_ElementBlockOffsets(_ptr(el), pc["count"], self.npe, self.nnode, _ptr(self.indptr),
+                                                     _ptr(self.indices), _ptr(b), _ptr(self.flags), st_),
+                            "fl_ElementBlockOffsets")
+                    pc["boff"] = b
+                boff = pc["boff"]
+            args = (_ptr(self.points), _ptr(el), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
+                    3, 3, self.nq, pc["count"], self.npe, self.nnode, 6, self.update, None, None,
+                    _ptr(self.indptr), _ptr(self.indices), _ptr(V), _ptr(T), 0, 1, None, None, None, None,
+                    1.0, mu, mu1, mu2, mu3, 0.0, lamb, 0.0, 0.0, 0.0, 0.0, _ptr(pc["orient"]), _ptr(self.flags), st_)
+            N.check(L.fl_GlobalAssemblyDF_Blocks(self.mat_id, _ptr(boff), _ptr(pc["geo"]), *args),
+                    "fl_GlobalAssemblyDF (colour)")
 
     def reference_geometry(self, stream=None):
         """(dX/dxi)^-1 and det(dX/dxi) per element and Gauss point (fl_ReferenceGeometry), computed
