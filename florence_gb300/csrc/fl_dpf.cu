@@ -7,8 +7,10 @@
 //
 // One CTA per element (grid-stride): the element's coordinates and potentials are staged in
 // shared memory; a thread per Gauss point computes the spatial gradients, weight, electric
-// displacement, stress and 9x9 Hessian (fl_dpf.cuh) into shared memory; then a thread per tangent
-// entry sums its Gauss-point contributions and scatters it, and a thread per dof its residual.
+// displacement, stress and 9x9 Hessian (fl_dpf.cuh) into shared memory; then a thread per node
+// pair a <= b sums its 4 x 4 tangent block over the Gauss points and scatters it and its mirror
+// (CSR positions found once per row of the block, the block's four columns consecutive in a
+// node-blocked pattern), and a thread per dof its residual.
 // Node ids and map entries are range-checked (FL_FLAG_BAD_INDEX, the entry is skipped);
 // det F <= 0 sets FL_FLAG_NONPOSITIVE_J.
 #include <algorithm>
@@ -75,50 +77,61 @@ __global__ void __launch_bounds__(DP_NT) dpf_kernel(const DpfArgs A, const MAT m
             if (!(J > 0.0) && A.err) atomicOr(A.err, FL_FLAG_NONPOSITIVE_J);
         }
         __syncthreads();
-        if (A.mode == 1) {  // triplets, entry e*ndof^2 + r*ndof + c
-            for (int64_t k = threadIdx.x; k < cap; k += DP_NT) {
-                const int r = (int)(k / ndof), c = (int)(k % ndof);
-                const int a = r / dpf::NV, v = r % dpf::NV, b = c / dpf::NV, u = c % dpf::NV;
-                double s = 0.0;
-                for (int g = 0; g < nq; ++g)
-                    s += dv[g] * dpf::entry(a, v, b, u, npe, SG + (size_t)3 * npe * g, H + 81 * g, sig + 9 * g);
+        // a thread per node pair a <= b: its 4 x 4 block summed over the Gauss points
+        // (dpf::pair_block), scattered at (a, v), (b, u) and, for a != b, mirrored to (b, u), (a, v)
+        // (the tangent is symmetric)
+        const int npairs = npe * (npe + 1) / 2;
+        for (int pi = threadIdx.x; pi < npairs; pi += DP_NT) {
+            int a = 0, rem = pi;  // node a has npe - a pairs (a, b >= a)
+            while (rem >= npe - a) {
+                rem -= npe - a;
+                ++a;
+            }
+            const int b = a + rem;
+            double B[dpf::NV][dpf::NV];
+#pragma unroll
+            for (int v = 0; v < dpf::NV; ++v)
+#pragma unroll
+                for (int u = 0; u < dpf::NV; ++u) B[v][u] = 0.0;
+            for (int g = 0; g < nq; ++g)
+                dpf::pair_block(a, b, npe, SG + (size_t)3 * npe * g, H + 81 * g, sig + 9 * g, dv[g], B);
+            if (A.mode == 1) {  // triplets, entry e*ndof^2 + r*ndof + c
                 const int64_t na = node[a] < 0 ? 0 : node[a], nb = node[b] < 0 ? 0 : node[b];
-                A.I[e * cap + k] = (int32_t)(dpf::NV * na + v);
-                A.J[e * cap + k] = (int32_t)(dpf::NV * nb + u);
-                A.V[e * cap + k] = s;
-            }
-        } else if (A.mode == 0) {  // CSR through the element-to-nonzero maps
-            for (int64_t k = threadIdx.x; k < cap; k += DP_NT) {
-                const int32_t lk = A.dl[e * cap + k], pos = A.dg[e * cap + k];
-                if (lk < 0 || lk >= cap || pos < 0 || pos >= A.nnz) {
-                    if (A.err) atomicOr(A.err, FL_FLAG_BAD_INDEX);
-                    continue;
-                }
-                const int r = lk / ndof, c = lk % ndof;
-                const int a = r / dpf::NV, v = r % dpf::NV, b = c / dpf::NV, u = c % dpf::NV;
-                double s = 0.0;
-                for (int g = 0; g < nq; ++g)
-                    s += dv[g] * dpf::entry(a, v, b, u, npe, SG + (size_t)3 * npe * g, H + 81 * g, sig + 9 * g);
-                atomicAdd(A.V + pos, s);
-            }
-        } else {  // CSR, the column searched in each row
-            for (int64_t k = threadIdx.x; k < cap; k += DP_NT) {
-                const int r = (int)(k / ndof), c = (int)(k % ndof);
-                const int a = r / dpf::NV, v = r % dpf::NV, b = c / dpf::NV, u = c % dpf::NV;
+                for (int v = 0; v < dpf::NV; ++v)
+                    for (int u = 0; u < dpf::NV; ++u) {
+                        const int64_t k1 = (int64_t)(dpf::NV * a + v) * ndof + dpf::NV * b + u;
+                        A.I[e * cap + k1] = (int32_t)(dpf::NV * na + v);
+                        A.J[e * cap + k1] = (int32_t)(dpf::NV * nb + u);
+                        A.V[e * cap + k1] = B[v][u];
+                        if (a != b) {
+                            const int64_t k2 = (int64_t)(dpf::NV * b + u) * ndof + dpf::NV * a + v;
+                            A.I[e * cap + k2] = (int32_t)(dpf::NV * nb + u);
+                            A.J[e * cap + k2] = (int32_t)(dpf::NV * na + v);
+                            A.V[e * cap + k2] = B[v][u];
+                        }
+                    }
+            } else {  // CSR (maps or row search alike: the block's four columns are found per row)
                 if (node[a] < 0 || node[b] < 0) continue;
-                double s = 0.0;
-                for (int g = 0; g < nq; ++g)
-                    s += dv[g] * dpf::entry(a, v, b, u, npe, SG + (size_t)3 * npe * g, H + 81 * g, sig + 9 * g);
-                const int64_t row = dpf::NV * node[a] + v;
-                const int32_t col = (int32_t)(dpf::NV * node[b] + u);
-                int lo = A.indptr[row], hi = A.indptr[row + 1];
-                while (lo < hi) {
-                    const int mid = lo + (hi - lo) / 2;
-                    if (A.indices[mid] < col) lo = mid + 1;
-                    else hi = mid;
+                for (int side = 0; side < (a != b ? 2 : 1); ++side) {
+                    const int64_t nr = side ? node[b] : node[a], nc = side ? node[a] : node[b];
+                    for (int v = 0; v < dpf::NV; ++v) {
+                        const int64_t row = dpf::NV * nr + v;
+                        const int32_t col0 = (int32_t)(dpf::NV * nc);
+                        const int r0 = A.indptr[row], r1 = A.indptr[row + 1];
+                        int lo = r0, hi = r1;
+                        while (lo < hi) {
+                            const int mid = lo + (hi - lo) / 2;
+                            if (A.indices[mid] < col0) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        for (int u = 0; u < dpf::NV; ++u) {
+                            const double val = side ? B[u][v] : B[v][u];
+                            const int p = lo + u;
+                            if (p < r1 && A.indices[p] == col0 + u) atomicAdd(A.V + p, val);
+                            else if (A.err) atomicOr(A.err, FL_FLAG_BAD_INDEX);
+                        }
+                    }
                 }
-                if (lo < A.indptr[row + 1] && A.indices[lo] == col) atomicAdd(A.V + lo, s);
-                else if (A.err) atomicOr(A.err, FL_FLAG_BAD_INDEX);
             }
         }
         if (A.update)
@@ -162,8 +175,9 @@ static int dpf_assemble(const double *points, const uint64_t *elements, const do
         if (!I_stiff || !J_stiff) return FL_ERR_ARG;  // indptr, indices (the reference's I/J slots)
         A.mode = 2; A.indptr = I_stiff; A.indices = J_stiff;
     } else {
-        if (!I_stiff || !data_local_indices || !data_global_indices) return FL_ERR_ARG;
-        A.mode = 0; A.dl = data_local_indices; A.dg = data_global_indices;
+        if (!I_stiff || !J_stiff || !data_local_indices || !data_global_indices) return FL_ERR_ARG;
+        // the positions the maps name are found in the pattern itself (the same positions)
+        A.mode = 0; A.dl = data_local_indices; A.dg = data_global_indices; A.indptr = I_stiff; A.indices = J_stiff;
         int32_t nnz32 = 0;  // indptr[4 N]: the pattern's size, read once
         FL_CUDA_TRY(cudaMemcpyAsync(&nnz32, I_stiff + 4 * nnode, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
         FL_CUDA_TRY(cudaStreamSynchronize(stream));

@@ -510,6 +510,32 @@ FL_HD double entry(int a, int v, int b, int u, int npe, const double *SG, const 
     return r;
 }
 
+// one Gauss point's contribution (without dv) to the 4 x 4 block of node pair (a, b), added to
+// K[v][u]: the same B H B^T plus geometric term as entry(), grouped as sum_p sa[p] W_u[ca[p]] with
+// W_u[c] = sum_q H[c][cb[q]] sb[q] formed once for the block's four columns (~10 FP64 operations
+// per entry instead of ~25)
+FL_HD void pair_block(int a, int b, int npe, const double *SG, const double *H, const double *sigma, double w,
+                      double K[NV][NV]) {
+    const double ga[3] = {SG[a], SG[npe + a], SG[2 * npe + a]};
+    const double gb[3] = {SG[b], SG[npe + b], SG[2 * npe + b]};
+    double W[NV][HV];
+    for (int u = 0; u < NV; ++u) {
+        int cb[3];
+        double sb[3];
+        brow(u, gb[0], gb[1], gb[2], cb, sb);
+        for (int c = 0; c < HV; ++c) W[u][c] = H[c * HV + cb[0]] * sb[0] + H[c * HV + cb[1]] * sb[1] + H[c * HV + cb[2]] * sb[2];
+    }
+    for (int v = 0; v < NV; ++v) {
+        int ca[3];
+        double sa[3];
+        brow(v, ga[0], ga[1], ga[2], ca, sa);
+        for (int u = 0; u < NV; ++u) K[v][u] += w * (sa[0] * W[u][ca[0]] + sa[1] * W[u][ca[1]] + sa[2] * W[u][ca[2]]);
+    }
+    double geo = 0.0;
+    for (int k = 0; k < 3; ++k) geo += ga[k] * (sigma[k * 3] * gb[0] + sigma[k * 3 + 1] * gb[1] + sigma[k * 3 + 2] * gb[2]);
+    for (int v = 0; v < 3; ++v) K[v][v] += w * geo;
+}
+
 // one Gauss point's contribution (without dv) to the residual of (node a, field v): the B row
 // against (sigma_xx, sigma_yy, sigma_zz, sigma_xy, sigma_xz, sigma_yz, D)
 FL_HD double residual(int a, int v, int npe, const double *SG, const double *D, const double *sigma) {

@@ -356,9 +356,11 @@ int fl_GlobalAssemblyExplicit_DF_DPF_(const double *points, const uint64_t *elem
  * _Piezoelectric_100_, called from
  * _LowLevelAssemblyDPF_.pyx:53-160. Same argument list and scatter modes as the DF entries:
  * recompute_sparsity_pattern -> triplets (I_stiff, J_stiff, V_stiff [nelem*(4 npe)^2]); else
- * I_stiff = indptr [4 nnode + 1], J_stiff = indices, V_stiff [nnz] += through the maps, or by row
- * search when squeeze_sparsity_pattern. Eulerp [nnode] is the electric potential; T [4 nnode] +=.
- * The maps mode reads indptr[4 nnode] once (one synchronisation). flags: optional device int
+ * I_stiff = indptr [4 nnode + 1], J_stiff = indices, V_stiff [nnz] += at the positions the maps
+ * name (found, as with squeeze_sparsity_pattern, by one search per row of a node pair's 4 x 4 block:
+ * the tangent is formed per node pair a <= b and mirrored, being symmetric). Eulerp [nnode] is the
+ * electric potential; T [4 nnode] +=. The maps mode reads indptr[4 nnode] once (one
+ * synchronisation). flags: optional device int
  * (FL_FLAG_* bits). FL_ERR_UNSUPPORTED when an element's Gauss-point data do not fit in shared
  * memory (more than about 64 nodes x 64 points).
  * ------------------------------------------------------------------------------------------ */

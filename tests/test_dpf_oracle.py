@@ -61,15 +61,18 @@ def dpf_host(tmp_path_factory):
     subprocess.check_call(["g++", "-O2", "-shared", "-fPIC", "-o", so, os.path.join(here, "dpf_host_shim.cpp")])
     L = ctypes.CDLL(so)
     P, I, D = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
-    L.dpf_element.argtypes = [I, I, I, P, P, P, P, P, I, P, P, P, P]
+    L.dpf_element.argtypes = [I, I, I, P, P, P, P, P, I, P, P, P, P, I]
     L.dpf_element.restype = D
     return L
 
 
+@pytest.mark.parametrize("blocks", [0, 1])
 @pytest.mark.parametrize("case", dpf_cases())
-def test_device_dpf_arithmetic_on_host(dpf_host, case):
-    """The Gauss-point and entry functions the device kernel runs, built for the host, give the
-    reference's element tangents and residuals."""
+def test_device_dpf_arithmetic_on_host(dpf_host, case, blocks):
+    """The Gauss-point and tangent functions the device kernel runs, built for the host, give the
+    reference's element tangents and residuals: entry by entry, and as the kernel forms them,
+    node-pair blocks for a <= b mirrored to b > a (the reference's element tangents are symmetric
+    to rounding)."""
     d = load_golden(case)
     Jm = np.ascontiguousarray(d["Jm"], np.float64)
     w = np.ascontiguousarray(np.ravel(d["AllGauss"]), np.float64)
@@ -86,7 +89,7 @@ def test_device_dpf_arithmetic_on_host(dpf_host, case):
         mat = SHIM_MATERIALS[str(d["material"])]
         minJ = dpf_host.dpf_element(mat, npe, nq, Jm.ctypes.data, w.ctypes.data, X.ctypes.data, x.ctypes.data,
                                     phi.ctypes.data, int(d["update"]), p.ctypes.data,
-                                    N.ctypes.data if N is not None else None, K.ctypes.data, t.ctypes.data)
+                                    N.ctypes.data if N is not None else None, K.ctypes.data, t.ctypes.data, blocks)
         assert minJ > 0
         assert rel_fro(K, d["emat_K"][k]) < TOL
         assert rel_fro(t, d["emat_t"][k]) < TOL
