@@ -374,6 +374,97 @@ class DeviceAssembler:
             N.check(L.fl_GlobalAssemblyDF_Blocks(self.mat_id, _ptr(boff), _ptr(pc["geo"]), *args),
                     "fl_GlobalAssemblyDF (colour)")
 
+    # -- pipelined assembly into host buffers (the drop-in's squeeze path) ---------------------------
+    def _pipeline_plan(self, pieces):
+        """Elements sorted by their smallest node id and split into `pieces` groups. A CSR row is
+        final once the last group holding its node is assembled: after group g the rows of the
+        nodes whose last group is g (as runs of consecutive nodes, gaps below 4 MB of values
+        merged) can go to the host while the later groups are assembled. Built once per mesh."""
+        el = self.elements.cpu().numpy()
+        order = np.argsort(el.min(1), kind="stable")
+        bounds = np.linspace(0, self.nelem, pieces + 1).astype(np.int64)
+        group = np.empty(self.nelem, np.int64)
+        for g in range(pieces):
+            group[order[bounds[g]:bounds[g + 1]]] = g
+        last = np.full(self.nnode, -1, np.int64)
+        np.maximum.at(last, el.ravel(), np.repeat(group, self.npe))
+        ptr = self.indptr.cpu().numpy().astype(np.int64)
+        gap = (4 << 20) // 8
+        plan = []
+        for g in range(pieces):
+            idx = order[bounds[g]:bounds[g + 1]]
+            nodes = np.nonzero(last == g)[0]
+            runs = []
+            if nodes.size:
+                cut = np.nonzero(np.diff(nodes) != 1)[0]
+                starts = np.concatenate([[nodes[0]], nodes[cut + 1]])
+                ends = np.concatenate([nodes[cut] + 1, [nodes[-1] + 1]])
+                for a, b in zip(starts, ends):
+                    if runs and ptr[3 * a] - ptr[3 * runs[-1][1]] < gap:
+                        runs[-1][1] = b            # merge: the rows between are copied again later
+                    else:
+                        runs.append([a, b])
+            sub = torch.from_numpy(el[idx]).to(self.device)
+            plan.append(dict(elements=sub.contiguous(), count=int(idx.size),
+                             orient=self.orient[torch.from_numpy(idx).to(self.device)].contiguous()
+                             if self.orient is not None else None,
+                             rows=[(int(ptr[3 * a]), int(ptr[3 * b]), 3 * int(a), 3 * int(b)) for a, b in runs]))
+        return plan
+
+    def assemble_to_host(self, Eulerx, V_host, T_host, pieces=8):
+        """Tangent (squeeze or csr mode) and residual into the pinned host tensors V_host [nnz] and
+        T_host [3N], the assembly in `pieces` groups of elements on the current stream and the
+        finished CSR rows copied out on a second stream meanwhile (the copy, ~190 GB/s over the
+        Grace-GPU link, is longer than the assembly). Returns when both host tensors are complete.
+        Flags as for assemble (check_flags)."""
+        if self.mode == "triplet":
+            raise ValueError("the pipelined assembly writes the CSR tangent")
+        if getattr(self, "_pipe", None) is None or len(self._pipe) != pieces:
+            self._pipe = self._pipeline_plan(pieces)
+        L = N.lib()
+        x = Eulerx if Eulerx.is_contiguous() else Eulerx.contiguous()
+        V = torch.zeros(self.nnz, dtype=torch.float64, device=self.device)
+        T = torch.zeros(self.nnode * 3, dtype=torch.float64, device=self.device)
+        mu, mu1, mu2, lamb, mu3 = _abi_params(self.mat_id, self.params)
+        rt = L.fl_GetAssemblyArithmetic() == N.FL_ARITH_REFERENCE_TENSOR and rt_supported(self.npe, self.nq)
+        comp = torch.cuda.current_stream(self.device)
+        copy = getattr(self, "_copy_stream", None)
+        if copy is None:
+            copy = self._copy_stream = torch.cuda.Stream(device=self.device)
+        st_ = ctypes.c_void_p(comp.cuda_stream)
+        for pc in self._pipe:
+            if pc["count"] == 0:
+                continue
+            if "geo" not in pc:
+                geo = torch.empty((10, pc["count"] * self.nq), dtype=torch.float64, device=self.device)
+                N.check(L.fl_ReferenceGeometry(_ptr(self.points), _ptr(pc["elements"]), _ptr(self.Jm), pc["count"],
+                                               self.npe, self.nq, self.nnode, _ptr(geo), _ptr(self.flags), st_),
+                        "fl_ReferenceGeometry")
+                pc["geo"] = geo
+            if rt and "boff" not in pc:
+                b = torch.empty((pc["count"], self.npe, self.npe), dtype=torch.int32, device=self.device)
+                N.check(L.fl_ElementBlockOffsets(_ptr(pc["elements"]), pc["count"], self.npe, self.nnode,
+                                                 _ptr(self.indptr), _ptr(self.indices), _ptr(b), _ptr(self.flags),
+                                                 st_), "fl_ElementBlockOffsets")
+                pc["boff"] = b
+            args = (_ptr(self.points), _ptr(pc["elements"]), _ptr(x), None, None, _ptr(self.Jm), _ptr(self.w),
+                    3, 3, self.nq, pc["count"], self.npe, self.nnode, 6, self.update, None, None,
+                    _ptr(self.indptr), _ptr(self.indices), _ptr(V), _ptr(T), 0, 1, None, None, None, None,
+                    1.0, mu, mu1, mu2, mu3, 0.0, lamb, 0.0, 0.0, 0.0, 0.0, _ptr(pc["orient"]), _ptr(self.flags), st_)
+            N.check(L.fl_GlobalAssemblyDF_Blocks(self.mat_id, _ptr(pc["boff"] if rt else None), _ptr(pc["geo"]),
+                                                 *args), "fl_GlobalAssemblyDF (pipelined)")
+            done = torch.cuda.Event()
+            done.record(comp)
+            copy.wait_event(done)
+            with torch.cuda.stream(copy):
+                for v0, v1, t0, t1 in pc["rows"]:
+                    V_host[v0:v1].copy_(V[v0:v1], non_blocking=True)
+                    T_host[t0:t1].copy_(T[t0:t1], non_blocking=True)
+        V.record_stream(copy)
+        T.record_stream(copy)
+        copy.synchronize()
+        return V_host, T_host
+
     def reference_geometry(self, stream=None):
         """(dX/dxi)^-1 and det(dX/dxi) per element and Gauss point (fl_ReferenceGeometry), computed
         on first use and kept: [10, nelem * nq] float64. The assembly then forms only the current
@@ -575,6 +666,9 @@ def release_device_meshes():
     _MESHES.clear()
 
 
+PIPELINE_MIN_ELEMENTS = 20000  # the drop-in's pipelined assembly-and-copy from this mesh size on
+
+
 def _low_level_df(name, fem_solver, function_space, formulation, mesh, material, Eulerx, Eulerp):
     _check_formulation(formulation, material)
     mat_id, params = material_params(material, name)
@@ -596,6 +690,18 @@ def _low_level_df(name, fem_solver, function_space, formulation, mesh, material,
                                               name, params, mode=mode, requires_geometry_update=update,
                                               sparsity=sparsity, orientations=orient))
     x = _to_dev(Eulerx, torch.float64, asm.device)
+    if mode == "squeeze" and asm.nelem >= PIPELINE_MIN_ELEMENTS:
+        # large meshes: the assembly in groups of elements, the finished rows copied to the host
+        # while the later groups are assembled
+        Vt, Va = _HOST.take((asm.nnz,), torch.float64, pinned=True)
+        Tt, Ta = _HOST.take((asm.nnode * 3,), torch.float64, pinned=True)
+        asm.assemble_to_host(x, Vt, Tt)
+        if int(asm.flags.item()) & N.FL_FLAG_PAIR_RANGE:
+            asm.flags.zero_()
+            with arithmetic("fp64"):
+                asm.assemble_to_host(x, Vt, Tt)
+        asm.check_flags("_LowLevelAssemblyDF_" + name)
+        return Va, Ta
     out = asm.assemble(x)
     if int(asm.flags.item()) & N.FL_FLAG_PAIR_RANGE:
         # values too small or too large for the float pairs of the default arithmetics (units far

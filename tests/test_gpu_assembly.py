@@ -423,6 +423,21 @@ def test_drop_in_callables(fl, case, recompute, squeeze):
     assert rel_fro(Ti, d["T"]) < TOL
 
 
+@pytest.mark.parametrize("case", ["tet_p3_mr_jitter", "hex_p2_nh_q5"])
+def test_drop_in_pipelined_assembly(fl, monkeypatch, case):
+    """The drop-in's pipelined path (element groups assembled in turn, finished rows copied to the
+    host meanwhile; taken for large meshes) forced on a golden case: the reference's values."""
+    from florence_gb300 import assembly
+    monkeypatch.setattr(assembly, "PIPELINE_MIN_ELEMENTS", 0)
+    d = load_golden(case)
+    solver, fs, form, mesh, material = _fake_florence_objects(d, False, True)
+    fn = getattr(fl, "_LowLevelAssemblyDF__" + str(d["material"]) + "_")
+    for _ in range(2):
+        V, T = fn(solver, fs, form, mesh, material, d["Eulerx"], np.zeros(d["points"].shape[0]))
+        assert rel_fro(V, d["K_data"]) < TOL and rel_fro(T, d["T"]) < TOL
+    fl.release_device_meshes()
+
+
 def test_drop_in_sparsity(fl):
     d = load_golden("tet_p3_mr_jitter")
     mesh = types.SimpleNamespace(points=d["points"], elements=d["elements"].astype(np.uint64))
